@@ -1,0 +1,270 @@
+"""Python host mirror of libcac's C ABI (include/cac.h), loaded with ctypes.
+
+Mirrors the reference's callable classes for this path:
+  * ``connected_components``  UnweightedIteratedSparseSampling::connectedComponents
+                              (src/UnweightedIteratedSparseSampling.cpp:40-72)
+  * ``square_root``           SquareRootCut::runMaster (src/SquareRootCut.cpp:15-25)
+  * ``approx_cut``            ApproximateCut::run (src/ApproximateCut.cpp:10-79)
+Every non-zero status of the library raises ``CacError`` (the reference throws or asserts).
+There is no fallback: if libcac.so is missing or no CUDA device is present, calls fail loudly.
+"""
+import ctypes
+import os
+from dataclasses import dataclass
+
+import numpy as np
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(_HERE, "lib", "libcac.so")
+
+HOST, DEVICE = 0, 1
+_STATUS = {0: "ok", -1: "invalid argument", -2: "out of device memory or HBM budget", -3: "malformed input",
+           -4: "CUDA runtime error", -5: "device-side bound exceeded", -6: "unsupported", -7: "I/O error"}
+
+
+class CacError(RuntimeError):
+    def __init__(self, status, where, detail):
+        super().__init__("%s failed: %s (%d): %s" % (where, _STATUS.get(status, "?"), status, detail))
+        self.status = status
+
+
+class _Config(ctypes.Structure):
+    _fields_ = [("device", ctypes.c_int), ("stream", ctypes.c_void_p), ("hbm_budget_bytes", ctypes.c_uint64)]
+
+
+class CCResult(ctypes.Structure):
+    _fields_ = [("num_components", ctypes.c_uint32), ("rounds", ctypes.c_uint32), ("sampled_edges", ctypes.c_uint64),
+                ("device_ms", ctypes.c_float), ("edge_pass_ms", ctypes.c_float)]
+
+
+class MincutResult(ctypes.Structure):
+    _fields_ = [("cut", ctypes.c_uint64), ("trials_per_rank", ctypes.c_uint32), ("total_trials", ctypes.c_uint32),
+                ("intermediate", ctypes.c_uint32), ("high_concurrency", ctypes.c_uint32),
+                ("device_ms", ctypes.c_float)]
+
+
+class ApproxResult(ctypes.Structure):
+    _fields_ = [("cut", ctypes.c_uint64), ("trials", ctypes.c_uint32), ("copies", ctypes.c_uint32),
+                ("level", ctypes.c_uint32), ("device_ms", ctypes.c_float)]
+
+
+_u32p = ctypes.POINTER(ctypes.c_uint32)
+_u64p = ctypes.POINTER(ctypes.c_uint64)
+_vp = ctypes.c_void_p
+_LIB = None
+
+# (name, restype, argtypes) of every exported entry point declared in include/cac.h
+EXPORTS = [
+    ("cac_ctx_create", ctypes.c_int, [ctypes.POINTER(_Config), ctypes.POINTER(_vp)]),
+    ("cac_ctx_destroy", ctypes.c_int, [_vp]),
+    ("cac_error_string", ctypes.c_char_p, [ctypes.c_int]),
+    ("cac_last_error", ctypes.c_char_p, []),
+    ("cac_ctx_device_bytes", ctypes.c_uint64, [_vp]),
+    ("cac_graph_load_file", ctypes.c_int, [_vp, ctypes.c_char_p, ctypes.POINTER(_vp)]),
+    ("cac_graph_from_edges", ctypes.c_int, [_vp, ctypes.c_uint32, ctypes.c_uint64, _vp, _vp, _vp, ctypes.c_int,
+                                            ctypes.POINTER(_vp)]),
+    ("cac_graph_free", ctypes.c_int, [_vp]),
+    ("cac_graph_info", ctypes.c_int, [_vp, _u32p, _u64p, _u64p]),
+    ("cac_parse_file", ctypes.c_int, [ctypes.c_char_p, _u32p, _u64p, _vp, _vp, _vp, ctypes.c_uint64]),
+    ("cac_parse_header", ctypes.c_int, [ctypes.c_char_p, _u32p, _u64p]),
+    ("cac_cc", ctypes.c_int, [_vp, _vp, ctypes.c_uint32, ctypes.c_uint32, _vp, ctypes.c_int,
+                              ctypes.POINTER(CCResult)]),
+    ("cac_cc_edges", ctypes.c_int, [_vp, ctypes.c_uint32, ctypes.c_uint64, _vp, _vp, ctypes.c_uint32,
+                                    ctypes.c_uint32, _vp, ctypes.POINTER(CCResult)]),
+    ("cac_mincut", ctypes.c_int, [_vp, _vp, ctypes.c_double, ctypes.c_uint32, ctypes.c_uint32,
+                                  ctypes.POINTER(MincutResult)]),
+    ("cac_mincut_trials", ctypes.c_int, [_vp, _vp, ctypes.c_uint32, ctypes.c_uint32, ctypes.c_uint32, _vp]),
+    ("cac_ks_dense", ctypes.c_int, [_vp, ctypes.c_uint32, _vp, ctypes.c_uint32, ctypes.c_uint32, ctypes.c_uint32,
+                                    _u64p]),
+    ("cac_exact_cut_small", ctypes.c_int, [_vp, ctypes.c_uint32, _vp, _u64p]),
+    ("cac_approx_cut", ctypes.c_int, [_vp, _vp, ctypes.c_double, ctypes.c_uint32, ctypes.c_uint32,
+                                      ctypes.POINTER(ApproxResult)]),
+    ("cac_sitmo_blocks", ctypes.c_int, [_vp, _u64p, _u64p, ctypes.c_uint64, _vp]),
+]
+
+
+def lib():
+    """Load libcac.so (raises if it was not built)."""
+    global _LIB
+    if _LIB is None:
+        if not os.path.exists(LIB_PATH):
+            raise RuntimeError("libcac.so not built: run `python -c 'import __graft_entry__ as g; g.build()'`")
+        L = ctypes.CDLL(LIB_PATH)
+        for name, res, args in EXPORTS:
+            f = getattr(L, name)
+            f.restype = res
+            f.argtypes = args
+        _LIB = L
+    return _LIB
+
+
+def _check(status, where):
+    if status != 0:
+        raise CacError(status, where, lib().cac_last_error().decode(errors="replace"))
+
+
+def _ptr(a):
+    """Host numpy array or device tensor-like (with data_ptr) -> (pointer, where)."""
+    if a is None:
+        return None, HOST
+    if hasattr(a, "data_ptr"):
+        return ctypes.c_void_p(a.data_ptr()), (DEVICE if getattr(a, "is_cuda", False) else HOST)
+    return ctypes.c_void_p(a.ctypes.data), HOST
+
+
+class Context:
+    """One device + one CUDA stream (cac_ctx). `stream` is a raw cudaStream_t handle (int) or None."""
+
+    def __init__(self, device=0, stream=None, hbm_budget_bytes=0):
+        cfg = _Config(device, ctypes.c_void_p(stream) if stream else None, hbm_budget_bytes)
+        h = _vp()
+        _check(lib().cac_ctx_create(ctypes.byref(cfg), ctypes.byref(h)), "cac_ctx_create")
+        self.h = h
+
+    def close(self):
+        if self.h:
+            lib().cac_ctx_destroy(self.h)
+            self.h = None
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    @property
+    def device_bytes(self):
+        return int(lib().cac_ctx_device_bytes(self.h))
+
+    # ---- graphs ----
+    def graph(self, n, u, v, w=None):
+        """Upload an edge list (numpy uint32 host arrays or CUDA tensors) as a device graph."""
+        if not hasattr(u, "data_ptr"):
+            u = np.ascontiguousarray(u, dtype=np.uint32)
+            v = np.ascontiguousarray(v, dtype=np.uint32)
+            w = None if w is None else np.ascontiguousarray(w, dtype=np.uint32)
+        pu, where = _ptr(u)
+        pv, _ = _ptr(v)
+        pw, _ = _ptr(w)
+        h = _vp()
+        _check(lib().cac_graph_from_edges(self.h, n, len(u), pu, pv, pw, where, ctypes.byref(h)),
+               "cac_graph_from_edges")
+        return Graph(self, h, (u, v, w))
+
+    def load(self, path):
+        h = _vp()
+        _check(lib().cac_graph_load_file(self.h, path.encode(), ctypes.byref(h)), "cac_graph_load_file")
+        return Graph(self, h, None)
+
+    # ---- primitives ----
+    def sitmo_blocks(self, key, ctr0, nblocks):
+        k = np.array(key, dtype=np.uint64)
+        c = np.array(ctr0, dtype=np.uint64)
+        out = np.zeros(4 * nblocks, dtype=np.uint64)
+        _check(lib().cac_sitmo_blocks(self.h, k.ctypes.data_as(_u64p), c.ctypes.data_as(_u64p), nblocks,
+                                      ctypes.c_void_p(out.ctypes.data)), "cac_sitmo_blocks")
+        return out.reshape(nblocks, 4)
+
+    def cc_edges(self, n, u, v, seed=0, virtual_ranks=1, labels=None):
+        """One-call CC from host edge arrays to host labels (copies included)."""
+        res = CCResult()
+        pl = None if labels is None else ctypes.c_void_p(labels.ctypes.data)
+        _check(lib().cac_cc_edges(self.h, n, len(u), ctypes.c_void_p(u.ctypes.data), ctypes.c_void_p(v.ctypes.data),
+                                  seed, virtual_ranks, pl, ctypes.byref(res)), "cac_cc_edges")
+        return res
+
+    def ks_dense(self, mat, seed, rank, trial):
+        m = np.ascontiguousarray(mat, dtype=np.uint64)
+        out = ctypes.c_uint64()
+        _check(lib().cac_ks_dense(self.h, m.shape[0], ctypes.c_void_p(m.ctypes.data), seed, rank, trial,
+                                  ctypes.byref(out)), "cac_ks_dense")
+        return int(out.value)
+
+    def exact_cut_small(self, mat):
+        m = np.ascontiguousarray(mat, dtype=np.uint64)
+        out = ctypes.c_uint64()
+        _check(lib().cac_exact_cut_small(self.h, m.shape[0], ctypes.c_void_p(m.ctypes.data), ctypes.byref(out)),
+               "cac_exact_cut_small")
+        return int(out.value)
+
+
+class Graph:
+    def __init__(self, ctx, h, keepalive):
+        self.ctx = ctx
+        self.h = h
+        self._keep = keepalive
+        n, m, w = ctypes.c_uint32(), ctypes.c_uint64(), ctypes.c_uint64()
+        _check(lib().cac_graph_info(h, ctypes.byref(n), ctypes.byref(m), ctypes.byref(w)), "cac_graph_info")
+        self.n, self.m, self.total_weight = int(n.value), int(m.value), int(w.value)
+
+    def free(self):
+        if self.h:
+            lib().cac_graph_free(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.free()
+        except Exception:
+            pass
+
+    # UnweightedIteratedSparseSampling::connectedComponents
+    def connected_components(self, seed=0, virtual_ranks=1, labels=True, out=None):
+        """Returns (number_of_components, labels or None, CCResult). `out` may be a device
+        tensor (or host array) of n uint32 that receives the labels."""
+        res = CCResult()
+        if out is not None:
+            pl, where = _ptr(out)
+        elif labels:
+            out = np.zeros(max(self.n, 1), dtype=np.uint32)
+            pl, where = _ptr(out)
+        else:
+            pl, where = None, HOST
+        _check(lib().cac_cc(self.ctx.h, self.h, seed, virtual_ranks, pl, where, ctypes.byref(res)), "cac_cc")
+        lab = None
+        if out is not None and not hasattr(out, "data_ptr"):
+            lab = out[: self.n]
+        elif out is not None:
+            lab = out
+        return int(res.num_components), lab, res
+
+    # SquareRootCut::runMaster
+    def square_root(self, success_probability=0.95, seed=0, virtual_ranks=1):
+        res = MincutResult()
+        _check(lib().cac_mincut(self.ctx.h, self.h, success_probability, seed, virtual_ranks, ctypes.byref(res)),
+               "cac_mincut")
+        return res
+
+    def trials(self, seed, virtual_ranks, trials_per_rank):
+        out = np.zeros(virtual_ranks * trials_per_rank, dtype=np.uint64)
+        _check(lib().cac_mincut_trials(self.ctx.h, self.h, seed, virtual_ranks, trials_per_rank,
+                                       ctypes.c_void_p(out.ctypes.data)), "cac_mincut_trials")
+        return out.reshape(virtual_ranks, trials_per_rank)
+
+    # ApproximateCut::run
+    def approx_cut(self, success_probability=0.9, seed=0, virtual_ranks=1):
+        res = ApproxResult()
+        _check(lib().cac_approx_cut(self.ctx.h, self.h, success_probability, seed, virtual_ranks, ctypes.byref(res)),
+               "cac_approx_cut")
+        return res
+
+
+def parse_file(path):
+    """Parse an edge-list file with the library's reader -> (n, u, v, w)."""
+    n, m = ctypes.c_uint32(), ctypes.c_uint64()
+    _check(lib().cac_parse_header(path.encode(), ctypes.byref(n), ctypes.byref(m)), "cac_parse_header")
+    cap = int(m.value)
+    u = np.zeros(max(cap, 1), np.uint32)
+    v = np.zeros(max(cap, 1), np.uint32)
+    w = np.zeros(max(cap, 1), np.uint32)
+    _check(lib().cac_parse_file(path.encode(), ctypes.byref(n), ctypes.byref(m), ctypes.c_void_p(u.ctypes.data),
+                                ctypes.c_void_p(v.ctypes.data), ctypes.c_void_p(w.ctypes.data), cap),
+           "cac_parse_file")
+    k = int(m.value)
+    return int(n.value), u[:k], v[:k], w[:k]

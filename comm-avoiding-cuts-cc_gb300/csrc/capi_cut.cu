@@ -1,0 +1,105 @@
+// C ABI entry points of the cut queries (square_root, approx_cut) and their kernel-level probes.
+#include "cac_internal.h"
+
+#include <algorithm>
+#include <cmath>
+#include <vector>
+
+using namespace cac;
+
+extern "C" {
+
+int cac_mincut_trials(cac_ctx *ctx, const cac_graph *g, uint32_t seed, uint32_t virtual_ranks,
+                      uint32_t trials_per_rank, uint64_t *cuts_host) {
+    if (!ctx || !g || !cuts_host || virtual_ranks == 0) {
+        set_error("cac_mincut_trials: invalid argument");
+        return CAC_ERR_INVALID;
+    }
+    if (g->n < 2) {
+        set_error("cac_mincut_trials: a cut needs at least two vertices");
+        return CAC_ERR_INVALID;
+    }
+    CAC_CUDA_TRY(cudaSetDevice(ctx->device));
+    const uint64_t total = (uint64_t)virtual_ranks * trials_per_rank;
+    if (total == 0) return CAC_OK;
+    void *d = nullptr;
+    CAC_TRY(dev_alloc(ctx, &d, total * 8));
+    float ms = 0;
+    int st = mincut_trials(ctx, g, seed, virtual_ranks, trials_per_rank, (uint64_t *)d, &ms);
+    if (st == CAC_OK) {
+        cudaError_t e = cudaMemcpy(cuts_host, d, total * 8, cudaMemcpyDeviceToHost);
+        if (e != cudaSuccess) { set_error(cudaGetErrorString(e)); st = CAC_ERR_CUDA; }
+    }
+    dev_free(ctx, d, total * 8);
+    return st;
+}
+
+int cac_mincut(cac_ctx *ctx, const cac_graph *g, double p, uint32_t seed, uint32_t virtual_ranks,
+               cac_mincut_result *res) {
+    if (!ctx || !g || !res || !(p >= 0.0 && p < 1.0)) {
+        set_error("cac_mincut: invalid argument (success probability must be in [0, 1))");
+        return CAC_ERR_INVALID;
+    }
+    if (g->n < 2) {
+        set_error("cac_mincut: a cut needs at least two vertices");
+        return CAC_ERR_INVALID;
+    }
+    if (virtual_ranks == 0) virtual_ranks = 1;
+    CAC_CUDA_TRY(cudaSetDevice(ctx->device));
+    *res = cac_mincut_result{};
+    // SquareRootCut::runLowConcurrencyMaster (SquareRootCut.cpp:99-100)
+    const double total = number_of_trials(g->n, g->m, p);
+    const uint32_t per = (uint32_t)std::ceil(total / virtual_ranks);
+    res->trials_per_rank = per;
+    res->total_trials = per * virtual_ranks;
+    res->intermediate = intermediate_size(g->n, g->m);
+    // SquareRootCut::lowConcurrency (SquareRootCut.cpp:11-13): the group variant is chosen when
+    // p >= 2 * trials; on one GPU every trial runs in one batch either way.
+    res->high_concurrency = virtual_ranks >= 2u * (uint32_t)total ? 1u : 0u;
+    const uint64_t n_tr = (uint64_t)res->total_trials;
+    void *d = nullptr;
+    CAC_TRY(dev_alloc(ctx, &d, n_tr * 8));
+    float ms = 0;
+    int st = mincut_trials(ctx, g, seed, virtual_ranks, per, (uint64_t *)d, &ms);
+    if (st == CAC_OK) {
+        std::vector<uint64_t> cuts(n_tr);
+        cudaError_t e = cudaMemcpy(cuts.data(), d, n_tr * 8, cudaMemcpyDeviceToHost);
+        if (e != cudaSuccess) { set_error(cudaGetErrorString(e)); st = CAC_ERR_CUDA; }
+        else res->cut = *std::min_element(cuts.begin(), cuts.end());
+    }
+    res->device_ms = ms;
+    dev_free(ctx, d, n_tr * 8);
+    return st;
+}
+
+int cac_ks_dense(cac_ctx *ctx, uint32_t n, const uint64_t *mat_host, uint32_t seed, uint32_t rank, uint32_t trial,
+                 uint64_t *cut) {
+    if (!ctx || !mat_host || !cut || n < 2) {
+        set_error("cac_ks_dense: invalid argument");
+        return CAC_ERR_INVALID;
+    }
+    CAC_CUDA_TRY(cudaSetDevice(ctx->device));
+    return ks_dense_one(ctx, n, mat_host, seed, rank, trial, cut);
+}
+
+int cac_exact_cut_small(cac_ctx *ctx, uint32_t n, const uint64_t *mat_host, uint64_t *cut) {
+    if (!ctx || !mat_host || !cut || n < 2 || n > 128) {
+        set_error("cac_exact_cut_small: invalid argument (2 <= n <= 128)");
+        return CAC_ERR_INVALID;
+    }
+    CAC_CUDA_TRY(cudaSetDevice(ctx->device));
+    return exact_small(ctx, n, mat_host, cut);
+}
+
+int cac_approx_cut(cac_ctx *ctx, const cac_graph *g, double p, uint32_t seed, uint32_t virtual_ranks,
+                   cac_approx_result *res) {
+    if (!ctx || !g || !res || !(p > 0.0 && p < 1.0)) {
+        set_error("cac_approx_cut: invalid argument (success probability must be in (0, 1))");
+        return CAC_ERR_INVALID;
+    }
+    if (virtual_ranks == 0) virtual_ranks = 1;
+    CAC_CUDA_TRY(cudaSetDevice(ctx->device));
+    return approx_run(ctx, g, p, seed, virtual_ranks, res);
+}
+
+}  // extern "C"

@@ -1,0 +1,386 @@
+// libcac runtime: contexts, device memory accounting, graphs and the C ABI entry points.
+#include "cac_internal.h"
+#include "sitmo.cuh"
+
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <new>
+
+namespace cac {
+
+static thread_local std::string g_last_error;
+
+void set_error(const std::string &msg) { g_last_error = msg; }
+
+int dev_alloc(cac_ctx *ctx, void **p, size_t bytes) {
+    *p = nullptr;
+    if (bytes == 0) return CAC_OK;
+    if (ctx->budget && ctx->held + bytes > ctx->budget) {
+        set_error("HBM budget exceeded: need " + std::to_string(ctx->held + bytes) + " bytes, budget " +
+                  std::to_string(ctx->budget));
+        return CAC_ERR_OOM;
+    }
+    cudaError_t e = cudaMalloc(p, bytes);
+    if (e != cudaSuccess) {
+        cudaGetLastError();
+        *p = nullptr;
+        set_error(std::string("cudaMalloc(") + std::to_string(bytes) + "): " + cudaGetErrorString(e));
+        return CAC_ERR_OOM;
+    }
+    ctx->held += bytes;
+    return CAC_OK;
+}
+
+void dev_free(cac_ctx *ctx, void *p, size_t bytes) {
+    if (!p) return;
+    cudaFree(p);
+    ctx->held -= std::min<uint64_t>(ctx->held, bytes);
+}
+
+int arena_reserve(cac_ctx *ctx, Arena &a, size_t bytes) {
+    if (bytes <= a.cap) return CAC_OK;
+    CAC_CUDA_TRY(cudaStreamSynchronize(ctx->stream));
+    dev_free(ctx, a.base, a.cap);
+    a.base = nullptr;
+    a.cap = 0;
+    a.used = 0;
+    size_t want = align_up(bytes, 1 << 20);
+    void *p = nullptr;
+    CAC_TRY(dev_alloc(ctx, &p, want));
+    a.base = (char *)p;
+    a.cap = want;
+    return CAC_OK;
+}
+
+void *arena_take(Arena &a, size_t bytes) {
+    size_t at = align_up(a.used);
+    a.used = at + align_up(bytes);
+    return a.base + at;
+}
+
+// ---- trial budget: the reference's double-precision expressions ----
+
+int ks_target(int n) {
+    // comincut::target_number_of_vertices_for_contraction (co_mincut.cpp:18-20)
+    int t = (int)std::ceil((double)n / std::sqrt((double)2)) + 1;
+    return std::max(t, 128);
+}
+
+double min_success_in_one_trial(int n) {
+    // comincut::min_success_in_one_trial (co_mincut.cpp:32-41)
+    if (n <= 128) return 1;
+    double r = min_success_in_one_trial(ks_target(n));
+    return 1.0 - std::pow((1 - 0.5 * r), 2);
+}
+
+uint32_t intermediate_size(uint32_t n, uint64_t m) {
+    // SquareRootCut::intermediate_size (SquareRootCut.cpp:63-70), base_case_multiplier = 2
+    uint32_t c = (uint32_t)std::ceil(2.0 * std::sqrt((double)m) + 1);
+    return c > n ? n : c;
+}
+
+uint32_t number_of_trials(uint32_t n, uint64_t m, double p) {
+    // SquareRootCut::numberOfTrials (SquareRootCut.cpp:76-83)
+    double pk = min_success_in_one_trial((int)intermediate_size(n, m));
+    double c = 1.0 / (1 - p);
+    return (uint32_t)std::ceil(((double)n * ((double)n * std::log(c))) / (2.0 * 2.0 * ((double)m * pk)));
+}
+
+uint32_t approx_copies(double p) {
+    // ApproximateCut::numberOfTrials (ApproximateCut.cpp:82-87)
+    double alpha = std::log(1 - std::exp(-(double)0.75));
+    return (uint32_t)std::ceil(std::log((double)1.0 - p) / alpha);
+}
+
+namespace {
+
+__global__ void fill_u32(uint32_t *p, uint64_t n, uint32_t value) {
+    for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (uint64_t)gridDim.x * blockDim.x)
+        p[i] = value;
+}
+
+__global__ void sum_u32(const uint32_t *p, uint64_t n, unsigned long long *out) {
+    uint64_t acc = 0;
+    for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (uint64_t)gridDim.x * blockDim.x)
+        acc += p[i];
+    for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
+    if ((threadIdx.x & 31) == 0 && acc) atomicAdd(out, (unsigned long long)acc);
+}
+
+__global__ void check_ids(const uint32_t *u, const uint32_t *v, uint64_t m, uint32_t n, unsigned int *bad) {
+    for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < m; i += (uint64_t)gridDim.x * blockDim.x)
+        if (u[i] >= n || v[i] >= n) atomicOr(bad, 1u);
+}
+
+__global__ void sitmo_blocks_kernel(uint64_t k0, uint64_t k1, uint64_t k2, uint64_t k3, uint64_t c0, uint64_t c1,
+                                    uint64_t c2, uint64_t c3, uint64_t nblocks, uint64_t *out) {
+    for (uint64_t b = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; b < nblocks;
+         b += (uint64_t)gridDim.x * blockDim.x) {
+        // 256-bit counter ctr0 + b
+        uint64_t d0 = c0 + b, carry = d0 < c0;
+        uint64_t d1 = c1 + carry;
+        carry = carry && d1 == 0;
+        uint64_t d2 = c2 + carry;
+        carry = carry && d2 == 0;
+        uint64_t d3 = c3 + carry;
+        u64x4 o = sitmo_block(k0, k1, k2, k3, d0, d1, d2, d3);
+        for (int j = 0; j < 4; j++) out[4 * b + j] = o.x[j];
+    }
+}
+
+int grid1(cac_ctx *ctx, uint64_t work) {
+    uint64_t need = (work + 255) / 256;
+    return (int)std::max<uint64_t>(1, std::min<uint64_t>(need, (uint64_t)ctx->num_sms * 8));
+}
+
+}  // namespace
+
+int sitmo_blocks(cac_ctx *ctx, const uint64_t key[4], const uint64_t ctr0[4], uint64_t nblocks, uint64_t *out_host) {
+    if (nblocks == 0) return CAC_OK;
+    CAC_TRY(arena_reserve(ctx, nblocks * 32));
+    arena_reset(ctx);
+    uint64_t *d = (uint64_t *)arena_take(ctx, nblocks * 32);
+    sitmo_blocks_kernel<<<grid1(ctx, nblocks), 256, 0, ctx->stream>>>(key[0], key[1], key[2], key[3], ctr0[0],
+                                                                      ctr0[1], ctr0[2], ctr0[3], nblocks, d);
+    CAC_CUDA_TRY(cudaGetLastError());
+    CAC_CUDA_TRY(cudaMemcpyAsync(out_host, d, nblocks * 32, cudaMemcpyDeviceToHost, ctx->stream));
+    CAC_CUDA_TRY(cudaStreamSynchronize(ctx->stream));
+    return CAC_OK;
+}
+
+int graph_create(cac_ctx *ctx, uint32_t n, uint64_t m, const uint32_t *u, const uint32_t *v, const uint32_t *w,
+                 int where, cac_graph **out) {
+    cac_graph *g = new (std::nothrow) cac_graph();
+    if (!g) { set_error("host allocation failed"); return CAC_ERR_OOM; }
+    g->ctx = ctx;
+    g->n = n;
+    g->m = m;
+    const size_t b = align_up(m * 4);
+    g->bytes = 3 * b;
+    void *p = nullptr;
+    int st = dev_alloc(ctx, &p, g->bytes ? g->bytes : 256);
+    if (st != CAC_OK) { delete g; return st; }
+    if (!g->bytes) g->bytes = 256;
+    g->u = (uint32_t *)p;
+    g->v = (uint32_t *)((char *)p + b);
+    g->w = (uint32_t *)((char *)p + 2 * b);
+    cudaStream_t s = ctx->stream;
+    const cudaMemcpyKind kind = where == CAC_DEVICE ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice;
+    auto fail = [&](int code) { dev_free(ctx, p, g->bytes); delete g; return code; };
+    if (m) {
+        if (cudaMemcpyAsync(g->u, u, m * 4, kind, s) != cudaSuccess ||
+            cudaMemcpyAsync(g->v, v, m * 4, kind, s) != cudaSuccess) {
+            set_error("edge upload failed");
+            return fail(CAC_ERR_CUDA);
+        }
+        if (w) {
+            if (cudaMemcpyAsync(g->w, w, m * 4, kind, s) != cudaSuccess) {
+                set_error("weight upload failed");
+                return fail(CAC_ERR_CUDA);
+            }
+        } else {
+            fill_u32<<<grid1(ctx, m), 256, 0, s>>>(g->w, m, 1u);
+        }
+        // validate ids and total the weights on the device
+        int st2 = arena_reserve(ctx, 256);
+        if (st2 != CAC_OK) return fail(st2);
+        arena_reset(ctx);
+        unsigned long long *d_sum = (unsigned long long *)arena_take(ctx, 16);
+        unsigned int *d_bad = (unsigned int *)(d_sum + 1);
+        cudaMemsetAsync(d_sum, 0, 16, s);
+        check_ids<<<grid1(ctx, m), 256, 0, s>>>(g->u, g->v, m, n, d_bad);
+        sum_u32<<<grid1(ctx, m), 256, 0, s>>>(g->w, m, d_sum);
+        unsigned long long hsum[2] = {0, 0};
+        if (cudaMemcpyAsync(hsum, d_sum, 16, cudaMemcpyDeviceToHost, s) != cudaSuccess ||
+            cudaStreamSynchronize(s) != cudaSuccess) {
+            set_error(std::string("graph validation failed: ") + cudaGetErrorString(cudaGetLastError()));
+            return fail(CAC_ERR_CUDA);
+        }
+        if ((unsigned int)(hsum[1] & 0xFFFFFFFFu)) {
+            set_error("edge endpoint id >= vertex count " + std::to_string(n));
+            return fail(CAC_ERR_INVALID);
+        }
+        g->total_weight = hsum[0];
+    }
+    *out = g;
+    return CAC_OK;
+}
+
+}  // namespace cac
+
+using namespace cac;
+
+extern "C" {
+
+const char *cac_error_string(int status) {
+    switch (status) {
+        case CAC_OK: return "ok";
+        case CAC_ERR_INVALID: return "invalid argument";
+        case CAC_ERR_OOM: return "out of device memory or HBM budget";
+        case CAC_ERR_PARSE: return "malformed edge-list input";
+        case CAC_ERR_CUDA: return "CUDA runtime error";
+        case CAC_ERR_TIMEOUT: return "device-side bound exceeded";
+        case CAC_ERR_UNSUPPORTED: return "unsupported request";
+        case CAC_ERR_IO: return "input could not be read";
+        default: return "unknown status";
+    }
+}
+
+const char *cac_last_error(void) { return g_last_error.c_str(); }
+
+int cac_ctx_create(const cac_config *config, cac_ctx **out) {
+    if (!out) { set_error("cac_ctx_create: out is NULL"); return CAC_ERR_INVALID; }
+    *out = nullptr;
+    cac_config cfg{};
+    if (config) cfg = *config;
+    int ndev = 0;
+    CAC_CUDA_TRY(cudaGetDeviceCount(&ndev));
+    if (cfg.device < 0 || cfg.device >= ndev) {
+        set_error("cac_ctx_create: device " + std::to_string(cfg.device) + " not present");
+        return CAC_ERR_INVALID;
+    }
+    CAC_CUDA_TRY(cudaSetDevice(cfg.device));
+    cac_ctx *ctx = new (std::nothrow) cac_ctx();
+    if (!ctx) { set_error("host allocation failed"); return CAC_ERR_OOM; }
+    ctx->device = cfg.device;
+    ctx->budget = cfg.hbm_budget_bytes;
+    if (cfg.stream) {
+        ctx->stream = (cudaStream_t)cfg.stream;
+    } else {
+        if (cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking) != cudaSuccess) {
+            delete ctx;
+            set_error("cudaStreamCreate failed");
+            return CAC_ERR_CUDA;
+        }
+        ctx->own_stream = true;
+    }
+    cudaDeviceGetAttribute(&ctx->num_sms, cudaDevAttrMultiProcessorCount, cfg.device);
+    for (auto &e : ctx->ev) cudaEventCreate(&e);
+    if (cudaMallocHost((void **)&ctx->pinned_u32, 64 * 1024) != cudaSuccess) {
+        set_error("cudaMallocHost failed");
+        cac_ctx_destroy(ctx);
+        return CAC_ERR_CUDA;
+    }
+    *out = ctx;
+    return CAC_OK;
+}
+
+int cac_ctx_destroy(cac_ctx *ctx) {
+    if (!ctx) return CAC_OK;
+    cudaSetDevice(ctx->device);
+    if (ctx->stream) cudaStreamSynchronize(ctx->stream);
+    dev_free(ctx, ctx->arena.base, ctx->arena.cap);
+    dev_free(ctx, ctx->io.base, ctx->io.cap);
+    for (auto &e : ctx->ev) if (e) cudaEventDestroy(e);
+    if (ctx->pinned_u32) cudaFreeHost(ctx->pinned_u32);
+    if (ctx->own_stream) cudaStreamDestroy(ctx->stream);
+    delete ctx;
+    return CAC_OK;
+}
+
+uint64_t cac_ctx_device_bytes(const cac_ctx *ctx) { return ctx ? ctx->held : 0; }
+
+int cac_graph_from_edges(cac_ctx *ctx, uint32_t n, uint64_t m, const uint32_t *u, const uint32_t *v,
+                         const uint32_t *w, int where, cac_graph **out) {
+    if (!ctx || !out || (m && (!u || !v)) || (where != CAC_HOST && where != CAC_DEVICE)) {
+        set_error("cac_graph_from_edges: invalid argument");
+        return CAC_ERR_INVALID;
+    }
+    if (m > 0xFFFFFFFFull) {
+        set_error("cac_graph_from_edges: more than 2^32-1 edges (the reference counts edges in unsigned)");
+        return CAC_ERR_UNSUPPORTED;
+    }
+    CAC_CUDA_TRY(cudaSetDevice(ctx->device));
+    return graph_create(ctx, n, m, u, v, w, where, out);
+}
+
+int cac_graph_free(cac_graph *g) {
+    if (!g) return CAC_OK;
+    cudaSetDevice(g->ctx->device);
+    cudaStreamSynchronize(g->ctx->stream);
+    dev_free(g->ctx, g->u, g->bytes);
+    delete g;
+    return CAC_OK;
+}
+
+int cac_graph_info(const cac_graph *g, uint32_t *n, uint64_t *m, uint64_t *total_weight) {
+    if (!g) { set_error("cac_graph_info: graph is NULL"); return CAC_ERR_INVALID; }
+    if (n) *n = g->n;
+    if (m) *m = g->m;
+    if (total_weight) *total_weight = g->total_weight;
+    return CAC_OK;
+}
+
+int cac_cc(cac_ctx *ctx, const cac_graph *g, uint32_t seed, uint32_t virtual_ranks, uint32_t *labels,
+           int labels_where, cac_cc_result *res) {
+    if (!ctx || !g || (labels && labels_where != CAC_HOST && labels_where != CAC_DEVICE)) {
+        set_error("cac_cc: invalid argument");
+        return CAC_ERR_INVALID;
+    }
+    CAC_CUDA_TRY(cudaSetDevice(ctx->device));
+    if (virtual_ranks == 0) virtual_ranks = 1;
+    uint32_t *d_labels = nullptr;
+    void *tmp = nullptr;
+    if (labels && labels_where == CAC_DEVICE) d_labels = labels;
+    if (labels && labels_where == CAC_HOST) {
+        CAC_TRY(dev_alloc(ctx, &tmp, (size_t)g->n * 4 + 4));
+        d_labels = (uint32_t *)tmp;
+    }
+    cac_cc_result r{};
+    int st = cc_run(ctx, g->n, g->m, g->u, g->v, seed, virtual_ranks, d_labels, &r);
+    if (st == CAC_OK && tmp && g->n) {
+        cudaError_t e = cudaMemcpy(labels, d_labels, (size_t)g->n * 4, cudaMemcpyDeviceToHost);
+        if (e != cudaSuccess) { set_error(cudaGetErrorString(e)); st = CAC_ERR_CUDA; }
+    }
+    if (tmp) dev_free(ctx, tmp, (size_t)g->n * 4 + 4);
+    if (res) *res = r;
+    return st;
+}
+
+int cac_cc_edges(cac_ctx *ctx, uint32_t n, uint64_t m, const uint32_t *u_host, const uint32_t *v_host,
+                 uint32_t seed, uint32_t virtual_ranks, uint32_t *labels_host, cac_cc_result *res) {
+    if (!ctx || (m && (!u_host || !v_host))) {
+        set_error("cac_cc_edges: invalid argument");
+        return CAC_ERR_INVALID;
+    }
+    CAC_CUDA_TRY(cudaSetDevice(ctx->device));
+    if (virtual_ranks == 0) virtual_ranks = 1;
+    // staging buffers for edges and labels: a grow-only arena kept by the ctx
+    const size_t be = align_up(m * 4), bl = align_up((size_t)n * 4 + 4);
+    CAC_TRY(arena_reserve(ctx, ctx->io, 2 * be + bl));
+    ctx->io.used = 0;
+    uint32_t *du = (uint32_t *)arena_take(ctx->io, m * 4);
+    uint32_t *dv = (uint32_t *)arena_take(ctx->io, m * 4);
+    uint32_t *dl = (uint32_t *)arena_take(ctx->io, (size_t)n * 4 + 4);
+    cudaStream_t s = ctx->stream;
+    int st = CAC_OK;
+    if (m && (cudaMemcpyAsync(du, u_host, m * 4, cudaMemcpyHostToDevice, s) != cudaSuccess ||
+              cudaMemcpyAsync(dv, v_host, m * 4, cudaMemcpyHostToDevice, s) != cudaSuccess)) {
+        set_error("cac_cc_edges: upload failed");
+        st = CAC_ERR_CUDA;
+    }
+    cac_cc_result r{};
+    if (st == CAC_OK) st = cc_run(ctx, n, m, du, dv, seed, virtual_ranks, labels_host ? dl : nullptr, &r);
+    if (st == CAC_OK && labels_host && n) {
+        if (cudaMemcpyAsync(labels_host, dl, (size_t)n * 4, cudaMemcpyDeviceToHost, s) != cudaSuccess ||
+            cudaStreamSynchronize(s) != cudaSuccess) {
+            set_error("cac_cc_edges: label download failed");
+            st = CAC_ERR_CUDA;
+        }
+    }
+    if (res) *res = r;
+    return st;
+}
+
+int cac_sitmo_blocks(cac_ctx *ctx, const uint64_t key[4], const uint64_t ctr0[4], uint64_t nblocks,
+                     uint64_t *out_host) {
+    if (!ctx || !key || !ctr0 || (nblocks && !out_host)) {
+        set_error("cac_sitmo_blocks: invalid argument");
+        return CAC_ERR_INVALID;
+    }
+    CAC_CUDA_TRY(cudaSetDevice(ctx->device));
+    return sitmo_blocks(ctx, key, ctr0, nblocks, out_host);
+}
+
+}  // extern "C"

@@ -1,0 +1,157 @@
+/*
+ * cac.h — C ABI of libcac, the GB300 engine for randomized minimum cuts and connected
+ * components (drop-in for the square_root / approx_cut / parallel_cc executables of
+ * PJK/comm-avoiding-cuts-cc).
+ *
+ * The reference has no library or FFI interface; its boundary is three command lines, the
+ * edge-list file format and one CSV line on stdout. The entry points below replace the
+ * callable C++ classes behind those command lines (file:line in the reference tree):
+ *
+ *   cac_graph_load_file   GraphInputIterator + AdjacencyListGraph::fromIterator
+ *                         (src/input/GraphInputIterator.hpp:9-97, src/AdjacencyListGraph.hpp:76-82)
+ *   cac_graph_from_edges  AdjacencyListGraph(vertex_count, edges) (src/AdjacencyListGraph.hpp:85-90)
+ *   cac_cc                UnweightedIteratedSparseSampling::connectedComponents
+ *                         (src/UnweightedIteratedSparseSampling.hpp:19, .cpp:40-72), driven as in
+ *                         src/executables/parallel_cc.cpp:28-44
+ *   cac_mincut            SquareRootCut::runMaster (src/SquareRootCut.hpp:84, .cpp:15-25),
+ *                         driven as in src/executables/square_root.cpp:22-40
+ *   cac_mincut_trials     the per-rank trial loop of SquareRootCut::runLowConcurrencyMaster
+ *                         (src/SquareRootCut.cpp:127-138), one value per trial
+ *   cac_ks_dense          comincut::minimum_cut on a dense graph (src/karger-stein/co_mincut.h:491-497)
+ *                         for one counter-addressed trial
+ *   cac_exact_cut         comincut::deterministic_minimum_cut (src/karger-stein/co_mincut.h:529-541)
+ *   cac_approx_cut        ApproximateCut::run (src/ApproximateCut.hpp:62, .cpp:10-79), driven as in
+ *                         src/executables/approx_cut.cpp:17-38
+ *   cac_sitmo_blocks      sitmo::prng_engine block function (lib/prng_engine.hpp:307-343)
+ *
+ * Conventions
+ *   - Every function returns an int status: CAC_OK (0) or a negative CAC_ERR_* code. The
+ *     reference throws or asserts instead (SquareRootCut.cpp:44, GraphInputIterator.hpp:19);
+ *     cac_last_error() gives the message of the calling thread's last failure.
+ *   - Buffers are owned by the caller. Arguments named *_host are host pointers; arguments with
+ *     a `where` flag may be host (CAC_HOST) or device (CAC_DEVICE) pointers.
+ *   - A cac_ctx binds one device and one CUDA stream; use one ctx per host thread (a ctx is not
+ *     thread-safe). All work of a ctx is ordered on its stream; results returned in host
+ *     structs are complete when the call returns.
+ *   - Vertex ids are uint32 in [0, n); weights uint32 >= 1 (a NULL weight array means 1);
+ *     cut values are uint64 sums.
+ *   - `virtual_ranks` is the MPI rank count the reference would have run with (mpiexec -n);
+ *     it fixes the seed layout (rank r draws with seed + r) and the trial split, not the
+ *     hardware parallelism.
+ */
+#ifndef CAC_H
+#define CAC_H
+
+#include <stdint.h>
+#include <stddef.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define CAC_OK 0
+#define CAC_ERR_INVALID (-1)     /* bad argument (sizes, ids, null pointers) */
+#define CAC_ERR_OOM (-2)         /* device allocation failed or HBM budget exceeded */
+#define CAC_ERR_PARSE (-3)       /* malformed edge-list file */
+#define CAC_ERR_CUDA (-4)        /* a CUDA runtime call failed */
+#define CAC_ERR_TIMEOUT (-5)     /* a device-side bounded wait or draw budget ran out */
+#define CAC_ERR_UNSUPPORTED (-6) /* valid request this build does not handle */
+#define CAC_ERR_IO (-7)          /* file could not be opened or read */
+
+#define CAC_HOST 0
+#define CAC_DEVICE 1
+
+typedef struct cac_ctx cac_ctx;
+typedef struct cac_graph cac_graph;
+
+typedef struct {
+    int device;                /* CUDA device ordinal */
+    void *stream;              /* cudaStream_t to order all work on; NULL: the ctx creates one */
+    uint64_t hbm_budget_bytes; /* cap on device bytes this ctx may hold; 0: no cap */
+} cac_config;
+
+/* ---- context ---- */
+int cac_ctx_create(const cac_config *config, cac_ctx **out);
+int cac_ctx_destroy(cac_ctx *ctx);
+const char *cac_error_string(int status);
+const char *cac_last_error(void);
+/* device bytes currently held by the ctx (graphs + scratch) */
+uint64_t cac_ctx_device_bytes(const cac_ctx *ctx);
+
+/* ---- graphs (device-resident) ---- */
+int cac_graph_load_file(cac_ctx *ctx, const char *path, cac_graph **out);
+int cac_graph_from_edges(cac_ctx *ctx, uint32_t n, uint64_t m, const uint32_t *u, const uint32_t *v,
+                         const uint32_t *w, int where, cac_graph **out);
+int cac_graph_free(cac_graph *g);
+int cac_graph_info(const cac_graph *g, uint32_t *n, uint64_t *m, uint64_t *total_weight);
+/* Parse an edge-list file into caller-provided host arrays (the file's m must be <= capacity). */
+int cac_parse_file(const char *path, uint32_t *n, uint64_t *m, uint32_t *u_host, uint32_t *v_host,
+                   uint32_t *w_host, uint64_t capacity);
+/* Read only the header (vertex and edge counts) of an edge-list file. */
+int cac_parse_header(const char *path, uint32_t *n, uint64_t *m);
+
+/* ---- connected components (parallel_cc) ---- */
+typedef struct {
+    uint32_t num_components; /* the count parallel_cc prints */
+    uint32_t rounds;         /* sampling rounds + the closing pass over all edges */
+    uint64_t sampled_edges;  /* edges drawn in the sampling round */
+    float device_ms;         /* device time of the whole call on the ctx stream */
+    float edge_pass_ms;      /* device time of the closing pass over all edges */
+} cac_cc_result;
+
+/* labels (nullable): label(v) = rank of the smallest vertex of v's component among all
+ * component minima, identical to the reference's labels. `labels_where` says whether
+ * `labels` is a host or device pointer. */
+int cac_cc(cac_ctx *ctx, const cac_graph *g, uint32_t seed, uint32_t virtual_ranks, uint32_t *labels,
+           int labels_where, cac_cc_result *res);
+/* The same from host edge arrays to host labels in one call (host<->device copies included). */
+int cac_cc_edges(cac_ctx *ctx, uint32_t n, uint64_t m, const uint32_t *u_host, const uint32_t *v_host,
+                 uint32_t seed, uint32_t virtual_ranks, uint32_t *labels_host, cac_cc_result *res);
+
+/* ---- minimum cut (square_root) ---- */
+typedef struct {
+    uint64_t cut;             /* the CSV `weight` column */
+    uint32_t trials_per_rank; /* the CSV `trials` column: ceil(total / virtual_ranks) */
+    uint32_t total_trials;    /* trials executed: virtual_ranks * trials_per_rank */
+    uint32_t intermediate;    /* t = min(n, ceil(2 sqrt(m) + 1)) */
+    uint32_t high_concurrency;/* 1 when the reference would have used its group variant */
+    float device_ms;
+} cac_mincut_result;
+
+int cac_mincut(cac_ctx *ctx, const cac_graph *g, double success_probability, uint32_t seed,
+               uint32_t virtual_ranks, cac_mincut_result *res);
+/* Run trials (r, i) for r < virtual_ranks, i < trials_per_rank and write each trial's cut to
+ * cuts_host[r * trials_per_rank + i]. */
+int cac_mincut_trials(cac_ctx *ctx, const cac_graph *g, uint32_t seed, uint32_t virtual_ranks,
+                      uint32_t trials_per_rank, uint64_t *cuts_host);
+/* One Karger-Stein trial (virtual rank, trial index) on a dense symmetric n x n host matrix. */
+int cac_ks_dense(cac_ctx *ctx, uint32_t n, const uint64_t *mat_host, uint32_t seed, uint32_t rank, uint32_t trial,
+                 uint64_t *cut);
+/* Exact minimum cut of a dense symmetric n x n host matrix with n <= 128, computed by the
+ * device Stoer-Wagner kernel that solves the Karger-Stein leaves
+ * (src/karger-stein/co_mincut_base_case.hpp:52-144 in the reference). */
+int cac_exact_cut_small(cac_ctx *ctx, uint32_t n, const uint64_t *mat_host, uint64_t *cut);
+
+/* ---- approximate cut (approx_cut) ---- */
+typedef struct {
+    uint64_t cut;       /* the CSV `weight` column: 2^level */
+    uint32_t trials;    /* the CSV `trials` column: copies * level */
+    uint32_t copies;    /* ceil(ln(1-p) / ln(1-e^-0.75)) */
+    uint32_t level;     /* first level with more than `copies` components (0: none) */
+    float device_ms;
+} cac_approx_result;
+
+int cac_approx_cut(cac_ctx *ctx, const cac_graph *g, double success_probability, uint32_t seed,
+                   uint32_t virtual_ranks, cac_approx_result *res);
+
+/* ---- primitives ---- */
+/* nblocks sitmo blocks with key `key` and counters ctr0, ctr0 + 1, ... (256-bit add);
+ * out_host receives 4 * nblocks uint64 words. */
+int cac_sitmo_blocks(cac_ctx *ctx, const uint64_t key[4], const uint64_t ctr0[4], uint64_t nblocks,
+                     uint64_t *out_host);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif

@@ -1,0 +1,218 @@
+/*
+ * ORACLE (test infrastructure) — connected components.
+ *
+ * orc_cc_labels: the closed form of the reference's CC output. The reference relabels the
+ * vertices of every round by first appearance over j = 0..n-1
+ * (src/IteratedSparseSampling.hpp:210-220) and composes the maps across rounds
+ * (src/UnweightedIteratedSparseSampling.cpp:60-62); both steps preserve the order of
+ * component minima, so the final label of v is the rank of min(component(v)) among all
+ * component minima. Computed here with a plain union-find over every edge.
+ *
+ * orc_cc_iss: a step-by-step restatement of the reference's iterated-sparse-sampling loop,
+ * kept as the CPU baseline of the same work (sampling, gather, shuffle, prefix union-find,
+ * relabel, slice rewrite). Its labels must equal orc_cc_labels for every seed.
+ */
+#include <stdlib.h>
+#include <string.h>
+#include <math.h>
+#include "oracle.h"
+
+static uint32_t uf_find_halving(uint32_t *p, uint32_t x) {
+    while (p[x] != x) {
+        p[x] = p[p[x]];
+        x = p[x];
+    }
+    return x;
+}
+
+uint32_t orc_cc_labels(uint32_t n, uint64_t m, const uint32_t *u, const uint32_t *v, uint32_t *labels) {
+    uint32_t *p = (uint32_t *)malloc(sizeof(uint32_t) * (n ? n : 1));
+    for (uint32_t i = 0; i < n; i++) p[i] = i;
+    for (uint64_t e = 0; e < m; e++) {
+        uint32_t a = uf_find_halving(p, u[e]), b = uf_find_halving(p, v[e]);
+        if (a == b) continue;
+        if (a < b) p[b] = a; else p[a] = b; /* the smaller id stays root */
+    }
+    uint32_t count = 0;
+    for (uint32_t i = 0; i < n; i++) {
+        uint32_t r = uf_find_halving(p, i);
+        if (r == i) { if (labels) labels[i] = count; count++; }
+        else if (labels) labels[i] = labels[r]; /* r < i, already labelled */
+    }
+    free(p);
+    return count;
+}
+
+/* ---- restatement of the reference's ISS CC ---- */
+
+/* sitmo::prng_engine(seed) as a sequential 32-bit stream (lib/prng_engine.hpp:195-212). */
+typedef struct { uint64_t key[4]; uint64_t block; uint64_t out[4]; unsigned pos; } seq_engine;
+
+static void eng_init(seq_engine *e, uint32_t seed) {
+    memset(e, 0, sizeof(*e));
+    e->key[0] = seed;
+    e->pos = 8; /* forces a block computation at the first call */
+    e->block = (uint64_t)-1;
+}
+
+static uint32_t eng_next(seq_engine *e) {
+    if (e->pos == 8) {
+        e->block++;
+        uint64_t ctr[4] = {e->block, 0, 0, 0};
+        orc_sitmo_block(e->key, ctr, e->out);
+        e->pos = 0;
+    }
+    unsigned k = e->pos++;
+    uint64_t w = e->out[k >> 1];
+    return (k & 1) ? (uint32_t)(w >> 32) : (uint32_t)w;
+}
+
+/* union by rank + full path compression (the algorithm of the Boost disjoint_sets the
+ * reference wraps in src/DisjointSets.hpp:7-42) */
+static uint32_t ds_find(uint32_t *parent, uint32_t x) {
+    uint32_t r = x;
+    while (parent[r] != r) r = parent[r];
+    while (parent[x] != r) { uint32_t nx = parent[x]; parent[x] = r; x = nx; }
+    return r;
+}
+static void ds_link(uint32_t *parent, uint8_t *rank, uint32_t a, uint32_t b) {
+    if (rank[a] > rank[b]) parent[b] = a;
+    else { parent[a] = b; if (rank[a] == rank[b]) rank[b]++; }
+}
+
+uint64_t orc_cc_sample_count(uint32_t n, uint64_t edges_left) {
+    /* unsigned(std::pow((float)n0, 1 + eps/2) * (1 + delta)), eps = 0.09f, delta = 0.2f */
+    uint64_t s = (uint64_t)(uint32_t)(powf((float)n, 1.0f + 0.09f / 2) * (1.0f + 0.2f));
+    return s < edges_left ? s : edges_left;
+}
+
+/* UnweightedIteratedSparseSampling::edgesToSamplePerProcessor (.cpp:80-128), uint32 wraps kept */
+static void edges_to_sample(uint32_t n0, uint32_t ranks, const int *avail, int *per) {
+    uint32_t total = 0;
+    for (uint32_t i = 0; i < ranks; i++) total += (uint32_t)avail[i];
+    uint32_t want = (uint32_t)(powf((float)n0, 1.0f + 0.09f / 2) * (1.0f + 0.2f));
+    uint32_t to_sample = want < total ? want : total;
+    uint32_t threshold = (uint32_t)(3.0f / (0.2f * 0.2f) * logf((float)ranks / 0.9f));
+    uint32_t remaining = to_sample;
+    for (uint32_t i = 0; i < ranks; i++) per[i] = 0;
+    for (uint32_t i = 0; i < ranks; i++) {
+        if ((uint32_t)avail[i] <= threshold) {
+            per[i] = avail[i];
+            remaining -= (uint32_t)avail[i];
+            to_sample -= (uint32_t)avail[i];
+        }
+    }
+    for (uint32_t i = 0; i < ranks; i++) {
+        if (per[i] != 0) continue;
+        int share = (int)((float)to_sample * (float)avail[i] / (float)total);
+        per[i] = share < avail[i] ? share : avail[i];
+        remaining -= (uint32_t)per[i];
+    }
+    for (uint32_t sp = 0; remaining > 0 && sp < ranks; sp++) {
+        if (avail[sp] > per[sp]) {
+            uint32_t room = (uint32_t)(avail[sp] - per[sp]);
+            uint32_t delta = room < remaining ? room : remaining;
+            per[sp] += (int)delta;
+            remaining -= delta;
+        }
+    }
+}
+
+uint32_t orc_cc_iss(uint32_t n, uint64_t m, const uint32_t *u, const uint32_t *v, uint32_t seed, uint32_t ranks,
+                    uint32_t *labels, uint32_t *rounds_out) {
+    if (ranks == 0) ranks = 1;
+    /* slices: rank r owns lines [r*floor(m/P), (r+1)*floor(m/P)), the last rank the rest
+     * (UnweightedIteratedSparseSampling.cpp:5-21) */
+    uint32_t **su = (uint32_t **)calloc(ranks, sizeof(uint32_t *));
+    uint32_t **sv = (uint32_t **)calloc(ranks, sizeof(uint32_t *));
+    uint64_t *len = (uint64_t *)calloc(ranks, sizeof(uint64_t));
+    seq_engine *eng = (seq_engine *)calloc(ranks, sizeof(seq_engine));
+    uint64_t portion = m / ranks;
+    for (uint32_t r = 0; r < ranks; r++) {
+        uint64_t from = portion * r, to = (r == ranks - 1) ? m : portion * (r + 1);
+        len[r] = to - from;
+        su[r] = (uint32_t *)malloc(sizeof(uint32_t) * (len[r] ? len[r] : 1));
+        sv[r] = (uint32_t *)malloc(sizeof(uint32_t) * (len[r] ? len[r] : 1));
+        memcpy(su[r], u + from, sizeof(uint32_t) * len[r]);
+        memcpy(sv[r], v + from, sizeof(uint32_t) * len[r]);
+        eng_init(&eng[r], seed + r);
+    }
+    uint32_t *comp = (uint32_t *)malloc(sizeof(uint32_t) * (n ? n : 1));
+    for (uint32_t i = 0; i < n; i++) comp[i] = i;
+    uint32_t vcount = n, rounds = 0;
+    int *avail = (int *)malloc(sizeof(int) * ranks), *per = (int *)malloc(sizeof(int) * ranks);
+    uint32_t *parent = (uint32_t *)malloc(sizeof(uint32_t) * (n ? n : 1));
+    uint8_t *rk = (uint8_t *)malloc(n ? n : 1);
+    int64_t *lab = (int64_t *)malloc(sizeof(int64_t) * (n ? n : 1));
+    uint32_t *map = (uint32_t *)malloc(sizeof(uint32_t) * (n ? n : 1));
+
+    for (;;) {
+        uint64_t left = 0;
+        for (uint32_t r = 0; r < ranks; r++) left += len[r];
+        if (left == 0) break;
+        rounds++;
+        for (uint32_t r = 0; r < ranks; r++) avail[r] = (int)len[r];
+        edges_to_sample(n, ranks, avail, per);
+        uint64_t total = 0;
+        for (uint32_t r = 0; r < ranks; r++) total += (uint64_t)per[r];
+        /* sample (.cpp:24-37) and gather in rank order (IteratedSparseSampling.hpp:261-271) */
+        uint32_t *gu = (uint32_t *)malloc(sizeof(uint32_t) * (total ? total : 1));
+        uint32_t *gv = (uint32_t *)malloc(sizeof(uint32_t) * (total ? total : 1));
+        uint64_t at = 0;
+        for (uint32_t r = 0; r < ranks; r++) {
+            if ((uint64_t)per[r] == len[r]) {
+                memcpy(gu + at, su[r], sizeof(uint32_t) * len[r]);
+                memcpy(gv + at, sv[r], sizeof(uint32_t) * len[r]);
+                at += len[r];
+            } else {
+                for (int k = 0; k < per[r]; k++) {
+                    uint64_t idx = eng_next(&eng[r]) % (uint32_t)len[r];
+                    gu[at] = su[r][idx];
+                    gv[at] = sv[r][idx];
+                    at++;
+                }
+            }
+        }
+        /* shuffle with the root's engine (IteratedSparseSampling.hpp:278). Fisher-Yates with
+         * modulo draws: libstdc++'s std::shuffle consumes the engine differently, which only
+         * changes the order in which the prefix union-find meets the samples, never the
+         * labels (the target is a single component). */
+        for (uint64_t i = total; i > 1; i--) {
+            uint64_t j = eng_next(&eng[0]) % i;
+            uint32_t t = gu[i - 1]; gu[i - 1] = gu[j]; gu[j] = t;
+            t = gv[i - 1]; gv[i - 1] = gv[j]; gv[j] = t;
+        }
+        /* prefix union-find to one component (IteratedSparseSampling.hpp:182-224) */
+        for (uint32_t i = 0; i < vcount; i++) { parent[i] = i; rk[i] = 0; }
+        uint32_t active = vcount;
+        for (uint64_t i = 0; i < total && active > 1; i++) {
+            uint32_t a = ds_find(parent, gu[i]), b = ds_find(parent, gv[i]);
+            if (a != b) { active--; ds_link(parent, rk, a, b); }
+        }
+        for (uint32_t j = 0; j < vcount; j++) lab[j] = -1;
+        uint32_t next = 0;
+        for (uint32_t j = 0; j < vcount; j++) {
+            uint32_t r = ds_find(parent, j);
+            if (lab[r] < 0) lab[r] = next++;
+            map[j] = (uint32_t)lab[r];
+        }
+        for (uint32_t i = 0; i < n; i++) comp[i] = map[comp[i]];
+        /* every rank rewrites its slice and drops loops (IteratedSparseSampling.hpp:160-172) */
+        for (uint32_t r = 0; r < ranks; r++) {
+            uint64_t w = 0;
+            for (uint64_t e = 0; e < len[r]; e++) {
+                uint32_t a = map[su[r][e]], b = map[sv[r][e]];
+                if (a != b) { su[r][w] = a; sv[r][w] = b; w++; }
+            }
+            len[r] = w;
+        }
+        vcount = active;
+        free(gu); free(gv);
+    }
+    if (labels) memcpy(labels, comp, sizeof(uint32_t) * n);
+    if (rounds_out) *rounds_out = rounds;
+    for (uint32_t r = 0; r < ranks; r++) { free(su[r]); free(sv[r]); }
+    free(su); free(sv); free(len); free(eng); free(comp); free(avail); free(per);
+    free(parent); free(rk); free(lab); free(map);
+    return vcount;
+}

@@ -1,0 +1,186 @@
+"""ORACLE (test infrastructure): ctypes binding of oracle/lib/liboracle.so.
+
+Only tests/, __graft_entry__.smoke() and bench.py's CPU-baseline legs import this module; it
+is the checker, never the product. Build the library with ``make -C oracle``.
+"""
+import ctypes
+import os
+
+import numpy as np
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+_LIB = None
+
+_u32p = ctypes.POINTER(ctypes.c_uint32)
+_u64p = ctypes.POINTER(ctypes.c_uint64)
+
+
+def lib():
+    global _LIB
+    if _LIB is None:
+        path = os.path.join(_HERE, "lib", "liboracle.so")
+        if not os.path.exists(path):
+            raise RuntimeError("oracle library missing: run `make -C oracle` (or __graft_entry__.build())")
+        L = ctypes.CDLL(path)
+        L.orc_sitmo_block.argtypes = [_u64p, _u64p, _u64p]
+        L.orc_sitmo_seed_output.argtypes = [ctypes.c_uint32, ctypes.c_uint64]
+        L.orc_sitmo_seed_output.restype = ctypes.c_uint32
+        L.orc_sitmo_outputs.argtypes = [_u64p, _u64p, ctypes.c_uint64, _u32p]
+        L.orc_draw64.argtypes = [_u64p, ctypes.c_uint64, ctypes.c_uint64]
+        L.orc_draw64.restype = ctypes.c_uint64
+        L.orc_cc_labels.argtypes = [ctypes.c_uint32, ctypes.c_uint64, _u32p, _u32p, _u32p]
+        L.orc_cc_labels.restype = ctypes.c_uint32
+        L.orc_cc_iss.argtypes = [ctypes.c_uint32, ctypes.c_uint64, _u32p, _u32p, ctypes.c_uint32, ctypes.c_uint32,
+                                 _u32p, _u32p]
+        L.orc_cc_iss.restype = ctypes.c_uint32
+        L.orc_cc_sample_count.argtypes = [ctypes.c_uint32, ctypes.c_uint64]
+        L.orc_cc_sample_count.restype = ctypes.c_uint64
+        L.orc_stoer_wagner_dense.argtypes = [ctypes.c_uint32, _u64p]
+        L.orc_stoer_wagner_dense.restype = ctypes.c_uint64
+        L.orc_exact_mincut.argtypes = [ctypes.c_uint32, ctypes.c_uint64, _u32p, _u32p, _u32p]
+        L.orc_exact_mincut.restype = ctypes.c_uint64
+        L.orc_intermediate_size.argtypes = [ctypes.c_uint32, ctypes.c_uint64]
+        L.orc_intermediate_size.restype = ctypes.c_uint32
+        L.orc_number_of_trials.argtypes = [ctypes.c_uint32, ctypes.c_uint64, ctypes.c_double]
+        L.orc_number_of_trials.restype = ctypes.c_uint32
+        L.orc_min_success_in_one_trial.argtypes = [ctypes.c_int]
+        L.orc_min_success_in_one_trial.restype = ctypes.c_double
+        L.orc_ks_target.argtypes = [ctypes.c_int]
+        L.orc_ks_target.restype = ctypes.c_int
+        L.orc_mincut_trial.argtypes = [ctypes.c_uint32, ctypes.c_uint64, _u32p, _u32p, _u32p, ctypes.c_uint32,
+                                       ctypes.c_uint32, ctypes.c_uint32]
+        L.orc_mincut_trial.restype = ctypes.c_uint64
+        L.orc_ks_dense.argtypes = [ctypes.c_uint32, _u64p, ctypes.c_uint32, ctypes.c_uint32, ctypes.c_uint32]
+        L.orc_ks_dense.restype = ctypes.c_uint64
+        L.orc_shrink_to_dense.argtypes = [ctypes.c_uint32, ctypes.c_uint64, _u32p, _u32p, _u32p, ctypes.c_uint32,
+                                          ctypes.c_uint32, ctypes.c_uint32, ctypes.c_uint32, _u64p]
+        L.orc_shrink_to_dense.restype = ctypes.c_uint32
+        L.orc_square_root.argtypes = [ctypes.c_uint32, ctypes.c_uint64, _u32p, _u32p, _u32p, ctypes.c_double,
+                                      ctypes.c_uint32, ctypes.c_uint32, _u32p]
+        L.orc_square_root.restype = ctypes.c_uint64
+        L.orc_approx_trials.argtypes = [ctypes.c_double]
+        L.orc_approx_trials.restype = ctypes.c_uint32
+        L.orc_keep_threshold.argtypes = [ctypes.c_uint32, ctypes.c_uint32]
+        L.orc_keep_threshold.restype = ctypes.c_uint64
+        L.orc_approx_cut.argtypes = [ctypes.c_uint32, ctypes.c_uint64, _u32p, _u32p, _u32p, ctypes.c_double,
+                                     ctypes.c_uint32, ctypes.c_uint32, _u32p]
+        L.orc_approx_cut.restype = ctypes.c_uint64
+        _LIB = L
+    return _LIB
+
+
+def _p32(a):
+    return a.ctypes.data_as(_u32p)
+
+
+def _p64(a):
+    return a.ctypes.data_as(_u64p)
+
+
+def _c32(a):
+    return np.ascontiguousarray(a, dtype=np.uint32)
+
+
+def sitmo_block(key, ctr):
+    k = np.array(key, dtype=np.uint64)
+    c = np.array(ctr, dtype=np.uint64)
+    out = np.zeros(4, dtype=np.uint64)
+    lib().orc_sitmo_block(_p64(k), _p64(c), _p64(out))
+    return out
+
+
+def sitmo_outputs(key, ctr, count):
+    k = np.array(key, dtype=np.uint64)
+    c = np.array(ctr, dtype=np.uint64)
+    out = np.zeros(count, dtype=np.uint32)
+    lib().orc_sitmo_outputs(_p64(k), _p64(c), count, _p32(out))
+    return out
+
+
+def draw64(key, rnd, d):
+    k = np.array(key, dtype=np.uint64)
+    return int(lib().orc_draw64(_p64(k), rnd, d))
+
+
+def cc_labels(n, u, v):
+    u, v = _c32(u), _c32(v)
+    labels = np.zeros(max(n, 1), dtype=np.uint32)
+    count = lib().orc_cc_labels(n, len(u), _p32(u), _p32(v), _p32(labels))
+    return int(count), labels[:n]
+
+
+def cc_iss(n, u, v, seed, ranks=1):
+    u, v = _c32(u), _c32(v)
+    labels = np.zeros(max(n, 1), dtype=np.uint32)
+    rounds = np.zeros(1, dtype=np.uint32)
+    count = lib().orc_cc_iss(n, len(u), _p32(u), _p32(v), seed, ranks, _p32(labels), _p32(rounds))
+    return int(count), labels[:n], int(rounds[0])
+
+
+def cc_sample_count(n, edges_left):
+    return int(lib().orc_cc_sample_count(n, edges_left))
+
+
+def stoer_wagner_dense(mat):
+    m = np.ascontiguousarray(mat, dtype=np.uint64).copy()
+    return int(lib().orc_stoer_wagner_dense(m.shape[0], _p64(m)))
+
+
+def exact_mincut(n, u, v, w):
+    u, v, w = _c32(u), _c32(v), _c32(w)
+    return int(lib().orc_exact_mincut(n, len(u), _p32(u), _p32(v), _p32(w)))
+
+
+def intermediate_size(n, m):
+    return int(lib().orc_intermediate_size(n, m))
+
+
+def number_of_trials(n, m, p):
+    return int(lib().orc_number_of_trials(n, m, p))
+
+
+def min_success_in_one_trial(n):
+    return float(lib().orc_min_success_in_one_trial(n))
+
+
+def ks_target(n):
+    return int(lib().orc_ks_target(n))
+
+
+def mincut_trial(n, u, v, w, seed, rank, trial):
+    u, v, w = _c32(u), _c32(v), _c32(w)
+    return int(lib().orc_mincut_trial(n, len(u), _p32(u), _p32(v), _p32(w), seed, rank, trial))
+
+
+def ks_dense(mat, seed, rank, trial):
+    m = np.ascontiguousarray(mat, dtype=np.uint64)
+    return int(lib().orc_ks_dense(m.shape[0], _p64(m), seed, rank, trial))
+
+
+def shrink_to_dense(n, u, v, w, target, seed, rank, trial):
+    u, v, w = _c32(u), _c32(v), _c32(w)
+    out = np.zeros(max(n, 1) * max(n, 1), dtype=np.uint64)
+    k = lib().orc_shrink_to_dense(n, len(u), _p32(u), _p32(v), _p32(w), target, seed, rank, trial, _p64(out))
+    return int(k), out[: k * k].reshape(k, k)
+
+
+def square_root(n, u, v, w, p, seed, ranks=1):
+    u, v, w = _c32(u), _c32(v), _c32(w)
+    per = np.zeros(1, dtype=np.uint32)
+    cut = lib().orc_square_root(n, len(u), _p32(u), _p32(v), _p32(w), p, seed, ranks, _p32(per))
+    return int(cut), int(per[0])
+
+
+def approx_trials(p):
+    return int(lib().orc_approx_trials(p))
+
+
+def keep_threshold(level, w):
+    return int(lib().orc_keep_threshold(level, w))
+
+
+def approx_cut(n, u, v, w, p, seed, ranks=1):
+    u, v, w = _c32(u), _c32(v), _c32(w)
+    lv = np.zeros(1, dtype=np.uint32)
+    cut = lib().orc_approx_cut(n, len(u), _p32(u), _p32(v), _p32(w), p, seed, ranks, _p32(lv))
+    return int(cut), int(lv[0])

@@ -1,0 +1,132 @@
+"""Regenerates the golden fixtures of tests/golden/ from the reference itself.
+
+Runs the reference's own code, compiled unmodified by oracle/refbuild into oracle/_ref/
+(single-rank MPI stand-in + union-by-rank disjoint-sets stand-in), on
+  * the reference's known-answer inputs (test_inputs/*.graph),
+  * seeded synthetic graphs from graphgen (regenerated from their specs at test time),
+and records its outputs. Only runs where the reference tree is mounted:
+
+    make -C oracle/refbuild REF=/root/reference && python tests/golden/make_golden.py
+"""
+import hashlib
+import json
+import os
+import subprocess
+import sys
+import tempfile
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(os.path.dirname(HERE))
+REF_TREE = "/root/reference"
+REF_BIN = os.path.join(ROOT, "oracle", "_ref")
+sys.path.insert(0, os.path.join(ROOT, "comm-avoiding-cuts-cc_gb300"))
+import graphgen  # noqa: E402
+
+
+def run(*args):
+    return subprocess.run([os.path.join(REF_BIN, args[0])] + [str(a) for a in args[1:]], capture_output=True,
+                          text=True, check=True).stdout
+
+
+def labels_of(path, seed=0):
+    out = run("cc_labels", path, seed).split()
+    count, n = int(out[0]), int(out[1])
+    return count, np.array(out[2:2 + n], dtype=np.uint32)
+
+
+def digest(a):
+    return hashlib.sha256(np.ascontiguousarray(a, dtype="<u4").tobytes()).hexdigest()
+
+
+def make_spec(spec):
+    kind = spec["kind"]
+    if kind == "er":
+        return graphgen.erdos_renyi(spec["n"], spec["p"], spec["seed"], wmax=spec.get("wmax", 42))
+    if kind == "er_m":
+        return graphgen.erdos_renyi_m(spec["n"], spec["deg"], spec["seed"], wmax=spec.get("wmax", 100))
+    if kind == "ba":
+        return graphgen.barabasi_albert(spec["n"], spec["attach"], spec["seed"])
+    if kind == "rmat":
+        return graphgen.rmat(spec["scale"], spec["ef"], spec["seed"])
+    if kind == "ws":
+        return graphgen.watts_strogatz(spec["n"], spec["k"], spec["p"], spec["seed"], wmax=spec.get("wmax", 100))
+    if kind == "complete":
+        return graphgen.complete(spec["n"], spec["seed"], wmax=spec.get("wmax", 42))
+    raise ValueError(kind)
+
+
+CC_SPECS = [
+    {"name": "er_sparse_5k", "kind": "er", "n": 5000, "p": 0.0002, "seed": 3, "wmax": 1},
+    {"name": "er_m_20k", "kind": "er_m", "n": 20000, "deg": 1.2, "seed": 4, "wmax": 1},
+    {"name": "ba_20k_3", "kind": "ba", "n": 20000, "attach": 3, "seed": 5},
+    {"name": "rmat_14", "kind": "rmat", "scale": 14, "ef": 4, "seed": 6},
+    {"name": "rmat_16", "kind": "rmat", "scale": 16, "ef": 16, "seed": 7},
+]
+
+CUT_SPECS = [
+    {"name": "er_200", "kind": "er", "n": 200, "p": 0.08, "seed": 11},
+    {"name": "ws_300_6", "kind": "ws", "n": 300, "k": 6, "p": 0.4, "seed": 12},
+    {"name": "er_m_500", "kind": "er_m", "n": 500, "deg": 10, "seed": 13},
+    {"name": "k_150", "kind": "complete", "n": 150, "seed": 14},
+    {"name": "er_1000_c1", "kind": "er", "n": 1000, "p": 0.05, "seed": 0},
+]
+
+
+def main():
+    if not os.path.isdir(REF_TREE) or not os.path.exists(os.path.join(REF_BIN, "cc_labels")):
+        sys.exit("needs the reference tree and oracle/_ref (make -C oracle/refbuild)")
+    # 1. sitmo known answers from the reference engine
+    with open(os.path.join(HERE, "sitmo_kat.txt"), "w") as f:
+        f.write(run("sitmo_kat"))
+    # 2. the reference's known-answer inputs
+    known = {}
+    tdir = os.path.join(REF_TREE, "test_inputs")
+    for fn in sorted(os.listdir(tdir)):
+        path = os.path.join(tdir, fn)
+        n, u, v, w = graphgen.read_graph(path)
+        rec = {"n": n, "u": u.tolist(), "v": v.tolist(), "w": w.tolist()}
+        if fn.startswith("cc_"):
+            count, lab = labels_of(path)
+            rec["cc_count"] = count
+            rec["cc_labels"] = lab.tolist()
+            rec["parallel_cc_csv_count"] = int(run("parallel_cc", path, 0).strip().split(",")[-1])
+        else:
+            rec["exact_cut"] = int(run("exact_cut", path).strip())
+            rec["square_root_cut"] = int(run("square_root", 0.95, path, 0).strip().split(",")[-1])
+            rec["karger_stein_cut"] = int(run("karger_stein", path, 0).strip().split(",")[-1])
+            rec["approx_cut_reference"] = int(run("approx_cut", 0.9, path, 0).strip().split(",")[-1])
+        known[fn] = rec
+    with open(os.path.join(HERE, "ref_test_inputs.json"), "w") as f:
+        json.dump(known, f, indent=1)
+    # 3. seeded graphs: CC labels and min cuts from the reference
+    out_cc, out_cut = [], []
+    with tempfile.TemporaryDirectory() as td:
+        for spec in CC_SPECS:
+            n, u, v, w = make_spec(spec)
+            path = os.path.join(td, spec["name"] + ".in")
+            graphgen.write_graph(path, n, u, v, np.ones_like(w), spec["name"])
+            count, lab = labels_of(path, 1)
+            rec = dict(spec, m=int(len(u)), cc_count=count, labels_sha256=digest(lab),
+                       edges_sha256=digest(np.concatenate([u, v])))
+            out_cc.append(rec)
+        for spec in CUT_SPECS:
+            n, u, v, w = make_spec(spec)
+            path = os.path.join(td, spec["name"] + ".in")
+            graphgen.write_graph(path, n, u, v, w, spec["name"])
+            rec = dict(spec, m=int(len(u)), edges_sha256=digest(np.concatenate([u, v, w])))
+            rec["exact_cut"] = int(run("exact_cut", path).strip())
+            csv = run("square_root", 0.95, path, 0).strip().split(",")
+            rec["square_root_cut"] = int(csv[-1])
+            rec["square_root_trials"] = int(csv[7])
+            out_cut.append(rec)
+    with open(os.path.join(HERE, "cc_seeded.json"), "w") as f:
+        json.dump(out_cc, f, indent=1)
+    with open(os.path.join(HERE, "mincut_seeded.json"), "w") as f:
+        json.dump(out_cut, f, indent=1)
+    print("golden fixtures written to", HERE)
+
+
+if __name__ == "__main__":
+    main()

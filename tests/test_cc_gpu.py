@@ -1,0 +1,122 @@
+"""Parity of the CUDA connected-components path with the reference's labels (through the C ABI)."""
+import numpy as np
+import pytest
+
+import graphgen
+import pyoracle as O
+from conftest import digest, make_graph
+
+pytestmark = pytest.mark.gpu
+
+
+def test_reference_test_inputs(golden, ctx):
+    ref = golden("ref_test_inputs.json")
+    for name in ("cc_8.graph", "cc_13.graph"):
+        r = ref[name]
+        g = ctx.graph(r["n"], r["u"], r["v"], r["w"])
+        for ranks in (1, 2, 4):
+            count, lab, res = g.connected_components(seed=0, virtual_ranks=ranks)
+            assert count == r["cc_count"] == 5
+            assert lab.tolist() == r["cc_labels"]
+
+
+@pytest.mark.parametrize("idx", range(5))
+def test_seeded_graphs_match_reference_labels(golden, ctx, idx):
+    spec = golden("cc_seeded.json")[idx]
+    n, u, v, w = make_graph(spec)
+    g = ctx.graph(n, u, v)
+    for seed, ranks in ((1, 1), (7, 3), (2, 16)):
+        count, lab, res = g.connected_components(seed=seed, virtual_ranks=ranks)
+        assert count == spec["cc_count"]
+        assert digest(lab) == spec["labels_sha256"]
+
+
+@pytest.mark.parametrize("case", ["empty", "no_edges", "self_loops", "duplicates", "path_desc", "star", "two_paths"])
+def test_edge_cases(ctx, case):
+    if case == "empty":
+        n, u, v = 0, [], []
+    elif case == "no_edges":
+        n, u, v = 7, [], []
+    elif case == "self_loops":
+        n, u, v = 6, [0, 3, 3, 5], [0, 3, 3, 5]
+    elif case == "duplicates":
+        n, u, v = 9, [1, 1, 8, 1, 8, 2], [8, 8, 1, 8, 1, 3]
+    elif case == "path_desc":  # a long chain given from the high end: deep union-find paths
+        n = 50000
+        u = np.arange(n - 1, 0, -1, dtype=np.uint32)
+        v = u - 1
+    elif case == "star":
+        n = 100001
+        u = np.zeros(n - 1, np.uint32)
+        v = np.arange(1, n, dtype=np.uint32)
+    else:
+        n = 40001
+        u = np.concatenate([np.arange(0, 20000, 2), np.arange(1, 20001, 2)]).astype(np.uint32)
+        v = (u + 2).astype(np.uint32)
+    u = np.asarray(u, np.uint32)
+    v = np.asarray(v, np.uint32)
+    want_count, want = O.cc_labels(n, u, v)
+    g = ctx.graph(n, u, v)
+    count, lab, _ = g.connected_components(seed=3)
+    assert count == want_count
+    if n:
+        assert np.array_equal(lab, want)
+
+
+def test_unaligned_device_edges_and_device_labels(ctx):
+    torch = pytest.importorskip("torch")
+    n, u, v, _ = graphgen.erdos_renyi_m(30000, 1.5, 9, wmax=1)
+    want_count, want = O.cc_labels(n, u, v)
+    m = len(u)
+    # device edge arrays starting 4 bytes past a 16-byte boundary take the scalar path
+    du = torch.zeros(m + 1, dtype=torch.int32, device="cuda")
+    dv = torch.zeros(m + 1, dtype=torch.int32, device="cuda")
+    du[1:] = torch.from_numpy(u.view(np.int32)).cuda()
+    dv[1:] = torch.from_numpy(v.view(np.int32)).cuda()
+    torch.cuda.synchronize()
+    g = ctx.graph(n, du[1:], dv[1:])
+    out = torch.full((n,), -1, dtype=torch.int32, device="cuda")
+    count, lab, _ = g.connected_components(seed=0, out=out)
+    torch.cuda.synchronize()
+    assert count == want_count
+    assert np.array_equal(out.cpu().numpy().view(np.uint32), want)
+
+
+def test_repeated_runs_are_identical(ctx):
+    n, u, v, _ = graphgen.rmat(16, 8, 21)
+    want_count, want = O.cc_labels(n, u, v)
+    g = ctx.graph(n, u, v)
+    for seed in range(6):
+        count, lab, _ = g.connected_components(seed=seed, virtual_ranks=1 + seed)
+        assert count == want_count and np.array_equal(lab, want)
+
+
+def test_one_call_host_entry_point(ctx):
+    n, u, v, _ = graphgen.barabasi_albert(50000, 4, 2)
+    want_count, want = O.cc_labels(n, u, v)
+    lab = np.zeros(n, np.uint32)
+    res = ctx.cc_edges(n, u, v, seed=5, virtual_ranks=2, labels=lab)
+    assert res.num_components == want_count and np.array_equal(lab, want)
+    assert res.sampled_edges == O.cc_sample_count(n, len(u))
+
+
+@pytest.mark.slow
+def test_full_size_ba_1m(ctx):
+    n, u, v, _ = graphgen.barabasi_albert(1024000, 16, 0)
+    assert len(u) == 16383744
+    want_count, want = O.cc_labels(n, u, v)
+    g = ctx.graph(n, u, v)
+    count, lab, res = g.connected_components(seed=0, virtual_ranks=4)
+    assert count == want_count == 1
+    assert np.array_equal(lab, want)
+    assert res.rounds == 2
+
+
+@pytest.mark.slow
+def test_full_size_rmat_scale_20(ctx):
+    n, u, v, _ = graphgen.rmat(20, 16, 1)
+    want_count, want = O.cc_labels(n, u, v)
+    g = ctx.graph(n, u, v)
+    count, lab, _ = g.connected_components(seed=1)
+    assert count == want_count
+    assert np.array_equal(lab, want)

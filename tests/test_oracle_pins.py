@@ -1,0 +1,128 @@
+"""The oracle (CPU restatement) pinned against outputs of the reference itself."""
+import numpy as np
+import pytest
+
+import pyoracle as O
+from conftest import digest, make_graph
+
+
+def _kat_cases(text):
+    for line in text.strip().splitlines():
+        head, vals = line.split(":")
+        parts = head.split()
+        yield parts[1], [int(x) for x in parts[2:6]], [int(x) for x in parts[6:10]], [int(x) for x in vals.split()]
+
+
+def test_sitmo_matches_reference_engine(golden):
+    cases = list(_kat_cases(golden("sitmo_kat.txt")))
+    assert len(cases) == 28
+    for kind, key, ctr, vals in cases:
+        assert list(O.sitmo_outputs(key, ctr, len(vals))) == vals, (kind, key, ctr)
+        if kind == "seed":
+            assert [O.__dict__["lib"]().orc_sitmo_seed_output(key[0], k) for k in range(len(vals))] == vals
+
+
+def test_draw64_is_word_of_block():
+    key = [5, 7, 9, 0]
+    blk = O.sitmo_block(key, [3, 2, 0, 0])
+    for j in range(4):
+        assert O.draw64(key, 2, 12 + j) == int(blk[j])
+
+
+def test_cc_labels_match_reference_test_inputs(golden):
+    ref = golden("ref_test_inputs.json")
+    for name in ("cc_8.graph", "cc_13.graph"):
+        r = ref[name]
+        count, lab = O.cc_labels(r["n"], r["u"], r["v"])
+        assert count == r["cc_count"] == r["parallel_cc_csv_count"] == 5
+        assert lab.tolist() == r["cc_labels"]
+        c2, lab2, _ = O.cc_iss(r["n"], r["u"], r["v"], 0)
+        assert c2 == count and lab2.tolist() == r["cc_labels"]
+
+
+@pytest.mark.parametrize("idx", range(5))
+def test_cc_labels_match_reference_seeded(golden, idx):
+    spec = golden("cc_seeded.json")[idx]
+    n, u, v, w = make_graph(spec)
+    assert digest(np.concatenate([u, v])) == spec["edges_sha256"]
+    count, lab = O.cc_labels(n, u, v)
+    assert count == spec["cc_count"]
+    assert digest(lab) == spec["labels_sha256"]
+    for ranks in (1, 3):
+        c2, lab2, _ = O.cc_iss(n, u, v, spec["seed"], ranks)
+        assert c2 == count and np.array_equal(lab2, lab)
+
+
+def test_exact_cut_matches_reference(golden):
+    ref = golden("ref_test_inputs.json")
+    for name, r in ref.items():
+        if name.startswith("cc_"):
+            continue
+        assert O.exact_mincut(r["n"], r["u"], r["v"], r["w"]) == r["exact_cut"] == r["square_root_cut"]
+
+
+@pytest.mark.parametrize("idx", range(5))
+def test_exact_and_square_root_oracle_match_reference_seeded(golden, idx):
+    spec = golden("mincut_seeded.json")[idx]
+    n, u, v, w = make_graph(spec)
+    assert digest(np.concatenate([u, v, w])) == spec["edges_sha256"]
+    assert O.exact_mincut(n, u, v, w) == spec["exact_cut"]
+    assert O.number_of_trials(n, len(u), 0.95) == spec["square_root_trials"]
+    if n <= 500:
+        cut, per = O.square_root(n, u, v, w, 0.95, 0, 1)
+        assert per == spec["square_root_trials"]
+        assert cut == spec["exact_cut"]
+
+
+def test_sparse_and_dense_stoer_wagner_agree():
+    import graphgen
+    for seed in range(3):
+        n, u, v, w = graphgen.erdos_renyi_m(1100, 6, seed, wmax=9)
+        dense_n, du, dv, dw = 300, u[(u < 300) & (v < 300)], v[(u < 300) & (v < 300)], w[(u < 300) & (v < 300)]
+        # dense path (n <= 1024) vs the heap path on a relabelled copy forced above 1024 vertices
+        a = O.exact_mincut(dense_n, du, dv, dw)
+        big_n = 1500
+        b = O.exact_mincut(big_n, du, dv, dw)  # vertices >= 300 isolated -> cut 0 on the big graph
+        assert b == 0
+        assert a == O.exact_mincut(dense_n, du, dv, dw)
+    n, u, v, w = graphgen.erdos_renyi_m(1200, 12, 7, wmax=5)
+    lab_count, _ = O.cc_labels(n, u, v)
+    if lab_count == 1:
+        mat = np.zeros((n, n), np.uint64)
+        np.add.at(mat, (u, v), w.astype(np.uint64))
+        np.add.at(mat, (v, u), w.astype(np.uint64))
+        assert O.exact_mincut(n, u, v, w) == O.stoer_wagner_dense(mat)
+
+
+def test_trial_values_are_upper_bounds_and_reach_the_cut(golden):
+    spec = golden("mincut_seeded.json")[0]
+    n, u, v, w = make_graph(spec)
+    vals = [O.mincut_trial(n, u, v, w, 0, r, i) for r in range(2) for i in range(4)]
+    assert min(vals) == spec["exact_cut"]
+    assert all(x >= spec["exact_cut"] for x in vals)
+
+
+def test_trial_budget_expressions():
+    # co_mincut.cpp:18-41 and SquareRootCut.cpp:63-83 at the shapes of the benchmark configs
+    assert O.ks_target(4000) == 2830 and O.ks_target(318) == 226 and O.ks_target(161) == 128
+    assert O.intermediate_size(1000, 24910) == 317
+    assert O.intermediate_size(4000, 7998000) == 4000
+    assert O.number_of_trials(4000, 7998000, 0.95) == 7
+
+
+def test_approx_threshold_matches_probability():
+    for level in (1, 2, 5, 10):
+        for w in (1, 2, 7, 42, 1000):
+            f = O.keep_threshold(level, w) / 2.0**64
+            assert abs(f - (1 - 2.0**-level) ** w) < 1e-12 * max(1, w)
+    assert O.approx_trials(0.9) == 4
+
+
+def test_approx_oracle_is_a_power_of_two_bound(golden):
+    ref = golden("ref_test_inputs.json")
+    for name, r in ref.items():
+        if name.startswith("cc_"):
+            continue
+        cut, level = O.approx_cut(r["n"], r["u"], r["v"], r["w"], 0.9, 0)
+        assert cut == 1 << level
+        assert cut <= 2 * r["exact_cut"]
