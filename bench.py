@@ -41,7 +41,8 @@ import numpy as np  # noqa: E402
 
 N_VERTICES, ATTACH, GRAPH_SEED = 1024000, 16, 0
 METRIC = "CC edges/s (parallel_cc, BA n=1,024,000 m=16)"
-KERNELS_PER_QUERY = 8  # init, sample_hook, compress, edge_pass, finalize_count, scan_tiles, rank_roots, label_all
+KERNELS_PER_QUERY = 10  # init, sample_hook, compress, find_giant, giant_bitmap, edge_pass, finalize_count,
+#                        scan_tiles, rank_roots, label_all
 
 
 def _peaks():

@@ -10,6 +10,7 @@ There is no fallback: if libcac.so is missing or no CUDA device is present, call
 """
 import ctypes
 import os
+import weakref
 from dataclasses import dataclass
 
 import numpy as np
@@ -120,9 +121,12 @@ class Context:
         h = _vp()
         _check(lib().cac_ctx_create(ctypes.byref(cfg), ctypes.byref(h)), "cac_ctx_create")
         self.h = h
+        self._graphs = weakref.WeakSet()
 
     def close(self):
         if self.h:
+            for g in list(self._graphs):
+                g.free()
             lib().cac_ctx_destroy(self.h)
             self.h = None
 
@@ -155,12 +159,16 @@ class Context:
         h = _vp()
         _check(lib().cac_graph_from_edges(self.h, n, len(u), pu, pv, pw, where, ctypes.byref(h)),
                "cac_graph_from_edges")
-        return Graph(self, h, (u, v, w))
+        g = Graph(self, h, (u, v, w))
+        self._graphs.add(g)
+        return g
 
     def load(self, path):
         h = _vp()
         _check(lib().cac_graph_load_file(self.h, path.encode(), ctypes.byref(h)), "cac_graph_load_file")
-        return Graph(self, h, None)
+        g = Graph(self, h, None)
+        self._graphs.add(g)
+        return g
 
     # ---- primitives ----
     def sitmo_blocks(self, key, ctr0, nblocks):
@@ -204,9 +212,9 @@ class Graph:
         self.n, self.m, self.total_weight = int(n.value), int(m.value), int(w.value)
 
     def free(self):
-        if self.h:
+        if self.h and self.ctx.h:
             lib().cac_graph_free(self.h)
-            self.h = None
+        self.h = None
 
     def __del__(self):
         try:

@@ -1,0 +1,42 @@
+// Drop-in for the reference's approx_cut executable (src/executables/approx_cut.cpp:5-43):
+// same arguments, same CSV line
+//   input,seed,p,n,m,cuttingTime,mpiTime,trials,weight
+#include <iostream>
+#include <string>
+
+#include "cli_common.h"
+
+int main(int argc, char *argv[]) {
+    if ((argc != 4) && (argc != 5)) {
+        std::cout << "Usage: slimGraph-Light PROBABILITY INPUT_FILE|CLICK [SIZE] SEED" << std::endl;
+        return 1;
+    }
+    float success_probability{std::stof(argv[1], nullptr)};
+    uint32_t seed = {(uint32_t)std::stoi(argv[argc == 4 ? 3 : 4])};
+    if (std::string(argv[2]) == "CLICK") {
+        std::cerr << "approx_cut: the in-memory CLICK generator is not part of this build; write the graph "
+                     "to an edge-list file instead"
+                  << std::endl;
+        return 2;
+    }
+    const unsigned ranks = cli_virtual_ranks();
+    cac_config cfg{cli_device(), nullptr, 0};
+    cac_ctx *ctx = nullptr;
+    int st = cac_ctx_create(&cfg, &ctx);
+    if (st) return cli_fail("cac_ctx_create", st);
+    cac_graph *g = nullptr;
+    st = cac_graph_load_file(ctx, argv[2], &g);
+    if (st) return cli_fail("cac_graph_load_file", st);
+    uint32_t n = 0;
+    uint64_t m = 0;
+    cac_graph_info(g, &n, &m, nullptr);
+    cac_approx_result res{};
+    st = cac_approx_cut(ctx, g, success_probability, seed, ranks, &res);
+    if (st) return cli_fail("cac_approx_cut", st);
+    std::cout << std::fixed;
+    std::cout << argv[2] << "," << seed << "," << ranks << "," << n << "," << m << "," << res.device_ms / 1000.0
+              << "," << 0.0 << "," << res.trials << "," << res.cut << std::endl;
+    cac_graph_free(g);
+    cac_ctx_destroy(ctx);
+    return 0;
+}

@@ -1,0 +1,26 @@
+// Shared helpers of the drop-in command lines.
+#pragma once
+#include <cstdio>
+#include <cstdlib>
+#include <string>
+
+#include "cac.h"
+
+// The MPI rank count the reference would have been launched with (`mpiexec -n P`): it fixes the
+// seed layout (rank r uses seed + r) and the trial split, and is printed in the CSV `p` column.
+inline unsigned cli_virtual_ranks() {
+    const char *s = std::getenv("CAC_VIRTUAL_RANKS");
+    if (!s || !*s) return 1;
+    long v = std::strtol(s, nullptr, 10);
+    return v > 0 ? (unsigned)v : 1;
+}
+
+inline int cli_device() {
+    const char *s = std::getenv("CAC_DEVICE");
+    return s && *s ? std::atoi(s) : 0;
+}
+
+inline int cli_fail(const char *what, int status) {
+    std::fprintf(stderr, "%s failed: %s (%d): %s\n", what, cac_error_string(status), status, cac_last_error());
+    return 1;
+}

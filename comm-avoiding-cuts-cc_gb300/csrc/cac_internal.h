@@ -5,6 +5,7 @@
 #include <cstdint>
 #include <cstdio>
 #include <string>
+#include <set>
 #include <vector>
 
 #include "../../include/cac.h"
@@ -38,6 +39,8 @@ struct Arena {
 
 }  // namespace cac
 
+struct cac_graph;
+
 struct cac_ctx {
     int device = 0;
     cudaStream_t stream = nullptr;
@@ -48,6 +51,7 @@ struct cac_ctx {
     cac::Arena arena;  // kernel scratch
     cac::Arena io;     // staging for host-buffer entry points
     cudaEvent_t ev[8] = {};  // phase timing events
+    std::set<cac_graph *> graphs;    // live graphs, released by cac_ctx_destroy
     uint32_t *pinned_u32 = nullptr;  // 64 KB pinned staging: [0,256) B scalar results, then descriptors
 };
 

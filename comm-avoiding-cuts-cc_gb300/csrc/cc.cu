@@ -31,6 +31,9 @@ constexpr int kThreads = 256;
 constexpr int kTileItems = 16;                       // vertices per thread in the labelling tiles
 constexpr int kTile = kThreads * kTileItems;         // vertices per labelling tile
 constexpr size_t kPinnedBytes = 60 * 1024;           // ctx pinned staging available for rank descriptors
+constexpr int kEdgeThreads = 1024;                   // closing-pass CTA (one per SM: the bitmap fills smem)
+constexpr uint32_t kSmemBitmapWords = 48 * 1024;     // 192 KB of bitmap in shared memory (1.57M vertices)
+constexpr uint32_t kGiantSample = 4096;              // vertices sampled to find the giant component
 
 struct RankDesc {
     uint64_t slice_off;
@@ -52,6 +55,15 @@ __device__ __forceinline__ uint32_t find_root(uint32_t *par, uint32_t v) {
             cur = next;
         }
     }
+    return cur;
+}
+
+// Root of v without writes. Used where no hooking happens any more: a path-halving write by
+// one thread could otherwise overwrite another thread's just-stored `parent[i] = root` with a
+// non-root ancestor and leave i uncompressed.
+__device__ __forceinline__ uint32_t find_root_ro(const uint32_t *par, uint32_t v) {
+    uint32_t cur = v, next;
+    while ((next = par[cur]) != cur) cur = next;
     return cur;
 }
 
@@ -104,7 +116,7 @@ __global__ void cc_sample_hook(uint32_t *par, const uint32_t *__restrict__ u, co
 
 __global__ void cc_compress(uint32_t *par, uint32_t n) {
     for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
-        par[i] = find_root(par, i);
+        par[i] = find_root_ro(par, i);
 }
 
 __device__ __forceinline__ void edge_hook(uint32_t *par, uint32_t a, uint32_t b) {
@@ -113,10 +125,77 @@ __device__ __forceinline__ void edge_hook(uint32_t *par, uint32_t a, uint32_t b)
     unite(par, pa, pb);
 }
 
-// Closing pass over every edge, 4 edges per thread step through 16-byte streaming loads.
-template <bool kVec>
-__global__ void __launch_bounds__(kThreads) cc_edge_pass(uint32_t *par, const uint32_t *__restrict__ u,
-                                                         const uint32_t *__restrict__ v, uint64_t m) {
+// The most frequent root among kGiantSample vertices spread over [0, n) (compressed parents):
+// one CTA sorts the sampled roots in shared memory and takes the longest run.
+__global__ void __launch_bounds__(1024) cc_find_giant(const uint32_t *par, uint32_t n, uint32_t *giant) {
+    __shared__ uint32_t r[kGiantSample];
+    for (uint32_t i = threadIdx.x; i < kGiantSample; i += blockDim.x) {
+        const uint64_t v = ((uint64_t)i * 2654435761u) % n;  // fixed spread of sample positions
+        r[i] = par[v];
+    }
+    __syncthreads();
+    // bitonic sort of kGiantSample (power of two) keys
+    for (uint32_t k = 2; k <= kGiantSample; k <<= 1) {
+        for (uint32_t j = k >> 1; j > 0; j >>= 1) {
+            for (uint32_t i = threadIdx.x; i < kGiantSample; i += blockDim.x) {
+                const uint32_t p = i ^ j;
+                if (p > i) {
+                    const bool up = (i & k) == 0;
+                    const uint32_t a = r[i], b = r[p];
+                    if ((a > b) == up) { r[i] = b; r[p] = a; }
+                }
+            }
+            __syncthreads();
+        }
+    }
+    if (threadIdx.x == 0) {
+        uint32_t best = r[0], best_len = 0, run = 0;
+        for (uint32_t i = 0; i < kGiantSample; i++) {
+            run = (i > 0 && r[i] == r[i - 1]) ? run + 1 : 1;
+            if (run > best_len) { best_len = run; best = r[i]; }
+        }
+        *giant = best;
+    }
+}
+
+// bit v of the bitmap = (parent[v] == giant root), one warp ballot per 32 vertices
+__global__ void cc_giant_bitmap(const uint32_t *par, uint32_t n, const uint32_t *giant, uint32_t *bits) {
+    const uint32_t g = *giant;
+    const uint64_t nw = ((uint64_t)n + 31) / 32;
+    const uint64_t warps = ((uint64_t)gridDim.x * blockDim.x) >> 5;
+    for (uint64_t w = ((uint64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5; w < nw; w += warps) {
+        const uint64_t v = w * 32 + (threadIdx.x & 31);
+        const bool in = v < n && par[v] == g;
+        const uint32_t word = __ballot_sync(0xffffffffu, in);
+        if ((threadIdx.x & 31) == 0) bits[w] = word;
+    }
+}
+
+__device__ __forceinline__ bool in_giant(const uint32_t *sbits, uint32_t swords, const uint32_t *gbits, uint32_t x) {
+    const uint32_t w = x >> 5;
+    const uint32_t word = w < swords ? sbits[w] : __ldg(gbits + w);
+    return (word >> (x & 31)) & 1u;
+}
+
+template <bool kSkip>
+__device__ __forceinline__ void visit_edge(uint32_t *par, const uint32_t *sbits, uint32_t swords,
+                                           const uint32_t *gbits, uint32_t a, uint32_t b) {
+    if (kSkip && in_giant(sbits, swords, gbits, a) && in_giant(sbits, swords, gbits, b)) return;  // same component
+    edge_hook(par, a, b);
+}
+
+// Closing pass over every edge, 4 edges per thread step through 16-byte streaming loads. The
+// membership bitmap of the giant component (its first `swords` words staged in shared memory,
+// the rest read through the read-only path) lets edges inside the giant component skip the
+// parent lookups entirely.
+template <bool kVec, bool kSkip>
+__global__ void __launch_bounds__(kEdgeThreads) cc_edge_pass(uint32_t *par, const uint32_t *__restrict__ u,
+                                                             const uint32_t *__restrict__ v, uint64_t m,
+                                                             const uint32_t *__restrict__ gbits, uint32_t nwords) {
+    extern __shared__ uint32_t sbits[];
+    const uint32_t swords = kSkip ? min(nwords, (uint32_t)kSmemBitmapWords) : 0;
+    for (uint32_t i = threadIdx.x; i < swords; i += blockDim.x) sbits[i] = gbits[i];
+    __syncthreads();
     const uint64_t tid = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
     const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
     uint64_t done = 0;
@@ -127,14 +206,15 @@ __global__ void __launch_bounds__(kThreads) cc_edge_pass(uint32_t *par, const ui
         for (uint64_t i = tid; i < m4; i += stride) {
             const uint4 a = __ldcs(u4 + i);
             const uint4 b = __ldcs(v4 + i);
-            edge_hook(par, a.x, b.x);
-            edge_hook(par, a.y, b.y);
-            edge_hook(par, a.z, b.z);
-            edge_hook(par, a.w, b.w);
+            visit_edge<kSkip>(par, sbits, swords, gbits, a.x, b.x);
+            visit_edge<kSkip>(par, sbits, swords, gbits, a.y, b.y);
+            visit_edge<kSkip>(par, sbits, swords, gbits, a.z, b.z);
+            visit_edge<kSkip>(par, sbits, swords, gbits, a.w, b.w);
         }
         done = m4 << 2;
     }
-    for (uint64_t e = done + tid; e < m; e += stride) edge_hook(par, __ldcs(u + e), __ldcs(v + e));
+    for (uint64_t e = done + tid; e < m; e += stride)
+        visit_edge<kSkip>(par, sbits, swords, gbits, __ldcs(u + e), __ldcs(v + e));
 }
 
 __device__ __forceinline__ uint32_t block_sum(uint32_t x, uint32_t *sh) {
@@ -160,7 +240,7 @@ __global__ void __launch_bounds__(kThreads) cc_finalize_count(uint32_t *par, uin
     for (int k = 0; k < kTileItems; k++) {
         const uint64_t i = base + (uint64_t)k * kThreads + threadIdx.x;
         if (i < n) {
-            const uint32_t r = find_root(par, (uint32_t)i);
+            const uint32_t r = find_root_ro(par, (uint32_t)i);
             par[i] = r;
             c += (r == (uint32_t)i);
         }
@@ -309,8 +389,9 @@ CCPlan cc_plan(uint32_t n, uint64_t m, uint32_t ranks) {
 
 size_t cc_scratch_bytes(uint32_t n, uint32_t ranks) {
     const size_t ntiles = ((size_t)n + kTile - 1) / kTile;
+    const size_t nwords = ((size_t)n + 31) / 32;
     return align_up((size_t)n * 4) + 2 * align_up(ntiles * 4 + 4) + align_up(256) +
-           align_up(sizeof(RankDesc) * (size_t)ranks);
+           align_up(sizeof(RankDesc) * (size_t)ranks) + align_up(nwords * 4 + 4);
 }
 
 int cc_run(cac_ctx *ctx, uint32_t n, uint64_t m, const uint32_t *d_u, const uint32_t *d_v, uint32_t seed,
@@ -331,7 +412,10 @@ int cc_run(cac_ctx *ctx, uint32_t n, uint64_t m, const uint32_t *d_u, const uint
     uint32_t *counts = (uint32_t *)arena_take(ctx, (size_t)ntiles * 4 + 4);
     uint32_t *offsets = (uint32_t *)arena_take(ctx, (size_t)ntiles * 4 + 4);
     uint32_t *total = (uint32_t *)arena_take(ctx, 256);
+    uint32_t *giant = total + 8;
     RankDesc *d_ranks = (RankDesc *)arena_take(ctx, sizeof(RankDesc) * ranks);
+    const uint32_t nwords = (uint32_t)(((uint64_t)n + 31) / 32);
+    uint32_t *bits = (uint32_t *)arena_take(ctx, (size_t)nwords * 4 + 4);
 
     // rank descriptors go through the ctx's pinned staging page when they fit (async copy)
     std::vector<RankDesc> hv;
@@ -360,13 +444,25 @@ int cc_run(cac_ctx *ctx, uint32_t n, uint64_t m, const uint32_t *d_u, const uint
         CAC_CUDA_TRY(cudaMemcpyAsync(d_ranks, hr, sizeof(RankDesc) * ranks, cudaMemcpyHostToDevice, s));
         cc_sample_hook<<<grid_for(ctx, blocks, 8), kThreads, 0, s>>>(par, d_u, d_v, d_ranks, (int)ranks, blocks);
         cc_compress<<<grid_for(ctx, n, 8), kThreads, 0, s>>>(par, n);
+        cc_find_giant<<<1, 1024, 0, s>>>(par, n, giant);
+        cc_giant_bitmap<<<grid_for(ctx, n, 8), kThreads, 0, s>>>(par, n, giant, bits);
     }
     CAC_CUDA_TRY(cudaEventRecord(ctx->ev[1], s));
     if (m > 0) {
         const bool vec = ((reinterpret_cast<uintptr_t>(d_u) | reinterpret_cast<uintptr_t>(d_v)) & 15) == 0;
-        const int grid = grid_for(ctx, (m + 3) / 4, 8);
-        if (vec) cc_edge_pass<true><<<grid, kThreads, 0, s>>>(par, d_u, d_v, m);
-        else cc_edge_pass<false><<<grid, kThreads, 0, s>>>(par, d_u, d_v, m);
+        const bool skip = blocks > 0;  // a sampling round ran, so a giant component exists
+        const size_t sm = skip ? (size_t)std::min(nwords, kSmemBitmapWords) * 4 : 0;
+        const int grid = (int)std::max<uint64_t>(1, std::min<uint64_t>((uint64_t)ctx->num_sms * (skip ? 1 : 2),
+                                                                        (m + 4 * kEdgeThreads - 1) / (4 * kEdgeThreads)));
+        auto launch = [&](auto kernel) -> int {
+            CAC_CUDA_TRY(cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
+            kernel<<<grid, kEdgeThreads, sm, s>>>(par, d_u, d_v, m, bits, nwords);
+            return CAC_OK;
+        };
+        if (vec && skip) CAC_TRY(launch(cc_edge_pass<true, true>));
+        else if (vec) CAC_TRY(launch(cc_edge_pass<true, false>));
+        else if (skip) CAC_TRY(launch(cc_edge_pass<false, true>));
+        else CAC_TRY(launch(cc_edge_pass<false, false>));
     }
     CAC_CUDA_TRY(cudaEventRecord(ctx->ev[2], s));
     cc_finalize_count<<<ntiles, kThreads, 0, s>>>(par, n, counts);

@@ -203,6 +203,7 @@ int graph_create(cac_ctx *ctx, uint32_t n, uint64_t m, const uint32_t *u, const 
         }
         g->total_weight = hsum[0];
     }
+    ctx->graphs.insert(g);
     *out = g;
     return CAC_OK;
 }
@@ -270,6 +271,12 @@ int cac_ctx_destroy(cac_ctx *ctx) {
     if (!ctx) return CAC_OK;
     cudaSetDevice(ctx->device);
     if (ctx->stream) cudaStreamSynchronize(ctx->stream);
+    // graphs still alive are released with their ctx; their handles become invalid
+    for (cac_graph *g : ctx->graphs) {
+        dev_free(ctx, g->u, g->bytes);
+        delete g;
+    }
+    ctx->graphs.clear();
     dev_free(ctx, ctx->arena.base, ctx->arena.cap);
     dev_free(ctx, ctx->io.base, ctx->io.cap);
     for (auto &e : ctx->ev) if (e) cudaEventDestroy(e);
@@ -297,9 +304,11 @@ int cac_graph_from_edges(cac_ctx *ctx, uint32_t n, uint64_t m, const uint32_t *u
 
 int cac_graph_free(cac_graph *g) {
     if (!g) return CAC_OK;
-    cudaSetDevice(g->ctx->device);
-    cudaStreamSynchronize(g->ctx->stream);
-    dev_free(g->ctx, g->u, g->bytes);
+    cac_ctx *ctx = g->ctx;
+    cudaSetDevice(ctx->device);
+    cudaStreamSynchronize(ctx->stream);
+    ctx->graphs.erase(g);
+    dev_free(ctx, g->u, g->bytes);
     delete g;
     return CAC_OK;
 }

@@ -72,6 +72,7 @@ typedef struct {
 
 /* ---- context ---- */
 int cac_ctx_create(const cac_config *config, cac_ctx **out);
+/* Destroys the ctx; graphs still alive are released with it and their handles become invalid. */
 int cac_ctx_destroy(cac_ctx *ctx);
 const char *cac_error_string(int status);
 const char *cac_last_error(void);

@@ -1,0 +1,49 @@
+"""Parity of the CUDA approx_cut path with the oracle's replay of the same counter-addressed keep
+tests, and the O(log n)-approximation bound against the exact cut."""
+import pytest
+
+import graphgen
+import pyoracle as O
+from conftest import make_graph
+
+pytestmark = pytest.mark.gpu
+
+
+def test_reference_test_inputs(golden, ctx):
+    for name, r in golden("ref_test_inputs.json").items():
+        if name.startswith("cc_"):
+            continue
+        g = ctx.graph(r["n"], r["u"], r["v"], r["w"])
+        for seed, ranks in ((0, 1), (3, 2), (11, 4)):
+            res = g.approx_cut(0.9, seed=seed, virtual_ranks=ranks)
+            want, level = O.approx_cut(r["n"], r["u"], r["v"], r["w"], 0.9, seed, ranks)
+            assert (res.cut, res.level) == (want, level)
+            assert res.copies == O.approx_trials(0.9) == 4
+            assert res.trials == res.copies * res.level
+
+
+@pytest.mark.parametrize("idx", range(5))
+def test_seeded_graphs(golden, ctx, idx):
+    spec = golden("mincut_seeded.json")[idx]
+    n, u, v, w = make_graph(spec)
+    g = ctx.graph(n, u, v, w)
+    for seed, ranks, p in ((0, 1, 0.9), (5, 3, 0.95)):
+        res = g.approx_cut(p, seed=seed, virtual_ranks=ranks)
+        want, level = O.approx_cut(n, u, v, w, p, seed, ranks)
+        assert (res.cut, res.level) == (want, level)
+        # an O(log n) estimate: never far above the true cut
+        assert res.cut <= 4 * spec["exact_cut"]
+
+
+def test_fewer_edges_than_ranks(ctx):
+    n, u, v, w = 3, [0, 1], [1, 2], [50, 60]
+    g = ctx.graph(n, u, v, w)
+    res = g.approx_cut(0.9, seed=1, virtual_ranks=5)
+    assert (res.cut, res.level) == O.approx_cut(n, u, v, w, 0.9, 1, 5)
+
+
+def test_larger_graph(ctx):
+    n, u, v, w = graphgen.erdos_renyi_m(20000, 16, 3, wmax=42)
+    g = ctx.graph(n, u, v, w)
+    res = g.approx_cut(0.9, seed=2)
+    assert (res.cut, res.level) == O.approx_cut(n, u, v, w, 0.9, 2, 1)

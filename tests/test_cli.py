@@ -1,0 +1,91 @@
+"""The drop-in command lines keep the reference's argument rules and CSV lines
+(src/executables/square_root.cpp:7-40, parallel_cc.cpp:8-60, approx_cut.cpp:7-38)."""
+import os
+import subprocess
+
+import numpy as np
+import pytest
+
+import graphgen
+import pyoracle as O
+from conftest import PKG
+
+BIN = os.path.join(PKG, "bin")
+
+
+def _run(name, *args, env=None):
+    e = dict(os.environ)
+    e.update(env or {})
+    return subprocess.run([os.path.join(BIN, name)] + [str(a) for a in args], capture_output=True, text=True,
+                          env=e, timeout=600)
+
+
+@pytest.fixture(scope="module", autouse=True)
+def _built(libcac):
+    for name in ("square_root", "parallel_cc", "approx_cut"):
+        assert os.path.exists(os.path.join(BIN, name)), "command lines not built"
+
+
+@pytest.mark.parametrize("name,args,usage", [
+    ("square_root", ["0.95"], "Usage: square_root PROBABILITY INPUT_FILE|CLICK [SIZE] SEED"),
+    ("parallel_cc", ["x"], "Usage: connected_components INPUT_FILE SEED [ITERATONS]"),
+    ("approx_cut", ["0.9", "x"], "Usage: slimGraph-Light PROBABILITY INPUT_FILE|CLICK [SIZE] SEED"),
+])
+def test_usage_on_wrong_argument_count(name, args, usage):
+    r = _run(name, *args)
+    assert r.returncode == 1
+    assert r.stdout.strip() == usage
+
+
+def _write(tmp_path, name, n, u, v, w):
+    p = str(tmp_path / name)
+    graphgen.write_graph(p, n, np.asarray(u, np.uint32), np.asarray(v, np.uint32), np.asarray(w, np.uint32), name)
+    return p
+
+
+@pytest.mark.gpu
+def test_square_root_csv(golden, tmp_path):
+    for name, r in golden("ref_test_inputs.json").items():
+        if name.startswith("cc_"):
+            continue
+        path = _write(tmp_path, name, r["n"], r["u"], r["v"], r["w"])
+        out = _run("square_root", "0.95", path, "0", env={"CAC_VIRTUAL_RANKS": "4"})
+        assert out.returncode == 0, out.stderr
+        f = out.stdout.strip().split(",")
+        assert len(f) == 10 and f[0] == path and f[1] == "0" and f[2] == "4"
+        assert int(f[3]) == r["n"] and int(f[4]) == len(r["u"])
+        assert f[8] in ("low", "high")
+        assert int(f[9]) == r["exact_cut"]
+        assert int(f[7]) == -(-O.number_of_trials(r["n"], len(r["u"]), 0.95) // 4)
+
+
+@pytest.mark.gpu
+def test_parallel_cc_csv_iterations(golden, tmp_path):
+    r = golden("ref_test_inputs.json")["cc_13.graph"]
+    path = _write(tmp_path, "cc_13.graph", r["n"], r["u"], r["v"], r["w"])
+    out = _run("parallel_cc", path, "7", "3")
+    assert out.returncode == 0, out.stderr
+    lines = out.stdout.strip().splitlines()
+    assert len(lines) == 3
+    for i, line in enumerate(lines):
+        f = line.split(",")
+        assert f[0] == path and int(f[1]) == 7 + i and f[2] == "1" and f[7] == "cc" and int(f[8]) == 5
+
+
+@pytest.mark.gpu
+def test_approx_cut_csv(golden, tmp_path):
+    r = golden("ref_test_inputs.json")["complete_4.graph"]
+    path = _write(tmp_path, "k4.graph", r["n"], r["u"], r["v"], r["w"])
+    out = _run("approx_cut", "0.9", path, "3")
+    assert out.returncode == 0, out.stderr
+    f = out.stdout.strip().split(",")
+    want, level = O.approx_cut(r["n"], r["u"], r["v"], r["w"], 0.9, 3, 1)
+    assert len(f) == 9 and int(f[8]) == want and int(f[7]) == 4 * level
+
+
+@pytest.mark.gpu
+def test_malformed_file_fails_cleanly(tmp_path):
+    p = tmp_path / "bad.graph"
+    p.write_text("hdr\n5 2\n0 1 1\n")
+    out = _run("square_root", "0.95", str(p), "0")
+    assert out.returncode == 1 and "malformed" in out.stderr

@@ -1,0 +1,123 @@
+"""Parity of the CUDA min-cut path (square_root) with the oracle, through the C ABI.
+
+Three tiers:
+  * kernel level: the Stoer-Wagner leaf kernel against the oracle's exact cut, one dense
+    Karger-Stein trial against the oracle's replay of the same counter-addressed trial;
+  * trial level: every trial value equal to the oracle's CPU replay of that trial, bit for bit;
+  * result level: the square_root answer equal to the exact minimum cut (Stoer-Wagner) and to the
+    reference's own square_root output on the pinned graphs.
+"""
+import numpy as np
+import pytest
+
+import graphgen
+import pyoracle as O
+from conftest import make_graph
+
+pytestmark = pytest.mark.gpu
+
+
+def _dense(n, u, v, w):
+    mat = np.zeros((n, n), np.uint64)
+    np.add.at(mat, (u, v), np.asarray(w, np.uint64))
+    np.add.at(mat, (v, u), np.asarray(w, np.uint64))
+    np.fill_diagonal(mat, 0)
+    return mat
+
+
+def _random_dense(n, seed, density=0.3, wmax=42, big=False):
+    rng = np.random.default_rng(seed)
+    mask = np.triu(rng.random((n, n)) < density, 1)
+    w = rng.integers(1, wmax + 1, size=(n, n)).astype(np.uint64)
+    if big:
+        w = w << np.uint64(33)
+    mat = np.where(mask, w, 0).astype(np.uint64)
+    return mat + mat.T
+
+
+@pytest.mark.parametrize("n,density,big", [(2, 1.0, False), (3, 0.7, False), (17, 0.4, False), (64, 0.2, False),
+                                           (100, 0.05, False), (128, 0.3, False), (128, 0.02, False),
+                                           (90, 0.3, True)])
+def test_leaf_stoer_wagner_kernel(ctx, n, density, big):
+    for seed in range(3):
+        mat = _random_dense(n, seed, density, big=big)
+        assert ctx.exact_cut_small(mat) == O.stoer_wagner_dense(mat)
+
+
+@pytest.mark.parametrize("n,density", [(129, 0.5), (200, 0.1), (318, 0.15), (500, 0.05)])
+def test_dense_karger_stein_trial_matches_replay(ctx, n, density):
+    mat = _random_dense(n, n, density)
+    for seed, rank, trial in ((0, 0, 0), (5, 1, 3), (123, 3, 17)):
+        assert ctx.ks_dense(mat, seed, rank, trial) == O.ks_dense(mat, seed, rank, trial)
+
+
+def test_dense_karger_stein_disconnected(ctx):
+    mat = _random_dense(300, 1, 0.2)
+    mat[:150, 150:] = 0
+    mat[150:, :150] = 0
+    assert ctx.ks_dense(mat, 0, 0, 0) == 0 == O.ks_dense(mat, 0, 0, 0)
+
+
+@pytest.mark.parametrize("idx", range(5))
+def test_every_trial_matches_replay(golden, ctx, idx):
+    spec = golden("mincut_seeded.json")[idx]
+    n, u, v, w = make_graph(spec)
+    g = ctx.graph(n, u, v, w)
+    ranks, per = (2, 3) if n <= 500 else (1, 4)
+    got = g.trials(seed=7, virtual_ranks=ranks, trials_per_rank=per)
+    for r in range(ranks):
+        for i in range(per):
+            assert int(got[r, i]) == O.mincut_trial(n, u, v, w, 7, r, i), (r, i)
+    assert got.min() >= spec["exact_cut"]
+
+
+@pytest.mark.parametrize("idx", range(5))
+def test_square_root_equals_exact_cut(golden, ctx, idx):
+    spec = golden("mincut_seeded.json")[idx]
+    n, u, v, w = make_graph(spec)
+    g = ctx.graph(n, u, v, w)
+    for ranks in (1, 4):
+        res = g.square_root(0.95, seed=0, virtual_ranks=ranks)
+        assert res.cut == spec["exact_cut"] == spec["square_root_cut"]
+        assert res.trials_per_rank == -(-spec["square_root_trials"] // ranks)
+
+
+def test_reference_known_answers(golden, ctx):
+    for name, r in golden("ref_test_inputs.json").items():
+        if name.startswith("cc_"):
+            continue
+        g = ctx.graph(r["n"], r["u"], r["v"], r["w"])
+        assert g.square_root(0.95, seed=0).cut == r["exact_cut"] == r["square_root_cut"]
+
+
+@pytest.mark.parametrize("case", ["single_edge", "disconnected", "isolated_vertex", "parallel_and_loops"])
+def test_edge_cases(ctx, case):
+    if case == "single_edge":
+        n, u, v, w = 2, [0], [1], [9]
+    elif case == "disconnected":
+        n, u, v, w = graphgen.erdos_renyi(300, 0.1, 3)
+        keep = (u < 150) == (v < 150)
+        u, v, w = u[keep], v[keep], w[keep]
+    elif case == "isolated_vertex":
+        n, u, v, w = graphgen.erdos_renyi(200, 0.2, 4)
+        keep = (u != 7) & (v != 7)
+        u, v, w = u[keep], v[keep], w[keep]
+    else:
+        n, u, v, w = graphgen.erdos_renyi(150, 0.2, 5)
+        u = np.concatenate([u, u[:50], np.arange(10, dtype=np.uint32)])
+        v = np.concatenate([v, v[:50], np.arange(10, dtype=np.uint32)])
+        w = np.concatenate([w, w[:50], np.full(10, 5, np.uint32)])
+    u, v, w = (np.asarray(x, np.uint32) for x in (u, v, w))
+    g = ctx.graph(n, u, v, w)
+    want = O.exact_mincut(n, u, v, w)
+    assert g.square_root(0.95, seed=1).cut == want
+    got = g.trials(seed=2, virtual_ranks=1, trials_per_rank=3)
+    for i in range(3):
+        assert int(got[0, i]) == O.mincut_trial(n, u, v, w, 2, 0, i)
+
+
+def test_rejects_single_vertex(ctx, libcac):
+    g = ctx.graph(1, np.zeros(0, np.uint32), np.zeros(0, np.uint32))
+    with pytest.raises(libcac.CacError) as e:
+        g.square_root(0.95, 0)
+    assert e.value.status == -1
