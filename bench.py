@@ -41,8 +41,9 @@ import numpy as np  # noqa: E402
 
 N_VERTICES, ATTACH, GRAPH_SEED = 1024000, 16, 0
 METRIC = "CC edges/s (parallel_cc, BA n=1,024,000 m=16)"
-KERNELS_PER_QUERY = 10  # init, sample_hook, compress, find_giant, giant_bitmap, edge_pass, finalize_count,
-#                        scan_tiles, rank_roots, label_all
+# init, 8 x (sample_hook + compress), find_giant, giant_bitmap, filter, hook_survivors, finalize_count, scan_tiles,
+# rank_roots, label_all
+KERNELS_PER_QUERY = 1 + 8 * 2 + 8
 
 
 def _peaks():
@@ -174,7 +175,7 @@ def run_cac(args, rank, world):
     torch.cuda.synchronize()
     starts = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
     ends = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
-    edge_ms = []
+    edge_ms, phases = [], []
     with Clocks(dev) as clk, torch.cuda.stream(stream):
         for i in range(args.steps):
             flush.zero_()
@@ -182,6 +183,7 @@ def run_cac(args, rank, world):
             count, _, res = step()
             ends[i].record(stream)
             edge_ms.append(res.edge_pass_ms)
+            phases.append((res.sample_ms, res.edge_pass_ms, res.hook_ms, res.label_ms))
             assert count == want_count
         torch.cuda.synchronize()
     step_ms = [s.elapsed_time(e) for s, e in zip(starts, ends)]
@@ -237,10 +239,12 @@ def run_cac(args, rank, world):
                    "parallelism": "replicas" if world > 1 else "single GPU"},
         "e2e": {"value": e2e_value, "unit": "edges/s", "h2d_bytes_per_step": 8 * m, "d2h_bytes_per_step": 4 * n,
                 "ms_per_step": e2e_total / args.steps},
-        "roofline": {"bound": "hbm", "kernel": "cc_edge_pass", "achieved": achieved, "peak": peak,
+        "roofline": {"bound": "hbm", "kernel": "cc_filter", "achieved": achieved, "peak": peak,
                      "peak_kind": peak_kind, "unit": "GB/s", "frac": achieved / peak, "traffic": traffic,
                      "alg_bytes_per_launch": alg_bytes, "avg_launch_ms": edge_avg_ms},
         "gpu_launches": KERNELS_PER_QUERY * args.steps,
+        "phases_ms": dict(zip(("sampling_round", "filter", "hook_survivors", "labels"),
+                              [round(statistics.mean(p[i] for p in phases), 4) for i in range(4)])),
         "clocks": clk.summary(),
     }
     if not args.no_cpu_baseline:

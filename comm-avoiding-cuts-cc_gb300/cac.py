@@ -35,7 +35,8 @@ class _Config(ctypes.Structure):
 
 class CCResult(ctypes.Structure):
     _fields_ = [("num_components", ctypes.c_uint32), ("rounds", ctypes.c_uint32), ("sampled_edges", ctypes.c_uint64),
-                ("device_ms", ctypes.c_float), ("edge_pass_ms", ctypes.c_float)]
+                ("device_ms", ctypes.c_float), ("edge_pass_ms", ctypes.c_float), ("sample_ms", ctypes.c_float),
+                ("hook_ms", ctypes.c_float), ("label_ms", ctypes.c_float)]
 
 
 class MincutResult(ctypes.Structure):

@@ -41,6 +41,18 @@ struct Arena {
 
 struct cac_graph;
 
+namespace cac {
+// Identity of a connected-components query whose launch sequence is cached as a CUDA graph.
+struct CCGraphKey {
+    const void *u = nullptr, *v = nullptr, *labels = nullptr;
+    uint32_t n = 0;
+    uint64_t m = 0;
+    uint32_t seed = 0, ranks = 0;
+    const void *arena_base = nullptr;
+    size_t arena_cap = 0;
+};
+}  // namespace cac
+
 struct cac_ctx {
     int device = 0;
     cudaStream_t stream = nullptr;
@@ -52,6 +64,8 @@ struct cac_ctx {
     cac::Arena io;     // staging for host-buffer entry points
     cudaEvent_t ev[8] = {};  // phase timing events
     std::set<cac_graph *> graphs;    // live graphs, released by cac_ctx_destroy
+    cac::CCGraphKey cc_key;          // last connected-components query
+    cudaGraphExec_t cc_exec = nullptr;  // its captured launch sequence (second sighting onwards)
     uint32_t *pinned_u32 = nullptr;  // 64 KB pinned staging: [0,256) B scalar results, then descriptors
 };
 
@@ -88,7 +102,8 @@ struct CCPlan {
 CCPlan cc_plan(uint32_t n, uint64_t m, uint32_t ranks);
 int cc_run(cac_ctx *ctx, uint32_t n, uint64_t m, const uint32_t *d_u, const uint32_t *d_v, uint32_t seed,
            uint32_t ranks, uint32_t *d_labels, cac_cc_result *res);
-size_t cc_scratch_bytes(uint32_t n, uint32_t ranks);
+size_t cc_scratch_bytes(uint32_t n, uint32_t ranks, uint64_t m);
+void cc_graph_reset(cac_ctx *ctx);
 
 // ---- min cut (mincut.cu) ----
 int mincut_trials(cac_ctx *ctx, const cac_graph *g, uint32_t seed, uint32_t ranks, uint32_t per_rank,

@@ -4,8 +4,9 @@
 // Reference round structure            ->  here
 //   root scatters per-rank draw counts    host restates edgesToSamplePerProcessor (cc_plan)
 //   rank r draws engine()%slice samples   cc_sample_hook: sitmo stream (seed + r, 0, 0, 0),
-//     with sitmo(seed + r)                  output k = word k % 8 of block k / 8, exactly the
-//                                           reference's k-th draw; every draw hooks its edge
+//     with sitmo(seed + r)                  output k = word k % 8 of block k / 8, the reference's
+//                                           k-th engine output; it picks a 32-edge chunk of the
+//                                           slice (coalesced) instead of one edge
 //   root: shuffle + prefix union-find     lock-free union-find in HBM (atomicCAS hooking of
 //     to one component (Boost sets)         the larger root under the smaller, so roots are
 //                                           component minima; order-free for target 1)
@@ -33,13 +34,16 @@ constexpr int kTile = kThreads * kTileItems;         // vertices per labelling t
 constexpr size_t kPinnedBytes = 60 * 1024;           // ctx pinned staging available for rank descriptors
 constexpr int kEdgeThreads = 1024;                   // closing-pass CTA (one per SM: the bitmap fills smem)
 constexpr uint32_t kSmemBitmapWords = 48 * 1024;     // 192 KB of bitmap in shared memory (1.57M vertices)
-constexpr uint32_t kGiantSample = 4096;              // vertices sampled to find the giant component
+constexpr uint32_t kGiantSample = 1024;              // vertices sampled to find the giant component
+constexpr uint32_t kSampleChunk = 32;                // consecutive edges behind one sampling draw
+constexpr uint32_t kSampleSubrounds = 8;             // slices of the sampling round, compressed in between
+constexpr uint32_t kMaxRegions = 1024;               // filter CTAs (regions of the survivor buffer)
 
 struct RankDesc {
     uint64_t slice_off;
     uint64_t slice_len;
     uint64_t draws;
-    uint64_t block_off;  // first sitmo block of this rank in the flattened launch
+    uint64_t block_off;  // first chunk draw of this rank in the flattened launch
     uint32_t key0;       // seed + rank
     uint32_t pad;
 };
@@ -88,29 +92,30 @@ __global__ void cc_init(uint32_t *par, uint32_t n) {
     for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) par[i] = i;
 }
 
-// One thread per sitmo block (8 draws of one virtual rank).
+// One warp per draw of the range [d0, d1) of all ranks' draws. The reference draws single edges (engine() % slice, a random 8-byte
+// gather each); here draw k of rank r (32-bit output k of stream (seed + r, 0, 0, 0)) selects
+// chunk (output % chunks) of kSampleChunk consecutive edges of the rank's slice, which the warp
+// reads with coalesced loads and hooks. The number of sampled edges matches the reference's
+// per-rank budget.
 __global__ void cc_sample_hook(uint32_t *par, const uint32_t *__restrict__ u, const uint32_t *__restrict__ v,
-                               const RankDesc *__restrict__ ranks, int nranks, uint64_t total_blocks) {
-    for (uint64_t blk = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; blk < total_blocks;
-         blk += (uint64_t)gridDim.x * blockDim.x) {
-        int lo = 0, hi = nranks - 1;  // last rank whose block_off <= blk
+                               const RankDesc *__restrict__ ranks, int nranks, uint64_t d0, uint64_t d1) {
+    const int lane = threadIdx.x & 31;
+    const uint64_t warps = ((uint64_t)gridDim.x * blockDim.x) >> 5;
+    for (uint64_t gd = d0 + (((uint64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5); gd < d1; gd += warps) {
+        int lo = 0, hi = nranks - 1;  // last rank whose first draw <= gd
         while (lo < hi) {
             int mid = (lo + hi + 1) >> 1;
-            if (ranks[mid].block_off <= blk) lo = mid; else hi = mid - 1;
+            if (ranks[mid].block_off <= gd) lo = mid; else hi = mid - 1;
         }
         const RankDesc rd = ranks[lo];
-        const uint64_t local = blk - rd.block_off;
-        const u64x4 o = sitmo_block(rd.key0, 0, 0, 0, local, 0, 0, 0);
-        const uint64_t first = local * 8;
-        const uint32_t len = (uint32_t)rd.slice_len;
-#pragma unroll
-        for (int j = 0; j < 8; j++) {
-            if (first + j >= rd.draws) break;
-            const uint64_t word = o.x[j >> 1];
-            const uint32_t x = (j & 1) ? (uint32_t)(word >> 32) : (uint32_t)word;
-            const uint64_t e = rd.slice_off + (rd.slice_len > 0xFFFFFFFFull ? (uint64_t)x : (uint64_t)(x % len));
-            unite(par, __ldg(u + e), __ldg(v + e));
-        }
+        const uint64_t k = gd - rd.block_off;  // draw index within the rank's stream
+        const u64x4 o = sitmo_block(rd.key0, 0, 0, 0, k >> 3, 0, 0, 0);
+        const unsigned j = (unsigned)(k & 7);
+        const uint64_t word = (j >> 1) == 0 ? o.x[0] : (j >> 1) == 1 ? o.x[1] : (j >> 1) == 2 ? o.x[2] : o.x[3];
+        const uint32_t x = (j & 1) ? (uint32_t)(word >> 32) : (uint32_t)word;
+        const uint64_t nchunks = (rd.slice_len + kSampleChunk - 1) / kSampleChunk;
+        const uint64_t e = rd.slice_off + (x % nchunks) * kSampleChunk + lane;
+        if (e < rd.slice_off + rd.slice_len) unite(par, __ldg(u + e), __ldg(v + e));
     }
 }
 
@@ -126,36 +131,37 @@ __device__ __forceinline__ void edge_hook(uint32_t *par, uint32_t a, uint32_t b)
 }
 
 // The most frequent root among kGiantSample vertices spread over [0, n) (compressed parents):
-// one CTA sorts the sampled roots in shared memory and takes the longest run.
-__global__ void __launch_bounds__(1024) cc_find_giant(const uint32_t *par, uint32_t n, uint32_t *giant) {
+// one CTA bitonic-sorts the sampled roots in shared memory; every run start measures its run by
+// binary search and a block argmax picks the longest (ties: the smaller root).
+__global__ void __launch_bounds__(kGiantSample) cc_find_giant(const uint32_t *par, uint32_t n, uint32_t *giant) {
     __shared__ uint32_t r[kGiantSample];
-    for (uint32_t i = threadIdx.x; i < kGiantSample; i += blockDim.x) {
-        const uint64_t v = ((uint64_t)i * 2654435761u) % n;  // fixed spread of sample positions
-        r[i] = par[v];
-    }
+    __shared__ unsigned long long best;
+    const uint32_t i = threadIdx.x;
+    r[i] = par[((uint64_t)i * 2654435761u) % n];  // fixed spread of sample positions
+    if (i == 0) best = 0;
     __syncthreads();
-    // bitonic sort of kGiantSample (power of two) keys
     for (uint32_t k = 2; k <= kGiantSample; k <<= 1) {
         for (uint32_t j = k >> 1; j > 0; j >>= 1) {
-            for (uint32_t i = threadIdx.x; i < kGiantSample; i += blockDim.x) {
-                const uint32_t p = i ^ j;
-                if (p > i) {
-                    const bool up = (i & k) == 0;
-                    const uint32_t a = r[i], b = r[p];
-                    if ((a > b) == up) { r[i] = b; r[p] = a; }
-                }
+            const uint32_t p = i ^ j;
+            if (p > i) {
+                const bool up = (i & k) == 0;
+                const uint32_t a = r[i], b = r[p];
+                if ((a > b) == up) { r[i] = b; r[p] = a; }
             }
             __syncthreads();
         }
     }
-    if (threadIdx.x == 0) {
-        uint32_t best = r[0], best_len = 0, run = 0;
-        for (uint32_t i = 0; i < kGiantSample; i++) {
-            run = (i > 0 && r[i] == r[i - 1]) ? run + 1 : 1;
-            if (run > best_len) { best_len = run; best = r[i]; }
+    if (i == 0 || r[i] != r[i - 1]) {
+        uint32_t lo = i, hi = kGiantSample;  // first position with a larger root
+        while (lo < hi) {
+            const uint32_t mid = (lo + hi) >> 1;
+            if (r[mid] > r[i]) hi = mid; else lo = mid + 1;
         }
-        *giant = best;
+        const unsigned long long key = ((unsigned long long)(lo - i) << 32) | (0xFFFFFFFFu - r[i]);
+        atomicMax(&best, key);
     }
+    __syncthreads();
+    if (i == 0) *giant = 0xFFFFFFFFu - (uint32_t)(best & 0xFFFFFFFFu);
 }
 
 // bit v of the bitmap = (parent[v] == giant root), one warp ballot per 32 vertices
@@ -171,31 +177,12 @@ __global__ void cc_giant_bitmap(const uint32_t *par, uint32_t n, const uint32_t 
     }
 }
 
-__device__ __forceinline__ bool in_giant(const uint32_t *sbits, uint32_t swords, const uint32_t *gbits, uint32_t x) {
-    const uint32_t w = x >> 5;
-    const uint32_t word = w < swords ? sbits[w] : __ldg(gbits + w);
-    return (word >> (x & 31)) & 1u;
-}
 
-template <bool kSkip>
-__device__ __forceinline__ void visit_edge(uint32_t *par, const uint32_t *sbits, uint32_t swords,
-                                           const uint32_t *gbits, uint32_t a, uint32_t b) {
-    if (kSkip && in_giant(sbits, swords, gbits, a) && in_giant(sbits, swords, gbits, b)) return;  // same component
-    edge_hook(par, a, b);
-}
-
-// Closing pass over every edge, 4 edges per thread step through 16-byte streaming loads. The
-// membership bitmap of the giant component (its first `swords` words staged in shared memory,
-// the rest read through the read-only path) lets edges inside the giant component skip the
-// parent lookups entirely.
-template <bool kVec, bool kSkip>
-__global__ void __launch_bounds__(kEdgeThreads) cc_edge_pass(uint32_t *par, const uint32_t *__restrict__ u,
-                                                             const uint32_t *__restrict__ v, uint64_t m,
-                                                             const uint32_t *__restrict__ gbits, uint32_t nwords) {
-    extern __shared__ uint32_t sbits[];
-    const uint32_t swords = kSkip ? min(nwords, (uint32_t)kSmemBitmapWords) : 0;
-    for (uint32_t i = threadIdx.x; i < swords; i += blockDim.x) sbits[i] = gbits[i];
-    __syncthreads();
+// Closing pass without a sampling round: every edge hooks, 4 edges per thread step through
+// 16-byte streaming loads.
+template <bool kVec>
+__global__ void __launch_bounds__(kThreads) cc_edge_pass(uint32_t *par, const uint32_t *__restrict__ u,
+                                                         const uint32_t *__restrict__ v, uint64_t m) {
     const uint64_t tid = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
     const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
     uint64_t done = 0;
@@ -206,15 +193,98 @@ __global__ void __launch_bounds__(kEdgeThreads) cc_edge_pass(uint32_t *par, cons
         for (uint64_t i = tid; i < m4; i += stride) {
             const uint4 a = __ldcs(u4 + i);
             const uint4 b = __ldcs(v4 + i);
-            visit_edge<kSkip>(par, sbits, swords, gbits, a.x, b.x);
-            visit_edge<kSkip>(par, sbits, swords, gbits, a.y, b.y);
-            visit_edge<kSkip>(par, sbits, swords, gbits, a.z, b.z);
-            visit_edge<kSkip>(par, sbits, swords, gbits, a.w, b.w);
+            edge_hook(par, a.x, b.x);
+            edge_hook(par, a.y, b.y);
+            edge_hook(par, a.z, b.z);
+            edge_hook(par, a.w, b.w);
         }
         done = m4 << 2;
     }
-    for (uint64_t e = done + tid; e < m; e += stride)
-        visit_edge<kSkip>(par, sbits, swords, gbits, __ldcs(u + e), __ldcs(v + e));
+    for (uint64_t e = done + tid; e < m; e += stride) edge_hook(par, __ldcs(u + e), __ldcs(v + e));
+}
+
+// Filter pass after the sampling round (the reference's slice rewrite that drops loops,
+// IteratedSparseSampling.hpp:160-172): a pure streaming read of every edge; edges with both
+// endpoints in the giant component are dropped, the others are appended to this CTA's region of
+// `surv` (region = the CTA's contiguous range of 256-edge tiles, so no global counter is
+// contended). A warp owns a tile: lane l reads edges 4l..4l+3 and 128+4l..128+4l+3 of it with
+// two fully coalesced 512-byte loads per endpoint array, keeps 8 edges in flight, and appends its
+// survivors after one warp scan and one shared-memory atomic. The membership bitmap's first
+// `swords` words are staged in shared memory, the rest read through the read-only path.
+__global__ void __launch_bounds__(kEdgeThreads) cc_filter(const uint32_t *__restrict__ u,
+                                                          const uint32_t *__restrict__ v, uint64_t tiles,
+                                                          const uint32_t *__restrict__ gbits, uint32_t nwords,
+                                                          uint2 *__restrict__ surv, uint32_t *__restrict__ counts) {
+    extern __shared__ uint32_t sbits[];
+    __shared__ uint32_t s_n;
+    const uint32_t swords = min(nwords, (uint32_t)kSmemBitmapWords);
+    for (uint32_t i = threadIdx.x; i < swords; i += blockDim.x) sbits[i] = gbits[i];
+    if (threadIdx.x == 0) s_n = 0;
+    __syncthreads();
+    const uint64_t per = (tiles + gridDim.x - 1) / gridDim.x;
+    const uint64_t t0 = min(tiles, (uint64_t)blockIdx.x * per), t1 = min(tiles, t0 + per);
+    uint2 *out = surv + t0 * 256;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarps = blockDim.x >> 5;
+    auto in_giant = [&](uint32_t x) -> bool {
+        const uint32_t w = x >> 5;
+        const uint32_t word = w < swords ? sbits[w] : __ldg(gbits + w);
+        return (word >> (x & 31)) & 1u;
+    };
+    const uint4 *u4 = reinterpret_cast<const uint4 *>(u);
+    const uint4 *v4 = reinterpret_cast<const uint4 *>(v);
+    for (uint64_t t = t0 + warp; t < t1; t += nwarps) {
+        const uint4 ua = __ldcs(u4 + t * 64 + lane), ub = __ldcs(u4 + t * 64 + 32 + lane);
+        const uint4 va = __ldcs(v4 + t * 64 + lane), vb = __ldcs(v4 + t * 64 + 32 + lane);
+        const uint32_t a[8] = {ua.x, ua.y, ua.z, ua.w, ub.x, ub.y, ub.z, ub.w};
+        const uint32_t b[8] = {va.x, va.y, va.z, va.w, vb.x, vb.y, vb.z, vb.w};
+        uint32_t keep = 0;
+#pragma unroll
+        for (int k = 0; k < 8; k++) keep |= (uint32_t)!(in_giant(a[k]) && in_giant(b[k])) << k;
+        const uint32_t cnt = __popc(keep);
+        uint32_t incl = cnt;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const uint32_t y = __shfl_up_sync(0xffffffffu, incl, o);
+            if (lane >= o) incl += y;
+        }
+        const uint32_t total = __shfl_sync(0xffffffffu, incl, 31);
+        if (total == 0) continue;
+        uint32_t base = 0;
+        if (lane == 31) base = atomicAdd(&s_n, total);
+        base = __shfl_sync(0xffffffffu, base, 31) + incl - cnt;
+#pragma unroll
+        for (int k = 0; k < 8; k++)
+            if ((keep >> k) & 1u) out[base++] = make_uint2(a[k], b[k]);
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) counts[blockIdx.x] = s_n;
+}
+
+// Union of the surviving edges (the reference's next round on the remaining slice). Regions of
+// the filter CTAs are addressed through the prefix of their counts.
+__global__ void __launch_bounds__(kThreads) cc_hook_survivors(uint32_t *par, const uint2 *__restrict__ surv,
+                                                              const uint32_t *__restrict__ counts, uint32_t nregions,
+                                                              uint64_t region_stride) {
+    __shared__ uint32_t pre[kMaxRegions + 1];
+    if (threadIdx.x == 0) {
+        uint32_t acc = 0;
+        for (uint32_t r = 0; r < nregions; r++) {
+            pre[r] = acc;
+            acc += counts[r];
+        }
+        pre[nregions] = acc;
+    }
+    __syncthreads();
+    const uint32_t total = pre[nregions];
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < total; i += gridDim.x * blockDim.x) {
+        uint32_t lo = 0, hi = nregions - 1;  // last region whose first survivor <= i
+        while (lo < hi) {
+            const uint32_t mid = (lo + hi + 1) >> 1;
+            if (pre[mid] <= i) lo = mid; else hi = mid - 1;
+        }
+        const uint2 e = surv[(uint64_t)lo * region_stride + (i - pre[lo])];
+        edge_hook(par, e.x, e.y);
+    }
 }
 
 __device__ __forceinline__ uint32_t block_sum(uint32_t x, uint32_t *sh) {
@@ -387,35 +457,147 @@ CCPlan cc_plan(uint32_t n, uint64_t m, uint32_t ranks) {
     return p;
 }
 
-size_t cc_scratch_bytes(uint32_t n, uint32_t ranks) {
+size_t cc_scratch_bytes(uint32_t n, uint32_t ranks, uint64_t m) {
     const size_t ntiles = ((size_t)n + kTile - 1) / kTile;
     const size_t nwords = ((size_t)n + 31) / 32;
     return align_up((size_t)n * 4) + 2 * align_up(ntiles * 4 + 4) + align_up(256) +
-           align_up(sizeof(RankDesc) * (size_t)ranks) + align_up(nwords * 4 + 4);
+           align_up(sizeof(RankDesc) * (size_t)ranks) + align_up(nwords * 4 + 4) + align_up(kMaxRegions * 4) +
+           align_up((m + 4 * (uint64_t)kMaxRegions) * 8);
+}
+
+namespace {
+
+// Everything one query enqueues, resolved on the host.
+struct CCLaunch {
+    uint32_t n = 0;
+    uint64_t m = 0;
+    const uint32_t *u = nullptr, *v = nullptr;
+    uint32_t *labels = nullptr;
+    uint32_t ranks = 1;
+    uint32_t *par = nullptr, *counts = nullptr, *offsets = nullptr, *total = nullptr, *giant = nullptr;
+    uint32_t *bits = nullptr, *region_counts = nullptr;
+    uint2 *surv = nullptr;
+    RankDesc *d_ranks = nullptr;
+    const RankDesc *h_ranks = nullptr;
+    uint32_t ntiles = 0, nwords = 0;
+    uint64_t draws = 0, drawn = 0;
+    bool vec = false;
+};
+
+int record(cac_ctx *ctx, int i, bool capturing) {
+    if (capturing) CAC_CUDA_TRY(cudaEventRecordWithFlags(ctx->ev[i], ctx->stream, cudaEventRecordExternal));
+    else CAC_CUDA_TRY(cudaEventRecord(ctx->ev[i], ctx->stream));
+    return CAC_OK;
+}
+
+// Enqueues the whole query on the ctx stream (directly, or into a graph being captured).
+int cc_enqueue(cac_ctx *ctx, const CCLaunch &L, bool capturing) {
+    cudaStream_t s = ctx->stream;
+    const uint32_t n = L.n;
+    const uint64_t m = L.m;
+    CAC_TRY(record(ctx, 0, capturing));
+    cc_init<<<grid_for(ctx, n, 8), kThreads, 0, s>>>(L.par, n);
+    if (L.draws > 0 && m > 0) {
+        CAC_CUDA_TRY(cudaMemcpyAsync(L.d_ranks, L.h_ranks, sizeof(RankDesc) * L.ranks, cudaMemcpyHostToDevice, s));
+        // The draws are hooked in kSampleSubrounds slices with a full compression after each:
+        // forest building from singletons is the expensive part of CC, and keeping every tree
+        // flat between slices keeps the union walks of the next slice one or two hops long.
+        const uint32_t sub = (uint32_t)std::min<uint64_t>(kSampleSubrounds, L.draws);
+        for (uint32_t k = 0; k < sub; k++) {
+            const uint64_t d0 = L.draws * k / sub, d1 = L.draws * (k + 1) / sub;
+            cc_sample_hook<<<grid_for(ctx, (d1 - d0) * 32, 8), kThreads, 0, s>>>(L.par, L.u, L.v, L.d_ranks,
+                                                                                  (int)L.ranks, d0, d1);
+            cc_compress<<<grid_for(ctx, n, 8), kThreads, 0, s>>>(L.par, n);
+        }
+        cc_find_giant<<<1, kGiantSample, 0, s>>>(L.par, n, L.giant);
+        cc_giant_bitmap<<<grid_for(ctx, n, 8), kThreads, 0, s>>>(L.par, n, L.giant, L.bits);
+    }
+    CAC_TRY(record(ctx, 1, capturing));
+    if (m > 0) {
+        if (L.draws > 0) {
+            // a sampling round ran, so a giant component exists: filter, then hook the survivors
+            const size_t sm = (size_t)std::min(L.nwords, kSmemBitmapWords) * 4;
+            const uint64_t tiles = L.vec ? m >> 8 : 0;  // 256-edge tiles; the rest goes to the scalar pass
+            const uint32_t regions = (uint32_t)std::max<uint64_t>(
+                1, std::min<uint64_t>({(uint64_t)ctx->num_sms, (uint64_t)kMaxRegions, tiles}));
+            const uint64_t per = (tiles + regions - 1) / regions;
+            if (tiles)
+                cc_filter<<<regions, kEdgeThreads, sm, s>>>(L.u, L.v, tiles, L.bits, L.nwords, L.surv,
+                                                            L.region_counts);
+            CAC_TRY(record(ctx, 4, capturing));
+            if (tiles)
+                cc_hook_survivors<<<(unsigned)ctx->num_sms * 4, kThreads, 0, s>>>(L.par, L.surv, L.region_counts,
+                                                                                   regions, per * 256);
+            const uint64_t done = tiles * 256;
+            if (done < m)
+                cc_edge_pass<false><<<grid_for(ctx, m - done, 8), kThreads, 0, s>>>(L.par, L.u + done, L.v + done,
+                                                                                     m - done);
+        } else {
+            const int grid = grid_for(ctx, (m + 3) / 4, 8);
+            if (L.vec) cc_edge_pass<true><<<grid, kThreads, 0, s>>>(L.par, L.u, L.v, m);
+            else cc_edge_pass<false><<<grid, kThreads, 0, s>>>(L.par, L.u, L.v, m);
+            CAC_TRY(record(ctx, 4, capturing));
+        }
+    } else {
+        CAC_TRY(record(ctx, 4, capturing));
+    }
+    CAC_TRY(record(ctx, 2, capturing));
+    cc_finalize_count<<<L.ntiles, kThreads, 0, s>>>(L.par, n, L.counts);
+    cc_scan_tiles<<<1, 1024, 0, s>>>(L.counts, L.offsets, L.ntiles, L.total);
+    if (L.labels) {
+        cc_rank_roots<<<L.ntiles, kThreads, 0, s>>>(L.par, n, L.offsets, L.labels);
+        cc_label_all<<<grid_for(ctx, n, 8), kThreads, 0, s>>>(L.par, n, L.labels);
+    }
+    CAC_CUDA_TRY(cudaGetLastError());
+    CAC_CUDA_TRY(cudaMemcpyAsync(ctx->pinned_u32, L.total, 4, cudaMemcpyDeviceToHost, s));
+    CAC_TRY(record(ctx, 3, capturing));
+    return CAC_OK;
+}
+
+bool same_key(const CCGraphKey &a, const CCGraphKey &b) {
+    return a.u == b.u && a.v == b.v && a.labels == b.labels && a.n == b.n && a.m == b.m && a.seed == b.seed &&
+           a.ranks == b.ranks && a.arena_base == b.arena_base && a.arena_cap == b.arena_cap;
+}
+
+}  // namespace
+
+void cc_graph_reset(cac_ctx *ctx) {
+    if (ctx->cc_exec) cudaGraphExecDestroy(ctx->cc_exec);
+    ctx->cc_exec = nullptr;
+    ctx->cc_key = CCGraphKey{};
 }
 
 int cc_run(cac_ctx *ctx, uint32_t n, uint64_t m, const uint32_t *d_u, const uint32_t *d_v, uint32_t seed,
            uint32_t ranks, uint32_t *d_labels, cac_cc_result *res) {
     if (ranks == 0) ranks = 1;
     cudaStream_t s = ctx->stream;
-    CAC_CUDA_TRY(cudaEventRecord(ctx->ev[0], s));
     if (n == 0) {
-        if (res) { *res = cac_cc_result{}; }
+        if (res) *res = cac_cc_result{};
         return CAC_OK;
     }
     const CCPlan plan = cc_plan(n, m, ranks);
-    const uint32_t ntiles = (uint32_t)(((uint64_t)n + kTile - 1) / kTile);
+    CCLaunch L;
+    L.n = n;
+    L.m = m;
+    L.u = d_u;
+    L.v = d_v;
+    L.labels = d_labels;
+    L.ranks = ranks;
+    L.ntiles = (uint32_t)(((uint64_t)n + kTile - 1) / kTile);
+    L.nwords = (uint32_t)(((uint64_t)n + 31) / 32);
+    L.vec = ((reinterpret_cast<uintptr_t>(d_u) | reinterpret_cast<uintptr_t>(d_v)) & 15) == 0;
 
-    CAC_TRY(arena_reserve(ctx, cc_scratch_bytes(n, ranks)));
+    CAC_TRY(arena_reserve(ctx, cc_scratch_bytes(n, ranks, m)));
     arena_reset(ctx);
-    uint32_t *par = (uint32_t *)arena_take(ctx, (size_t)n * 4);
-    uint32_t *counts = (uint32_t *)arena_take(ctx, (size_t)ntiles * 4 + 4);
-    uint32_t *offsets = (uint32_t *)arena_take(ctx, (size_t)ntiles * 4 + 4);
-    uint32_t *total = (uint32_t *)arena_take(ctx, 256);
-    uint32_t *giant = total + 8;
-    RankDesc *d_ranks = (RankDesc *)arena_take(ctx, sizeof(RankDesc) * ranks);
-    const uint32_t nwords = (uint32_t)(((uint64_t)n + 31) / 32);
-    uint32_t *bits = (uint32_t *)arena_take(ctx, (size_t)nwords * 4 + 4);
+    L.par = (uint32_t *)arena_take(ctx, (size_t)n * 4);
+    L.counts = (uint32_t *)arena_take(ctx, (size_t)L.ntiles * 4 + 4);
+    L.offsets = (uint32_t *)arena_take(ctx, (size_t)L.ntiles * 4 + 4);
+    L.total = (uint32_t *)arena_take(ctx, 256);
+    L.giant = L.total + 8;
+    L.d_ranks = (RankDesc *)arena_take(ctx, sizeof(RankDesc) * ranks);
+    L.bits = (uint32_t *)arena_take(ctx, (size_t)L.nwords * 4 + 4);
+    L.region_counts = (uint32_t *)arena_take(ctx, kMaxRegions * 4);
+    L.surv = (uint2 *)arena_take(ctx, (m + 4 * (uint64_t)kMaxRegions) * 8);
 
     // rank descriptors go through the ctx's pinned staging page when they fit (async copy)
     std::vector<RankDesc> hv;
@@ -427,60 +609,64 @@ int cc_run(cac_ctx *ctx, uint32_t n, uint64_t m, const uint32_t *d_u, const uint
         hv.resize(ranks);
         hr = hv.data();
     }
-    uint64_t blocks = 0, drawn = 0;
     for (uint32_t r = 0; r < ranks; r++) {
         hr[r].slice_off = plan.slice_off[r];
         hr[r].slice_len = plan.slice_len[r];
         hr[r].draws = plan.draws[r];
-        hr[r].block_off = blocks;
+        hr[r].block_off = L.draws;
         hr[r].key0 = seed + r;
         hr[r].pad = 0;
-        blocks += (plan.draws[r] + 7) / 8;
-        drawn += plan.draws[r];
+        const uint64_t chunk_draws = (plan.draws[r] + kSampleChunk - 1) / kSampleChunk;
+        L.draws += chunk_draws;
+        L.drawn += chunk_draws * kSampleChunk;
     }
+    L.h_ranks = hr;
+    if (L.draws > 0 && m > 0)
+        CAC_CUDA_TRY(cudaFuncSetAttribute(cc_filter, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                          (int)((size_t)std::min(L.nwords, kSmemBitmapWords) * 4)));
 
-    cc_init<<<grid_for(ctx, n, 8), kThreads, 0, s>>>(par, n);
-    if (blocks > 0 && m > 0) {
-        CAC_CUDA_TRY(cudaMemcpyAsync(d_ranks, hr, sizeof(RankDesc) * ranks, cudaMemcpyHostToDevice, s));
-        cc_sample_hook<<<grid_for(ctx, blocks, 8), kThreads, 0, s>>>(par, d_u, d_v, d_ranks, (int)ranks, blocks);
-        cc_compress<<<grid_for(ctx, n, 8), kThreads, 0, s>>>(par, n);
-        cc_find_giant<<<1, 1024, 0, s>>>(par, n, giant);
-        cc_giant_bitmap<<<grid_for(ctx, n, 8), kThreads, 0, s>>>(par, n, giant, bits);
+    // Repeated identical queries replay a captured CUDA graph: one launch instead of a dozen
+    // kernel launches and copies. The first sighting of a key runs directly; the second captures.
+    CCGraphKey key{d_u, d_v, d_labels, n, m, seed, ranks, ctx->arena.base, ctx->arena.cap};
+    if (!pinned) {
+        cc_graph_reset(ctx);
+        CAC_TRY(cc_enqueue(ctx, L, false));
+    } else if (same_key(key, ctx->cc_key) && ctx->cc_exec) {
+        CAC_CUDA_TRY(cudaGraphLaunch(ctx->cc_exec, s));
+    } else if (same_key(key, ctx->cc_key)) {
+        cudaGraph_t graph = nullptr;
+        CAC_CUDA_TRY(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
+        const int st = cc_enqueue(ctx, L, true);
+        const cudaError_t ce = cudaStreamEndCapture(s, &graph);
+        if (st != CAC_OK) {
+            if (graph) cudaGraphDestroy(graph);
+            return st;
+        }
+        CAC_CUDA_TRY(ce);
+        const cudaError_t ie = cudaGraphInstantiate(&ctx->cc_exec, graph, 0);
+        cudaGraphDestroy(graph);
+        if (ie != cudaSuccess) {
+            ctx->cc_exec = nullptr;
+            cudaGetLastError();
+            CAC_TRY(cc_enqueue(ctx, L, false));
+        } else {
+            CAC_CUDA_TRY(cudaGraphLaunch(ctx->cc_exec, s));
+        }
+    } else {
+        cc_graph_reset(ctx);
+        ctx->cc_key = key;
+        CAC_TRY(cc_enqueue(ctx, L, false));
     }
-    CAC_CUDA_TRY(cudaEventRecord(ctx->ev[1], s));
-    if (m > 0) {
-        const bool vec = ((reinterpret_cast<uintptr_t>(d_u) | reinterpret_cast<uintptr_t>(d_v)) & 15) == 0;
-        const bool skip = blocks > 0;  // a sampling round ran, so a giant component exists
-        const size_t sm = skip ? (size_t)std::min(nwords, kSmemBitmapWords) * 4 : 0;
-        const int grid = (int)std::max<uint64_t>(1, std::min<uint64_t>((uint64_t)ctx->num_sms * (skip ? 1 : 2),
-                                                                        (m + 4 * kEdgeThreads - 1) / (4 * kEdgeThreads)));
-        auto launch = [&](auto kernel) -> int {
-            CAC_CUDA_TRY(cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
-            kernel<<<grid, kEdgeThreads, sm, s>>>(par, d_u, d_v, m, bits, nwords);
-            return CAC_OK;
-        };
-        if (vec && skip) CAC_TRY(launch(cc_edge_pass<true, true>));
-        else if (vec) CAC_TRY(launch(cc_edge_pass<true, false>));
-        else if (skip) CAC_TRY(launch(cc_edge_pass<false, true>));
-        else CAC_TRY(launch(cc_edge_pass<false, false>));
-    }
-    CAC_CUDA_TRY(cudaEventRecord(ctx->ev[2], s));
-    cc_finalize_count<<<ntiles, kThreads, 0, s>>>(par, n, counts);
-    cc_scan_tiles<<<1, 1024, 0, s>>>(counts, offsets, ntiles, total);
-    if (d_labels) {
-        cc_rank_roots<<<ntiles, kThreads, 0, s>>>(par, n, offsets, d_labels);
-        cc_label_all<<<grid_for(ctx, n, 8), kThreads, 0, s>>>(par, n, d_labels);
-    }
-    CAC_CUDA_TRY(cudaGetLastError());
-    CAC_CUDA_TRY(cudaMemcpyAsync(ctx->pinned_u32, total, 4, cudaMemcpyDeviceToHost, s));
-    CAC_CUDA_TRY(cudaEventRecord(ctx->ev[3], s));
     CAC_CUDA_TRY(cudaStreamSynchronize(s));
     if (res) {
         res->num_components = ctx->pinned_u32[0];
-        res->rounds = (blocks > 0 ? 1u : 0u) + (m > 0 ? 1u : 0u);
-        res->sampled_edges = drawn;
+        res->rounds = (L.draws > 0 ? 1u : 0u) + (m > 0 ? 1u : 0u);
+        res->sampled_edges = L.drawn;
         CAC_CUDA_TRY(cudaEventElapsedTime(&res->device_ms, ctx->ev[0], ctx->ev[3]));
-        CAC_CUDA_TRY(cudaEventElapsedTime(&res->edge_pass_ms, ctx->ev[1], ctx->ev[2]));
+        CAC_CUDA_TRY(cudaEventElapsedTime(&res->edge_pass_ms, ctx->ev[1], ctx->ev[4]));
+        CAC_CUDA_TRY(cudaEventElapsedTime(&res->sample_ms, ctx->ev[0], ctx->ev[1]));
+        CAC_CUDA_TRY(cudaEventElapsedTime(&res->hook_ms, ctx->ev[4], ctx->ev[2]));
+        CAC_CUDA_TRY(cudaEventElapsedTime(&res->label_ms, ctx->ev[2], ctx->ev[3]));
     }
     return CAC_OK;
 }

@@ -544,7 +544,6 @@ struct PendingTask {
     uint32_t src;     // index into this iteration's source list
 };
 
-constexpr size_t kSmemLimit = 227 * 1024;
 
 size_t contract_smem(uint32_t N) { return kBatch * sizeof(uint2) + (size_t)2 * N * 4; }
 size_t quotient_smem(uint32_t k, uint32_t N) { return (size_t)k * 8 + (size_t)N * 4; }

@@ -277,6 +277,7 @@ int cac_ctx_destroy(cac_ctx *ctx) {
         delete g;
     }
     ctx->graphs.clear();
+    cc_graph_reset(ctx);
     dev_free(ctx, ctx->arena.base, ctx->arena.cap);
     dev_free(ctx, ctx->io.base, ctx->io.cap);
     for (auto &e : ctx->ev) if (e) cudaEventDestroy(e);
@@ -330,19 +331,21 @@ int cac_cc(cac_ctx *ctx, const cac_graph *g, uint32_t seed, uint32_t virtual_ran
     CAC_CUDA_TRY(cudaSetDevice(ctx->device));
     if (virtual_ranks == 0) virtual_ranks = 1;
     uint32_t *d_labels = nullptr;
-    void *tmp = nullptr;
     if (labels && labels_where == CAC_DEVICE) d_labels = labels;
     if (labels && labels_where == CAC_HOST) {
-        CAC_TRY(dev_alloc(ctx, &tmp, (size_t)g->n * 4 + 4));
-        d_labels = (uint32_t *)tmp;
+        // device staging for host labels: the ctx's grow-only io arena (a stable address, so a
+        // repeated query can replay its captured launch sequence)
+        CAC_TRY(arena_reserve(ctx, ctx->io, (size_t)g->n * 4 + 4));
+        ctx->io.used = 0;
+        d_labels = (uint32_t *)arena_take(ctx->io, (size_t)g->n * 4 + 4);
     }
     cac_cc_result r{};
     int st = cc_run(ctx, g->n, g->m, g->u, g->v, seed, virtual_ranks, d_labels, &r);
-    if (st == CAC_OK && tmp && g->n) {
-        cudaError_t e = cudaMemcpy(labels, d_labels, (size_t)g->n * 4, cudaMemcpyDeviceToHost);
+    if (st == CAC_OK && labels && labels_where == CAC_HOST && g->n) {
+        cudaError_t e = cudaMemcpyAsync(labels, d_labels, (size_t)g->n * 4, cudaMemcpyDeviceToHost, ctx->stream);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
         if (e != cudaSuccess) { set_error(cudaGetErrorString(e)); st = CAC_ERR_CUDA; }
     }
-    if (tmp) dev_free(ctx, tmp, (size_t)g->n * 4 + 4);
     if (res) *res = r;
     return st;
 }

@@ -97,7 +97,11 @@ typedef struct {
     uint32_t rounds;         /* sampling rounds + the closing pass over all edges */
     uint64_t sampled_edges;  /* edges drawn in the sampling round */
     float device_ms;         /* device time of the whole call on the ctx stream */
-    float edge_pass_ms;      /* device time of the closing pass over all edges */
+    float edge_pass_ms;      /* device time of the streaming pass over every edge (the loop-dropping
+                                filter after a sampling round, else the single hooking pass) */
+    float sample_ms;         /* device time of the sampling round (init, draws, compression, bitmap) */
+    float hook_ms;           /* device time of hooking the edges that survived the filter */
+    float label_ms;          /* device time of the final compression, count and labels */
 } cac_cc_result;
 
 /* labels (nullable): label(v) = rank of the smallest vertex of v's component among all

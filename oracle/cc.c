@@ -45,6 +45,8 @@ uint32_t orc_cc_labels(uint32_t n, uint64_t m, const uint32_t *u, const uint32_t
 
 /* ---- restatement of the reference's ISS CC ---- */
 
+typedef struct { uint32_t from, to; } edge2;
+
 /* sitmo::prng_engine(seed) as a sequential 32-bit stream (lib/prng_engine.hpp:195-212). */
 typedef struct { uint64_t key[4]; uint64_t block; uint64_t out[4]; unsigned pos; } seq_engine;
 
@@ -123,18 +125,16 @@ uint32_t orc_cc_iss(uint32_t n, uint64_t m, const uint32_t *u, const uint32_t *v
     if (ranks == 0) ranks = 1;
     /* slices: rank r owns lines [r*floor(m/P), (r+1)*floor(m/P)), the last rank the rest
      * (UnweightedIteratedSparseSampling.cpp:5-21) */
-    uint32_t **su = (uint32_t **)calloc(ranks, sizeof(uint32_t *));
-    uint32_t **sv = (uint32_t **)calloc(ranks, sizeof(uint32_t *));
+    /* slices hold {from, to} records like the reference's UnweightedGraph::Edge (8 bytes) */
+    edge2 **sl = (edge2 **)calloc(ranks, sizeof(edge2 *));
     uint64_t *len = (uint64_t *)calloc(ranks, sizeof(uint64_t));
     seq_engine *eng = (seq_engine *)calloc(ranks, sizeof(seq_engine));
     uint64_t portion = m / ranks;
     for (uint32_t r = 0; r < ranks; r++) {
         uint64_t from = portion * r, to = (r == ranks - 1) ? m : portion * (r + 1);
         len[r] = to - from;
-        su[r] = (uint32_t *)malloc(sizeof(uint32_t) * (len[r] ? len[r] : 1));
-        sv[r] = (uint32_t *)malloc(sizeof(uint32_t) * (len[r] ? len[r] : 1));
-        memcpy(su[r], u + from, sizeof(uint32_t) * len[r]);
-        memcpy(sv[r], v + from, sizeof(uint32_t) * len[r]);
+        sl[r] = (edge2 *)malloc(sizeof(edge2) * (len[r] ? len[r] : 1));
+        for (uint64_t e = 0; e < len[r]; e++) { sl[r][e].from = u[from + e]; sl[r][e].to = v[from + e]; }
         eng_init(&eng[r], seed + r);
     }
     uint32_t *comp = (uint32_t *)malloc(sizeof(uint32_t) * (n ? n : 1));
@@ -156,37 +156,32 @@ uint32_t orc_cc_iss(uint32_t n, uint64_t m, const uint32_t *u, const uint32_t *v
         uint64_t total = 0;
         for (uint32_t r = 0; r < ranks; r++) total += (uint64_t)per[r];
         /* sample (.cpp:24-37) and gather in rank order (IteratedSparseSampling.hpp:261-271) */
-        uint32_t *gu = (uint32_t *)malloc(sizeof(uint32_t) * (total ? total : 1));
-        uint32_t *gv = (uint32_t *)malloc(sizeof(uint32_t) * (total ? total : 1));
+        edge2 *gs = (edge2 *)malloc(sizeof(edge2) * (total ? total : 1));
         uint64_t at = 0;
         for (uint32_t r = 0; r < ranks; r++) {
             if ((uint64_t)per[r] == len[r]) {
-                memcpy(gu + at, su[r], sizeof(uint32_t) * len[r]);
-                memcpy(gv + at, sv[r], sizeof(uint32_t) * len[r]);
+                memcpy(gs + at, sl[r], sizeof(edge2) * len[r]);
                 at += len[r];
             } else {
                 for (int k = 0; k < per[r]; k++) {
                     uint64_t idx = eng_next(&eng[r]) % (uint32_t)len[r];
-                    gu[at] = su[r][idx];
-                    gv[at] = sv[r][idx];
-                    at++;
+                    gs[at++] = sl[r][idx];
                 }
             }
         }
         /* shuffle with the root's engine (IteratedSparseSampling.hpp:278). Fisher-Yates with
-         * modulo draws: libstdc++'s std::shuffle consumes the engine differently, which only
-         * changes the order in which the prefix union-find meets the samples, never the
+         * multiply-shift draws: libstdc++'s std::shuffle consumes the engine differently, which
+         * only changes the order in which the prefix union-find meets the samples, never the
          * labels (the target is a single component). */
         for (uint64_t i = total; i > 1; i--) {
-            uint64_t j = eng_next(&eng[0]) % i;
-            uint32_t t = gu[i - 1]; gu[i - 1] = gu[j]; gu[j] = t;
-            t = gv[i - 1]; gv[i - 1] = gv[j]; gv[j] = t;
+            uint64_t j = ((uint64_t)eng_next(&eng[0]) * i) >> 32;
+            edge2 t = gs[i - 1]; gs[i - 1] = gs[j]; gs[j] = t;
         }
         /* prefix union-find to one component (IteratedSparseSampling.hpp:182-224) */
         for (uint32_t i = 0; i < vcount; i++) { parent[i] = i; rk[i] = 0; }
         uint32_t active = vcount;
         for (uint64_t i = 0; i < total && active > 1; i++) {
-            uint32_t a = ds_find(parent, gu[i]), b = ds_find(parent, gv[i]);
+            uint32_t a = ds_find(parent, gs[i].from), b = ds_find(parent, gs[i].to);
             if (a != b) { active--; ds_link(parent, rk, a, b); }
         }
         for (uint32_t j = 0; j < vcount; j++) lab[j] = -1;
@@ -201,18 +196,18 @@ uint32_t orc_cc_iss(uint32_t n, uint64_t m, const uint32_t *u, const uint32_t *v
         for (uint32_t r = 0; r < ranks; r++) {
             uint64_t w = 0;
             for (uint64_t e = 0; e < len[r]; e++) {
-                uint32_t a = map[su[r][e]], b = map[sv[r][e]];
-                if (a != b) { su[r][w] = a; sv[r][w] = b; w++; }
+                uint32_t a = map[sl[r][e].from], b = map[sl[r][e].to];
+                if (a != b) { sl[r][w].from = a; sl[r][w].to = b; w++; }
             }
             len[r] = w;
         }
         vcount = active;
-        free(gu); free(gv);
+        free(gs);
     }
     if (labels) memcpy(labels, comp, sizeof(uint32_t) * n);
     if (rounds_out) *rounds_out = rounds;
-    for (uint32_t r = 0; r < ranks; r++) { free(su[r]); free(sv[r]); }
-    free(su); free(sv); free(len); free(eng); free(comp); free(avail); free(per);
+    for (uint32_t r = 0; r < ranks; r++) free(sl[r]);
+    free(sl); free(len); free(eng); free(comp); free(avail); free(per);
     free(parent); free(rk); free(lab); free(map);
     return vcount;
 }

@@ -91,13 +91,26 @@ def test_repeated_runs_are_identical(ctx):
         assert count == want_count and np.array_equal(lab, want)
 
 
+def test_replayed_queries_match(ctx):
+    # the second identical query is captured into a CUDA graph, later ones replay it; a different
+    # query in between must not be served by the stale capture
+    n1, u1, v1, _ = graphgen.rmat(15, 8, 31)
+    n2, u2, v2, _ = graphgen.erdos_renyi_m(40000, 1.1, 32, wmax=1)
+    g1, g2 = ctx.graph(n1, u1, v1), ctx.graph(n2, u2, v2)
+    w1, w2 = O.cc_labels(n1, u1, v1), O.cc_labels(n2, u2, v2)
+    for g, (wc, wl) in [(g1, w1)] * 4 + [(g2, w2)] * 3 + [(g1, w1)] * 3:
+        count, lab, _ = g.connected_components(seed=4, virtual_ranks=2)
+        assert count == wc and np.array_equal(lab, wl)
+
+
 def test_one_call_host_entry_point(ctx):
     n, u, v, _ = graphgen.barabasi_albert(50000, 4, 2)
     want_count, want = O.cc_labels(n, u, v)
     lab = np.zeros(n, np.uint32)
     res = ctx.cc_edges(n, u, v, seed=5, virtual_ranks=2, labels=lab)
     assert res.num_components == want_count and np.array_equal(lab, want)
-    assert res.sampled_edges == O.cc_sample_count(n, len(u))
+    # 32-edge chunks per draw: the sampled edge count rounds each rank's budget up to a chunk
+    assert 0 <= res.sampled_edges - O.cc_sample_count(n, len(u)) < 32 * 2
 
 
 @pytest.mark.slow
