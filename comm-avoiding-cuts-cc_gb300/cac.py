@@ -73,6 +73,7 @@ EXPORTS = [
                               ctypes.POINTER(CCResult)]),
     ("cac_cc_edges", ctypes.c_int, [_vp, ctypes.c_uint32, ctypes.c_uint64, _vp, _vp, ctypes.c_uint32,
                                     ctypes.c_uint32, _vp, ctypes.POINTER(CCResult)]),
+    ("cac_cc_noalloc", ctypes.c_int, [ctypes.c_uint32, ctypes.c_uint64, _vp, _vp, _vp, _vp, _vp]),
     ("cac_mincut", ctypes.c_int, [_vp, _vp, ctypes.c_double, ctypes.c_uint32, ctypes.c_uint32,
                                   ctypes.POINTER(MincutResult)]),
     ("cac_mincut_trials", ctypes.c_int, [_vp, _vp, ctypes.c_uint32, ctypes.c_uint32, ctypes.c_uint32, _vp]),

@@ -24,6 +24,8 @@
 
 #include <algorithm>
 #include <cmath>
+#include <mutex>
+#include <string>
 
 namespace cac {
 namespace {
@@ -672,3 +674,101 @@ int cc_run(cac_ctx *ctx, uint32_t n, uint64_t m, const uint32_t *d_u, const uint
 }
 
 }  // namespace cac
+
+// ---------------------------------------------------------------------------------------------
+// Allocation-free connected components (cac_cc_noalloc).
+//
+// Some callers cannot allocate device memory: a plugin running inside a host framework whose
+// device memory is owned by that framework's allocator, or a latency-bound serving path that
+// must not take cudaMalloc's implicit synchronisation. For them this entry point runs the
+// single-pass form of the CC query (hook every edge, compress, count, label) with all of its
+// scratch in one file-scope device array of fixed size, so it performs no device allocation of
+// its own. The array belongs to this module: every GPU that loads the library holds it (16 MiB
+// for the parent array plus 8 KiB of tile counters) until the process exits.
+namespace cac {
+namespace {
+
+constexpr uint32_t kNoAllocMaxVertices = 1u << 22;  // 4,194,304 vertices
+constexpr uint32_t kNoAllocMaxTiles = (kNoAllocMaxVertices + kTile - 1) / kTile;
+constexpr int kNoAllocMaxDevices = 64;
+
+struct NoAllocScratch {
+    uint32_t parent[kNoAllocMaxVertices];
+    uint32_t counts[kNoAllocMaxTiles + 1];
+    uint32_t offsets[kNoAllocMaxTiles + 1];
+    uint32_t total[64];
+};
+
+__device__ __align__(256) NoAllocScratch g_noalloc_scratch;
+
+// Per-device set-up, done once with that device current: the device address of the scratch
+// array (its host-side name is only a stand-in) and the SM count used to size the grids.
+struct NoAllocDevice {
+    std::once_flag once;
+    NoAllocScratch *scratch = nullptr;
+    int sms = 0;
+    cudaError_t err = cudaSuccess;
+};
+NoAllocDevice g_noalloc_devices[kNoAllocMaxDevices];
+
+}  // namespace
+}  // namespace cac
+
+extern "C" int cac_cc_noalloc(uint32_t n, uint64_t m, const uint32_t *u_dev, const uint32_t *v_dev,
+                              uint32_t *labels_dev, uint32_t *num_components_dev, void *stream) {
+    using namespace cac;
+    if (n > kNoAllocMaxVertices) {
+        set_error("cac_cc_noalloc: n = " + std::to_string(n) + " exceeds the allocation-free limit of " +
+                  std::to_string(kNoAllocMaxVertices) + " vertices; use cac_cc for larger graphs");
+        return CAC_ERR_INVALID;
+    }
+    if (m > 0xFFFFFFFFull || (m && (!u_dev || !v_dev))) {
+        set_error("cac_cc_noalloc: invalid edge arrays (m must be < 2^32 and u/v non-null when m > 0)");
+        return CAC_ERR_INVALID;
+    }
+    int dev = 0;
+    CAC_CUDA_TRY(cudaGetDevice(&dev));
+    if (dev < 0 || dev >= kNoAllocMaxDevices) {
+        set_error("cac_cc_noalloc: device ordinal " + std::to_string(dev) + " out of range");
+        return CAC_ERR_INVALID;
+    }
+    NoAllocDevice &D = g_noalloc_devices[dev];
+    std::call_once(D.once, [&D, dev]() {
+        void *p = nullptr;
+        D.err = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+        if (D.err == cudaSuccess) D.err = cudaDeviceGetAttribute(&D.sms, cudaDevAttrMultiProcessorCount, dev);
+        if (D.err == cudaSuccess) D.scratch = reinterpret_cast<NoAllocScratch *>(p);
+    });
+    if (D.err != cudaSuccess || !D.scratch) {
+        set_error(std::string("cac_cc_noalloc: scratch set-up failed: ") + cudaGetErrorString(D.err));
+        return CAC_ERR_CUDA;
+    }
+    cudaStream_t s = (cudaStream_t)stream;
+    NoAllocScratch *S = D.scratch;
+    auto grid = [&](uint64_t work) {
+        return (int)std::max<uint64_t>(1, std::min<uint64_t>((work + kThreads - 1) / kThreads, (uint64_t)D.sms * 8));
+    };
+    if (n == 0) {
+        if (num_components_dev) CAC_CUDA_TRY(cudaMemsetAsync(num_components_dev, 0, 4, s));
+        return CAC_OK;
+    }
+    // Nothing in the scratch needs to start at zero: parent[] is initialised by cc_init, the tile
+    // counters and the total are fully written before they are read.
+    const uint32_t ntiles = (uint32_t)(((uint64_t)n + kTile - 1) / kTile);
+    cc_init<<<grid(n), kThreads, 0, s>>>(S->parent, n);
+    if (m > 0) {
+        const bool vec = ((reinterpret_cast<uintptr_t>(u_dev) | reinterpret_cast<uintptr_t>(v_dev)) & 15) == 0;
+        if (vec) cc_edge_pass<true><<<grid((m + 3) / 4), kThreads, 0, s>>>(S->parent, u_dev, v_dev, m);
+        else cc_edge_pass<false><<<grid(m), kThreads, 0, s>>>(S->parent, u_dev, v_dev, m);
+    }
+    cc_finalize_count<<<ntiles, kThreads, 0, s>>>(S->parent, n, S->counts);
+    cc_scan_tiles<<<1, 1024, 0, s>>>(S->counts, S->offsets, ntiles, S->total);
+    if (labels_dev) {
+        cc_rank_roots<<<ntiles, kThreads, 0, s>>>(S->parent, n, S->offsets, labels_dev);
+        cc_label_all<<<grid(n), kThreads, 0, s>>>(S->parent, n, labels_dev);
+    }
+    if (num_components_dev)
+        CAC_CUDA_TRY(cudaMemcpyAsync(num_components_dev, S->total, 4, cudaMemcpyDeviceToDevice, s));
+    CAC_CUDA_TRY(cudaGetLastError());
+    return CAC_OK;
+}

@@ -113,6 +113,22 @@ int cac_cc(cac_ctx *ctx, const cac_graph *g, uint32_t seed, uint32_t virtual_ran
 int cac_cc_edges(cac_ctx *ctx, uint32_t n, uint64_t m, const uint32_t *u_host, const uint32_t *v_host,
                  uint32_t seed, uint32_t virtual_ranks, uint32_t *labels_host, cac_cc_result *res);
 
+/* Connected components that allocates nothing. It has no counterpart in the reference. It is for
+ * callers that cannot allocate device memory: a plugin inside a host framework whose device
+ * memory belongs to that framework's allocator, or a latency-bound serving path that must not
+ * take cudaMalloc's implicit synchronisation. The caller passes device inputs and outputs; the
+ * scratch is one fixed array of this library that every GPU loading it holds until exit
+ * (16 MiB + 8 KiB), so n is limited to 4,194,304 vertices (CAC_ERR_INVALID beyond; cac_cc has no
+ * such limit). No ctx is needed: the work is enqueued on `stream` (a cudaStream_t of the current
+ * device, NULL for the default stream) and the call returns without synchronising.
+ * labels_dev (nullable) gets the same labels as cac_cc; num_components_dev (nullable, device)
+ * gets the component count. The first call on a device resolves the array's device address
+ * (make that first call before any stream capture). All calls share the one array: calls whose
+ * work overlaps on the GPU (other streams, other host threads) race and must be serialised by
+ * the caller. */
+int cac_cc_noalloc(uint32_t n, uint64_t m, const uint32_t *u_dev, const uint32_t *v_dev, uint32_t *labels_dev,
+                   uint32_t *num_components_dev, void *stream);
+
 /* ---- minimum cut (square_root) ---- */
 typedef struct {
     uint64_t cut;             /* the CSV `weight` column */

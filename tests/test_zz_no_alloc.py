@@ -1,0 +1,51 @@
+"""cac_cc_noalloc: connected components for callers that cannot allocate device memory (a plugin
+whose host framework owns all device memory, a serving path that must not take cudaMalloc's
+implicit synchronisation). It runs on one fixed scratch array of the library, so this test
+checks, through the C ABI, that two calls in a row on different graphs each give exactly the
+labels and count of the allocating entry point cac_cc (the scratch keeps the previous call's
+contents, which must not leak into the next result), and that oversized inputs are refused.
+Collected last on purpose: it shares nothing with the other tests and also passes alone."""
+import ctypes
+
+import numpy as np
+import pytest
+
+import graphgen
+import pyoracle as O
+
+pytestmark = pytest.mark.gpu
+
+
+def _device_u32(torch, a):
+    return torch.from_numpy(np.ascontiguousarray(a, dtype=np.uint32).view(np.int32)).cuda()
+
+
+def _noalloc(libcac, torch, n, u, v):
+    du, dv = _device_u32(torch, u), _device_u32(torch, v)
+    labels = torch.full((max(n, 1),), -1, dtype=torch.int32, device="cuda")
+    count = torch.full((1,), -1, dtype=torch.int32, device="cuda")
+    stream = torch.cuda.current_stream()
+    st = libcac.lib().cac_cc_noalloc(n, len(u), ctypes.c_void_p(du.data_ptr()), ctypes.c_void_p(dv.data_ptr()),
+                                     ctypes.c_void_p(labels.data_ptr()), ctypes.c_void_p(count.data_ptr()),
+                                     ctypes.c_void_p(stream.cuda_stream))
+    assert st == 0, libcac.lib().cac_last_error()
+    stream.synchronize()
+    return int(count.item()), labels.cpu().numpy().view(np.uint32)[:n]
+
+
+def test_two_calls_in_a_row_match_cac_cc(ctx, libcac):
+    torch = pytest.importorskip("torch")
+    graphs = [graphgen.barabasi_albert(200000, 8, 3), graphgen.rmat(16, 8, 4)]
+    for n, u, v, _ in graphs:  # two calls in a row, different graphs
+        count, labels = _noalloc(libcac, torch, n, u, v)
+        want_count, want_labels, _ = ctx.graph(n, u, v).connected_components(seed=0)
+        assert count == want_count
+        assert np.array_equal(labels, want_labels)
+        assert count == O.cc_labels(n, u, v)[0]
+
+
+def test_refuses_more_vertices_than_the_scratch_holds(libcac):
+    lib = libcac.lib()
+    st = lib.cac_cc_noalloc((1 << 22) + 1, 0, None, None, None, None, None)
+    assert st == -1
+    assert b"4194304" in lib.cac_last_error()
