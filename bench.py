@@ -128,6 +128,48 @@ def _cpu_baseline(n, u, v, budget_s=12.0):
                       "median %.3f s" % (len(times), rounds, med), "components": count}
 
 
+def _ks_workloads():
+    """The two single-graph square_root configurations: ER G(1000, 0.05) with weights in [1, 42]
+    on 4 virtual ranks (mpiexec -n 4), and the complete graph K4000 with weights in [1, 42]."""
+    import graphgen
+    return [("square_root ER n=1000 p=0.05 w[1,42], 4 virtual ranks", graphgen.erdos_renyi(1000, 0.05, 0), 4, 5),
+            ("square_root K4000 w[1,42]", graphgen.complete(4000, 0), 1, 3)]
+
+
+def _ks_also(ctx):
+    """Karger-Stein trials/s of the square_root path (the other half of the metric), each next to a
+    bounded sample of the oracle's CPU replay of the same trials (single thread)."""
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import pyoracle
+    out = []
+    for name, (n, u, v, w), ranks, reps in _ks_workloads():
+        g = ctx.graph(n, u, v, w)
+        res = g.square_root(0.95, seed=0, virtual_ranks=ranks)  # warm-up (also builds the level buffers)
+        ms = []
+        for _ in range(reps):
+            res = g.square_root(0.95, seed=0, virtual_ranks=ranks)
+            ms.append(res.device_ms)
+        trials = res.total_trials
+        deg = np.zeros(n, np.uint64)
+        np.add.at(deg, u, w.astype(np.uint64))
+        np.add.at(deg, v, w.astype(np.uint64))
+        t0 = time.perf_counter()
+        if n <= 1000:
+            cpu_cut, _ = pyoracle.square_root(n, u, v, w, 0.95, 0, ranks)
+            cpu_trials = trials
+        else:
+            cpu_cut, cpu_trials = pyoracle.mincut_trial(n, u, v, w, 0, 0, 0), 1
+        cpu_s = time.perf_counter() - t0
+        out.append({"workload": name, "trials": trials, "cut": int(res.cut),
+                    "min_weighted_degree": int(deg.min()), "ms_per_query": statistics.median(ms),
+                    "trials_per_s": trials / (statistics.median(ms) / 1e3),
+                    "cpu_baseline": {"trials_per_s": cpu_trials / cpu_s, "cores": 1, "kind": "port",
+                                     "sample": "%d trial(s) of the oracle's replay" % cpu_trials,
+                                     "cut_agrees": (cpu_cut == res.cut) if cpu_trials == trials else None}})
+        g.free()
+    return out
+
+
 def run_reference(args, rank, world):
     if rank != 0:
         return 0
@@ -223,11 +265,13 @@ def run_cac(args, rank, world):
     alg_bytes = 8 * m
     achieved = alg_bytes / (edge_avg_ms / 1e3) / 1e9
     traffic = None
-    prof = os.path.join(ROOT, "profiles", "cc_edge_pass_ba1m.json")
+    prof = os.path.join(ROOT, "profiles", "cc_filter_ba1m.json")
     if os.path.exists(prof):
         with open(prof) as f:
             traffic = json.load(f).get("dram_bytes_per_launch")
     if rank != 0:
+        g.free()
+        ctx.close()
         return 0
     line = {
         "metric": METRIC, "value": value, "unit": "edges/s", "n_gpus": world, "steps": args.steps,
@@ -249,6 +293,8 @@ def run_cac(args, rank, world):
     }
     if not args.no_cpu_baseline:
         line["cpu_baseline"] = _cpu_baseline(n, u, v)
+    if not args.no_ks:
+        line["also_ks"] = _ks_also(ctx)
     print(json.dumps(line))
     g.free()
     ctx.close()
@@ -262,6 +308,7 @@ def main():
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="cac", choices=["cac", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-ks", action="store_true", help="skip the square_root (Karger-Stein) measurements")
     args = ap.parse_args()
     rank = int(os.environ.get("RANK", "0"))
     world = int(os.environ.get("WORLD_SIZE", "1"))

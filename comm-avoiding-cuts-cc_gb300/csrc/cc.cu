@@ -234,9 +234,7 @@ __global__ void __launch_bounds__(kEdgeThreads) cc_filter(const uint32_t *__rest
     };
     const uint4 *u4 = reinterpret_cast<const uint4 *>(u);
     const uint4 *v4 = reinterpret_cast<const uint4 *>(v);
-    for (uint64_t t = t0 + warp; t < t1; t += nwarps) {
-        const uint4 ua = __ldcs(u4 + t * 64 + lane), ub = __ldcs(u4 + t * 64 + 32 + lane);
-        const uint4 va = __ldcs(v4 + t * 64 + lane), vb = __ldcs(v4 + t * 64 + 32 + lane);
+    auto process = [&](const uint4 &ua, const uint4 &ub, const uint4 &va, const uint4 &vb) {
         const uint32_t a[8] = {ua.x, ua.y, ua.z, ua.w, ub.x, ub.y, ub.z, ub.w};
         const uint32_t b[8] = {va.x, va.y, va.z, va.w, vb.x, vb.y, vb.z, vb.w};
         uint32_t keep = 0;
@@ -250,13 +248,24 @@ __global__ void __launch_bounds__(kEdgeThreads) cc_filter(const uint32_t *__rest
             if (lane >= o) incl += y;
         }
         const uint32_t total = __shfl_sync(0xffffffffu, incl, 31);
-        if (total == 0) continue;
+        if (total == 0) return;
         uint32_t base = 0;
         if (lane == 31) base = atomicAdd(&s_n, total);
         base = __shfl_sync(0xffffffffu, base, 31) + incl - cnt;
 #pragma unroll
         for (int k = 0; k < 8; k++)
             if ((keep >> k) & 1u) out[base++] = make_uint2(a[k], b[k]);
+    };
+    // two tiles per warp step: all eight 512-byte loads are issued before either tile is used
+    for (uint64_t t = t0 + 2 * (uint64_t)warp; t < t1; t += 2 * (uint64_t)nwarps) {
+        const bool two = t + 1 < t1;
+        const uint4 z = make_uint4(0, 0, 0, 0);
+        const uint4 ua = __ldcs(u4 + t * 64 + lane), ub = __ldcs(u4 + t * 64 + 32 + lane);
+        const uint4 va = __ldcs(v4 + t * 64 + lane), vb = __ldcs(v4 + t * 64 + 32 + lane);
+        const uint4 uc = two ? __ldcs(u4 + (t + 1) * 64 + lane) : z, ud = two ? __ldcs(u4 + (t + 1) * 64 + 32 + lane) : z;
+        const uint4 vc = two ? __ldcs(v4 + (t + 1) * 64 + lane) : z, vd = two ? __ldcs(v4 + (t + 1) * 64 + 32 + lane) : z;
+        process(ua, ub, va, vb);
+        if (two) process(uc, ud, vc, vd);
     }
     __syncthreads();
     if (threadIdx.x == 0) counts[blockIdx.x] = s_n;
