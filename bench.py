@@ -41,9 +41,9 @@ import numpy as np  # noqa: E402
 
 N_VERTICES, ATTACH, GRAPH_SEED = 1024000, 16, 0
 METRIC = "CC edges/s (parallel_cc, BA n=1,024,000 m=16)"
-# init, 8 x (sample_hook + compress), find_giant, giant_bitmap, filter, hook_survivors, finalize_count, scan_tiles,
-# rank_roots, label_all
-KERNELS_PER_QUERY = 1 + 8 * 2 + 8
+# init, sample_draws, 8 x (sample_hook + compress4), find_giant, giant_bitmap, filter, hook_survivors,
+# finalize_count, scan_tiles, rank_roots, label_all
+KERNELS_PER_QUERY = 2 + 8 * 2 + 8
 
 
 def _peaks():

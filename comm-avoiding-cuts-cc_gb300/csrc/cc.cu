@@ -44,8 +44,9 @@ constexpr uint32_t kMaxRegions = 1024;               // filter CTAs (regions of 
 struct RankDesc {
     uint64_t slice_off;
     uint64_t slice_len;
-    uint64_t draws;
-    uint64_t block_off;  // first chunk draw of this rank in the flattened launch
+    uint64_t draws;      // chunk draws of this rank
+    uint64_t block_off;  // first sitmo block (8 chunk draws) of this rank in the flattened launch
+    uint64_t draw_off;   // first chunk draw of this rank in the flattened draw list
     uint32_t key0;       // seed + rank
     uint32_t pad;
 };
@@ -90,47 +91,89 @@ __device__ __forceinline__ void unite(uint32_t *par, uint32_t a, uint32_t b) {
     }
 }
 
-__global__ void cc_init(uint32_t *par, uint32_t n) {
-    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) par[i] = i;
-}
-
-// One warp per draw of the range [d0, d1) of all ranks' draws. The reference draws single edges (engine() % slice, a random 8-byte
-// gather each); here draw k of rank r (32-bit output k of stream (seed + r, 0, 0, 0)) selects
-// chunk (output % chunks) of kSampleChunk consecutive edges of the rank's slice, which the warp
-// reads with coalesced loads and hooks. The number of sampled edges matches the reference's
-// per-rank budget.
-__global__ void cc_sample_hook(uint32_t *par, const uint32_t *__restrict__ u, const uint32_t *__restrict__ v,
-                               const RankDesc *__restrict__ ranks, int nranks, uint64_t d0, uint64_t d1) {
-    const int lane = threadIdx.x & 31;
-    const uint64_t warps = ((uint64_t)gridDim.x * blockDim.x) >> 5;
-    for (uint64_t gd = d0 + (((uint64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5); gd < d1; gd += warps) {
-        int lo = 0, hi = nranks - 1;  // last rank whose first draw <= gd
-        while (lo < hi) {
-            int mid = (lo + hi + 1) >> 1;
-            if (ranks[mid].block_off <= gd) lo = mid; else hi = mid - 1;
-        }
-        const RankDesc rd = ranks[lo];
-        const uint64_t k = gd - rd.block_off;  // draw index within the rank's stream
-        const u64x4 o = sitmo_block(rd.key0, 0, 0, 0, k >> 3, 0, 0, 0);
-        const unsigned j = (unsigned)(k & 7);
-        const uint64_t word = (j >> 1) == 0 ? o.x[0] : (j >> 1) == 1 ? o.x[1] : (j >> 1) == 2 ? o.x[2] : o.x[3];
-        const uint32_t x = (j & 1) ? (uint32_t)(word >> 32) : (uint32_t)word;
-        const uint64_t nchunks = (rd.slice_len + kSampleChunk - 1) / kSampleChunk;
-        const uint64_t e = rd.slice_off + (x % nchunks) * kSampleChunk + lane;
-        if (e < rd.slice_off + rd.slice_len) unite(par, __ldg(u + e), __ldg(v + e));
-    }
-}
-
-__global__ void cc_compress(uint32_t *par, uint32_t n) {
-    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
-        par[i] = find_root_ro(par, i);
-}
-
 __device__ __forceinline__ void edge_hook(uint32_t *par, uint32_t a, uint32_t b) {
     const uint32_t pa = par[a], pb = par[b];
     if (pa == pb) return;  // already one component: the reference drops this edge as a loop
     unite(par, pa, pb);
 }
+
+__global__ void cc_init(uint32_t *par, uint32_t n) {
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) par[i] = i;
+}
+
+// The draws of the sampling round, one thread per sitmo block (8 draws of one rank). The reference
+// draws single edges (engine() % slice, a random 8-byte gather each); here draw k of rank r
+// (32-bit output k of stream (seed + r, 0, 0, 0), word k % 8 of block k / 8) selects chunk
+// (output % chunks) of kSampleChunk consecutive edges of the rank's slice. The chunk is stored as
+// (first edge | edge count << 32) at the draw's flattened index.
+__global__ void cc_sample_draws(const RankDesc *__restrict__ ranks, int nranks, uint64_t nblocks,
+                                uint64_t *__restrict__ chunks) {
+    for (uint64_t gb = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; gb < nblocks;
+         gb += (uint64_t)gridDim.x * blockDim.x) {
+        int lo = 0, hi = nranks - 1;  // last rank whose first block <= gb
+        while (lo < hi) {
+            int mid = (lo + hi + 1) >> 1;
+            if (ranks[mid].block_off <= gb) lo = mid; else hi = mid - 1;
+        }
+        const RankDesc rd = ranks[lo];
+        const uint64_t blk = gb - rd.block_off;  // sitmo block index within the rank's stream
+        const u64x4 o = sitmo_block(rd.key0, 0, 0, 0, blk, 0, 0, 0);
+        const uint64_t nchunks = (rd.slice_len + kSampleChunk - 1) / kSampleChunk;
+        const uint64_t end = rd.slice_off + rd.slice_len;
+#pragma unroll
+        for (int j = 0; j < 8; j++) {
+            const uint64_t k = blk * 8 + j;
+            if (k >= rd.draws) break;  // rd.draws counts chunk draws
+            const uint64_t word = o.x[j >> 1];
+            const uint32_t x = (j & 1) ? (uint32_t)(word >> 32) : (uint32_t)word;
+            const uint64_t first = rd.slice_off + (x % nchunks) * kSampleChunk;
+            const uint64_t count = min((uint64_t)kSampleChunk, end - first);
+            chunks[rd.draw_off + k] = first | (count << 32);
+        }
+    }
+}
+
+// One warp per sampled chunk of the draw range [d0, d1): coalesced loads of its edges, each hooked.
+__global__ void cc_sample_hook(uint32_t *par, const uint32_t *__restrict__ u, const uint32_t *__restrict__ v,
+                               const uint64_t *__restrict__ chunks, uint64_t d0, uint64_t d1) {
+    const uint32_t lane = threadIdx.x & 31;
+    const uint64_t warps = ((uint64_t)gridDim.x * blockDim.x) >> 5;
+    for (uint64_t d = d0 + (((uint64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5); d < d1; d += warps) {
+        const uint64_t c = chunks[d];
+        if (lane < (uint32_t)(c >> 32)) {
+            const uint64_t e = (c & 0xFFFFFFFFull) + lane;
+            edge_hook(par, __ldg(u + e), __ldg(v + e));
+        }
+    }
+}
+
+__global__ void cc_compress(uint32_t *par, uint32_t lo, uint32_t hi) {
+    for (uint32_t i = lo + blockIdx.x * blockDim.x + threadIdx.x; i < hi; i += gridDim.x * blockDim.x)
+        par[i] = find_root_ro(par, i);
+}
+
+// Full compression, 4 consecutive vertices per thread: one 16-byte load of their parents, then
+// the grandparents of all four requested together (most chains end there), then the rare longer
+// chains; one 16-byte store. Only roots are written, as in cc_compress.
+__global__ void cc_compress4(uint32_t *par, uint32_t n4) {
+    uint4 *p4 = reinterpret_cast<uint4 *>(par);
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n4; i += gridDim.x * blockDim.x) {
+        const uint4 p = p4[i];
+        const uint32_t v0 = 4 * i;
+        uint32_t r0 = p.x, r1 = p.y, r2 = p.z, r3 = p.w;
+        const uint32_t g0 = r0 != v0 ? par[r0] : r0, g1 = r1 != v0 + 1 ? par[r1] : r1;
+        const uint32_t g2 = r2 != v0 + 2 ? par[r2] : r2, g3 = r3 != v0 + 3 ? par[r3] : r3;
+        r0 = g0 == r0 ? r0 : find_root_ro(par, g0);
+        r1 = g1 == r1 ? r1 : find_root_ro(par, g1);
+        r2 = g2 == r2 ? r2 : find_root_ro(par, g2);
+        r3 = g3 == r3 ? r3 : find_root_ro(par, g3);
+        if (r0 != p.x || r1 != p.y || r2 != p.z || r3 != p.w) p4[i] = make_uint4(r0, r1, r2, r3);
+    }
+}
+
+// Compression of [0, n): the vectorised body over whole 4-vertex groups, the scalar kernel for
+// the tail (the parent array is 256-byte aligned).
+void compress_all(cac_ctx *ctx, uint32_t *par, uint32_t n, cudaStream_t s);
 
 // The most frequent root among kGiantSample vertices spread over [0, n) (compressed parents):
 // one CTA bitonic-sorts the sampled roots in shared memory; every run start measures its run by
@@ -213,6 +256,7 @@ __global__ void __launch_bounds__(kThreads) cc_edge_pass(uint32_t *par, const ui
 // two fully coalesced 512-byte loads per endpoint array, keeps 8 edges in flight, and appends its
 // survivors after one warp scan and one shared-memory atomic. The membership bitmap's first
 // `swords` words are staged in shared memory, the rest read through the read-only path.
+template <bool kAllSmem>
 __global__ void __launch_bounds__(kEdgeThreads) cc_filter(const uint32_t *__restrict__ u,
                                                           const uint32_t *__restrict__ v, uint64_t tiles,
                                                           const uint32_t *__restrict__ gbits, uint32_t nwords,
@@ -229,7 +273,7 @@ __global__ void __launch_bounds__(kEdgeThreads) cc_filter(const uint32_t *__rest
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarps = blockDim.x >> 5;
     auto in_giant = [&](uint32_t x) -> bool {
         const uint32_t w = x >> 5;
-        const uint32_t word = w < swords ? sbits[w] : __ldg(gbits + w);
+        const uint32_t word = (kAllSmem || w < swords) ? sbits[w] : __ldg(gbits + w);
         return (word >> (x & 31)) & 1u;
     };
     const uint4 *u4 = reinterpret_cast<const uint4 *>(u);
@@ -418,6 +462,12 @@ int grid_for(cac_ctx *ctx, uint64_t work, int per_sm) {
     return (int)std::max<uint64_t>(1, std::min(need, cap));
 }
 
+void compress_all(cac_ctx *ctx, uint32_t *par, uint32_t n, cudaStream_t s) {
+    const uint32_t n4 = n / 4;
+    if (n4) cc_compress4<<<grid_for(ctx, n4, 8), kThreads, 0, s>>>(par, n4);
+    if (n & 3) cc_compress<<<1, 32, 0, s>>>(par, 4 * n4, n);
+}
+
 }  // namespace
 
 CCPlan cc_plan(uint32_t n, uint64_t m, uint32_t ranks) {
@@ -491,7 +541,8 @@ struct CCLaunch {
     RankDesc *d_ranks = nullptr;
     const RankDesc *h_ranks = nullptr;
     uint32_t ntiles = 0, nwords = 0;
-    uint64_t draws = 0, drawn = 0;
+    uint64_t blocks = 0, draws = 0, drawn = 0;  // sitmo blocks, chunk draws, sampled edges
+    uint64_t *chunks = nullptr;                  // per draw: first edge | count << 32
     bool vec = false;
 };
 
@@ -513,12 +564,14 @@ int cc_enqueue(cac_ctx *ctx, const CCLaunch &L, bool capturing) {
         // The draws are hooked in kSampleSubrounds slices with a full compression after each:
         // forest building from singletons is the expensive part of CC, and keeping every tree
         // flat between slices keeps the union walks of the next slice one or two hops long.
+        cc_sample_draws<<<grid_for(ctx, L.blocks, 8), kThreads, 0, s>>>(L.d_ranks, (int)L.ranks, L.blocks,
+                                                                        L.chunks);
         const uint32_t sub = (uint32_t)std::min<uint64_t>(kSampleSubrounds, L.draws);
         for (uint32_t k = 0; k < sub; k++) {
             const uint64_t d0 = L.draws * k / sub, d1 = L.draws * (k + 1) / sub;
-            cc_sample_hook<<<grid_for(ctx, (d1 - d0) * 32, 8), kThreads, 0, s>>>(L.par, L.u, L.v, L.d_ranks,
-                                                                                  (int)L.ranks, d0, d1);
-            cc_compress<<<grid_for(ctx, n, 8), kThreads, 0, s>>>(L.par, n);
+            cc_sample_hook<<<grid_for(ctx, (d1 - d0) * 32, 8), kThreads, 0, s>>>(L.par, L.u, L.v, L.chunks, d0,
+                                                                                  d1);
+            compress_all(ctx, L.par, n, s);
         }
         cc_find_giant<<<1, kGiantSample, 0, s>>>(L.par, n, L.giant);
         cc_giant_bitmap<<<grid_for(ctx, n, 8), kThreads, 0, s>>>(L.par, n, L.giant, L.bits);
@@ -532,9 +585,10 @@ int cc_enqueue(cac_ctx *ctx, const CCLaunch &L, bool capturing) {
             const uint32_t regions = (uint32_t)std::max<uint64_t>(
                 1, std::min<uint64_t>({(uint64_t)ctx->num_sms, (uint64_t)kMaxRegions, tiles}));
             const uint64_t per = (tiles + regions - 1) / regions;
-            if (tiles)
-                cc_filter<<<regions, kEdgeThreads, sm, s>>>(L.u, L.v, tiles, L.bits, L.nwords, L.surv,
-                                                            L.region_counts);
+            if (tiles) {
+                auto filt = L.nwords <= kSmemBitmapWords ? cc_filter<true> : cc_filter<false>;
+                filt<<<regions, kEdgeThreads, sm, s>>>(L.u, L.v, tiles, L.bits, L.nwords, L.surv, L.region_counts);
+            }
             CAC_TRY(record(ctx, 4, capturing));
             if (tiles)
                 cc_hook_survivors<<<(unsigned)ctx->num_sms * 4, kThreads, 0, s>>>(L.par, L.surv, L.region_counts,
@@ -587,6 +641,8 @@ int cc_run(cac_ctx *ctx, uint32_t n, uint64_t m, const uint32_t *d_u, const uint
         return CAC_OK;
     }
     const CCPlan plan = cc_plan(n, m, ranks);
+    uint64_t chunk_slots = 1;
+    for (uint32_t r = 0; r < ranks; r++) chunk_slots += (plan.draws[r] + kSampleChunk - 1) / kSampleChunk;
     CCLaunch L;
     L.n = n;
     L.m = m;
@@ -598,7 +654,7 @@ int cc_run(cac_ctx *ctx, uint32_t n, uint64_t m, const uint32_t *d_u, const uint
     L.nwords = (uint32_t)(((uint64_t)n + 31) / 32);
     L.vec = ((reinterpret_cast<uintptr_t>(d_u) | reinterpret_cast<uintptr_t>(d_v)) & 15) == 0;
 
-    CAC_TRY(arena_reserve(ctx, cc_scratch_bytes(n, ranks, m)));
+    CAC_TRY(arena_reserve(ctx, cc_scratch_bytes(n, ranks, m) + align_up(chunk_slots * 8)));
     arena_reset(ctx);
     L.par = (uint32_t *)arena_take(ctx, (size_t)n * 4);
     L.counts = (uint32_t *)arena_take(ctx, (size_t)L.ntiles * 4 + 4);
@@ -609,6 +665,7 @@ int cc_run(cac_ctx *ctx, uint32_t n, uint64_t m, const uint32_t *d_u, const uint
     L.bits = (uint32_t *)arena_take(ctx, (size_t)L.nwords * 4 + 4);
     L.region_counts = (uint32_t *)arena_take(ctx, kMaxRegions * 4);
     L.surv = (uint2 *)arena_take(ctx, (m + 4 * (uint64_t)kMaxRegions) * 8);
+    L.chunks = (uint64_t *)arena_take(ctx, chunk_slots * 8);
 
     // rank descriptors go through the ctx's pinned staging page when they fit (async copy)
     std::vector<RankDesc> hv;
@@ -621,20 +678,24 @@ int cc_run(cac_ctx *ctx, uint32_t n, uint64_t m, const uint32_t *d_u, const uint
         hr = hv.data();
     }
     for (uint32_t r = 0; r < ranks; r++) {
+        const uint64_t chunk_draws = (plan.draws[r] + kSampleChunk - 1) / kSampleChunk;
         hr[r].slice_off = plan.slice_off[r];
         hr[r].slice_len = plan.slice_len[r];
-        hr[r].draws = plan.draws[r];
-        hr[r].block_off = L.draws;
+        hr[r].draws = chunk_draws;
+        hr[r].block_off = L.blocks;
+        hr[r].draw_off = L.draws;
         hr[r].key0 = seed + r;
         hr[r].pad = 0;
-        const uint64_t chunk_draws = (plan.draws[r] + kSampleChunk - 1) / kSampleChunk;
+        L.blocks += (chunk_draws + 7) / 8;
         L.draws += chunk_draws;
         L.drawn += chunk_draws * kSampleChunk;
     }
     L.h_ranks = hr;
-    if (L.draws > 0 && m > 0)
-        CAC_CUDA_TRY(cudaFuncSetAttribute(cc_filter, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                          (int)((size_t)std::min(L.nwords, kSmemBitmapWords) * 4)));
+    if (L.draws > 0 && m > 0) {
+        const int sm = (int)((size_t)std::min(L.nwords, kSmemBitmapWords) * 4);
+        CAC_CUDA_TRY(cudaFuncSetAttribute(cc_filter<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, sm));
+        CAC_CUDA_TRY(cudaFuncSetAttribute(cc_filter<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, sm));
+    }
 
     // Repeated identical queries replay a captured CUDA graph: one launch instead of a dozen
     // kernel launches and copies. The first sighting of a key runs directly; the second captures.
@@ -671,7 +732,7 @@ int cc_run(cac_ctx *ctx, uint32_t n, uint64_t m, const uint32_t *d_u, const uint
     CAC_CUDA_TRY(cudaStreamSynchronize(s));
     if (res) {
         res->num_components = ctx->pinned_u32[0];
-        res->rounds = (L.draws > 0 ? 1u : 0u) + (m > 0 ? 1u : 0u);
+        res->rounds = (L.draws > 0 ? 1u : 0u) + (m > 0 ? 1u : 0u);  // sampling round + closing pass
         res->sampled_edges = L.drawn;
         CAC_CUDA_TRY(cudaEventElapsedTime(&res->device_ms, ctx->ev[0], ctx->ev[3]));
         CAC_CUDA_TRY(cudaEventElapsedTime(&res->edge_pass_ms, ctx->ev[1], ctx->ev[4]));
