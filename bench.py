@@ -170,6 +170,43 @@ def _ks_also(ctx):
     return out
 
 
+def run_ks(args, rank, world):
+    """--workload ks-er1000 | ks-k4000: only the square_root (Karger-Stein) measurement, one JSON line."""
+    import torch
+    import cac
+    dev = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(dev)
+    name, (n, u, v, w), ranks, _ = _ks_workloads()[0 if args.workload == "ks-er1000" else 1]
+    stream = torch.cuda.Stream(device=dev)
+    ctx = cac.Context(dev, stream=stream.cuda_stream)
+    g = ctx.graph(n, u, v, w)
+    for _ in range(args.warmup):
+        res = g.square_root(0.95, seed=0, virtual_ranks=ranks)
+    torch.cuda.synchronize()
+    ms = []
+    with Clocks(dev) as clk:
+        for _ in range(args.steps):
+            res = g.square_root(0.95, seed=0, virtual_ranks=ranks)
+            ms.append(res.device_ms)
+    total_ms = sum(ms)
+    if world > 1:
+        t = torch.tensor([total_ms], device="cuda")
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        total_ms = float(t.item())
+    line = {"metric": "Karger-Stein trials/s (%s)" % name, "value": world * res.total_trials * args.steps / (total_ms / 1e3),
+            "unit": "trials/s", "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": total_ms / args.steps, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "u64", "data": "synthetic (seeded)", "cut": int(res.cut),
+            "config": {"workload": name, "vertices": n, "edges": int(len(u)), "virtual_ranks": ranks,
+                       "trials_per_query": res.total_trials, "intermediate_size": res.intermediate},
+            "clocks": clk.summary()}
+    if rank == 0:
+        print(json.dumps(line))
+    g.free()
+    ctx.close()
+    return 0
+
+
 def run_reference(args, rank, world):
     if rank != 0:
         return 0
@@ -309,6 +346,8 @@ def main():
     ap.add_argument("--impl", default="cac", choices=["cac", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-ks", action="store_true", help="skip the square_root (Karger-Stein) measurements")
+    ap.add_argument("--workload", default="cc", choices=["cc", "ks-er1000", "ks-k4000"],
+                    help="cc: the benchmark line; ks-*: only one square_root configuration")
     args = ap.parse_args()
     rank = int(os.environ.get("RANK", "0"))
     world = int(os.environ.get("WORLD_SIZE", "1"))
@@ -319,6 +358,8 @@ def main():
         torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", "0")))
         torch.distributed.init_process_group("nccl")
     try:
+        if args.workload != "cc":
+            return run_ks(args, rank, world)
         return run_cac(args, rank, world)
     finally:
         if world > 1:

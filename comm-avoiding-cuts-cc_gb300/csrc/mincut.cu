@@ -382,48 +382,60 @@ __global__ void __launch_bounds__(NT) contract_kernel(const TaskDesc *__restrict
     if (threadIdx.x == 0) k_out[blockIdx.x] = k;
 }
 
+// One CTA per group of `rows` consecutive output rows of one child. For each row a: the sum of the
+// member rows of group a, accumulated column by column in shared memory (each thread owns its
+// columns, one pass per member row, coalesced reads); then every output column b gathers its
+// members' entries of that sum through the member lists (no atomics). The diagonal (b == a) is 0.
 template <int NT>
 __global__ void __launch_bounds__(NT) quotient_kernel(const TaskDesc *__restrict__ tasks,
                                                       const SrcDesc *__restrict__ srcs,
                                                       const uint32_t *__restrict__ kdim,
-                                                      const uint64_t *__restrict__ row_task_off, uint32_t ntasks,
-                                                      const uint64_t *__restrict__ out_off, uint64_t *out_base) {
+                                                      const uint64_t *__restrict__ group_task_off, uint32_t ntasks,
+                                                      uint32_t rows, const uint64_t *__restrict__ out_off,
+                                                      uint64_t *out_base) {
     extern __shared__ __align__(16) unsigned char dsm[];
-    const uint64_t gr = blockIdx.x;
+    const uint64_t gg = blockIdx.x;
     uint32_t lo = 0, hi = ntasks - 1;
-    while (lo < hi) {  // last task whose first output row <= gr
+    while (lo < hi) {  // last task whose first row group <= gg
         const uint32_t mid = (lo + hi + 1) >> 1;
-        if (row_task_off[mid] <= gr) lo = mid; else hi = mid - 1;
+        if (group_task_off[mid] <= gg) lo = mid; else hi = mid - 1;
     }
     const TaskDesc T = tasks[lo];
     const SrcDesc S = srcs[T.src];
     const uint32_t k = kdim[lo];
-    const uint32_t a = (uint32_t)(gr - row_task_off[lo]);
     const uint32_t N = S.N;
-    unsigned long long *acc = reinterpret_cast<unsigned long long *>(dsm);
-    uint32_t *labs = reinterpret_cast<uint32_t *>(dsm + (size_t)k * 8);
-    for (uint32_t b = threadIdx.x; b < k; b += NT) acc[b] = 0;
-    for (uint32_t j = threadIdx.x; j < N; j += NT) labs[j] = T.lab[j];
-    __syncthreads();
-    const uint32_t p0 = T.memb_off[a], p1 = T.memb_off[a + 1];
-    for (uint32_t p = p0; p < p1; p++) {
-        const uint64_t *row = S.mat + (uint64_t)T.members[p] * N;
-        for (uint32_t j = threadIdx.x; j < N; j += NT) {
-            const uint64_t x = row[j];
-            if (x) {
-                const uint32_t l = labs[j];
-                if (l != a) atomicAdd(&acc[l], (unsigned long long)x);
+    const uint32_t a0 = (uint32_t)(gg - group_task_off[lo]) * rows, a1 = min(k, a0 + rows);
+    uint64_t *rowsum = reinterpret_cast<uint64_t *>(dsm);  // N entries
+    uint64_t *Qt = out_base + out_off[lo];
+    for (uint32_t a = a0; a < a1; a++) {
+        const uint32_t p0 = T.memb_off[a], p1 = T.memb_off[a + 1];
+        for (uint32_t p = p0; p < p1; p++) {
+            const uint64_t *row = S.mat + (uint64_t)T.members[p] * N;
+            if (p == p0) {
+                for (uint32_t j = threadIdx.x; j < N; j += NT) rowsum[j] = row[j];
+            } else {
+                for (uint32_t j = threadIdx.x; j < N; j += NT) rowsum[j] += row[j];
             }
         }
+        __syncthreads();
+        uint64_t *Q = Qt + (uint64_t)a * k;
+        for (uint32_t b = threadIdx.x; b < k; b += NT) {
+            uint64_t acc = 0;
+            if (b != a) {
+                const uint32_t q1 = T.memb_off[b + 1];
+                for (uint32_t q = T.memb_off[b]; q < q1; q++) acc += rowsum[T.members[q]];
+            }
+            Q[b] = acc;
+        }
+        __syncthreads();
     }
-    __syncthreads();
-    uint64_t *Q = out_base + out_off[lo] + (uint64_t)a * k;
-    for (uint32_t b = threadIdx.x; b < k; b += NT) Q[b] = acc[b];
 }
 
 // Stoer-Wagner on one leaf (n <= 128) by one warp: lane l owns vertices l, l+32, l+64, l+96.
 // Maximum-adjacency order by warp argmax of (key << 8 | 255 - vertex): the largest key wins,
 // ties go to the smallest vertex; keys stay below 2^56 (total graph weight checked on the host).
+// Any maximum-adjacency order gives the exact cut, so the tie rule only fixes determinism.
+// The full matrix sits in shared memory so that a row read is conflict-free.
 template <typename Tm>
 __global__ void __launch_bounds__(32) sw_leaf_kernel(const LeafDesc *__restrict__ leaves, uint64_t *cuts) {
     extern __shared__ __align__(16) unsigned char dsm[];
@@ -452,11 +464,12 @@ __global__ void __launch_bounds__(32) sw_leaf_kernel(const LeafDesc *__restrict_
                     local = cand > local ? cand : local;
                 }
             }
-#pragma unroll
-            for (int o = 16; o > 0; o >>= 1) {
-                const uint64_t y = __shfl_xor_sync(0xffffffffu, local, o);
-                local = y > local ? y : local;
-            }
+            // warp argmax of the packed keys: max of the high words, then of the low words among
+            // the lanes holding that high word (two redux.sync reductions)
+            const uint32_t hi = (uint32_t)(local >> 32);
+            const uint32_t top = __reduce_max_sync(0xffffffffu, hi);
+            const uint32_t lo = __reduce_max_sync(0xffffffffu, hi == top ? (uint32_t)local : 0u);
+            local = ((uint64_t)top << 32) | lo;
             const uint32_t sv = 255u - (uint32_t)(local & 255u);
             if (step + 1 == cnt) {
                 last = sv;
@@ -546,7 +559,7 @@ struct PendingTask {
 
 
 size_t contract_smem(uint32_t N) { return kBatch * sizeof(uint2) + (size_t)2 * N * 4; }
-size_t quotient_smem(uint32_t k, uint32_t N) { return (size_t)k * 8 + (size_t)N * 4; }
+size_t quotient_smem(uint32_t k, uint32_t N) { return (size_t)N * 8; }
 
 // Runs Stage 3 for the root matrices of one wave; cuts[] (wave slots) must hold the Stage-1/2
 // bounds (UINT64_MAX before the root nodes' minimum-degree bound is applied).
@@ -680,30 +693,32 @@ int ks_levels(cac_ctx *ctx, std::vector<Node> nodes, DevBuf *cur, DevBuf *next, 
         CAC_CUDA_TRY(cudaMemcpyAsync(kk.data(), d_kout.p, tasks.size() * 4, cudaMemcpyDeviceToHost, s));
         CAC_CUDA_TRY(cudaStreamSynchronize(s));
         // output matrices of this iteration
-        std::vector<uint64_t> out_off(tasks.size(), 0), row_task_off(tasks.size(), 0);
+        std::vector<uint64_t> out_off(tasks.size(), 0), group_task_off(tasks.size(), 0);
         std::vector<uint32_t> kq(tasks.size(), 0);
-        uint64_t out_elems = 0, out_rows = 0;
+        uint64_t out_elems = 0, groups = 0;
         size_t qsm = 0;
+        // rows per quotient CTA: one for wide matrices, up to 16 as rows get short
+        const uint32_t qrows = std::max<uint32_t>(1, std::min<uint32_t>(16, 4096 / std::max<uint32_t>(maxN, 1)));
         for (size_t i = 0; i < tasks.size(); i++) {
             const uint32_t k = kk[i] == kDropped ? 0 : kk[i];
             kq[i] = k;
             out_off[i] = out_elems;
-            row_task_off[i] = out_rows;
+            group_task_off[i] = groups;
             out_elems += (uint64_t)k * k;
-            out_rows += k;
+            groups += (k + qrows - 1) / qrows;
             if (k) qsm = std::max(qsm, quotient_smem(k, srcs[tasks[i].src].N));
         }
         CAC_TRY(next->ensure(std::max<uint64_t>(out_elems, 1) * 8));
-        if (out_rows) {
+        if (groups) {
             CAC_TRY(upload(ctx, d_qoff, out_off));
-            CAC_TRY(upload(ctx, d_rto, row_task_off));
+            CAC_TRY(upload(ctx, d_rto, group_task_off));
             CAC_TRY(d_kout.ensure(tasks.size() * 4));
             CAC_CUDA_TRY(cudaMemcpyAsync(d_kout.p, kq.data(), tasks.size() * 4, cudaMemcpyHostToDevice, s));
             CAC_CUDA_TRY(cudaFuncSetAttribute(quotient_kernel<kQT>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                               (int)qsm));
-            quotient_kernel<kQT><<<(unsigned)out_rows, kQT, qsm, s>>>(
+            quotient_kernel<kQT><<<(unsigned)groups, kQT, qsm, s>>>(
                 d_task.as<TaskDesc>(), d_src.as<SrcDesc>(), d_kout.as<uint32_t>(), d_rto.as<uint64_t>(),
-                (uint32_t)tasks.size(), d_qoff.as<uint64_t>(), next->as<uint64_t>());
+                (uint32_t)tasks.size(), qrows, d_qoff.as<uint64_t>(), next->as<uint64_t>());
             CAC_CUDA_TRY(cudaGetLastError());
         }
         CAC_CUDA_TRY(cudaStreamSynchronize(s));
