@@ -431,28 +431,59 @@ __global__ void __launch_bounds__(NT) quotient_kernel(const TaskDesc *__restrict
     }
 }
 
-// Stoer-Wagner on one leaf (n <= 128) by one warp: lane l owns vertices l, l+32, l+64, l+96.
-// Maximum-adjacency order by warp argmax of (key << 8 | 255 - vertex): the largest key wins,
-// ties go to the smallest vertex; keys stay below 2^56 (total graph weight checked on the host).
-// Any maximum-adjacency order gives the exact cut, so the tie rule only fixes determinism.
-// The full matrix sits in shared memory so that a row read is conflict-free.
+// Exact minimum cut of one leaf (n <= 128) by one warp: maximum-adjacency orderings as in the
+// reference's Stoer-Wagner base case (co_mincut_base_case.hpp:52-144), with the Nagamochi-Ono-
+// Ibaraki contraction rule (Nagamochi & Ibaraki 1992; Nagamochi, Ono & Ibaraki 1994): when vertex
+// w's key reaches q >= lambda while vertex v is scanned, then lambda(v, w) >= q, so the edge (v, w)
+// can be contracted without losing any cut below lambda, the best cut value found so far (initially
+// the leaf's minimum weighted degree). Every ordering contracts all such certified edges plus the
+// last two vertices (the cut of the phase updates lambda), so far fewer orderings are needed than
+// the n - 1 of plain Stoer-Wagner; the returned value is the exact minimum cut of the leaf.
+//   lane l owns vertices l, l+32, l+64, l+96; argmax by warp reduction of (key << 8 | 255 - v),
+//   ties to the smallest vertex; keys stay below 2^56 (total graph weight checked on the host).
+//   The full matrix sits in shared memory so that a row read is conflict-free; contractions use a
+//   small union-find over vertex slots in shared memory.
+__device__ __forceinline__ uint64_t warp_min_u64(uint64_t x) {
+    const uint32_t hi = (uint32_t)(x >> 32);
+    const uint32_t top = __reduce_min_sync(0xffffffffu, hi);
+    const uint32_t lo = __reduce_min_sync(0xffffffffu, hi == top ? (uint32_t)x : 0xFFFFFFFFu);
+    return ((uint64_t)top << 32) | lo;
+}
+
 template <typename Tm>
 __global__ void __launch_bounds__(32) sw_leaf_kernel(const LeafDesc *__restrict__ leaves, uint64_t *cuts) {
     extern __shared__ __align__(16) unsigned char dsm[];
     Tm *M = reinterpret_cast<Tm *>(dsm);
+    __shared__ uint8_t uf[128];
+    __shared__ uint32_t pairs[128];
+    __shared__ uint32_t npairs;
     const LeafDesc L = leaves[blockIdx.x];
     const uint32_t N = L.N;
     const int lane = threadIdx.x;
     for (uint32_t x = lane; x < N * N; x += 32) M[x] = (Tm)L.mat[x];
+    for (uint32_t x = lane; x < 128; x += 32) uf[x] = (uint8_t)x;
     __syncwarp();
     uint32_t active = 0;
 #pragma unroll
     for (int s = 0; s < 4; s++)
         if ((uint32_t)(lane + 32 * s) < N) active |= 1u << s;
-    uint64_t best = kU64Max;
-    for (uint32_t cnt = N; cnt > 1; cnt--) {
+    // lambda starts at the minimum weighted degree (a cut of the leaf)
+    uint64_t deg_min = kU64Max;
+#pragma unroll
+    for (int s = 0; s < 4; s++) {
+        if ((active >> s) & 1u) {
+            const Tm *row = M + (size_t)(lane + 32 * s) * N;
+            uint64_t d = 0;
+            for (uint32_t x = 0; x < N; x++) d += (uint64_t)row[x];
+            deg_min = d < deg_min ? d : deg_min;
+        }
+    }
+    uint64_t lambda = warp_min_u64(deg_min);
+    uint32_t cnt = N;
+    while (cnt > 1) {
         uint64_t key[4] = {0, 0, 0, 0};
         uint32_t in_a = 0;
+        uint32_t mark[4] = {0xFFu, 0xFFu, 0xFFu, 0xFFu};  // vertex to contract into, 0xFF: none
         uint32_t prev = 0, last = 0;
         uint64_t cut_phase = 0;
         for (uint32_t step = 0; step < cnt; step++) {
@@ -464,8 +495,6 @@ __global__ void __launch_bounds__(32) sw_leaf_kernel(const LeafDesc *__restrict_
                     local = cand > local ? cand : local;
                 }
             }
-            // warp argmax of the packed keys: max of the high words, then of the low words among
-            // the lanes holding that high word (two redux.sync reductions)
             const uint32_t hi = (uint32_t)(local >> 32);
             const uint32_t top = __reduce_max_sync(0xffffffffu, hi);
             const uint32_t lo = __reduce_max_sync(0xffffffffu, hi == top ? (uint32_t)local : 0u);
@@ -480,26 +509,59 @@ __global__ void __launch_bounds__(32) sw_leaf_kernel(const LeafDesc *__restrict_
             prev = sv;
             const Tm *row = M + (size_t)sv * N;
 #pragma unroll
-            for (int s = 0; s < 4; s++)
-                if (((active & ~in_a) >> s) & 1u) key[s] += (uint64_t)row[lane + 32 * s];
-        }
-        best = cut_phase < best ? cut_phase : best;
-        // merge `last` into `prev` (rows and columns)
-        Tm *rp = M + (size_t)prev * N;
-        const Tm *rl = M + (size_t)last * N;
-#pragma unroll
-        for (int s = 0; s < 4; s++) {
-            const uint32_t v = lane + 32 * s;
-            if (((active >> s) & 1u) && v != prev && v != last) {
-                const Tm x = rp[v] + rl[v];
-                rp[v] = x;
-                M[(size_t)v * N + prev] = x;
+            for (int s = 0; s < 4; s++) {
+                if (((active & ~in_a) >> s) & 1u) {
+                    const uint64_t c = (uint64_t)row[lane + 32 * s];
+                    if (c) {
+                        key[s] += c;
+                        if (key[s] >= lambda) mark[s] = sv;  // lambda(sv, v) >= key: contractible
+                    }
+                }
             }
         }
-        if ((uint32_t)lane == (last & 31u)) active &= ~(1u << (last >> 5));
+        lambda = cut_phase < lambda ? cut_phase : lambda;
+        // contraction list: (prev, last), then every certified edge (v, mark[v])
+        if (lane == 0) {
+            pairs[0] = (prev << 8) | last;
+            npairs = 1;
+        }
         __syncwarp();
+#pragma unroll
+        for (int s = 0; s < 4; s++) {
+            const bool has = ((active >> s) & 1u) && mark[s] != 0xFFu;
+            const uint32_t bal = __ballot_sync(0xffffffffu, has);
+            const uint32_t base = npairs;
+            if (has) pairs[base + __popc(bal & ((1u << lane) - 1u))] = (mark[s] << 8) | (uint32_t)(lane + 32 * s);
+            __syncwarp();
+            if (lane == 0) npairs = base + __popc(bal);
+            __syncwarp();
+        }
+        const uint32_t np = npairs;
+        for (uint32_t q = 0; q < np && cnt > 1; q++) {
+            uint32_t x = pairs[q] >> 8, y = pairs[q] & 255u;
+            while (uf[x] != x) x = uf[x];
+            while (uf[y] != y) y = uf[y];
+            if (x == y) continue;  // already merged (warp-uniform)
+            // merge y into x: entry (x, v) += entry (y, v) for every other active v, both halves
+            Tm *rx = M + (size_t)x * N;
+            const Tm *ry = M + (size_t)y * N;
+#pragma unroll
+            for (int s = 0; s < 4; s++) {
+                const uint32_t v = lane + 32 * s;
+                if (((active >> s) & 1u) && v != x && v != y) {
+                    const Tm val = rx[v] + ry[v];
+                    rx[v] = val;
+                    M[(size_t)v * N + x] = val;
+                }
+            }
+            if ((uint32_t)lane == (y & 31u)) active &= ~(1u << (y >> 5));
+            __syncwarp();
+            if (lane == 0) uf[y] = (uint8_t)x;
+            __syncwarp();
+            cnt--;
+        }
     }
-    if (lane == 0) atomicMin((unsigned long long *)&cuts[L.trial], (unsigned long long)best);
+    if (lane == 0) atomicMin((unsigned long long *)&cuts[L.trial], (unsigned long long)lambda);
 }
 
 __global__ void fill_u64(uint64_t *p, uint64_t n, uint64_t value) {
