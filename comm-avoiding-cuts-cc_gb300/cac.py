@@ -45,10 +45,33 @@ class MincutResult(ctypes.Structure):
                 ("device_ms", ctypes.c_float)]
 
 
+class MincutQuery(ctypes.Structure):
+    _fields_ = [("graph", ctypes.c_void_p), ("success_probability", ctypes.c_double), ("seed", ctypes.c_uint32),
+                ("virtual_ranks", ctypes.c_uint32)]
+
+
 class ApproxResult(ctypes.Structure):
     _fields_ = [("cut", ctypes.c_uint64), ("trials", ctypes.c_uint32), ("copies", ctypes.c_uint32),
                 ("level", ctypes.c_uint32), ("device_ms", ctypes.c_float)]
 
+
+class _ServerConfig(ctypes.Structure):
+    _fields_ = [("device", ctypes.c_int), ("hbm_budget_bytes", ctypes.c_uint64)]
+
+
+class Request(ctypes.Structure):
+    _fields_ = [("kind", ctypes.c_int), ("graph", ctypes.c_void_p), ("success_probability", ctypes.c_double),
+                ("seed", ctypes.c_uint32), ("virtual_ranks", ctypes.c_uint32), ("labels_host", ctypes.c_void_p)]
+
+
+class Response(ctypes.Structure):
+    _fields_ = [("status", ctypes.c_int), ("cut", ctypes.c_uint64), ("trials", ctypes.c_uint32),
+                ("num_components", ctypes.c_uint32), ("queue_ms", ctypes.c_double), ("service_ms", ctypes.c_double),
+                ("message", ctypes.c_char * 160)]
+
+
+QUERY_MINCUT, QUERY_APPROX, QUERY_CC = 1, 2, 3
+PENDING = 1
 
 _u32p = ctypes.POINTER(ctypes.c_uint32)
 _u64p = ctypes.POINTER(ctypes.c_uint64)
@@ -76,6 +99,7 @@ EXPORTS = [
     ("cac_cc_noalloc", ctypes.c_int, [ctypes.c_uint32, ctypes.c_uint64, _vp, _vp, _vp, _vp, _vp]),
     ("cac_mincut", ctypes.c_int, [_vp, _vp, ctypes.c_double, ctypes.c_uint32, ctypes.c_uint32,
                                   ctypes.POINTER(MincutResult)]),
+    ("cac_mincut_batch", ctypes.c_int, [_vp, _vp, ctypes.c_uint32, _vp]),
     ("cac_mincut_trials", ctypes.c_int, [_vp, _vp, ctypes.c_uint32, ctypes.c_uint32, ctypes.c_uint32, _vp]),
     ("cac_ks_dense", ctypes.c_int, [_vp, ctypes.c_uint32, _vp, ctypes.c_uint32, ctypes.c_uint32, ctypes.c_uint32,
                                     _u64p]),
@@ -83,6 +107,11 @@ EXPORTS = [
     ("cac_approx_cut", ctypes.c_int, [_vp, _vp, ctypes.c_double, ctypes.c_uint32, ctypes.c_uint32,
                                       ctypes.POINTER(ApproxResult)]),
     ("cac_sitmo_blocks", ctypes.c_int, [_vp, _u64p, _u64p, ctypes.c_uint64, _vp]),
+    ("cac_server_create", ctypes.c_int, [ctypes.POINTER(_ServerConfig), ctypes.POINTER(_vp)]),
+    ("cac_server_graph", ctypes.c_int, [_vp, ctypes.c_uint32, ctypes.c_uint64, _vp, _vp, _vp, ctypes.POINTER(_vp)]),
+    ("cac_server_submit", ctypes.c_int, [_vp, ctypes.POINTER(Request), _u64p]),
+    ("cac_server_poll", ctypes.c_int, [_vp, ctypes.c_uint64, ctypes.c_int, ctypes.POINTER(Response)]),
+    ("cac_server_destroy", ctypes.c_int, [_vp]),
 ]
 
 
@@ -196,6 +225,17 @@ class Context:
                                   ctypes.byref(out)), "cac_ks_dense")
         return int(out.value)
 
+    def mincut_batch(self, graphs, success_probability=0.95, seeds=None, virtual_ranks=1):
+        """square_root on many graphs in one batch -> list of MincutResult (same values as one by one)."""
+        k = len(graphs)
+        qs = (MincutQuery * max(k, 1))()
+        for i, g in enumerate(graphs):
+            qs[i] = MincutQuery(g.h, success_probability, 0 if seeds is None else seeds[i], virtual_ranks)
+        res = (MincutResult * max(k, 1))()
+        _check(lib().cac_mincut_batch(self.h, ctypes.cast(qs, ctypes.c_void_p), k, ctypes.cast(res, ctypes.c_void_p)),
+               "cac_mincut_batch")
+        return [res[i] for i in range(k)]
+
     def exact_cut_small(self, mat):
         m = np.ascontiguousarray(mat, dtype=np.uint64)
         out = ctypes.c_uint64()
@@ -205,8 +245,9 @@ class Context:
 
 
 class Graph:
-    def __init__(self, ctx, h, keepalive):
-        self.ctx = ctx
+    def __init__(self, ctx, h, keepalive, queries=True):
+        self.ctx = ctx if queries else None
+        self._owner = ctx
         self.h = h
         self._keep = keepalive
         n, m, w = ctypes.c_uint32(), ctypes.c_uint64(), ctypes.c_uint64()
@@ -214,7 +255,7 @@ class Graph:
         self.n, self.m, self.total_weight = int(n.value), int(m.value), int(w.value)
 
     def free(self):
-        if self.h and self.ctx.h:
+        if self.h and self._owner.h:
             lib().cac_graph_free(self.h)
         self.h = None
 
@@ -263,6 +304,74 @@ class Graph:
         _check(lib().cac_approx_cut(self.ctx.h, self.h, success_probability, seed, virtual_ranks, ctypes.byref(res)),
                "cac_approx_cut")
         return res
+
+
+class Server:
+    """Serving loop (cac_server): graphs stay resident; square_root, approx_cut and parallel_cc
+    queries are submitted as they arrive and answered with the values of the single-query calls."""
+
+    def __init__(self, device=0, hbm_budget_bytes=0):
+        h = _vp()
+        _check(lib().cac_server_create(ctypes.byref(_ServerConfig(device, hbm_budget_bytes)), ctypes.byref(h)),
+               "cac_server_create")
+        self.h = h
+        self._graphs = weakref.WeakSet()
+        self._labels = {}
+
+    def graph(self, n, u, v, w=None):
+        u = np.ascontiguousarray(u, dtype=np.uint32)
+        v = np.ascontiguousarray(v, dtype=np.uint32)
+        w = None if w is None else np.ascontiguousarray(w, dtype=np.uint32)
+        h = _vp()
+        _check(lib().cac_server_graph(self.h, n, len(u), ctypes.c_void_p(u.ctypes.data), ctypes.c_void_p(v.ctypes.data),
+                                      None if w is None else ctypes.c_void_p(w.ctypes.data), ctypes.byref(h)),
+               "cac_server_graph")
+        g = Graph(self, h, None, queries=False)
+        self._graphs.add(g)
+        return g
+
+    def submit(self, kind, graph, success_probability=0.0, seed=0, virtual_ranks=1, labels=False):
+        """-> ticket. kind: "square_root", "approx_cut" or "parallel_cc"."""
+        k = {"square_root": QUERY_MINCUT, "approx_cut": QUERY_APPROX, "parallel_cc": QUERY_CC}[kind]
+        out = np.zeros(max(graph.n, 1), np.uint32) if (labels and k == QUERY_CC) else None
+        req = Request(k, graph.h, success_probability, seed, virtual_ranks,
+                      None if out is None else ctypes.c_void_p(out.ctypes.data))
+        t = ctypes.c_uint64()
+        _check(lib().cac_server_submit(self.h, ctypes.byref(req), ctypes.byref(t)), "cac_server_submit")
+        if out is not None:
+            self._labels[int(t.value)] = out[: graph.n]
+        return int(t.value)
+
+    def poll(self, ticket, wait=True):
+        """-> (Response, labels or None), or None while pending (wait=False). A failed query raises."""
+        r = Response()
+        st = lib().cac_server_poll(self.h, ticket, 1 if wait else 0, ctypes.byref(r))
+        if st == PENDING:
+            return None
+        _check(st, "cac_server_poll")
+        labels = self._labels.pop(ticket, None)
+        if r.status != 0:
+            raise CacError(r.status, "server query %d" % ticket, r.message.decode(errors="replace"))
+        return r, labels
+
+    def close(self):
+        if self.h:
+            lib().cac_server_destroy(self.h)  # frees the server's graphs too
+            for g in list(self._graphs):
+                g.h = None
+            self.h = None
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
 
 
 def parse_file(path):

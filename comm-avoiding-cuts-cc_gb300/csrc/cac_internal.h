@@ -64,6 +64,7 @@ struct cac_ctx {
     cac::Arena io;     // staging for host-buffer entry points
     cudaEvent_t ev[8] = {};  // phase timing events
     std::set<cac_graph *> graphs;    // live graphs, released by cac_ctx_destroy
+    cudaMemPool_t pool = nullptr;    // stream-ordered pool of the Karger-Stein level buffers (keeps its memory)
     cac::CCGraphKey cc_key;          // last connected-components query
     cudaGraphExec_t cc_exec = nullptr;  // its captured launch sequence (second sighting onwards)
     uint32_t *pinned_u32 = nullptr;  // 64 KB pinned staging: [0,256) B scalar results, then descriptors
@@ -106,6 +107,71 @@ size_t cc_scratch_bytes(uint32_t n, uint32_t ranks, uint64_t m);
 void cc_graph_reset(cac_ctx *ctx);
 
 // ---- min cut (mincut.cu) ----
+// Stream-ordered, reference-counted device buffer holding the matrices made by one admission or
+// one Karger-Stein step; freed when the last node or task reading it has been consumed.
+struct MatBuf {
+    void *p;
+    size_t bytes;
+    int refs;
+};
+
+// A Karger-Stein recursion node of one trial: its matrix and where its trial's cut goes.
+struct KNode {
+    uint64_t *cut;     // the trial's cut (device)
+    uint32_t k0, idx;  // stream key words 0, 1 (seed + virtual rank, trial index within the rank)
+    uint64_t h;        // heap index (root 1, children 2h, 2h + 1)
+    uint32_t N;
+    uint32_t is_root;  // roots also deliver the minimum weighted degree bound
+    uint32_t small;    // entries fit in 32 bits (total graph weight < 2^32)
+    uint32_t query;    // owner query (engine bookkeeping)
+    const uint64_t *mat;
+    MatBuf *buf;
+};
+
+// A child being contracted from `src` (round > 0: continuing on the quotient of earlier rounds).
+struct KTask {
+    KNode src;
+    uint64_t h;
+    uint32_t round;
+    uint32_t target;
+    uint32_t src_index;
+};
+
+// Level-synchronous Karger-Stein over any set of trials of any graphs: every step solves the
+// leaves, and contracts and builds the children of every other node, in a few launches. Nodes
+// can be added between steps (continuous batching of queries).
+class KsEngine {
+  public:
+    explicit KsEngine(cac_ctx *ctx);
+    ~KsEngine();
+    KsEngine(const KsEngine &) = delete;
+    KsEngine &operator=(const KsEngine &) = delete;
+    int alloc(size_t bytes, MatBuf **out);  // refs start at 0
+    void release(MatBuf *b);                // drops one reference
+    void add(const KNode &nd);              // takes one reference on nd.buf
+    bool idle() const { return nodes_.empty() && carried_.empty(); }
+    int step();
+    int init_err();
+    int read_err(uint32_t *err);
+    std::vector<int64_t> outstanding;  // live nodes and tasks per query
+
+  private:
+    cac_ctx *ctx_;
+    std::vector<KNode> nodes_;
+    std::vector<KTask> carried_;
+    void *d_src_, *d_task_, *d_leaf_, *d_rowoff_, *d_kout_, *d_prep_, *d_tscratch_, *d_qoff_, *d_gto_, *d_err_;
+};
+
+struct MincutQuery {
+    const cac_graph *g;
+    uint32_t seed, ranks, per_rank;
+    uint64_t *d_cuts;  // ranks * per_rank trial cuts (device)
+};
+// Stage 1 and Stage 2 of one query into a running engine: its trial cuts start at 2^64 - 1 and
+// its root nodes carry engine query id `query`; the query is done when outstanding[query] is 0.
+int mincut_admit_query(cac_ctx *ctx, KsEngine &eng, const MincutQuery &q, uint32_t query);
+// All trials of all queries through one engine, admitted as memory allows.
+int mincut_run_queries(cac_ctx *ctx, std::vector<MincutQuery> &queries, float *device_ms);
 int mincut_trials(cac_ctx *ctx, const cac_graph *g, uint32_t seed, uint32_t ranks, uint32_t per_rank,
                   uint64_t *d_cuts, float *device_ms);
 int ks_dense_one(cac_ctx *ctx, uint32_t n, const uint64_t *mat_host, uint32_t seed, uint32_t rank, uint32_t trial,

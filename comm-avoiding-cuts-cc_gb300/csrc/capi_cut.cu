@@ -3,6 +3,7 @@
 
 #include <algorithm>
 #include <cmath>
+#include <string>
 #include <vector>
 
 using namespace cac;
@@ -69,6 +70,65 @@ int cac_mincut(cac_ctx *ctx, const cac_graph *g, double p, uint32_t seed, uint32
     }
     res->device_ms = ms;
     dev_free(ctx, d, n_tr * 8);
+    return st;
+}
+
+int cac_mincut_batch(cac_ctx *ctx, const cac_mincut_query *queries, uint32_t count, cac_mincut_result *results) {
+    if (!ctx || (count && (!queries || !results))) {
+        set_error("cac_mincut_batch: invalid argument");
+        return CAC_ERR_INVALID;
+    }
+    CAC_CUDA_TRY(cudaSetDevice(ctx->device));
+    std::vector<MincutQuery> qs(count);
+    uint64_t total = 0;
+    for (uint32_t i = 0; i < count; i++) {
+        const cac_mincut_query &q = queries[i];
+        if (!q.graph || !(q.success_probability >= 0.0 && q.success_probability < 1.0)) {
+            set_error("cac_mincut_batch: query " + std::to_string(i) + " is invalid");
+            return CAC_ERR_INVALID;
+        }
+        if (q.graph->n < 2) {
+            set_error("cac_mincut_batch: query " + std::to_string(i) + " has fewer than two vertices");
+            return CAC_ERR_INVALID;
+        }
+        const uint32_t ranks = q.virtual_ranks ? q.virtual_ranks : 1;
+        const double trials = number_of_trials(q.graph->n, q.graph->m, q.success_probability);
+        const uint32_t per = (uint32_t)std::ceil(trials / ranks);
+        results[i] = cac_mincut_result{};
+        results[i].trials_per_rank = per;
+        results[i].total_trials = per * ranks;
+        results[i].intermediate = intermediate_size(q.graph->n, q.graph->m);
+        results[i].high_concurrency = ranks >= 2u * (uint32_t)trials ? 1u : 0u;
+        qs[i] = MincutQuery{q.graph, q.seed, ranks, per, nullptr};
+        total += (uint64_t)per * ranks;
+    }
+    if (total == 0) return CAC_OK;
+    void *d = nullptr;
+    CAC_TRY(dev_alloc(ctx, &d, total * 8));
+    uint64_t off = 0;
+    for (auto &q : qs) {
+        q.d_cuts = static_cast<uint64_t *>(d) + off;
+        off += (uint64_t)q.ranks * q.per_rank;
+    }
+    float ms = 0;
+    int st = mincut_run_queries(ctx, qs, &ms);
+    if (st == CAC_OK) {
+        std::vector<uint64_t> cuts(total);
+        cudaError_t e = cudaMemcpy(cuts.data(), d, total * 8, cudaMemcpyDeviceToHost);
+        if (e != cudaSuccess) {
+            set_error(cudaGetErrorString(e));
+            st = CAC_ERR_CUDA;
+        } else {
+            off = 0;
+            for (uint32_t i = 0; i < count; i++) {
+                const uint64_t t = (uint64_t)qs[i].ranks * qs[i].per_rank;
+                results[i].cut = t ? *std::min_element(cuts.begin() + off, cuts.begin() + off + t) : 0;
+                results[i].device_ms = ms;
+                off += t;
+            }
+        }
+    }
+    dev_free(ctx, d, total * 8);
     return st;
 }
 

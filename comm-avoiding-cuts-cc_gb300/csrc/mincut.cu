@@ -42,36 +42,53 @@ constexpr int kQT = 256;                      // threads of the quotient CTAs
 constexpr uint32_t kDropped = 0xFFFFFFFFu;    // task whose source matrix has no edges left
 constexpr uint64_t kU64Max = 0xFFFFFFFFFFFFFFFFull;
 
-struct TrialKey {
-    uint32_t k0;   // seed + virtual rank
-    uint32_t idx;  // trial index within the rank
+// Stage 1 of one trial: its graph, its contraction target and its stream key, its scratch.
+struct ShrinkDesc {
+    const uint32_t *U, *V, *W;
+    uint64_t m;
+    uint64_t *pre;     // m: inclusive prefix of the non-loop weights
+    uint32_t *lab;     // n: output labels (rank of the smallest member)
+    uint32_t *k_out;   // output: number of vertices left
+    uint32_t n, target;
+    uint32_t k0, idx;  // stream key words 0, 1: seed + virtual rank, trial index within the rank
+};
+
+// Stage 2 of one trial: scatter its (relabelled) edges into its k x k matrix.
+struct DenseDesc {
+    const uint32_t *U, *V, *W;
+    const uint32_t *lab;  // nullable: identity
+    uint64_t *mat;
+    uint64_t m;
+    uint32_t k, pad;
 };
 
 struct SrcDesc {
     const uint64_t *mat;  // N x N row-major
     uint64_t *rowpre;     // N: inclusive prefix of row sums
     uint64_t *blk;        // N x nb: per row, inclusive prefix of 32-column block sums
+    uint64_t *cut;        // the trial's cut (root matrices deliver the minimum weighted degree bound)
     uint32_t N, nb;
-    uint32_t trial;
-    uint32_t is_root;     // root matrices also deliver the minimum weighted degree bound
+    uint32_t is_root, pad;
 };
 
 struct TaskDesc {
     uint64_t tag;         // stream key word 2 (1 + heap index)
-    uint32_t src;         // index into the SrcDesc array
-    uint32_t target;
-    uint32_t round;
-    uint32_t trial;       // trial slot (index into cuts)
-    uint32_t k0, idx;     // stream key words 0, 1
+    uint64_t *cut;        // the trial's cut
     uint32_t *lab;        // N labels (output)
     uint32_t *memb_off;   // k + 1 offsets (output)
     uint32_t *members;    // N vertices grouped by label (output)
+    uint32_t src;         // index into the SrcDesc array
+    uint32_t target;
+    uint32_t round;
+    uint32_t k0, idx;     // stream key words 0, 1
+    uint32_t pad;
 };
 
 struct LeafDesc {
     const uint64_t *mat;
+    uint64_t *cut;
     uint32_t N;
-    uint32_t trial;
+    uint32_t small;  // entries fit in 32 bits
 };
 
 // ---------------------------------------------------------------- block helpers
@@ -160,20 +177,18 @@ __device__ void rank_labels(const uint32_t *par, uint32_t n, uint32_t *lab) {
 // ---------------------------------------------------------------- stage 1
 
 template <int NT>
-__global__ void __launch_bounds__(NT) iss_shrink_kernel(uint32_t n, uint64_t m, const uint32_t *__restrict__ U,
-                                                         const uint32_t *__restrict__ V,
-                                                         const uint32_t *__restrict__ Wt, uint32_t target,
-                                                         const TrialKey *__restrict__ keys,
-                                                         uint64_t *__restrict__ pre_all, uint32_t *__restrict__ lab_all,
-                                                         uint32_t *__restrict__ k_out) {
+__global__ void __launch_bounds__(NT) iss_shrink_kernel(const ShrinkDesc *__restrict__ descs) {
     extern __shared__ __align__(16) unsigned char dsm[];
     uint2 *sb = reinterpret_cast<uint2 *>(dsm);
     uint32_t *par = reinterpret_cast<uint32_t *>(dsm + kBatch * sizeof(uint2));
     __shared__ uint32_t s_count;
-    const uint32_t t = blockIdx.x;
-    const TrialKey key = keys[t];
-    uint64_t *pre = pre_all + (size_t)t * m;
-    uint32_t *lab = lab_all + (size_t)t * n;
+    const ShrinkDesc D = descs[blockIdx.x];
+    const uint32_t n = D.n, target = D.target;
+    const uint64_t m = D.m;
+    const uint32_t *__restrict__ U = D.U;
+    const uint32_t *__restrict__ V = D.V;
+    const uint32_t *__restrict__ Wt = D.W;
+    uint64_t *pre = D.pre;
     for (uint32_t v = threadIdx.x; v < n; v += NT) par[v] = v;
     if (threadIdx.x == 0) s_count = n;
     __syncthreads();
@@ -196,7 +211,7 @@ __global__ void __launch_bounds__(NT) iss_shrink_kernel(uint32_t n, uint64_t m, 
         for (uint32_t base = 0; base < c_start; base += kBatch) {
             const uint32_t nb = min((uint32_t)kBatch, c_start - base);
             for (uint32_t j = threadIdx.x; j < nb; j += NT) {
-                const uint64_t y = mulhi64(draw64(key.k0, key.idx, 1, 0, rnd, base + j), W);
+                const uint64_t y = mulhi64(draw64(D.k0, D.idx, 1, 0, rnd, base + j), W);
                 const uint64_t e = upper_bound_u64(pre, m, y);
                 sb[j] = make_uint2(U[e], V[e]);
             }
@@ -218,30 +233,25 @@ __global__ void __launch_bounds__(NT) iss_shrink_kernel(uint32_t n, uint64_t m, 
         for (uint32_t v = threadIdx.x; v < n; v += NT) par[v] = sfind_ro(par, v);
         __syncthreads();
     }
-    rank_labels<NT>(par, n, lab);
-    if (threadIdx.x == 0) k_out[t] = s_count;
+    rank_labels<NT>(par, n, D.lab);
+    if (threadIdx.x == 0) *D.k_out = s_count;
 }
 
 // ---------------------------------------------------------------- stage 2
 
-__global__ void dense_build_kernel(uint64_t m, const uint32_t *__restrict__ U, const uint32_t *__restrict__ V,
-                                   const uint32_t *__restrict__ Wt, const uint32_t *__restrict__ lab_all, uint32_t n,
-                                   const uint32_t *__restrict__ kdim, const uint64_t *__restrict__ mat_off,
-                                   uint64_t *mats) {
-    const uint32_t t = blockIdx.y;
-    const uint64_t k = kdim[t];
-    uint64_t *M = mats + mat_off[t];
-    const uint32_t *lab = lab_all ? lab_all + (size_t)t * n : nullptr;
-    for (uint64_t e = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; e < m; e += (uint64_t)gridDim.x * blockDim.x) {
-        uint32_t a = U[e], b = V[e];
-        if (lab) {
-            a = lab[a];
-            b = lab[b];
+__global__ void dense_build_kernel(const DenseDesc *__restrict__ descs) {
+    const DenseDesc D = descs[blockIdx.y];
+    const uint64_t k = D.k;
+    for (uint64_t e = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; e < D.m; e += (uint64_t)gridDim.x * blockDim.x) {
+        uint32_t a = D.U[e], b = D.V[e];
+        if (D.lab) {
+            a = D.lab[a];
+            b = D.lab[b];
         }
         if (a == b) continue;
-        const unsigned long long w = Wt[e];
-        atomicAdd((unsigned long long *)&M[(uint64_t)a * k + b], w);
-        atomicAdd((unsigned long long *)&M[(uint64_t)b * k + a], w);
+        const unsigned long long w = D.W[e];
+        atomicAdd((unsigned long long *)&D.mat[(uint64_t)a * k + b], w);
+        atomicAdd((unsigned long long *)&D.mat[(uint64_t)b * k + a], w);
     }
 }
 
@@ -249,7 +259,7 @@ __global__ void dense_build_kernel(uint64_t m, const uint32_t *__restrict__ U, c
 
 // One warp per matrix row: 32-column block prefixes and the row sum.
 __global__ void prep_rows_kernel(const SrcDesc *__restrict__ srcs, const uint64_t *__restrict__ row_off,
-                                 uint32_t nsrc, uint64_t total_rows, uint64_t *cuts) {
+                                 uint32_t nsrc, uint64_t total_rows) {
     const uint64_t gw = ((uint64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     const int lane = threadIdx.x & 31;
     if (gw >= total_rows) return;
@@ -272,7 +282,7 @@ __global__ void prep_rows_kernel(const SrcDesc *__restrict__ srcs, const uint64_
     }
     if (lane == 0) {
         S.rowpre[i] = run;
-        if (S.is_root) atomicMin((unsigned long long *)&cuts[S.trial], (unsigned long long)run);
+        if (S.is_root) atomicMin((unsigned long long *)S.cut, (unsigned long long)run);
     }
 }
 
@@ -294,7 +304,7 @@ __global__ void __launch_bounds__(NT) prefix_rows_kernel(const SrcDesc *__restri
 template <int NT>
 __global__ void __launch_bounds__(NT) contract_kernel(const TaskDesc *__restrict__ tasks,
                                                       const SrcDesc *__restrict__ srcs, uint32_t *__restrict__ k_out,
-                                                      uint64_t *cuts, uint32_t *err) {
+                                                      uint32_t *err) {
     extern __shared__ __align__(16) unsigned char dsm[];
     uint2 *sb = reinterpret_cast<uint2 *>(dsm);
     __shared__ uint32_t s_count;
@@ -307,7 +317,7 @@ __global__ void __launch_bounds__(NT) contract_kernel(const TaskDesc *__restrict
     if (W == 0) {  // no edges between the vertices: the cut is 0, nothing to contract
         if (threadIdx.x == 0) {
             k_out[blockIdx.x] = kDropped;
-            atomicMin((unsigned long long *)&cuts[T.trial], 0ull);
+            atomicMin((unsigned long long *)T.cut, 0ull);
         }
         return;
     }
@@ -451,7 +461,7 @@ __device__ __forceinline__ uint64_t warp_min_u64(uint64_t x) {
 }
 
 template <typename Tm>
-__global__ void __launch_bounds__(32) sw_leaf_kernel(const LeafDesc *__restrict__ leaves, uint64_t *cuts) {
+__global__ void __launch_bounds__(32) sw_leaf_kernel(const LeafDesc *__restrict__ leaves) {
     extern __shared__ __align__(16) unsigned char dsm[];
     Tm *M = reinterpret_cast<Tm *>(dsm);
     __shared__ uint8_t uf[128];
@@ -561,7 +571,7 @@ __global__ void __launch_bounds__(32) sw_leaf_kernel(const LeafDesc *__restrict_
             cnt--;
         }
     }
-    if (lane == 0) atomicMin((unsigned long long *)&cuts[L.trial], (unsigned long long)lambda);
+    if (lane == 0) atomicMin((unsigned long long *)L.cut, (unsigned long long)lambda);
 }
 
 __global__ void fill_u64(uint64_t *p, uint64_t n, uint64_t value) {
@@ -603,294 +613,458 @@ int upload(cac_ctx *ctx, DevBuf &buf, const std::vector<T> &v) {
     return CAC_OK;
 }
 
-struct Node {
-    uint32_t trial;  // slot in this wave
-    uint64_t h;      // heap index
-    uint32_t N;
-    uint64_t off;    // element offset of the matrix in the level buffer it lives in
-    uint32_t is_root;
-};
-
-struct PendingTask {
-    uint32_t trial;
-    uint64_t h;       // heap index of the child being built
-    uint32_t round;
-    uint32_t target;
-    uint32_t src;     // index into this iteration's source list
-};
-
-
 size_t contract_smem(uint32_t N) { return kBatch * sizeof(uint2) + (size_t)2 * N * 4; }
-size_t quotient_smem(uint32_t k, uint32_t N) { return (size_t)N * 8; }
+size_t quotient_smem(uint32_t N) { return (size_t)N * 8; }
 
-// Runs Stage 3 for the root matrices of one wave; cuts[] (wave slots) must hold the Stage-1/2
-// bounds (UINT64_MAX before the root nodes' minimum-degree bound is applied).
-int ks_levels(cac_ctx *ctx, std::vector<Node> nodes, DevBuf *cur, DevBuf *next, const std::vector<TrialKey> &keys,
-              uint64_t *d_cuts, bool small_entries, uint32_t *d_err) {
-    cudaStream_t s = ctx->stream;
-    DevBuf d_src(ctx), d_task(ctx), d_leaf(ctx), d_rowoff(ctx), d_kout(ctx), d_prep(ctx), d_tscratch(ctx),
-        d_qoff(ctx), d_rto(ctx);
-    std::vector<PendingTask> carried;      // tasks continuing with another round (sources in `cur`)
-    std::vector<Node> carried_src;         // their source matrices
-    while (!nodes.empty() || !carried.empty()) {
-        // leaves -> Stoer-Wagner
-        std::vector<LeafDesc> leaves;
-        std::vector<Node> inner;
-        for (const Node &nd : nodes) {
-            if (nd.N <= 128) {
-                if (nd.N >= 2) leaves.push_back(LeafDesc{cur->as<uint64_t>() + nd.off, nd.N, nd.trial});
-            } else {
-                inner.push_back(nd);
-            }
-        }
-        if (!leaves.empty()) {
-            // group by size so that each launch uses one dynamic shared-memory size
-            std::sort(leaves.begin(), leaves.end(), [](const LeafDesc &a, const LeafDesc &b) { return a.N > b.N; });
-            CAC_TRY(upload(ctx, d_leaf, leaves));
-            size_t first = 0;
-            while (first < leaves.size()) {
-                size_t last = first;
-                while (last < leaves.size() && leaves[last].N == leaves[first].N) last++;
-                const uint32_t N = leaves[first].N;
-                const LeafDesc *dl = d_leaf.as<LeafDesc>() + first;
-                if (small_entries) {
-                    const size_t sm = (size_t)N * N * 4;
-                    CAC_CUDA_TRY(cudaFuncSetAttribute(sw_leaf_kernel<uint32_t>,
-                                                      cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
-                    sw_leaf_kernel<uint32_t><<<(unsigned)(last - first), 32, sm, s>>>(dl, d_cuts);
-                } else {
-                    const size_t sm = (size_t)N * N * 8;
-                    CAC_CUDA_TRY(cudaFuncSetAttribute(sw_leaf_kernel<uint64_t>,
-                                                      cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
-                    sw_leaf_kernel<uint64_t><<<(unsigned)(last - first), 32, sm, s>>>(dl, d_cuts);
-                }
-                first = last;
-            }
-            CAC_CUDA_TRY(cudaGetLastError());
-        }
-        // sources of this iteration: inner nodes (children 0 and 1) + matrices of carried tasks
-        std::vector<SrcDesc> srcs;
-        std::vector<PendingTask> tasks;
-        std::vector<uint64_t> row_off;
-        uint64_t rows = 0, prep_elems = 0;
-        std::vector<const Node *> src_nodes;
-        for (const Node &nd : inner) src_nodes.push_back(&nd);
-        for (const Node &nd : carried_src) src_nodes.push_back(&nd);
-        for (size_t i = 0; i < src_nodes.size(); i++) {
-            const Node &nd = *src_nodes[i];
-            const uint32_t nb = (nd.N + 31) / 32;
-            prep_elems += nd.N + (uint64_t)nd.N * nb;
-        }
-        if (src_nodes.empty()) break;
-        CAC_TRY(d_prep.ensure(prep_elems * 8));
-        uint64_t pe = 0, tscratch = 0;
-        for (size_t i = 0; i < src_nodes.size(); i++) {
-            const Node &nd = *src_nodes[i];
-            SrcDesc S;
-            S.mat = cur->as<uint64_t>() + nd.off;
-            S.N = nd.N;
-            S.nb = (nd.N + 31) / 32;
-            S.rowpre = d_prep.as<uint64_t>() + pe;
-            S.blk = S.rowpre + nd.N;
-            pe += nd.N + (uint64_t)nd.N * S.nb;
-            S.trial = nd.trial;
-            S.is_root = nd.is_root;
-            srcs.push_back(S);
-            row_off.push_back(rows);
-            rows += nd.N;
-        }
-        for (size_t i = 0; i < inner.size(); i++) {
-            const uint32_t target = (uint32_t)ks_target((int)inner[i].N);
-            for (uint64_t c = 0; c < 2; c++)
-                tasks.push_back(PendingTask{inner[i].trial, 2 * inner[i].h + c, 0, target, (uint32_t)i});
-        }
-        for (size_t i = 0; i < carried.size(); i++) {
-            PendingTask t = carried[i];
-            t.src = (uint32_t)(inner.size() + i);
-            tasks.push_back(t);
-        }
-        for (const PendingTask &t : tasks) tscratch += 2 * (uint64_t)srcs[t.src].N + srcs[t.src].N + 1;
-        CAC_TRY(upload(ctx, d_src, srcs));
-        CAC_TRY(upload(ctx, d_rowoff, row_off));
-        {
-            const uint64_t threads = rows * 32;
-            const unsigned grid = (unsigned)((threads + 255) / 256);
-            prep_rows_kernel<<<grid, 256, 0, s>>>(d_src.as<SrcDesc>(), d_rowoff.as<uint64_t>(),
-                                                  (uint32_t)srcs.size(), rows, d_cuts);
-            prefix_rows_kernel<kNT><<<(unsigned)srcs.size(), kNT, 0, s>>>(d_src.as<SrcDesc>());
-        }
-        // contraction tasks
-        CAC_TRY(d_tscratch.ensure(tscratch * 4));
-        std::vector<TaskDesc> td(tasks.size());
-        uint64_t ts = 0;
-        uint32_t maxN = 0;
-        for (size_t i = 0; i < tasks.size(); i++) {
-            const PendingTask &t = tasks[i];
-            const uint32_t N = srcs[t.src].N;
-            maxN = std::max(maxN, N);
-            TaskDesc &d = td[i];
-            d.tag = 1 + t.h;
-            d.src = t.src;
-            d.target = t.target;
-            d.round = t.round;
-            d.trial = t.trial;
-            d.k0 = keys[t.trial].k0;
-            d.idx = keys[t.trial].idx;
-            d.lab = d_tscratch.as<uint32_t>() + ts;
-            d.members = d.lab + N;
-            d.memb_off = d.members + N;
-            ts += 2 * (uint64_t)N + N + 1;
-        }
-        CAC_TRY(upload(ctx, d_task, td));
-        CAC_TRY(d_kout.ensure(tasks.size() * 4));
-        {
-            const size_t sm = contract_smem(maxN);
-            CAC_CUDA_TRY(cudaFuncSetAttribute(contract_kernel<kNT>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                              (int)sm));
-            contract_kernel<kNT><<<(unsigned)tasks.size(), kNT, sm, s>>>(d_task.as<TaskDesc>(), d_src.as<SrcDesc>(),
-                                                                         d_kout.as<uint32_t>(), d_cuts, d_err);
-            CAC_CUDA_TRY(cudaGetLastError());
-        }
-        std::vector<uint32_t> kk(tasks.size());
-        CAC_CUDA_TRY(cudaMemcpyAsync(kk.data(), d_kout.p, tasks.size() * 4, cudaMemcpyDeviceToHost, s));
-        CAC_CUDA_TRY(cudaStreamSynchronize(s));
-        // output matrices of this iteration
-        std::vector<uint64_t> out_off(tasks.size(), 0), group_task_off(tasks.size(), 0);
-        std::vector<uint32_t> kq(tasks.size(), 0);
-        uint64_t out_elems = 0, groups = 0;
-        size_t qsm = 0;
-        // rows per quotient CTA: one for wide matrices, up to 16 as rows get short
-        const uint32_t qrows = std::max<uint32_t>(1, std::min<uint32_t>(16, 4096 / std::max<uint32_t>(maxN, 1)));
-        for (size_t i = 0; i < tasks.size(); i++) {
-            const uint32_t k = kk[i] == kDropped ? 0 : kk[i];
-            kq[i] = k;
-            out_off[i] = out_elems;
-            group_task_off[i] = groups;
-            out_elems += (uint64_t)k * k;
-            groups += (k + qrows - 1) / qrows;
-            if (k) qsm = std::max(qsm, quotient_smem(k, srcs[tasks[i].src].N));
-        }
-        CAC_TRY(next->ensure(std::max<uint64_t>(out_elems, 1) * 8));
-        if (groups) {
-            CAC_TRY(upload(ctx, d_qoff, out_off));
-            CAC_TRY(upload(ctx, d_rto, group_task_off));
-            CAC_TRY(d_kout.ensure(tasks.size() * 4));
-            CAC_CUDA_TRY(cudaMemcpyAsync(d_kout.p, kq.data(), tasks.size() * 4, cudaMemcpyHostToDevice, s));
-            CAC_CUDA_TRY(cudaFuncSetAttribute(quotient_kernel<kQT>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                              (int)qsm));
-            quotient_kernel<kQT><<<(unsigned)groups, kQT, qsm, s>>>(
-                d_task.as<TaskDesc>(), d_src.as<SrcDesc>(), d_kout.as<uint32_t>(), d_rto.as<uint64_t>(),
-                (uint32_t)tasks.size(), qrows, d_qoff.as<uint64_t>(), next->as<uint64_t>());
-            CAC_CUDA_TRY(cudaGetLastError());
-        }
-        CAC_CUDA_TRY(cudaStreamSynchronize(s));
-        // next iteration
-        std::vector<Node> next_nodes;
-        std::vector<PendingTask> next_carried;
-        std::vector<Node> next_carried_src;
-        for (size_t i = 0; i < tasks.size(); i++) {
-            const uint32_t k = kq[i];
-            if (k == 0) continue;  // dropped: the source had no edges, its cut 0 is recorded
-            Node nd{tasks[i].trial, tasks[i].h, k, out_off[i], 0};
-            if (k <= tasks[i].target) {
-                next_nodes.push_back(nd);
-            } else {
-                PendingTask t = tasks[i];
-                t.round += 1;
-                next_carried.push_back(t);
-                next_carried_src.push_back(nd);
-            }
-        }
-        std::swap(cur, next);
-        nodes.swap(next_nodes);
-        carried.swap(next_carried);
-        carried_src.swap(next_carried_src);
+}  // namespace
+
+// ---- Karger-Stein engine (declared in cac_internal.h) ----
+
+KsEngine::KsEngine(cac_ctx *ctx)
+    : ctx_(ctx), d_src_(new DevBuf(ctx)), d_task_(new DevBuf(ctx)), d_leaf_(new DevBuf(ctx)),
+      d_rowoff_(new DevBuf(ctx)), d_kout_(new DevBuf(ctx)), d_prep_(new DevBuf(ctx)), d_tscratch_(new DevBuf(ctx)),
+      d_qoff_(new DevBuf(ctx)), d_gto_(new DevBuf(ctx)), d_err_(new DevBuf(ctx)) {}
+
+KsEngine::~KsEngine() {
+    cudaStreamSynchronize(ctx_->stream);
+    for (const KNode &nd : nodes_) release(nd.buf);
+    for (const KTask &t : carried_) release(t.src.buf);
+    nodes_.clear();
+    carried_.clear();
+    for (void *b : {d_src_, d_task_, d_leaf_, d_rowoff_, d_kout_, d_prep_, d_tscratch_, d_qoff_, d_gto_, d_err_})
+        delete static_cast<DevBuf *>(b);
+}
+
+int KsEngine::init_err() {
+    DevBuf *e = static_cast<DevBuf *>(d_err_);
+    CAC_TRY(e->ensure(4));
+    CAC_CUDA_TRY(cudaMemsetAsync(e->p, 0, 4, ctx_->stream));
+    return CAC_OK;
+}
+
+int KsEngine::read_err(uint32_t *err) {
+    DevBuf *e = static_cast<DevBuf *>(d_err_);
+    *err = 0;
+    if (!e->p) return CAC_OK;
+    CAC_CUDA_TRY(cudaMemcpyAsync(err, e->p, 4, cudaMemcpyDeviceToHost, ctx_->stream));
+    CAC_CUDA_TRY(cudaStreamSynchronize(ctx_->stream));
+    return CAC_OK;
+}
+
+int KsEngine::alloc(size_t bytes, MatBuf **out) {
+    *out = nullptr;
+    bytes = std::max<size_t>(bytes, 256);
+    if (ctx_->budget && ctx_->held + bytes > ctx_->budget) {
+        set_error("HBM budget exceeded by a Karger-Stein level buffer of " + std::to_string(bytes) + " bytes");
+        return CAC_ERR_OOM;
     }
+    void *p = nullptr;
+    cudaError_t e = ctx_->pool ? cudaMallocFromPoolAsync(&p, bytes, ctx_->pool, ctx_->stream)
+                               : cudaMallocAsync(&p, bytes, ctx_->stream);
+    if (e != cudaSuccess) {
+        cudaGetLastError();
+        set_error(std::string("cudaMallocAsync: ") + cudaGetErrorString(e));
+        return CAC_ERR_OOM;
+    }
+    ctx_->held += bytes;
+    MatBuf *b = new MatBuf{p, bytes, 0};
+    *out = b;
+    return CAC_OK;
+}
+
+void KsEngine::release(MatBuf *b) {
+    if (!b) return;
+    if (--b->refs > 0) return;
+    cudaFreeAsync(b->p, ctx_->stream);
+    ctx_->held -= std::min<uint64_t>(ctx_->held, b->bytes);
+    delete b;
+}
+
+void KsEngine::add(const KNode &nd) {
+    nd.buf->refs++;
+    nodes_.push_back(nd);
+    if (nd.query >= outstanding.size()) outstanding.resize(nd.query + 1, 0);
+    outstanding[nd.query]++;
+}
+
+int KsEngine::step() {
+    cudaStream_t s = ctx_->stream;
+    DevBuf &d_src = *static_cast<DevBuf *>(d_src_), &d_task = *static_cast<DevBuf *>(d_task_);
+    DevBuf &d_leaf = *static_cast<DevBuf *>(d_leaf_), &d_rowoff = *static_cast<DevBuf *>(d_rowoff_);
+    DevBuf &d_kout = *static_cast<DevBuf *>(d_kout_), &d_prep = *static_cast<DevBuf *>(d_prep_);
+    DevBuf &d_tscratch = *static_cast<DevBuf *>(d_tscratch_), &d_qoff = *static_cast<DevBuf *>(d_qoff_);
+    DevBuf &d_gto = *static_cast<DevBuf *>(d_gto_);
+    uint32_t *d_err = static_cast<DevBuf *>(d_err_)->as<uint32_t>();
+    std::vector<MatBuf *> consumed;
+
+    // leaves (n <= 128) -> exact cut; grouped by size and entry width, one launch each
+    std::vector<LeafDesc> leaves;
+    std::vector<uint8_t> leaf_small;
+    std::vector<KNode> inner;
+    for (const KNode &nd : nodes_) {
+        if (nd.N <= 128) {
+            if (nd.N >= 2) {
+                leaves.push_back(LeafDesc{nd.mat, nd.cut, nd.N, nd.small});
+            }
+            consumed.push_back(nd.buf);
+            outstanding[nd.query]--;
+        } else {
+            inner.push_back(nd);
+        }
+    }
+    nodes_.clear();
+    if (!leaves.empty()) {
+        std::sort(leaves.begin(), leaves.end(),
+                  [](const LeafDesc &a, const LeafDesc &b) { return a.N != b.N ? a.N > b.N : a.small > b.small; });
+        CAC_TRY(upload(ctx_, d_leaf, leaves));
+        size_t first = 0;
+        while (first < leaves.size()) {
+            size_t last = first;
+            while (last < leaves.size() && leaves[last].N == leaves[first].N && leaves[last].small == leaves[first].small)
+                last++;
+            const uint32_t N = leaves[first].N;
+            const LeafDesc *dl = d_leaf.as<LeafDesc>() + first;
+            if (leaves[first].small) {
+                const size_t sm = (size_t)N * N * 4;
+                CAC_CUDA_TRY(cudaFuncSetAttribute(sw_leaf_kernel<uint32_t>,
+                                                  cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
+                sw_leaf_kernel<uint32_t><<<(unsigned)(last - first), 32, sm, s>>>(dl);
+            } else {
+                const size_t sm = (size_t)N * N * 8;
+                CAC_CUDA_TRY(cudaFuncSetAttribute(sw_leaf_kernel<uint64_t>,
+                                                  cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
+                sw_leaf_kernel<uint64_t><<<(unsigned)(last - first), 32, sm, s>>>(dl);
+            }
+            first = last;
+        }
+        CAC_CUDA_TRY(cudaGetLastError());
+    }
+
+    // sources: inner nodes (two children each) and the matrices of tasks continuing another round
+    std::vector<KTask> tasks;
+    std::vector<KNode> src_nodes;
+    for (const KNode &nd : inner) {
+        src_nodes.push_back(nd);
+        const uint32_t target = (uint32_t)ks_target((int)nd.N);
+        for (uint64_t c = 0; c < 2; c++) tasks.push_back(KTask{nd, 2 * nd.h + c, 0, target, (uint32_t)(src_nodes.size() - 1)});
+        outstanding[nd.query]++;  // two tasks replace the node
+        consumed.push_back(nd.buf);
+    }
+    for (KTask t : carried_) {
+        src_nodes.push_back(t.src);
+        t.src_index = (uint32_t)(src_nodes.size() - 1);
+        tasks.push_back(t);
+        consumed.push_back(t.src.buf);
+    }
+    carried_.clear();
+    if (tasks.empty()) {
+        for (MatBuf *b : consumed) release(b);
+        return CAC_OK;
+    }
+    std::vector<SrcDesc> srcs(src_nodes.size());
+    std::vector<uint64_t> row_off(src_nodes.size());
+    uint64_t rows = 0, prep_elems = 0;
+    for (size_t i = 0; i < src_nodes.size(); i++) {
+        const uint32_t nb = (src_nodes[i].N + 31) / 32;
+        prep_elems += src_nodes[i].N + (uint64_t)src_nodes[i].N * nb;
+    }
+    CAC_TRY(d_prep.ensure(prep_elems * 8));
+    uint64_t pe = 0;
+    for (size_t i = 0; i < src_nodes.size(); i++) {
+        const KNode &nd = src_nodes[i];
+        SrcDesc &S = srcs[i];
+        S.mat = nd.mat;
+        S.N = nd.N;
+        S.nb = (nd.N + 31) / 32;
+        S.rowpre = d_prep.as<uint64_t>() + pe;
+        S.blk = S.rowpre + nd.N;
+        S.cut = nd.cut;
+        S.is_root = nd.is_root;
+        S.pad = 0;
+        pe += nd.N + (uint64_t)nd.N * S.nb;
+        row_off[i] = rows;
+        rows += nd.N;
+    }
+    CAC_TRY(upload(ctx_, d_src, srcs));
+    CAC_TRY(upload(ctx_, d_rowoff, row_off));
+    prep_rows_kernel<<<(unsigned)((rows * 32 + 255) / 256), 256, 0, s>>>(d_src.as<SrcDesc>(),
+                                                                         d_rowoff.as<uint64_t>(),
+                                                                         (uint32_t)srcs.size(), rows);
+    prefix_rows_kernel<kNT><<<(unsigned)srcs.size(), kNT, 0, s>>>(d_src.as<SrcDesc>());
+
+    // contraction of every child
+    uint64_t tscratch = 0;
+    uint32_t maxN = 0;
+    for (const KTask &t : tasks) {
+        tscratch += 3 * (uint64_t)t.src.N + 1;
+        maxN = std::max(maxN, t.src.N);
+    }
+    CAC_TRY(d_tscratch.ensure(tscratch * 4));
+    std::vector<TaskDesc> td(tasks.size());
+    uint64_t ts = 0;
+    for (size_t i = 0; i < tasks.size(); i++) {
+        const KTask &t = tasks[i];
+        TaskDesc &d = td[i];
+        d.tag = 1 + t.h;
+        d.cut = t.src.cut;
+        d.src = t.src_index;
+        d.target = t.target;
+        d.round = t.round;
+        d.k0 = t.src.k0;
+        d.idx = t.src.idx;
+        d.pad = 0;
+        d.lab = d_tscratch.as<uint32_t>() + ts;
+        d.members = d.lab + t.src.N;
+        d.memb_off = d.members + t.src.N;
+        ts += 3 * (uint64_t)t.src.N + 1;
+    }
+    CAC_TRY(upload(ctx_, d_task, td));
+    CAC_TRY(d_kout.ensure(tasks.size() * 4));
+    {
+        const size_t sm = contract_smem(maxN);
+        CAC_CUDA_TRY(cudaFuncSetAttribute(contract_kernel<kNT>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
+        contract_kernel<kNT><<<(unsigned)tasks.size(), kNT, sm, s>>>(d_task.as<TaskDesc>(), d_src.as<SrcDesc>(),
+                                                                     d_kout.as<uint32_t>(), d_err);
+        CAC_CUDA_TRY(cudaGetLastError());
+    }
+    std::vector<uint32_t> kk(tasks.size());
+    CAC_CUDA_TRY(cudaMemcpyAsync(kk.data(), d_kout.p, tasks.size() * 4, cudaMemcpyDeviceToHost, s));
     CAC_CUDA_TRY(cudaStreamSynchronize(s));
+
+    // quotient matrices of this step, in one stream-ordered buffer
+    std::vector<uint64_t> out_off(tasks.size(), 0), group_task_off(tasks.size(), 0);
+    std::vector<uint32_t> kq(tasks.size(), 0);
+    uint64_t out_elems = 0, groups = 0;
+    size_t qsm = 0;
+    const uint32_t qrows = std::max<uint32_t>(1, std::min<uint32_t>(16, 4096 / std::max<uint32_t>(maxN, 1)));
+    for (size_t i = 0; i < tasks.size(); i++) {
+        const uint32_t k = kk[i] == kDropped ? 0 : kk[i];
+        kq[i] = k;
+        out_off[i] = out_elems;
+        group_task_off[i] = groups;
+        out_elems += (uint64_t)k * k;
+        groups += (k + qrows - 1) / qrows;
+        if (k) qsm = std::max(qsm, quotient_smem(tasks[i].src.N));
+    }
+    MatBuf *out = nullptr;
+    if (groups) {
+        CAC_TRY(alloc(out_elems * 8, &out));
+        CAC_TRY(upload(ctx_, d_qoff, out_off));
+        CAC_TRY(upload(ctx_, d_gto, group_task_off));
+        CAC_CUDA_TRY(cudaMemcpyAsync(d_kout.p, kq.data(), tasks.size() * 4, cudaMemcpyHostToDevice, s));
+        CAC_CUDA_TRY(cudaFuncSetAttribute(quotient_kernel<kQT>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)qsm));
+        quotient_kernel<kQT><<<(unsigned)groups, kQT, qsm, s>>>(
+            d_task.as<TaskDesc>(), d_src.as<SrcDesc>(), d_kout.as<uint32_t>(), d_gto.as<uint64_t>(),
+            (uint32_t)tasks.size(), qrows, d_qoff.as<uint64_t>(), static_cast<uint64_t *>(out->p));
+        CAC_CUDA_TRY(cudaGetLastError());
+    }
+    // the sources are read by everything enqueued above: their buffers may now be released
+    for (MatBuf *b : consumed) release(b);
+    for (size_t i = 0; i < tasks.size(); i++) {
+        const KTask &t = tasks[i];
+        outstanding[t.src.query]--;
+        const uint32_t k = kq[i];
+        if (k == 0) continue;  // dropped: the source had no edges, its cut 0 is recorded
+        KNode nd = t.src;
+        nd.h = t.h;
+        nd.N = k;
+        nd.is_root = 0;
+        nd.mat = static_cast<uint64_t *>(out->p) + out_off[i];
+        nd.buf = out;
+        out->refs++;
+        outstanding[nd.query]++;
+        if (k <= t.target) {
+            nodes_.push_back(nd);
+        } else {
+            KTask c = t;
+            c.src = nd;
+            c.round += 1;
+            carried_.push_back(c);
+        }
+    }
+    if (out && out->refs == 0) {  // every child was dropped
+        out->refs = 1;
+        release(out);
+    }
+    return CAC_OK;
+}
+
+namespace {
+
+// Admission of square_root queries: trial keys, per-trial cut slots, Stage 1 and Stage 2, root nodes.
+struct QueryPlan {
+    const cac_graph *g;
+    uint32_t seed, ranks, per_rank;
+    uint32_t t;
+    uint64_t trials;
+    uint64_t *cuts;       // device, one per trial
+    uint32_t query;       // engine bookkeeping id
+};
+
+int admit(cac_ctx *ctx, KsEngine &eng, const QueryPlan &q) {
+    cudaStream_t s = ctx->stream;
+    const cac_graph *g = q.g;
+    const uint32_t n = g->n;
+    const uint64_t m = g->m;
+    const uint32_t small = g->total_weight < (1ull << 32) ? 1u : 0u;
+    if (q.trials == 0) return CAC_OK;
+    if (q.t >= n) {
+        // no pre-contraction: every trial starts from the same dense matrix, built once
+        MatBuf *root = nullptr;
+        CAC_TRY(eng.alloc((size_t)n * n * 8, &root));
+        CAC_CUDA_TRY(cudaMemsetAsync(root->p, 0, (size_t)n * n * 8, s));
+        if (m) {
+            DevBuf d(ctx);
+            std::vector<DenseDesc> dd{DenseDesc{g->u, g->v, g->w, nullptr, static_cast<uint64_t *>(root->p), m, n, 0}};
+            CAC_TRY(upload(ctx, d, dd));
+            dim3 grid((unsigned)std::max<uint64_t>(1, std::min<uint64_t>((m + 255) / 256, (uint64_t)ctx->num_sms * 8)), 1);
+            dense_build_kernel<<<grid, 256, 0, s>>>(d.as<DenseDesc>());
+            CAC_CUDA_TRY(cudaGetLastError());
+            CAC_CUDA_TRY(cudaStreamSynchronize(s));  // the descriptor buffer goes out of scope
+        }
+        root->refs++;  // held until every root node has been added
+        for (uint64_t i = 0; i < q.trials; i++) {
+            const uint32_t r = (uint32_t)(i / q.per_rank), idx = (uint32_t)(i % q.per_rank);
+            eng.add(KNode{q.cuts + i, q.seed + r, idx, 1, n, 1, small, q.query, static_cast<uint64_t *>(root->p), root});
+        }
+        eng.release(root);
+        return CAC_OK;
+    }
+    if (n > kMaxSmemVertices) {
+        set_error("graphs with more than 16384 vertices that need sparse pre-contraction are not supported yet");
+        return CAC_ERR_UNSUPPORTED;
+    }
+    // Stage 1 in chunks whose scratch (prefix array + labels per trial) stays within 4 GB
+    const uint64_t per_trial = 8 * std::max<uint64_t>(m, 1) + 4 * (uint64_t)n + 64;
+    const uint64_t chunk = std::max<uint64_t>(1, std::min<uint64_t>({q.trials, (4ull << 30) / per_trial, (uint64_t)65535}));
+    DevBuf d_pre(ctx), d_lab(ctx), d_k(ctx), d_sd(ctx), d_dd(ctx);
+    const size_t sm = kBatch * sizeof(uint2) + (size_t)n * 4;
+    CAC_CUDA_TRY(cudaFuncSetAttribute(iss_shrink_kernel<kNT>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
+    for (uint64_t c0 = 0; c0 < q.trials; c0 += chunk) {
+        const uint32_t B = (uint32_t)std::min<uint64_t>(chunk, q.trials - c0);
+        CAC_TRY(d_pre.ensure((size_t)B * std::max<uint64_t>(m, 1) * 8));
+        CAC_TRY(d_lab.ensure((size_t)B * n * 4));
+        CAC_TRY(d_k.ensure((size_t)B * 4));
+        std::vector<ShrinkDesc> sd(B);
+        for (uint32_t b = 0; b < B; b++) {
+            const uint64_t i = c0 + b;
+            ShrinkDesc &D = sd[b];
+            D.U = g->u;
+            D.V = g->v;
+            D.W = g->w;
+            D.m = m;
+            D.pre = d_pre.as<uint64_t>() + (size_t)b * std::max<uint64_t>(m, 1);
+            D.lab = d_lab.as<uint32_t>() + (size_t)b * n;
+            D.k_out = d_k.as<uint32_t>() + b;
+            D.n = n;
+            D.target = q.t;
+            D.k0 = q.seed + (uint32_t)(i / q.per_rank);
+            D.idx = (uint32_t)(i % q.per_rank);
+        }
+        CAC_TRY(upload(ctx, d_sd, sd));
+        iss_shrink_kernel<kNT><<<B, kNT, sm, s>>>(d_sd.as<ShrinkDesc>());
+        CAC_CUDA_TRY(cudaGetLastError());
+        std::vector<uint32_t> kdim(B);
+        CAC_CUDA_TRY(cudaMemcpyAsync(kdim.data(), d_k.p, (size_t)B * 4, cudaMemcpyDeviceToHost, s));
+        CAC_CUDA_TRY(cudaStreamSynchronize(s));
+        uint64_t elems = 0;
+        for (uint32_t b = 0; b < B; b++) elems += (uint64_t)kdim[b] * kdim[b];
+        MatBuf *roots = nullptr;
+        CAC_TRY(eng.alloc(std::max<uint64_t>(elems, 1) * 8, &roots));
+        CAC_CUDA_TRY(cudaMemsetAsync(roots->p, 0, elems * 8, s));
+        std::vector<DenseDesc> dd(B);
+        uint64_t off = 0;
+        for (uint32_t b = 0; b < B; b++) {
+            dd[b] = DenseDesc{g->u, g->v, g->w, sd[b].lab, static_cast<uint64_t *>(roots->p) + off, m, kdim[b], 0};
+            off += (uint64_t)kdim[b] * kdim[b];
+        }
+        CAC_TRY(upload(ctx, d_dd, dd));
+        if (m) {
+            dim3 grid((unsigned)std::max<uint64_t>(1, std::min<uint64_t>((m + 255) / 256, std::max<uint64_t>(1, (uint64_t)ctx->num_sms * 8 / B))), B);
+            dense_build_kernel<<<grid, 256, 0, s>>>(d_dd.as<DenseDesc>());
+            CAC_CUDA_TRY(cudaGetLastError());
+        }
+        roots->refs++;
+        for (uint32_t b = 0; b < B; b++) {
+            const uint64_t i = c0 + b;
+            if (kdim[b] < 2) {
+                // a single vertex left: no cut edge
+                fill_u64<<<1, 32, 0, s>>>(q.cuts + i, 1, 0);
+                continue;
+            }
+            eng.add(KNode{q.cuts + i, sd[b].k0, sd[b].idx, 1, kdim[b], 1, small, q.query, dd[b].mat, roots});
+        }
+        eng.release(roots);
+        CAC_CUDA_TRY(cudaStreamSynchronize(s));  // the scratch is reused by the next chunk
+    }
+    return CAC_OK;
+}
+
+int check_graph(const cac_graph *g) {
+    if (g->total_weight >= (1ull << 55)) {
+        set_error("total edge weight >= 2^55 is not supported by the Stoer-Wagner leaf kernel");
+        return CAC_ERR_UNSUPPORTED;
+    }
+    const uint32_t t = intermediate_size(g->n, g->m);
+    if (t > kMaxSmemVertices) {
+        set_error("contracted graphs with more than 16384 vertices are not supported yet");
+        return CAC_ERR_UNSUPPORTED;
+    }
     return CAC_OK;
 }
 
 }  // namespace
 
-int mincut_trials(cac_ctx *ctx, const cac_graph *g, uint32_t seed, uint32_t ranks, uint32_t per_rank,
-                  uint64_t *d_cuts, float *device_ms) {
+int mincut_admit_query(cac_ctx *ctx, KsEngine &eng, const MincutQuery &q, uint32_t query) {
+    CAC_TRY(check_graph(q.g));
+    QueryPlan p{q.g, q.seed, q.ranks, q.per_rank, intermediate_size(q.g->n, q.g->m), (uint64_t)q.ranks * q.per_rank,
+                q.d_cuts, query};
+    if (p.trials)
+        fill_u64<<<(unsigned)std::max<uint64_t>(1, std::min<uint64_t>((p.trials + 255) / 256, 4096)), 256, 0,
+                   ctx->stream>>>(p.cuts, p.trials, kU64Max);
+    CAC_CUDA_TRY(cudaGetLastError());
+    return admit(ctx, eng, p);
+}
+
+int mincut_run_queries(cac_ctx *ctx, std::vector<MincutQuery> &queries, float *device_ms) {
     cudaStream_t s = ctx->stream;
-    const uint32_t n = g->n;
-    const uint64_t m = g->m;
-    const uint64_t R = (uint64_t)ranks * per_rank;
-    if (g->total_weight >= (1ull << 55)) {
-        set_error("total edge weight >= 2^55 is not supported by the Stoer-Wagner leaf kernel");
-        return CAC_ERR_UNSUPPORTED;
-    }
-    const uint32_t t = intermediate_size(n, m);
-    if (t < n && n > kMaxSmemVertices) {
-        set_error("graphs with more than 16384 vertices that need sparse pre-contraction are not supported yet");
-        return CAC_ERR_UNSUPPORTED;
-    }
-    if (t > kMaxSmemVertices) {
-        set_error("contracted graphs with more than 16384 vertices are not supported yet");
-        return CAC_ERR_UNSUPPORTED;
-    }
-    const bool small_entries = g->total_weight < (1ull << 32);
+    for (const MincutQuery &q : queries) CAC_TRY(check_graph(q.g));
     CAC_CUDA_TRY(cudaEventRecord(ctx->ev[0], s));
-    fill_u64<<<std::max<unsigned>(1, (unsigned)std::min<uint64_t>((R + 255) / 256, 4096)), 256, 0, s>>>(d_cuts, R,
-                                                                                                       kU64Max);
-    std::vector<TrialKey> all(R);
-    for (uint32_t r = 0; r < ranks; r++)
-        for (uint32_t i = 0; i < per_rank; i++) all[(uint64_t)r * per_rank + i] = TrialKey{seed + r, i};
-
-    // wave size: trials whose Stage-1 scratch and three levels of matrices fit the budget
-    const uint64_t per_trial = (t < n ? 8 * m + 4 * (uint64_t)n : 0) + 3 * 8 * (uint64_t)t * t + 64;
-    const uint64_t budget = ctx->budget ? ctx->budget / 2 : (24ull << 30);
-    const uint64_t wave = std::max<uint64_t>(1, std::min<uint64_t>({R, budget / per_trial, (uint64_t)65535}));
-
-    DevBuf d_keys(ctx), d_pre(ctx), d_lab(ctx), d_k(ctx), d_moff(ctx), bufA(ctx), bufB(ctx), d_err(ctx);
-    CAC_TRY(d_err.ensure(4));
-    CAC_CUDA_TRY(cudaMemsetAsync(d_err.p, 0, 4, s));
-    for (uint64_t w0 = 0; w0 < R; w0 += wave) {
-        const uint32_t B = (uint32_t)std::min<uint64_t>(wave, R - w0);
-        std::vector<TrialKey> keys(all.begin() + w0, all.begin() + w0 + B);
-        CAC_TRY(upload(ctx, d_keys, keys));
-        std::vector<uint32_t> kdim(B, n);
-        CAC_TRY(d_k.ensure((size_t)B * 4));
-        const uint32_t *lab_ptr = nullptr;
-        if (t < n) {
-            CAC_TRY(d_pre.ensure((size_t)B * std::max<uint64_t>(m, 1) * 8));
-            CAC_TRY(d_lab.ensure((size_t)B * n * 4));
-            const size_t sm = kBatch * sizeof(uint2) + (size_t)n * 4;
-            CAC_CUDA_TRY(cudaFuncSetAttribute(iss_shrink_kernel<kNT>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                              (int)sm));
-            iss_shrink_kernel<kNT><<<B, kNT, sm, s>>>(n, m, g->u, g->v, g->w, t, d_keys.as<TrialKey>(),
-                                                       d_pre.as<uint64_t>(), d_lab.as<uint32_t>(), d_k.as<uint32_t>());
-            CAC_CUDA_TRY(cudaGetLastError());
-            CAC_CUDA_TRY(cudaMemcpyAsync(kdim.data(), d_k.p, (size_t)B * 4, cudaMemcpyDeviceToHost, s));
-            CAC_CUDA_TRY(cudaStreamSynchronize(s));
-            lab_ptr = d_lab.as<uint32_t>();
-        } else {
-            CAC_CUDA_TRY(cudaMemcpyAsync(d_k.p, kdim.data(), (size_t)B * 4, cudaMemcpyHostToDevice, s));
+    KsEngine eng(ctx);
+    CAC_TRY(eng.init_err());
+    std::vector<QueryPlan> plans(queries.size());
+    for (size_t i = 0; i < queries.size(); i++) {
+        MincutQuery &q = queries[i];
+        QueryPlan &p = plans[i];
+        p.g = q.g;
+        p.seed = q.seed;
+        p.ranks = q.ranks;
+        p.per_rank = q.per_rank;
+        p.t = intermediate_size(q.g->n, q.g->m);
+        p.trials = (uint64_t)q.ranks * q.per_rank;
+        p.cuts = q.d_cuts;
+        p.query = (uint32_t)i;
+        if (p.trials)
+            fill_u64<<<(unsigned)std::max<uint64_t>(1, std::min<uint64_t>((p.trials + 255) / 256, 4096)), 256, 0, s>>>(
+                p.cuts, p.trials, kU64Max);
+    }
+    // admission by memory: a query is admitted when the engine's buffers leave room for its
+    // estimated footprint (roots and two more levels of matrices); otherwise the engine steps first
+    const uint64_t budget = ctx->budget ? ctx->budget / 2 : (48ull << 30);
+    size_t next = 0;
+    while (next < plans.size() || !eng.idle()) {
+        while (next < plans.size()) {
+            const QueryPlan &p = plans[next];
+            const uint64_t t = std::min<uint64_t>(p.t, p.g->n);
+            const uint64_t est = (p.t < p.g->n ? p.trials : 1) * t * t * 8 * 3;
+            if (!eng.idle() && ctx->held + est > budget) break;
+            CAC_TRY(admit(ctx, eng, p));
+            next++;
         }
-        std::vector<uint64_t> moff(B);
-        uint64_t elems = 0;
-        std::vector<Node> roots;
-        for (uint32_t b = 0; b < B; b++) {
-            moff[b] = elems;
-            elems += (uint64_t)kdim[b] * kdim[b];
-            if (kdim[b] >= 2) roots.push_back(Node{b, 1, kdim[b], moff[b], 1});
-            else fill_u64<<<1, 32, 0, s>>>(d_cuts + w0 + b, 1, 0);  // a single vertex left: no cut edge
-        }
-        CAC_TRY(upload(ctx, d_moff, moff));
-        CAC_TRY(bufA.ensure(std::max<uint64_t>(elems, 1) * 8));
-        CAC_CUDA_TRY(cudaMemsetAsync(bufA.p, 0, elems * 8, s));
-        if (m) {
-            dim3 grid((unsigned)std::min<uint64_t>((m + 255) / 256, std::max(1, 4 * ctx->num_sms / (int)std::min<uint32_t>(B, 64u) + 1)), B);
-            dense_build_kernel<<<grid, 256, 0, s>>>(m, g->u, g->v, g->w, lab_ptr, n, d_k.as<uint32_t>(),
-                                                    d_moff.as<uint64_t>(), bufA.as<uint64_t>());
-            CAC_CUDA_TRY(cudaGetLastError());
-        }
-        CAC_TRY(ks_levels(ctx, roots, &bufA, &bufB, keys, d_cuts + w0, small_entries, d_err.as<uint32_t>()));
+        if (!eng.idle()) CAC_TRY(eng.step());
     }
     uint32_t err = 0;
-    CAC_CUDA_TRY(cudaMemcpyAsync(&err, d_err.p, 4, cudaMemcpyDeviceToHost, s));
+    CAC_TRY(eng.read_err(&err));
     CAC_CUDA_TRY(cudaEventRecord(ctx->ev[1], s));
     CAC_CUDA_TRY(cudaStreamSynchronize(s));
     if (device_ms) CAC_CUDA_TRY(cudaEventElapsedTime(device_ms, ctx->ev[0], ctx->ev[1]));
@@ -899,6 +1073,12 @@ int mincut_trials(cac_ctx *ctx, const cac_graph *g, uint32_t seed, uint32_t rank
         return CAC_ERR_CUDA;
     }
     return CAC_OK;
+}
+
+int mincut_trials(cac_ctx *ctx, const cac_graph *g, uint32_t seed, uint32_t ranks, uint32_t per_rank,
+                  uint64_t *d_cuts, float *device_ms) {
+    std::vector<MincutQuery> q{MincutQuery{g, seed, ranks, per_rank, d_cuts}};
+    return mincut_run_queries(ctx, q, device_ms);
 }
 
 int ks_dense_one(cac_ctx *ctx, uint32_t n, const uint64_t *mat_host, uint32_t seed, uint32_t rank, uint32_t trial,
@@ -914,25 +1094,27 @@ int ks_dense_one(cac_ctx *ctx, uint32_t n, const uint64_t *mat_host, uint32_t se
         return CAC_ERR_UNSUPPORTED;
     }
     cudaStream_t s = ctx->stream;
-    DevBuf bufA(ctx), bufB(ctx), d_cuts(ctx), d_err(ctx);
-    CAC_TRY(bufA.ensure((size_t)n * n * 8));
-    CAC_TRY(d_cuts.ensure(8));
-    CAC_TRY(d_err.ensure(4));
-    CAC_CUDA_TRY(cudaMemcpyAsync(bufA.p, mat_host, (size_t)n * n * 8, cudaMemcpyHostToDevice, s));
-    CAC_CUDA_TRY(cudaMemsetAsync(d_err.p, 0, 4, s));
-    fill_u64<<<1, 32, 0, s>>>(d_cuts.as<uint64_t>(), 1, kU64Max);
-    std::vector<TrialKey> keys{TrialKey{seed + rank, trial}};
-    std::vector<Node> roots{Node{0, 1, n, 0, 1}};
-    CAC_TRY(ks_levels(ctx, roots, &bufA, &bufB, keys, d_cuts.as<uint64_t>(), total / 2 < (1ull << 32),
-                      d_err.as<uint32_t>()));
-    uint32_t err = 0;
-    CAC_CUDA_TRY(cudaMemcpyAsync(cut, d_cuts.p, 8, cudaMemcpyDeviceToHost, s));
-    CAC_CUDA_TRY(cudaMemcpyAsync(&err, d_err.p, 4, cudaMemcpyDeviceToHost, s));
-    CAC_CUDA_TRY(cudaStreamSynchronize(s));
-    if (err) {
-        set_error("inconsistent selection prefix in the contraction kernel");
-        return CAC_ERR_CUDA;
+    DevBuf d_cut(ctx);
+    CAC_TRY(d_cut.ensure(8));
+    {
+        KsEngine eng(ctx);
+        CAC_TRY(eng.init_err());
+        MatBuf *root = nullptr;
+        CAC_TRY(eng.alloc((size_t)n * n * 8, &root));
+        CAC_CUDA_TRY(cudaMemcpyAsync(root->p, mat_host, (size_t)n * n * 8, cudaMemcpyHostToDevice, s));
+        fill_u64<<<1, 32, 0, s>>>(d_cut.as<uint64_t>(), 1, kU64Max);
+        eng.add(KNode{d_cut.as<uint64_t>(), seed + rank, trial, 1, n, 1, total / 2 < (1ull << 32) ? 1u : 0u, 0,
+                      static_cast<uint64_t *>(root->p), root});
+        while (!eng.idle()) CAC_TRY(eng.step());
+        uint32_t err = 0;
+        CAC_TRY(eng.read_err(&err));
+        if (err) {
+            set_error("inconsistent selection prefix in the contraction kernel");
+            return CAC_ERR_CUDA;
+        }
     }
+    CAC_CUDA_TRY(cudaMemcpyAsync(cut, d_cut.p, 8, cudaMemcpyDeviceToHost, s));
+    CAC_CUDA_TRY(cudaStreamSynchronize(s));
     return CAC_OK;
 }
 
@@ -949,18 +1131,19 @@ int exact_small(cac_ctx *ctx, uint32_t n, const uint64_t *mat_host, uint64_t *cu
     CAC_TRY(d_cuts.ensure(8));
     CAC_CUDA_TRY(cudaMemcpyAsync(buf.p, mat_host, (size_t)n * n * 8, cudaMemcpyHostToDevice, s));
     fill_u64<<<1, 32, 0, s>>>(d_cuts.as<uint64_t>(), 1, kU64Max);
-    std::vector<LeafDesc> leaves{LeafDesc{buf.as<uint64_t>(), n, 0}};
+    const uint32_t small = total / 2 < (1ull << 32) ? 1u : 0u;
+    std::vector<LeafDesc> leaves{LeafDesc{buf.as<uint64_t>(), d_cuts.as<uint64_t>(), n, small}};
     CAC_TRY(upload(ctx, d_leaf, leaves));
-    if (total / 2 < (1ull << 32)) {
+    if (small) {
         const size_t sm = (size_t)n * n * 4;
         CAC_CUDA_TRY(cudaFuncSetAttribute(sw_leaf_kernel<uint32_t>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                           (int)sm));
-        sw_leaf_kernel<uint32_t><<<1, 32, sm, s>>>(d_leaf.as<LeafDesc>(), d_cuts.as<uint64_t>());
+        sw_leaf_kernel<uint32_t><<<1, 32, sm, s>>>(d_leaf.as<LeafDesc>());
     } else {
         const size_t sm = (size_t)n * n * 8;
         CAC_CUDA_TRY(cudaFuncSetAttribute(sw_leaf_kernel<uint64_t>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                           (int)sm));
-        sw_leaf_kernel<uint64_t><<<1, 32, sm, s>>>(d_leaf.as<LeafDesc>(), d_cuts.as<uint64_t>());
+        sw_leaf_kernel<uint64_t><<<1, 32, sm, s>>>(d_leaf.as<LeafDesc>());
     }
     CAC_CUDA_TRY(cudaGetLastError());
     CAC_CUDA_TRY(cudaMemcpyAsync(cut, d_cuts.p, 8, cudaMemcpyDeviceToHost, s));

@@ -257,6 +257,20 @@ int cac_ctx_create(const cac_config *config, cac_ctx **out) {
         ctx->own_stream = true;
     }
     cudaDeviceGetAttribute(&ctx->num_sms, cudaDevAttrMultiProcessorCount, cfg.device);
+    {
+        // a pool of its own for the level buffers, which keeps freed memory for the next level
+        cudaMemPoolProps props{};
+        props.allocType = cudaMemAllocationTypePinned;
+        props.location.type = cudaMemLocationTypeDevice;
+        props.location.id = cfg.device;
+        if (cudaMemPoolCreate(&ctx->pool, &props) == cudaSuccess) {
+            uint64_t keep = ~0ull;
+            cudaMemPoolSetAttribute(ctx->pool, cudaMemPoolAttrReleaseThreshold, &keep);
+        } else {
+            cudaGetLastError();
+            ctx->pool = nullptr;
+        }
+    }
     for (auto &e : ctx->ev) cudaEventCreate(&e);
     if (cudaMallocHost((void **)&ctx->pinned_u32, 64 * 1024) != cudaSuccess) {
         set_error("cudaMallocHost failed");
@@ -280,6 +294,7 @@ int cac_ctx_destroy(cac_ctx *ctx) {
     cc_graph_reset(ctx);
     dev_free(ctx, ctx->arena.base, ctx->arena.cap);
     dev_free(ctx, ctx->io.base, ctx->io.cap);
+    if (ctx->pool) cudaMemPoolDestroy(ctx->pool);
     for (auto &e : ctx->ev) if (e) cudaEventDestroy(e);
     if (ctx->pinned_u32) cudaFreeHost(ctx->pinned_u32);
     if (ctx->own_stream) cudaStreamDestroy(ctx->stream);

@@ -141,6 +141,17 @@ typedef struct {
 
 int cac_mincut(cac_ctx *ctx, const cac_graph *g, double success_probability, uint32_t seed,
                uint32_t virtual_ranks, cac_mincut_result *res);
+/* Many square_root queries (graphs of any sizes) in one batch: every trial of every query runs
+ * through one level-synchronous Karger-Stein engine, admitted as device memory allows. results[i]
+ * is what cac_mincut would return for queries[i] alone (device_ms is the whole batch's time).
+ * Replaces a loop of SquareRootCut::runMaster calls, one per input graph. */
+typedef struct {
+    const cac_graph *graph;
+    double success_probability;
+    uint32_t seed;
+    uint32_t virtual_ranks;
+} cac_mincut_query;
+int cac_mincut_batch(cac_ctx *ctx, const cac_mincut_query *queries, uint32_t count, cac_mincut_result *results);
 /* Run trials (r, i) for r < virtual_ranks, i < trials_per_rank and write each trial's cut to
  * cuts_host[r * trials_per_rank + i]. */
 int cac_mincut_trials(cac_ctx *ctx, const cac_graph *g, uint32_t seed, uint32_t virtual_ranks,
@@ -164,6 +175,59 @@ typedef struct {
 
 int cac_approx_cut(cac_ctx *ctx, const cac_graph *g, double success_probability, uint32_t seed,
                    uint32_t virtual_ranks, cac_approx_result *res);
+
+/* ---- serving loop ----
+ * The reference answers one query per process launch. A cac_server keeps graphs resident in HBM
+ * and answers square_root, approx_cut and parallel_cc queries as they arrive:
+ *   - square_root queries join one persistent Karger-Stein engine between its level steps
+ *     (continuous batching: a query admitted while others run shares their launches), admitted
+ *     while the estimated footprint of the running queries stays within hbm_budget_bytes
+ *     (0: no limit);
+ *   - parallel_cc and approx_cut queries run on a second worker and stream, concurrently.
+ * Every response equals what the single-query entry point returns for the same arguments
+ * (cac_mincut cut and trials_per_rank, cac_approx_cut cut and trials, cac_cc count and labels).
+ * Submit and poll may be called from any threads. A graph must outlive the queries on it. */
+typedef struct cac_server cac_server;
+typedef struct {
+    int device;
+    uint64_t hbm_budget_bytes;
+} cac_server_config;
+
+#define CAC_QUERY_MINCUT 1 /* square_root */
+#define CAC_QUERY_APPROX 2 /* approx_cut */
+#define CAC_QUERY_CC 3     /* parallel_cc */
+#define CAC_PENDING 1      /* cac_server_poll: not finished yet */
+
+typedef struct {
+    int kind;                   /* CAC_QUERY_* */
+    const cac_graph *graph;     /* from cac_server_graph */
+    double success_probability; /* square_root, approx_cut */
+    uint32_t seed;
+    uint32_t virtual_ranks;     /* 0 is read as 1 */
+    uint32_t *labels_host;      /* parallel_cc, optional: n labels written before completion */
+} cac_request;
+
+typedef struct {
+    int status;              /* CAC_OK or the query's CAC_ERR_* code */
+    uint64_t cut;            /* square_root and approx_cut weight */
+    uint32_t trials;         /* square_root trials per rank; approx_cut copies * level */
+    uint32_t num_components; /* parallel_cc */
+    double queue_ms;         /* submit -> admitted */
+    double service_ms;       /* admitted -> finished */
+    char message[160];       /* the error message when status != CAC_OK */
+} cac_response;
+
+int cac_server_create(const cac_server_config *config, cac_server **out);
+/* Upload a graph for the server's queries (same arguments as cac_graph_from_edges with host
+ * arrays); free it with cac_graph_free after its last query has finished. */
+int cac_server_graph(cac_server *server, uint32_t n, uint64_t m, const uint32_t *u, const uint32_t *v,
+                     const uint32_t *w, cac_graph **out);
+int cac_server_submit(cac_server *server, const cac_request *request, uint64_t *ticket);
+/* CAC_OK with *response filled (the ticket is then retired), CAC_PENDING when wait == 0 and the
+ * query has not finished, CAC_ERR_INVALID for an unknown ticket. */
+int cac_server_poll(cac_server *server, uint64_t ticket, int wait, cac_response *response);
+/* Finishes every submitted query, then stops the workers. */
+int cac_server_destroy(cac_server *server);
 
 /* ---- primitives ---- */
 /* nblocks sitmo blocks with key `key` and counters ctr0, ctr0 + 1, ... (256-bit add);
