@@ -27,6 +27,7 @@ ranks / max time over ranks.
 """
 import argparse
 import json
+import math
 import os
 import statistics
 import subprocess
@@ -226,37 +227,29 @@ def run_reference(args, rank, world):
     return 0
 
 
-def run_cac(args, rank, world):
+def _cc_measure(ctx, stream, g, n, hu_np, hv_np, steps, warmup, world, flush):
+    """Device-resident CC queries (CUDA events) and host-to-host queries through cac_cc_edges."""
     import torch
-    import cac
-
-    dev = int(os.environ.get("LOCAL_RANK", "0"))
-    torch.cuda.set_device(dev)
-    n, u, v, _ = _workload()
-    m = len(u)
-    stream = torch.cuda.Stream(device=dev)
-    ctx = cac.Context(dev, stream=stream.cuda_stream)
-    g = ctx.graph(n, u, v)
-    labels = torch.empty(n, dtype=torch.int32, device="cuda")
-    flush = torch.empty(512 << 20, dtype=torch.uint8, device="cuda")
-    want_count = None
+    m = g.m
+    labels = torch.empty(max(n, 1), dtype=torch.int32, device="cuda")
 
     def step():
         return g.connected_components(seed=GRAPH_SEED, virtual_ranks=1, out=labels)
 
+    want_count = None
     with torch.cuda.stream(stream):
-        for _ in range(args.warmup):
+        for _ in range(warmup):
             flush.zero_()
             want_count = step()[0]
     torch.cuda.synchronize()
     if world > 1:
         torch.distributed.barrier()
     torch.cuda.synchronize()
-    starts = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
-    ends = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
+    starts = [torch.cuda.Event(enable_timing=True) for _ in range(steps)]
+    ends = [torch.cuda.Event(enable_timing=True) for _ in range(steps)]
     edge_ms, phases = [], []
-    with Clocks(dev) as clk, torch.cuda.stream(stream):
-        for i in range(args.steps):
+    with torch.cuda.stream(stream):
+        for i in range(steps):
             flush.zero_()
             starts[i].record(stream)
             count, _, res = step()
@@ -265,25 +258,16 @@ def run_cac(args, rank, world):
             phases.append((res.sample_ms, res.edge_pass_ms, res.hook_ms, res.label_ms))
             assert count == want_count
         torch.cuda.synchronize()
-    step_ms = [s.elapsed_time(e) for s, e in zip(starts, ends)]
-    total_ms = sum(step_ms)
+    total_ms = sum(s.elapsed_time(e) for s, e in zip(starts, ends))
     if world > 1:
         t = torch.tensor([total_ms], device="cuda")
         torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
         total_ms = float(t.item())
-    value = world * m * args.steps / (total_ms / 1e3)
-
-    # e2e: pinned host edges -> host labels through the one-call entry point
-    hu = torch.from_numpy(u.view(np.int32)).pin_memory()
-    hv = torch.from_numpy(v.view(np.int32)).pin_memory()
-    hl = torch.empty(n, dtype=torch.int32).pin_memory()
-    hu_np = hu.numpy().view(np.uint32)
-    hv_np = hv.numpy().view(np.uint32)
-    hl_np = hl.numpy().view(np.uint32)
-    for _ in range(max(1, args.warmup)):
+    hl_np = torch.empty(max(n, 1), dtype=torch.int32).pin_memory().numpy().view(np.uint32)
+    for _ in range(max(1, warmup)):
         ctx.cc_edges(n, hu_np, hv_np, GRAPH_SEED, 1, hl_np)
     e2e_ms = []
-    for _ in range(args.steps):
+    for _ in range(steps):
         flush.zero_()
         torch.cuda.synchronize()
         t0 = time.perf_counter()
@@ -295,12 +279,70 @@ def run_cac(args, rank, world):
         t = torch.tensor([e2e_total], device="cuda")
         torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
         e2e_total = float(t.item())
-    e2e_value = world * m * args.steps / (e2e_total / 1e3)
+    return {"value": world * m * steps / (total_ms / 1e3), "ms_per_step": total_ms / steps,
+            "e2e": {"value": world * m * steps / (e2e_total / 1e3), "unit": "edges/s", "h2d_bytes_per_step": 8 * m,
+                    "d2h_bytes_per_step": 4 * n, "ms_per_step": e2e_total / steps},
+            "edge_avg_ms": statistics.mean(edge_ms), "components": want_count,
+            "phases_ms": dict(zip(("sampling_round", "filter", "hook_survivors", "labels"),
+                                  [round(statistics.mean(p[i] for p in phases), 4) for i in range(4)]))}
 
+
+def _pinned_u32(a):
+    import torch
+    t = torch.from_numpy(np.ascontiguousarray(a, dtype=np.uint32).view(np.int32)).pin_memory()
+    return t, t.numpy().view(np.uint32)
+
+
+def _rmat22(ctx, stream, steps, warmup, world, flush):
+    """CC edges/s on R-MAT scale 22 (edge factor 16, a=0.57 b=0.19 c=0.19, isolated vertices kept),
+    generated on the device."""
+    t0 = time.perf_counter()
+    g = ctx.generate("rmat", seed=GRAPH_SEED, scale=22, edge_factor=16)
+    gen_s = time.perf_counter() - t0
+    u, v, _ = g.edges()
+    keep = (_pinned_u32(u), _pinned_u32(v))
+    r = _cc_measure(ctx, stream, g, g.n, keep[0][1], keep[1][1], steps, warmup, world, flush)
+    r.update({"workload": "parallel_cc R-MAT scale 22 (4,194,304 vertices, 67,108,864 edges)", "unit": "edges/s",
+              "vertices": g.n, "edges": g.m, "generate_s": round(gen_s, 3)})
+    g.free()
+    return r
+
+
+def run_cac(args, rank, world):
+    import torch
+    import cac
+
+    dev = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(dev)
+    stream = torch.cuda.Stream(device=dev)
+    ctx = cac.Context(dev, stream=stream.cuda_stream)
+    flush = torch.empty(512 << 20, dtype=torch.uint8, device="cuda")
+    if args.workload == "cc-rmat22":
+        with Clocks(dev) as clk:
+            r = _rmat22(ctx, stream, args.steps, args.warmup, world, flush)
+        line = {"metric": "CC edges/s (parallel_cc, R-MAT scale 22)", "value": r["value"], "unit": "edges/s",
+                "n_gpus": world, "steps": args.steps, "warmup": args.warmup, "ms_per_step": r["ms_per_step"],
+                "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "u32",
+                "data": "synthetic (R-MAT generated on the device, seed 0)",
+                "config": {"workload": r["workload"], "vertices": r["vertices"], "edges": r["edges"],
+                           "virtual_ranks": 1, "l2": "flushed (512 MB write) before every timed query"},
+                "e2e": r["e2e"], "components": r["components"], "phases_ms": r["phases_ms"],
+                "gpu_launches": KERNELS_PER_QUERY * args.steps, "clocks": clk.summary()}
+        if rank == 0:
+            print(json.dumps(line))
+        ctx.close()
+        return 0
+
+    n, u, v, _ = _workload()
+    m = len(u)
+    g = ctx.graph(n, u, v)
+    hu, hu_np = _pinned_u32(u)
+    hv, hv_np = _pinned_u32(v)
+    with Clocks(dev) as clk:
+        r = _cc_measure(ctx, stream, g, n, hu_np, hv_np, args.steps, args.warmup, world, flush)
     peak, peak_kind = _peaks()
-    edge_avg_ms = statistics.mean(edge_ms)
     alg_bytes = 8 * m
-    achieved = alg_bytes / (edge_avg_ms / 1e3) / 1e9
+    achieved = alg_bytes / (r["edge_avg_ms"] / 1e3) / 1e9
     traffic = None
     prof = os.path.join(ROOT, "profiles", "cc_filter_ba1m.json")
     if os.path.exists(prof):
@@ -311,25 +353,27 @@ def run_cac(args, rank, world):
         ctx.close()
         return 0
     line = {
-        "metric": METRIC, "value": value, "unit": "edges/s", "n_gpus": world, "steps": args.steps,
-        "warmup": args.warmup, "ms_per_step": total_ms / args.steps, "higher_is_better": True, "scaling": "weak",
+        "metric": METRIC, "value": r["value"], "unit": "edges/s", "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": r["ms_per_step"], "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "u32", "data": "synthetic (seeded Barabasi-Albert, n=1,024,000, attach 16, "
                                                      "permuted)",
         "config": {"workload": "parallel_cc BA n=1024000 m=16 (16,383,744 edges)", "vertices": n, "edges": m,
                    "virtual_ranks": 1, "l2": "flushed (512 MB write) before every timed query",
                    "parallelism": "replicas" if world > 1 else "single GPU"},
-        "e2e": {"value": e2e_value, "unit": "edges/s", "h2d_bytes_per_step": 8 * m, "d2h_bytes_per_step": 4 * n,
-                "ms_per_step": e2e_total / args.steps},
+        "e2e": r["e2e"],
         "roofline": {"bound": "hbm", "kernel": "cc_filter", "achieved": achieved, "peak": peak,
                      "peak_kind": peak_kind, "unit": "GB/s", "frac": achieved / peak, "traffic": traffic,
-                     "alg_bytes_per_launch": alg_bytes, "avg_launch_ms": edge_avg_ms},
+                     "alg_bytes_per_launch": alg_bytes, "avg_launch_ms": r["edge_avg_ms"]},
         "gpu_launches": KERNELS_PER_QUERY * args.steps,
-        "phases_ms": dict(zip(("sampling_round", "filter", "hook_survivors", "labels"),
-                              [round(statistics.mean(p[i] for p in phases), 4) for i in range(4)])),
+        "phases_ms": r["phases_ms"],
         "clocks": clk.summary(),
     }
     if not args.no_cpu_baseline:
         line["cpu_baseline"] = _cpu_baseline(n, u, v)
+    if not args.no_rmat:
+        rr = _rmat22(ctx, stream, max(3, args.steps // 4), 3, 1, flush)
+        line["also_cc_rmat22"] = {k: rr[k] for k in ("workload", "value", "unit", "ms_per_step", "e2e", "components",
+                                                     "phases_ms", "generate_s")}
     if not args.no_ks:
         line["also_ks"] = _ks_also(ctx)
     print(json.dumps(line))
@@ -338,17 +382,195 @@ def run_cac(args, rank, world):
     return 0
 
 
+def run_batch(args, rank, world):
+    """--workload ks-batch: square_root on a population of uneven graphs (4096 by default) in one
+    batch, next to the plain path (one cac_mincut call per graph) on a subset of the same graphs."""
+    import torch
+    import cac
+    import workloads
+    dev = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(dev)
+    stream = torch.cuda.Stream(device=dev)
+    ctx = cac.Context(dev, stream=stream.cuda_stream)
+    specs = workloads.uneven_population(args.graphs)
+    t0 = time.perf_counter()
+    graphs = [workloads.make(ctx, sp) for sp in specs]
+    gen_s = time.perf_counter() - t0
+    seeds = [sp["seed"] for sp in specs]
+    sub = min(len(graphs), 256)
+    ctx.mincut_batch(graphs[:16], 0.9, seeds=seeds[:16])  # warm-up of both paths
+    for g, sd in zip(graphs[:4], seeds[:4]):
+        g.square_root(0.9, seed=sd)
+    t0 = time.perf_counter()
+    plain = [g.square_root(0.9, seed=sd) for g, sd in zip(graphs[:sub], seeds[:sub])]
+    plain_s = time.perf_counter() - t0
+    t0 = time.perf_counter()
+    bsub = ctx.mincut_batch(graphs[:sub], 0.9, seeds=seeds[:sub])
+    bsub_s = time.perf_counter() - t0
+    assert all(a.cut == b.cut and a.total_trials == b.total_trials for a, b in zip(plain, bsub))
+    for _ in range(args.warmup):
+        res = ctx.mincut_batch(graphs, 0.9, seeds=seeds)
+    wall = []
+    with Clocks(dev) as clk:
+        for _ in range(args.steps):
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            res = ctx.mincut_batch(graphs, 0.9, seeds=seeds)
+            wall.append(time.perf_counter() - t0)
+    trials = sum(r.total_trials for r in res)
+    sub_trials = sum(r.total_trials for r in plain)
+    total_s = sum(wall)
+    line = {"metric": "Karger-Stein trials/s (square_root, %d uneven graphs in one batch)" % len(graphs),
+            "value": world * trials * args.steps / total_s, "unit": "trials/s", "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": total_s / args.steps * 1e3, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "u64",
+            "data": "synthetic (device-generated Watts-Strogatz and G(n, M), seeds base + index)",
+            "config": {"workload": "uneven square_root batch", "graphs": len(graphs),
+                       "edges": int(sum(g.m for g in graphs)), "trials_per_batch": trials,
+                       "success_probability": 0.9, "n_range": [64, 8192], "timing": "host wall clock per batch"},
+            "queries_per_s": world * len(graphs) * args.steps / total_s,
+            "device_ms_per_batch": float(res[0].device_ms),
+            "plain_path_subset": {"graphs": sub, "trials": sub_trials, "one_call_per_graph_s": plain_s,
+                                  "batched_s": bsub_s, "plain_queries_per_s": sub / plain_s,
+                                  "batched_queries_per_s": sub / bsub_s, "speedup": plain_s / bsub_s,
+                                  "cuts_equal": True},
+            "generate_s": round(gen_s, 3), "clocks": clk.summary()}
+    if rank == 0:
+        print(json.dumps(line))
+    for g in graphs:
+        g.free()
+    ctx.close()
+    return 0
+
+
+def _percentile(xs, q):
+    xs = sorted(xs)
+    if not xs:
+        return None
+    k = min(len(xs) - 1, max(0, int(math.ceil(q / 100.0 * len(xs))) - 1))
+    return xs[k]
+
+
+def run_serve(args, rank, world):
+    """--workload serve: a mixed stream of square_root : approx_cut : parallel_cc = 2:1:1 queries
+    over graphs of 10^3 - 10^7 edges, served by cac_server under a 120 GB HBM budget: queries/s at
+    saturation (every query submitted at once), p50/p99 latency under Poisson arrivals at 60% of
+    that rate, and the plain path (one single-query call after another) on the same trace."""
+    import threading
+    import torch
+    import cac
+    import workloads
+    dev = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(dev)
+    specs = workloads.served_population(32)
+    ctx = cac.Context(dev)
+    srv = cac.Server(dev, hbm_budget_bytes=120 << 30)
+    cg = [workloads.make(ctx, sp) for sp in specs]
+    sg = []
+    for sp in specs:
+        d = dict(sp)
+        sg.append(srv.generate(d.pop("family"), **d))
+    probs = {"square_root": 0.95, "approx_cut": 0.9, "parallel_cc": 0.0}
+
+    def plain_one(kind, gi, sd):
+        g = cg[gi]
+        if kind == "square_root":
+            r = g.square_root(probs[kind], seed=sd)
+            return (int(r.cut), int(r.trials_per_rank))
+        if kind == "approx_cut":
+            r = g.approx_cut(probs[kind], seed=sd)
+            return (int(r.cut), int(r.trials))
+        return (int(g.connected_components(seed=sd, labels=False)[0]),)
+
+    def served_value(kind, resp):
+        if kind == "parallel_cc":
+            return (int(resp.num_components),)
+        return (int(resp.cut), int(resp.trials))
+
+    trace = workloads.served_trace(args.queries, len(specs), None, seed=7)
+    for kind in ("square_root", "approx_cut", "parallel_cc"):  # warm-up
+        plain_one(kind, 0, 1)
+        srv.poll(srv.submit(kind, sg[0], probs[kind], 1))
+    # plain path: one query after another through the single-query calls
+    t0 = time.perf_counter()
+    plain_lat, want = [], []
+    for _, kind, gi, sd in trace:
+        q0 = time.perf_counter()
+        want.append(plain_one(kind, gi, sd))
+        plain_lat.append((time.perf_counter() - q0) * 1e3)
+    plain_s = time.perf_counter() - t0
+    # saturation: every query submitted at once
+    with Clocks(dev) as clk:
+        t0 = time.perf_counter()
+        tickets = [srv.submit(kind, sg[gi], probs[kind], sd) for _, kind, gi, sd in trace]
+        got = [srv.poll(t)[0] for t in tickets]
+        sat_s = time.perf_counter() - t0
+    sat_lat = [r.queue_ms + r.service_ms for r in got]
+    equal = all(served_value(kind, r) == w for (_, kind, _, _), r, w in zip(trace, got, want))
+    # Poisson arrivals at 60% of the saturated rate
+    rate = 0.6 * len(trace) / sat_s
+    ptrace = workloads.served_trace(args.queries, len(specs), rate, seed=8)
+    ptickets = [None] * len(ptrace)
+
+    def submitter():
+        start = time.perf_counter()
+        for i, (at, kind, gi, sd) in enumerate(ptrace):
+            delay = start + at - time.perf_counter()
+            if delay > 0:
+                time.sleep(delay)
+            ptickets[i] = srv.submit(kind, sg[gi], probs[kind], sd)
+
+    t0 = time.perf_counter()
+    th = threading.Thread(target=submitter)
+    th.start()
+    th.join()
+    pres = [srv.poll(t)[0] for t in ptickets]
+    poisson_s = time.perf_counter() - t0
+    lat = [r.queue_ms + r.service_ms for r in pres]
+    by_kind = {}
+    for (_, kind, _, _), x in zip(ptrace, lat):
+        by_kind.setdefault(kind, []).append(x)
+    line = {"metric": "served queries/s (square_root : approx_cut : parallel_cc = 2:1:1, 10^3-10^7 edges)",
+            "value": len(trace) / sat_s, "unit": "queries/s", "n_gpus": 1, "steps": len(trace), "warmup": 3,
+            "ms_per_step": sat_s / len(trace) * 1e3, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "u64", "data": "synthetic (device-generated G(n, p) and R-MAT)",
+            "config": {"workload": "served mixed stream", "graphs": len(specs),
+                       "edges_range": [int(min(g.m for g in cg)), int(max(g.m for g in cg))],
+                       "hbm_budget_bytes": 120 << 30, "queries": len(trace)},
+            "saturation": {"queries_per_s": len(trace) / sat_s, "p50_ms": _percentile(sat_lat, 50),
+                           "p99_ms": _percentile(sat_lat, 99)},
+            "poisson": {"rate_per_s": rate, "queries_per_s": len(ptrace) / poisson_s,
+                        "p50_ms": _percentile(lat, 50), "p99_ms": _percentile(lat, 99),
+                        "p99_ms_by_kind": {k: _percentile(v, 99) for k, v in by_kind.items()}},
+            "plain_path": {"queries_per_s": len(trace) / plain_s, "p50_ms": _percentile(plain_lat, 50),
+                           "p99_ms": _percentile(plain_lat, 99)},
+            "speedup_vs_plain": plain_s / sat_s, "results_equal_plain": equal, "clocks": clk.summary()}
+    if rank == 0:
+        print(json.dumps(line))
+    srv.close()
+    ctx.close()
+    return 0 if equal else 1
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=20)
-    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--steps", type=int, default=None, help="default 20 (cc), 10 (ks-er1000, ks-k4000), 3 (ks-batch)")
+    ap.add_argument("--warmup", type=int, default=None, help="default 5 (cc), 3 otherwise")
     ap.add_argument("--impl", default="cac", choices=["cac", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-ks", action="store_true", help="skip the square_root (Karger-Stein) measurements")
-    ap.add_argument("--workload", default="cc", choices=["cc", "ks-er1000", "ks-k4000"],
-                    help="cc: the benchmark line; ks-*: only one square_root configuration")
+    ap.add_argument("--no-rmat", action="store_true", help="skip the R-MAT scale 22 CC measurement")
+    ap.add_argument("--workload", default="cc",
+                    choices=["cc", "cc-rmat22", "ks-er1000", "ks-k4000", "ks-batch", "serve"],
+                    help="cc: the benchmark line; the others: one workload's line")
+    ap.add_argument("--graphs", type=int, default=4096, help="ks-batch: graphs in the batch")
+    ap.add_argument("--queries", type=int, default=200, help="serve: queries in the trace")
     args = ap.parse_args()
+    if args.steps is None:
+        args.steps = {"cc": 20, "cc-rmat22": 20, "ks-batch": 3}.get(args.workload, 10)
+    if args.warmup is None:
+        args.warmup = 5 if args.workload == "cc" else 3
     rank = int(os.environ.get("RANK", "0"))
     world = int(os.environ.get("WORLD_SIZE", "1"))
     if args.impl == "reference":
@@ -358,8 +580,12 @@ def main():
         torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", "0")))
         torch.distributed.init_process_group("nccl")
     try:
-        if args.workload != "cc":
+        if args.workload in ("ks-er1000", "ks-k4000"):
             return run_ks(args, rank, world)
+        if args.workload == "ks-batch":
+            return run_batch(args, rank, world)
+        if args.workload == "serve":
+            return run_serve(args, rank, world)
         return run_cac(args, rank, world)
     finally:
         if world > 1:

@@ -55,6 +55,16 @@ class ApproxResult(ctypes.Structure):
                 ("level", ctypes.c_uint32), ("device_ms", ctypes.c_float)]
 
 
+class GenSpec(ctypes.Structure):
+    _fields_ = [("family", ctypes.c_int), ("n", ctypes.c_uint32), ("p", ctypes.c_double),
+                ("avg_degree", ctypes.c_double), ("k", ctypes.c_uint32), ("scale", ctypes.c_uint32),
+                ("edge_factor", ctypes.c_uint32), ("a", ctypes.c_double), ("b", ctypes.c_double),
+                ("c", ctypes.c_double), ("seed", ctypes.c_uint32), ("wmin", ctypes.c_uint32), ("wmax", ctypes.c_uint32)]
+
+
+GEN_FAMILIES = {"erdos_renyi": 1, "erdos_renyi_m": 2, "watts_strogatz": 3, "rmat": 4, "complete": 5}
+
+
 class _ServerConfig(ctypes.Structure):
     _fields_ = [("device", ctypes.c_int), ("hbm_budget_bytes", ctypes.c_uint64)]
 
@@ -90,6 +100,7 @@ EXPORTS = [
                                             ctypes.POINTER(_vp)]),
     ("cac_graph_free", ctypes.c_int, [_vp]),
     ("cac_graph_info", ctypes.c_int, [_vp, _u32p, _u64p, _u64p]),
+    ("cac_graph_copy_edges", ctypes.c_int, [_vp, _vp, _vp, _vp, ctypes.c_int]),
     ("cac_parse_file", ctypes.c_int, [ctypes.c_char_p, _u32p, _u64p, _vp, _vp, _vp, ctypes.c_uint64]),
     ("cac_parse_header", ctypes.c_int, [ctypes.c_char_p, _u32p, _u64p]),
     ("cac_cc", ctypes.c_int, [_vp, _vp, ctypes.c_uint32, ctypes.c_uint32, _vp, ctypes.c_int,
@@ -107,8 +118,10 @@ EXPORTS = [
     ("cac_approx_cut", ctypes.c_int, [_vp, _vp, ctypes.c_double, ctypes.c_uint32, ctypes.c_uint32,
                                       ctypes.POINTER(ApproxResult)]),
     ("cac_sitmo_blocks", ctypes.c_int, [_vp, _u64p, _u64p, ctypes.c_uint64, _vp]),
+    ("cac_graph_generate", ctypes.c_int, [_vp, ctypes.POINTER(GenSpec), ctypes.POINTER(_vp)]),
     ("cac_server_create", ctypes.c_int, [ctypes.POINTER(_ServerConfig), ctypes.POINTER(_vp)]),
     ("cac_server_graph", ctypes.c_int, [_vp, ctypes.c_uint32, ctypes.c_uint64, _vp, _vp, _vp, ctypes.POINTER(_vp)]),
+    ("cac_server_generate", ctypes.c_int, [_vp, ctypes.POINTER(GenSpec), ctypes.POINTER(_vp)]),
     ("cac_server_submit", ctypes.c_int, [_vp, ctypes.POINTER(Request), _u64p]),
     ("cac_server_poll", ctypes.c_int, [_vp, ctypes.c_uint64, ctypes.c_int, ctypes.POINTER(Response)]),
     ("cac_server_destroy", ctypes.c_int, [_vp]),
@@ -194,6 +207,16 @@ class Context:
         self._graphs.add(g)
         return g
 
+    def generate(self, family, seed=0, n=0, p=0.0, avg_degree=0.0, k=0, scale=0, edge_factor=0,
+                 a=0.57, b=0.19, c=0.19, wmin=1, wmax=1):
+        """A seeded synthetic graph made on the device; the same edges as graphgen.<family>."""
+        spec = GenSpec(GEN_FAMILIES[family], n, p, avg_degree, k, scale, edge_factor, a, b, c, seed, wmin, wmax)
+        h = _vp()
+        _check(lib().cac_graph_generate(self.h, ctypes.byref(spec), ctypes.byref(h)), "cac_graph_generate")
+        g = Graph(self, h, None)
+        self._graphs.add(g)
+        return g
+
     def load(self, path):
         h = _vp()
         _check(lib().cac_graph_load_file(self.h, path.encode(), ctypes.byref(h)), "cac_graph_load_file")
@@ -265,6 +288,14 @@ class Graph:
         except Exception:
             pass
 
+    def edges(self):
+        """-> (u, v, w) host copies of the device edge arrays."""
+        k = max(self.m, 1)
+        u, v, w = np.zeros(k, np.uint32), np.zeros(k, np.uint32), np.zeros(k, np.uint32)
+        _check(lib().cac_graph_copy_edges(self.h, ctypes.c_void_p(u.ctypes.data), ctypes.c_void_p(v.ctypes.data),
+                                          ctypes.c_void_p(w.ctypes.data), HOST), "cac_graph_copy_edges")
+        return u[: self.m], v[: self.m], w[: self.m]
+
     # UnweightedIteratedSparseSampling::connectedComponents
     def connected_components(self, seed=0, virtual_ranks=1, labels=True, out=None):
         """Returns (number_of_components, labels or None, CCResult). `out` may be a device
@@ -326,6 +357,15 @@ class Server:
         _check(lib().cac_server_graph(self.h, n, len(u), ctypes.c_void_p(u.ctypes.data), ctypes.c_void_p(v.ctypes.data),
                                       None if w is None else ctypes.c_void_p(w.ctypes.data), ctypes.byref(h)),
                "cac_server_graph")
+        g = Graph(self, h, None, queries=False)
+        self._graphs.add(g)
+        return g
+
+    def generate(self, family, seed=0, n=0, p=0.0, avg_degree=0.0, k=0, scale=0, edge_factor=0,
+                 a=0.57, b=0.19, c=0.19, wmin=1, wmax=1):
+        spec = GenSpec(GEN_FAMILIES[family], n, p, avg_degree, k, scale, edge_factor, a, b, c, seed, wmin, wmax)
+        h = _vp()
+        _check(lib().cac_server_generate(self.h, ctypes.byref(spec), ctypes.byref(h)), "cac_server_generate")
         g = Graph(self, h, None, queries=False)
         self._graphs.add(g)
         return g

@@ -95,6 +95,10 @@ inline void *arena_take(cac_ctx *ctx, size_t bytes) { return arena_take(ctx->are
 inline void arena_reset(cac_ctx *ctx) { ctx->arena.used = 0; }
 inline size_t align_up(size_t x, size_t a = 256) { return (x + a - 1) / a * a; }
 
+// Graph from edge arrays (host or device): copies, validates ids, totals the weights.
+int graph_create(cac_ctx *ctx, uint32_t n, uint64_t m, const uint32_t *u, const uint32_t *v, const uint32_t *w,
+                 int where, cac_graph **out);
+
 // ---- CC (cc.cu) ----
 struct CCPlan {
     // per virtual rank: slice offset/length in the edge array and number of draws

@@ -20,7 +20,8 @@
 //              quotient_kernel   one CTA per output row: member rows summed by column label in
 //                                shared memory (u64 shared atomics), one coalesced row store
 //              sw_leaf_kernel    one warp per leaf (n <= 128): Stoer-Wagner maximum-adjacency
-//                                phases on the matrix held in shared memory; atomicMin into the
+//                                phases with Nagamochi-Ono-Ibaraki contractions on the matrix held
+//                                in shared memory (circulant half storage); atomicMin into the
 //                                trial's cut
 // The random stream of every draw is addressed by (seed + r, i, tag, 0) and (round, draw index),
 // tag 1 for Stage 1 and 1 + h for the Karger-Stein child with heap index h, so a CPU replay of
@@ -272,13 +273,23 @@ __global__ void prep_rows_kernel(const SrcDesc *__restrict__ srcs, const uint64_
     const uint64_t i = gw - row_off[lo];
     const uint64_t *row = S.mat + i * S.N;
     uint64_t run = 0;
-    for (uint32_t b = 0; b < S.nb; b++) {
-        const uint32_t j = b * 32 + lane;
-        uint64_t x = j < S.N ? row[j] : 0;
+    for (uint32_t b0 = 0; b0 < S.nb; b0 += 8) {  // eight 32-column blocks per pass, loads in flight together
+        uint64_t x[8];
 #pragma unroll
-        for (int o = 16; o > 0; o >>= 1) x += __shfl_xor_sync(0xffffffffu, x, o);
-        run += x;
-        if (lane == 0) S.blk[i * S.nb + b] = run;
+        for (int u = 0; u < 8; u++) {
+            const uint32_t j = (b0 + u) * 32 + lane;
+            x[u] = (b0 + u < S.nb && j < S.N) ? __ldg(row + j) : 0;
+        }
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) {
+#pragma unroll
+            for (int u = 0; u < 8; u++) x[u] += __shfl_xor_sync(0xffffffffu, x[u], o);
+        }
+#pragma unroll
+        for (int u = 0; u < 8; u++) {
+            run += x[u];
+            if (lane == u && b0 + u < S.nb) S.blk[i * S.nb + b0 + u] = run;
+        }
     }
     if (lane == 0) {
         S.rowpre[i] = run;
@@ -441,6 +452,71 @@ __global__ void __launch_bounds__(NT) quotient_kernel(const TaskDesc *__restrict
     }
 }
 
+// One CTA per group of `rows` consecutive output rows of one child, one warp per output row at a
+// time: the child's member lists are staged in shared memory once per CTA; a warp sums the member
+// rows of its output row into its own shared-memory row (lanes stride the columns with eight
+// independent loads in flight each), then gathers every output column through the member lists
+// and stores the row. No block-wide barrier inside the row loop. Shared memory: the lists, then
+// one N-entry row per warp.
+__global__ void __launch_bounds__(256) quotient_warp_kernel(const TaskDesc *__restrict__ tasks,
+                                                            const SrcDesc *__restrict__ srcs,
+                                                            const uint32_t *__restrict__ kdim,
+                                                            const uint64_t *__restrict__ group_task_off,
+                                                            uint32_t ntasks, uint32_t rows,
+                                                            const uint64_t *__restrict__ out_off, uint64_t *out_base,
+                                                            uint32_t stage_words) {
+    extern __shared__ __align__(16) unsigned char dsm[];
+    const uint64_t gg = blockIdx.x;
+    uint32_t lo = 0, hi = ntasks - 1;
+    while (lo < hi) {  // last task whose first row group <= gg
+        const uint32_t mid = (lo + hi + 1) >> 1;
+        if (group_task_off[mid] <= gg) lo = mid; else hi = mid - 1;
+    }
+    const TaskDesc T = tasks[lo];
+    const SrcDesc S = srcs[T.src];
+    const uint32_t k = kdim[lo];
+    const uint32_t N = S.N;
+    const uint32_t a0 = (uint32_t)(gg - group_task_off[lo]) * rows, a1 = min(k, a0 + rows);
+    uint32_t *s_moff = reinterpret_cast<uint32_t *>(dsm);  // k + 1
+    uint32_t *s_memb = s_moff + (k + 1);                     // N
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+    uint64_t *rs = reinterpret_cast<uint64_t *>(dsm) + stage_words / 2 + (size_t)warp * N;
+    for (uint32_t i = threadIdx.x; i <= k; i += blockDim.x) s_moff[i] = T.memb_off[i];
+    for (uint32_t i = threadIdx.x; i < N; i += blockDim.x) s_memb[i] = T.members[i];
+    __syncthreads();
+    uint64_t *Qt = out_base + out_off[lo];
+    for (uint32_t a = a0 + warp; a < a1; a += nw) {
+        const uint32_t p0 = s_moff[a], p1 = s_moff[a + 1];
+        for (uint32_t j0 = 0; j0 < N; j0 += 256) {
+            uint64_t x[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+            for (uint32_t p = p0; p < p1; p++) {
+                const uint64_t *row = S.mat + (uint64_t)s_memb[p] * N;
+#pragma unroll
+                for (int u = 0; u < 8; u++) {
+                    const uint32_t j = j0 + u * 32 + lane;
+                    if (j < N) x[u] += __ldg(row + j);
+                }
+            }
+#pragma unroll
+            for (int u = 0; u < 8; u++) {
+                const uint32_t j = j0 + u * 32 + lane;
+                if (j < N) rs[j] = x[u];
+            }
+        }
+        __syncwarp();
+        uint64_t *Q = Qt + (uint64_t)a * k;
+        for (uint32_t b = lane; b < k; b += 32) {
+            uint64_t acc = 0;
+            if (b != a) {
+                const uint32_t q1 = s_moff[b + 1];
+                for (uint32_t q = s_moff[b]; q < q1; q++) acc += rs[s_memb[q]];
+            }
+            Q[b] = acc;
+        }
+        __syncwarp();
+    }
+}
+
 // Exact minimum cut of one leaf (n <= 128) by one warp: maximum-adjacency orderings as in the
 // reference's Stoer-Wagner base case (co_mincut_base_case.hpp:52-144), with the Nagamochi-Ono-
 // Ibaraki contraction rule (Nagamochi & Ibaraki 1992; Nagamochi, Ono & Ibaraki 1994): when vertex
@@ -460,6 +536,28 @@ __device__ __forceinline__ uint64_t warp_min_u64(uint64_t x) {
     return ((uint64_t)top << 32) | lo;
 }
 
+// Circulant half storage of a symmetric N x N matrix with a zero diagonal: row i holds the entries
+// (i, (i + d) mod N) for d = 1 .. H, H = floor(N / 2), so every pair is stored once (twice when N
+// is even and d = N / 2; both copies are kept equal). A warp reading the entries (x, v) for its
+// lanes' v touches consecutive words for the v after x and words H - 1 apart for the v before x,
+// so neither half has bank conflicts; a 128-vertex leaf takes half the shared memory of the full
+// matrix and twice as many leaves are resident per SM.
+__device__ __forceinline__ uint32_t cpos(uint32_t i, uint32_t j, uint32_t N, uint32_t H) {
+    const uint32_t d = j >= i ? j - i : j + N - i;
+    return d <= H ? i * H + d - 1 : j * H + (N - d) - 1;
+}
+
+template <typename Tm>
+__device__ __forceinline__ void cset(Tm *M, uint32_t i, uint32_t j, uint32_t N, uint32_t H, Tm val) {
+    const uint32_t d = j >= i ? j - i : j + N - i;
+    if (d <= H) {
+        M[i * H + d - 1] = val;
+        if (d == H && !(N & 1u)) M[j * H + H - 1] = val;  // the twin of an even-N antipodal pair
+    } else {
+        M[j * H + (N - d) - 1] = val;
+    }
+}
+
 template <typename Tm>
 __global__ void __launch_bounds__(32) sw_leaf_kernel(const LeafDesc *__restrict__ leaves) {
     extern __shared__ __align__(16) unsigned char dsm[];
@@ -468,9 +566,13 @@ __global__ void __launch_bounds__(32) sw_leaf_kernel(const LeafDesc *__restrict_
     __shared__ uint32_t pairs[128];
     __shared__ uint32_t npairs;
     const LeafDesc L = leaves[blockIdx.x];
-    const uint32_t N = L.N;
+    const uint32_t N = L.N, H = N / 2;
     const int lane = threadIdx.x;
-    for (uint32_t x = lane; x < N * N; x += 32) M[x] = (Tm)L.mat[x];
+    for (uint32_t x = lane; x < N * H; x += 32) {
+        const uint32_t i = x / H, d = x - i * H + 1;
+        const uint32_t j = i + d < N ? i + d : i + d - N;
+        M[x] = (Tm)L.mat[(size_t)i * N + j];
+    }
     for (uint32_t x = lane; x < 128; x += 32) uf[x] = (uint8_t)x;
     __syncwarp();
     uint32_t active = 0;
@@ -482,9 +584,10 @@ __global__ void __launch_bounds__(32) sw_leaf_kernel(const LeafDesc *__restrict_
 #pragma unroll
     for (int s = 0; s < 4; s++) {
         if ((active >> s) & 1u) {
-            const Tm *row = M + (size_t)(lane + 32 * s) * N;
+            const uint32_t i = lane + 32 * s;
             uint64_t d = 0;
-            for (uint32_t x = 0; x < N; x++) d += (uint64_t)row[x];
+            for (uint32_t x = 0; x < N; x++)
+                if (x != i) d += (uint64_t)M[cpos(i, x, N, H)];
             deg_min = d < deg_min ? d : deg_min;
         }
     }
@@ -517,11 +620,10 @@ __global__ void __launch_bounds__(32) sw_leaf_kernel(const LeafDesc *__restrict_
             }
             if ((uint32_t)lane == (sv & 31u)) in_a |= 1u << (sv >> 5);
             prev = sv;
-            const Tm *row = M + (size_t)sv * N;
 #pragma unroll
             for (int s = 0; s < 4; s++) {
                 if (((active & ~in_a) >> s) & 1u) {
-                    const uint64_t c = (uint64_t)row[lane + 32 * s];
+                    const uint64_t c = (uint64_t)M[cpos(sv, lane + 32 * s, N, H)];
                     if (c) {
                         key[s] += c;
                         if (key[s] >= lambda) mark[s] = sv;  // lambda(sv, v) >= key: contractible
@@ -552,16 +654,13 @@ __global__ void __launch_bounds__(32) sw_leaf_kernel(const LeafDesc *__restrict_
             while (uf[x] != x) x = uf[x];
             while (uf[y] != y) y = uf[y];
             if (x == y) continue;  // already merged (warp-uniform)
-            // merge y into x: entry (x, v) += entry (y, v) for every other active v, both halves
-            Tm *rx = M + (size_t)x * N;
-            const Tm *ry = M + (size_t)y * N;
+            // merge y into x: entry (x, v) += entry (y, v) for every other active v
 #pragma unroll
             for (int s = 0; s < 4; s++) {
                 const uint32_t v = lane + 32 * s;
                 if (((active >> s) & 1u) && v != x && v != y) {
-                    const Tm val = rx[v] + ry[v];
-                    rx[v] = val;
-                    M[(size_t)v * N + x] = val;
+                    const Tm val = M[cpos(x, v, N, H)] + M[cpos(y, v, N, H)];
+                    cset(M, x, v, N, H, val);
                 }
             }
             if ((uint32_t)lane == (y & 31u)) active &= ~(1u << (y >> 5));
@@ -613,6 +712,7 @@ int upload(cac_ctx *ctx, DevBuf &buf, const std::vector<T> &v) {
     return CAC_OK;
 }
 
+size_t leaf_smem(uint32_t N, bool small) { return (size_t)N * (N / 2) * (small ? 4 : 8); }
 size_t contract_smem(uint32_t N) { return kBatch * sizeof(uint2) + (size_t)2 * N * 4; }
 size_t quotient_smem(uint32_t N) { return (size_t)N * 8; }
 
@@ -725,12 +825,12 @@ int KsEngine::step() {
             const uint32_t N = leaves[first].N;
             const LeafDesc *dl = d_leaf.as<LeafDesc>() + first;
             if (leaves[first].small) {
-                const size_t sm = (size_t)N * N * 4;
+                const size_t sm = leaf_smem(N, true);
                 CAC_CUDA_TRY(cudaFuncSetAttribute(sw_leaf_kernel<uint32_t>,
                                                   cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
                 sw_leaf_kernel<uint32_t><<<(unsigned)(last - first), 32, sm, s>>>(dl);
             } else {
-                const size_t sm = (size_t)N * N * 8;
+                const size_t sm = leaf_smem(N, false);
                 CAC_CUDA_TRY(cudaFuncSetAttribute(sw_leaf_kernel<uint64_t>,
                                                   cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
                 sw_leaf_kernel<uint64_t><<<(unsigned)(last - first), 32, sm, s>>>(dl);
@@ -846,16 +946,40 @@ int KsEngine::step() {
         groups += (k + qrows - 1) / qrows;
         if (k) qsm = std::max(qsm, quotient_smem(tasks[i].src.N));
     }
+    // warp-per-row quotient (8 warps) where three or more of its CTAs fit on an SM (lists + one
+    // row per warp within 80 KB, N up to about 1100), else the CTA-per-row-group kernel, whose
+    // 256 threads share one row and keep the SM occupied at large N
+    const size_t stage_words = (2 * (size_t)maxN + 2 + 3) & ~(size_t)3;  // k + 1 + N u32, 16-byte rounded
+    const uint32_t qwarps = stage_words * 4 + 8 * 8 * (size_t)maxN <= 80 * 1024 ? 8u : 0u;
+    const uint32_t wrows = qwarps * 4;
+    if (qwarps) {
+        groups = 0;
+        for (size_t i = 0; i < tasks.size(); i++) {
+            group_task_off[i] = groups;
+            groups += (kq[i] + wrows - 1) / wrows;
+        }
+    }
     MatBuf *out = nullptr;
     if (groups) {
         CAC_TRY(alloc(out_elems * 8, &out));
         CAC_TRY(upload(ctx_, d_qoff, out_off));
         CAC_TRY(upload(ctx_, d_gto, group_task_off));
         CAC_CUDA_TRY(cudaMemcpyAsync(d_kout.p, kq.data(), tasks.size() * 4, cudaMemcpyHostToDevice, s));
-        CAC_CUDA_TRY(cudaFuncSetAttribute(quotient_kernel<kQT>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)qsm));
-        quotient_kernel<kQT><<<(unsigned)groups, kQT, qsm, s>>>(
-            d_task.as<TaskDesc>(), d_src.as<SrcDesc>(), d_kout.as<uint32_t>(), d_gto.as<uint64_t>(),
-            (uint32_t)tasks.size(), qrows, d_qoff.as<uint64_t>(), static_cast<uint64_t *>(out->p));
+        if (qwarps) {
+            const size_t wsm = stage_words * 4 + (size_t)qwarps * maxN * 8;
+            CAC_CUDA_TRY(cudaFuncSetAttribute(quotient_warp_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                              (int)wsm));
+            quotient_warp_kernel<<<(unsigned)groups, qwarps * 32, wsm, s>>>(
+                d_task.as<TaskDesc>(), d_src.as<SrcDesc>(), d_kout.as<uint32_t>(), d_gto.as<uint64_t>(),
+                (uint32_t)tasks.size(), wrows, d_qoff.as<uint64_t>(), static_cast<uint64_t *>(out->p),
+                (uint32_t)stage_words);
+        } else {
+            CAC_CUDA_TRY(cudaFuncSetAttribute(quotient_kernel<kQT>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                              (int)qsm));
+            quotient_kernel<kQT><<<(unsigned)groups, kQT, qsm, s>>>(
+                d_task.as<TaskDesc>(), d_src.as<SrcDesc>(), d_kout.as<uint32_t>(), d_gto.as<uint64_t>(),
+                (uint32_t)tasks.size(), qrows, d_qoff.as<uint64_t>(), static_cast<uint64_t *>(out->p));
+        }
         CAC_CUDA_TRY(cudaGetLastError());
     }
     // the sources are read by everything enqueued above: their buffers may now be released
@@ -1135,12 +1259,12 @@ int exact_small(cac_ctx *ctx, uint32_t n, const uint64_t *mat_host, uint64_t *cu
     std::vector<LeafDesc> leaves{LeafDesc{buf.as<uint64_t>(), d_cuts.as<uint64_t>(), n, small}};
     CAC_TRY(upload(ctx, d_leaf, leaves));
     if (small) {
-        const size_t sm = (size_t)n * n * 4;
+        const size_t sm = leaf_smem(n, true);
         CAC_CUDA_TRY(cudaFuncSetAttribute(sw_leaf_kernel<uint32_t>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                           (int)sm));
         sw_leaf_kernel<uint32_t><<<1, 32, sm, s>>>(d_leaf.as<LeafDesc>());
     } else {
-        const size_t sm = (size_t)n * n * 8;
+        const size_t sm = leaf_smem(n, false);
         CAC_CUDA_TRY(cudaFuncSetAttribute(sw_leaf_kernel<uint64_t>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                           (int)sm));
         sw_leaf_kernel<uint64_t><<<1, 32, sm, s>>>(d_leaf.as<LeafDesc>());

@@ -329,6 +329,24 @@ int cac_graph_free(cac_graph *g) {
     return CAC_OK;
 }
 
+int cac_graph_copy_edges(const cac_graph *g, uint32_t *u, uint32_t *v, uint32_t *w, int where) {
+    if (!g || (where != CAC_HOST && where != CAC_DEVICE)) {
+        set_error("cac_graph_copy_edges: invalid argument");
+        return CAC_ERR_INVALID;
+    }
+    cac_ctx *ctx = g->ctx;
+    CAC_CUDA_TRY(cudaSetDevice(ctx->device));
+    const cudaMemcpyKind kind = where == CAC_DEVICE ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost;
+    const size_t b = g->m * 4;
+    if (b) {
+        if (u) CAC_CUDA_TRY(cudaMemcpyAsync(u, g->u, b, kind, ctx->stream));
+        if (v) CAC_CUDA_TRY(cudaMemcpyAsync(v, g->v, b, kind, ctx->stream));
+        if (w) CAC_CUDA_TRY(cudaMemcpyAsync(w, g->w, b, kind, ctx->stream));
+    }
+    CAC_CUDA_TRY(cudaStreamSynchronize(ctx->stream));
+    return CAC_OK;
+}
+
 int cac_graph_info(const cac_graph *g, uint32_t *n, uint64_t *m, uint64_t *total_weight) {
     if (!g) { set_error("cac_graph_info: graph is NULL"); return CAC_ERR_INVALID; }
     if (n) *n = g->n;

@@ -318,6 +318,18 @@ int cac_server_graph(cac_server *s, uint32_t n, uint64_t m, const uint32_t *u, c
     return CAC_OK;
 }
 
+int cac_server_generate(cac_server *s, const cac_gen_spec *spec, cac_graph **out) {
+    if (!s) {
+        set_error("cac_server_generate: server is NULL");
+        return CAC_ERR_INVALID;
+    }
+    std::lock_guard<std::mutex> lk(s->up_mu);
+    cudaSetDevice(s->up->device);
+    CAC_TRY(cac_graph_generate(s->up, spec, out));
+    CAC_CUDA_TRY(cudaStreamSynchronize(s->up->stream));
+    return CAC_OK;
+}
+
 int cac_server_submit(cac_server *s, const cac_request *req, uint64_t *ticket) {
     if (!s || !req || !ticket || !req->graph ||
         (req->kind != CAC_QUERY_MINCUT && req->kind != CAC_QUERY_APPROX && req->kind != CAC_QUERY_CC)) {

@@ -134,10 +134,10 @@ def barabasi_albert(n, m_attach, seed, permute=True):
     return n, u, v, w
 
 
-def rmat(scale, edge_factor, seed, a=0.57, b=0.19, c=0.19, chunk=1 << 22):
+def rmat(scale, edge_factor, seed, a=0.57, b=0.19, c=0.19, chunk=1 << 22, wmax=1, wmin=1):
     """R-MAT (Chakrabarti et al.): each of edge_factor * 2^scale edges picks one quadrant per
-    bit level with probabilities a, b, c, d = 1 - a - b - c. Isolated vertices are kept, so
-    n = 2^scale exactly. Unweighted."""
+    bit level with probabilities a, b, c, d = 1 - a - b - c (stream 100 + level). Isolated
+    vertices are kept, so n = 2^scale exactly. Unweighted unless wmax > 1."""
     n = 1 << scale
     m = edge_factor * n
     ta, tb, tc = _threshold(a), _threshold(a + b), _threshold(a + b + c)
@@ -155,7 +155,8 @@ def rmat(scale, edge_factor, seed, a=0.57, b=0.19, c=0.19, chunk=1 << 22):
             vv = (vv << np.uint32(1)) | bit_v
         u[s:s + len(idx)] = uu
         v[s:s + len(idx)] = vv
-    return n, u, v, np.ones(m, dtype=np.uint32)
+    w = weights(seed, m, wmax, wmin) if wmax > 1 else np.ones(m, dtype=np.uint32)
+    return n, u, v, w
 
 
 def watts_strogatz(n, k, p, seed, wmax=100, wmin=1):

@@ -84,6 +84,8 @@ int cac_graph_load_file(cac_ctx *ctx, const char *path, cac_graph **out);
 int cac_graph_from_edges(cac_ctx *ctx, uint32_t n, uint64_t m, const uint32_t *u, const uint32_t *v,
                          const uint32_t *w, int where, cac_graph **out);
 int cac_graph_free(cac_graph *g);
+/* Copy a graph's edge arrays (m entries each; any pointer may be NULL) to host or device memory. */
+int cac_graph_copy_edges(const cac_graph *graph, uint32_t *u, uint32_t *v, uint32_t *w, int where);
 int cac_graph_info(const cac_graph *g, uint32_t *n, uint64_t *m, uint64_t *total_weight);
 /* Parse an edge-list file into caller-provided host arrays (the file's m must be <= capacity). */
 int cac_parse_file(const char *path, uint32_t *n, uint64_t *m, uint32_t *u_host, uint32_t *v_host,
@@ -176,6 +178,31 @@ typedef struct {
 int cac_approx_cut(cac_ctx *ctx, const cac_graph *g, double success_probability, uint32_t seed,
                    uint32_t virtual_ranks, cac_approx_result *res);
 
+/* ---- synthetic graphs generated on the device ----
+ * Replaces the reference's external generators (utils/generate.py:10-32, er_generator.cpp,
+ * sw_generator.cpp, input_generators/rmat_driver.sh:13-16) for the benchmark families. The edge
+ * list (order included) and the weights are identical to graphgen.py's host generators for the
+ * same arguments. Weights are uniform integers in [wmin, wmax]; the G(n, p) and R-MAT families
+ * are unweighted (all 1) when wmax == 1. */
+#define CAC_GEN_ERDOS_RENYI 1   /* G(n, p): n, p */
+#define CAC_GEN_ERDOS_RENYI_M 2 /* G(n, M), M = floor(n * avg_degree / 2) draws, self-loops dropped: n, avg_degree */
+#define CAC_GEN_WATTS_STROGATZ 3 /* ring lattice of k neighbours (k even), rewired with probability p: n, k, p */
+#define CAC_GEN_RMAT 4          /* 2^scale vertices, edge_factor * 2^scale edges, quadrants a, b, c, 1-a-b-c */
+#define CAC_GEN_COMPLETE 5      /* K_n: n */
+typedef struct {
+    int family;
+    uint32_t n;
+    double p;
+    double avg_degree;
+    uint32_t k;
+    uint32_t scale;
+    uint32_t edge_factor;
+    double a, b, c;
+    uint32_t seed;
+    uint32_t wmin, wmax;
+} cac_gen_spec;
+int cac_graph_generate(cac_ctx *ctx, const cac_gen_spec *spec, cac_graph **out);
+
 /* ---- serving loop ----
  * The reference answers one query per process launch. A cac_server keeps graphs resident in HBM
  * and answers square_root, approx_cut and parallel_cc queries as they arrive:
@@ -222,6 +249,8 @@ int cac_server_create(const cac_server_config *config, cac_server **out);
  * arrays); free it with cac_graph_free after its last query has finished. */
 int cac_server_graph(cac_server *server, uint32_t n, uint64_t m, const uint32_t *u, const uint32_t *v,
                      const uint32_t *w, cac_graph **out);
+/* A generated graph (cac_graph_generate) for the server's queries. */
+int cac_server_generate(cac_server *server, const cac_gen_spec *spec, cac_graph **out);
 int cac_server_submit(cac_server *server, const cac_request *request, uint64_t *ticket);
 /* CAC_OK with *response filled (the ticket is then retired), CAC_PENDING when wait == 0 and the
  * query has not finished, CAC_ERR_INVALID for an unknown ticket. */
