@@ -14,12 +14,19 @@ namespace cac {
 
 // Thread-local last-error message (cac_last_error).
 void set_error(const std::string &msg);
+inline const char *src_base(const char *path) {
+    const char *b = path;
+    for (const char *c = path; *c; c++)
+        if (*c == '/') b = c + 1;
+    return b;
+}
 
 #define CAC_CUDA_TRY(expr)                                                                        \
     do {                                                                                          \
         cudaError_t _e = (expr);                                                                  \
         if (_e != cudaSuccess) {                                                                  \
-            ::cac::set_error(std::string(#expr) + ": " + cudaGetErrorString(_e));                 \
+            ::cac::set_error(std::string(#expr) + ": " + cudaGetErrorString(_e) + " (" +          \
+                             ::cac::src_base(__FILE__) + ":" + std::to_string(__LINE__) + ")");   \
             return CAC_ERR_CUDA;                                                                  \
         }                                                                                         \
     } while (0)
@@ -83,6 +90,16 @@ struct cac_graph {
 
 namespace cac {
 
+// Raise a kernel's dynamic shared-memory limit to the device's opt-in maximum, once per device.
+// The limit belongs to the function, process-wide: setting it per launch to that launch's size
+// would break a concurrent launch of the same kernel with a larger size from another thread, so
+// it is only ever raised.
+int smem_optin(cac_ctx *ctx, const void *func);
+template <typename F>
+inline int smem_optin(cac_ctx *ctx, F *func) {
+    return smem_optin(ctx, reinterpret_cast<const void *>(func));
+}
+
 // Device memory accounting against the ctx budget.
 int dev_alloc(cac_ctx *ctx, void **p, size_t bytes);
 void dev_free(cac_ctx *ctx, void *p, size_t bytes);
@@ -130,6 +147,7 @@ struct KNode {
     uint32_t query;    // owner query (engine bookkeeping)
     const uint64_t *mat;
     MatBuf *buf;
+    uint64_t *pre = nullptr;  // row sums (N) + 32-column block prefixes (N x ceil(N/32)), when made with the matrix
 };
 
 // A child being contracted from `src` (round > 0: continuing on the quotient of earlier rounds).
@@ -163,7 +181,8 @@ class KsEngine {
     cac_ctx *ctx_;
     std::vector<KNode> nodes_;
     std::vector<KTask> carried_;
-    void *d_src_, *d_task_, *d_leaf_, *d_rowoff_, *d_kout_, *d_prep_, *d_tscratch_, *d_qoff_, *d_gto_, *d_err_;
+    bool release_err_ = false;
+    void *d_src_, *d_task_, *d_leaf_, *d_rowoff_, *d_kout_, *d_prep_, *d_tscratch_, *d_qoff_, *d_gto_, *d_err_, *d_psrc_;
 };
 
 struct MincutQuery {
@@ -174,6 +193,11 @@ struct MincutQuery {
 // Stage 1 and Stage 2 of one query into a running engine: its trial cuts start at 2^64 - 1 and
 // its root nodes carry engine query id `query`; the query is done when outstanding[query] is 0.
 int mincut_admit_query(cac_ctx *ctx, KsEngine &eng, const MincutQuery &q, uint32_t query);
+// Stage 1 of B trials (keys k0[b], idx[b]) of a graph with more than 16384 vertices in global
+// memory (shrink_big.cu): labels to d_lab[b * n ..], vertices left to d_kout[b].
+uint64_t shrink_big_scratch(uint32_t n, uint64_t m, uint32_t B);
+int shrink_big(cac_ctx *ctx, const cac_graph *g, uint32_t target, uint32_t B, const uint32_t *k0, const uint32_t *idx,
+               uint32_t *d_lab, uint32_t *d_kout, void *scratch);
 // All trials of all queries through one engine, admitted as memory allows.
 int mincut_run_queries(cac_ctx *ctx, std::vector<MincutQuery> &queries, float *device_ms);
 int mincut_trials(cac_ctx *ctx, const cac_graph *g, uint32_t seed, uint32_t ranks, uint32_t per_rank,

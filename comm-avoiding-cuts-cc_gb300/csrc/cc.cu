@@ -693,8 +693,8 @@ int cc_run(cac_ctx *ctx, uint32_t n, uint64_t m, const uint32_t *d_u, const uint
     L.h_ranks = hr;
     if (L.draws > 0 && m > 0) {
         const int sm = (int)((size_t)std::min(L.nwords, kSmemBitmapWords) * 4);
-        CAC_CUDA_TRY(cudaFuncSetAttribute(cc_filter<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, sm));
-        CAC_CUDA_TRY(cudaFuncSetAttribute(cc_filter<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, sm));
+        CAC_TRY(smem_optin(ctx, cc_filter<true>));
+        CAC_TRY(smem_optin(ctx, cc_filter<false>));
     }
 
     // Repeated identical queries replay a captured CUDA graph: one launch instead of a dozen

@@ -82,7 +82,7 @@ struct TaskDesc {
     uint32_t target;
     uint32_t round;
     uint32_t k0, idx;     // stream key words 0, 1
-    uint32_t pad;
+    uint32_t pad;         // 1: the graph's total weight is below 2^32 (every entry fits 32 bits)
 };
 
 struct LeafDesc {
@@ -144,6 +144,67 @@ __device__ __forceinline__ uint32_t sfind_ro(const uint32_t *par, uint32_t x) {
     return x;
 }
 
+// Contract the draw pairs sb[0, nb) into the shared-memory union-find `par` (roots are component
+// minima) in draw order until *s_count reaches target -- the sequential rule of the trial.
+// Fast path: every thread links its draws concurrently (CAS of the larger root onto the smaller,
+// finds without compression) and logs each successful link; a successful CAS always joins two
+// different components, so the number of links is the exact count drop, and when the count stays
+// above target the partition equals the sequential one. Otherwise the logged links are undone
+// (only roots were written, so this restores `par` exactly) and thread 0 replays the batch in
+// draw order, stopping at target. Afterwards every endpoint of the batch points at its root.
+// s_log: nb entries of shared memory; s_nlog: one shared counter.
+template <int NT>
+__device__ void contract_batch(uint32_t *par, const uint2 *sb, uint32_t nb, uint32_t target, uint32_t *s_count,
+                               uint32_t *s_log, uint32_t *s_nlog) {
+    volatile uint32_t *vp = par;
+    const uint32_t c0 = *s_count;
+    __syncthreads();
+    if (threadIdx.x == 0) *s_nlog = 0;
+    __syncthreads();
+    for (uint32_t j = threadIdx.x; j < nb; j += NT) {
+        uint32_t a = sb[j].x, b = sb[j].y;
+        for (;;) {
+            while (vp[a] != a) a = vp[a];
+            while (vp[b] != b) b = vp[b];
+            if (a == b) break;
+            const uint32_t hi = a > b ? a : b, lo = a > b ? b : a;
+            if (atomicCAS(&par[hi], hi, lo) == hi) {
+                s_log[atomicAdd(s_nlog, 1u)] = hi;
+                break;
+            }
+            a = hi;  // hi was linked meanwhile: find both roots again
+            b = lo;
+        }
+    }
+    __syncthreads();
+    const uint32_t links = *s_nlog;
+    if (c0 - links > target) {
+        for (uint32_t j = threadIdx.x; j < nb; j += NT) {  // point the endpoints at their roots
+            const uint32_t a = sb[j].x, b = sb[j].y;
+            par[a] = sfind_ro(par, a);
+            par[b] = sfind_ro(par, b);
+        }
+        __syncthreads();
+        if (threadIdx.x == 0) *s_count = c0 - links;
+        __syncthreads();
+        return;
+    }
+    for (uint32_t i = threadIdx.x; i < links; i += NT) par[s_log[i]] = s_log[i];
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        uint32_t c = c0;
+        for (uint32_t j = 0; j < nb && c > target; j++) {
+            const uint32_t a = sfind(par, sb[j].x), b = sfind(par, sb[j].y);
+            if (a != b) {
+                if (a < b) par[b] = a; else par[a] = b;
+                c--;
+            }
+        }
+        *s_count = c;
+    }
+    __syncthreads();
+}
+
 // first index i in [0, len) with a[i] > y (a non-decreasing, a[len-1] > y)
 __device__ __forceinline__ uint64_t upper_bound_u64(const uint64_t *a, uint64_t len, uint64_t y) {
     uint64_t lo = 0, hi = len - 1;
@@ -181,8 +242,9 @@ template <int NT>
 __global__ void __launch_bounds__(NT) iss_shrink_kernel(const ShrinkDesc *__restrict__ descs) {
     extern __shared__ __align__(16) unsigned char dsm[];
     uint2 *sb = reinterpret_cast<uint2 *>(dsm);
-    uint32_t *par = reinterpret_cast<uint32_t *>(dsm + kBatch * sizeof(uint2));
-    __shared__ uint32_t s_count;
+    uint32_t *s_log = reinterpret_cast<uint32_t *>(dsm + kBatch * sizeof(uint2));
+    uint32_t *par = s_log + kBatch;
+    __shared__ uint32_t s_count, s_nlog;
     const ShrinkDesc D = descs[blockIdx.x];
     const uint32_t n = D.n, target = D.target;
     const uint64_t m = D.m;
@@ -217,18 +279,7 @@ __global__ void __launch_bounds__(NT) iss_shrink_kernel(const ShrinkDesc *__rest
                 sb[j] = make_uint2(U[e], V[e]);
             }
             __syncthreads();
-            if (threadIdx.x == 0) {
-                uint32_t c = s_count;
-                for (uint32_t j = 0; j < nb && c > target; j++) {
-                    const uint32_t a = sfind(par, sb[j].x), b = sfind(par, sb[j].y);
-                    if (a != b) {
-                        if (a < b) par[b] = a; else par[a] = b;
-                        c--;
-                    }
-                }
-                s_count = c;
-            }
-            __syncthreads();
+            contract_batch<NT>(par, sb, nb, target, &s_count, s_log, &s_nlog);
             if (s_count <= target) break;
         }
         for (uint32_t v = threadIdx.x; v < n; v += NT) par[v] = sfind_ro(par, v);
@@ -318,11 +369,12 @@ __global__ void __launch_bounds__(NT) contract_kernel(const TaskDesc *__restrict
                                                       uint32_t *err) {
     extern __shared__ __align__(16) unsigned char dsm[];
     uint2 *sb = reinterpret_cast<uint2 *>(dsm);
-    __shared__ uint32_t s_count;
+    __shared__ uint32_t s_count, s_nlog;
     const TaskDesc T = tasks[blockIdx.x];
     const SrcDesc S = srcs[T.src];
     const uint32_t N = S.N;
-    uint32_t *par = reinterpret_cast<uint32_t *>(dsm + kBatch * sizeof(uint2));
+    uint32_t *s_log = reinterpret_cast<uint32_t *>(dsm + kBatch * sizeof(uint2));
+    uint32_t *par = s_log + kBatch;
     uint32_t *cnt = par + N;  // counting-sort counters, N entries
     const uint64_t W = S.rowpre[N - 1];
     if (W == 0) {  // no edges between the vertices: the cut is 0, nothing to contract
@@ -359,18 +411,7 @@ __global__ void __launch_bounds__(NT) contract_kernel(const TaskDesc *__restrict
             sb[j] = make_uint2(a, b * 32 + c);
         }
         __syncthreads();
-        if (threadIdx.x == 0) {
-            uint32_t cc = s_count;
-            for (uint32_t j = 0; j < nb && cc > T.target; j++) {
-                const uint32_t x = sfind(par, sb[j].x), y = sfind(par, sb[j].y);
-                if (x != y) {
-                    if (x < y) par[y] = x; else par[x] = y;
-                    cc--;
-                }
-            }
-            s_count = cc;
-        }
-        __syncthreads();
+        contract_batch<NT>(par, sb, nb, T.target, &s_count, s_log, &s_nlog);
         if (s_count <= T.target) break;
     }
     for (uint32_t v = threadIdx.x; v < N; v += NT) par[v] = sfind_ro(par, v);
@@ -458,6 +499,7 @@ __global__ void __launch_bounds__(NT) quotient_kernel(const TaskDesc *__restrict
 // independent loads in flight each), then gathers every output column through the member lists
 // and stores the row. No block-wide barrier inside the row loop. Shared memory: the lists, then
 // one N-entry row per warp.
+template <typename Ts>
 __global__ void __launch_bounds__(256) quotient_warp_kernel(const TaskDesc *__restrict__ tasks,
                                                             const SrcDesc *__restrict__ srcs,
                                                             const uint32_t *__restrict__ kdim,
@@ -465,6 +507,7 @@ __global__ void __launch_bounds__(256) quotient_warp_kernel(const TaskDesc *__re
                                                             uint32_t ntasks, uint32_t rows,
                                                             const uint64_t *__restrict__ out_off, uint64_t *out_base,
                                                             uint32_t stage_words) {
+    // out_off[ntasks + i]: where task i's row sums and block prefixes go (the next step's row prep)
     extern __shared__ __align__(16) unsigned char dsm[];
     const uint64_t gg = blockIdx.x;
     uint32_t lo = 0, hi = ntasks - 1;
@@ -480,11 +523,16 @@ __global__ void __launch_bounds__(256) quotient_warp_kernel(const TaskDesc *__re
     uint32_t *s_moff = reinterpret_cast<uint32_t *>(dsm);  // k + 1
     uint32_t *s_memb = s_moff + (k + 1);                     // N
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
-    uint64_t *rs = reinterpret_cast<uint64_t *>(dsm) + stage_words / 2 + (size_t)warp * N;
+    // Ts: uint32_t when every task of the launch has total weight below 2^32 (member-row sums fit)
+    Ts *rs = reinterpret_cast<Ts *>(dsm + (size_t)stage_words * 4) + (size_t)warp * N;
     for (uint32_t i = threadIdx.x; i <= k; i += blockDim.x) s_moff[i] = T.memb_off[i];
     for (uint32_t i = threadIdx.x; i < N; i += blockDim.x) s_memb[i] = T.members[i];
     __syncthreads();
     uint64_t *Qt = out_base + out_off[lo];
+    uint64_t *rowsum_out = out_base + out_off[ntasks + lo];
+    const bool small = T.pad != 0;  // the graph's total weight is below 2^32
+    const uint32_t nbk = (k + 31) / 32;
+    uint64_t *blk = rowsum_out + k;
     for (uint32_t a = a0 + warp; a < a1; a += nw) {
         const uint32_t p0 = s_moff[a], p1 = s_moff[a + 1];
         for (uint32_t j0 = 0; j0 < N; j0 += 256) {
@@ -500,19 +548,44 @@ __global__ void __launch_bounds__(256) quotient_warp_kernel(const TaskDesc *__re
 #pragma unroll
             for (int u = 0; u < 8; u++) {
                 const uint32_t j = j0 + u * 32 + lane;
-                if (j < N) rs[j] = x[u];
+                if (j < N) rs[j] = (Ts)x[u];
             }
         }
         __syncwarp();
         uint64_t *Q = Qt + (uint64_t)a * k;
-        for (uint32_t b = lane; b < k; b += 32) {
-            uint64_t acc = 0;
-            if (b != a) {
-                const uint32_t q1 = s_moff[b + 1];
-                for (uint32_t q = s_moff[b]; q < q1; q++) acc += rs[s_memb[q]];
+        uint64_t run = 0;
+        for (uint32_t b0 = 0; b0 < k; b0 += 128) {  // four 32-column blocks per pass (warp-uniform trip count)
+            uint64_t acc[4];
+#pragma unroll
+            for (int u = 0; u < 4; u++) {  // four independent gather chains in flight
+                const uint32_t b = b0 + 32 * u + lane;
+                acc[u] = 0;
+                if (b < k && b != a) {
+                    const uint32_t q1 = s_moff[b + 1];
+                    for (uint32_t q = s_moff[b]; q < q1; q++) acc[u] += rs[s_memb[q]];
+                }
+                if (b < k) Q[b] = acc[u];
             }
-            Q[b] = acc;
+#pragma unroll
+            for (int u = 0; u < 4; u++) {
+                if (small) {  // every entry < 2^32: two 32-bit reductions of the 16-bit halves are exact
+                    const uint32_t lo16 = __reduce_add_sync(0xffffffffu, (uint32_t)(acc[u] & 0xFFFFu));
+                    const uint32_t hi16 = __reduce_add_sync(0xffffffffu, (uint32_t)(acc[u] >> 16));
+                    acc[u] = (uint64_t)lo16 + ((uint64_t)hi16 << 16);
+                } else {
+#pragma unroll
+                    for (int o = 16; o > 0; o >>= 1) acc[u] += __shfl_xor_sync(0xffffffffu, acc[u], o);
+                }
+            }
+#pragma unroll
+            for (int u = 0; u < 4; u++) {
+                if (b0 + 32 * u < k) {
+                    run += acc[u];
+                    if (lane == u) blk[(uint64_t)a * nbk + (b0 >> 5) + u] = run;
+                }
+            }
         }
+        if (lane == 0) rowsum_out[a] = run;
         __syncwarp();
     }
 }
@@ -713,7 +786,7 @@ int upload(cac_ctx *ctx, DevBuf &buf, const std::vector<T> &v) {
 }
 
 size_t leaf_smem(uint32_t N, bool small) { return (size_t)N * (N / 2) * (small ? 4 : 8); }
-size_t contract_smem(uint32_t N) { return kBatch * sizeof(uint2) + (size_t)2 * N * 4; }
+size_t contract_smem(uint32_t N) { return kBatch * (sizeof(uint2) + 4) + (size_t)2 * N * 4; }
 size_t quotient_smem(uint32_t N) { return (size_t)N * 8; }
 
 }  // namespace
@@ -723,7 +796,7 @@ size_t quotient_smem(uint32_t N) { return (size_t)N * 8; }
 KsEngine::KsEngine(cac_ctx *ctx)
     : ctx_(ctx), d_src_(new DevBuf(ctx)), d_task_(new DevBuf(ctx)), d_leaf_(new DevBuf(ctx)),
       d_rowoff_(new DevBuf(ctx)), d_kout_(new DevBuf(ctx)), d_prep_(new DevBuf(ctx)), d_tscratch_(new DevBuf(ctx)),
-      d_qoff_(new DevBuf(ctx)), d_gto_(new DevBuf(ctx)), d_err_(new DevBuf(ctx)) {}
+      d_qoff_(new DevBuf(ctx)), d_gto_(new DevBuf(ctx)), d_err_(new DevBuf(ctx)), d_psrc_(new DevBuf(ctx)) {}
 
 KsEngine::~KsEngine() {
     cudaStreamSynchronize(ctx_->stream);
@@ -731,7 +804,7 @@ KsEngine::~KsEngine() {
     for (const KTask &t : carried_) release(t.src.buf);
     nodes_.clear();
     carried_.clear();
-    for (void *b : {d_src_, d_task_, d_leaf_, d_rowoff_, d_kout_, d_prep_, d_tscratch_, d_qoff_, d_gto_, d_err_})
+    for (void *b : {d_src_, d_task_, d_leaf_, d_rowoff_, d_kout_, d_prep_, d_tscratch_, d_qoff_, d_gto_, d_err_, d_psrc_})
         delete static_cast<DevBuf *>(b);
 }
 
@@ -775,7 +848,14 @@ int KsEngine::alloc(size_t bytes, MatBuf **out) {
 void KsEngine::release(MatBuf *b) {
     if (!b) return;
     if (--b->refs > 0) return;
-    cudaFreeAsync(b->p, ctx_->stream);
+    if (b->refs < 0) {  // released more often than referenced: keep it, report at the next step
+        release_err_ = true;
+        return;
+    }
+    if (cudaFreeAsync(b->p, ctx_->stream) != cudaSuccess) {
+        cudaGetLastError();  // reported through the engine's error state, not as a sticky CUDA error
+        release_err_ = true;
+    }
     ctx_->held -= std::min<uint64_t>(ctx_->held, b->bytes);
     delete b;
 }
@@ -789,11 +869,15 @@ void KsEngine::add(const KNode &nd) {
 
 int KsEngine::step() {
     cudaStream_t s = ctx_->stream;
+    if (release_err_) {
+        set_error("Karger-Stein engine: a level buffer was released more often than referenced or could not be freed");
+        return CAC_ERR_CUDA;
+    }
     DevBuf &d_src = *static_cast<DevBuf *>(d_src_), &d_task = *static_cast<DevBuf *>(d_task_);
     DevBuf &d_leaf = *static_cast<DevBuf *>(d_leaf_), &d_rowoff = *static_cast<DevBuf *>(d_rowoff_);
     DevBuf &d_kout = *static_cast<DevBuf *>(d_kout_), &d_prep = *static_cast<DevBuf *>(d_prep_);
     DevBuf &d_tscratch = *static_cast<DevBuf *>(d_tscratch_), &d_qoff = *static_cast<DevBuf *>(d_qoff_);
-    DevBuf &d_gto = *static_cast<DevBuf *>(d_gto_);
+    DevBuf &d_gto = *static_cast<DevBuf *>(d_gto_), &d_psrc = *static_cast<DevBuf *>(d_psrc_);
     uint32_t *d_err = static_cast<DevBuf *>(d_err_)->as<uint32_t>();
     std::vector<MatBuf *> consumed;
 
@@ -826,13 +910,11 @@ int KsEngine::step() {
             const LeafDesc *dl = d_leaf.as<LeafDesc>() + first;
             if (leaves[first].small) {
                 const size_t sm = leaf_smem(N, true);
-                CAC_CUDA_TRY(cudaFuncSetAttribute(sw_leaf_kernel<uint32_t>,
-                                                  cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
+                CAC_TRY(smem_optin(ctx_, sw_leaf_kernel<uint32_t>));
                 sw_leaf_kernel<uint32_t><<<(unsigned)(last - first), 32, sm, s>>>(dl);
             } else {
                 const size_t sm = leaf_smem(N, false);
-                CAC_CUDA_TRY(cudaFuncSetAttribute(sw_leaf_kernel<uint64_t>,
-                                                  cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
+                CAC_TRY(smem_optin(ctx_, sw_leaf_kernel<uint64_t>));
                 sw_leaf_kernel<uint64_t><<<(unsigned)(last - first), 32, sm, s>>>(dl);
             }
             first = last;
@@ -861,14 +943,17 @@ int KsEngine::step() {
         for (MatBuf *b : consumed) release(b);
         return CAC_OK;
     }
-    std::vector<SrcDesc> srcs(src_nodes.size());
-    std::vector<uint64_t> row_off(src_nodes.size());
+    // sources whose row sums and block prefixes came with their matrix (warp quotient) skip the
+    // row prep; the others (roots, large-N quotients) are prepped here from their own list
+    std::vector<SrcDesc> srcs(src_nodes.size()), psrcs;
+    std::vector<uint64_t> row_off;
     uint64_t rows = 0, prep_elems = 0;
     for (size_t i = 0; i < src_nodes.size(); i++) {
+        if (src_nodes[i].pre) continue;
         const uint32_t nb = (src_nodes[i].N + 31) / 32;
         prep_elems += src_nodes[i].N + (uint64_t)src_nodes[i].N * nb;
     }
-    CAC_TRY(d_prep.ensure(prep_elems * 8));
+    CAC_TRY(d_prep.ensure(std::max<uint64_t>(prep_elems, 1) * 8));
     uint64_t pe = 0;
     for (size_t i = 0; i < src_nodes.size(); i++) {
         const KNode &nd = src_nodes[i];
@@ -876,20 +961,28 @@ int KsEngine::step() {
         S.mat = nd.mat;
         S.N = nd.N;
         S.nb = (nd.N + 31) / 32;
-        S.rowpre = d_prep.as<uint64_t>() + pe;
-        S.blk = S.rowpre + nd.N;
         S.cut = nd.cut;
         S.is_root = nd.is_root;
         S.pad = 0;
-        pe += nd.N + (uint64_t)nd.N * S.nb;
-        row_off[i] = rows;
-        rows += nd.N;
+        if (nd.pre) {
+            S.rowpre = nd.pre;
+        } else {
+            S.rowpre = d_prep.as<uint64_t>() + pe;
+            pe += nd.N + (uint64_t)nd.N * S.nb;
+            row_off.push_back(rows);
+            rows += nd.N;
+        }
+        S.blk = S.rowpre + nd.N;
+        if (!nd.pre) psrcs.push_back(S);
     }
     CAC_TRY(upload(ctx_, d_src, srcs));
-    CAC_TRY(upload(ctx_, d_rowoff, row_off));
-    prep_rows_kernel<<<(unsigned)((rows * 32 + 255) / 256), 256, 0, s>>>(d_src.as<SrcDesc>(),
-                                                                         d_rowoff.as<uint64_t>(),
-                                                                         (uint32_t)srcs.size(), rows);
+    if (rows) {
+        CAC_TRY(upload(ctx_, d_rowoff, row_off));
+        CAC_TRY(upload(ctx_, d_psrc, psrcs));
+        prep_rows_kernel<<<(unsigned)((rows * 32 + 255) / 256), 256, 0, s>>>(d_psrc.as<SrcDesc>(),
+                                                                             d_rowoff.as<uint64_t>(),
+                                                                             (uint32_t)row_off.size(), rows);
+    }
     prefix_rows_kernel<kNT><<<(unsigned)srcs.size(), kNT, 0, s>>>(d_src.as<SrcDesc>());
 
     // contraction of every child
@@ -912,7 +1005,7 @@ int KsEngine::step() {
         d.round = t.round;
         d.k0 = t.src.k0;
         d.idx = t.src.idx;
-        d.pad = 0;
+        d.pad = t.src.small;  // entries (and row sums) below 2^32
         d.lab = d_tscratch.as<uint32_t>() + ts;
         d.members = d.lab + t.src.N;
         d.memb_off = d.members + t.src.N;
@@ -922,7 +1015,7 @@ int KsEngine::step() {
     CAC_TRY(d_kout.ensure(tasks.size() * 4));
     {
         const size_t sm = contract_smem(maxN);
-        CAC_CUDA_TRY(cudaFuncSetAttribute(contract_kernel<kNT>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
+        CAC_TRY(smem_optin(ctx_, contract_kernel<kNT>));
         contract_kernel<kNT><<<(unsigned)tasks.size(), kNT, sm, s>>>(d_task.as<TaskDesc>(), d_src.as<SrcDesc>(),
                                                                      d_kout.as<uint32_t>(), d_err);
         CAC_CUDA_TRY(cudaGetLastError());
@@ -950,13 +1043,20 @@ int KsEngine::step() {
     // row per warp within 80 KB, N up to about 1100), else the CTA-per-row-group kernel, whose
     // 256 threads share one row and keep the SM occupied at large N
     const size_t stage_words = (2 * (size_t)maxN + 2 + 3) & ~(size_t)3;  // k + 1 + N u32, 16-byte rounded
-    const uint32_t qwarps = stage_words * 4 + 8 * 8 * (size_t)maxN <= 80 * 1024 ? 8u : 0u;
+    bool all_small = true;
+    for (const KTask &t : tasks) all_small = all_small && t.src.small;
+    const size_t rs_bytes = all_small ? 4 : 8;
+    const uint32_t qwarps = stage_words * 4 + 8 * rs_bytes * (size_t)maxN <= 80 * 1024 ? 8u : 0u;
     const uint32_t wrows = qwarps * 4;
     if (qwarps) {
         groups = 0;
+        // after the matrices: each child's row sums and block prefixes, written by the warp kernel
+        out_off.resize(2 * tasks.size());
         for (size_t i = 0; i < tasks.size(); i++) {
             group_task_off[i] = groups;
             groups += (kq[i] + wrows - 1) / wrows;
+            out_off[tasks.size() + i] = out_elems;
+            out_elems += kq[i] + (uint64_t)kq[i] * ((kq[i] + 31) / 32);
         }
     }
     MatBuf *out = nullptr;
@@ -966,16 +1066,15 @@ int KsEngine::step() {
         CAC_TRY(upload(ctx_, d_gto, group_task_off));
         CAC_CUDA_TRY(cudaMemcpyAsync(d_kout.p, kq.data(), tasks.size() * 4, cudaMemcpyHostToDevice, s));
         if (qwarps) {
-            const size_t wsm = stage_words * 4 + (size_t)qwarps * maxN * 8;
-            CAC_CUDA_TRY(cudaFuncSetAttribute(quotient_warp_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                              (int)wsm));
-            quotient_warp_kernel<<<(unsigned)groups, qwarps * 32, wsm, s>>>(
+            const size_t wsm = stage_words * 4 + (size_t)qwarps * maxN * rs_bytes;
+            auto kern = all_small ? quotient_warp_kernel<uint32_t> : quotient_warp_kernel<uint64_t>;
+            CAC_TRY(smem_optin(ctx_, kern));
+            kern<<<(unsigned)groups, qwarps * 32, wsm, s>>>(
                 d_task.as<TaskDesc>(), d_src.as<SrcDesc>(), d_kout.as<uint32_t>(), d_gto.as<uint64_t>(),
                 (uint32_t)tasks.size(), wrows, d_qoff.as<uint64_t>(), static_cast<uint64_t *>(out->p),
                 (uint32_t)stage_words);
         } else {
-            CAC_CUDA_TRY(cudaFuncSetAttribute(quotient_kernel<kQT>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                              (int)qsm));
+            CAC_TRY(smem_optin(ctx_, quotient_kernel<kQT>));
             quotient_kernel<kQT><<<(unsigned)groups, kQT, qsm, s>>>(
                 d_task.as<TaskDesc>(), d_src.as<SrcDesc>(), d_kout.as<uint32_t>(), d_gto.as<uint64_t>(),
                 (uint32_t)tasks.size(), qrows, d_qoff.as<uint64_t>(), static_cast<uint64_t *>(out->p));
@@ -994,6 +1093,7 @@ int KsEngine::step() {
         nd.N = k;
         nd.is_root = 0;
         nd.mat = static_cast<uint64_t *>(out->p) + out_off[i];
+        nd.pre = qwarps ? static_cast<uint64_t *>(out->p) + out_off[tasks.size() + i] : nullptr;
         nd.buf = out;
         out->refs++;
         outstanding[nd.query]++;
@@ -1054,19 +1154,19 @@ int admit(cac_ctx *ctx, KsEngine &eng, const QueryPlan &q) {
         eng.release(root);
         return CAC_OK;
     }
-    if (n > kMaxSmemVertices) {
-        set_error("graphs with more than 16384 vertices that need sparse pre-contraction are not supported yet");
-        return CAC_ERR_UNSUPPORTED;
-    }
-    // Stage 1 in chunks whose scratch (prefix array + labels per trial) stays within 4 GB
-    const uint64_t per_trial = 8 * std::max<uint64_t>(m, 1) + 4 * (uint64_t)n + 64;
+    // Stage 1 in chunks whose scratch stays within 4 GB: shared-memory union-find per trial up to
+    // 16384 vertices, the global-memory rounds of shrink_big.cu above
+    const bool big = n > kMaxSmemVertices;
+    const uint64_t per_trial = big ? shrink_big_scratch(n, m, 1) + 4ull * n
+                                   : 8 * std::max<uint64_t>(m, 1) + 4 * (uint64_t)n + 64;
     const uint64_t chunk = std::max<uint64_t>(1, std::min<uint64_t>({q.trials, (4ull << 30) / per_trial, (uint64_t)65535}));
     DevBuf d_pre(ctx), d_lab(ctx), d_k(ctx), d_sd(ctx), d_dd(ctx);
-    const size_t sm = kBatch * sizeof(uint2) + (size_t)n * 4;
-    CAC_CUDA_TRY(cudaFuncSetAttribute(iss_shrink_kernel<kNT>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
+    const size_t sm = kBatch * (sizeof(uint2) + 4) + (size_t)std::min(n, kMaxSmemVertices) * 4;
+    if (!big)
+        CAC_TRY(smem_optin(ctx, iss_shrink_kernel<kNT>));
     for (uint64_t c0 = 0; c0 < q.trials; c0 += chunk) {
         const uint32_t B = (uint32_t)std::min<uint64_t>(chunk, q.trials - c0);
-        CAC_TRY(d_pre.ensure((size_t)B * std::max<uint64_t>(m, 1) * 8));
+        CAC_TRY(d_pre.ensure(big ? shrink_big_scratch(n, m, B) : (size_t)B * std::max<uint64_t>(m, 1) * 8));
         CAC_TRY(d_lab.ensure((size_t)B * n * 4));
         CAC_TRY(d_k.ensure((size_t)B * 4));
         std::vector<ShrinkDesc> sd(B);
@@ -1085,12 +1185,29 @@ int admit(cac_ctx *ctx, KsEngine &eng, const QueryPlan &q) {
             D.k0 = q.seed + (uint32_t)(i / q.per_rank);
             D.idx = (uint32_t)(i % q.per_rank);
         }
-        CAC_TRY(upload(ctx, d_sd, sd));
-        iss_shrink_kernel<kNT><<<B, kNT, sm, s>>>(d_sd.as<ShrinkDesc>());
-        CAC_CUDA_TRY(cudaGetLastError());
+        if (big) {
+            std::vector<uint32_t> k0(B), idx(B);
+            for (uint32_t b = 0; b < B; b++) {
+                k0[b] = sd[b].k0;
+                idx[b] = sd[b].idx;
+            }
+            CAC_TRY(shrink_big(ctx, g, q.t, B, k0.data(), idx.data(), d_lab.as<uint32_t>(), d_k.as<uint32_t>(), d_pre.p));
+        } else {
+            CAC_TRY(upload(ctx, d_sd, sd));
+            iss_shrink_kernel<kNT><<<B, kNT, sm, s>>>(d_sd.as<ShrinkDesc>());
+            CAC_CUDA_TRY(cudaGetLastError());
+        }
         std::vector<uint32_t> kdim(B);
         CAC_CUDA_TRY(cudaMemcpyAsync(kdim.data(), d_k.p, (size_t)B * 4, cudaMemcpyDeviceToHost, s));
         CAC_CUDA_TRY(cudaStreamSynchronize(s));
+        // more than 16384 vertices left only when Stage 1 stopped with no edge between them
+        // (a disconnected graph): every vertex is isolated and the trial's cut is exactly 0
+        std::vector<uint8_t> isolated(B, 0);
+        for (uint32_t b = 0; b < B; b++)
+            if (kdim[b] > kMaxSmemVertices) {
+                isolated[b] = 1;
+                kdim[b] = 0;
+            }
         uint64_t elems = 0;
         for (uint32_t b = 0; b < B; b++) elems += (uint64_t)kdim[b] * kdim[b];
         MatBuf *roots = nullptr;
@@ -1099,7 +1216,9 @@ int admit(cac_ctx *ctx, KsEngine &eng, const QueryPlan &q) {
         std::vector<DenseDesc> dd(B);
         uint64_t off = 0;
         for (uint32_t b = 0; b < B; b++) {
-            dd[b] = DenseDesc{g->u, g->v, g->w, sd[b].lab, static_cast<uint64_t *>(roots->p) + off, m, kdim[b], 0};
+            // no scatter for a trial without a matrix (its labels would index past the buffer)
+            dd[b] = DenseDesc{g->u, g->v, g->w, sd[b].lab, static_cast<uint64_t *>(roots->p) + off,
+                              kdim[b] >= 2 ? m : 0, kdim[b], 0};
             off += (uint64_t)kdim[b] * kdim[b];
         }
         CAC_TRY(upload(ctx, d_dd, dd));
@@ -1112,7 +1231,7 @@ int admit(cac_ctx *ctx, KsEngine &eng, const QueryPlan &q) {
         for (uint32_t b = 0; b < B; b++) {
             const uint64_t i = c0 + b;
             if (kdim[b] < 2) {
-                // a single vertex left: no cut edge
+                // a single vertex left, or only isolated vertices: no cut edge
                 fill_u64<<<1, 32, 0, s>>>(q.cuts + i, 1, 0);
                 continue;
             }
@@ -1260,13 +1379,11 @@ int exact_small(cac_ctx *ctx, uint32_t n, const uint64_t *mat_host, uint64_t *cu
     CAC_TRY(upload(ctx, d_leaf, leaves));
     if (small) {
         const size_t sm = leaf_smem(n, true);
-        CAC_CUDA_TRY(cudaFuncSetAttribute(sw_leaf_kernel<uint32_t>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                          (int)sm));
+        CAC_TRY(smem_optin(ctx, sw_leaf_kernel<uint32_t>));
         sw_leaf_kernel<uint32_t><<<1, 32, sm, s>>>(d_leaf.as<LeafDesc>());
     } else {
         const size_t sm = leaf_smem(n, false);
-        CAC_CUDA_TRY(cudaFuncSetAttribute(sw_leaf_kernel<uint64_t>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                          (int)sm));
+        CAC_TRY(smem_optin(ctx, sw_leaf_kernel<uint64_t>));
         sw_leaf_kernel<uint64_t><<<1, 32, sm, s>>>(d_leaf.as<LeafDesc>());
     }
     CAC_CUDA_TRY(cudaGetLastError());

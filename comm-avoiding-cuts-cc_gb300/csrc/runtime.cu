@@ -1,5 +1,9 @@
 // libcac runtime: contexts, device memory accounting, graphs and the C ABI entry points.
 #include "cac_internal.h"
+
+#include <mutex>
+#include <set>
+#include <utility>
 #include "sitmo.cuh"
 
 #include <algorithm>
@@ -12,6 +16,21 @@ namespace cac {
 static thread_local std::string g_last_error;
 
 void set_error(const std::string &msg) { g_last_error = msg; }
+
+int smem_optin(cac_ctx *ctx, const void *func) {
+    static std::mutex mu;
+    static std::set<std::pair<int, const void *>> raised;
+    std::lock_guard<std::mutex> lk(mu);
+    if (raised.count({ctx->device, func})) return CAC_OK;
+    int optin = 0;
+    CAC_CUDA_TRY(cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, ctx->device));
+    cudaFuncAttributes fa{};
+    CAC_CUDA_TRY(cudaFuncGetAttributes(&fa, func));
+    CAC_CUDA_TRY(cudaFuncSetAttribute(func, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                      optin - (int)fa.sharedSizeBytes));
+    raised.insert({ctx->device, func});
+    return CAC_OK;
+}
 
 int dev_alloc(cac_ctx *ctx, void **p, size_t bytes) {
     *p = nullptr;
@@ -34,7 +53,10 @@ int dev_alloc(cac_ctx *ctx, void **p, size_t bytes) {
 
 void dev_free(cac_ctx *ctx, void *p, size_t bytes) {
     if (!p) return;
-    cudaFree(p);
+    if (cudaFree(p) != cudaSuccess) {
+        const cudaError_t e = cudaGetLastError();  // not left behind as a sticky error for an unrelated check
+        set_error(std::string("cudaFree: ") + cudaGetErrorString(e));
+    }
     ctx->held -= std::min<uint64_t>(ctx->held, bytes);
 }
 

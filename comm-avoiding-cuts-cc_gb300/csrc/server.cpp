@@ -289,8 +289,9 @@ int cac_server_create(const cac_server_config *config, cac_server **out) {
     auto *s = new cac_server();
     s->budget = cfg.hbm_budget_bytes;
     cac_config c{cfg.device, nullptr, 0};
+    cac_config cc{cfg.device, nullptr, cfg.hbm_budget_bytes};  // the engine's buffers count against the budget
     int st = cac_ctx_create(&c, &s->up);
-    if (st == CAC_OK) st = cac_ctx_create(&c, &s->cut);
+    if (st == CAC_OK) st = cac_ctx_create(&cc, &s->cut);
     if (st == CAC_OK) st = cac_ctx_create(&c, &s->graph);
     if (st != CAC_OK) {
         cac_ctx_destroy(s->graph);

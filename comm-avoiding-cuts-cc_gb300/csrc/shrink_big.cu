@@ -1,0 +1,446 @@
+// Stage 1 of square_root trials on graphs with more than 16384 vertices (the union-find no longer
+// fits one SM's shared memory). Same trial rule as iss_shrink_kernel in mincut.cu and as the
+// reference's SequentialSquareRootCut::iteratedSampling (src/SequentialSquareRootCut.cpp:21-67):
+// rounds of (vertex count) weighted draws over the edges that are not loops at the start of the
+// round, contracted in draw order until exactly `target` vertices remain, vertices renamed to the
+// rank of their smallest member. Here every trial of a chunk runs as grid-wide kernels over
+// global memory:
+//   big_edge_tiles   per 1024-edge tile: non-loop weights, their inclusive prefix inside the tile
+//                    and the tile total (u, v, w read as 16-byte vectors)
+//   big_tile_scan    per trial: inclusive prefix of the tile totals -> the round's total weight
+//   big_draws        per draw: the selected edge by a binary search over the tile prefix, then
+//                    inside the tile
+//   big_link         draws [lo, mid) linked concurrently into the union-find (CAS of the larger
+//                    root onto the smaller, finds without compression), every link logged; a
+//                    successful CAS always joins two components, so the link count is the exact
+//                    drop of the vertex count
+//   big_decide       per trial: keep the links if the count stays above target, otherwise undo
+//                    them; bisection over the draw prefix finds the draw at which the sequential
+//                    rule stops (the first attempt is the whole round, which is kept in every
+//                    round but the last)
+//   big_undo / big_apply_one   undo logged links; apply the single stopping draw
+//   big_compress     every vertex points at its root (roots are component minima)
+//   big_root_count / big_vscan / big_label_roots / big_label_rest   rank-of-minimum labels
+// The host steps rounds until every trial is done (its count reached target, or no edge is left
+// between its vertices); a fixed number of bisection iterations per round is enough because each
+// one halves the open draw range.
+#include "cac_internal.h"
+#include "sitmo.cuh"
+
+#include <algorithm>
+#include <vector>
+
+namespace cac {
+namespace {
+
+constexpr int kBT = 256;         // threads per block
+constexpr uint32_t kET = 1024;   // edges per tile (4 per thread)
+constexpr uint32_t kVT = 1024;   // vertices per tile (4 per thread)
+constexpr uint32_t kPhaseOpen = 0, kPhaseRoundDone = 2;
+
+struct BigTrial {
+    uint32_t *par;    // n
+    uint64_t *pre;    // m: inclusive prefix of non-loop weights inside each edge tile
+    uint64_t *tsum;   // edge tiles: tile totals, then their inclusive prefix
+    uint2 *draws;     // n
+    uint32_t *log;    // n
+    uint32_t *lab;    // n (output)
+    uint32_t *vsum;   // vertex tiles: root counts, then exclusive offsets
+    uint32_t *k_out;  // output: vertices left
+    uint32_t k0, idx; // stream key words 0, 1
+};
+
+struct BigState {
+    uint64_t W;
+    uint32_t count, ndraw, lo, hi, mid, nlog, undo_n, apply_one, round, done, phase, err;
+};
+
+struct BigGraph {
+    const uint32_t *U, *V, *Wt;
+    uint64_t m;
+    uint32_t n, target;
+    uint32_t etiles, vtiles;
+};
+
+template <int NT>
+__device__ __forceinline__ uint64_t bscan_u64(uint64_t x, uint64_t &total) {
+    __shared__ uint64_t ws[NT / 32];
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    uint64_t inc = x;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        const uint64_t y = __shfl_up_sync(0xffffffffu, inc, o);
+        if (lane >= o) inc += y;
+    }
+    if (lane == 31) ws[wid] = inc;
+    __syncthreads();
+    if (wid == 0) {
+        uint64_t s = lane < NT / 32 ? ws[lane] : 0;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const uint64_t y = __shfl_up_sync(0xffffffffu, s, o);
+            if (lane >= o) s += y;
+        }
+        if (lane < NT / 32) ws[lane] = s;
+    }
+    __syncthreads();
+    total = ws[NT / 32 - 1];
+    const uint64_t off = wid ? ws[wid - 1] : 0;
+    __syncthreads();
+    return off + inc - x;
+}
+
+__device__ __forceinline__ uint64_t ub_u64(const uint64_t *a, uint64_t len, uint64_t y) {
+    uint64_t lo = 0, hi = len - 1;  // first i with a[i] > y; a[len - 1] > y
+    while (lo < hi) {
+        const uint64_t mid = (lo + hi) >> 1;
+        if (a[mid] > y) hi = mid; else lo = mid + 1;
+    }
+    return lo;
+}
+
+__device__ __forceinline__ uint32_t groot(const uint32_t *par, uint32_t x) {
+    const volatile uint32_t *vp = par;
+    uint32_t p;
+    while ((p = vp[x]) != x) x = p;
+    return x;
+}
+
+__global__ void big_init(const BigTrial *T, BigState *st, BigGraph G) {
+    const uint32_t b = blockIdx.y;
+    uint32_t *par = T[b].par;
+    for (uint32_t v = blockIdx.x * blockDim.x + threadIdx.x; v < G.n; v += gridDim.x * blockDim.x) par[v] = v;
+    if (blockIdx.x == 0 && threadIdx.x == 0) {
+        BigState s{};
+        s.count = G.n;
+        s.done = G.n <= G.target ? 1u : 0u;
+        s.phase = kPhaseRoundDone;
+        st[b] = s;
+    }
+}
+
+__global__ void __launch_bounds__(kBT) big_edge_tiles(const BigTrial *T, const BigState *st, BigGraph G) {
+    const uint32_t b = blockIdx.y;
+    if (st[b].done) return;
+    const uint32_t *par = T[b].par;
+    const uint64_t e0 = (uint64_t)blockIdx.x * kET + threadIdx.x * 4;
+    uint32_t u[4], v[4], w[4];
+    if (e0 + 3 < G.m) {
+        const uint4 uu = *reinterpret_cast<const uint4 *>(G.U + e0);
+        const uint4 vv = *reinterpret_cast<const uint4 *>(G.V + e0);
+        const uint4 ww = *reinterpret_cast<const uint4 *>(G.Wt + e0);
+        u[0] = uu.x; u[1] = uu.y; u[2] = uu.z; u[3] = uu.w;
+        v[0] = vv.x; v[1] = vv.y; v[2] = vv.z; v[3] = vv.w;
+        w[0] = ww.x; w[1] = ww.y; w[2] = ww.z; w[3] = ww.w;
+    } else {
+#pragma unroll
+        for (int k = 0; k < 4; k++) {
+            const bool in = e0 + k < G.m;
+            u[k] = in ? G.U[e0 + k] : 0;
+            v[k] = in ? G.V[e0 + k] : 0;
+            w[k] = in ? G.Wt[e0 + k] : 0;
+        }
+    }
+    uint64_t x[4], local = 0;
+#pragma unroll
+    for (int k = 0; k < 4; k++) {
+        x[k] = (w[k] && par[u[k]] != par[v[k]]) ? w[k] : 0;
+        local += x[k];
+    }
+    uint64_t tot;
+    uint64_t acc = bscan_u64<kBT>(local, tot);
+    uint64_t *pre = T[b].pre;
+#pragma unroll
+    for (int k = 0; k < 4; k++) {
+        acc += x[k];
+        if (e0 + k < G.m) pre[e0 + k] = acc;
+    }
+    if (threadIdx.x == 0) T[b].tsum[blockIdx.x] = tot;
+}
+
+__global__ void __launch_bounds__(1024) big_tile_scan(const BigTrial *T, BigState *st, BigGraph G) {
+    const uint32_t b = blockIdx.x;
+    if (st[b].done) return;
+    uint64_t *ts = T[b].tsum;
+    uint64_t carry = 0;
+    for (uint32_t base = 0; base < G.etiles; base += 1024) {
+        const uint32_t i = base + threadIdx.x;
+        const uint64_t x = i < G.etiles ? ts[i] : 0;
+        uint64_t tot;
+        const uint64_t ex = bscan_u64<1024>(x, tot);
+        if (i < G.etiles) ts[i] = carry + ex + x;
+        carry += tot;
+    }
+    if (threadIdx.x == 0) {
+        BigState &s = st[b];
+        s.W = carry;
+        if (carry == 0) {  // no edge left between the vertices: the trial keeps its count
+            s.done = 1;
+            s.phase = kPhaseRoundDone;
+        } else {
+            s.ndraw = s.count;
+            s.lo = 0;
+            s.hi = s.count;
+            s.mid = s.count;
+            s.nlog = 0;
+            s.undo_n = 0;
+            s.apply_one = 0;
+            s.phase = kPhaseOpen;
+        }
+    }
+}
+
+__global__ void __launch_bounds__(kBT) big_draws(const BigTrial *T, const BigState *st, BigGraph G) {
+    const uint32_t b = blockIdx.y;
+    const BigState s = st[b];
+    if (s.done) return;
+    const BigTrial t = T[b];
+    for (uint32_t j = blockIdx.x * kBT + threadIdx.x; j < s.ndraw; j += gridDim.x * kBT) {
+        const uint64_t y = mulhi64(draw64(t.k0, t.idx, 1, 0, s.round, j), s.W);
+        const uint32_t tile = (uint32_t)ub_u64(t.tsum, G.etiles, y);
+        const uint64_t base = tile ? t.tsum[tile - 1] : 0;
+        const uint64_t e0 = (uint64_t)tile * kET;
+        const uint64_t len = min((uint64_t)kET, G.m - e0);
+        const uint64_t e = e0 + ub_u64(t.pre + e0, len, y - base);
+        t.draws[j] = make_uint2(G.U[e], G.V[e]);
+    }
+}
+
+__global__ void __launch_bounds__(kBT) big_link(const BigTrial *T, BigState *st) {
+    const uint32_t b = blockIdx.y;
+    const BigState s = st[b];
+    if (s.done || s.phase != kPhaseOpen) return;
+    const BigTrial t = T[b];
+    for (uint32_t j = s.lo + blockIdx.x * kBT + threadIdx.x; j < s.mid; j += gridDim.x * kBT) {
+        uint32_t x = t.draws[j].x, y = t.draws[j].y;
+        for (;;) {
+            x = groot(t.par, x);
+            y = groot(t.par, y);
+            if (x == y) break;
+            const uint32_t hi = max(x, y), lo = min(x, y);
+            if (atomicCAS(&t.par[hi], hi, lo) == hi) {
+                t.log[atomicAdd(&st[b].nlog, 1u)] = hi;
+                break;
+            }
+            x = hi;  // hi was linked meanwhile: find both roots again
+            y = lo;
+        }
+    }
+}
+
+__global__ void big_decide(BigState *st, uint32_t B, uint32_t target) {
+    const uint32_t b = blockIdx.x * blockDim.x + threadIdx.x;
+    if (b >= B) return;
+    BigState &s = st[b];
+    if (s.done || s.phase != kPhaseOpen) return;
+    const uint32_t links = s.nlog;
+    s.nlog = 0;
+    if (s.count - links > target) {  // keep: the sequential rule would not stop inside [lo, mid)
+        s.count -= links;
+        s.lo = s.mid;
+        s.undo_n = 0;
+        if (s.lo == s.hi) {
+            if (s.hi == s.ndraw) s.phase = kPhaseRoundDone;  // the whole round was applied
+            else s.err = 1;  // cannot happen: [lo, hi) is known to reach target
+        } else {
+            s.mid = s.lo + max(1u, (s.hi - s.lo) / 2);
+        }
+    } else {  // the stop lies inside [lo, mid): undo, then search the lower half
+        s.undo_n = links;
+        s.hi = s.mid;
+        if (s.hi - s.lo == 1) s.apply_one = 1;  // draw lo alone reaches target
+        else s.mid = s.lo + (s.hi - s.lo) / 2;
+    }
+}
+
+__global__ void __launch_bounds__(kBT) big_undo(const BigTrial *T, const BigState *st) {
+    const uint32_t b = blockIdx.y;
+    const uint32_t n = st[b].undo_n;
+    if (!n) return;
+    const BigTrial t = T[b];
+    for (uint32_t i = blockIdx.x * kBT + threadIdx.x; i < n; i += gridDim.x * kBT) t.par[t.log[i]] = t.log[i];
+}
+
+__global__ void big_apply_one(const BigTrial *T, BigState *st, uint32_t B, uint32_t target) {
+    const uint32_t b = blockIdx.x * blockDim.x + threadIdx.x;
+    if (b >= B) return;
+    BigState &s = st[b];
+    s.undo_n = 0;
+    if (!s.apply_one) return;
+    s.apply_one = 0;
+    const BigTrial t = T[b];
+    const uint32_t x = groot(t.par, t.draws[s.lo].x), y = groot(t.par, t.draws[s.lo].y);
+    if (x != y) {
+        t.par[max(x, y)] = min(x, y);
+        s.count -= 1;
+    }
+    if (s.count != target) s.err = 1;  // cannot happen: this draw was shown to reach target
+    s.done = 1;
+    s.phase = kPhaseRoundDone;
+}
+
+__global__ void big_compress(const BigTrial *T, BigGraph G) {
+    const uint32_t b = blockIdx.y;
+    uint32_t *par = T[b].par;
+    for (uint32_t v = blockIdx.x * blockDim.x + threadIdx.x; v < G.n; v += gridDim.x * blockDim.x)
+        par[v] = groot(par, v);
+}
+
+__global__ void big_round_end(BigState *st, uint32_t B, uint32_t target, uint32_t *active) {
+    const uint32_t b = blockIdx.x * blockDim.x + threadIdx.x;
+    if (b >= B) return;
+    BigState &s = st[b];
+    if (!s.done && s.phase != kPhaseRoundDone) s.err = 1;  // bisection did not close
+    s.round += 1;
+    if (s.count <= target) s.done = 1;
+    if (!s.done) atomicAdd(active, 1u);
+}
+
+__global__ void __launch_bounds__(kBT) big_root_count(const BigTrial *T, BigGraph G) {
+    const uint32_t b = blockIdx.y;
+    const uint32_t *par = T[b].par;
+    const uint32_t v0 = blockIdx.x * kVT + threadIdx.x * 4;
+    uint32_t c = 0;
+#pragma unroll
+    for (int k = 0; k < 4; k++) c += (v0 + k < G.n && par[v0 + k] == v0 + k) ? 1u : 0u;
+    c = __reduce_add_sync(0xffffffffu, c);
+    __shared__ uint32_t ws[kBT / 32];
+    if ((threadIdx.x & 31) == 0) ws[threadIdx.x >> 5] = c;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        uint32_t s = 0;
+        for (int i = 0; i < kBT / 32; i++) s += ws[i];
+        T[b].vsum[blockIdx.x] = s;
+    }
+}
+
+__global__ void __launch_bounds__(1024) big_vscan(const BigTrial *T, const BigState *st, BigGraph G) {
+    const uint32_t b = blockIdx.x;
+    uint32_t *vs = T[b].vsum;
+    uint64_t carry = 0;
+    for (uint32_t base = 0; base < G.vtiles; base += 1024) {
+        const uint32_t i = base + threadIdx.x;
+        const uint64_t x = i < G.vtiles ? vs[i] : 0;
+        uint64_t tot;
+        const uint64_t ex = bscan_u64<1024>(x, tot);
+        if (i < G.vtiles) vs[i] = (uint32_t)(carry + ex);
+        carry += tot;
+    }
+    if (threadIdx.x == 0) *T[b].k_out = (uint32_t)carry;
+}
+
+__global__ void __launch_bounds__(kBT) big_label_roots(const BigTrial *T, BigGraph G) {
+    const uint32_t b = blockIdx.y;
+    const BigTrial t = T[b];
+    const uint32_t v0 = blockIdx.x * kVT + threadIdx.x * 4;
+    uint32_t f[4], c = 0;
+#pragma unroll
+    for (int k = 0; k < 4; k++) {
+        f[k] = (v0 + k < G.n && t.par[v0 + k] == v0 + k) ? 1u : 0u;
+        c += f[k];
+    }
+    uint64_t tot;
+    uint32_t r = t.vsum[blockIdx.x] + (uint32_t)bscan_u64<kBT>(c, tot);
+#pragma unroll
+    for (int k = 0; k < 4; k++)
+        if (f[k]) t.lab[v0 + k] = r++;
+}
+
+__global__ void big_label_rest(const BigTrial *T, BigGraph G) {
+    const uint32_t b = blockIdx.y;
+    const BigTrial t = T[b];
+    for (uint32_t v = blockIdx.x * blockDim.x + threadIdx.x; v < G.n; v += gridDim.x * blockDim.x) {
+        const uint32_t r = t.par[v];
+        if (r != v) t.lab[v] = t.lab[r];
+    }
+}
+
+}  // namespace
+
+// Scratch of shrink_big for B trials, carved in the order shrink_big takes it.
+uint64_t shrink_big_scratch(uint32_t n, uint64_t m, uint32_t B) {
+    const uint64_t etiles = (m + kET - 1) / kET, vtiles = ((uint64_t)n + kVT - 1) / kVT;
+    const uint64_t per = align_up(4ull * n) + align_up(8 * std::max<uint64_t>(m, 1)) +
+                         align_up(8 * std::max<uint64_t>(etiles, 1)) + align_up(8ull * n) + align_up(4ull * n) +
+                         align_up(4 * vtiles);
+    return per * B + align_up(sizeof(BigTrial) * B) + align_up(sizeof(BigState) * B) + align_up(16);
+}
+
+int shrink_big(cac_ctx *ctx, const cac_graph *g, uint32_t target, uint32_t B, const uint32_t *k0, const uint32_t *idx,
+               uint32_t *d_lab, uint32_t *d_kout, void *scratch) {
+    cudaStream_t s = ctx->stream;
+    const uint32_t n = g->n;
+    const uint64_t m = g->m;
+    BigGraph G{g->u, g->v, g->w, m, n, target, (uint32_t)((m + kET - 1) / kET), (uint32_t)((n + kVT - 1) / kVT)};
+    std::vector<BigTrial> T(B);
+    char *p = static_cast<char *>(scratch);
+    auto take = [&](size_t bytes) {
+        char *q = p;
+        p += align_up(bytes);
+        return q;
+    };
+    for (uint32_t b = 0; b < B; b++) {
+        BigTrial &t = T[b];
+        t.par = reinterpret_cast<uint32_t *>(take(4ull * n));
+        t.pre = reinterpret_cast<uint64_t *>(take(8 * std::max<uint64_t>(m, 1)));
+        t.tsum = reinterpret_cast<uint64_t *>(take(8ull * std::max<uint32_t>(G.etiles, 1)));
+        t.draws = reinterpret_cast<uint2 *>(take(8ull * n));
+        t.log = reinterpret_cast<uint32_t *>(take(4ull * n));
+        t.vsum = reinterpret_cast<uint32_t *>(take(4ull * G.vtiles));
+        t.lab = d_lab + (size_t)b * n;
+        t.k_out = d_kout + b;
+        t.k0 = k0[b];
+        t.idx = idx[b];
+    }
+    BigTrial *dT = reinterpret_cast<BigTrial *>(take(sizeof(BigTrial) * B));
+    BigState *dS = reinterpret_cast<BigState *>(take(sizeof(BigState) * B));
+    uint32_t *d_active = reinterpret_cast<uint32_t *>(take(16));
+    CAC_CUDA_TRY(cudaMemcpyAsync(dT, T.data(), sizeof(BigTrial) * B, cudaMemcpyHostToDevice, s));
+    const uint32_t vgrid = std::max(1u, std::min<uint32_t>((n + kBT - 1) / kBT, 2048u / std::max(1u, B / 8 + 1)));
+    big_init<<<dim3(vgrid, B), kBT, 0, s>>>(dT, dS, G);
+    const uint32_t dgrid = std::max(1u, std::min<uint32_t>((n + kBT - 1) / kBT, 4096u / B + 1));
+    uint32_t iters = 3;
+    while ((1ull << (iters - 3)) < n) iters++;  // ceil(log2 n) + 3 bisection steps close every round
+    const unsigned tb = (B + 31) / 32;
+    for (uint32_t round = 0;; round++) {
+        if (round > n) {  // every round with edges left links at least its first draw
+            set_error("Stage 1: more sampling rounds than vertices");
+            return CAC_ERR_CUDA;
+        }
+        if (m) {
+            big_edge_tiles<<<dim3(G.etiles, B), kBT, 0, s>>>(dT, dS, G);
+            big_tile_scan<<<B, 1024, 0, s>>>(dT, dS, G);
+            big_draws<<<dim3(dgrid, B), kBT, 0, s>>>(dT, dS, G);
+            for (uint32_t it = 0; it < iters; it++) {
+                big_link<<<dim3(dgrid, B), kBT, 0, s>>>(dT, dS);
+                big_decide<<<tb, 32, 0, s>>>(dS, B, target);
+                big_undo<<<dim3(dgrid, B), kBT, 0, s>>>(dT, dS);
+                big_apply_one<<<tb, 32, 0, s>>>(dT, dS, B, target);
+            }
+        }
+        big_compress<<<dim3(vgrid, B), kBT, 0, s>>>(dT, G);
+        CAC_CUDA_TRY(cudaMemsetAsync(d_active, 0, 4, s));
+        big_round_end<<<tb, 32, 0, s>>>(dS, B, target, d_active);
+        CAC_CUDA_TRY(cudaGetLastError());
+        uint32_t active = 0;
+        CAC_CUDA_TRY(cudaMemcpyAsync(&active, d_active, 4, cudaMemcpyDeviceToHost, s));
+        CAC_CUDA_TRY(cudaStreamSynchronize(s));
+        if (!active || !m) break;
+    }
+    std::vector<BigState> hs(B);
+    CAC_CUDA_TRY(cudaMemcpyAsync(hs.data(), dS, sizeof(BigState) * B, cudaMemcpyDeviceToHost, s));
+    CAC_CUDA_TRY(cudaStreamSynchronize(s));
+    for (const BigState &x : hs)
+        if (x.err) {
+            set_error("Stage 1: inconsistent contraction state");
+            return CAC_ERR_CUDA;
+        }
+    big_root_count<<<dim3(G.vtiles, B), kBT, 0, s>>>(dT, G);
+    big_vscan<<<B, 1024, 0, s>>>(dT, dS, G);
+    big_label_roots<<<dim3(G.vtiles, B), kBT, 0, s>>>(dT, G);
+    big_label_rest<<<dim3(vgrid, B), kBT, 0, s>>>(dT, G);
+    CAC_CUDA_TRY(cudaGetLastError());
+    return CAC_OK;
+}
+
+}  // namespace cac

@@ -211,6 +211,9 @@ int cac_graph_generate(cac_ctx *ctx, const cac_gen_spec *spec, cac_graph **out);
  *     while the estimated footprint of the running queries stays within hbm_budget_bytes
  *     (0: no limit);
  *   - parallel_cc and approx_cut queries run on a second worker and stream, concurrently.
+ * The Karger-Stein engine's device buffers count against hbm_budget_bytes: a query whose matrices
+ * cannot fit fails alone with CAC_ERR_OOM (a failure inside a shared engine step ends every query
+ * running in it with that step's error).
  * Every response equals what the single-query entry point returns for the same arguments
  * (cac_mincut cut and trials_per_rank, cac_approx_cut cut and trials, cac_cc count and labels).
  * Submit and poll may be called from any threads. A graph must outlive the queries on it. */

@@ -121,3 +121,42 @@ def test_rejects_single_vertex(ctx, libcac):
     with pytest.raises(libcac.CacError) as e:
         g.square_root(0.95, 0)
     assert e.value.status == -1
+
+
+# Stage 1 of graphs with more than 16384 vertices runs in global memory (shrink_big.cu); every
+# trial still equals the oracle's replay of the same counter stream.
+def _ring_plus_er(n, deg, seed):
+    """A weighted ring (connected, no isolated vertex) plus G(n, M) edges."""
+    _, u, v, w = graphgen.erdos_renyi_m(n, deg, seed, wmax=100)
+    ring = np.arange(n, dtype=np.uint32)
+    rw = graphgen.weights(seed + 1, n, 60, 20)
+    return n, np.concatenate([ring, u]), np.concatenate([(ring + 1) % n, v]).astype(np.uint32), np.concatenate([rw, w])
+
+
+@pytest.mark.parametrize("spec", [
+    ("ring_er", 20000, 6.0, 3),  # t ~ 500: bisection of the last round's draws
+    ("ring_er", 40000, 3.0, 4),  # sparser, more rounds
+    ("ws", 17000, 4, 5),         # ring lattice, rewired: long paths
+])
+def test_large_graph_trials_match_replay(ctx, spec):
+    if spec[0] == "ring_er":
+        n, u, v, w = _ring_plus_er(spec[1], spec[2], spec[3])
+    else:
+        n, u, v, w = graphgen.watts_strogatz(spec[1], spec[2], 0.3, spec[3], wmax=100)
+    g = ctx.graph(n, u, v, w)
+    got = g.trials(seed=9, virtual_ranks=2, trials_per_rank=2)
+    for r in range(2):
+        for i in range(2):
+            assert int(got[r, i]) == O.mincut_trial(n, u, v, w, 9, r, i), (spec, r, i)
+
+
+def test_large_disconnected_graph_trials(ctx):
+    # 30000 vertices, edges only among the first 2000: Stage 1 stops with every remaining edge a
+    # loop and more than 16384 vertices left; the cut is 0, as in the replay
+    n0, u, v, w = graphgen.erdos_renyi_m(2000, 10.0, 6, wmax=50)
+    n = 30000
+    g = ctx.graph(n, u, v, w)
+    got = g.trials(seed=1, virtual_ranks=1, trials_per_rank=3)
+    for i in range(3):
+        assert int(got[0, i]) == O.mincut_trial(n, u, v, w, 1, 0, i) == 0
+    assert g.square_root(0.5, seed=1).cut == 0

@@ -81,10 +81,21 @@ def test_mixed_stream_matches_single_queries(libcac, ctx):
             assert expect[i][0] == count and np.array_equal(expect[i][1], labels)
 
 
+def _estimate(n, m, p):
+    """The server's admission estimate of one square_root query (roots and two more levels)."""
+    t = O.intermediate_size(n, m)
+    trials = O.number_of_trials(n, m, p)
+    tt = min(t, n)
+    return (trials if t < n else 1) * tt * tt * 8 * 3 + trials * 8
+
+
 def test_small_budget_serialises_but_keeps_values(libcac, ctx):
     specs = _graphs()[:3]
     singles = [ctx.graph(*s) for s in specs]
-    with libcac.Server(0, hbm_budget_bytes=1) as srv:  # every query is admitted alone
+    est = [_estimate(n, len(u), 0.95) for n, u, _, _ in specs]
+    budget = max(est) + (1 << 20)  # each query fits alone, not all together
+    assert sum(est) > budget
+    with libcac.Server(0, hbm_budget_bytes=budget) as srv:
         sg = [srv.graph(*s) for s in specs]
         tickets = [srv.submit("square_root", g, 0.95, seed=i) for i, g in enumerate(sg)]
         for i, t in enumerate(tickets):
@@ -108,12 +119,28 @@ def test_poll_without_wait_and_unknown_ticket(libcac):
             srv.submit("square_root", g, 1.5)
 
 
-def test_unsupported_query_fails_alone(libcac):
-    # more than 16384 vertices with sparse pre-contraction: refused at admission on the host,
-    # reported in that query's response; the queries around it are answered
-    big = graphgen.erdos_renyi_m(20000, 4.0, 3, wmax=10)
-    n, u, v, w = graphgen.erdos_renyi(150, 0.1, 4)
+def test_large_sparse_graph_in_the_mix(libcac, ctx):
+    # 20000 vertices with sparse pre-contraction (global-memory Stage 1) served between small queries
+    n, u, v, w = graphgen.watts_strogatz(20000, 4, 0.3, 8, wmax=100)
+    ns, us, vs, ws = graphgen.erdos_renyi(150, 0.1, 4)
+    want = ctx.graph(n, u, v, w).square_root(0.5, seed=2)
     with libcac.Server(0) as srv:
+        gb, gs = srv.graph(n, u, v, w), srv.graph(ns, us, vs, ws)
+        t0 = srv.submit("square_root", gs, 0.9, seed=2)
+        t1 = srv.submit("square_root", gb, 0.5, seed=2)
+        t2 = srv.submit("parallel_cc", gb, seed=2)
+        assert srv.poll(t0)[0].cut == O.exact_mincut(ns, us, vs, ws)
+        r = srv.poll(t1)[0]
+        assert (r.cut, r.trials) == (want.cut, want.trials_per_rank)
+        assert srv.poll(t2)[0].num_components == O.cc_labels(n, u, v)[0]
+
+
+def test_over_budget_query_fails_alone(libcac):
+    # K2500's root matrix (50 MB) exceeds a 32 MB budget: that query fails with CAC_ERR_OOM at
+    # admission, reported in its own response; the queries around it are answered
+    big = graphgen.complete(2500, 3)
+    n, u, v, w = graphgen.erdos_renyi(150, 0.1, 4)
+    with libcac.Server(0, hbm_budget_bytes=32 << 20) as srv:
         gb, gs = srv.graph(*big), srv.graph(n, u, v, w)
         t0 = srv.submit("square_root", gs, 0.9, seed=2)
         t1 = srv.submit("square_root", gb, 0.9, seed=2)
@@ -121,5 +148,5 @@ def test_unsupported_query_fails_alone(libcac):
         assert srv.poll(t0)[0].cut == O.exact_mincut(n, u, v, w)
         with pytest.raises(libcac.CacError) as e:
             srv.poll(t1)
-        assert e.value.status == -6
+        assert e.value.status == -2
         assert srv.poll(t2)[0].cut == O.exact_mincut(n, u, v, w)
