@@ -530,6 +530,9 @@ def run_serve(args, rank, world):
     by_kind = {}
     for (_, kind, _, _), x in zip(ptrace, lat):
         by_kind.setdefault(kind, []).append(x)
+    slowest = sorted(range(len(ptrace)), key=lambda i: -lat[i])[:5]
+    slow = [{"kind": ptrace[i][1], "edges": int(cg[ptrace[i][2]].m), "queue_ms": round(pres[i].queue_ms, 3),
+             "service_ms": round(pres[i].service_ms, 3)} for i in slowest]
     line = {"metric": "served queries/s (square_root : approx_cut : parallel_cc = 2:1:1, 10^3-10^7 edges)",
             "value": len(trace) / sat_s, "unit": "queries/s", "n_gpus": 1, "steps": len(trace), "warmup": 3,
             "ms_per_step": sat_s / len(trace) * 1e3, "higher_is_better": True, "scaling": "weak",
@@ -541,7 +544,8 @@ def run_serve(args, rank, world):
                            "p99_ms": _percentile(sat_lat, 99)},
             "poisson": {"rate_per_s": rate, "queries_per_s": len(ptrace) / poisson_s,
                         "p50_ms": _percentile(lat, 50), "p99_ms": _percentile(lat, 99),
-                        "p99_ms_by_kind": {k: _percentile(v, 99) for k, v in by_kind.items()}},
+                        "p99_ms_by_kind": {k: _percentile(v, 99) for k, v in by_kind.items()},
+                        "slowest": slow},
             "plain_path": {"queries_per_s": len(trace) / plain_s, "p50_ms": _percentile(plain_lat, 50),
                            "p99_ms": _percentile(plain_lat, 99)},
             "speedup_vs_plain": plain_s / sat_s, "results_equal_plain": equal, "clocks": clk.summary()}

@@ -146,61 +146,66 @@ __device__ __forceinline__ uint32_t sfind_ro(const uint32_t *par, uint32_t x) {
 
 // Contract the draw pairs sb[0, nb) into the shared-memory union-find `par` (roots are component
 // minima) in draw order until *s_count reaches target -- the sequential rule of the trial.
-// Fast path: every thread links its draws concurrently (CAS of the larger root onto the smaller,
-// finds without compression) and logs each successful link; a successful CAS always joins two
-// different components, so the number of links is the exact count drop, and when the count stays
-// above target the partition equals the sequential one. Otherwise the logged links are undone
-// (only roots were written, so this restores `par` exactly) and thread 0 replays the batch in
-// draw order, stopping at target. Afterwards every endpoint of the batch points at its root.
-// s_log: nb entries of shared memory; s_nlog: one shared counter.
+// With need = count - target links still allowed, the next `need` draws are linked by all threads
+// at once (CAS of the larger root onto the smaller, finds without compression): each draw links
+// at most once, so the count cannot fall below target, and since draws after the one that reaches
+// target link nothing, the partition equals the sequential one. A successful CAS always joins
+// two different components, so the number of links is the exact count drop. Repeated until the
+// target or the end of the batch; the last few links (need <= 16) are made by thread 0 in draw
+// order. Endpoints of linked draws are pointed at their roots after each step.
+constexpr uint32_t kSeqTail = 16;
+
 template <int NT>
 __device__ void contract_batch(uint32_t *par, const uint2 *sb, uint32_t nb, uint32_t target, uint32_t *s_count,
-                               uint32_t *s_log, uint32_t *s_nlog) {
+                               uint32_t *s_nlog) {
     volatile uint32_t *vp = par;
-    const uint32_t c0 = *s_count;
-    __syncthreads();
-    if (threadIdx.x == 0) *s_nlog = 0;
-    __syncthreads();
-    for (uint32_t j = threadIdx.x; j < nb; j += NT) {
-        uint32_t a = sb[j].x, b = sb[j].y;
-        for (;;) {
-            while (vp[a] != a) a = vp[a];
-            while (vp[b] != b) b = vp[b];
-            if (a == b) break;
-            const uint32_t hi = a > b ? a : b, lo = a > b ? b : a;
-            if (atomicCAS(&par[hi], hi, lo) == hi) {
-                s_log[atomicAdd(s_nlog, 1u)] = hi;
-                break;
+    uint32_t j0 = 0;
+    for (;;) {
+        __syncthreads();
+        const uint32_t c = *s_count;
+        if (c <= target || j0 >= nb) break;
+        const uint32_t need = c - target;
+        if (need <= kSeqTail) {
+            if (threadIdx.x == 0) {
+                uint32_t cc = c;
+                for (uint32_t j = j0; j < nb && cc > target; j++) {
+                    const uint32_t x = sfind(par, sb[j].x), y = sfind(par, sb[j].y);
+                    if (x != y) {
+                        if (x < y) par[y] = x; else par[x] = y;
+                        cc--;
+                    }
+                }
+                *s_count = cc;
             }
-            a = hi;  // hi was linked meanwhile: find both roots again
-            b = lo;
+            __syncthreads();
+            break;
         }
-    }
-    __syncthreads();
-    const uint32_t links = *s_nlog;
-    if (c0 - links > target) {
-        for (uint32_t j = threadIdx.x; j < nb; j += NT) {  // point the endpoints at their roots
-            const uint32_t a = sb[j].x, b = sb[j].y;
-            par[a] = sfind_ro(par, a);
-            par[b] = sfind_ro(par, b);
-        }
+        const uint32_t j1 = min(nb, j0 + need);
+        if (threadIdx.x == 0) *s_nlog = 0;
         __syncthreads();
-        if (threadIdx.x == 0) *s_count = c0 - links;
-        __syncthreads();
-        return;
-    }
-    for (uint32_t i = threadIdx.x; i < links; i += NT) par[s_log[i]] = s_log[i];
-    __syncthreads();
-    if (threadIdx.x == 0) {
-        uint32_t c = c0;
-        for (uint32_t j = 0; j < nb && c > target; j++) {
-            const uint32_t a = sfind(par, sb[j].x), b = sfind(par, sb[j].y);
-            if (a != b) {
-                if (a < b) par[b] = a; else par[a] = b;
-                c--;
+        for (uint32_t j = j0 + threadIdx.x; j < j1; j += NT) {
+            uint32_t x = sb[j].x, y = sb[j].y;
+            for (;;) {
+                while (vp[x] != x) x = vp[x];
+                while (vp[y] != y) y = vp[y];
+                if (x == y) break;
+                const uint32_t hi = x > y ? x : y, lo = x > y ? y : x;
+                if (atomicCAS(&par[hi], hi, lo) == hi) {
+                    atomicAdd(s_nlog, 1u);
+                    break;
+                }
+                x = hi;  // hi was linked meanwhile: find both roots again
+                y = lo;
             }
         }
-        *s_count = c;
+        __syncthreads();
+        for (uint32_t j = j0 + threadIdx.x; j < j1; j += NT) {  // point the endpoints at their roots
+            const uint32_t x = sb[j].x, y = sb[j].y;
+            par[x] = sfind_ro(par, x);
+            par[y] = sfind_ro(par, y);
+        }
+        if (threadIdx.x == 0) *s_count = c - *s_nlog;
+        j0 = j1;
     }
     __syncthreads();
 }
@@ -242,8 +247,7 @@ template <int NT>
 __global__ void __launch_bounds__(NT) iss_shrink_kernel(const ShrinkDesc *__restrict__ descs) {
     extern __shared__ __align__(16) unsigned char dsm[];
     uint2 *sb = reinterpret_cast<uint2 *>(dsm);
-    uint32_t *s_log = reinterpret_cast<uint32_t *>(dsm + kBatch * sizeof(uint2));
-    uint32_t *par = s_log + kBatch;
+    uint32_t *par = reinterpret_cast<uint32_t *>(dsm + kBatch * sizeof(uint2));
     __shared__ uint32_t s_count, s_nlog;
     const ShrinkDesc D = descs[blockIdx.x];
     const uint32_t n = D.n, target = D.target;
@@ -279,7 +283,7 @@ __global__ void __launch_bounds__(NT) iss_shrink_kernel(const ShrinkDesc *__rest
                 sb[j] = make_uint2(U[e], V[e]);
             }
             __syncthreads();
-            contract_batch<NT>(par, sb, nb, target, &s_count, s_log, &s_nlog);
+            contract_batch<NT>(par, sb, nb, target, &s_count, &s_nlog);
             if (s_count <= target) break;
         }
         for (uint32_t v = threadIdx.x; v < n; v += NT) par[v] = sfind_ro(par, v);
@@ -373,8 +377,7 @@ __global__ void __launch_bounds__(NT) contract_kernel(const TaskDesc *__restrict
     const TaskDesc T = tasks[blockIdx.x];
     const SrcDesc S = srcs[T.src];
     const uint32_t N = S.N;
-    uint32_t *s_log = reinterpret_cast<uint32_t *>(dsm + kBatch * sizeof(uint2));
-    uint32_t *par = s_log + kBatch;
+    uint32_t *par = reinterpret_cast<uint32_t *>(dsm + kBatch * sizeof(uint2));
     uint32_t *cnt = par + N;  // counting-sort counters, N entries
     const uint64_t W = S.rowpre[N - 1];
     if (W == 0) {  // no edges between the vertices: the cut is 0, nothing to contract
@@ -411,7 +414,7 @@ __global__ void __launch_bounds__(NT) contract_kernel(const TaskDesc *__restrict
             sb[j] = make_uint2(a, b * 32 + c);
         }
         __syncthreads();
-        contract_batch<NT>(par, sb, nb, T.target, &s_count, s_log, &s_nlog);
+        contract_batch<NT>(par, sb, nb, T.target, &s_count, &s_nlog);
         if (s_count <= T.target) break;
     }
     for (uint32_t v = threadIdx.x; v < N; v += NT) par[v] = sfind_ro(par, v);
@@ -786,7 +789,7 @@ int upload(cac_ctx *ctx, DevBuf &buf, const std::vector<T> &v) {
 }
 
 size_t leaf_smem(uint32_t N, bool small) { return (size_t)N * (N / 2) * (small ? 4 : 8); }
-size_t contract_smem(uint32_t N) { return kBatch * (sizeof(uint2) + 4) + (size_t)2 * N * 4; }
+size_t contract_smem(uint32_t N) { return kBatch * sizeof(uint2) + (size_t)2 * N * 4; }
 size_t quotient_smem(uint32_t N) { return (size_t)N * 8; }
 
 }  // namespace
@@ -1161,7 +1164,7 @@ int admit(cac_ctx *ctx, KsEngine &eng, const QueryPlan &q) {
                                    : 8 * std::max<uint64_t>(m, 1) + 4 * (uint64_t)n + 64;
     const uint64_t chunk = std::max<uint64_t>(1, std::min<uint64_t>({q.trials, (4ull << 30) / per_trial, (uint64_t)65535}));
     DevBuf d_pre(ctx), d_lab(ctx), d_k(ctx), d_sd(ctx), d_dd(ctx);
-    const size_t sm = kBatch * (sizeof(uint2) + 4) + (size_t)std::min(n, kMaxSmemVertices) * 4;
+    const size_t sm = kBatch * sizeof(uint2) + (size_t)std::min(n, kMaxSmemVertices) * 4;
     if (!big)
         CAC_TRY(smem_optin(ctx, iss_shrink_kernel<kNT>));
     for (uint64_t c0 = 0; c0 < q.trials; c0 += chunk) {
