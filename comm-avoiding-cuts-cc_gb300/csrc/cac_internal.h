@@ -75,6 +75,8 @@ struct cac_ctx {
     cac::CCGraphKey cc_key;          // last connected-components query
     cudaGraphExec_t cc_exec = nullptr;  // its captured launch sequence (second sighting onwards)
     uint32_t *pinned_u32 = nullptr;  // 64 KB pinned staging: [0,256) B scalar results, then descriptors
+    cudaStream_t copy_stream = nullptr;  // host-to-device chunks of cac_cc_edges (created on first use)
+    cudaEvent_t chunk_ev[16] = {};       // one per chunk in flight
 };
 
 struct cac_graph {
@@ -125,6 +127,10 @@ CCPlan cc_plan(uint32_t n, uint64_t m, uint32_t ranks);
 int cc_run(cac_ctx *ctx, uint32_t n, uint64_t m, const uint32_t *d_u, const uint32_t *d_v, uint32_t seed,
            uint32_t ranks, uint32_t *d_labels, cac_cc_result *res);
 size_t cc_scratch_bytes(uint32_t n, uint32_t ranks, uint64_t m);
+// CC of an edge list in host memory: chunks copied to d_u/d_v on a second stream while the ctx
+// stream hooks each chunk that has arrived (cac_cc_edges).
+int cc_run_streamed(cac_ctx *ctx, uint32_t n, uint64_t m, const uint32_t *h_u, const uint32_t *h_v, uint32_t *d_u,
+                    uint32_t *d_v, uint32_t *d_labels, cac_cc_result *res);
 void cc_graph_reset(cac_ctx *ctx);
 
 // ---- min cut (mincut.cu) ----

@@ -692,7 +692,6 @@ int cc_run(cac_ctx *ctx, uint32_t n, uint64_t m, const uint32_t *d_u, const uint
     }
     L.h_ranks = hr;
     if (L.draws > 0 && m > 0) {
-        const int sm = (int)((size_t)std::min(L.nwords, kSmemBitmapWords) * 4);
         CAC_TRY(smem_optin(ctx, cc_filter<true>));
         CAC_TRY(smem_optin(ctx, cc_filter<false>));
     }
@@ -738,6 +737,119 @@ int cc_run(cac_ctx *ctx, uint32_t n, uint64_t m, const uint32_t *d_u, const uint
         CAC_CUDA_TRY(cudaEventElapsedTime(&res->edge_pass_ms, ctx->ev[1], ctx->ev[4]));
         CAC_CUDA_TRY(cudaEventElapsedTime(&res->sample_ms, ctx->ev[0], ctx->ev[1]));
         CAC_CUDA_TRY(cudaEventElapsedTime(&res->hook_ms, ctx->ev[4], ctx->ev[2]));
+        CAC_CUDA_TRY(cudaEventElapsedTime(&res->label_ms, ctx->ev[2], ctx->ev[3]));
+    }
+    return CAC_OK;
+}
+
+// Connected components of an edge list that is still in host memory (cac_cc_edges). The
+// host-to-device link (about 200 GB/s on a GB300 host, measured) is slower than the device's
+// from-scratch hooking of all edges, so the edges cross it in chunks on a second stream while the
+// ctx stream hooks every chunk that has arrived into the union-find: the query ends about one
+// chunk's hook after its last byte arrived, instead of copy time plus compute time. No sampling
+// round is needed (it only serves to skip edges of a device-resident graph); the labels -- rank
+// of each component's smallest vertex -- are the same as cc_run's for any edge order.
+int cc_run_streamed(cac_ctx *ctx, uint32_t n, uint64_t m, const uint32_t *h_u, const uint32_t *h_v, uint32_t *d_u,
+                    uint32_t *d_v, uint32_t *d_labels, cac_cc_result *res) {
+    cudaStream_t s = ctx->stream;
+    if (res) *res = cac_cc_result{};
+    if (n == 0) return CAC_OK;
+    if (!ctx->copy_stream) {
+        CAC_CUDA_TRY(cudaStreamCreateWithFlags(&ctx->copy_stream, cudaStreamNonBlocking));
+        for (auto &e : ctx->chunk_ev) CAC_CUDA_TRY(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+    }
+    const uint32_t ntiles = (uint32_t)(((uint64_t)n + kTile - 1) / kTile);
+    const uint32_t nwords = (uint32_t)(((uint64_t)n + 31) / 32);
+    // Chunks of at least 4 Mi edges (32 MB of u and v: smaller copies lose link bandwidth to
+    // per-copy overhead), at most 16, each a multiple of 1024 edges (16-byte aligned starts).
+    const uint64_t per = m ? (std::max<uint64_t>(4ull << 20, (m + 15) / 16) + 1023) / 1024 * 1024 : 0;
+    const uint32_t nchunks = per ? (uint32_t)((m + per - 1) / per) : 0;
+    const bool vec = ((reinterpret_cast<uintptr_t>(d_u) | reinterpret_cast<uintptr_t>(d_v)) & 15) == 0;
+    // The first `whole` chunks are hooked edge by edge: they play the sampling round's part and
+    // cover at least the reference's sample budget (edgesToSamplePerProcessor: n^1.045 * 1.2).
+    // The giant component they reveal is fixed as a bitmap, and every later chunk is streamed
+    // through the filter, which hooks only the edges that leave the giant component.
+    const uint64_t budget = (uint64_t)(std::pow((float)n, 1.0f + 0.09f / 2) * (1.0f + 0.2f));
+    const uint32_t whole = per ? (uint32_t)std::max<uint64_t>(1, (budget + per - 1) / per) : 0;
+    const bool filtered = vec && nchunks > whole;
+    CAC_TRY(arena_reserve(ctx, align_up((size_t)n * 4) + 2 * align_up((size_t)ntiles * 4 + 4) + align_up(256) +
+                                   (filtered ? align_up((size_t)nwords * 4 + 4) + align_up(kMaxRegions * 4) +
+                                                   align_up((per + 4 * (uint64_t)kMaxRegions) * 8)
+                                             : 0)));
+    arena_reset(ctx);
+    uint32_t *par = (uint32_t *)arena_take(ctx, (size_t)n * 4);
+    uint32_t *counts = (uint32_t *)arena_take(ctx, (size_t)ntiles * 4 + 4);
+    uint32_t *offsets = (uint32_t *)arena_take(ctx, (size_t)ntiles * 4 + 4);
+    uint32_t *total = (uint32_t *)arena_take(ctx, 256);
+    uint32_t *giant = total + 8;
+    uint32_t *bits = nullptr, *region_counts = nullptr;
+    uint2 *surv = nullptr;
+    if (filtered) {
+        bits = (uint32_t *)arena_take(ctx, (size_t)nwords * 4 + 4);
+        region_counts = (uint32_t *)arena_take(ctx, kMaxRegions * 4);
+        surv = (uint2 *)arena_take(ctx, (per + 4 * (uint64_t)kMaxRegions) * 8);
+        CAC_TRY(smem_optin(ctx, cc_filter<true>));
+        CAC_TRY(smem_optin(ctx, cc_filter<false>));
+    }
+    CAC_CUDA_TRY(cudaEventRecord(ctx->ev[0], s));
+    cc_init<<<grid_for(ctx, n, 8), kThreads, 0, s>>>(par, n);
+    // the copies start after everything already queued on the ctx stream (the staging buffers
+    // may still be read by the previous query)
+    CAC_CUDA_TRY(cudaEventRecord(ctx->chunk_ev[0], s));
+    CAC_CUDA_TRY(cudaStreamWaitEvent(ctx->copy_stream, ctx->chunk_ev[0], 0));
+    for (uint32_t c = 0; c < nchunks && per; c++) {
+        const uint64_t e0 = std::min<uint64_t>(m, c * per), e1 = std::min<uint64_t>(m, e0 + per);
+        if (e0 >= e1) break;
+        CAC_CUDA_TRY(cudaMemcpyAsync(d_u + e0, h_u + e0, (e1 - e0) * 4, cudaMemcpyHostToDevice, ctx->copy_stream));
+        CAC_CUDA_TRY(cudaMemcpyAsync(d_v + e0, h_v + e0, (e1 - e0) * 4, cudaMemcpyHostToDevice, ctx->copy_stream));
+        CAC_CUDA_TRY(cudaEventRecord(ctx->chunk_ev[c], ctx->copy_stream));
+        CAC_CUDA_TRY(cudaStreamWaitEvent(s, ctx->chunk_ev[c], 0));
+        const uint64_t len = e1 - e0;
+        if (!filtered || c < whole) {
+            const int grid = grid_for(ctx, (len + 3) / 4, 8);
+            if (vec) cc_edge_pass<true><<<grid, kThreads, 0, s>>>(par, d_u + e0, d_v + e0, len);
+            else cc_edge_pass<false><<<grid, kThreads, 0, s>>>(par, d_u + e0, d_v + e0, len);
+            // flat trees keep the next chunk's union walks one or two hops long (hidden behind the copy)
+            if (c + 1 < nchunks) compress_all(ctx, par, n, s);
+            if (filtered && c + 1 == whole) {
+                cc_find_giant<<<1, kGiantSample, 0, s>>>(par, n, giant);
+                cc_giant_bitmap<<<grid_for(ctx, n, 8), kThreads, 0, s>>>(par, n, giant, bits);
+            }
+        } else {
+            const uint64_t tiles = len >> 8;  // 256-edge tiles; the rest goes to the scalar pass
+            const uint32_t regions = (uint32_t)std::max<uint64_t>(
+                1, std::min<uint64_t>({(uint64_t)ctx->num_sms, (uint64_t)kMaxRegions, tiles}));
+            const uint64_t tper = (tiles + regions - 1) / regions;
+            if (tiles) {
+                const size_t sm = (size_t)std::min(nwords, kSmemBitmapWords) * 4;
+                auto filt = nwords <= kSmemBitmapWords ? cc_filter<true> : cc_filter<false>;
+                filt<<<regions, kEdgeThreads, sm, s>>>(d_u + e0, d_v + e0, tiles, bits, nwords, surv, region_counts);
+                cc_hook_survivors<<<(unsigned)ctx->num_sms * 4, kThreads, 0, s>>>(par, surv, region_counts, regions,
+                                                                                   tper * 256);
+            }
+            const uint64_t done = tiles * 256;
+            if (done < len)
+                cc_edge_pass<false><<<grid_for(ctx, len - done, 8), kThreads, 0, s>>>(par, d_u + e0 + done,
+                                                                                     d_v + e0 + done, len - done);
+        }
+    }
+    CAC_CUDA_TRY(cudaEventRecord(ctx->ev[2], s));
+    cc_finalize_count<<<ntiles, kThreads, 0, s>>>(par, n, counts);
+    cc_scan_tiles<<<1, 1024, 0, s>>>(counts, offsets, ntiles, total);
+    if (d_labels) {
+        cc_rank_roots<<<ntiles, kThreads, 0, s>>>(par, n, offsets, d_labels);
+        cc_label_all<<<grid_for(ctx, n, 8), kThreads, 0, s>>>(par, n, d_labels);
+    }
+    CAC_CUDA_TRY(cudaGetLastError());
+    CAC_CUDA_TRY(cudaMemcpyAsync(ctx->pinned_u32, total, 4, cudaMemcpyDeviceToHost, s));
+    CAC_CUDA_TRY(cudaEventRecord(ctx->ev[3], s));
+    CAC_CUDA_TRY(cudaStreamSynchronize(s));
+    if (res) {
+        res->num_components = ctx->pinned_u32[0];
+        res->rounds = m > 0 ? 1u : 0u;
+        res->sampled_edges = 0;
+        CAC_CUDA_TRY(cudaEventElapsedTime(&res->device_ms, ctx->ev[0], ctx->ev[3]));
+        CAC_CUDA_TRY(cudaEventElapsedTime(&res->edge_pass_ms, ctx->ev[0], ctx->ev[2]));
         CAC_CUDA_TRY(cudaEventElapsedTime(&res->label_ms, ctx->ev[2], ctx->ev[3]));
     }
     return CAC_OK;

@@ -114,6 +114,24 @@ def test_one_call_host_entry_point(ctx):
 
 
 @pytest.mark.slow
+def test_one_call_host_entry_point_streams_chunks(ctx):
+    # 35 M edges (above 32 Mi): chunks cross the host link while earlier ones are hooked, the
+    # later ones through the giant-component filter; a second, disconnected copy of the graph and
+    # isolated vertices check the labels of many components
+    n0, u0, v0, _ = graphgen.barabasi_albert(1100000, 16, 3)
+    n = 2 * n0 + 1001
+    u = np.concatenate([u0, u0 + n0]).astype(np.uint32)
+    v = np.concatenate([v0, v0 + n0]).astype(np.uint32)
+    u, v = u[:-3], v[:-3]  # a length that is not a multiple of 4 or of the chunk
+    want_count, want = O.cc_labels(n, u, v)
+    lab = np.zeros(n, np.uint32)
+    for _ in range(2):  # the staging buffers are reused by the next call
+        res = ctx.cc_edges(n, u, v, labels=lab)
+        assert res.num_components == want_count and np.array_equal(lab, want)
+        assert res.rounds == 1 and res.sampled_edges == 0  # every edge hooked as it arrives
+
+
+@pytest.mark.slow
 def test_full_size_ba_1m(ctx):
     n, u, v, _ = graphgen.barabasi_albert(1024000, 16, 0)
     assert len(u) == 16383744
