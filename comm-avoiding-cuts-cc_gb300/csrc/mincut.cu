@@ -496,12 +496,19 @@ __global__ void __launch_bounds__(NT) quotient_kernel(const TaskDesc *__restrict
     }
 }
 
+__device__ __forceinline__ void sadd(uint32_t *p, uint64_t v) { atomicAdd(p, (uint32_t)v); }
+__device__ __forceinline__ void sadd(uint64_t *p, uint64_t v) {
+    atomicAdd(reinterpret_cast<unsigned long long *>(p), (unsigned long long)v);
+}
+
 // One CTA per group of `rows` consecutive output rows of one child, one warp per output row at a
-// time: the child's member lists are staged in shared memory once per CTA; a warp sums the member
-// rows of its output row into its own shared-memory row (lanes stride the columns with eight
-// independent loads in flight each), then gathers every output column through the member lists
-// and stores the row. No block-wide barrier inside the row loop. Shared memory: the lists, then
-// one N-entry row per warp.
+// time. The child's labels are staged in shared memory once per CTA. For output row a the warp
+// sums the member rows of group a (lanes stride the columns, eight independent loads in flight
+// each) and adds every column's sum straight into its label's slot of the warp's output row in
+// shared memory (an integer atomic, exact in any order); then it stores the row with the diagonal
+// zeroed, and writes the row's 32-column block prefixes and its sum (the next step's row prep).
+// Shared memory: the labels, then one k-entry row per warp.
+//   Q[a][b] = sum over u in group a, v in group b of A[u][v]
 template <typename Ts>
 __global__ void __launch_bounds__(256) quotient_warp_kernel(const TaskDesc *__restrict__ tasks,
                                                             const SrcDesc *__restrict__ srcs,
@@ -509,7 +516,7 @@ __global__ void __launch_bounds__(256) quotient_warp_kernel(const TaskDesc *__re
                                                             const uint64_t *__restrict__ group_task_off,
                                                             uint32_t ntasks, uint32_t rows,
                                                             const uint64_t *__restrict__ out_off, uint64_t *out_base,
-                                                            uint32_t stage_words) {
+                                                            uint32_t lab_words, uint32_t kmax) {
     // out_off[ntasks + i]: where task i's row sums and block prefixes go (the next step's row prep)
     extern __shared__ __align__(16) unsigned char dsm[];
     const uint64_t gg = blockIdx.x;
@@ -523,25 +530,25 @@ __global__ void __launch_bounds__(256) quotient_warp_kernel(const TaskDesc *__re
     const uint32_t k = kdim[lo];
     const uint32_t N = S.N;
     const uint32_t a0 = (uint32_t)(gg - group_task_off[lo]) * rows, a1 = min(k, a0 + rows);
-    uint32_t *s_moff = reinterpret_cast<uint32_t *>(dsm);  // k + 1
-    uint32_t *s_memb = s_moff + (k + 1);                     // N
+    uint32_t *s_lab = reinterpret_cast<uint32_t *>(dsm);  // N
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
-    // Ts: uint32_t when every task of the launch has total weight below 2^32 (member-row sums fit)
-    Ts *rs = reinterpret_cast<Ts *>(dsm + (size_t)stage_words * 4) + (size_t)warp * N;
-    for (uint32_t i = threadIdx.x; i <= k; i += blockDim.x) s_moff[i] = T.memb_off[i];
-    for (uint32_t i = threadIdx.x; i < N; i += blockDim.x) s_memb[i] = T.members[i];
+    // Ts: uint32_t when the graph's total weight is below 2^32 (every entry and row sum fits)
+    Ts *qrow = reinterpret_cast<Ts *>(dsm + (size_t)lab_words * 4) + (size_t)warp * kmax;
+    for (uint32_t i = threadIdx.x; i < N; i += blockDim.x) s_lab[i] = T.lab[i];
     __syncthreads();
     uint64_t *Qt = out_base + out_off[lo];
     uint64_t *rowsum_out = out_base + out_off[ntasks + lo];
-    const bool small = T.pad != 0;  // the graph's total weight is below 2^32
+    const bool small = T.pad != 0;
     const uint32_t nbk = (k + 31) / 32;
     uint64_t *blk = rowsum_out + k;
     for (uint32_t a = a0 + warp; a < a1; a += nw) {
-        const uint32_t p0 = s_moff[a], p1 = s_moff[a + 1];
+        for (uint32_t b = lane; b < k; b += 32) qrow[b] = 0;
+        __syncwarp();
+        const uint32_t p0 = T.memb_off[a], p1 = T.memb_off[a + 1];
         for (uint32_t j0 = 0; j0 < N; j0 += 256) {
             uint64_t x[8] = {0, 0, 0, 0, 0, 0, 0, 0};
             for (uint32_t p = p0; p < p1; p++) {
-                const uint64_t *row = S.mat + (uint64_t)s_memb[p] * N;
+                const uint64_t *row = S.mat + (uint64_t)T.members[p] * N;
 #pragma unroll
                 for (int u = 0; u < 8; u++) {
                     const uint32_t j = j0 + u * 32 + lane;
@@ -551,7 +558,7 @@ __global__ void __launch_bounds__(256) quotient_warp_kernel(const TaskDesc *__re
 #pragma unroll
             for (int u = 0; u < 8; u++) {
                 const uint32_t j = j0 + u * 32 + lane;
-                if (j < N) rs[j] = (Ts)x[u];
+                if (j < N && x[u]) sadd(&qrow[s_lab[j]], x[u]);
             }
         }
         __syncwarp();
@@ -560,13 +567,9 @@ __global__ void __launch_bounds__(256) quotient_warp_kernel(const TaskDesc *__re
         for (uint32_t b0 = 0; b0 < k; b0 += 128) {  // four 32-column blocks per pass (warp-uniform trip count)
             uint64_t acc[4];
 #pragma unroll
-            for (int u = 0; u < 4; u++) {  // four independent gather chains in flight
+            for (int u = 0; u < 4; u++) {
                 const uint32_t b = b0 + 32 * u + lane;
-                acc[u] = 0;
-                if (b < k && b != a) {
-                    const uint32_t q1 = s_moff[b + 1];
-                    for (uint32_t q = s_moff[b]; q < q1; q++) acc[u] += rs[s_memb[q]];
-                }
+                acc[u] = (b < k && b != a) ? (uint64_t)qrow[b] : 0;
                 if (b < k) Q[b] = acc[u];
             }
 #pragma unroll
@@ -1042,14 +1045,20 @@ int KsEngine::step() {
         groups += (k + qrows - 1) / qrows;
         if (k) qsm = std::max(qsm, quotient_smem(tasks[i].src.N));
     }
-    // warp-per-row quotient (8 warps) where three or more of its CTAs fit on an SM (lists + one
-    // row per warp within 80 KB, N up to about 1100), else the CTA-per-row-group kernel, whose
+    // warp-per-row quotient with 8 (or 4) warps where three or more of its CTAs fit on an SM
+    // (labels + one k-entry row per warp within 80 KB), else the CTA-per-row-group kernel, whose
     // 256 threads share one row and keep the SM occupied at large N
-    const size_t stage_words = (2 * (size_t)maxN + 2 + 3) & ~(size_t)3;  // k + 1 + N u32, 16-byte rounded
+    const size_t stage_words = ((size_t)maxN + 3) & ~(size_t)3;  // N u32 labels, 16-byte rounded
     bool all_small = true;
-    for (const KTask &t : tasks) all_small = all_small && t.src.small;
+    uint32_t kmax = 0;
+    for (size_t i = 0; i < tasks.size(); i++) {
+        all_small = all_small && tasks[i].src.small;
+        kmax = std::max(kmax, kq[i]);
+    }
     const size_t rs_bytes = all_small ? 4 : 8;
-    const uint32_t qwarps = stage_words * 4 + 8 * rs_bytes * (size_t)maxN <= 80 * 1024 ? 8u : 0u;
+    const uint32_t qwarps = stage_words * 4 + 8 * rs_bytes * (size_t)kmax <= 80 * 1024   ? 8u
+                            : stage_words * 4 + 4 * rs_bytes * (size_t)kmax <= 80 * 1024 ? 4u
+                                                                                         : 0u;
     const uint32_t wrows = qwarps * 4;
     if (qwarps) {
         groups = 0;
@@ -1069,13 +1078,13 @@ int KsEngine::step() {
         CAC_TRY(upload(ctx_, d_gto, group_task_off));
         CAC_CUDA_TRY(cudaMemcpyAsync(d_kout.p, kq.data(), tasks.size() * 4, cudaMemcpyHostToDevice, s));
         if (qwarps) {
-            const size_t wsm = stage_words * 4 + (size_t)qwarps * maxN * rs_bytes;
+            const size_t wsm = stage_words * 4 + (size_t)qwarps * kmax * rs_bytes;
             auto kern = all_small ? quotient_warp_kernel<uint32_t> : quotient_warp_kernel<uint64_t>;
             CAC_TRY(smem_optin(ctx_, kern));
             kern<<<(unsigned)groups, qwarps * 32, wsm, s>>>(
                 d_task.as<TaskDesc>(), d_src.as<SrcDesc>(), d_kout.as<uint32_t>(), d_gto.as<uint64_t>(),
                 (uint32_t)tasks.size(), wrows, d_qoff.as<uint64_t>(), static_cast<uint64_t *>(out->p),
-                (uint32_t)stage_words);
+                (uint32_t)stage_words, kmax);
         } else {
             CAC_TRY(smem_optin(ctx_, quotient_kernel<kQT>));
             quotient_kernel<kQT><<<(unsigned)groups, kQT, qsm, s>>>(
