@@ -243,12 +243,23 @@ __device__ void rank_labels(const uint32_t *par, uint32_t n, uint32_t *lab) {
 
 // ---------------------------------------------------------------- stage 1
 
+// Stage 1 of one trial per CTA. Per round: the weights of the edges that are not loops and their
+// inclusive prefix in edge order (warp w owns a contiguous range, its lanes read consecutive
+// edges; warp sums, one block-level offset step, then a warp scan per 32 edges writes the
+// prefix), a coarse index of the prefix at the end of every `cs`-edge segment in shared memory,
+// then (vertex count) draws in batches: each draw finds its segment in the shared index and its
+// edge by a short binary search inside the segment, and the batch is contracted in draw order.
+constexpr uint32_t kCoarse = 2048;  // coarse prefix index entries (shared memory)
+
 template <int NT>
 __global__ void __launch_bounds__(NT) iss_shrink_kernel(const ShrinkDesc *__restrict__ descs) {
+    constexpr int NW = NT / 32;
     extern __shared__ __align__(16) unsigned char dsm[];
     uint2 *sb = reinterpret_cast<uint2 *>(dsm);
-    uint32_t *par = reinterpret_cast<uint32_t *>(dsm + kBatch * sizeof(uint2));
+    uint64_t *coarse = reinterpret_cast<uint64_t *>(dsm + kBatch * sizeof(uint2));
+    uint32_t *par = reinterpret_cast<uint32_t *>(dsm + kBatch * sizeof(uint2) + kCoarse * sizeof(uint64_t));
     __shared__ uint32_t s_count, s_nlog;
+    __shared__ uint64_t s_w[NW];
     const ShrinkDesc D = descs[blockIdx.x];
     const uint32_t n = D.n, target = D.target;
     const uint64_t m = D.m;
@@ -256,30 +267,51 @@ __global__ void __launch_bounds__(NT) iss_shrink_kernel(const ShrinkDesc *__rest
     const uint32_t *__restrict__ V = D.V;
     const uint32_t *__restrict__ Wt = D.W;
     uint64_t *pre = D.pre;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     for (uint32_t v = threadIdx.x; v < n; v += NT) par[v] = v;
     if (threadIdx.x == 0) s_count = n;
     __syncthreads();
-    const uint64_t seg = (m + NT - 1) / NT;
-    const uint64_t lo = min(m, (uint64_t)threadIdx.x * seg), hi = min(m, lo + seg);
+    const uint64_t wseg = (m + NW - 1) / NW;
+    const uint64_t wlo = min(m, (uint64_t)warp * wseg), whi = min(m, wlo + wseg);
+    // coarse segments of a multiple of 32 edges, at most kCoarse of them
+    const uint64_t cs = max((uint64_t)32, ((m + kCoarse - 1) / kCoarse + 31) / 32 * 32);
+    const uint32_t ncs = (uint32_t)((m + cs - 1) / cs);
     for (uint64_t rnd = 0; s_count > target; rnd++) {
-        // weights of the edges that are not loops, and their inclusive prefix in edge order
-        uint64_t local = 0;
-        for (uint64_t e = lo; e < hi; e++)
-            if (par[U[e]] != par[V[e]]) local += Wt[e];
-        uint64_t W;
-        uint64_t acc = block_excl_scan_u64<NT>(local, W);
-        for (uint64_t e = lo; e < hi; e++) {
-            if (par[U[e]] != par[V[e]]) acc += Wt[e];
-            pre[e] = acc;
+        uint64_t wsum = 0;
+        for (uint64_t e = wlo + lane; e < whi; e += 32)
+            if (par[U[e]] != par[V[e]]) wsum += Wt[e];
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) wsum += __shfl_xor_sync(0xffffffffu, wsum, o);
+        if (lane == 0) s_w[warp] = wsum;
+        __syncthreads();
+        uint64_t carry = 0, W = 0;
+        for (int i = 0; i < NW; i++) {
+            if (i < warp) carry += s_w[i];
+            W += s_w[i];
+        }
+        for (uint64_t e0 = wlo; e0 < whi; e0 += 32) {
+            const uint64_t e = e0 + lane;
+            uint64_t x = (e < whi && par[U[e]] != par[V[e]]) ? Wt[e] : 0;
+#pragma unroll
+            for (int o = 1; o < 32; o <<= 1) {
+                const uint64_t y = __shfl_up_sync(0xffffffffu, x, o);
+                if (lane >= o) x += y;
+            }
+            if (e < whi) pre[e] = carry + x;
+            carry += __shfl_sync(0xffffffffu, x, 31);
         }
         __syncthreads();
         if (W == 0) break;  // the remaining graph has no edges between its vertices
+        for (uint32_t i = threadIdx.x; i < ncs; i += NT) coarse[i] = pre[min(m, (i + 1) * cs) - 1];
+        __syncthreads();
         const uint32_t c_start = s_count;
         for (uint32_t base = 0; base < c_start; base += kBatch) {
             const uint32_t nb = min((uint32_t)kBatch, c_start - base);
             for (uint32_t j = threadIdx.x; j < nb; j += NT) {
                 const uint64_t y = mulhi64(draw64(D.k0, D.idx, 1, 0, rnd, base + j), W);
-                const uint64_t e = upper_bound_u64(pre, m, y);
+                const uint64_t sg = upper_bound_u64(coarse, ncs, y);
+                const uint64_t s0 = sg * cs;
+                const uint64_t e = s0 + upper_bound_u64(pre + s0, min(cs, m - s0), y);
                 sb[j] = make_uint2(U[e], V[e]);
             }
             __syncthreads();
@@ -1173,7 +1205,7 @@ int admit(cac_ctx *ctx, KsEngine &eng, const QueryPlan &q) {
                                    : 8 * std::max<uint64_t>(m, 1) + 4 * (uint64_t)n + 64;
     const uint64_t chunk = std::max<uint64_t>(1, std::min<uint64_t>({q.trials, (4ull << 30) / per_trial, (uint64_t)65535}));
     DevBuf d_pre(ctx), d_lab(ctx), d_k(ctx), d_sd(ctx), d_dd(ctx);
-    const size_t sm = kBatch * sizeof(uint2) + (size_t)std::min(n, kMaxSmemVertices) * 4;
+    const size_t sm = kBatch * sizeof(uint2) + kCoarse * sizeof(uint64_t) + (size_t)std::min(n, kMaxSmemVertices) * 4;
     if (!big)
         CAC_TRY(smem_optin(ctx, iss_shrink_kernel<kNT>));
     for (uint64_t c0 = 0; c0 < q.trials; c0 += chunk) {
