@@ -249,7 +249,8 @@ __device__ void rank_labels(const uint32_t *par, uint32_t n, uint32_t *lab) {
 // prefix), a coarse index of the prefix at the end of every `cs`-edge segment in shared memory,
 // then (vertex count) draws in batches: each draw finds its segment in the shared index and its
 // edge by a short binary search inside the segment, and the batch is contracted in draw order.
-constexpr uint32_t kCoarse = 2048;  // coarse prefix index entries (shared memory)
+constexpr uint32_t kCoarse = 2048;      // Stage 1 coarse prefix index entries (shared memory)
+constexpr uint32_t kCoarseRows = 1024;  // contraction: coarse row-prefix index entries (shared memory)
 
 template <int NT>
 __global__ void __launch_bounds__(NT) iss_shrink_kernel(const ShrinkDesc *__restrict__ descs) {
@@ -405,11 +406,12 @@ __global__ void __launch_bounds__(NT) contract_kernel(const TaskDesc *__restrict
                                                       uint32_t *err) {
     extern __shared__ __align__(16) unsigned char dsm[];
     uint2 *sb = reinterpret_cast<uint2 *>(dsm);
+    uint64_t *crow = reinterpret_cast<uint64_t *>(dsm + kBatch * sizeof(uint2));  // coarse row index
     __shared__ uint32_t s_count, s_nlog;
     const TaskDesc T = tasks[blockIdx.x];
     const SrcDesc S = srcs[T.src];
     const uint32_t N = S.N;
-    uint32_t *par = reinterpret_cast<uint32_t *>(dsm + kBatch * sizeof(uint2));
+    uint32_t *par = reinterpret_cast<uint32_t *>(dsm + kBatch * sizeof(uint2) + kCoarseRows * sizeof(uint64_t));
     uint32_t *cnt = par + N;  // counting-sort counters, N entries
     const uint64_t W = S.rowpre[N - 1];
     if (W == 0) {  // no edges between the vertices: the cut is 0, nothing to contract
@@ -419,25 +421,47 @@ __global__ void __launch_bounds__(NT) contract_kernel(const TaskDesc *__restrict
         }
         return;
     }
+    // row prefix at the end of every `cr`-row segment (every row when N <= kCoarseRows)
+    const uint32_t cr = (N + kCoarseRows - 1) / kCoarseRows;
+    const uint32_t ncr = (N + cr - 1) / cr;
     for (uint32_t v = threadIdx.x; v < N; v += NT) par[v] = v;
+    for (uint32_t i = threadIdx.x; i < ncr; i += NT) crow[i] = S.rowpre[min(N, (i + 1) * cr) - 1];
     if (threadIdx.x == 0) s_count = N;
     __syncthreads();
     for (uint32_t base = 0; base < N; base += kBatch) {
         const uint32_t nb = min((uint32_t)kBatch, N - base);
         for (uint32_t j = threadIdx.x; j < nb; j += NT) {
             const uint64_t y = mulhi64(draw64(T.k0, T.idx, T.tag, 0, T.round, base + j), W);
-            const uint32_t a = (uint32_t)upper_bound_u64(S.rowpre, N, y);
-            const uint64_t rem = y - (a ? S.rowpre[a - 1] : 0);
+            // row: first whose inclusive prefix exceeds y (segment in shared memory, then inside it)
+            const uint32_t sg = (uint32_t)upper_bound_u64(crow, ncr, y);
+            uint32_t a;
+            uint64_t before;
+            if (cr == 1) {
+                a = sg;
+                before = a ? crow[a - 1] : 0;
+            } else {
+                const uint32_t r0 = sg * cr;
+                a = r0 + (uint32_t)upper_bound_u64(S.rowpre + r0, min(cr, N - r0), y);
+                before = a ? S.rowpre[a - 1] : 0;
+            }
+            const uint64_t rem = y - before;
             const uint64_t *B = S.blk + (uint64_t)a * S.nb;
             const uint32_t b = (uint32_t)upper_bound_u64(B, S.nb, rem);
             const uint64_t rem2 = rem - (b ? B[b - 1] : 0);
             const uint64_t *row = S.mat + (uint64_t)a * N + (uint64_t)b * 32;
             const uint32_t lim = min(32u, N - b * 32);
+            // column: first whose running sum exceeds rem2, eight entries loaded together per step
             uint64_t acc = 0;
-            uint32_t c = 0;
-            for (; c < lim; c++) {
-                acc += row[c];
-                if (acc > rem2) break;
+            uint32_t c = lim;
+            for (uint32_t c0 = 0; c0 < lim && c == lim; c0 += 8) {
+                uint64_t x[8];
+#pragma unroll
+                for (int k = 0; k < 8; k++) x[k] = c0 + k < lim ? __ldg(row + c0 + k) : 0;
+#pragma unroll
+                for (int k = 0; k < 8; k++) {
+                    acc += x[k];
+                    if (c == lim && c0 + k < lim && acc > rem2) c = c0 + k;
+                }
             }
             if (c >= lim) {  // cannot happen with consistent prefixes; record and clamp
                 atomicOr(err, 1u);
@@ -824,7 +848,7 @@ int upload(cac_ctx *ctx, DevBuf &buf, const std::vector<T> &v) {
 }
 
 size_t leaf_smem(uint32_t N, bool small) { return (size_t)N * (N / 2) * (small ? 4 : 8); }
-size_t contract_smem(uint32_t N) { return kBatch * sizeof(uint2) + (size_t)2 * N * 4; }
+size_t contract_smem(uint32_t N) { return kBatch * sizeof(uint2) + kCoarseRows * sizeof(uint64_t) + (size_t)2 * N * 4; }
 size_t quotient_smem(uint32_t N) { return (size_t)N * 8; }
 
 }  // namespace
