@@ -151,7 +151,7 @@ struct KNode {
     uint32_t is_root;  // roots also deliver the minimum weighted degree bound
     uint32_t small;    // entries fit in 32 bits (total graph weight < 2^32)
     uint32_t query;    // owner query (engine bookkeeping)
-    const uint64_t *mat;
+    const void *mat;   // N x N row-major: u32 entries when `small`, else u64
     MatBuf *buf;
     uint64_t *pre = nullptr;  // row sums (N) + 32-column block prefixes (N x ceil(N/32)), when made with the matrix
 };

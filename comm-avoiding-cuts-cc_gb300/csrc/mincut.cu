@@ -58,18 +58,18 @@ struct ShrinkDesc {
 struct DenseDesc {
     const uint32_t *U, *V, *W;
     const uint32_t *lab;  // nullable: identity
-    uint64_t *mat;
+    void *mat;            // k x k, u32 entries when `small`, else u64
     uint64_t m;
-    uint32_t k, pad;
+    uint32_t k, small;
 };
 
 struct SrcDesc {
-    const uint64_t *mat;  // N x N row-major
+    const void *mat;      // N x N row-major, u32 entries when `small`, else u64
     uint64_t *rowpre;     // N: inclusive prefix of row sums
     uint64_t *blk;        // N x nb: per row, inclusive prefix of 32-column block sums
     uint64_t *cut;        // the trial's cut (root matrices deliver the minimum weighted degree bound)
     uint32_t N, nb;
-    uint32_t is_root, pad;
+    uint32_t is_root, small;  // small: the graph's total weight is below 2^32
 };
 
 struct TaskDesc {
@@ -86,11 +86,21 @@ struct TaskDesc {
 };
 
 struct LeafDesc {
-    const uint64_t *mat;
+    const void *mat;  // u32 entries when `small`, else u64
     uint64_t *cut;
     uint32_t N;
     uint32_t small;  // entries fit in 32 bits
 };
+
+// Node matrices are stored with u32 entries when the graph's total weight is below 2^32 (every
+// entry, row sum and cut of every node fits), else u64.
+// Kernels that read or write node matrices are instantiated for one entry width Tm each and
+// skip the nodes of the other width; the host launches the u64 instance only when some node of
+// the step needs it.
+template <typename Tm>
+__device__ __forceinline__ bool width_is(uint32_t small) {
+    return (small != 0) == (sizeof(Tm) == 4);
+}
 
 // ---------------------------------------------------------------- block helpers
 
@@ -338,15 +348,21 @@ __global__ void dense_build_kernel(const DenseDesc *__restrict__ descs) {
             b = D.lab[b];
         }
         if (a == b) continue;
-        const unsigned long long w = D.W[e];
-        atomicAdd((unsigned long long *)&D.mat[(uint64_t)a * k + b], w);
-        atomicAdd((unsigned long long *)&D.mat[(uint64_t)b * k + a], w);
+        const uint32_t w = D.W[e];
+        if (D.small) {
+            atomicAdd(reinterpret_cast<uint32_t *>(D.mat) + (uint64_t)a * k + b, w);
+            atomicAdd(reinterpret_cast<uint32_t *>(D.mat) + (uint64_t)b * k + a, w);
+        } else {
+            atomicAdd(reinterpret_cast<unsigned long long *>(D.mat) + (uint64_t)a * k + b, (unsigned long long)w);
+            atomicAdd(reinterpret_cast<unsigned long long *>(D.mat) + (uint64_t)b * k + a, (unsigned long long)w);
+        }
     }
 }
 
 // ---------------------------------------------------------------- stage 3: Karger-Stein
 
 // One warp per matrix row: 32-column block prefixes and the row sum.
+template <typename Tm>
 __global__ void prep_rows_kernel(const SrcDesc *__restrict__ srcs, const uint64_t *__restrict__ row_off,
                                  uint32_t nsrc, uint64_t total_rows) {
     const uint64_t gw = ((uint64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
@@ -359,14 +375,15 @@ __global__ void prep_rows_kernel(const SrcDesc *__restrict__ srcs, const uint64_
     }
     const SrcDesc S = srcs[lo];
     const uint64_t i = gw - row_off[lo];
-    const uint64_t *row = S.mat + i * S.N;
+    if (!width_is<Tm>(S.small)) return;
+    const Tm *mat = reinterpret_cast<const Tm *>(S.mat) + i * S.N;
     uint64_t run = 0;
     for (uint32_t b0 = 0; b0 < S.nb; b0 += 8) {  // eight 32-column blocks per pass, loads in flight together
         uint64_t x[8];
 #pragma unroll
         for (int u = 0; u < 8; u++) {
             const uint32_t j = (b0 + u) * 32 + lane;
-            x[u] = (b0 + u < S.nb && j < S.N) ? __ldg(row + j) : 0;
+            x[u] = (b0 + u < S.nb && j < S.N) ? (uint64_t)__ldg(mat + j) : 0;
         }
 #pragma unroll
         for (int o = 16; o > 0; o >>= 1) {
@@ -400,7 +417,7 @@ __global__ void __launch_bounds__(NT) prefix_rows_kernel(const SrcDesc *__restri
     }
 }
 
-template <int NT>
+template <int NT, typename Tm>
 __global__ void __launch_bounds__(NT) contract_kernel(const TaskDesc *__restrict__ tasks,
                                                       const SrcDesc *__restrict__ srcs, uint32_t *__restrict__ k_out,
                                                       uint32_t *err) {
@@ -413,6 +430,8 @@ __global__ void __launch_bounds__(NT) contract_kernel(const TaskDesc *__restrict
     const uint32_t N = S.N;
     uint32_t *par = reinterpret_cast<uint32_t *>(dsm + kBatch * sizeof(uint2) + kCoarseRows * sizeof(uint64_t));
     uint32_t *cnt = par + N;  // counting-sort counters, N entries
+    if (!width_is<Tm>(S.small)) return;
+    const Tm *mat = reinterpret_cast<const Tm *>(S.mat);
     const uint64_t W = S.rowpre[N - 1];
     if (W == 0) {  // no edges between the vertices: the cut is 0, nothing to contract
         if (threadIdx.x == 0) {
@@ -448,7 +467,7 @@ __global__ void __launch_bounds__(NT) contract_kernel(const TaskDesc *__restrict
             const uint64_t *B = S.blk + (uint64_t)a * S.nb;
             const uint32_t b = (uint32_t)upper_bound_u64(B, S.nb, rem);
             const uint64_t rem2 = rem - (b ? B[b - 1] : 0);
-            const uint64_t *row = S.mat + (uint64_t)a * N + (uint64_t)b * 32;
+            const uint64_t rb = (uint64_t)a * N + (uint64_t)b * 32;
             const uint32_t lim = min(32u, N - b * 32);
             // column: first whose running sum exceeds rem2, eight entries loaded together per step
             uint64_t acc = 0;
@@ -456,7 +475,7 @@ __global__ void __launch_bounds__(NT) contract_kernel(const TaskDesc *__restrict
             for (uint32_t c0 = 0; c0 < lim && c == lim; c0 += 8) {
                 uint64_t x[8];
 #pragma unroll
-                for (int k = 0; k < 8; k++) x[k] = c0 + k < lim ? __ldg(row + c0 + k) : 0;
+                for (int k = 0; k < 8; k++) x[k] = c0 + k < lim ? (uint64_t)__ldg(mat + rb + c0 + k) : 0;
 #pragma unroll
                 for (int k = 0; k < 8; k++) {
                     acc += x[k];
@@ -507,13 +526,14 @@ __global__ void __launch_bounds__(NT) contract_kernel(const TaskDesc *__restrict
 // member rows of group a, accumulated column by column in shared memory (each thread owns its
 // columns, one pass per member row, coalesced reads); then every output column b gathers its
 // members' entries of that sum through the member lists (no atomics). The diagonal (b == a) is 0.
-template <int NT>
+template <int NT, typename Tm>
 __global__ void __launch_bounds__(NT) quotient_kernel(const TaskDesc *__restrict__ tasks,
                                                       const SrcDesc *__restrict__ srcs,
                                                       const uint32_t *__restrict__ kdim,
                                                       const uint64_t *__restrict__ group_task_off, uint32_t ntasks,
                                                       uint32_t rows, const uint64_t *__restrict__ out_off,
-                                                      uint64_t *out_base) {
+                                                      unsigned char *out_base) {
+    // out_off[i]: byte offset of task i's matrix in out_base
     extern __shared__ __align__(16) unsigned char dsm[];
     const uint64_t gg = blockIdx.x;
     uint32_t lo = 0, hi = ntasks - 1;
@@ -526,27 +546,28 @@ __global__ void __launch_bounds__(NT) quotient_kernel(const TaskDesc *__restrict
     const uint32_t k = kdim[lo];
     const uint32_t N = S.N;
     const uint32_t a0 = (uint32_t)(gg - group_task_off[lo]) * rows, a1 = min(k, a0 + rows);
+    if (!width_is<Tm>(S.small)) return;
+    const Tm *mat = reinterpret_cast<const Tm *>(S.mat);
     uint64_t *rowsum = reinterpret_cast<uint64_t *>(dsm);  // N entries
-    uint64_t *Qt = out_base + out_off[lo];
+    Tm *Qt = reinterpret_cast<Tm *>(out_base + out_off[lo]);
     for (uint32_t a = a0; a < a1; a++) {
         const uint32_t p0 = T.memb_off[a], p1 = T.memb_off[a + 1];
         for (uint32_t p = p0; p < p1; p++) {
-            const uint64_t *row = S.mat + (uint64_t)T.members[p] * N;
+            const uint64_t rb = (uint64_t)T.members[p] * N;
             if (p == p0) {
-                for (uint32_t j = threadIdx.x; j < N; j += NT) rowsum[j] = row[j];
+                for (uint32_t j = threadIdx.x; j < N; j += NT) rowsum[j] = __ldg(mat + rb + j);
             } else {
-                for (uint32_t j = threadIdx.x; j < N; j += NT) rowsum[j] += row[j];
+                for (uint32_t j = threadIdx.x; j < N; j += NT) rowsum[j] += __ldg(mat + rb + j);
             }
         }
         __syncthreads();
-        uint64_t *Q = Qt + (uint64_t)a * k;
         for (uint32_t b = threadIdx.x; b < k; b += NT) {
             uint64_t acc = 0;
             if (b != a) {
                 const uint32_t q1 = T.memb_off[b + 1];
                 for (uint32_t q = T.memb_off[b]; q < q1; q++) acc += rowsum[T.members[q]];
             }
-            Q[b] = acc;
+            Qt[(uint64_t)a * k + b] = (Tm)acc;
         }
         __syncthreads();
     }
@@ -565,15 +586,17 @@ __device__ __forceinline__ void sadd(uint64_t *p, uint64_t v) {
 // zeroed, and writes the row's 32-column block prefixes and its sum (the next step's row prep).
 // Shared memory: the labels, then one k-entry row per warp.
 //   Q[a][b] = sum over u in group a, v in group b of A[u][v]
-template <typename Ts>
+template <typename Ts, typename Tm>
 __global__ void __launch_bounds__(256) quotient_warp_kernel(const TaskDesc *__restrict__ tasks,
                                                             const SrcDesc *__restrict__ srcs,
                                                             const uint32_t *__restrict__ kdim,
                                                             const uint64_t *__restrict__ group_task_off,
                                                             uint32_t ntasks, uint32_t rows,
-                                                            const uint64_t *__restrict__ out_off, uint64_t *out_base,
-                                                            uint32_t lab_words, uint32_t kmax) {
-    // out_off[ntasks + i]: where task i's row sums and block prefixes go (the next step's row prep)
+                                                            const uint64_t *__restrict__ out_off,
+                                                            unsigned char *out_base, uint32_t lab_words,
+                                                            uint32_t kmax) {
+    // out_off[i]: byte offset of task i's matrix; out_off[ntasks + i]: of its row sums and block
+    // prefixes (the next step's row prep)
     extern __shared__ __align__(16) unsigned char dsm[];
     const uint64_t gg = blockIdx.x;
     uint32_t lo = 0, hi = ntasks - 1;
@@ -586,15 +609,17 @@ __global__ void __launch_bounds__(256) quotient_warp_kernel(const TaskDesc *__re
     const uint32_t k = kdim[lo];
     const uint32_t N = S.N;
     const uint32_t a0 = (uint32_t)(gg - group_task_off[lo]) * rows, a1 = min(k, a0 + rows);
+    if (!width_is<Tm>(S.small)) return;
+    const Tm *mat = reinterpret_cast<const Tm *>(S.mat);
     uint32_t *s_lab = reinterpret_cast<uint32_t *>(dsm);  // N
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
     // Ts: uint32_t when the graph's total weight is below 2^32 (every entry and row sum fits)
     Ts *qrow = reinterpret_cast<Ts *>(dsm + (size_t)lab_words * 4) + (size_t)warp * kmax;
     for (uint32_t i = threadIdx.x; i < N; i += blockDim.x) s_lab[i] = T.lab[i];
     __syncthreads();
-    uint64_t *Qt = out_base + out_off[lo];
-    uint64_t *rowsum_out = out_base + out_off[ntasks + lo];
-    const bool small = T.pad != 0;
+    Tm *Qt = reinterpret_cast<Tm *>(out_base + out_off[lo]);
+    uint64_t *rowsum_out = reinterpret_cast<uint64_t *>(out_base + out_off[ntasks + lo]);
+    const uint32_t small = S.small;
     const uint32_t nbk = (k + 31) / 32;
     uint64_t *blk = rowsum_out + k;
     for (uint32_t a = a0 + warp; a < a1; a += nw) {
@@ -604,11 +629,11 @@ __global__ void __launch_bounds__(256) quotient_warp_kernel(const TaskDesc *__re
         for (uint32_t j0 = 0; j0 < N; j0 += 256) {
             uint64_t x[8] = {0, 0, 0, 0, 0, 0, 0, 0};
             for (uint32_t p = p0; p < p1; p++) {
-                const uint64_t *row = S.mat + (uint64_t)T.members[p] * N;
+                const uint64_t rb = (uint64_t)T.members[p] * N;
 #pragma unroll
                 for (int u = 0; u < 8; u++) {
                     const uint32_t j = j0 + u * 32 + lane;
-                    if (j < N) x[u] += __ldg(row + j);
+                    if (j < N) x[u] += __ldg(mat + rb + j);
                 }
             }
 #pragma unroll
@@ -618,7 +643,7 @@ __global__ void __launch_bounds__(256) quotient_warp_kernel(const TaskDesc *__re
             }
         }
         __syncwarp();
-        uint64_t *Q = Qt + (uint64_t)a * k;
+        const uint64_t qb = (uint64_t)a * k;
         uint64_t run = 0;
         for (uint32_t b0 = 0; b0 < k; b0 += 128) {  // four 32-column blocks per pass (warp-uniform trip count)
             uint64_t acc[4];
@@ -626,7 +651,7 @@ __global__ void __launch_bounds__(256) quotient_warp_kernel(const TaskDesc *__re
             for (int u = 0; u < 4; u++) {
                 const uint32_t b = b0 + 32 * u + lane;
                 acc[u] = (b < k && b != a) ? (uint64_t)qrow[b] : 0;
-                if (b < k) Q[b] = acc[u];
+                if (b < k) Qt[qb + b] = (Tm)acc[u];
             }
 #pragma unroll
             for (int u = 0; u < 4; u++) {
@@ -706,7 +731,7 @@ __global__ void __launch_bounds__(32) sw_leaf_kernel(const LeafDesc *__restrict_
     for (uint32_t x = lane; x < N * H; x += 32) {
         const uint32_t i = x / H, d = x - i * H + 1;
         const uint32_t j = i + d < N ? i + d : i + d - N;
-        M[x] = (Tm)L.mat[(size_t)i * N + j];
+        M[x] = __ldg(reinterpret_cast<const Tm *>(L.mat) + (size_t)i * N + j);
     }
     for (uint32_t x = lane; x < 128; x += 32) uf[x] = (uint8_t)x;
     __syncwarp();
@@ -1025,7 +1050,7 @@ int KsEngine::step() {
         S.nb = (nd.N + 31) / 32;
         S.cut = nd.cut;
         S.is_root = nd.is_root;
-        S.pad = 0;
+        S.small = nd.small;
         if (nd.pre) {
             S.rowpre = nd.pre;
         } else {
@@ -1041,9 +1066,15 @@ int KsEngine::step() {
     if (rows) {
         CAC_TRY(upload(ctx_, d_rowoff, row_off));
         CAC_TRY(upload(ctx_, d_psrc, psrcs));
-        prep_rows_kernel<<<(unsigned)((rows * 32 + 255) / 256), 256, 0, s>>>(d_psrc.as<SrcDesc>(),
-                                                                             d_rowoff.as<uint64_t>(),
-                                                                             (uint32_t)row_off.size(), rows);
+        bool p32 = false, p64 = false;
+        for (const SrcDesc &S : psrcs) (S.small ? p32 : p64) = true;
+        const unsigned pg = (unsigned)((rows * 32 + 255) / 256);
+        if (p32)
+            prep_rows_kernel<uint32_t><<<pg, 256, 0, s>>>(d_psrc.as<SrcDesc>(), d_rowoff.as<uint64_t>(),
+                                                          (uint32_t)row_off.size(), rows);
+        if (p64)
+            prep_rows_kernel<uint64_t><<<pg, 256, 0, s>>>(d_psrc.as<SrcDesc>(), d_rowoff.as<uint64_t>(),
+                                                          (uint32_t)row_off.size(), rows);
     }
     prefix_rows_kernel<kNT><<<(unsigned)srcs.size(), kNT, 0, s>>>(d_src.as<SrcDesc>());
 
@@ -1075,11 +1106,20 @@ int KsEngine::step() {
     }
     CAC_TRY(upload(ctx_, d_task, td));
     CAC_TRY(d_kout.ensure(tasks.size() * 4));
+    bool t32 = false, t64 = false;  // entry widths present among the tasks' sources
+    for (const KTask &t : tasks) (t.src.small ? t32 : t64) = true;
     {
         const size_t sm = contract_smem(maxN);
-        CAC_TRY(smem_optin(ctx_, contract_kernel<kNT>));
-        contract_kernel<kNT><<<(unsigned)tasks.size(), kNT, sm, s>>>(d_task.as<TaskDesc>(), d_src.as<SrcDesc>(),
-                                                                     d_kout.as<uint32_t>(), d_err);
+        if (t32) {
+            CAC_TRY(smem_optin(ctx_, contract_kernel<kNT, uint32_t>));
+            contract_kernel<kNT, uint32_t><<<(unsigned)tasks.size(), kNT, sm, s>>>(
+                d_task.as<TaskDesc>(), d_src.as<SrcDesc>(), d_kout.as<uint32_t>(), d_err);
+        }
+        if (t64) {
+            CAC_TRY(smem_optin(ctx_, contract_kernel<kNT, uint64_t>));
+            contract_kernel<kNT, uint64_t><<<(unsigned)tasks.size(), kNT, sm, s>>>(
+                d_task.as<TaskDesc>(), d_src.as<SrcDesc>(), d_kout.as<uint32_t>(), d_err);
+        }
         CAC_CUDA_TRY(cudaGetLastError());
     }
     std::vector<uint32_t> kk(tasks.size());
@@ -1089,15 +1129,15 @@ int KsEngine::step() {
     // quotient matrices of this step, in one stream-ordered buffer
     std::vector<uint64_t> out_off(tasks.size(), 0), group_task_off(tasks.size(), 0);
     std::vector<uint32_t> kq(tasks.size(), 0);
-    uint64_t out_elems = 0, groups = 0;
+    uint64_t out_bytes = 0, groups = 0;
     size_t qsm = 0;
     const uint32_t qrows = std::max<uint32_t>(1, std::min<uint32_t>(16, 4096 / std::max<uint32_t>(maxN, 1)));
     for (size_t i = 0; i < tasks.size(); i++) {
         const uint32_t k = kk[i] == kDropped ? 0 : kk[i];
         kq[i] = k;
-        out_off[i] = out_elems;
+        out_off[i] = out_bytes;
         group_task_off[i] = groups;
-        out_elems += (uint64_t)k * k;
+        out_bytes += ((uint64_t)k * k * (tasks[i].src.small ? 4 : 8) + 15) / 16 * 16;
         groups += (k + qrows - 1) / qrows;
         if (k) qsm = std::max(qsm, quotient_smem(tasks[i].src.N));
     }
@@ -1123,29 +1163,42 @@ int KsEngine::step() {
         for (size_t i = 0; i < tasks.size(); i++) {
             group_task_off[i] = groups;
             groups += (kq[i] + wrows - 1) / wrows;
-            out_off[tasks.size() + i] = out_elems;
-            out_elems += kq[i] + (uint64_t)kq[i] * ((kq[i] + 31) / 32);
+            out_off[tasks.size() + i] = out_bytes;
+            out_bytes += ((kq[i] + (uint64_t)kq[i] * ((kq[i] + 31) / 32)) * 8 + 15) / 16 * 16;
         }
     }
     MatBuf *out = nullptr;
     if (groups) {
-        CAC_TRY(alloc(out_elems * 8, &out));
+        CAC_TRY(alloc(out_bytes, &out));
         CAC_TRY(upload(ctx_, d_qoff, out_off));
         CAC_TRY(upload(ctx_, d_gto, group_task_off));
         CAC_CUDA_TRY(cudaMemcpyAsync(d_kout.p, kq.data(), tasks.size() * 4, cudaMemcpyHostToDevice, s));
         if (qwarps) {
+            // shared rows are u32 only when every task's sums fit (all sources small)
             const size_t wsm = stage_words * 4 + (size_t)qwarps * kmax * rs_bytes;
-            auto kern = all_small ? quotient_warp_kernel<uint32_t> : quotient_warp_kernel<uint64_t>;
-            CAC_TRY(smem_optin(ctx_, kern));
-            kern<<<(unsigned)groups, qwarps * 32, wsm, s>>>(
-                d_task.as<TaskDesc>(), d_src.as<SrcDesc>(), d_kout.as<uint32_t>(), d_gto.as<uint64_t>(),
-                (uint32_t)tasks.size(), wrows, d_qoff.as<uint64_t>(), static_cast<uint64_t *>(out->p),
-                (uint32_t)stage_words, kmax);
+            std::vector<decltype(&quotient_warp_kernel<uint32_t, uint32_t>)> kerns;
+            if (all_small) kerns.push_back(quotient_warp_kernel<uint32_t, uint32_t>);
+            else {
+                if (t32) kerns.push_back(quotient_warp_kernel<uint64_t, uint32_t>);
+                if (t64) kerns.push_back(quotient_warp_kernel<uint64_t, uint64_t>);
+            }
+            for (auto kern : kerns) {
+                CAC_TRY(smem_optin(ctx_, kern));
+                kern<<<(unsigned)groups, qwarps * 32, wsm, s>>>(
+                    d_task.as<TaskDesc>(), d_src.as<SrcDesc>(), d_kout.as<uint32_t>(), d_gto.as<uint64_t>(),
+                    (uint32_t)tasks.size(), wrows, d_qoff.as<uint64_t>(), static_cast<unsigned char *>(out->p),
+                    (uint32_t)stage_words, kmax);
+            }
         } else {
-            CAC_TRY(smem_optin(ctx_, quotient_kernel<kQT>));
-            quotient_kernel<kQT><<<(unsigned)groups, kQT, qsm, s>>>(
-                d_task.as<TaskDesc>(), d_src.as<SrcDesc>(), d_kout.as<uint32_t>(), d_gto.as<uint64_t>(),
-                (uint32_t)tasks.size(), qrows, d_qoff.as<uint64_t>(), static_cast<uint64_t *>(out->p));
+            std::vector<decltype(&quotient_kernel<kQT, uint32_t>)> kerns;
+            if (t32) kerns.push_back(quotient_kernel<kQT, uint32_t>);
+            if (t64) kerns.push_back(quotient_kernel<kQT, uint64_t>);
+            for (auto kern : kerns) {
+                CAC_TRY(smem_optin(ctx_, kern));
+                kern<<<(unsigned)groups, kQT, qsm, s>>>(
+                    d_task.as<TaskDesc>(), d_src.as<SrcDesc>(), d_kout.as<uint32_t>(), d_gto.as<uint64_t>(),
+                    (uint32_t)tasks.size(), qrows, d_qoff.as<uint64_t>(), static_cast<unsigned char *>(out->p));
+            }
         }
         CAC_CUDA_TRY(cudaGetLastError());
     }
@@ -1160,8 +1213,9 @@ int KsEngine::step() {
         nd.h = t.h;
         nd.N = k;
         nd.is_root = 0;
-        nd.mat = static_cast<uint64_t *>(out->p) + out_off[i];
-        nd.pre = qwarps ? static_cast<uint64_t *>(out->p) + out_off[tasks.size() + i] : nullptr;
+        nd.mat = static_cast<unsigned char *>(out->p) + out_off[i];
+        nd.pre = qwarps ? reinterpret_cast<uint64_t *>(static_cast<unsigned char *>(out->p) + out_off[tasks.size() + i])
+                        : nullptr;
         nd.buf = out;
         out->refs++;
         outstanding[nd.query]++;
@@ -1203,11 +1257,12 @@ int admit(cac_ctx *ctx, KsEngine &eng, const QueryPlan &q) {
     if (q.t >= n) {
         // no pre-contraction: every trial starts from the same dense matrix, built once
         MatBuf *root = nullptr;
-        CAC_TRY(eng.alloc((size_t)n * n * 8, &root));
-        CAC_CUDA_TRY(cudaMemsetAsync(root->p, 0, (size_t)n * n * 8, s));
+        const size_t bytes = (size_t)n * n * (small ? 4 : 8);
+        CAC_TRY(eng.alloc(bytes, &root));
+        CAC_CUDA_TRY(cudaMemsetAsync(root->p, 0, bytes, s));
         if (m) {
             DevBuf d(ctx);
-            std::vector<DenseDesc> dd{DenseDesc{g->u, g->v, g->w, nullptr, static_cast<uint64_t *>(root->p), m, n, 0}};
+            std::vector<DenseDesc> dd{DenseDesc{g->u, g->v, g->w, nullptr, root->p, m, n, small}};
             CAC_TRY(upload(ctx, d, dd));
             dim3 grid((unsigned)std::max<uint64_t>(1, std::min<uint64_t>((m + 255) / 256, (uint64_t)ctx->num_sms * 8)), 1);
             dense_build_kernel<<<grid, 256, 0, s>>>(d.as<DenseDesc>());
@@ -1217,7 +1272,7 @@ int admit(cac_ctx *ctx, KsEngine &eng, const QueryPlan &q) {
         root->refs++;  // held until every root node has been added
         for (uint64_t i = 0; i < q.trials; i++) {
             const uint32_t r = (uint32_t)(i / q.per_rank), idx = (uint32_t)(i % q.per_rank);
-            eng.add(KNode{q.cuts + i, q.seed + r, idx, 1, n, 1, small, q.query, static_cast<uint64_t *>(root->p), root});
+            eng.add(KNode{q.cuts + i, q.seed + r, idx, 1, n, 1, small, q.query, root->p, root});
         }
         eng.release(root);
         return CAC_OK;
@@ -1276,18 +1331,19 @@ int admit(cac_ctx *ctx, KsEngine &eng, const QueryPlan &q) {
                 isolated[b] = 1;
                 kdim[b] = 0;
             }
-        uint64_t elems = 0;
-        for (uint32_t b = 0; b < B; b++) elems += (uint64_t)kdim[b] * kdim[b];
+        const uint64_t esize = small ? 4 : 8;
+        uint64_t bytes = 0;
+        for (uint32_t b = 0; b < B; b++) bytes += ((uint64_t)kdim[b] * kdim[b] * esize + 15) / 16 * 16;
         MatBuf *roots = nullptr;
-        CAC_TRY(eng.alloc(std::max<uint64_t>(elems, 1) * 8, &roots));
-        CAC_CUDA_TRY(cudaMemsetAsync(roots->p, 0, elems * 8, s));
+        CAC_TRY(eng.alloc(std::max<uint64_t>(bytes, 16), &roots));
+        CAC_CUDA_TRY(cudaMemsetAsync(roots->p, 0, bytes, s));
         std::vector<DenseDesc> dd(B);
         uint64_t off = 0;
         for (uint32_t b = 0; b < B; b++) {
             // no scatter for a trial without a matrix (its labels would index past the buffer)
-            dd[b] = DenseDesc{g->u, g->v, g->w, sd[b].lab, static_cast<uint64_t *>(roots->p) + off,
-                              kdim[b] >= 2 ? m : 0, kdim[b], 0};
-            off += (uint64_t)kdim[b] * kdim[b];
+            dd[b] = DenseDesc{g->u, g->v, g->w, sd[b].lab, static_cast<unsigned char *>(roots->p) + off,
+                              kdim[b] >= 2 ? m : 0, kdim[b], small};
+            off += ((uint64_t)kdim[b] * kdim[b] * esize + 15) / 16 * 16;
         }
         CAC_TRY(upload(ctx, d_dd, dd));
         if (m) {
@@ -1392,18 +1448,32 @@ int mincut_trials(cac_ctx *ctx, const cac_graph *g, uint32_t seed, uint32_t rank
     return mincut_run_queries(ctx, q, device_ms);
 }
 
+// A dense host matrix for the device: checks the weight bound and, when the total weight is below
+// 2^32 (and so every entry), narrows it to the u32 node storage.
+int host_matrix(uint32_t n, const uint64_t *mat_host, uint32_t *small, std::vector<uint32_t> &narrow) {
+    uint64_t total = 0, top = 0;
+    for (uint64_t i = 0; i < (uint64_t)n * n; i++) {
+        total += mat_host[i];
+        top = std::max(top, mat_host[i]);
+    }
+    if (total / 2 >= (1ull << 55)) {
+        set_error("total edge weight >= 2^55 is not supported");
+        return CAC_ERR_UNSUPPORTED;
+    }
+    *small = (total / 2 < (1ull << 32) && top < (1ull << 32)) ? 1u : 0u;
+    if (*small) narrow.assign(mat_host, mat_host + (uint64_t)n * n);
+    return CAC_OK;
+}
+
 int ks_dense_one(cac_ctx *ctx, uint32_t n, const uint64_t *mat_host, uint32_t seed, uint32_t rank, uint32_t trial,
                  uint64_t *cut) {
     if (n > kMaxSmemVertices) {
         set_error("dense Karger-Stein supports at most 16384 vertices");
         return CAC_ERR_UNSUPPORTED;
     }
-    uint64_t total = 0;
-    for (uint64_t i = 0; i < (uint64_t)n * n; i++) total += mat_host[i];
-    if (total / 2 >= (1ull << 55)) {
-        set_error("total edge weight >= 2^55 is not supported");
-        return CAC_ERR_UNSUPPORTED;
-    }
+    std::vector<uint32_t> narrow;
+    uint32_t small = 0;
+    CAC_TRY(host_matrix(n, mat_host, &small, narrow));
     cudaStream_t s = ctx->stream;
     DevBuf d_cut(ctx);
     CAC_TRY(d_cut.ensure(8));
@@ -1411,11 +1481,12 @@ int ks_dense_one(cac_ctx *ctx, uint32_t n, const uint64_t *mat_host, uint32_t se
         KsEngine eng(ctx);
         CAC_TRY(eng.init_err());
         MatBuf *root = nullptr;
-        CAC_TRY(eng.alloc((size_t)n * n * 8, &root));
-        CAC_CUDA_TRY(cudaMemcpyAsync(root->p, mat_host, (size_t)n * n * 8, cudaMemcpyHostToDevice, s));
+        const size_t bytes = (size_t)n * n * (small ? 4 : 8);
+        CAC_TRY(eng.alloc(bytes, &root));
+        CAC_CUDA_TRY(cudaMemcpyAsync(root->p, small ? (const void *)narrow.data() : (const void *)mat_host, bytes,
+                                     cudaMemcpyHostToDevice, s));
         fill_u64<<<1, 32, 0, s>>>(d_cut.as<uint64_t>(), 1, kU64Max);
-        eng.add(KNode{d_cut.as<uint64_t>(), seed + rank, trial, 1, n, 1, total / 2 < (1ull << 32) ? 1u : 0u, 0,
-                      static_cast<uint64_t *>(root->p), root});
+        eng.add(KNode{d_cut.as<uint64_t>(), seed + rank, trial, 1, n, 1, small, 0, root->p, root});
         while (!eng.idle()) CAC_TRY(eng.step());
         uint32_t err = 0;
         CAC_TRY(eng.read_err(&err));
@@ -1430,20 +1501,18 @@ int ks_dense_one(cac_ctx *ctx, uint32_t n, const uint64_t *mat_host, uint32_t se
 }
 
 int exact_small(cac_ctx *ctx, uint32_t n, const uint64_t *mat_host, uint64_t *cut) {
-    uint64_t total = 0;
-    for (uint64_t i = 0; i < (uint64_t)n * n; i++) total += mat_host[i];
-    if (total / 2 >= (1ull << 55)) {
-        set_error("total edge weight >= 2^55 is not supported");
-        return CAC_ERR_UNSUPPORTED;
-    }
+    std::vector<uint32_t> narrow;
+    uint32_t small = 0;
+    CAC_TRY(host_matrix(n, mat_host, &small, narrow));
     cudaStream_t s = ctx->stream;
     DevBuf buf(ctx), d_cuts(ctx), d_leaf(ctx);
-    CAC_TRY(buf.ensure((size_t)n * n * 8));
+    const size_t bytes = (size_t)n * n * (small ? 4 : 8);
+    CAC_TRY(buf.ensure(bytes));
     CAC_TRY(d_cuts.ensure(8));
-    CAC_CUDA_TRY(cudaMemcpyAsync(buf.p, mat_host, (size_t)n * n * 8, cudaMemcpyHostToDevice, s));
+    CAC_CUDA_TRY(cudaMemcpyAsync(buf.p, small ? (const void *)narrow.data() : (const void *)mat_host, bytes,
+                                 cudaMemcpyHostToDevice, s));
     fill_u64<<<1, 32, 0, s>>>(d_cuts.as<uint64_t>(), 1, kU64Max);
-    const uint32_t small = total / 2 < (1ull << 32) ? 1u : 0u;
-    std::vector<LeafDesc> leaves{LeafDesc{buf.as<uint64_t>(), d_cuts.as<uint64_t>(), n, small}};
+    std::vector<LeafDesc> leaves{LeafDesc{buf.p, d_cuts.as<uint64_t>(), n, small}};
     CAC_TRY(upload(ctx, d_leaf, leaves));
     if (small) {
         const size_t sm = leaf_smem(n, true);

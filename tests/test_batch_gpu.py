@@ -48,3 +48,21 @@ def test_batch_per_trial_values_unchanged(ctx):
 
 def test_empty_batch(ctx):
     assert ctx.mincut_batch([], 0.9) == []
+
+
+def test_batch_mixes_entry_widths(ctx):
+    # graphs whose total weight is at or above 2^32 keep u64 matrix entries, the others u32; one
+    # batch holds both kinds in the same engine steps, and every answer is the exact cut
+    light = [graphgen.erdos_renyi(150, 0.1, 21), graphgen.watts_strogatz(300, 8, 0.3, 22, wmax=100)]
+    heavy = []
+    for seed in (23, 24):
+        n, u, v, _ = graphgen.erdos_renyi(140, 0.12, seed)
+        w = graphgen.weights(seed, len(u), 2**31, 2**30)  # total weight far above 2^32
+        heavy.append((n, u, v, w))
+    specs = [light[0], heavy[0], light[1], heavy[1]]
+    assert sum(int(w.astype(np.uint64).sum()) >= 2**32 for _, _, _, w in specs) == 2
+    graphs = [ctx.graph(*sp) for sp in specs]
+    res = ctx.mincut_batch(graphs, 0.9, seeds=[5, 6, 7, 8])
+    for sp, g, r, sd in zip(specs, graphs, res, [5, 6, 7, 8]):
+        assert r.cut == O.exact_mincut(*sp)
+        assert r.cut == g.square_root(0.9, seed=sd).cut
