@@ -119,6 +119,9 @@ EXPORTS = [
                                       ctypes.POINTER(ApproxResult)]),
     ("cac_sitmo_blocks", ctypes.c_int, [_vp, _u64p, _u64p, ctypes.c_uint64, _vp]),
     ("cac_graph_generate", ctypes.c_int, [_vp, ctypes.POINTER(GenSpec), ctypes.POINTER(_vp)]),
+    ("cac_click_edges", ctypes.c_int, [ctypes.c_uint32, ctypes.c_uint32, ctypes.c_uint32, _vp, _vp, _vp,
+                                       ctypes.c_uint64, _u64p]),
+    ("cac_graph_click", ctypes.c_int, [_vp, ctypes.c_uint32, ctypes.c_uint32, ctypes.c_uint32, ctypes.POINTER(_vp)]),
     ("cac_server_create", ctypes.c_int, [ctypes.POINTER(_ServerConfig), ctypes.POINTER(_vp)]),
     ("cac_server_graph", ctypes.c_int, [_vp, ctypes.c_uint32, ctypes.c_uint64, _vp, _vp, _vp, ctypes.POINTER(_vp)]),
     ("cac_server_generate", ctypes.c_int, [_vp, ctypes.POINTER(GenSpec), ctypes.POINTER(_vp)]),
@@ -213,6 +216,14 @@ class Context:
         spec = GenSpec(GEN_FAMILIES[family], n, p, avg_degree, k, scale, edge_factor, a, b, c, seed, wmin, wmax)
         h = _vp()
         _check(lib().cac_graph_generate(self.h, ctypes.byref(spec), ctypes.byref(h)), "cac_graph_generate")
+        g = Graph(self, h, None)
+        self._graphs.add(g)
+        return g
+
+    def click(self, n, virtual_ranks=1, seed=0):
+        """The reference's CLICK graph on the device (cac_graph_click)."""
+        h = _vp()
+        _check(lib().cac_graph_click(self.h, n, virtual_ranks, seed, ctypes.byref(h)), "cac_graph_click")
         g = Graph(self, h, None)
         self._graphs.add(g)
         return g
@@ -412,6 +423,17 @@ class Server:
             self.close()
         except Exception:
             pass
+
+
+def click_edges(n, virtual_ranks=1, seed=0):
+    """The reference's CLICK graph (host code, no device) -> (n, u, v, w)."""
+    m = ctypes.c_uint64()
+    _check(lib().cac_click_edges(n, virtual_ranks, seed, None, None, None, 0, ctypes.byref(m)), "cac_click_edges")
+    k = int(m.value)
+    u, v, w = (np.zeros(max(k, 1), np.uint32) for _ in range(3))
+    _check(lib().cac_click_edges(n, virtual_ranks, seed, ctypes.c_void_p(u.ctypes.data), ctypes.c_void_p(v.ctypes.data),
+                                 ctypes.c_void_p(w.ctypes.data), k, ctypes.byref(m)), "cac_click_edges")
+    return n, u[:k], v[:k], w[:k]
 
 
 def parse_file(path):

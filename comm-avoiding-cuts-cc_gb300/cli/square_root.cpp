@@ -15,23 +15,26 @@ int main(int argc, char *argv[]) {
     }
     float success_probability{std::stof(argv[1], nullptr)};
     uint32_t seed = {(uint32_t)std::stoi(argv[argc == 4 ? 3 : 4])};
-    if (std::string(argv[2]) == "CLICK") {
-        std::cerr << "square_root: the in-memory CLICK generator is not part of this build; write the graph "
-                     "to an edge-list file instead"
-                  << std::endl;
-        return 2;
-    }
     const unsigned ranks = cli_virtual_ranks();
     cac_config cfg{cli_device(), nullptr, 0};
     cac_ctx *ctx = nullptr;
     int st = cac_ctx_create(&cfg, &ctx);
     if (st) return cli_fail("cac_ctx_create", st);
     cac_graph *g = nullptr;
-    st = cac_graph_load_file(ctx, argv[2], &g);
-    if (st) return cli_fail("cac_graph_load_file", st);
     uint32_t n = 0;
     uint64_t m = 0;
-    cac_graph_info(g, &n, &m, nullptr);
+    if (std::string(argv[2]) == "CLICK") {
+        // the in-memory complete graph of the reference (CLICK::generateSlice on every rank); like
+        // the reference, the CSV line reports its n (n - 1) / 2 enumerated edges
+        n = (uint32_t)std::stoul(argv[3]);
+        st = cac_graph_click(ctx, n, ranks, seed, &g);
+        if (st) return cli_fail("cac_graph_click", st);
+        m = (uint64_t)n * (n - 1) / 2;
+    } else {
+        st = cac_graph_load_file(ctx, argv[2], &g);
+        if (st) return cli_fail("cac_graph_load_file", st);
+        cac_graph_info(g, &n, &m, nullptr);
+    }
     cac_mincut_result res{};
     st = cac_mincut(ctx, g, success_probability, seed, ranks, &res);
     if (st) return cli_fail("cac_mincut", st);

@@ -206,6 +206,18 @@ typedef struct {
 } cac_gen_spec;
 int cac_graph_generate(cac_ctx *ctx, const cac_gen_spec *spec, cac_graph **out);
 
+/* ---- CLICK: the reference's in-memory test graph ----
+ * The graph that `square_root|approx_cut PROB CLICK SIZE SEED` builds: the reference's
+ * CLICK::generateSlice (src/input/CLICK.hpp:10-49) on every virtual rank r with seed + r, as
+ * ApproximateCut::loadFromCLICK does (ApproximateCut.hpp:35, :70-82). K_n in 10 clusters; rank r's
+ * enumeration slice gets weights max(0, N(8,4)) (same cluster) or max(0, N(4,4)) from
+ * std::mt19937(seed + r), truncated; the E mod P leftover edges belong to no rank, as in the
+ * reference. Host code: cac_click_edges needs no device (u == NULL returns the edge count in *m;
+ * the arrays must hold it). */
+int cac_click_edges(uint32_t n, uint32_t virtual_ranks, uint32_t seed, uint32_t *u, uint32_t *v, uint32_t *w,
+                    uint64_t capacity, uint64_t *m);
+int cac_graph_click(cac_ctx *ctx, uint32_t n, uint32_t virtual_ranks, uint32_t seed, cac_graph **out);
+
 /* ---- serving loop ----
  * The reference answers one query per process launch. A cac_server keeps graphs resident in HBM
  * and answers square_root, approx_cut and parallel_cc queries as they arrive:

@@ -74,6 +74,10 @@ CUT_SPECS = [
 ]
 
 
+# (vertices, ranks, seed) of the CLICK graphs pinned against the reference's generator
+CLICK_CASES = [(2, 1, 0), (12, 2, 5), (50, 1, 0), (101, 3, 7), (120, 4, 11), (700, 5, 42), (2000, 1, 3)]
+
+
 def main():
     if not os.path.isdir(REF_TREE) or not os.path.exists(os.path.join(REF_BIN, "cc_labels")):
         sys.exit("needs the reference tree and oracle/_ref (make -C oracle/refbuild)")
@@ -121,6 +125,24 @@ def main():
             rec["square_root_cut"] = int(csv[-1])
             rec["square_root_trials"] = int(csv[7])
             out_cut.append(rec)
+    # 4. CLICK graphs (the reference's CLICK::generateSlice on every rank, via oracle/refbuild's
+    # click_edges harness) and their exact minimum cuts
+    out_click = []
+    with tempfile.TemporaryDirectory() as td:
+        for n, p, seed in CLICK_CASES:
+            toks = run("click_edges", n, p, seed).split()
+            k = int(toks[1])
+            a = np.array(toks[2:2 + 3 * k], dtype=np.uint64).reshape(k, 3)
+            u, v, w = (a[:, i].astype(np.uint32) for i in range(3))
+            rec = dict(n=n, ranks=p, seed=seed, m=k, total_weight=int(w.astype(np.uint64).sum()),
+                       edges_sha256=digest(np.concatenate([u, v, w])), first=[[int(x) for x in r] for r in a[:4]])
+            if n <= 120:
+                path = os.path.join(td, "click.in")
+                graphgen.write_graph(path, n, u, v, w, "click")
+                rec["exact_cut"] = int(run("exact_cut", path).strip())
+            out_click.append(rec)
+    with open(os.path.join(HERE, "click.json"), "w") as f:
+        json.dump(out_click, f, indent=1)
     with open(os.path.join(HERE, "cc_seeded.json"), "w") as f:
         json.dump(out_cc, f, indent=1)
     with open(os.path.join(HERE, "mincut_seeded.json"), "w") as f:

@@ -89,3 +89,22 @@ def test_malformed_file_fails_cleanly(tmp_path):
     p.write_text("hdr\n5 2\n0 1 1\n")
     out = _run("square_root", "0.95", str(p), "0")
     assert out.returncode == 1 and "malformed" in out.stderr
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("ranks", ["1", "3"])
+def test_click_square_root_and_approx_cut(golden, ranks):
+    # the in-memory CLICK graph: the CSV line reports n and the n (n - 1) / 2 enumerated pairs, and
+    # square_root's answer is the exact minimum cut of the graph the reference generates
+    case = next(c for c in golden("click.json") if c["n"] == 101 and c["ranks"] == 3)
+    seed = str(case["seed"])
+    out = _run("square_root", "0.95", "CLICK", "101", seed, env={"CAC_VIRTUAL_RANKS": ranks})
+    f = out.stdout.strip().split(",")
+    assert out.returncode == 0, out.stderr
+    assert f[0] == "CLICK" and f[1] == seed and f[2] == ranks and f[3] == "101" and f[4] == "5050"
+    if ranks == "3":
+        assert int(f[-1]) == case["exact_cut"]
+    out = _run("approx_cut", "0.9", "CLICK", "101", seed, env={"CAC_VIRTUAL_RANKS": ranks})
+    assert out.returncode == 0, out.stderr
+    f = out.stdout.strip().split(",")
+    assert f[0] == "CLICK" and f[3] == "101" and f[4] == "5050" and int(f[-1]) >= 1

@@ -160,3 +160,16 @@ def test_large_disconnected_graph_trials(ctx):
     for i in range(3):
         assert int(got[0, i]) == O.mincut_trial(n, u, v, w, 1, 0, i) == 0
     assert g.square_root(0.5, seed=1).cut == 0
+
+
+def test_click_graph_on_device(golden, libcac, ctx):
+    # the device form of CLICK equals the host generator; square_root finds the exact cut that the
+    # reference's exact Stoer-Wagner reports for the reference's own CLICK graph
+    for case in golden("click.json"):
+        if "exact_cut" not in case or case["n"] < 3:
+            continue
+        g = ctx.click(case["n"], case["ranks"], case["seed"])
+        _, u, v, w = libcac.click_edges(case["n"], case["ranks"], case["seed"])
+        gu, gv, gw = g.edges()
+        assert np.array_equal(gu, u) and np.array_equal(gv, v) and np.array_equal(gw, w)
+        assert g.square_root(0.95, seed=case["seed"]).cut == case["exact_cut"]
