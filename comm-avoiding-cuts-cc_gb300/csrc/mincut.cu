@@ -32,6 +32,7 @@
 #include <algorithm>
 #include <cmath>
 #include <numeric>
+#include <type_traits>
 
 namespace cac {
 namespace {
@@ -97,6 +98,10 @@ struct LeafDesc {
 // Kernels that read or write node matrices are instantiated for one entry width Tm each and
 // skip the nodes of the other width; the host launches the u64 instance only when some node of
 // the step needs it.
+// Row stride of an N x N node matrix: N rounded up to a multiple of 4 entries, so that every row
+// starts on a 16-byte boundary (16-byte loads). Entries past column N - 1 are never used.
+__host__ __device__ __forceinline__ uint64_t ld_of(uint32_t N) { return ((uint64_t)N + 3) & ~(uint64_t)3; }
+
 template <typename Tm>
 __device__ __forceinline__ bool width_is(uint32_t small) {
     return (small != 0) == (sizeof(Tm) == 4);
@@ -340,7 +345,7 @@ __global__ void __launch_bounds__(NT) iss_shrink_kernel(const ShrinkDesc *__rest
 
 __global__ void dense_build_kernel(const DenseDesc *__restrict__ descs) {
     const DenseDesc D = descs[blockIdx.y];
-    const uint64_t k = D.k;
+    const uint64_t ldk = ld_of(D.k);
     for (uint64_t e = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; e < D.m; e += (uint64_t)gridDim.x * blockDim.x) {
         uint32_t a = D.U[e], b = D.V[e];
         if (D.lab) {
@@ -350,11 +355,11 @@ __global__ void dense_build_kernel(const DenseDesc *__restrict__ descs) {
         if (a == b) continue;
         const uint32_t w = D.W[e];
         if (D.small) {
-            atomicAdd(reinterpret_cast<uint32_t *>(D.mat) + (uint64_t)a * k + b, w);
-            atomicAdd(reinterpret_cast<uint32_t *>(D.mat) + (uint64_t)b * k + a, w);
+            atomicAdd(reinterpret_cast<uint32_t *>(D.mat) + (uint64_t)a * ldk + b, w);
+            atomicAdd(reinterpret_cast<uint32_t *>(D.mat) + (uint64_t)b * ldk + a, w);
         } else {
-            atomicAdd(reinterpret_cast<unsigned long long *>(D.mat) + (uint64_t)a * k + b, (unsigned long long)w);
-            atomicAdd(reinterpret_cast<unsigned long long *>(D.mat) + (uint64_t)b * k + a, (unsigned long long)w);
+            atomicAdd(reinterpret_cast<unsigned long long *>(D.mat) + (uint64_t)a * ldk + b, (unsigned long long)w);
+            atomicAdd(reinterpret_cast<unsigned long long *>(D.mat) + (uint64_t)b * ldk + a, (unsigned long long)w);
         }
     }
 }
@@ -376,7 +381,7 @@ __global__ void prep_rows_kernel(const SrcDesc *__restrict__ srcs, const uint64_
     const SrcDesc S = srcs[lo];
     const uint64_t i = gw - row_off[lo];
     if (!width_is<Tm>(S.small)) return;
-    const Tm *mat = reinterpret_cast<const Tm *>(S.mat) + i * S.N;
+    const Tm *mat = reinterpret_cast<const Tm *>(S.mat) + i * ld_of(S.N);
     uint64_t run = 0;
     for (uint32_t b0 = 0; b0 < S.nb; b0 += 8) {  // eight 32-column blocks per pass, loads in flight together
         uint64_t x[8];
@@ -467,7 +472,7 @@ __global__ void __launch_bounds__(NT) contract_kernel(const TaskDesc *__restrict
             const uint64_t *B = S.blk + (uint64_t)a * S.nb;
             const uint32_t b = (uint32_t)upper_bound_u64(B, S.nb, rem);
             const uint64_t rem2 = rem - (b ? B[b - 1] : 0);
-            const uint64_t rb = (uint64_t)a * N + (uint64_t)b * 32;
+            const uint64_t rb = (uint64_t)a * ld_of(N) + (uint64_t)b * 32;
             const uint32_t lim = min(32u, N - b * 32);
             // column: first whose running sum exceeds rem2, eight entries loaded together per step
             uint64_t acc = 0;
@@ -553,7 +558,7 @@ __global__ void __launch_bounds__(NT) quotient_kernel(const TaskDesc *__restrict
     for (uint32_t a = a0; a < a1; a++) {
         const uint32_t p0 = T.memb_off[a], p1 = T.memb_off[a + 1];
         for (uint32_t p = p0; p < p1; p++) {
-            const uint64_t rb = (uint64_t)T.members[p] * N;
+            const uint64_t rb = (uint64_t)T.members[p] * ld_of(N);
             if (p == p0) {
                 for (uint32_t j = threadIdx.x; j < N; j += NT) rowsum[j] = __ldg(mat + rb + j);
             } else {
@@ -567,7 +572,7 @@ __global__ void __launch_bounds__(NT) quotient_kernel(const TaskDesc *__restrict
                 const uint32_t q1 = T.memb_off[b + 1];
                 for (uint32_t q = T.memb_off[b]; q < q1; q++) acc += rowsum[T.members[q]];
             }
-            Qt[(uint64_t)a * k + b] = (Tm)acc;
+            Qt[(uint64_t)a * ld_of(k) + b] = (Tm)acc;
         }
         __syncthreads();
     }
@@ -611,6 +616,9 @@ __global__ void __launch_bounds__(256) quotient_warp_kernel(const TaskDesc *__re
     const uint32_t a0 = (uint32_t)(gg - group_task_off[lo]) * rows, a1 = min(k, a0 + rows);
     if (!width_is<Tm>(S.small)) return;
     const Tm *mat = reinterpret_cast<const Tm *>(S.mat);
+    constexpr int VEC = 16 / sizeof(Tm);  // columns per 16-byte load
+    using Vec = typename std::conditional<sizeof(Tm) == 4, uint4, ulonglong2>::type;
+    const uint64_t ldN = ld_of(N);
     uint32_t *s_lab = reinterpret_cast<uint32_t *>(dsm);  // N
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
     // Ts: uint32_t when the graph's total weight is below 2^32 (every entry and row sum fits)
@@ -626,24 +634,37 @@ __global__ void __launch_bounds__(256) quotient_warp_kernel(const TaskDesc *__re
         for (uint32_t b = lane; b < k; b += 32) qrow[b] = 0;
         __syncwarp();
         const uint32_t p0 = T.memb_off[a], p1 = T.memb_off[a + 1];
-        for (uint32_t j0 = 0; j0 < N; j0 += 256) {
-            uint64_t x[8] = {0, 0, 0, 0, 0, 0, 0, 0};
-            for (uint32_t p = p0; p < p1; p++) {
-                const uint64_t rb = (uint64_t)T.members[p] * N;
+        // 16-byte loads: lane l reads columns j0 + (32 u + l) VEC .. + VEC - 1 (4 loads per pass);
+        // the padding columns of a row are read but never scattered
+        for (uint32_t j0 = 0; j0 < N; j0 += 4 * 32 * VEC) {
+            Tm x[4][VEC];
 #pragma unroll
-                for (int u = 0; u < 8; u++) {
-                    const uint32_t j = j0 + u * 32 + lane;
-                    if (j < N) x[u] += __ldg(mat + rb + j);
+            for (int u = 0; u < 4; u++)
+#pragma unroll
+                for (int t = 0; t < VEC; t++) x[u][t] = 0;
+            for (uint32_t p = p0; p < p1; p++) {
+                const Vec *row = reinterpret_cast<const Vec *>(mat + (uint64_t)T.members[p] * ldN);
+#pragma unroll
+                for (int u = 0; u < 4; u++) {
+                    const uint32_t c = j0 + (u * 32 + lane) * VEC;
+                    if (c < N) {
+                        const Vec q = __ldg(row + c / VEC);
+                        const Tm *e = reinterpret_cast<const Tm *>(&q);
+#pragma unroll
+                        for (int t = 0; t < VEC; t++) x[u][t] += e[t];
+                    }
                 }
             }
 #pragma unroll
-            for (int u = 0; u < 8; u++) {
-                const uint32_t j = j0 + u * 32 + lane;
-                if (j < N && x[u]) sadd(&qrow[s_lab[j]], x[u]);
-            }
+            for (int u = 0; u < 4; u++)
+#pragma unroll
+                for (int t = 0; t < VEC; t++) {
+                    const uint32_t j = j0 + (u * 32 + lane) * VEC + t;
+                    if (j < N && x[u][t]) sadd(&qrow[s_lab[j]], (uint64_t)x[u][t]);
+                }
         }
         __syncwarp();
-        const uint64_t qb = (uint64_t)a * k;
+        const uint64_t qb = (uint64_t)a * ld_of(k);
         uint64_t run = 0;
         for (uint32_t b0 = 0; b0 < k; b0 += 128) {  // four 32-column blocks per pass (warp-uniform trip count)
             uint64_t acc[4];
@@ -731,7 +752,7 @@ __global__ void __launch_bounds__(32) sw_leaf_kernel(const LeafDesc *__restrict_
     for (uint32_t x = lane; x < N * H; x += 32) {
         const uint32_t i = x / H, d = x - i * H + 1;
         const uint32_t j = i + d < N ? i + d : i + d - N;
-        M[x] = __ldg(reinterpret_cast<const Tm *>(L.mat) + (size_t)i * N + j);
+        M[x] = __ldg(reinterpret_cast<const Tm *>(L.mat) + (size_t)i * ld_of(N) + j);
     }
     for (uint32_t x = lane; x < 128; x += 32) uf[x] = (uint8_t)x;
     __syncwarp();
@@ -1137,7 +1158,7 @@ int KsEngine::step() {
         kq[i] = k;
         out_off[i] = out_bytes;
         group_task_off[i] = groups;
-        out_bytes += ((uint64_t)k * k * (tasks[i].src.small ? 4 : 8) + 15) / 16 * 16;
+        out_bytes += ((uint64_t)k * ld_of(k) * (tasks[i].src.small ? 4 : 8) + 15) / 16 * 16;
         groups += (k + qrows - 1) / qrows;
         if (k) qsm = std::max(qsm, quotient_smem(tasks[i].src.N));
     }
@@ -1257,7 +1278,7 @@ int admit(cac_ctx *ctx, KsEngine &eng, const QueryPlan &q) {
     if (q.t >= n) {
         // no pre-contraction: every trial starts from the same dense matrix, built once
         MatBuf *root = nullptr;
-        const size_t bytes = (size_t)n * n * (small ? 4 : 8);
+        const size_t bytes = (size_t)n * ld_of(n) * (small ? 4 : 8);
         CAC_TRY(eng.alloc(bytes, &root));
         CAC_CUDA_TRY(cudaMemsetAsync(root->p, 0, bytes, s));
         if (m) {
@@ -1333,7 +1354,7 @@ int admit(cac_ctx *ctx, KsEngine &eng, const QueryPlan &q) {
             }
         const uint64_t esize = small ? 4 : 8;
         uint64_t bytes = 0;
-        for (uint32_t b = 0; b < B; b++) bytes += ((uint64_t)kdim[b] * kdim[b] * esize + 15) / 16 * 16;
+        for (uint32_t b = 0; b < B; b++) bytes += ((uint64_t)kdim[b] * ld_of(kdim[b]) * esize + 15) / 16 * 16;
         MatBuf *roots = nullptr;
         CAC_TRY(eng.alloc(std::max<uint64_t>(bytes, 16), &roots));
         CAC_CUDA_TRY(cudaMemsetAsync(roots->p, 0, bytes, s));
@@ -1343,7 +1364,7 @@ int admit(cac_ctx *ctx, KsEngine &eng, const QueryPlan &q) {
             // no scatter for a trial without a matrix (its labels would index past the buffer)
             dd[b] = DenseDesc{g->u, g->v, g->w, sd[b].lab, static_cast<unsigned char *>(roots->p) + off,
                               kdim[b] >= 2 ? m : 0, kdim[b], small};
-            off += ((uint64_t)kdim[b] * kdim[b] * esize + 15) / 16 * 16;
+            off += ((uint64_t)kdim[b] * ld_of(kdim[b]) * esize + 15) / 16 * 16;
         }
         CAC_TRY(upload(ctx, d_dd, dd));
         if (m) {
@@ -1450,7 +1471,7 @@ int mincut_trials(cac_ctx *ctx, const cac_graph *g, uint32_t seed, uint32_t rank
 
 // A dense host matrix for the device: checks the weight bound and, when the total weight is below
 // 2^32 (and so every entry), narrows it to the u32 node storage.
-int host_matrix(uint32_t n, const uint64_t *mat_host, uint32_t *small, std::vector<uint32_t> &narrow) {
+int host_matrix(uint32_t n, const uint64_t *mat_host, uint32_t *small, std::vector<unsigned char> &dev) {
     uint64_t total = 0, top = 0;
     for (uint64_t i = 0; i < (uint64_t)n * n; i++) {
         total += mat_host[i];
@@ -1461,7 +1482,15 @@ int host_matrix(uint32_t n, const uint64_t *mat_host, uint32_t *small, std::vect
         return CAC_ERR_UNSUPPORTED;
     }
     *small = (total / 2 < (1ull << 32) && top < (1ull << 32)) ? 1u : 0u;
-    if (*small) narrow.assign(mat_host, mat_host + (uint64_t)n * n);
+    // the device layout: rows padded to ld_of(n) entries of 4 or 8 bytes
+    const uint64_t ld = ld_of(n), es = *small ? 4 : 8;
+    dev.assign(n * ld * es, 0);
+    for (uint64_t i = 0; i < n; i++)
+        for (uint64_t j = 0; j < n; j++) {
+            const uint64_t x = mat_host[i * n + j];
+            if (*small) reinterpret_cast<uint32_t *>(dev.data())[i * ld + j] = (uint32_t)x;
+            else reinterpret_cast<uint64_t *>(dev.data())[i * ld + j] = x;
+        }
     return CAC_OK;
 }
 
@@ -1471,9 +1500,9 @@ int ks_dense_one(cac_ctx *ctx, uint32_t n, const uint64_t *mat_host, uint32_t se
         set_error("dense Karger-Stein supports at most 16384 vertices");
         return CAC_ERR_UNSUPPORTED;
     }
-    std::vector<uint32_t> narrow;
+    std::vector<unsigned char> dev;
     uint32_t small = 0;
-    CAC_TRY(host_matrix(n, mat_host, &small, narrow));
+    CAC_TRY(host_matrix(n, mat_host, &small, dev));
     cudaStream_t s = ctx->stream;
     DevBuf d_cut(ctx);
     CAC_TRY(d_cut.ensure(8));
@@ -1481,10 +1510,9 @@ int ks_dense_one(cac_ctx *ctx, uint32_t n, const uint64_t *mat_host, uint32_t se
         KsEngine eng(ctx);
         CAC_TRY(eng.init_err());
         MatBuf *root = nullptr;
-        const size_t bytes = (size_t)n * n * (small ? 4 : 8);
-        CAC_TRY(eng.alloc(bytes, &root));
-        CAC_CUDA_TRY(cudaMemcpyAsync(root->p, small ? (const void *)narrow.data() : (const void *)mat_host, bytes,
-                                     cudaMemcpyHostToDevice, s));
+        CAC_TRY(eng.alloc(dev.size(), &root));
+        CAC_CUDA_TRY(cudaMemcpyAsync(root->p, dev.data(), dev.size(), cudaMemcpyHostToDevice, s));
+        CAC_CUDA_TRY(cudaStreamSynchronize(s));  // `dev` is pageable and goes out of scope
         fill_u64<<<1, 32, 0, s>>>(d_cut.as<uint64_t>(), 1, kU64Max);
         eng.add(KNode{d_cut.as<uint64_t>(), seed + rank, trial, 1, n, 1, small, 0, root->p, root});
         while (!eng.idle()) CAC_TRY(eng.step());
@@ -1501,16 +1529,14 @@ int ks_dense_one(cac_ctx *ctx, uint32_t n, const uint64_t *mat_host, uint32_t se
 }
 
 int exact_small(cac_ctx *ctx, uint32_t n, const uint64_t *mat_host, uint64_t *cut) {
-    std::vector<uint32_t> narrow;
+    std::vector<unsigned char> dev;
     uint32_t small = 0;
-    CAC_TRY(host_matrix(n, mat_host, &small, narrow));
+    CAC_TRY(host_matrix(n, mat_host, &small, dev));
     cudaStream_t s = ctx->stream;
     DevBuf buf(ctx), d_cuts(ctx), d_leaf(ctx);
-    const size_t bytes = (size_t)n * n * (small ? 4 : 8);
-    CAC_TRY(buf.ensure(bytes));
+    CAC_TRY(buf.ensure(dev.size()));
     CAC_TRY(d_cuts.ensure(8));
-    CAC_CUDA_TRY(cudaMemcpyAsync(buf.p, small ? (const void *)narrow.data() : (const void *)mat_host, bytes,
-                                 cudaMemcpyHostToDevice, s));
+    CAC_CUDA_TRY(cudaMemcpyAsync(buf.p, dev.data(), dev.size(), cudaMemcpyHostToDevice, s));
     fill_u64<<<1, 32, 0, s>>>(d_cuts.as<uint64_t>(), 1, kU64Max);
     std::vector<LeafDesc> leaves{LeafDesc{buf.p, d_cuts.as<uint64_t>(), n, small}};
     CAC_TRY(upload(ctx, d_leaf, leaves));
