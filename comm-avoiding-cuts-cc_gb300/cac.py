@@ -111,6 +111,7 @@ EXPORTS = [
     ("cac_mincut", ctypes.c_int, [_vp, _vp, ctypes.c_double, ctypes.c_uint32, ctypes.c_uint32,
                                   ctypes.POINTER(MincutResult)]),
     ("cac_mincut_batch", ctypes.c_int, [_vp, _vp, ctypes.c_uint32, _vp]),
+    ("cac_karger_stein", ctypes.c_int, [_vp, _vp, ctypes.c_double, ctypes.c_uint32, ctypes.POINTER(MincutResult)]),
     ("cac_mincut_trials", ctypes.c_int, [_vp, _vp, ctypes.c_uint32, ctypes.c_uint32, ctypes.c_uint32, _vp]),
     ("cac_ks_dense", ctypes.c_int, [_vp, ctypes.c_uint32, _vp, ctypes.c_uint32, ctypes.c_uint32, ctypes.c_uint32,
                                     _u64p]),
@@ -332,6 +333,13 @@ class Graph:
         res = MincutResult()
         _check(lib().cac_mincut(self.ctx.h, self.h, success_probability, seed, virtual_ranks, ctypes.byref(res)),
                "cac_mincut")
+        return res
+
+    # comincut::minimum_cut (the karger_stein executable)
+    def karger_stein(self, success_probability=0.9, seed=0):
+        res = MincutResult()
+        _check(lib().cac_karger_stein(self.ctx.h, self.h, success_probability, seed, ctypes.byref(res)),
+               "cac_karger_stein")
         return res
 
     def trials(self, seed, virtual_ranks, trials_per_rank):

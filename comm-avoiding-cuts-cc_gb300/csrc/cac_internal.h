@@ -195,6 +195,7 @@ struct MincutQuery {
     const cac_graph *g;
     uint32_t seed, ranks, per_rank;
     uint64_t *d_cuts;  // ranks * per_rank trial cuts (device)
+    uint32_t t = 0;    // contraction size before Karger-Stein (0: square_root's intermediate size)
 };
 // Stage 1 and Stage 2 of one query into a running engine: its trial cuts start at 2^64 - 1 and
 // its root nodes carry engine query id `query`; the query is done when outstanding[query] is 0.
@@ -221,6 +222,10 @@ int sitmo_blocks(cac_ctx *ctx, const uint64_t key[4], const uint64_t ctr0[4], ui
 // ---- trial budget (host math shared with the CLI; restated from the reference) ----
 uint32_t intermediate_size(uint32_t n, uint64_t m);
 uint32_t number_of_trials(uint32_t n, uint64_t m, double p);
+uint32_t ks_number_of_trials(uint32_t n, double p);
+// largest contracted graph the Karger-Stein engine holds as a dense matrix (its contraction
+// union-find lives in shared memory)
+constexpr uint32_t kMaxDenseVertices = 16384;
 int ks_target(int n);
 double min_success_in_one_trial(int n);
 uint32_t approx_copies(double p);

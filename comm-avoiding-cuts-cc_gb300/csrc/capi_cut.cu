@@ -73,6 +73,46 @@ int cac_mincut(cac_ctx *ctx, const cac_graph *g, double p, uint32_t seed, uint32
     return st;
 }
 
+int cac_karger_stein(cac_ctx *ctx, const cac_graph *g, double p, uint32_t seed, cac_mincut_result *res) {
+    if (!ctx || !g || !res || !(p >= 0.0 && p < 1.0)) {
+        set_error("cac_karger_stein: invalid argument (success probability must be in [0, 1))");
+        return CAC_ERR_INVALID;
+    }
+    if (g->n < 2) {
+        set_error("cac_karger_stein: a cut needs at least two vertices");
+        return CAC_ERR_INVALID;
+    }
+    if (g->n > kMaxDenseVertices) {
+        // every trial starts from the dense n x n matrix; cac_mincut pre-contracts larger graphs
+        set_error("cac_karger_stein: plain Karger-Stein works on the dense n x n matrix, at most 16384 vertices");
+        return CAC_ERR_UNSUPPORTED;
+    }
+    CAC_CUDA_TRY(cudaSetDevice(ctx->device));
+    *res = cac_mincut_result{};
+    const uint32_t trials = ks_number_of_trials(g->n, p);
+    res->trials_per_rank = trials;
+    res->total_trials = trials;
+    res->intermediate = g->n;
+    void *d = nullptr;
+    CAC_TRY(dev_alloc(ctx, &d, (uint64_t)trials * 8));
+    std::vector<MincutQuery> q{MincutQuery{g, seed, 1, trials, static_cast<uint64_t *>(d), g->n}};
+    float ms = 0;
+    int st = mincut_run_queries(ctx, q, &ms);
+    if (st == CAC_OK) {
+        std::vector<uint64_t> cuts(trials);
+        cudaError_t e = cudaMemcpy(cuts.data(), d, (uint64_t)trials * 8, cudaMemcpyDeviceToHost);
+        if (e != cudaSuccess) {
+            set_error(cudaGetErrorString(e));
+            st = CAC_ERR_CUDA;
+        } else {
+            res->cut = *std::min_element(cuts.begin(), cuts.end());
+        }
+    }
+    res->device_ms = ms;
+    dev_free(ctx, d, (uint64_t)trials * 8);
+    return st;
+}
+
 int cac_mincut_batch(cac_ctx *ctx, const cac_mincut_query *queries, uint32_t count, cac_mincut_result *results) {
     if (!ctx || (count && (!queries || !results))) {
         set_error("cac_mincut_batch: invalid argument");

@@ -37,7 +37,7 @@
 namespace cac {
 namespace {
 
-constexpr uint32_t kMaxSmemVertices = 16384;  // union-find of a contraction held in shared memory
+constexpr uint32_t kMaxSmemVertices = kMaxDenseVertices;  // union-find of a contraction held in shared memory
 constexpr int kBatch = 1024;                  // draws gathered before the ordered contraction
 constexpr int kNT = 512;                      // threads of the per-trial / per-task CTAs
 constexpr int kQT = 256;                      // threads of the quotient CTAs
@@ -1388,12 +1388,12 @@ int admit(cac_ctx *ctx, KsEngine &eng, const QueryPlan &q) {
     return CAC_OK;
 }
 
-int check_graph(const cac_graph *g) {
+int check_graph(const cac_graph *g, uint32_t t_override) {
     if (g->total_weight >= (1ull << 55)) {
         set_error("total edge weight >= 2^55 is not supported by the Stoer-Wagner leaf kernel");
         return CAC_ERR_UNSUPPORTED;
     }
-    const uint32_t t = intermediate_size(g->n, g->m);
+    const uint32_t t = t_override ? t_override : intermediate_size(g->n, g->m);
     if (t > kMaxSmemVertices) {
         set_error("contracted graphs with more than 16384 vertices are not supported yet");
         return CAC_ERR_UNSUPPORTED;
@@ -1404,8 +1404,9 @@ int check_graph(const cac_graph *g) {
 }  // namespace
 
 int mincut_admit_query(cac_ctx *ctx, KsEngine &eng, const MincutQuery &q, uint32_t query) {
-    CAC_TRY(check_graph(q.g));
-    QueryPlan p{q.g, q.seed, q.ranks, q.per_rank, intermediate_size(q.g->n, q.g->m), (uint64_t)q.ranks * q.per_rank,
+    CAC_TRY(check_graph(q.g, q.t));
+    QueryPlan p{q.g, q.seed, q.ranks, q.per_rank, q.t ? q.t : intermediate_size(q.g->n, q.g->m),
+                (uint64_t)q.ranks * q.per_rank,
                 q.d_cuts, query};
     if (p.trials)
         fill_u64<<<(unsigned)std::max<uint64_t>(1, std::min<uint64_t>((p.trials + 255) / 256, 4096)), 256, 0,
@@ -1416,7 +1417,7 @@ int mincut_admit_query(cac_ctx *ctx, KsEngine &eng, const MincutQuery &q, uint32
 
 int mincut_run_queries(cac_ctx *ctx, std::vector<MincutQuery> &queries, float *device_ms) {
     cudaStream_t s = ctx->stream;
-    for (const MincutQuery &q : queries) CAC_TRY(check_graph(q.g));
+    for (const MincutQuery &q : queries) CAC_TRY(check_graph(q.g, q.t));
     CAC_CUDA_TRY(cudaEventRecord(ctx->ev[0], s));
     KsEngine eng(ctx);
     CAC_TRY(eng.init_err());
@@ -1428,7 +1429,7 @@ int mincut_run_queries(cac_ctx *ctx, std::vector<MincutQuery> &queries, float *d
         p.seed = q.seed;
         p.ranks = q.ranks;
         p.per_rank = q.per_rank;
-        p.t = intermediate_size(q.g->n, q.g->m);
+        p.t = q.t ? q.t : intermediate_size(q.g->n, q.g->m);
         p.trials = (uint64_t)q.ranks * q.per_rank;
         p.cuts = q.d_cuts;
         p.query = (uint32_t)i;

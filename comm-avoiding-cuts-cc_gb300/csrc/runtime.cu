@@ -109,6 +109,20 @@ uint32_t number_of_trials(uint32_t n, uint64_t m, double p) {
     return (uint32_t)std::ceil(((double)n * ((double)n * std::log(c))) / (2.0 * 2.0 * ((double)m * pk)));
 }
 
+uint32_t ks_number_of_trials(uint32_t n, double p) {
+    // comincut::number_of_trials (co_mincut.cpp:44-73): multiply the failure probability of one
+    // trial until it is at most 1 - p
+    if (n <= 128 || p == 0) return 1;
+    const double one = min_success_in_one_trial((int)n);
+    double failure = 1.0;
+    uint32_t trials = 0;
+    while (failure > 1.0 - p) {
+        failure *= 1.0 - one;
+        trials++;
+    }
+    return trials;
+}
+
 uint32_t approx_copies(double p) {
     // ApproximateCut::numberOfTrials (ApproximateCut.cpp:82-87)
     double alpha = std::log(1 - std::exp(-(double)0.75));

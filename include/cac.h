@@ -157,6 +157,14 @@ typedef struct {
     uint32_t virtual_ranks;
 } cac_mincut_query;
 int cac_mincut_batch(cac_ctx *ctx, const cac_mincut_query *queries, uint32_t count, cac_mincut_result *results);
+/* Plain Karger-Stein on the whole graph, as the reference's karger_stein executable runs
+ * comincut::minimum_cut (src/executables/karger_stein.cpp, co_mincut.h:515-521): the Karger-Stein
+ * library's own trial count for n vertices (comincut::number_of_trials, co_mincut.cpp:44-73), each
+ * trial a recursion from the dense matrix of the whole graph (no sqrt(m) pre-contraction); trial i
+ * draws from key (seed, i, 1 + heap index). n <= 16384 (CAC_ERR_UNSUPPORTED above).
+ * res->trials_per_rank = res->total_trials = the trial count; res->intermediate = n. */
+int cac_karger_stein(cac_ctx *ctx, const cac_graph *g, double success_probability, uint32_t seed,
+                     cac_mincut_result *res);
 /* Run trials (r, i) for r < virtual_ranks, i < trials_per_rank and write each trial's cut to
  * cuts_host[r * trials_per_rank + i]. */
 int cac_mincut_trials(cac_ctx *ctx, const cac_graph *g, uint32_t seed, uint32_t virtual_ranks,

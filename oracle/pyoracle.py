@@ -143,6 +143,30 @@ def min_success_in_one_trial(n):
     return float(lib().orc_min_success_in_one_trial(n))
 
 
+def ks_number_of_trials(n, p):
+    """comincut::number_of_trials (src/karger-stein/co_mincut.cpp:44-73): the failure probability of
+    one trial is multiplied in until it is at most 1 - p; one trial at n <= 128 or p == 0."""
+    if n <= 128 or p == 0:
+        return 1
+    one = min_success_in_one_trial(n)
+    failure, trials = 1.0, 0
+    while failure > 1.0 - p:
+        failure *= 1.0 - one
+        trials += 1
+    return trials
+
+
+def karger_stein(n, u, v, w, p, seed):
+    """Plain Karger-Stein on the whole graph (src/executables/karger_stein.cpp:34): trial i recurses
+    from the full n x n matrix with the counter-addressed draws of (seed, rank 0, trial i); the
+    answer is the minimum over ks_number_of_trials(n, p) trials. Returns (cut, trials)."""
+    k, mat = shrink_to_dense(n, u, v, w, n, seed, 0, 0)
+    trials = ks_number_of_trials(n, p)
+    if k < 2:
+        return 0, trials
+    return min(ks_dense(mat, seed, 0, i) for i in range(trials)), trials
+
+
 def ks_target(n):
     return int(lib().orc_ks_target(n))
 

@@ -77,6 +77,10 @@ CUT_SPECS = [
 # (vertices, ranks, seed) of the CLICK graphs pinned against the reference's generator
 CLICK_CASES = [(2, 1, 0), (12, 2, 5), (50, 1, 0), (101, 3, 7), (120, 4, 11), (700, 5, 42), (2000, 1, 3)]
 
+# vertex counts and success probabilities at which comincut::number_of_trials is pinned
+KS_TRIAL_SIZES = [2, 100, 128, 129, 150, 181, 182, 200, 500, 1000, 2830, 4000, 16384, 100000, 1000000]
+KS_TRIAL_PROBABILITIES = [0.0, 0.5, 0.9, 0.95, 0.99]
+
 
 def main():
     if not os.path.isdir(REF_TREE) or not os.path.exists(os.path.join(REF_BIN, "cc_labels")):
@@ -124,6 +128,7 @@ def main():
             csv = run("square_root", 0.95, path, 0).strip().split(",")
             rec["square_root_cut"] = int(csv[-1])
             rec["square_root_trials"] = int(csv[7])
+            rec["karger_stein_cut"] = int(run("karger_stein", path, 0).strip().split(",")[-1])
             out_cut.append(rec)
     # 4. CLICK graphs (the reference's CLICK::generateSlice on every rank, via oracle/refbuild's
     # click_edges harness) and their exact minimum cuts
@@ -141,6 +146,15 @@ def main():
                 graphgen.write_graph(path, n, u, v, w, "click")
                 rec["exact_cut"] = int(run("exact_cut", path).strip())
             out_click.append(rec)
+    # 5. comincut::number_of_trials, the karger_stein executable's trial count (oracle/refbuild's
+    # ks_trials harness around the reference's own function)
+    ks = []
+    for p in KS_TRIAL_PROBABILITIES:
+        for line in run("ks_trials", p, *KS_TRIAL_SIZES).splitlines():
+            n, _, t = line.split()
+            ks.append({"n": int(n), "p": p, "trials": int(t)})
+    with open(os.path.join(HERE, "ks_trials.json"), "w") as f:
+        json.dump(ks, f, indent=0)
     with open(os.path.join(HERE, "click.json"), "w") as f:
         json.dump(out_click, f, indent=1)
     with open(os.path.join(HERE, "cc_seeded.json"), "w") as f:

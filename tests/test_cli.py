@@ -1,5 +1,6 @@
 """The drop-in command lines keep the reference's argument rules and CSV lines
-(src/executables/square_root.cpp:7-40, parallel_cc.cpp:8-60, approx_cut.cpp:7-38)."""
+(src/executables/square_root.cpp:7-40, parallel_cc.cpp:8-60, approx_cut.cpp:7-38,
+karger_stein.cpp:9-47, seq_square_root.cpp:5-34)."""
 import os
 import subprocess
 
@@ -8,7 +9,7 @@ import pytest
 
 import graphgen
 import pyoracle as O
-from conftest import PKG
+from conftest import PKG, make_graph
 
 BIN = os.path.join(PKG, "bin")
 
@@ -22,7 +23,7 @@ def _run(name, *args, env=None):
 
 @pytest.fixture(scope="module", autouse=True)
 def _built(libcac):
-    for name in ("square_root", "parallel_cc", "approx_cut"):
+    for name in ("square_root", "parallel_cc", "approx_cut", "karger_stein", "seq_square_root"):
         assert os.path.exists(os.path.join(BIN, name)), "command lines not built"
 
 
@@ -30,6 +31,8 @@ def _built(libcac):
     ("square_root", ["0.95"], "Usage: square_root PROBABILITY INPUT_FILE|CLICK [SIZE] SEED"),
     ("parallel_cc", ["x"], "Usage: connected_components INPUT_FILE SEED [ITERATONS]"),
     ("approx_cut", ["0.9", "x"], "Usage: slimGraph-Light PROBABILITY INPUT_FILE|CLICK [SIZE] SEED"),
+    ("karger_stein", ["x"], "Usage: karger_stein INPUT_FILE SEED"),
+    ("seq_square_root", ["0.9", "x"], "Usage: square_root PROBABILITY INPUT_FILE SEED"),
 ])
 def test_usage_on_wrong_argument_count(name, args, usage):
     r = _run(name, *args)
@@ -108,3 +111,35 @@ def test_click_square_root_and_approx_cut(golden, ranks):
     assert out.returncode == 0, out.stderr
     f = out.stdout.strip().split(",")
     assert f[0] == "CLICK" and f[3] == "101" and f[4] == "5050" and int(f[-1]) >= 1
+
+
+@pytest.mark.gpu
+def test_karger_stein_csv(golden, tmp_path):
+    # input,seed,1,n,m,time,?,co-karger-stein,cut; the cut equals the reference executable's
+    for name, r in golden("ref_test_inputs.json").items():
+        if name.startswith("cc_"):
+            continue
+        path = _write(tmp_path, name, r["n"], r["u"], r["v"], r["w"])
+        out = _run("karger_stein", path, "0")
+        assert out.returncode == 0, out.stderr
+        f = out.stdout.strip().split(",")
+        assert len(f) == 9 and f[0] == path and f[1:3] == ["0", "1"] and f[6:8] == ["?", "co-karger-stein"]
+        assert int(f[3]) == r["n"] and int(f[4]) == len(r["u"]) and float(f[5]) >= 0
+        assert int(f[8]) == r["karger_stein_cut"]
+
+
+@pytest.mark.gpu
+def test_seq_square_root_csv(golden, tmp_path):
+    # input,seed,1,n,m,cuttingTime,mpiTime,trials,low,weight: the one-process square_root
+    spec = golden("mincut_seeded.json")[1]
+    n, u, v, w = make_graph(spec)
+    path = _write(tmp_path, spec["name"], n, u, v, w)
+    out = _run("seq_square_root", "0.95", path, "3")
+    assert out.returncode == 0, out.stderr
+    f = out.stdout.strip().split(",")
+    assert len(f) == 10 and f[0] == path and f[1:3] == ["3", "1"] and f[6] == "0.000000" and f[8] == "low"
+    assert int(f[3]) == n and int(f[4]) == len(u)
+    assert int(f[7]) == spec["square_root_trials"] and int(f[9]) == spec["exact_cut"]
+    # the same trials and answer as square_root on one virtual rank
+    one = _run("square_root", "0.95", path, "3", env={"CAC_VIRTUAL_RANKS": "1"}).stdout.strip().split(",")
+    assert one[7] == f[7] and one[9] == f[9]

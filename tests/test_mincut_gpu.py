@@ -173,3 +173,54 @@ def test_click_graph_on_device(golden, libcac, ctx):
         gu, gv, gw = g.edges()
         assert np.array_equal(gu, u) and np.array_equal(gv, v) and np.array_equal(gw, w)
         assert g.square_root(0.95, seed=case["seed"]).cut == case["exact_cut"]
+
+
+# Plain Karger-Stein on the whole graph (the reference's karger_stein executable,
+# src/executables/karger_stein.cpp:34, comincut::minimum_cut with its own trial count): every
+# answer equals the oracle's replay of the same trials from the full n x n matrix.
+def _ks_cases(golden):
+    for name, r in golden("ref_test_inputs.json").items():
+        if not name.startswith("cc_"):
+            yield name, (r["n"], np.asarray(r["u"], np.uint32), np.asarray(r["v"], np.uint32),
+                         np.asarray(r["w"], np.uint32)), r["karger_stein_cut"]
+    for spec in golden("mincut_seeded.json"):
+        if spec["n"] <= 500:
+            yield spec["name"], make_graph(spec), spec["karger_stein_cut"]
+    yield "ws_700", graphgen.watts_strogatz(700, 8, 0.3, 21, wmax=100), None
+    # total weight above 2^32: 64-bit node matrices
+    yield "er_300_big", graphgen.erdos_renyi(300, 0.2, 22, wmin=1 << 24, wmax=1 << 26), None
+
+
+def test_karger_stein_matches_replay_and_reference(golden, ctx):
+    for name, (n, u, v, w), ref_cut in _ks_cases(golden):
+        g = ctx.graph(n, u, v, w)
+        for seed in (0, 9):
+            r = g.karger_stein(0.9, seed)
+            cut, trials = O.karger_stein(n, u, v, w, 0.9, seed)
+            assert (int(r.cut), r.trials_per_rank, r.total_trials, r.intermediate) == (cut, trials, trials, n), name
+            if seed == 0 and ref_cut is not None:
+                assert cut == ref_cut
+
+
+def test_karger_stein_probabilities_and_edges(ctx, libcac):
+    n, u, v, w = graphgen.erdos_renyi(260, 0.1, 23)
+    g = ctx.graph(n, u, v, w)
+    for p in (0.0, 0.5, 0.99):
+        r = g.karger_stein(p, 4)
+        assert (int(r.cut), r.trials_per_rank) == O.karger_stein(n, u, v, w, p, 4)
+    # two vertices, a disconnected graph
+    assert ctx.graph(2, [0], [1], [9]).karger_stein(0.9, 0).cut == 9
+    keep = (u < 130) == (v < 130)
+    assert ctx.graph(n, u[keep], v[keep], w[keep]).karger_stein(0.9, 1).cut == 0
+    for bad in (1.0, -0.1):
+        with pytest.raises(libcac.CacError):
+            g.karger_stein(bad, 0)
+    with pytest.raises(libcac.CacError):
+        ctx.graph(1, np.zeros(0, np.uint32), np.zeros(0, np.uint32)).karger_stein(0.9, 0)
+
+
+def test_karger_stein_rejects_graphs_above_the_dense_limit(ctx, libcac):
+    n, u, v, w = _ring_plus_er(20000, 2, 24)
+    with pytest.raises(libcac.CacError) as e:
+        ctx.graph(n, u, v, w).karger_stein(0.9, 0)
+    assert e.value.status == -6

@@ -126,3 +126,22 @@ def test_approx_oracle_is_a_power_of_two_bound(golden):
         cut, level = O.approx_cut(r["n"], r["u"], r["v"], r["w"], 0.9, 0)
         assert cut == 1 << level
         assert cut <= 2 * r["exact_cut"]
+
+
+def test_ks_trial_count_matches_reference(golden):
+    # comincut::number_of_trials (co_mincut.cpp:44-73), printed by the reference's own function
+    for r in golden("ks_trials.json"):
+        assert O.ks_number_of_trials(r["n"], r["p"]) == r["trials"], r
+
+
+def test_karger_stein_oracle_matches_reference(golden):
+    # the karger_stein executable's answers (src/executables/karger_stein.cpp, seed 0, p = 0.90)
+    for name, r in golden("ref_test_inputs.json").items():
+        if not name.startswith("cc_"):
+            assert O.karger_stein(r["n"], r["u"], r["v"], r["w"], 0.9, 0)[0] == r["karger_stein_cut"], name
+    for spec in golden("mincut_seeded.json"):
+        if spec["n"] <= 500:
+            n, u, v, w = make_graph(spec)
+            cut, trials = O.karger_stein(n, u, v, w, 0.9, 0)
+            assert trials == O.ks_number_of_trials(n, 0.9)
+            assert cut == spec["karger_stein_cut"] == spec["exact_cut"], spec["name"]
