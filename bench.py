@@ -279,12 +279,34 @@ def _cc_measure(ctx, stream, g, n, hu_np, hv_np, steps, warmup, world, flush):
         t = torch.tensor([e2e_total], device="cuda")
         torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
         e2e_total = float(t.item())
+    link = _link_gbs(hu_np, hv_np)
     return {"value": world * m * steps / (total_ms / 1e3), "ms_per_step": total_ms / steps,
             "e2e": {"value": world * m * steps / (e2e_total / 1e3), "unit": "edges/s", "h2d_bytes_per_step": 8 * m,
-                    "d2h_bytes_per_step": 4 * n, "ms_per_step": e2e_total / steps},
+                    "d2h_bytes_per_step": 4 * n, "ms_per_step": e2e_total / steps, "link_gbs": round(link, 1),
+                    "link_floor_ms": round((8 * m + 4 * n) / link / 1e6, 4)},
             "edge_avg_ms": statistics.mean(edge_ms), "components": want_count,
             "phases_ms": dict(zip(("sampling_round", "filter", "hook_survivors", "labels"),
                                   [round(statistics.mean(p[i] for p in phases), 4) for i in range(4)]))}
+
+
+def _link_gbs(hu_np, hv_np, reps=5):
+    """Host-to-device bandwidth of the pinned edge arrays themselves (one copy of each, CUDA events;
+    best of reps): the floor of the e2e query is its bytes over this rate."""
+    import torch
+    hu = torch.from_numpy(hu_np.view(np.int32))
+    hv = torch.from_numpy(hv_np.view(np.int32))
+    du, dv = torch.empty_like(hu, device="cuda"), torch.empty_like(hv, device="cuda")
+    best = 0.0
+    for _ in range(reps):
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        torch.cuda.synchronize()
+        a.record()
+        du.copy_(hu, non_blocking=True)
+        dv.copy_(hv, non_blocking=True)
+        b.record()
+        b.synchronize()
+        best = max(best, (hu.numel() + hv.numel()) * 4 / (a.elapsed_time(b) * 1e6))
+    return best
 
 
 def _pinned_u32(a):

@@ -50,6 +50,16 @@ struct cac_graph;
 
 namespace cac {
 // Identity of a connected-components query whose launch sequence is cached as a CUDA graph.
+struct CCStreamKey {
+    const void *h_u = nullptr, *h_v = nullptr, *h_labels = nullptr, *d_u = nullptr, *d_v = nullptr,
+               *d_labels = nullptr;
+    uint32_t n = 0;
+    uint64_t m = 0;
+    bool zero_copy = false;
+    const void *arena_base = nullptr;
+    size_t arena_cap = 0;
+};
+
 struct CCGraphKey {
     const void *u = nullptr, *v = nullptr, *labels = nullptr;
     uint32_t n = 0;
@@ -73,10 +83,12 @@ struct cac_ctx {
     std::set<cac_graph *> graphs;    // live graphs, released by cac_ctx_destroy
     cudaMemPool_t pool = nullptr;    // stream-ordered pool of the Karger-Stein level buffers (keeps its memory)
     cac::CCGraphKey cc_key;          // last connected-components query
+    cac::CCStreamKey cc_stream_key;  // last host-edge (streamed) connected-components query
+    cudaGraphExec_t cc_stream_exec = nullptr;  // its captured launch sequence
     cudaGraphExec_t cc_exec = nullptr;  // its captured launch sequence (second sighting onwards)
     uint32_t *pinned_u32 = nullptr;  // 64 KB pinned staging: [0,256) B scalar results, then descriptors
     cudaStream_t copy_stream = nullptr;  // host-to-device chunks of cac_cc_edges (created on first use)
-    cudaEvent_t chunk_ev[16] = {};       // one per chunk in flight
+    cudaEvent_t chunk_ev[40] = {};       // start + one per piece and gap copy in flight
 };
 
 struct cac_graph {
@@ -127,10 +139,10 @@ CCPlan cc_plan(uint32_t n, uint64_t m, uint32_t ranks);
 int cc_run(cac_ctx *ctx, uint32_t n, uint64_t m, const uint32_t *d_u, const uint32_t *d_v, uint32_t seed,
            uint32_t ranks, uint32_t *d_labels, cac_cc_result *res);
 size_t cc_scratch_bytes(uint32_t n, uint32_t ranks, uint64_t m);
-// CC of an edge list in host memory: chunks copied to d_u/d_v on a second stream while the ctx
-// stream hooks each chunk that has arrived (cac_cc_edges).
+// CC of an edge list in host memory: parts copied to d_u/d_v on a second stream while the ctx
+// stream hooks or filters each part that has arrived (cac_cc_edges); labels copied to h_labels.
 int cc_run_streamed(cac_ctx *ctx, uint32_t n, uint64_t m, const uint32_t *h_u, const uint32_t *h_v, uint32_t *d_u,
-                    uint32_t *d_v, uint32_t *d_labels, cac_cc_result *res);
+                    uint32_t *d_v, uint32_t *d_labels, uint32_t *h_labels, cac_cc_result *res);
 void cc_graph_reset(cac_ctx *ctx);
 
 // ---- min cut (mincut.cu) ----

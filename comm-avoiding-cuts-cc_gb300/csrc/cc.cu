@@ -40,6 +40,7 @@ constexpr uint32_t kGiantSample = 1024;              // vertices sampled to find
 constexpr uint32_t kSampleChunk = 32;                // consecutive edges behind one sampling draw
 constexpr uint32_t kSampleSubrounds = 8;             // slices of the sampling round, compressed in between
 constexpr uint32_t kMaxRegions = 1024;               // filter CTAs (regions of the survivor buffer)
+constexpr uint32_t kStreamPieces = 8;                // sample pieces (and gaps) of a host edge list
 
 struct RankDesc {
     uint64_t slice_off;
@@ -321,14 +322,35 @@ __global__ void __launch_bounds__(kThreads) cc_hook_survivors(uint32_t *par, con
                                                               const uint32_t *__restrict__ counts, uint32_t nregions,
                                                               uint64_t region_stride) {
     __shared__ uint32_t pre[kMaxRegions + 1];
-    if (threadIdx.x == 0) {
-        uint32_t acc = 0;
-        for (uint32_t r = 0; r < nregions; r++) {
-            pre[r] = acc;
-            acc += counts[r];
-        }
-        pre[nregions] = acc;
+    __shared__ uint32_t wsum[kThreads / 32];
+    static_assert(kMaxRegions == 4 * kThreads, "four region counts per thread");
+    // exclusive prefix of the region counts: four per thread, then a block scan of the sums
+    uint32_t c[4], local = 0;
+#pragma unroll
+    for (int k = 0; k < 4; k++) {
+        const uint32_t r = 4 * threadIdx.x + k;
+        c[k] = r < nregions ? counts[r] : 0;
+        local += c[k];
     }
+    const uint32_t lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    uint32_t incl = local;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        const uint32_t y = __shfl_up_sync(0xffffffffu, incl, o);
+        if (lane >= (uint32_t)o) incl += y;
+    }
+    if (lane == 31) wsum[warp] = incl;
+    __syncthreads();
+    uint32_t before = 0;
+    for (uint32_t w = 0; w < warp; w++) before += wsum[w];
+    uint32_t acc = before + incl - local;
+#pragma unroll
+    for (int k = 0; k < 4; k++) {
+        const uint32_t r = 4 * threadIdx.x + k;
+        if (r <= nregions) pre[r] = acc;
+        acc += c[k];
+    }
+    if (threadIdx.x == kThreads - 1 && nregions == kMaxRegions) pre[kMaxRegions] = acc;
     __syncthreads();
     const uint32_t total = pre[nregions];
     for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < total; i += gridDim.x * blockDim.x) {
@@ -630,6 +652,9 @@ void cc_graph_reset(cac_ctx *ctx) {
     if (ctx->cc_exec) cudaGraphExecDestroy(ctx->cc_exec);
     ctx->cc_exec = nullptr;
     ctx->cc_key = CCGraphKey{};
+    if (ctx->cc_stream_exec) cudaGraphExecDestroy(ctx->cc_stream_exec);
+    ctx->cc_stream_exec = nullptr;
+    ctx->cc_stream_key = CCStreamKey{};
 }
 
 int cc_run(cac_ctx *ctx, uint32_t n, uint64_t m, const uint32_t *d_u, const uint32_t *d_v, uint32_t seed,
@@ -742,78 +767,111 @@ int cc_run(cac_ctx *ctx, uint32_t n, uint64_t m, const uint32_t *d_u, const uint
     return CAC_OK;
 }
 
-// Connected components of an edge list that is still in host memory (cac_cc_edges). The
-// host-to-device link (about 200 GB/s on a GB300 host, measured) is slower than the device's
-// from-scratch hooking of all edges, so the edges cross it in chunks on a second stream while the
-// ctx stream hooks every chunk that has arrived into the union-find: the query ends about one
-// chunk's hook after its last byte arrived, instead of copy time plus compute time. No sampling
-// round is needed (it only serves to skip edges of a device-resident graph); the labels -- rank
-// of each component's smallest vertex -- are the same as cc_run's for any edge order.
-int cc_run_streamed(cac_ctx *ctx, uint32_t n, uint64_t m, const uint32_t *h_u, const uint32_t *h_v, uint32_t *d_u,
-                    uint32_t *d_v, uint32_t *d_labels, cac_cc_result *res) {
-    cudaStream_t s = ctx->stream;
-    if (res) *res = cac_cc_result{};
-    if (n == 0) return CAC_OK;
-    if (!ctx->copy_stream) {
-        CAC_CUDA_TRY(cudaStreamCreateWithFlags(&ctx->copy_stream, cudaStreamNonBlocking));
-        for (auto &e : ctx->chunk_ev) CAC_CUDA_TRY(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+// Device address of a pinned (page-locked, mapped) host array, or null for pageable memory.
+static const uint32_t *pinned_device_view(const uint32_t *h) {
+    cudaPointerAttributes a{};
+    if (cudaPointerGetAttributes(&a, h) != cudaSuccess) {
+        cudaGetLastError();
+        return nullptr;
     }
-    const uint32_t ntiles = (uint32_t)(((uint64_t)n + kTile - 1) / kTile);
-    const uint32_t nwords = (uint32_t)(((uint64_t)n + 31) / 32);
-    // Chunks of at least 4 Mi edges (32 MB of u and v: smaller copies lose link bandwidth to
-    // per-copy overhead), at most 16, each a multiple of 1024 edges (16-byte aligned starts).
-    const uint64_t per = m ? (std::max<uint64_t>(4ull << 20, (m + 15) / 16) + 1023) / 1024 * 1024 : 0;
-    const uint32_t nchunks = per ? (uint32_t)((m + per - 1) / per) : 0;
-    const bool vec = ((reinterpret_cast<uintptr_t>(d_u) | reinterpret_cast<uintptr_t>(d_v)) & 15) == 0;
-    // The first `whole` chunks are hooked edge by edge: they play the sampling round's part and
-    // cover at least the reference's sample budget (edgesToSamplePerProcessor: n^1.045 * 1.2).
-    // The giant component they reveal is fixed as a bitmap, and every later chunk is streamed
-    // through the filter, which hooks only the edges that leave the giant component.
-    const uint64_t budget = (uint64_t)(std::pow((float)n, 1.0f + 0.09f / 2) * (1.0f + 0.2f));
-    const uint32_t whole = per ? (uint32_t)std::max<uint64_t>(1, (budget + per - 1) / per) : 0;
-    const bool filtered = vec && nchunks > whole;
-    CAC_TRY(arena_reserve(ctx, align_up((size_t)n * 4) + 2 * align_up((size_t)ntiles * 4 + 4) + align_up(256) +
-                                   (filtered ? align_up((size_t)nwords * 4 + 4) + align_up(kMaxRegions * 4) +
-                                                   align_up((per + 4 * (uint64_t)kMaxRegions) * 8)
-                                             : 0)));
-    arena_reset(ctx);
-    uint32_t *par = (uint32_t *)arena_take(ctx, (size_t)n * 4);
-    uint32_t *counts = (uint32_t *)arena_take(ctx, (size_t)ntiles * 4 + 4);
-    uint32_t *offsets = (uint32_t *)arena_take(ctx, (size_t)ntiles * 4 + 4);
-    uint32_t *total = (uint32_t *)arena_take(ctx, 256);
-    uint32_t *giant = total + 8;
+    return a.type == cudaMemoryTypeHost ? static_cast<const uint32_t *>(a.devicePointer) : nullptr;
+}
+
+// Connected components of an edge list that is still in host memory (cac_cc_edges). The
+// host-to-device link (about 209 GB/s on a GB300 host, measured for copy-engine copies and for
+// kernels reading pinned host memory alike) is the bound: BA n=1,024,000 needs 0.63 ms to cross it
+// and 0.23 ms to solve once resident. So the edges cross in an order that lets the ctx stream do
+// its work behind the copy:
+//   1. kStreamPieces evenly spaced pieces, together as large as the reference's sample budget
+//      (edgesToSamplePerProcessor: n^1.045 * 1.2 edges), land first: pulled by one kernel from
+//      pinned host arrays while the copy engine starts on the gaps, else as one strided copy per
+//      array. They are hooked piece by piece, one edge per thread, with a full compression after
+//      each: this is the sampling round (the pieces are spread over the whole list, so an edge list
+//      sorted by vertex still yields a sample of the whole graph).
+//   2. The giant component of the sample is fixed as a bitmap.
+//   3. The gaps between the pieces cross on the copy stream, each streamed through the filter as
+//      it lands: edges with both ends in the giant component are dropped, the others hooked.
+// What is left after the last byte arrives is one gap's filter and the labelling. Labels -- rank
+// of each component's smallest vertex -- are the same as cc_run's for any edge order and sample.
+// h_labels (optional) receives the labels before the call returns. A repeated call with the same
+// buffers replays the whole sequence as one captured CUDA graph.
+namespace {
+
+// Everything one streamed query enqueues, resolved on the host.
+struct StreamLaunch {
+    uint32_t n = 0;
+    uint64_t m = 0;
+    const uint32_t *h_u = nullptr, *h_v = nullptr;  // host edge arrays (copy-engine source)
+    const uint32_t *z_u = nullptr, *z_v = nullptr;  // their device views when pinned and aligned, else null
+    uint32_t *d_u = nullptr, *d_v = nullptr, *d_labels = nullptr, *h_labels = nullptr;
+    uint32_t *par = nullptr, *counts = nullptr, *offsets = nullptr, *total = nullptr, *giant = nullptr;
     uint32_t *bits = nullptr, *region_counts = nullptr;
     uint2 *surv = nullptr;
-    if (filtered) {
-        bits = (uint32_t *)arena_take(ctx, (size_t)nwords * 4 + 4);
-        region_counts = (uint32_t *)arena_take(ctx, kMaxRegions * 4);
-        surv = (uint2 *)arena_take(ctx, (per + 4 * (uint64_t)kMaxRegions) * 8);
-        CAC_TRY(smem_optin(ctx, cc_filter<true>));
-        CAC_TRY(smem_optin(ctx, cc_filter<false>));
+    uint32_t ntiles = 0, nwords = 0;
+    bool vec = false, filtered = false;
+    std::vector<std::pair<uint64_t, uint64_t>> parts;  // (first edge, count): pieces, then gaps
+};
+
+// Copies the sample pieces of a pinned host edge list into the device arrays: kernel loads of
+// pinned host memory cross the link at the copy engine's rate, and one launch moves all pieces
+// (the copy engine would take one copy per piece and array). Piece i is the 16-byte words
+// [i * seg4, i * seg4 + piece4) of each array.
+__global__ void cc_pull_pieces(const uint4 *__restrict__ hu, const uint4 *__restrict__ hv, uint4 *__restrict__ du,
+                               uint4 *__restrict__ dv, uint64_t seg4, uint64_t piece4, uint32_t pieces) {
+    const uint64_t total = piece4 * pieces;
+    for (uint64_t k = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; k < total; k += (uint64_t)gridDim.x * blockDim.x) {
+        const uint64_t i = k / piece4, x = i * seg4 + (k - i * piece4);
+        const uint4 a = hu[x], b = hv[x];
+        du[x] = a;
+        dv[x] = b;
     }
-    CAC_CUDA_TRY(cudaEventRecord(ctx->ev[0], s));
-    cc_init<<<grid_for(ctx, n, 8), kThreads, 0, s>>>(par, n);
+}
+
+int stream_enqueue(cac_ctx *ctx, const StreamLaunch &L, bool capturing) {
+    cudaStream_t s = ctx->stream;
+    const uint32_t n = L.n;
+    CAC_TRY(record(ctx, 0, capturing));
+    cc_init<<<grid_for(ctx, n, 8), kThreads, 0, s>>>(L.par, n);
     // the copies start after everything already queued on the ctx stream (the staging buffers
     // may still be read by the previous query)
-    CAC_CUDA_TRY(cudaEventRecord(ctx->chunk_ev[0], s));
-    CAC_CUDA_TRY(cudaStreamWaitEvent(ctx->copy_stream, ctx->chunk_ev[0], 0));
-    for (uint32_t c = 0; c < nchunks && per; c++) {
-        const uint64_t e0 = std::min<uint64_t>(m, c * per), e1 = std::min<uint64_t>(m, e0 + per);
-        if (e0 >= e1) break;
-        CAC_CUDA_TRY(cudaMemcpyAsync(d_u + e0, h_u + e0, (e1 - e0) * 4, cudaMemcpyHostToDevice, ctx->copy_stream));
-        CAC_CUDA_TRY(cudaMemcpyAsync(d_v + e0, h_v + e0, (e1 - e0) * 4, cudaMemcpyHostToDevice, ctx->copy_stream));
-        CAC_CUDA_TRY(cudaEventRecord(ctx->chunk_ev[c], ctx->copy_stream));
-        CAC_CUDA_TRY(cudaStreamWaitEvent(s, ctx->chunk_ev[c], 0));
-        const uint64_t len = e1 - e0;
-        if (!filtered || c < whole) {
-            const int grid = grid_for(ctx, (len + 3) / 4, 8);
-            if (vec) cc_edge_pass<true><<<grid, kThreads, 0, s>>>(par, d_u + e0, d_v + e0, len);
-            else cc_edge_pass<false><<<grid, kThreads, 0, s>>>(par, d_u + e0, d_v + e0, len);
-            // flat trees keep the next chunk's union walks one or two hops long (hidden behind the copy)
-            if (c + 1 < nchunks) compress_all(ctx, par, n, s);
-            if (filtered && c + 1 == whole) {
-                cc_find_giant<<<1, kGiantSample, 0, s>>>(par, n, giant);
-                cc_giant_bitmap<<<grid_for(ctx, n, 8), kThreads, 0, s>>>(par, n, giant, bits);
+    cudaEvent_t *ev = ctx->chunk_ev;
+    CAC_CUDA_TRY(cudaEventRecord(ev[0], s));
+    CAC_CUDA_TRY(cudaStreamWaitEvent(ctx->copy_stream, ev[0], 0));
+    // The pieces land first: pulled by a kernel on the ctx stream from pinned host arrays (the
+    // copy engine meanwhile starts on the gaps), else as one strided copy per array ahead of the
+    // gaps on the copy stream.
+    const uint64_t seg = L.filtered ? L.parts[1].first : 0, piece = L.filtered ? L.parts[0].second : 0;
+    if (L.filtered && L.z_u) {
+        cc_pull_pieces<<<grid_for(ctx, piece / 4 * kStreamPieces, 8), kThreads, 0, s>>>(
+            reinterpret_cast<const uint4 *>(L.z_u), reinterpret_cast<const uint4 *>(L.z_v),
+            reinterpret_cast<uint4 *>(L.d_u), reinterpret_cast<uint4 *>(L.d_v), seg / 4, piece / 4, kStreamPieces);
+    } else if (L.filtered) {
+        CAC_CUDA_TRY(cudaMemcpy2DAsync(L.d_u, seg * 4, L.h_u, seg * 4, piece * 4, kStreamPieces,
+                                       cudaMemcpyHostToDevice, ctx->copy_stream));
+        CAC_CUDA_TRY(cudaMemcpy2DAsync(L.d_v, seg * 4, L.h_v, seg * 4, piece * 4, kStreamPieces,
+                                       cudaMemcpyHostToDevice, ctx->copy_stream));
+        CAC_CUDA_TRY(cudaEventRecord(ev[1], ctx->copy_stream));
+    }
+    for (size_t c = L.filtered ? kStreamPieces : 0; c < L.parts.size(); c++) {
+        const uint64_t e0 = L.parts[c].first, len = L.parts[c].second;
+        CAC_CUDA_TRY(cudaMemcpyAsync(L.d_u + e0, L.h_u + e0, len * 4, cudaMemcpyHostToDevice, ctx->copy_stream));
+        CAC_CUDA_TRY(cudaMemcpyAsync(L.d_v + e0, L.h_v + e0, len * 4, cudaMemcpyHostToDevice, ctx->copy_stream));
+        CAC_CUDA_TRY(cudaEventRecord(ev[1 + c], ctx->copy_stream));
+    }
+    for (size_t c = 0; c < L.parts.size(); c++) {
+        const uint64_t e0 = L.parts[c].first, len = L.parts[c].second;
+        // a part copied by the copy engine is waited for (the strided piece copy: before piece 0)
+        if (!L.filtered || c >= kStreamPieces || (c == 0 && !L.z_u)) CAC_CUDA_TRY(cudaStreamWaitEvent(s, ev[1 + c], 0));
+        if (!L.filtered || c < kStreamPieces) {
+            // a piece of the sample (or, unfiltered, a chunk): every edge hooks, one edge per
+            // thread (union walks are latency chains, so more of them run at once), then the
+            // trees are flattened so the next part's walks stay one or two hops long
+            cc_edge_pass<false><<<grid_for(ctx, len, 8), kThreads, 0, s>>>(L.par, L.d_u + e0, L.d_v + e0, len);
+            if (c + 1 < L.parts.size()) compress_all(ctx, L.par, n, s);
+            if (L.filtered && c + 1 == kStreamPieces) {
+                cc_find_giant<<<1, kGiantSample, 0, s>>>(L.par, n, L.giant);
+                cc_giant_bitmap<<<grid_for(ctx, n, 8), kThreads, 0, s>>>(L.par, n, L.giant, L.bits);
+                CAC_TRY(record(ctx, 1, capturing));
             }
         } else {
             const uint64_t tiles = len >> 8;  // 256-edge tiles; the rest goes to the scalar pass
@@ -821,35 +879,143 @@ int cc_run_streamed(cac_ctx *ctx, uint32_t n, uint64_t m, const uint32_t *h_u, c
                 1, std::min<uint64_t>({(uint64_t)ctx->num_sms, (uint64_t)kMaxRegions, tiles}));
             const uint64_t tper = (tiles + regions - 1) / regions;
             if (tiles) {
-                const size_t sm = (size_t)std::min(nwords, kSmemBitmapWords) * 4;
-                auto filt = nwords <= kSmemBitmapWords ? cc_filter<true> : cc_filter<false>;
-                filt<<<regions, kEdgeThreads, sm, s>>>(d_u + e0, d_v + e0, tiles, bits, nwords, surv, region_counts);
-                cc_hook_survivors<<<(unsigned)ctx->num_sms * 4, kThreads, 0, s>>>(par, surv, region_counts, regions,
-                                                                                   tper * 256);
+                const size_t sm = (size_t)std::min(L.nwords, kSmemBitmapWords) * 4;
+                auto filt = L.nwords <= kSmemBitmapWords ? cc_filter<true> : cc_filter<false>;
+                filt<<<regions, kEdgeThreads, sm, s>>>(L.d_u + e0, L.d_v + e0, tiles, L.bits, L.nwords, L.surv,
+                                                       L.region_counts);
+                cc_hook_survivors<<<(unsigned)ctx->num_sms * 4, kThreads, 0, s>>>(L.par, L.surv, L.region_counts,
+                                                                                   regions, tper * 256);
             }
             const uint64_t done = tiles * 256;
             if (done < len)
-                cc_edge_pass<false><<<grid_for(ctx, len - done, 8), kThreads, 0, s>>>(par, d_u + e0 + done,
-                                                                                     d_v + e0 + done, len - done);
+                cc_edge_pass<false><<<grid_for(ctx, len - done, 8), kThreads, 0, s>>>(L.par, L.d_u + e0 + done,
+                                                                                     L.d_v + e0 + done, len - done);
         }
     }
-    CAC_CUDA_TRY(cudaEventRecord(ctx->ev[2], s));
-    cc_finalize_count<<<ntiles, kThreads, 0, s>>>(par, n, counts);
-    cc_scan_tiles<<<1, 1024, 0, s>>>(counts, offsets, ntiles, total);
-    if (d_labels) {
-        cc_rank_roots<<<ntiles, kThreads, 0, s>>>(par, n, offsets, d_labels);
-        cc_label_all<<<grid_for(ctx, n, 8), kThreads, 0, s>>>(par, n, d_labels);
+    if (!L.filtered) CAC_TRY(record(ctx, 1, capturing));
+    CAC_TRY(record(ctx, 2, capturing));
+    cc_finalize_count<<<L.ntiles, kThreads, 0, s>>>(L.par, n, L.counts);
+    cc_scan_tiles<<<1, 1024, 0, s>>>(L.counts, L.offsets, L.ntiles, L.total);
+    if (L.d_labels) {
+        cc_rank_roots<<<L.ntiles, kThreads, 0, s>>>(L.par, n, L.offsets, L.d_labels);
+        cc_label_all<<<grid_for(ctx, n, 8), kThreads, 0, s>>>(L.par, n, L.d_labels);
     }
     CAC_CUDA_TRY(cudaGetLastError());
-    CAC_CUDA_TRY(cudaMemcpyAsync(ctx->pinned_u32, total, 4, cudaMemcpyDeviceToHost, s));
-    CAC_CUDA_TRY(cudaEventRecord(ctx->ev[3], s));
+    CAC_CUDA_TRY(cudaMemcpyAsync(ctx->pinned_u32, L.total, 4, cudaMemcpyDeviceToHost, s));
+    CAC_TRY(record(ctx, 3, capturing));
+    if (L.d_labels && L.h_labels)
+        CAC_CUDA_TRY(cudaMemcpyAsync(L.h_labels, L.d_labels, (size_t)n * 4, cudaMemcpyDeviceToHost, s));
+    return CAC_OK;
+}
+
+bool same_stream_key(const CCStreamKey &a, const CCStreamKey &b) {
+    return a.h_u == b.h_u && a.h_v == b.h_v && a.h_labels == b.h_labels && a.d_u == b.d_u && a.d_v == b.d_v &&
+           a.d_labels == b.d_labels && a.n == b.n && a.m == b.m && a.zero_copy == b.zero_copy &&
+           a.arena_base == b.arena_base && a.arena_cap == b.arena_cap;
+}
+
+}  // namespace
+
+int cc_run_streamed(cac_ctx *ctx, uint32_t n, uint64_t m, const uint32_t *h_u, const uint32_t *h_v, uint32_t *d_u,
+                    uint32_t *d_v, uint32_t *d_labels, uint32_t *h_labels, cac_cc_result *res) {
+    cudaStream_t s = ctx->stream;
+    if (res) *res = cac_cc_result{};
+    if (n == 0) return CAC_OK;
+    if (!ctx->copy_stream) {
+        CAC_CUDA_TRY(cudaStreamCreateWithFlags(&ctx->copy_stream, cudaStreamNonBlocking));
+        for (auto &e : ctx->chunk_ev) CAC_CUDA_TRY(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+    }
+    StreamLaunch L;
+    L.n = n;
+    L.m = m;
+    L.h_u = h_u;
+    L.h_v = h_v;
+    L.d_u = d_u;
+    L.d_v = d_v;
+    L.d_labels = d_labels;
+    L.h_labels = h_labels;
+    L.ntiles = (uint32_t)(((uint64_t)n + kTile - 1) / kTile);
+    L.nwords = (uint32_t)(((uint64_t)n + 31) / 32);
+    L.vec = ((reinterpret_cast<uintptr_t>(d_u) | reinterpret_cast<uintptr_t>(d_v)) & 15) == 0;
+    // Segment i of the list is [i * seg, (i + 1) * seg), the last one running to m; its piece is
+    // the first `piece` edges, its gap the rest. seg and piece are multiples of 256 edges, so
+    // every piece and gap starts 1 KB aligned and all but the last gap are whole filter tiles.
+    const uint64_t budget = std::min<uint64_t>(m, (uint64_t)(std::pow((float)n, 1.0f + 0.09f / 2) * (1.0f + 0.2f)));
+    const uint64_t seg = (m / kStreamPieces) & ~255ull;
+    const uint64_t piece = seg ? std::min<uint64_t>(seg, ((budget + kStreamPieces - 1) / kStreamPieces + 255) & ~255ull)
+                               : 0;
+    L.filtered = L.vec && seg > 0;
+    const uint64_t max_gap = L.filtered ? m - (kStreamPieces - 1) * seg - piece : 0;
+    CAC_TRY(arena_reserve(ctx, align_up((size_t)n * 4) + 2 * align_up((size_t)L.ntiles * 4 + 4) + align_up(256) +
+                                   (L.filtered ? align_up((size_t)L.nwords * 4 + 4) + align_up(kMaxRegions * 4) +
+                                                     align_up((max_gap + 4 * (uint64_t)kMaxRegions) * 8)
+                                               : 0)));
+    arena_reset(ctx);
+    L.par = (uint32_t *)arena_take(ctx, (size_t)n * 4);
+    L.counts = (uint32_t *)arena_take(ctx, (size_t)L.ntiles * 4 + 4);
+    L.offsets = (uint32_t *)arena_take(ctx, (size_t)L.ntiles * 4 + 4);
+    L.total = (uint32_t *)arena_take(ctx, 256);
+    L.giant = L.total + 8;
+    if (L.filtered) {
+        L.bits = (uint32_t *)arena_take(ctx, (size_t)L.nwords * 4 + 4);
+        L.region_counts = (uint32_t *)arena_take(ctx, kMaxRegions * 4);
+        L.surv = (uint2 *)arena_take(ctx, (max_gap + 4 * (uint64_t)kMaxRegions) * 8);
+        CAC_TRY(smem_optin(ctx, cc_filter<true>));
+        CAC_TRY(smem_optin(ctx, cc_filter<false>));
+        // pinned, 16-byte aligned host arrays: the pieces are pulled by a kernel
+        L.z_u = pinned_device_view(h_u);
+        L.z_v = pinned_device_view(h_v);
+        if (!L.z_u || !L.z_v || ((reinterpret_cast<uintptr_t>(L.z_u) | reinterpret_cast<uintptr_t>(L.z_v)) & 15))
+            L.z_u = L.z_v = nullptr;
+        for (uint32_t i = 0; i < kStreamPieces; i++) L.parts.push_back({i * seg, piece});
+        for (uint32_t i = 0; i < kStreamPieces; i++) {
+            const uint64_t g0 = i * seg + piece, g1 = (i + 1 == kStreamPieces) ? m : (i + 1) * seg;
+            if (g1 > g0) L.parts.push_back({g0, g1 - g0});
+        }
+    } else if (m) {
+        // no filter: the whole list in kStreamPieces chunks with 16-byte aligned starts
+        const uint64_t per = ((m + kStreamPieces - 1) / kStreamPieces + 1023) & ~1023ull;
+        for (uint64_t e0 = 0; e0 < m; e0 += per) L.parts.push_back({e0, std::min(per, m - e0)});
+    }
+
+    // A repeated identical call replays a captured CUDA graph, as cc_run does: the first sighting
+    // of a key runs directly, the second captures.
+    CCStreamKey key{h_u, h_v, h_labels, d_u, d_v, d_labels, n, m, L.z_u != nullptr, ctx->arena.base, ctx->arena.cap};
+    if (same_stream_key(key, ctx->cc_stream_key) && ctx->cc_stream_exec) {
+        CAC_CUDA_TRY(cudaGraphLaunch(ctx->cc_stream_exec, s));
+    } else if (same_stream_key(key, ctx->cc_stream_key)) {
+        cudaGraph_t graph = nullptr;
+        CAC_CUDA_TRY(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
+        const int st = stream_enqueue(ctx, L, true);
+        const cudaError_t ce = cudaStreamEndCapture(s, &graph);
+        if (st != CAC_OK) {
+            if (graph) cudaGraphDestroy(graph);
+            return st;
+        }
+        CAC_CUDA_TRY(ce);
+        const cudaError_t ie = cudaGraphInstantiate(&ctx->cc_stream_exec, graph, 0);
+        cudaGraphDestroy(graph);
+        if (ie != cudaSuccess) {
+            ctx->cc_stream_exec = nullptr;
+            cudaGetLastError();
+            CAC_TRY(stream_enqueue(ctx, L, false));
+        } else {
+            CAC_CUDA_TRY(cudaGraphLaunch(ctx->cc_stream_exec, s));
+        }
+    } else {
+        if (ctx->cc_stream_exec) cudaGraphExecDestroy(ctx->cc_stream_exec);
+        ctx->cc_stream_exec = nullptr;
+        ctx->cc_stream_key = key;
+        CAC_TRY(stream_enqueue(ctx, L, false));
+    }
     CAC_CUDA_TRY(cudaStreamSynchronize(s));
     if (res) {
         res->num_components = ctx->pinned_u32[0];
-        res->rounds = m > 0 ? 1u : 0u;
-        res->sampled_edges = 0;
+        res->rounds = (L.filtered ? 1u : 0u) + (m > 0 ? 1u : 0u);  // sample pieces + streamed gaps
+        res->sampled_edges = L.filtered ? kStreamPieces * piece : 0;
         CAC_CUDA_TRY(cudaEventElapsedTime(&res->device_ms, ctx->ev[0], ctx->ev[3]));
-        CAC_CUDA_TRY(cudaEventElapsedTime(&res->edge_pass_ms, ctx->ev[0], ctx->ev[2]));
+        CAC_CUDA_TRY(cudaEventElapsedTime(&res->sample_ms, ctx->ev[0], ctx->ev[1]));
+        CAC_CUDA_TRY(cudaEventElapsedTime(&res->edge_pass_ms, ctx->ev[1], ctx->ev[2]));
         CAC_CUDA_TRY(cudaEventElapsedTime(&res->label_ms, ctx->ev[2], ctx->ev[3]));
     }
     return CAC_OK;

@@ -442,10 +442,12 @@ int cac_cc_edges(cac_ctx *ctx, uint32_t n, uint64_t m, const uint32_t *u_host, c
     cudaStream_t s = ctx->stream;
     int st = CAC_OK;
     cac_cc_result r{};
-    // Up to 32 Mi edges, copy then run the device-resident query (sampling round + filter):
-    // measured faster than streaming on BA n=1,024,000 (0.91 vs 1.08 ms). Above, stream the
-    // edges in chunks and hook them as they arrive (R-MAT scale 22: 2.83 vs 3.37 ms).
-    if (m <= (32ull << 20)) {
+    // Up to 2 Mi edges, copy then run the device-resident query (sampling round + filter). Above,
+    // the edges cross in an order that lets the query run behind the copy (cc_run_streamed),
+    // measured faster from 4 M edges on (e.g. 0.36 vs 0.41 ms on G(500000, M) with 4 M edges, 0.75
+    // vs 0.91 ms on BA n=1,024,000, 2.82 vs 3.35 ms on R-MAT scale 22) and equal at 2 Mi.
+    bool streamed = false;
+    if (m <= (2ull << 20)) {
         if (m && (cudaMemcpyAsync(du, u_host, m * 4, cudaMemcpyHostToDevice, s) != cudaSuccess ||
                   cudaMemcpyAsync(dv, v_host, m * 4, cudaMemcpyHostToDevice, s) != cudaSuccess)) {
             set_error("cac_cc_edges: upload failed");
@@ -453,9 +455,10 @@ int cac_cc_edges(cac_ctx *ctx, uint32_t n, uint64_t m, const uint32_t *u_host, c
         }
         if (st == CAC_OK) st = cc_run(ctx, n, m, du, dv, seed, virtual_ranks, labels_host ? dl : nullptr, &r);
     } else {
-        st = cc_run_streamed(ctx, n, m, u_host, v_host, du, dv, labels_host ? dl : nullptr, &r);
+        st = cc_run_streamed(ctx, n, m, u_host, v_host, du, dv, labels_host ? dl : nullptr, labels_host, &r);
+        streamed = true;
     }
-    if (st == CAC_OK && labels_host && n) {
+    if (st == CAC_OK && labels_host && n && !streamed) {
         if (cudaMemcpyAsync(labels_host, dl, (size_t)n * 4, cudaMemcpyDeviceToHost, s) != cudaSuccess ||
             cudaStreamSynchronize(s) != cudaSuccess) {
             set_error("cac_cc_edges: label download failed");

@@ -112,9 +112,12 @@ typedef struct {
 int cac_cc(cac_ctx *ctx, const cac_graph *g, uint32_t seed, uint32_t virtual_ranks, uint32_t *labels,
            int labels_where, cac_cc_result *res);
 /* The same from host edge arrays to host labels in one call (host<->device copies included).
- * Above 32 Mi edges the edges cross the host link in chunks while the device hooks the chunks
- * that have arrived (res->rounds is then 1 and res->sampled_edges 0: no sampling round); below,
- * they are copied and the device-resident query runs. The labels are the same either way. */
+ * Up to 2 Mi edges the edges are copied and the device-resident query runs. Above, the query runs
+ * behind the copy: 8 evenly spaced pieces of the list holding the reference's sample budget
+ * (n^1.045 * 1.2 edges) cross first and are hooked (res->sampled_edges = their size), then the
+ * gaps between them stream through the giant-component filter as they land. Pinned host arrays
+ * are faster (the pieces are pulled by a kernel while the gaps are copied); a repeated call with
+ * the same arrays replays one captured CUDA graph. The labels are the same either way. */
 int cac_cc_edges(cac_ctx *ctx, uint32_t n, uint64_t m, const uint32_t *u_host, const uint32_t *v_host,
                  uint32_t seed, uint32_t virtual_ranks, uint32_t *labels_host, cac_cc_result *res);
 

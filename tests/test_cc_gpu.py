@@ -113,22 +113,63 @@ def test_one_call_host_entry_point(ctx):
     assert 0 <= res.sampled_edges - O.cc_sample_count(n, len(u)) < 32 * 2
 
 
+def _pinned(a):
+    torch = pytest.importorskip("torch")
+    t = torch.from_numpy(np.ascontiguousarray(a, np.uint32).view(np.int32)).pin_memory()
+    return t, t.numpy().view(np.uint32)
+
+
+@pytest.mark.parametrize("kind", ["connected_parts", "sparse_forest"])
+def test_host_entry_point_streamed_piece_paths(ctx, kind):
+    # above 2 Mi edges the host edge list streams: pageable arrays (pieces in one strided copy per
+    # array), pinned arrays (pieces pulled by a kernel), pinned arrays 4 bytes off a 16-byte
+    # boundary (strided copy again), and a call without labels. The sparse forest's sample budget
+    # covers the whole list (no gaps, no filter).
+    if kind == "connected_parts":
+        n0, u0, v0, _ = graphgen.erdos_renyi_m(300000, 16.0, 8)
+        extra = np.arange(n0, n0 + 4000, 2, dtype=np.uint32)  # 2000 two-vertex components
+        n = n0 + 4000 + 77                                      # and 77 isolated vertices
+        u = np.concatenate([u0, extra]).astype(np.uint32)
+        v = np.concatenate([v0, extra + 1]).astype(np.uint32)
+    else:
+        n, u, v, _ = graphgen.erdos_renyi_m(3000000, 1.47, 9)
+    assert len(u) > (2 << 20)
+    want_count, want = O.cc_labels(n, u, v)
+    (ta, pua), (tb, pva) = _pinned(u), _pinned(v)
+    (tc, puo), (td, pvo) = _pinned(np.concatenate([[0], u])), _pinned(np.concatenate([[0], v]))
+    assert pua.ctypes.data % 16 == 0 and puo[1:].ctypes.data % 16 == 4
+    lab = np.zeros(n, np.uint32)
+    for hu, hv in ((u, v), (pua, pva), (puo[1:], pvo[1:])):
+        for _ in range(3):  # direct, captured, replayed
+            lab[:] = 0
+            res = ctx.cc_edges(n, hu, hv, seed=3, labels=lab)
+            assert res.num_components == want_count and np.array_equal(lab, want)
+    assert ctx.cc_edges(n, pua, pva, seed=3).num_components == want_count
+
+
 @pytest.mark.slow
 def test_one_call_host_entry_point_streams_chunks(ctx):
-    # 35 M edges (above 32 Mi): chunks cross the host link while earlier ones are hooked, the
-    # later ones through the giant-component filter; a second, disconnected copy of the graph and
-    # isolated vertices check the labels of many components
+    # 35 M edges from host arrays: the sample pieces are hooked as they arrive, the gaps between
+    # them stream through the giant-component filter; a second, disconnected copy of the graph and
+    # isolated vertices check the labels of many components. Pageable arrays (pieces through the
+    # copy engine), pinned arrays (pieces read by the kernels directly) and a vertex-sorted list;
+    # three calls each: run directly, captured into a graph, replayed.
     n0, u0, v0, _ = graphgen.barabasi_albert(1100000, 16, 3)
     n = 2 * n0 + 1001
     u = np.concatenate([u0, u0 + n0]).astype(np.uint32)
     v = np.concatenate([v0, v0 + n0]).astype(np.uint32)
     u, v = u[:-3], v[:-3]  # a length that is not a multiple of 4 or of the chunk
     want_count, want = O.cc_labels(n, u, v)
+    order = np.lexsort((v, u))
+    (tu, pu), (tv, pv) = _pinned(u), _pinned(v)
     lab = np.zeros(n, np.uint32)
-    for _ in range(2):  # the staging buffers are reused by the next call
-        res = ctx.cc_edges(n, u, v, labels=lab)
-        assert res.num_components == want_count and np.array_equal(lab, want)
-        assert res.rounds == 1 and res.sampled_edges == 0  # every edge hooked as it arrives
+    for hu, hv in ((u, v), (pu, pv), (u[order], v[order])):
+        for _ in range(3):  # the staging buffers are reused by the next call
+            lab[:] = 0
+            res = ctx.cc_edges(n, hu, hv, labels=lab)
+            assert res.num_components == want_count and np.array_equal(lab, want)
+            # the pieces hold the reference's sample budget, rounded up to 256-edge pieces
+            assert res.rounds == 2 and 0 <= res.sampled_edges - O.cc_sample_count(n, len(u)) < 8 * 256
 
 
 @pytest.mark.slow
