@@ -37,6 +37,7 @@
 namespace cac {
 namespace {
 
+constexpr uint32_t kSharedRowMinN = 2000;  // quotient steps from this N on use the shared-row kernel
 constexpr uint32_t kMaxSmemVertices = kMaxDenseVertices;  // union-find of a contraction held in shared memory
 constexpr int kBatch = 1024;                  // draws gathered before the ordered contraction
 constexpr int kNT = 512;                      // threads of the per-trial / per-task CTAs
@@ -581,6 +582,123 @@ __global__ void __launch_bounds__(NT) quotient_kernel(const TaskDesc *__restrict
 __device__ __forceinline__ void sadd(uint32_t *p, uint64_t v) { atomicAdd(p, (uint32_t)v); }
 __device__ __forceinline__ void sadd(uint64_t *p, uint64_t v) {
     atomicAdd(reinterpret_cast<unsigned long long *>(p), (unsigned long long)v);
+}
+
+// The quotient for large N: one CTA of 8 warps per group of `rows` consecutive output rows, all
+// warps on the same output row at a time. The warp kernel below gives every warp its own k-entry
+// row in shared memory, which at N in the thousands leaves room for only a few warps per SM; here
+// the CTA shares one row (labels + one row: 8 CTAs, 64 warps per SM at N = 4000), and the warps
+// split the columns: 128-column chunks (one 16-byte load per lane), chunk c to warp c mod 8, four
+// chunks per warp in flight. Per output row: zero the row, sum the member rows chunk by chunk and
+// add every column into its label's slot (shared atomics), store the row with the diagonal zeroed
+// and its 32-column block sums, then one warp turns the block sums into the block prefixes and the
+// row sum (the next step's row prep).
+template <typename Ts, typename Tm>
+__global__ void __launch_bounds__(256) quotient_shared_row_kernel(const TaskDesc *__restrict__ tasks,
+                                                                  const SrcDesc *__restrict__ srcs,
+                                                                  const uint32_t *__restrict__ kdim,
+                                                                  const uint64_t *__restrict__ group_task_off,
+                                                                  uint32_t ntasks, uint32_t rows,
+                                                                  const uint64_t *__restrict__ out_off,
+                                                                  unsigned char *out_base, uint32_t lab_words,
+                                                                  uint32_t kmax) {
+    extern __shared__ __align__(16) unsigned char dsm[];
+    const uint64_t gg = blockIdx.x;
+    uint32_t lo = 0, hi = ntasks - 1;
+    while (lo < hi) {  // last task whose first row group <= gg
+        const uint32_t mid = (lo + hi + 1) >> 1;
+        if (group_task_off[mid] <= gg) lo = mid; else hi = mid - 1;
+    }
+    const TaskDesc T = tasks[lo];
+    const SrcDesc S = srcs[T.src];
+    const uint32_t k = kdim[lo];
+    const uint32_t N = S.N;
+    const uint32_t a0 = (uint32_t)(gg - group_task_off[lo]) * rows, a1 = min(k, a0 + rows);
+    if (!width_is<Tm>(S.small)) return;
+    const Tm *mat = reinterpret_cast<const Tm *>(S.mat);
+    constexpr int VEC = 16 / sizeof(Tm);  // columns per 16-byte load
+    constexpr uint32_t NWARP = 8;
+    using Vec = typename std::conditional<sizeof(Tm) == 4, uint4, ulonglong2>::type;
+    const uint64_t ldN = ld_of(N);
+    uint32_t *s_lab = reinterpret_cast<uint32_t *>(dsm);  // N
+    Ts *qrow = reinterpret_cast<Ts *>(dsm + (size_t)lab_words * 4);  // kmax
+    uint64_t *bsum = reinterpret_cast<uint64_t *>(dsm + (size_t)lab_words * 4 + (((size_t)kmax * sizeof(Ts) + 15) & ~(size_t)15));
+    const uint32_t lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    for (uint32_t i = threadIdx.x; i < N; i += blockDim.x) s_lab[i] = T.lab[i];
+    Tm *Qt = reinterpret_cast<Tm *>(out_base + out_off[lo]);
+    uint64_t *rowsum_out = reinterpret_cast<uint64_t *>(out_base + out_off[ntasks + lo]);
+    const uint32_t small = S.small;
+    const uint32_t nbk = (k + 31) / 32;
+    uint64_t *blk = rowsum_out + k;
+    const uint32_t nchunk = (N + 32 * VEC - 1) / (32 * VEC);
+    for (uint32_t a = a0; a < a1; a++) {
+        for (uint32_t b = threadIdx.x; b < k; b += blockDim.x) qrow[b] = 0;
+        __syncthreads();  // labels staged (first row), row zeroed
+        const uint32_t p0 = T.memb_off[a], p1 = T.memb_off[a + 1];
+        for (uint32_t c0 = warp; c0 < nchunk; c0 += 4 * NWARP) {
+            Tm x[4][VEC];
+#pragma unroll
+            for (int u = 0; u < 4; u++)
+#pragma unroll
+                for (int t = 0; t < VEC; t++) x[u][t] = 0;
+            for (uint32_t p = p0; p < p1; p++) {
+                const Vec *row = reinterpret_cast<const Vec *>(mat + (uint64_t)T.members[p] * ldN);
+#pragma unroll
+                for (int u = 0; u < 4; u++) {
+                    const uint32_t c = (c0 + u * NWARP) * 32 * VEC + lane * VEC;
+                    if (c < N) {
+                        const Vec q = __ldg(row + c / VEC);
+                        const Tm *e = reinterpret_cast<const Tm *>(&q);
+#pragma unroll
+                        for (int t = 0; t < VEC; t++) x[u][t] += e[t];
+                    }
+                }
+            }
+#pragma unroll
+            for (int u = 0; u < 4; u++)
+#pragma unroll
+                for (int t = 0; t < VEC; t++) {
+                    const uint32_t j = (c0 + u * NWARP) * 32 * VEC + lane * VEC + t;
+                    if (j < N && x[u][t]) sadd(&qrow[s_lab[j]], (uint64_t)x[u][t]);
+                }
+        }
+        __syncthreads();  // the row is complete
+        const uint64_t qb = (uint64_t)a * ld_of(k);
+        for (uint32_t b0 = warp * 32; b0 < k; b0 += NWARP * 32) {
+            const uint32_t b = b0 + lane;
+            uint64_t v = (b < k && b != a) ? (uint64_t)qrow[b] : 0;
+            if (b < k) Qt[qb + b] = (Tm)v;
+            if (small) {  // every entry < 2^32: two 32-bit reductions of the 16-bit halves are exact
+                const uint32_t lo16 = __reduce_add_sync(0xffffffffu, (uint32_t)(v & 0xFFFFu));
+                const uint32_t hi16 = __reduce_add_sync(0xffffffffu, (uint32_t)(v >> 16));
+                v = (uint64_t)lo16 + ((uint64_t)hi16 << 16);
+            } else {
+#pragma unroll
+                for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+            }
+            if (lane == 0) bsum[b0 >> 5] = v;
+        }
+        __syncthreads();  // block sums complete; the row may be zeroed again after the next barrier
+        if (warp == 0) {
+            // inclusive prefix of the block sums: lane l owns blocks [l * per, (l + 1) * per)
+            const uint32_t per = (nbk + 31) / 32;
+            const uint32_t j0 = lane * per, j1 = min(nbk, j0 + per);
+            uint64_t own = 0;
+            for (uint32_t j = j0; j < j1; j++) own += bsum[j];
+            uint64_t incl = own;
+#pragma unroll
+            for (int o = 1; o < 32; o <<= 1) {
+                const uint64_t y = __shfl_up_sync(0xffffffffu, incl, o);
+                if (lane >= (uint32_t)o) incl += y;
+            }
+            uint64_t run = incl - own;
+            for (uint32_t j = j0; j < j1; j++) {
+                run += bsum[j];
+                blk[(uint64_t)a * nbk + j] = run;
+            }
+            if (lane == 31) rowsum_out[a] = incl;
+        }
+    }
 }
 
 // One CTA per group of `rows` consecutive output rows of one child, one warp per output row at a
@@ -1164,7 +1282,8 @@ int KsEngine::step() {
     }
     // warp-per-row quotient with 8 (or 4) warps where three or more of its CTAs fit on an SM
     // (labels + one k-entry row per warp within 80 KB), else the CTA-per-row-group kernel, whose
-    // 256 threads share one row and keep the SM occupied at large N
+    // 256 threads share one row and keep the SM occupied at large N; large steps take the
+    // shared-row kernel
     const size_t stage_words = ((size_t)maxN + 3) & ~(size_t)3;  // N u32 labels, 16-byte rounded
     bool all_small = true;
     uint32_t kmax = 0;
@@ -1173,10 +1292,14 @@ int KsEngine::step() {
         kmax = std::max(kmax, kq[i]);
     }
     const size_t rs_bytes = all_small ? 4 : 8;
-    const uint32_t qwarps = stage_words * 4 + 8 * rs_bytes * (size_t)kmax <= 80 * 1024   ? 8u
+    // from N = 2000 on, the shared-row kernel (8 warps on one output row): K4000 14.5 vs 15.2-15.8
+    // ms per query; from N = 500 or 1000 on it slows the 256-graph batch (by 41% and 9%)
+    const bool shared_row = maxN >= kSharedRowMinN;
+    const uint32_t qwarps = shared_row ? 8u
+                            : stage_words * 4 + 8 * rs_bytes * (size_t)kmax <= 80 * 1024   ? 8u
                             : stage_words * 4 + 4 * rs_bytes * (size_t)kmax <= 80 * 1024 ? 4u
                                                                                          : 0u;
-    const uint32_t wrows = qwarps * 4;
+    const uint32_t wrows = shared_row ? 8u : qwarps * 4;
     if (qwarps) {
         groups = 0;
         // after the matrices: each child's row sums and block prefixes, written by the warp kernel
@@ -1194,7 +1317,23 @@ int KsEngine::step() {
         CAC_TRY(upload(ctx_, d_qoff, out_off));
         CAC_TRY(upload(ctx_, d_gto, group_task_off));
         CAC_CUDA_TRY(cudaMemcpyAsync(d_kout.p, kq.data(), tasks.size() * 4, cudaMemcpyHostToDevice, s));
-        if (qwarps) {
+        if (shared_row) {
+            const size_t ssm = stage_words * 4 + (((size_t)kmax * rs_bytes + 15) & ~(size_t)15) +
+                               ((size_t)kmax / 32 + 1) * 8;
+            std::vector<decltype(&quotient_shared_row_kernel<uint32_t, uint32_t>)> kerns;
+            if (all_small) kerns.push_back(quotient_shared_row_kernel<uint32_t, uint32_t>);
+            else {
+                if (t32) kerns.push_back(quotient_shared_row_kernel<uint64_t, uint32_t>);
+                if (t64) kerns.push_back(quotient_shared_row_kernel<uint64_t, uint64_t>);
+            }
+            for (auto kern : kerns) {
+                CAC_TRY(smem_optin(ctx_, kern));
+                kern<<<(unsigned)groups, 256, ssm, s>>>(
+                    d_task.as<TaskDesc>(), d_src.as<SrcDesc>(), d_kout.as<uint32_t>(), d_gto.as<uint64_t>(),
+                    (uint32_t)tasks.size(), wrows, d_qoff.as<uint64_t>(), static_cast<unsigned char *>(out->p),
+                    (uint32_t)stage_words, kmax);
+            }
+        } else if (qwarps) {
             // shared rows are u32 only when every task's sums fit (all sources small)
             const size_t wsm = stage_words * 4 + (size_t)qwarps * kmax * rs_bytes;
             std::vector<decltype(&quotient_warp_kernel<uint32_t, uint32_t>)> kerns;

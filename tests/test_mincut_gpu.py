@@ -224,3 +224,18 @@ def test_karger_stein_rejects_graphs_above_the_dense_limit(ctx, libcac):
     with pytest.raises(libcac.CacError) as e:
         ctx.graph(n, u, v, w).karger_stein(0.9, 0)
     assert e.value.status == -6
+
+
+@pytest.mark.parametrize("big", [False, True])
+def test_shared_row_quotient_trials_match_replay(ctx, big):
+    # K2100 keeps t = n, so the first quotient steps have N >= 2000 and take the shared-row kernel
+    # (8 warps on one output row); u32 node matrices, and u64 when the total weight passes 2^32
+    n = 2100
+    if big:
+        n, u, v, w = graphgen.complete(n, 31, wmin=1 << 20, wmax=1 << 22)
+    else:
+        n, u, v, w = graphgen.complete(n, 31)
+    assert O.intermediate_size(n, len(u)) >= n
+    got = ctx.graph(n, u, v, w).trials(seed=5, virtual_ranks=1, trials_per_rank=2)
+    for i in range(2):
+        assert int(got[0, i]) == O.mincut_trial(n, u, v, w, 5, 0, i)
