@@ -1003,6 +1003,26 @@ struct DevBuf {
     template <typename T> T *as() const { return reinterpret_cast<T *>(p); }
 };
 
+// Grow-only scratch buffers kept by the ctx between calls: a fresh device allocation per query
+// (cudaMalloc, and a cudaFree that waits for the whole device) cost more than the kernels of a
+// small query (C1 admission: 303 us, of which about 100 us of kernels). Slots 0..10 belong to the
+// Karger-Stein engine, 11..15 to admission, 16.. to the one-shot probes; one engine runs per ctx at
+// a time.
+enum ScratchSlot : int {
+    kSlotSrc, kSlotTask, kSlotLeaf, kSlotRowoff, kSlotKout, kSlotPrep, kSlotTscratch, kSlotQoff, kSlotGto, kSlotErr,
+    kSlotPsrc, kSlotPre, kSlotLab, kSlotK, kSlotSd, kSlotDd, kSlotProbe0, kSlotProbe1, kSlotProbe2, kSlotCount
+};
+
+struct CtxScratch {
+    std::vector<DevBuf> slots;
+    explicit CtxScratch(cac_ctx *ctx) : slots(kSlotCount, DevBuf(ctx)) {}
+};
+
+DevBuf &scratch(cac_ctx *ctx, ScratchSlot slot) {
+    if (!ctx->ks_scratch) ctx->ks_scratch = new CtxScratch(ctx);
+    return static_cast<CtxScratch *>(ctx->ks_scratch)->slots[slot];
+}
+
 template <typename T>
 int upload(cac_ctx *ctx, DevBuf &buf, const std::vector<T> &v) {
     CAC_TRY(buf.ensure(sizeof(T) * std::max<size_t>(v.size(), 1)));
@@ -1017,12 +1037,18 @@ size_t quotient_smem(uint32_t N) { return (size_t)N * 8; }
 
 }  // namespace
 
+void ctx_scratch_free(cac_ctx *ctx) {
+    delete static_cast<CtxScratch *>(ctx->ks_scratch);
+    ctx->ks_scratch = nullptr;
+}
+
 // ---- Karger-Stein engine (declared in cac_internal.h) ----
 
 KsEngine::KsEngine(cac_ctx *ctx)
-    : ctx_(ctx), d_src_(new DevBuf(ctx)), d_task_(new DevBuf(ctx)), d_leaf_(new DevBuf(ctx)),
-      d_rowoff_(new DevBuf(ctx)), d_kout_(new DevBuf(ctx)), d_prep_(new DevBuf(ctx)), d_tscratch_(new DevBuf(ctx)),
-      d_qoff_(new DevBuf(ctx)), d_gto_(new DevBuf(ctx)), d_err_(new DevBuf(ctx)), d_psrc_(new DevBuf(ctx)) {}
+    : ctx_(ctx), d_src_(&scratch(ctx, kSlotSrc)), d_task_(&scratch(ctx, kSlotTask)), d_leaf_(&scratch(ctx, kSlotLeaf)),
+      d_rowoff_(&scratch(ctx, kSlotRowoff)), d_kout_(&scratch(ctx, kSlotKout)), d_prep_(&scratch(ctx, kSlotPrep)),
+      d_tscratch_(&scratch(ctx, kSlotTscratch)), d_qoff_(&scratch(ctx, kSlotQoff)), d_gto_(&scratch(ctx, kSlotGto)),
+      d_err_(&scratch(ctx, kSlotErr)), d_psrc_(&scratch(ctx, kSlotPsrc)) {}
 
 KsEngine::~KsEngine() {
     cudaStreamSynchronize(ctx_->stream);
@@ -1030,8 +1056,6 @@ KsEngine::~KsEngine() {
     for (const KTask &t : carried_) release(t.src.buf);
     nodes_.clear();
     carried_.clear();
-    for (void *b : {d_src_, d_task_, d_leaf_, d_rowoff_, d_kout_, d_prep_, d_tscratch_, d_qoff_, d_gto_, d_err_, d_psrc_})
-        delete static_cast<DevBuf *>(b);
 }
 
 int KsEngine::init_err() {
@@ -1421,7 +1445,7 @@ int admit(cac_ctx *ctx, KsEngine &eng, const QueryPlan &q) {
         CAC_TRY(eng.alloc(bytes, &root));
         CAC_CUDA_TRY(cudaMemsetAsync(root->p, 0, bytes, s));
         if (m) {
-            DevBuf d(ctx);
+            DevBuf &d = scratch(ctx, kSlotDd);
             std::vector<DenseDesc> dd{DenseDesc{g->u, g->v, g->w, nullptr, root->p, m, n, small}};
             CAC_TRY(upload(ctx, d, dd));
             dim3 grid((unsigned)std::max<uint64_t>(1, std::min<uint64_t>((m + 255) / 256, (uint64_t)ctx->num_sms * 8)), 1);
@@ -1443,7 +1467,8 @@ int admit(cac_ctx *ctx, KsEngine &eng, const QueryPlan &q) {
     const uint64_t per_trial = big ? shrink_big_scratch(n, m, 1) + 4ull * n
                                    : 8 * std::max<uint64_t>(m, 1) + 4 * (uint64_t)n + 64;
     const uint64_t chunk = std::max<uint64_t>(1, std::min<uint64_t>({q.trials, (4ull << 30) / per_trial, (uint64_t)65535}));
-    DevBuf d_pre(ctx), d_lab(ctx), d_k(ctx), d_sd(ctx), d_dd(ctx);
+    DevBuf &d_pre = scratch(ctx, kSlotPre), &d_lab = scratch(ctx, kSlotLab), &d_k = scratch(ctx, kSlotK),
+           &d_sd = scratch(ctx, kSlotSd), &d_dd = scratch(ctx, kSlotDd);
     const size_t sm = kBatch * sizeof(uint2) + kCoarse * sizeof(uint64_t) + (size_t)std::min(n, kMaxSmemVertices) * 4;
     if (!big)
         CAC_TRY(smem_optin(ctx, iss_shrink_kernel<kNT>));
@@ -1644,7 +1669,7 @@ int ks_dense_one(cac_ctx *ctx, uint32_t n, const uint64_t *mat_host, uint32_t se
     uint32_t small = 0;
     CAC_TRY(host_matrix(n, mat_host, &small, dev));
     cudaStream_t s = ctx->stream;
-    DevBuf d_cut(ctx);
+    DevBuf &d_cut = scratch(ctx, kSlotProbe0);
     CAC_TRY(d_cut.ensure(8));
     {
         KsEngine eng(ctx);
@@ -1673,7 +1698,7 @@ int exact_small(cac_ctx *ctx, uint32_t n, const uint64_t *mat_host, uint64_t *cu
     uint32_t small = 0;
     CAC_TRY(host_matrix(n, mat_host, &small, dev));
     cudaStream_t s = ctx->stream;
-    DevBuf buf(ctx), d_cuts(ctx), d_leaf(ctx);
+    DevBuf &buf = scratch(ctx, kSlotProbe0), &d_cuts = scratch(ctx, kSlotProbe1), &d_leaf = scratch(ctx, kSlotProbe2);
     CAC_TRY(buf.ensure(dev.size()));
     CAC_TRY(d_cuts.ensure(8));
     CAC_CUDA_TRY(cudaMemcpyAsync(buf.p, dev.data(), dev.size(), cudaMemcpyHostToDevice, s));

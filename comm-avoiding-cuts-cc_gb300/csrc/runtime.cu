@@ -328,6 +328,7 @@ int cac_ctx_destroy(cac_ctx *ctx) {
     }
     ctx->graphs.clear();
     cc_graph_reset(ctx);
+    ctx_scratch_free(ctx);
     dev_free(ctx, ctx->arena.base, ctx->arena.cap);
     dev_free(ctx, ctx->io.base, ctx->io.cap);
     if (ctx->pool) cudaMemPoolDestroy(ctx->pool);
