@@ -118,6 +118,10 @@ inline int smem_optin(cac_ctx *ctx, F *func) {
 // Device memory accounting against the ctx budget.
 int dev_alloc(cac_ctx *ctx, void **p, size_t bytes);
 void dev_free(cac_ctx *ctx, void *p, size_t bytes);
+// Per-query temporaries, stream-ordered on the ctx stream from the ctx's pool (no device-wide
+// synchronisation as with cudaFree; the pool keeps freed memory for the next query).
+int stream_alloc(cac_ctx *ctx, void **p, size_t bytes);
+void stream_free(cac_ctx *ctx, void *p, size_t bytes);
 // Scratch arena: reset, then carve aligned chunks (grows by reallocating when too small;
 // growing invalidates earlier chunks, so callers size everything before carving).
 int arena_reserve(cac_ctx *ctx, Arena &a, size_t bytes);

@@ -24,14 +24,14 @@ int cac_mincut_trials(cac_ctx *ctx, const cac_graph *g, uint32_t seed, uint32_t 
     const uint64_t total = (uint64_t)virtual_ranks * trials_per_rank;
     if (total == 0) return CAC_OK;
     void *d = nullptr;
-    CAC_TRY(dev_alloc(ctx, &d, total * 8));
+    CAC_TRY(stream_alloc(ctx, &d, total * 8));
     float ms = 0;
     int st = mincut_trials(ctx, g, seed, virtual_ranks, trials_per_rank, (uint64_t *)d, &ms);
     if (st == CAC_OK) {
         cudaError_t e = cudaMemcpy(cuts_host, d, total * 8, cudaMemcpyDeviceToHost);
         if (e != cudaSuccess) { set_error(cudaGetErrorString(e)); st = CAC_ERR_CUDA; }
     }
-    dev_free(ctx, d, total * 8);
+    stream_free(ctx, d, total * 8);
     return st;
 }
 
@@ -59,7 +59,7 @@ int cac_mincut(cac_ctx *ctx, const cac_graph *g, double p, uint32_t seed, uint32
     res->high_concurrency = virtual_ranks >= 2u * (uint32_t)total ? 1u : 0u;
     const uint64_t n_tr = (uint64_t)res->total_trials;
     void *d = nullptr;
-    CAC_TRY(dev_alloc(ctx, &d, n_tr * 8));
+    CAC_TRY(stream_alloc(ctx, &d, n_tr * 8));
     float ms = 0;
     int st = mincut_trials(ctx, g, seed, virtual_ranks, per, (uint64_t *)d, &ms);
     if (st == CAC_OK) {
@@ -69,7 +69,7 @@ int cac_mincut(cac_ctx *ctx, const cac_graph *g, double p, uint32_t seed, uint32
         else res->cut = *std::min_element(cuts.begin(), cuts.end());
     }
     res->device_ms = ms;
-    dev_free(ctx, d, n_tr * 8);
+    stream_free(ctx, d, n_tr * 8);
     return st;
 }
 
@@ -94,7 +94,7 @@ int cac_karger_stein(cac_ctx *ctx, const cac_graph *g, double p, uint32_t seed, 
     res->total_trials = trials;
     res->intermediate = g->n;
     void *d = nullptr;
-    CAC_TRY(dev_alloc(ctx, &d, (uint64_t)trials * 8));
+    CAC_TRY(stream_alloc(ctx, &d, (uint64_t)trials * 8));
     std::vector<MincutQuery> q{MincutQuery{g, seed, 1, trials, static_cast<uint64_t *>(d), g->n}};
     float ms = 0;
     int st = mincut_run_queries(ctx, q, &ms);
@@ -109,7 +109,7 @@ int cac_karger_stein(cac_ctx *ctx, const cac_graph *g, double p, uint32_t seed, 
         }
     }
     res->device_ms = ms;
-    dev_free(ctx, d, (uint64_t)trials * 8);
+    stream_free(ctx, d, (uint64_t)trials * 8);
     return st;
 }
 
@@ -144,7 +144,7 @@ int cac_mincut_batch(cac_ctx *ctx, const cac_mincut_query *queries, uint32_t cou
     }
     if (total == 0) return CAC_OK;
     void *d = nullptr;
-    CAC_TRY(dev_alloc(ctx, &d, total * 8));
+    CAC_TRY(stream_alloc(ctx, &d, total * 8));
     uint64_t off = 0;
     for (auto &q : qs) {
         q.d_cuts = static_cast<uint64_t *>(d) + off;
@@ -168,7 +168,7 @@ int cac_mincut_batch(cac_ctx *ctx, const cac_mincut_query *queries, uint32_t cou
             }
         }
     }
-    dev_free(ctx, d, total * 8);
+    stream_free(ctx, d, total * 8);
     return st;
 }
 

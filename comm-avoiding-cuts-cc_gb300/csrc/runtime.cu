@@ -51,6 +51,35 @@ int dev_alloc(cac_ctx *ctx, void **p, size_t bytes) {
     return CAC_OK;
 }
 
+int stream_alloc(cac_ctx *ctx, void **p, size_t bytes) {
+    *p = nullptr;
+    if (bytes == 0) return CAC_OK;
+    if (ctx->budget && ctx->held + bytes > ctx->budget) {
+        set_error("HBM budget exceeded: need " + std::to_string(ctx->held + bytes) + " bytes, budget " +
+                  std::to_string(ctx->budget));
+        return CAC_ERR_OOM;
+    }
+    cudaError_t e = ctx->pool ? cudaMallocFromPoolAsync(p, bytes, ctx->pool, ctx->stream)
+                              : cudaMallocAsync(p, bytes, ctx->stream);
+    if (e != cudaSuccess) {
+        cudaGetLastError();
+        *p = nullptr;
+        set_error(std::string("cudaMallocAsync(") + std::to_string(bytes) + "): " + cudaGetErrorString(e));
+        return CAC_ERR_OOM;
+    }
+    ctx->held += bytes;
+    return CAC_OK;
+}
+
+void stream_free(cac_ctx *ctx, void *p, size_t bytes) {
+    if (!p) return;
+    if (cudaFreeAsync(p, ctx->stream) != cudaSuccess) {
+        const cudaError_t e = cudaGetLastError();
+        set_error(std::string("cudaFreeAsync: ") + cudaGetErrorString(e));
+    }
+    ctx->held -= std::min<uint64_t>(ctx->held, bytes);
+}
+
 void dev_free(cac_ctx *ctx, void *p, size_t bytes) {
     if (!p) return;
     if (cudaFree(p) != cudaSuccess) {

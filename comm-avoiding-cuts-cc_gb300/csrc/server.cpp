@@ -88,7 +88,7 @@ int run_cc(cac_ctx *ctx, Request *r) {
     const cac_graph *g = r->req.graph;
     cac_cc_result cr{};
     void *d_labels = nullptr;
-    if (r->req.labels_host && g->n) CAC_TRY(dev_alloc(ctx, &d_labels, (size_t)g->n * 4));
+    if (r->req.labels_host && g->n) CAC_TRY(stream_alloc(ctx, &d_labels, (size_t)g->n * 4));
     int st = cc_run(ctx, g->n, g->m, g->u, g->v, r->req.seed, r->ranks, static_cast<uint32_t *>(d_labels), &cr);
     if (st == CAC_OK && d_labels) {
         if (cudaMemcpyAsync(r->req.labels_host, d_labels, (size_t)g->n * 4, cudaMemcpyDeviceToHost, ctx->stream) !=
@@ -98,7 +98,7 @@ int run_cc(cac_ctx *ctx, Request *r) {
             st = CAC_ERR_CUDA;
         }
     }
-    if (d_labels) dev_free(ctx, d_labels, (size_t)g->n * 4);
+    if (d_labels) stream_free(ctx, d_labels, (size_t)g->n * 4);
     r->resp.num_components = cr.num_components;
     return st;
 }
@@ -152,7 +152,7 @@ struct CutWorker {
     }
 
     void retire(Request *r, int st, const std::string &msg) {
-        if (r->d_cuts) dev_free(s->cut, r->d_cuts, std::max<uint64_t>(r->trials, 1) * 8);
+        if (r->d_cuts) stream_free(s->cut, r->d_cuts, std::max<uint64_t>(r->trials, 1) * 8);
         r->d_cuts = nullptr;
         held_est -= r->est_bytes;
         free_ids.push_back(r->query);
@@ -162,7 +162,7 @@ struct CutWorker {
     void admit(Request *r) {
         r->query = take_id();
         running.push_back(r);
-        int st = dev_alloc(s->cut, &r->d_cuts, std::max<uint64_t>(r->trials, 1) * 8);
+        int st = stream_alloc(s->cut, &r->d_cuts, std::max<uint64_t>(r->trials, 1) * 8);
         if (st == CAC_OK) {
             MincutQuery q{r->req.graph, r->req.seed, r->ranks, r->per_rank, static_cast<uint64_t *>(r->d_cuts)};
             st = mincut_admit_query(s->cut, *eng, q, r->query);
