@@ -592,9 +592,10 @@ __device__ __forceinline__ void sadd(uint64_t *p, uint64_t v) {
 // chunks per warp in flight. Per output row: zero the row, sum the member rows chunk by chunk and
 // add every column into its label's slot (shared atomics), store the row with the diagonal zeroed
 // and its 32-column block sums, then one warp turns the block sums into the block prefixes and the
-// row sum (the next step's row prep).
+// row sum (the next step's row prep). Five CTAs per SM (48 registers): measured 1-3% faster on
+// K4000 than the four that 60 registers allow.
 template <typename Ts, typename Tm>
-__global__ void __launch_bounds__(256) quotient_shared_row_kernel(const TaskDesc *__restrict__ tasks,
+__global__ void __launch_bounds__(256, 5) quotient_shared_row_kernel(const TaskDesc *__restrict__ tasks,
                                                                   const SrcDesc *__restrict__ srcs,
                                                                   const uint32_t *__restrict__ kdim,
                                                                   const uint64_t *__restrict__ group_task_off,
