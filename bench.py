@@ -42,9 +42,9 @@ import numpy as np  # noqa: E402
 
 N_VERTICES, ATTACH, GRAPH_SEED = 1024000, 16, 0
 METRIC = "CC edges/s (parallel_cc, BA n=1,024,000 m=16)"
-# init, sample_draws, 8 x (sample_hook + compress4), find_giant, giant_bitmap, filter, hook_survivors,
-# finalize_count, scan_tiles, rank_roots, label_all
-KERNELS_PER_QUERY = 2 + 8 * 2 + 8
+# init, sample_draws, 8 x sample_hook, 4 x compress4 (after the first three slices and the last),
+# find_giant, giant_bitmap, filter, hook_survivors, finalize_count, scan_tiles, rank_roots, label_all
+KERNELS_PER_QUERY = 2 + 8 + 4 + 8
 
 
 def _peaks():
