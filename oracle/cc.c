@@ -12,6 +12,7 @@
  * kept as the CPU baseline of the same work (sampling, gather, shuffle, prefix union-find,
  * relabel, slice rewrite). Its labels must equal orc_cc_labels for every seed.
  */
+#include <pthread.h>
 #include <stdlib.h>
 #include <string.h>
 #include <math.h>
@@ -120,9 +121,82 @@ static void edges_to_sample(uint32_t n0, uint32_t ranks, const int *avail, int *
     }
 }
 
+/* The per-rank phases of a round (slice load, sampling, slice rewrite) run on `threads` host
+ * threads, rank r on thread r mod threads, as the reference's MPI ranks run them side by side;
+ * the root's gather, shuffle, prefix union-find and relabelling stay sequential. */
+typedef struct {
+    uint32_t ranks, threads, t, phase, n;
+    const uint32_t *u, *v, *map;
+    edge2 **sl;
+    uint64_t *len, *off;
+    uint64_t portion, m;
+    seq_engine *eng;
+    const int *per;
+    edge2 *gs;
+} rank_job;
+
+static void rank_phase(rank_job *J, uint32_t r) {
+    if (J->phase == 0) { /* load the slice as {from, to} records */
+        uint64_t from = J->portion * r;
+        for (uint64_t e = 0; e < J->len[r]; e++) { J->sl[r][e].from = J->u[from + e]; J->sl[r][e].to = J->v[from + e]; }
+    } else if (J->phase == 1) { /* sample (.cpp:24-37) into the rank's place of the gather */
+        edge2 *dst = J->gs + J->off[r];
+        if ((uint64_t)J->per[r] == J->len[r]) {
+            memcpy(dst, J->sl[r], sizeof(edge2) * J->len[r]);
+        } else {
+            for (int k = 0; k < J->per[r]; k++) {
+                uint64_t idx = eng_next(&J->eng[r]) % (uint32_t)J->len[r];
+                dst[k] = J->sl[r][idx];
+            }
+        }
+    } else { /* rewrite the slice and drop loops (IteratedSparseSampling.hpp:160-172) */
+        uint64_t w = 0;
+        for (uint64_t e = 0; e < J->len[r]; e++) {
+            uint32_t a = J->map[J->sl[r][e].from], b = J->map[J->sl[r][e].to];
+            if (a != b) { J->sl[r][w].from = a; J->sl[r][w].to = b; w++; }
+        }
+        J->len[r] = w;
+    }
+}
+
+static void *rank_worker(void *arg) {
+    rank_job *J = (rank_job *)arg;
+    for (uint32_t r = J->t; r < J->ranks; r += J->threads) rank_phase(J, r);
+    return NULL;
+}
+
+static void run_ranks(rank_job *base, uint32_t phase) {
+    uint32_t T = base->threads < base->ranks ? base->threads : base->ranks;
+    if (T <= 1) {
+        base->phase = phase;
+        for (uint32_t r = 0; r < base->ranks; r++) rank_phase(base, r);
+        return;
+    }
+    pthread_t *th = (pthread_t *)malloc(sizeof(pthread_t) * T);
+    rank_job *jobs = (rank_job *)malloc(sizeof(rank_job) * T);
+    uint32_t started = 0;
+    for (uint32_t t = 0; t < T; t++) {
+        jobs[t] = *base;
+        jobs[t].phase = phase;
+        jobs[t].t = t;
+        jobs[t].threads = T;
+        if (pthread_create(&th[t], NULL, rank_worker, &jobs[t]) == 0) started++;
+        else { jobs[t].threads = T; rank_worker(&jobs[t]); th[t] = 0; } /* run it here */
+    }
+    for (uint32_t t = 0; t < T; t++) if (th[t]) pthread_join(th[t], NULL);
+    (void)started;
+    free(th); free(jobs);
+}
+
 uint32_t orc_cc_iss(uint32_t n, uint64_t m, const uint32_t *u, const uint32_t *v, uint32_t seed, uint32_t ranks,
                     uint32_t *labels, uint32_t *rounds_out) {
+    return orc_cc_iss_mt(n, m, u, v, seed, ranks, 1, labels, rounds_out);
+}
+
+uint32_t orc_cc_iss_mt(uint32_t n, uint64_t m, const uint32_t *u, const uint32_t *v, uint32_t seed, uint32_t ranks,
+                       uint32_t threads, uint32_t *labels, uint32_t *rounds_out) {
     if (ranks == 0) ranks = 1;
+    if (threads == 0) threads = 1;
     /* slices: rank r owns lines [r*floor(m/P), (r+1)*floor(m/P)), the last rank the rest
      * (UnweightedIteratedSparseSampling.cpp:5-21) */
     /* slices hold {from, to} records like the reference's UnweightedGraph::Edge (8 bytes) */
@@ -134,9 +208,14 @@ uint32_t orc_cc_iss(uint32_t n, uint64_t m, const uint32_t *u, const uint32_t *v
         uint64_t from = portion * r, to = (r == ranks - 1) ? m : portion * (r + 1);
         len[r] = to - from;
         sl[r] = (edge2 *)malloc(sizeof(edge2) * (len[r] ? len[r] : 1));
-        for (uint64_t e = 0; e < len[r]; e++) { sl[r][e].from = u[from + e]; sl[r][e].to = v[from + e]; }
         eng_init(&eng[r], seed + r);
     }
+    uint64_t *off = (uint64_t *)calloc(ranks, sizeof(uint64_t));
+    rank_job job;
+    memset(&job, 0, sizeof(job));
+    job.ranks = ranks; job.threads = threads; job.n = n; job.u = u; job.v = v; job.sl = sl; job.len = len;
+    job.off = off; job.portion = portion; job.m = m; job.eng = eng;
+    run_ranks(&job, 0);
     uint32_t *comp = (uint32_t *)malloc(sizeof(uint32_t) * (n ? n : 1));
     for (uint32_t i = 0; i < n; i++) comp[i] = i;
     uint32_t vcount = n, rounds = 0;
@@ -158,17 +237,9 @@ uint32_t orc_cc_iss(uint32_t n, uint64_t m, const uint32_t *u, const uint32_t *v
         /* sample (.cpp:24-37) and gather in rank order (IteratedSparseSampling.hpp:261-271) */
         edge2 *gs = (edge2 *)malloc(sizeof(edge2) * (total ? total : 1));
         uint64_t at = 0;
-        for (uint32_t r = 0; r < ranks; r++) {
-            if ((uint64_t)per[r] == len[r]) {
-                memcpy(gs + at, sl[r], sizeof(edge2) * len[r]);
-                at += len[r];
-            } else {
-                for (int k = 0; k < per[r]; k++) {
-                    uint64_t idx = eng_next(&eng[r]) % (uint32_t)len[r];
-                    gs[at++] = sl[r][idx];
-                }
-            }
-        }
+        for (uint32_t r = 0; r < ranks; r++) { off[r] = at; at += (uint64_t)per[r]; }
+        job.per = per; job.gs = gs;
+        run_ranks(&job, 1);
         /* shuffle with the root's engine (IteratedSparseSampling.hpp:278). Fisher-Yates with
          * multiply-shift draws: libstdc++'s std::shuffle consumes the engine differently, which
          * only changes the order in which the prefix union-find meets the samples, never the
@@ -193,21 +264,15 @@ uint32_t orc_cc_iss(uint32_t n, uint64_t m, const uint32_t *u, const uint32_t *v
         }
         for (uint32_t i = 0; i < n; i++) comp[i] = map[comp[i]];
         /* every rank rewrites its slice and drops loops (IteratedSparseSampling.hpp:160-172) */
-        for (uint32_t r = 0; r < ranks; r++) {
-            uint64_t w = 0;
-            for (uint64_t e = 0; e < len[r]; e++) {
-                uint32_t a = map[sl[r][e].from], b = map[sl[r][e].to];
-                if (a != b) { sl[r][w].from = a; sl[r][w].to = b; w++; }
-            }
-            len[r] = w;
-        }
+        job.map = map;
+        run_ranks(&job, 2);
         vcount = active;
         free(gs);
     }
     if (labels) memcpy(labels, comp, sizeof(uint32_t) * n);
     if (rounds_out) *rounds_out = rounds;
     for (uint32_t r = 0; r < ranks; r++) free(sl[r]);
-    free(sl); free(len); free(eng); free(comp); free(avail); free(per);
+    free(sl); free(len); free(eng); free(comp); free(avail); free(per); free(off);
     free(parent); free(rk); free(lab); free(map);
     return vcount;
 }

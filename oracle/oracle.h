@@ -52,6 +52,9 @@ uint32_t orc_cc_labels(uint32_t n, uint64_t m, const uint32_t *u, const uint32_t
  * returns #components; *rounds_out (nullable) receives the number of rounds. */
 uint32_t orc_cc_iss(uint32_t n, uint64_t m, const uint32_t *u, const uint32_t *v, uint32_t seed, uint32_t ranks,
                     uint32_t *labels, uint32_t *rounds_out);
+/* the same with the per-rank phases on `threads` host threads (results identical) */
+uint32_t orc_cc_iss_mt(uint32_t n, uint64_t m, const uint32_t *u, const uint32_t *v, uint32_t seed, uint32_t ranks,
+                       uint32_t threads, uint32_t *labels, uint32_t *rounds_out);
 /* Sample count the reference asks for per round (UnweightedIteratedSparseSampling.cpp:82-85). */
 uint64_t orc_cc_sample_count(uint32_t n, uint64_t edges_left);
 

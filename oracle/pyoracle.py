@@ -33,6 +33,9 @@ def lib():
         L.orc_cc_iss.argtypes = [ctypes.c_uint32, ctypes.c_uint64, _u32p, _u32p, ctypes.c_uint32, ctypes.c_uint32,
                                  _u32p, _u32p]
         L.orc_cc_iss.restype = ctypes.c_uint32
+        L.orc_cc_iss_mt.argtypes = [ctypes.c_uint32, ctypes.c_uint64, _u32p, _u32p, ctypes.c_uint32, ctypes.c_uint32,
+                                    ctypes.c_uint32, _u32p, _u32p]
+        L.orc_cc_iss_mt.restype = ctypes.c_uint32
         L.orc_cc_sample_count.argtypes = [ctypes.c_uint32, ctypes.c_uint64]
         L.orc_cc_sample_count.restype = ctypes.c_uint64
         L.orc_stoer_wagner_dense.argtypes = [ctypes.c_uint32, _u64p]
@@ -109,11 +112,13 @@ def cc_labels(n, u, v):
     return int(count), labels[:n]
 
 
-def cc_iss(n, u, v, seed, ranks=1):
+def cc_iss(n, u, v, seed, ranks=1, threads=1):
+    """The reference's iterated-sparse-sampling CC loop over `ranks` ranks, their per-rank phases
+    on `threads` host threads (same result for any thread count)."""
     u, v = _c32(u), _c32(v)
     labels = np.zeros(max(n, 1), dtype=np.uint32)
     rounds = np.zeros(1, dtype=np.uint32)
-    count = lib().orc_cc_iss(n, len(u), _p32(u), _p32(v), seed, ranks, _p32(labels), _p32(rounds))
+    count = lib().orc_cc_iss_mt(n, len(u), _p32(u), _p32(v), seed, ranks, threads, _p32(labels), _p32(rounds))
     return int(count), labels[:n], int(rounds[0])
 
 

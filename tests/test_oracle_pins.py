@@ -145,3 +145,16 @@ def test_karger_stein_oracle_matches_reference(golden):
             cut, trials = O.karger_stein(n, u, v, w, 0.9, 0)
             assert trials == O.ks_number_of_trials(n, 0.9)
             assert cut == spec["karger_stein_cut"] == spec["exact_cut"], spec["name"]
+
+
+def test_threaded_iss_restatement_equals_sequential():
+    # the CPU baseline runs the reference's per-rank phases on one host thread per rank: the same
+    # sample draws per rank, so the same rounds and labels as the sequential restatement
+    import graphgen
+    n, u, v, _ = graphgen.barabasi_albert(20000, 4, 3)
+    want_count, want = O.cc_labels(n, u, v)
+    for ranks in (1, 3, 8):
+        c1, l1, r1 = O.cc_iss(n, u, v, 5, ranks, 1)
+        c4, l4, r4 = O.cc_iss(n, u, v, 5, ranks, 4)
+        assert (c1, r1) == (c4, r4) and c1 == want_count
+        assert np.array_equal(l1, l4) and np.array_equal(l1, want)
