@@ -67,6 +67,7 @@ struct CCGraphKey {
     uint32_t seed = 0, ranks = 0;
     const void *arena_base = nullptr;
     size_t arena_cap = 0;
+    bool check = false;
 };
 }  // namespace cac
 
@@ -141,8 +142,10 @@ struct CCPlan {
     std::vector<uint64_t> slice_off, slice_len, draws;
 };
 CCPlan cc_plan(uint32_t n, uint64_t m, uint32_t ranks);
+// check_ids: the endpoints were not validated (caller arrays); every kernel checks them and an
+// endpoint >= n fails the query with CAC_ERR_INVALID.
 int cc_run(cac_ctx *ctx, uint32_t n, uint64_t m, const uint32_t *d_u, const uint32_t *d_v, uint32_t seed,
-           uint32_t ranks, uint32_t *d_labels, cac_cc_result *res);
+           uint32_t ranks, uint32_t *d_labels, cac_cc_result *res, bool check_ids = false);
 size_t cc_scratch_bytes(uint32_t n, uint32_t ranks, uint64_t m);
 // CC of an edge list in host memory: parts copied to d_u/d_v on a second stream while the ctx
 // stream hooks or filters each part that has arrived (cac_cc_edges); labels copied to h_labels.

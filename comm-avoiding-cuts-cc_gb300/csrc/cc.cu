@@ -42,6 +42,8 @@ constexpr uint32_t kSampleSubrounds = 8;             // slices of the sampling r
 constexpr uint32_t kCompressedSubrounds = 3;         // slices followed by a full compression (and the last)
 constexpr uint32_t kMaxRegions = 1024;               // filter CTAs (regions of the survivor buffer)
 constexpr uint32_t kStreamPieces = 8;                // sample pieces (and gaps) of a host edge list
+constexpr uint32_t kErrWord = 9;                     // a query's error word (after its count and giant root)
+constexpr uint32_t kErrBadId = 1;                    // an edge endpoint was >= n (the edge was skipped)
 
 struct RankDesc {
     uint64_t slice_off;
@@ -99,6 +101,18 @@ __device__ __forceinline__ void edge_hook(uint32_t *par, uint32_t a, uint32_t b)
     unite(par, pa, pb);
 }
 
+// Edge lists handed in by the caller (host arrays of cac_cc_edges, device arrays of
+// cac_cc_noalloc) are not validated beforehand: an endpoint >= n skips the edge and sets the
+// query's error word instead of indexing past the parent array.
+template <bool kCheck>
+__device__ __forceinline__ void edge_hook_checked(uint32_t *par, uint32_t a, uint32_t b, uint32_t n, uint32_t *err) {
+    if (kCheck && (a >= n || b >= n)) {
+        atomicOr(err, kErrBadId);
+        return;
+    }
+    edge_hook(par, a, b);
+}
+
 __global__ void cc_init(uint32_t *par, uint32_t n) {
     for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) par[i] = i;
 }
@@ -136,15 +150,17 @@ __global__ void cc_sample_draws(const RankDesc *__restrict__ ranks, int nranks, 
 }
 
 // One warp per sampled chunk of the draw range [d0, d1): coalesced loads of its edges, each hooked.
+template <bool kCheck>
 __global__ void cc_sample_hook(uint32_t *par, const uint32_t *__restrict__ u, const uint32_t *__restrict__ v,
-                               const uint64_t *__restrict__ chunks, uint64_t d0, uint64_t d1) {
+                               const uint64_t *__restrict__ chunks, uint64_t d0, uint64_t d1, uint32_t n,
+                               uint32_t *err) {
     const uint32_t lane = threadIdx.x & 31;
     const uint64_t warps = ((uint64_t)gridDim.x * blockDim.x) >> 5;
     for (uint64_t d = d0 + (((uint64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5); d < d1; d += warps) {
         const uint64_t c = chunks[d];
         if (lane < (uint32_t)(c >> 32)) {
             const uint64_t e = (c & 0xFFFFFFFFull) + lane;
-            edge_hook(par, __ldg(u + e), __ldg(v + e));
+            edge_hook_checked<kCheck>(par, __ldg(u + e), __ldg(v + e), n, err);
         }
     }
 }
@@ -227,9 +243,10 @@ __global__ void cc_giant_bitmap(const uint32_t *par, uint32_t n, const uint32_t 
 
 // Closing pass without a sampling round: every edge hooks, 4 edges per thread step through
 // 16-byte streaming loads.
-template <bool kVec>
+template <bool kVec, bool kCheck>
 __global__ void __launch_bounds__(kThreads) cc_edge_pass(uint32_t *par, const uint32_t *__restrict__ u,
-                                                         const uint32_t *__restrict__ v, uint64_t m) {
+                                                         const uint32_t *__restrict__ v, uint64_t m, uint32_t n,
+                                                         uint32_t *err) {
     const uint64_t tid = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
     const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
     uint64_t done = 0;
@@ -240,14 +257,15 @@ __global__ void __launch_bounds__(kThreads) cc_edge_pass(uint32_t *par, const ui
         for (uint64_t i = tid; i < m4; i += stride) {
             const uint4 a = __ldcs(u4 + i);
             const uint4 b = __ldcs(v4 + i);
-            edge_hook(par, a.x, b.x);
-            edge_hook(par, a.y, b.y);
-            edge_hook(par, a.z, b.z);
-            edge_hook(par, a.w, b.w);
+            edge_hook_checked<kCheck>(par, a.x, b.x, n, err);
+            edge_hook_checked<kCheck>(par, a.y, b.y, n, err);
+            edge_hook_checked<kCheck>(par, a.z, b.z, n, err);
+            edge_hook_checked<kCheck>(par, a.w, b.w, n, err);
         }
         done = m4 << 2;
     }
-    for (uint64_t e = done + tid; e < m; e += stride) edge_hook(par, __ldcs(u + e), __ldcs(v + e));
+    for (uint64_t e = done + tid; e < m; e += stride)
+        edge_hook_checked<kCheck>(par, __ldcs(u + e), __ldcs(v + e), n, err);
 }
 
 // Filter pass after the sampling round (the reference's slice rewrite that drops loops,
@@ -258,11 +276,12 @@ __global__ void __launch_bounds__(kThreads) cc_edge_pass(uint32_t *par, const ui
 // two fully coalesced 512-byte loads per endpoint array, keeps 8 edges in flight, and appends its
 // survivors after one warp scan and one shared-memory atomic. The membership bitmap's first
 // `swords` words are staged in shared memory, the rest read through the read-only path.
-template <bool kAllSmem>
+template <bool kAllSmem, bool kCheck>
 __global__ void __launch_bounds__(kEdgeThreads) cc_filter(const uint32_t *__restrict__ u,
                                                           const uint32_t *__restrict__ v, uint64_t tiles,
                                                           const uint32_t *__restrict__ gbits, uint32_t nwords,
-                                                          uint2 *__restrict__ surv, uint32_t *__restrict__ counts) {
+                                                          uint2 *__restrict__ surv, uint32_t *__restrict__ counts,
+                                                          uint32_t n, uint32_t *err) {
     extern __shared__ uint32_t sbits[];
     __shared__ uint32_t s_n;
     const uint32_t swords = min(nwords, (uint32_t)kSmemBitmapWords);
@@ -283,9 +302,14 @@ __global__ void __launch_bounds__(kEdgeThreads) cc_filter(const uint32_t *__rest
     auto process = [&](const uint4 &ua, const uint4 &ub, const uint4 &va, const uint4 &vb) {
         const uint32_t a[8] = {ua.x, ua.y, ua.z, ua.w, ub.x, ub.y, ub.z, ub.w};
         const uint32_t b[8] = {va.x, va.y, va.z, va.w, vb.x, vb.y, vb.z, vb.w};
-        uint32_t keep = 0;
+        uint32_t keep = 0, bad = 0;
 #pragma unroll
-        for (int k = 0; k < 8; k++) keep |= (uint32_t)!(in_giant(a[k]) && in_giant(b[k])) << k;
+        for (int k = 0; k < 8; k++) {
+            const bool ok = !kCheck || (a[k] < n && b[k] < n);  // an invalid edge is neither tested nor kept
+            bad |= !ok;
+            keep |= (uint32_t)(ok && !(in_giant(ok ? a[k] : 0u) && in_giant(ok ? b[k] : 0u))) << k;
+        }
+        if (kCheck && bad) atomicOr(err, kErrBadId);
         const uint32_t cnt = __popc(keep);
         uint32_t incl = cnt;
 #pragma unroll
@@ -566,7 +590,9 @@ struct CCLaunch {
     uint32_t ntiles = 0, nwords = 0;
     uint64_t blocks = 0, draws = 0, drawn = 0;  // sitmo blocks, chunk draws, sampled edges
     uint64_t *chunks = nullptr;                  // per draw: first edge | count << 32
+    uint32_t *err = nullptr;                     // total + kErrWord
     bool vec = false;
+    bool check = false;                          // endpoints not validated: every kernel checks them
 };
 
 int record(cac_ctx *ctx, int i, bool capturing) {
@@ -582,6 +608,7 @@ int cc_enqueue(cac_ctx *ctx, const CCLaunch &L, bool capturing) {
     const uint64_t m = L.m;
     CAC_TRY(record(ctx, 0, capturing));
     cc_init<<<grid_for(ctx, n, 8), kThreads, 0, s>>>(L.par, n);
+    CAC_CUDA_TRY(cudaMemsetAsync(L.err, 0, 4, s));
     if (L.draws > 0 && m > 0) {
         CAC_CUDA_TRY(cudaMemcpyAsync(L.d_ranks, L.h_ranks, sizeof(RankDesc) * L.ranks, cudaMemcpyHostToDevice, s));
         // The draws are hooked in kSampleSubrounds slices: forest building from singletons is the
@@ -596,8 +623,8 @@ int cc_enqueue(cac_ctx *ctx, const CCLaunch &L, bool capturing) {
         const uint32_t sub = (uint32_t)std::min<uint64_t>(kSampleSubrounds, L.draws);
         for (uint32_t k = 0; k < sub; k++) {
             const uint64_t d0 = L.draws * k / sub, d1 = L.draws * (k + 1) / sub;
-            cc_sample_hook<<<grid_for(ctx, (d1 - d0) * 32, 8), kThreads, 0, s>>>(L.par, L.u, L.v, L.chunks, d0,
-                                                                                  d1);
+            auto hook = L.check ? cc_sample_hook<true> : cc_sample_hook<false>;
+            hook<<<grid_for(ctx, (d1 - d0) * 32, 8), kThreads, 0, s>>>(L.par, L.u, L.v, L.chunks, d0, d1, n, L.err);
             if (k < kCompressedSubrounds || k + 1 == sub) compress_all(ctx, L.par, n, s);
         }
         cc_find_giant<<<1, kGiantSample, 0, s>>>(L.par, n, L.giant);
@@ -613,8 +640,10 @@ int cc_enqueue(cac_ctx *ctx, const CCLaunch &L, bool capturing) {
                 1, std::min<uint64_t>({(uint64_t)ctx->num_sms, (uint64_t)kMaxRegions, tiles}));
             const uint64_t per = (tiles + regions - 1) / regions;
             if (tiles) {
-                auto filt = L.nwords <= kSmemBitmapWords ? cc_filter<true> : cc_filter<false>;
-                filt<<<regions, kEdgeThreads, sm, s>>>(L.u, L.v, tiles, L.bits, L.nwords, L.surv, L.region_counts);
+                auto filt = L.nwords <= kSmemBitmapWords ? (L.check ? cc_filter<true, true> : cc_filter<true, false>)
+                                                         : (L.check ? cc_filter<false, true> : cc_filter<false, false>);
+                filt<<<regions, kEdgeThreads, sm, s>>>(L.u, L.v, tiles, L.bits, L.nwords, L.surv, L.region_counts, n,
+                                                       L.err);
             }
             CAC_TRY(record(ctx, 4, capturing));
             if (tiles)
@@ -622,12 +651,14 @@ int cc_enqueue(cac_ctx *ctx, const CCLaunch &L, bool capturing) {
                                                                                    regions, per * 256);
             const uint64_t done = tiles * 256;
             if (done < m)
-                cc_edge_pass<false><<<grid_for(ctx, m - done, 8), kThreads, 0, s>>>(L.par, L.u + done, L.v + done,
-                                                                                     m - done);
+                (L.check ? cc_edge_pass<false, true> : cc_edge_pass<false, false>)<<<grid_for(ctx, m - done, 8), kThreads,
+                                                                                       0, s>>>(
+                    L.par, L.u + done, L.v + done, m - done, n, L.err);
         } else {
             const int grid = grid_for(ctx, (m + 3) / 4, 8);
-            if (L.vec) cc_edge_pass<true><<<grid, kThreads, 0, s>>>(L.par, L.u, L.v, m);
-            else cc_edge_pass<false><<<grid, kThreads, 0, s>>>(L.par, L.u, L.v, m);
+            auto pass = L.vec ? (L.check ? cc_edge_pass<true, true> : cc_edge_pass<true, false>)
+                              : (L.check ? cc_edge_pass<false, true> : cc_edge_pass<false, false>);
+            pass<<<grid, kThreads, 0, s>>>(L.par, L.u, L.v, m, n, L.err);
             CAC_TRY(record(ctx, 4, capturing));
         }
     } else {
@@ -641,14 +672,24 @@ int cc_enqueue(cac_ctx *ctx, const CCLaunch &L, bool capturing) {
         cc_label_all<<<grid_for(ctx, n, 8), kThreads, 0, s>>>(L.par, n, L.labels);
     }
     CAC_CUDA_TRY(cudaGetLastError());
-    CAC_CUDA_TRY(cudaMemcpyAsync(ctx->pinned_u32, L.total, 4, cudaMemcpyDeviceToHost, s));
+    CAC_CUDA_TRY(cudaMemcpyAsync(ctx->pinned_u32, L.total, (kErrWord + 1) * 4, cudaMemcpyDeviceToHost, s));
     CAC_TRY(record(ctx, 3, capturing));
+    return CAC_OK;
+}
+
+// The query's error word, copied back with its count.
+int check_ids_word(cac_ctx *ctx, uint32_t n) {
+    if (ctx->pinned_u32[kErrWord] & kErrBadId) {
+        set_error("connected components: an edge endpoint is >= n = " + std::to_string(n) +
+                  " (such edges were skipped; the labels are not valid)");
+        return CAC_ERR_INVALID;
+    }
     return CAC_OK;
 }
 
 bool same_key(const CCGraphKey &a, const CCGraphKey &b) {
     return a.u == b.u && a.v == b.v && a.labels == b.labels && a.n == b.n && a.m == b.m && a.seed == b.seed &&
-           a.ranks == b.ranks && a.arena_base == b.arena_base && a.arena_cap == b.arena_cap;
+           a.ranks == b.ranks && a.arena_base == b.arena_base && a.arena_cap == b.arena_cap && a.check == b.check;
 }
 
 }  // namespace
@@ -663,7 +704,7 @@ void cc_graph_reset(cac_ctx *ctx) {
 }
 
 int cc_run(cac_ctx *ctx, uint32_t n, uint64_t m, const uint32_t *d_u, const uint32_t *d_v, uint32_t seed,
-           uint32_t ranks, uint32_t *d_labels, cac_cc_result *res) {
+           uint32_t ranks, uint32_t *d_labels, cac_cc_result *res, bool check_ids) {
     if (ranks == 0) ranks = 1;
     cudaStream_t s = ctx->stream;
     if (n == 0) {
@@ -683,6 +724,7 @@ int cc_run(cac_ctx *ctx, uint32_t n, uint64_t m, const uint32_t *d_u, const uint
     L.ntiles = (uint32_t)(((uint64_t)n + kTile - 1) / kTile);
     L.nwords = (uint32_t)(((uint64_t)n + 31) / 32);
     L.vec = ((reinterpret_cast<uintptr_t>(d_u) | reinterpret_cast<uintptr_t>(d_v)) & 15) == 0;
+    L.check = check_ids;
 
     CAC_TRY(arena_reserve(ctx, cc_scratch_bytes(n, ranks, m) + align_up(chunk_slots * 8)));
     arena_reset(ctx);
@@ -691,6 +733,7 @@ int cc_run(cac_ctx *ctx, uint32_t n, uint64_t m, const uint32_t *d_u, const uint
     L.offsets = (uint32_t *)arena_take(ctx, (size_t)L.ntiles * 4 + 4);
     L.total = (uint32_t *)arena_take(ctx, 256);
     L.giant = L.total + 8;
+    L.err = L.total + kErrWord;
     L.d_ranks = (RankDesc *)arena_take(ctx, sizeof(RankDesc) * ranks);
     L.bits = (uint32_t *)arena_take(ctx, (size_t)L.nwords * 4 + 4);
     L.region_counts = (uint32_t *)arena_take(ctx, kMaxRegions * 4);
@@ -722,13 +765,15 @@ int cc_run(cac_ctx *ctx, uint32_t n, uint64_t m, const uint32_t *d_u, const uint
     }
     L.h_ranks = hr;
     if (L.draws > 0 && m > 0) {
-        CAC_TRY(smem_optin(ctx, cc_filter<true>));
-        CAC_TRY(smem_optin(ctx, cc_filter<false>));
+        CAC_TRY(smem_optin(ctx, cc_filter<true, true>));
+        CAC_TRY(smem_optin(ctx, cc_filter<false, true>));
+        CAC_TRY(smem_optin(ctx, cc_filter<true, false>));
+        CAC_TRY(smem_optin(ctx, cc_filter<false, false>));
     }
 
     // Repeated identical queries replay a captured CUDA graph: one launch instead of a dozen
     // kernel launches and copies. The first sighting of a key runs directly; the second captures.
-    CCGraphKey key{d_u, d_v, d_labels, n, m, seed, ranks, ctx->arena.base, ctx->arena.cap};
+    CCGraphKey key{d_u, d_v, d_labels, n, m, seed, ranks, ctx->arena.base, ctx->arena.cap, check_ids};
     if (!pinned) {
         cc_graph_reset(ctx);
         CAC_TRY(cc_enqueue(ctx, L, false));
@@ -759,6 +804,7 @@ int cc_run(cac_ctx *ctx, uint32_t n, uint64_t m, const uint32_t *d_u, const uint
         CAC_TRY(cc_enqueue(ctx, L, false));
     }
     CAC_CUDA_TRY(cudaStreamSynchronize(s));
+    CAC_TRY(check_ids_word(ctx, n));
     if (res) {
         res->num_components = ctx->pinned_u32[0];
         res->rounds = (L.draws > 0 ? 1u : 0u) + (m > 0 ? 1u : 0u);  // sampling round + closing pass
@@ -837,6 +883,7 @@ int stream_enqueue(cac_ctx *ctx, const StreamLaunch &L, bool capturing) {
     const uint32_t n = L.n;
     CAC_TRY(record(ctx, 0, capturing));
     cc_init<<<grid_for(ctx, n, 8), kThreads, 0, s>>>(L.par, n);
+    CAC_CUDA_TRY(cudaMemsetAsync(L.total + kErrWord, 0, 4, s));
     // the copies start after everything already queued on the ctx stream (the staging buffers
     // may still be read by the previous query)
     cudaEvent_t *ev = ctx->chunk_ev;
@@ -871,7 +918,8 @@ int stream_enqueue(cac_ctx *ctx, const StreamLaunch &L, bool capturing) {
             // a piece of the sample (or, unfiltered, a chunk): every edge hooks, one edge per
             // thread (union walks are latency chains, so more of them run at once), then the
             // trees are flattened so the next part's walks stay one or two hops long
-            cc_edge_pass<false><<<grid_for(ctx, len, 8), kThreads, 0, s>>>(L.par, L.d_u + e0, L.d_v + e0, len);
+            cc_edge_pass<false, true><<<grid_for(ctx, len, 8), kThreads, 0, s>>>(L.par, L.d_u + e0, L.d_v + e0, len, n,
+                                                                           L.total + kErrWord);
             if (c + 1 < L.parts.size()) compress_all(ctx, L.par, n, s);
             if (L.filtered && c + 1 == kStreamPieces) {
                 cc_find_giant<<<1, kGiantSample, 0, s>>>(L.par, n, L.giant);
@@ -885,16 +933,16 @@ int stream_enqueue(cac_ctx *ctx, const StreamLaunch &L, bool capturing) {
             const uint64_t tper = (tiles + regions - 1) / regions;
             if (tiles) {
                 const size_t sm = (size_t)std::min(L.nwords, kSmemBitmapWords) * 4;
-                auto filt = L.nwords <= kSmemBitmapWords ? cc_filter<true> : cc_filter<false>;
+                auto filt = L.nwords <= kSmemBitmapWords ? cc_filter<true, true> : cc_filter<false, true>;
                 filt<<<regions, kEdgeThreads, sm, s>>>(L.d_u + e0, L.d_v + e0, tiles, L.bits, L.nwords, L.surv,
-                                                       L.region_counts);
+                                                       L.region_counts, n, L.total + kErrWord);
                 cc_hook_survivors<<<(unsigned)ctx->num_sms * 4, kThreads, 0, s>>>(L.par, L.surv, L.region_counts,
                                                                                    regions, tper * 256);
             }
             const uint64_t done = tiles * 256;
             if (done < len)
-                cc_edge_pass<false><<<grid_for(ctx, len - done, 8), kThreads, 0, s>>>(L.par, L.d_u + e0 + done,
-                                                                                     L.d_v + e0 + done, len - done);
+                cc_edge_pass<false, true><<<grid_for(ctx, len - done, 8), kThreads, 0, s>>>(
+                    L.par, L.d_u + e0 + done, L.d_v + e0 + done, len - done, n, L.total + kErrWord);
         }
     }
     if (!L.filtered) CAC_TRY(record(ctx, 1, capturing));
@@ -906,7 +954,7 @@ int stream_enqueue(cac_ctx *ctx, const StreamLaunch &L, bool capturing) {
         cc_label_all<<<grid_for(ctx, n, 8), kThreads, 0, s>>>(L.par, n, L.d_labels);
     }
     CAC_CUDA_TRY(cudaGetLastError());
-    CAC_CUDA_TRY(cudaMemcpyAsync(ctx->pinned_u32, L.total, 4, cudaMemcpyDeviceToHost, s));
+    CAC_CUDA_TRY(cudaMemcpyAsync(ctx->pinned_u32, L.total, (kErrWord + 1) * 4, cudaMemcpyDeviceToHost, s));
     CAC_TRY(record(ctx, 3, capturing));
     if (L.d_labels && L.h_labels)
         CAC_CUDA_TRY(cudaMemcpyAsync(L.h_labels, L.d_labels, (size_t)n * 4, cudaMemcpyDeviceToHost, s));
@@ -965,8 +1013,10 @@ int cc_run_streamed(cac_ctx *ctx, uint32_t n, uint64_t m, const uint32_t *h_u, c
         L.bits = (uint32_t *)arena_take(ctx, (size_t)L.nwords * 4 + 4);
         L.region_counts = (uint32_t *)arena_take(ctx, kMaxRegions * 4);
         L.surv = (uint2 *)arena_take(ctx, (max_gap + 4 * (uint64_t)kMaxRegions) * 8);
-        CAC_TRY(smem_optin(ctx, cc_filter<true>));
-        CAC_TRY(smem_optin(ctx, cc_filter<false>));
+        CAC_TRY(smem_optin(ctx, cc_filter<true, true>));
+        CAC_TRY(smem_optin(ctx, cc_filter<false, true>));
+        CAC_TRY(smem_optin(ctx, cc_filter<true, false>));
+        CAC_TRY(smem_optin(ctx, cc_filter<false, false>));
         // pinned, 16-byte aligned host arrays: the pieces are pulled by a kernel
         L.z_u = pinned_device_view(h_u);
         L.z_v = pinned_device_view(h_v);
@@ -1014,6 +1064,7 @@ int cc_run_streamed(cac_ctx *ctx, uint32_t n, uint64_t m, const uint32_t *h_u, c
         CAC_TRY(stream_enqueue(ctx, L, false));
     }
     CAC_CUDA_TRY(cudaStreamSynchronize(s));
+    CAC_TRY(check_ids_word(ctx, n));
     if (res) {
         res->num_components = ctx->pinned_u32[0];
         res->rounds = (L.filtered ? 1u : 0u) + (m > 0 ? 1u : 0u);  // sample pieces + streamed gaps
@@ -1053,6 +1104,11 @@ struct NoAllocScratch {
 };
 
 __device__ __align__(256) NoAllocScratch g_noalloc_scratch;
+
+// The component count, or 0xFFFFFFFF when an edge endpoint was >= n (the edge was skipped).
+__global__ void cc_noalloc_count(const uint32_t *total, uint32_t *out) {
+    *out = total[kErrWord] ? 0xFFFFFFFFu : total[0];
+}
 
 // Per-device set-up, done once with that device current: the device address of the scratch
 // array (its host-side name is only a stand-in) and the SM count used to size the grids.
@@ -1109,10 +1165,12 @@ extern "C" int cac_cc_noalloc(uint32_t n, uint64_t m, const uint32_t *u_dev, con
     // counters and the total are fully written before they are read.
     const uint32_t ntiles = (uint32_t)(((uint64_t)n + kTile - 1) / kTile);
     cc_init<<<grid(n), kThreads, 0, s>>>(S->parent, n);
+    CAC_CUDA_TRY(cudaMemsetAsync(S->total + kErrWord, 0, 4, s));
     if (m > 0) {
         const bool vec = ((reinterpret_cast<uintptr_t>(u_dev) | reinterpret_cast<uintptr_t>(v_dev)) & 15) == 0;
-        if (vec) cc_edge_pass<true><<<grid((m + 3) / 4), kThreads, 0, s>>>(S->parent, u_dev, v_dev, m);
-        else cc_edge_pass<false><<<grid(m), kThreads, 0, s>>>(S->parent, u_dev, v_dev, m);
+        if (vec) cc_edge_pass<true, true><<<grid((m + 3) / 4), kThreads, 0, s>>>(S->parent, u_dev, v_dev, m, n,
+                                                                                 S->total + kErrWord);
+        else cc_edge_pass<false, true><<<grid(m), kThreads, 0, s>>>(S->parent, u_dev, v_dev, m, n, S->total + kErrWord);
     }
     cc_finalize_count<<<ntiles, kThreads, 0, s>>>(S->parent, n, S->counts);
     cc_scan_tiles<<<1, 1024, 0, s>>>(S->counts, S->offsets, ntiles, S->total);
@@ -1120,8 +1178,7 @@ extern "C" int cac_cc_noalloc(uint32_t n, uint64_t m, const uint32_t *u_dev, con
         cc_rank_roots<<<ntiles, kThreads, 0, s>>>(S->parent, n, S->offsets, labels_dev);
         cc_label_all<<<grid(n), kThreads, 0, s>>>(S->parent, n, labels_dev);
     }
-    if (num_components_dev)
-        CAC_CUDA_TRY(cudaMemcpyAsync(num_components_dev, S->total, 4, cudaMemcpyDeviceToDevice, s));
+    if (num_components_dev) cc_noalloc_count<<<1, 1, 0, s>>>(S->total, num_components_dev);
     CAC_CUDA_TRY(cudaGetLastError());
     return CAC_OK;
 }

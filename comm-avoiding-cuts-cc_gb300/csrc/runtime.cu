@@ -483,7 +483,7 @@ int cac_cc_edges(cac_ctx *ctx, uint32_t n, uint64_t m, const uint32_t *u_host, c
             set_error("cac_cc_edges: upload failed");
             st = CAC_ERR_CUDA;
         }
-        if (st == CAC_OK) st = cc_run(ctx, n, m, du, dv, seed, virtual_ranks, labels_host ? dl : nullptr, &r);
+        if (st == CAC_OK) st = cc_run(ctx, n, m, du, dv, seed, virtual_ranks, labels_host ? dl : nullptr, &r, true);
     } else {
         st = cc_run_streamed(ctx, n, m, u_host, v_host, du, dv, labels_host ? dl : nullptr, labels_host, &r);
         streamed = true;

@@ -117,7 +117,9 @@ int cac_cc(cac_ctx *ctx, const cac_graph *g, uint32_t seed, uint32_t virtual_ran
  * (n^1.045 * 1.2 edges) cross first and are hooked (res->sampled_edges = their size), then the
  * gaps between them stream through the giant-component filter as they land. Pinned host arrays
  * are faster (the pieces are pulled by a kernel while the gaps are copied); a repeated call with
- * the same arrays replays one captured CUDA graph. The labels are the same either way. */
+ * the same arrays replays one captured CUDA graph. The labels are the same either way. The edge
+ * arrays are not validated beforehand: an endpoint >= n is skipped by the kernels and the call
+ * returns CAC_ERR_INVALID. */
 int cac_cc_edges(cac_ctx *ctx, uint32_t n, uint64_t m, const uint32_t *u_host, const uint32_t *v_host,
                  uint32_t seed, uint32_t virtual_ranks, uint32_t *labels_host, cac_cc_result *res);
 
@@ -130,7 +132,9 @@ int cac_cc_edges(cac_ctx *ctx, uint32_t n, uint64_t m, const uint32_t *u_host, c
  * such limit). No ctx is needed: the work is enqueued on `stream` (a cudaStream_t of the current
  * device, NULL for the default stream) and the call returns without synchronising.
  * labels_dev (nullable) gets the same labels as cac_cc; num_components_dev (nullable, device)
- * gets the component count. The first call on a device resolves the array's device address
+ * gets the component count, or 0xFFFFFFFF when an edge endpoint was >= n (such edges are skipped:
+ * the edge arrays are not validated beforehand, every endpoint is checked before it is used and
+ * the labels are then not valid). The first call on a device resolves the array's device address
  * (make that first call before any stream capture). All calls share the one array: calls whose
  * work overlaps on the GPU (other streams, other host threads) race and must be serialised by
  * the caller. */

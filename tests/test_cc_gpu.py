@@ -192,3 +192,31 @@ def test_full_size_rmat_scale_20(ctx):
     count, lab, _ = g.connected_components(seed=1)
     assert count == want_count
     assert np.array_equal(lab, want)
+
+
+@pytest.mark.parametrize("m_kind", ["copied", "streamed"])
+def test_host_edges_with_an_endpoint_out_of_range(ctx, libcac, m_kind):
+    # cac_cc_edges takes raw host arrays: an endpoint >= n is skipped by the kernels (every
+    # endpoint is checked before it indexes) and the call fails with CAC_ERR_INVALID; the ctx
+    # stays usable
+    if m_kind == "copied":
+        n, u, v, _ = graphgen.erdos_renyi_m(20000, 8.0, 11)
+    else:
+        n, u, v, _ = graphgen.erdos_renyi_m(400000, 12.0, 12)
+        assert len(u) > (2 << 20)
+    bad = v.copy()
+    bad[len(bad) // 3] = 0xFFFFFFF0
+    with pytest.raises(libcac.CacError) as e:
+        ctx.cc_edges(n, u, bad)
+    assert e.value.status == -1 and "endpoint" in str(e.value)
+    want_count, want = O.cc_labels(n, u, v)
+    lab = np.zeros(n, np.uint32)
+    assert ctx.cc_edges(n, u, v, labels=lab).num_components == want_count
+    assert np.array_equal(lab, want)
+
+
+def test_graph_with_an_endpoint_out_of_range_is_refused(ctx, libcac):
+    with pytest.raises(libcac.CacError) as e:
+        ctx.graph(10, np.array([0, 3], np.uint32), np.array([1, 10], np.uint32))
+    assert e.value.status == -1
+    assert ctx.graph(10, np.array([0, 3], np.uint32), np.array([1, 9], np.uint32)).connected_components()[0] == 8

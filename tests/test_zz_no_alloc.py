@@ -49,3 +49,17 @@ def test_refuses_more_vertices_than_the_scratch_holds(libcac):
     st = lib.cac_cc_noalloc((1 << 22) + 1, 0, None, None, None, None, None)
     assert st == -1
     assert b"4194304" in lib.cac_last_error()
+
+
+def test_endpoint_out_of_range_is_reported_in_the_count(ctx, libcac):
+    # an endpoint >= n: the edge is skipped (the kernels check every endpoint before indexing)
+    # and the count reads 0xFFFFFFFF; the next valid call is unaffected
+    torch = pytest.importorskip("torch")
+    n, u, v, _ = graphgen.erdos_renyi(5000, 0.002, 6)
+    bad_v = v.copy()
+    bad_v[17] = n + 3
+    count, _ = _noalloc(libcac, torch, n, u, bad_v)
+    assert count & 0xFFFFFFFF == 0xFFFFFFFF
+    count, labels = _noalloc(libcac, torch, n, u, v)
+    want_count, want = O.cc_labels(n, u, v)
+    assert count == want_count and np.array_equal(labels, want)
