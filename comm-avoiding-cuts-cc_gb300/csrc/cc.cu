@@ -194,35 +194,33 @@ __global__ void cc_compress4(uint32_t *par, uint32_t n4) {
 void compress_all(cac_ctx *ctx, uint32_t *par, uint32_t n, cudaStream_t s);
 
 // The most frequent root among kGiantSample vertices spread over [0, n) (compressed parents):
-// one CTA bitonic-sorts the sampled roots in shared memory; every run start measures its run by
-// binary search and a block argmax picks the longest (ties: the smaller root).
+// every warp finds the mode of its 32 samples (__match_any_sync groups equal roots; ties to the
+// smaller root), each of those 32 candidates is counted over all samples with shared atomics, and
+// the candidate with the largest count wins (ties: the smaller root). The giant component is the
+// mode of most warps whenever it holds a sizeable share of the vertices; the choice only decides
+// which edges the filter can drop, never the labels.
 __global__ void __launch_bounds__(kGiantSample) cc_find_giant(const uint32_t *par, uint32_t n, uint32_t *giant) {
-    __shared__ uint32_t r[kGiantSample];
+    __shared__ uint32_t cand[kGiantSample / 32], cnt[kGiantSample / 32];
     __shared__ unsigned long long best;
-    const uint32_t i = threadIdx.x;
-    r[i] = par[((uint64_t)i * 2654435761u) % n];  // fixed spread of sample positions
+    const uint32_t i = threadIdx.x, lane = i & 31, w = i >> 5;
+    const uint32_t r = par[((uint64_t)i * 2654435761u) % n];  // fixed spread of sample positions
+    const uint32_t same = __match_any_sync(0xffffffffu, r);
+    // warp argmax of (count, -root) in two 32-bit reductions
+    const uint32_t c = __popc(same);
+    const uint32_t top = __reduce_max_sync(0xffffffffu, c);
+    const uint32_t lo = __reduce_max_sync(0xffffffffu, c == top ? 0xFFFFFFFFu - r : 0u);
+    if (lane == 0) {
+        cand[w] = 0xFFFFFFFFu - lo;
+        cnt[w] = 0;
+    }
     if (i == 0) best = 0;
     __syncthreads();
-    for (uint32_t k = 2; k <= kGiantSample; k <<= 1) {
-        for (uint32_t j = k >> 1; j > 0; j >>= 1) {
-            const uint32_t p = i ^ j;
-            if (p > i) {
-                const bool up = (i & k) == 0;
-                const uint32_t a = r[i], b = r[p];
-                if ((a > b) == up) { r[i] = b; r[p] = a; }
-            }
-            __syncthreads();
-        }
-    }
-    if (i == 0 || r[i] != r[i - 1]) {
-        uint32_t lo = i, hi = kGiantSample;  // first position with a larger root
-        while (lo < hi) {
-            const uint32_t mid = (lo + hi) >> 1;
-            if (r[mid] > r[i]) hi = mid; else lo = mid + 1;
-        }
-        const unsigned long long key = ((unsigned long long)(lo - i) << 32) | (0xFFFFFFFFu - r[i]);
-        atomicMax(&best, key);
-    }
+#pragma unroll 8
+    for (uint32_t k = 0; k < kGiantSample / 32; k++)
+        if (r == cand[k]) atomicAdd(&cnt[k], 1u);
+    __syncthreads();
+    if (i < kGiantSample / 32)
+        atomicMax(&best, ((unsigned long long)cnt[i] << 32) | (0xFFFFFFFFu - cand[i]));
     __syncthreads();
     if (i == 0) *giant = 0xFFFFFFFFu - (uint32_t)(best & 0xFFFFFFFFu);
 }
