@@ -103,6 +103,8 @@ EXPORTS = [
     ("cac_graph_copy_edges", ctypes.c_int, [_vp, _vp, _vp, _vp, ctypes.c_int]),
     ("cac_parse_file", ctypes.c_int, [ctypes.c_char_p, _u32p, _u64p, _vp, _vp, _vp, ctypes.c_uint64]),
     ("cac_parse_header", ctypes.c_int, [ctypes.c_char_p, _u32p, _u64p]),
+    ("cac_cache_write", ctypes.c_int, [ctypes.c_char_p, ctypes.c_uint32, ctypes.c_uint64, _vp, _vp, _vp]),
+    ("cac_cache_convert", ctypes.c_int, [ctypes.c_char_p, ctypes.c_char_p]),
     ("cac_cc", ctypes.c_int, [_vp, _vp, ctypes.c_uint32, ctypes.c_uint32, _vp, ctypes.c_int,
                               ctypes.POINTER(CCResult)]),
     ("cac_cc_edges", ctypes.c_int, [_vp, ctypes.c_uint32, ctypes.c_uint64, _vp, _vp, ctypes.c_uint32,
@@ -457,3 +459,20 @@ def parse_file(path):
            "cac_parse_file")
     k = int(m.value)
     return int(n.value), u[:k], v[:k], w[:k]
+
+
+def cache_write(path, n, u, v, w=None):
+    """Binary cache of an edge list (host arrays; w None: unweighted, read back as weights 1)."""
+    u = np.ascontiguousarray(u, dtype=np.uint32)
+    v = np.ascontiguousarray(v, dtype=np.uint32)
+    pw = None
+    if w is not None:
+        w = np.ascontiguousarray(w, dtype=np.uint32)
+        pw = ctypes.c_void_p(w.ctypes.data)
+    _check(lib().cac_cache_write(path.encode(), n, len(u), ctypes.c_void_p(u.ctypes.data),
+                                 ctypes.c_void_p(v.ctypes.data), pw), "cac_cache_write")
+
+
+def cache_convert(input_path, cache_path):
+    """Parses a text edge list and writes its binary cache."""
+    _check(lib().cac_cache_convert(input_path.encode(), cache_path.encode()), "cac_cache_convert")

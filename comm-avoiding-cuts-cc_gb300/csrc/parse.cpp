@@ -7,6 +7,11 @@
 // The triples are parsed by all host threads at once: the body is split into chunks at
 // whitespace, a first pass counts the tokens of every chunk, and the second pass converts
 // each chunk straight into the caller's arrays at its token offset.
+//
+// Binary cache: a parsed edge list can be written once and read back without parsing. Layout
+// (little-endian): "CACG", u32 version (1), u32 n, u32 flags (bit 0: weights stored), u64 m,
+// u64 total weight, then u[m], v[m] and, with bit 0, w[m] as u32 (weights 1 otherwise). The
+// readers below recognise the magic, so every loader and command line accepts either form.
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -73,6 +78,93 @@ inline bool parse_u32(const char *&p, const char *end, uint32_t &out) {
 }
 
 // Positions just past the header: skip line 1, then read n and m.
+constexpr char kCacheMagic[4] = {'C', 'A', 'C', 'G'};
+constexpr uint32_t kCacheVersion = 1;
+constexpr size_t kCacheHeader = 32;
+
+struct CacheHeader {
+    uint32_t n = 0, flags = 0;
+    uint64_t m = 0, total = 0;
+};
+
+uint32_t get_u32(const unsigned char *p) {
+    return (uint32_t)p[0] | (uint32_t)p[1] << 8 | (uint32_t)p[2] << 16 | (uint32_t)p[3] << 24;
+}
+uint64_t get_u64(const unsigned char *p) { return (uint64_t)get_u32(p) | (uint64_t)get_u32(p + 4) << 32; }
+void put_u32(unsigned char *p, uint32_t x) {
+    for (int i = 0; i < 4; i++) p[i] = (unsigned char)(x >> (8 * i));
+}
+void put_u64(unsigned char *p, uint64_t x) {
+    put_u32(p, (uint32_t)x);
+    put_u32(p + 4, (uint32_t)(x >> 32));
+}
+bool host_little_endian() {
+    const uint32_t one = 1;
+    unsigned char c;
+    std::memcpy(&c, &one, 1);
+    return c == 1;
+}
+
+// 1: the file is a cache (header read into h), 0: not a cache, <0: error
+int read_cache_header(FILE *f, const char *path, CacheHeader &h) {
+    unsigned char hd[kCacheHeader];
+    const size_t got = std::fread(hd, 1, kCacheHeader, f);
+    // the magic and a binary version word: a text file whose (skipped) first line starts with the
+    // magic still reads as text
+    if (got < 8 || std::memcmp(hd, kCacheMagic, 4) != 0 || get_u32(hd + 4) != kCacheVersion) return 0;
+    if (got < kCacheHeader) {
+        set_error(std::string("truncated graph cache header in ") + path);
+        return CAC_ERR_PARSE;
+    }
+    h.n = get_u32(hd + 8);
+    h.flags = get_u32(hd + 12);
+    h.m = get_u64(hd + 16);
+    h.total = get_u64(hd + 24);
+    return 1;
+}
+
+// Reads a cache's arrays (after its header) into the caller's arrays, checks its length, its
+// endpoints and its total weight.
+int read_cache_body(FILE *f, const char *path, const CacheHeader &h, uint32_t *u, uint32_t *v, uint32_t *w) {
+    const uint64_t m = h.m;
+    auto read_u32s = [&](uint32_t *dst) -> bool {
+        if (m == 0) return true;
+        if (std::fread(dst, 4, (size_t)m, f) != (size_t)m) return false;
+        if (!host_little_endian())
+            for (uint64_t i = 0; i < m; i++) dst[i] = get_u32(reinterpret_cast<const unsigned char *>(dst + i));
+        return true;
+    };
+    std::vector<uint32_t> wtmp;
+    uint32_t *wd = w;
+    if ((h.flags & 1u) && !wd) {
+        wtmp.resize(m ? m : 1);
+        wd = wtmp.data();
+    }
+    if (!read_u32s(u) || !read_u32s(v) || ((h.flags & 1u) && !read_u32s(wd))) {
+        set_error(std::string("truncated graph cache ") + path);
+        return CAC_ERR_PARSE;
+    }
+    if (std::fgetc(f) != EOF) {
+        set_error(std::string("graph cache ") + path + " is longer than its header declares");
+        return CAC_ERR_PARSE;
+    }
+    if (!(h.flags & 1u) && w)
+        for (uint64_t i = 0; i < m; i++) w[i] = 1;
+    uint64_t total = 0;
+    for (uint64_t e = 0; e < m; e++) {
+        if (u[e] >= h.n || v[e] >= h.n) {
+            set_error("edge " + std::to_string(e) + " has an endpoint >= n = " + std::to_string(h.n));
+            return CAC_ERR_PARSE;
+        }
+        total += (h.flags & 1u) ? wd[e] : 1u;
+    }
+    if (total != h.total) {
+        set_error(std::string("graph cache ") + path + ": total weight does not match its header");
+        return CAC_ERR_PARSE;
+    }
+    return CAC_OK;
+}
+
 int parse_header_buf(const char *b, const char *end, uint32_t *n, uint64_t *m, const char **body) {
     const char *p = (const char *)std::memchr(b, '\n', (size_t)(end - b));
     if (!p) {
@@ -105,6 +197,18 @@ int cac_parse_header(const char *path, uint32_t *n, uint64_t *m) {
     if (!path || !n || !m) { set_error("cac_parse_header: invalid argument"); return CAC_ERR_INVALID; }
     FILE *f = std::fopen(path, "rb");
     if (!f) { set_error(std::string("cannot open ") + path); return CAC_ERR_IO; }
+    {
+        CacheHeader h;
+        const int c = read_cache_header(f, path, h);
+        if (c != 0) {
+            std::fclose(f);
+            if (c < 0) return c;
+            *n = h.n;
+            *m = h.m;
+            return CAC_OK;
+        }
+        std::rewind(f);
+    }
     std::vector<char> head(1 << 16);
     size_t got = std::fread(head.data(), 1, head.size(), f);
     // the first line may be long: keep reading until the counts are in the buffer
@@ -122,6 +226,29 @@ int cac_parse_header(const char *path, uint32_t *n, uint64_t *m) {
 int cac_parse_file(const char *path, uint32_t *n, uint64_t *m, uint32_t *u, uint32_t *v, uint32_t *w,
                    uint64_t capacity) {
     if (!path || !n || !m) { set_error("cac_parse_file: invalid argument"); return CAC_ERR_INVALID; }
+    {
+        FILE *f = std::fopen(path, "rb");
+        if (!f) { set_error(std::string("cannot open ") + path); return CAC_ERR_IO; }
+        CacheHeader h;
+        const int c = read_cache_header(f, path, h);
+        if (c != 0) {
+            int st = c < 0 ? c : CAC_OK;
+            if (st == CAC_OK) {
+                *n = h.n;
+                *m = h.m;
+                if (h.m > capacity || (h.m && (!u || !v))) {
+                    set_error("cac_parse_file: output capacity " + std::to_string(capacity) + " < edge count " +
+                              std::to_string(h.m));
+                    st = CAC_ERR_INVALID;
+                } else {
+                    st = read_cache_body(f, path, h, u, v, w);
+                }
+            }
+            std::fclose(f);
+            return st;
+        }
+        std::fclose(f);
+    }
     FileBuf fb;
     CAC_TRY(read_all(path, fb));
     const char *b = fb.data.data(), *end = b + fb.data.size();
@@ -199,6 +326,57 @@ int cac_parse_file(const char *path, uint32_t *n, uint64_t *m, uint32_t *u, uint
         }
     }
     return CAC_OK;
+}
+
+int cac_cache_write(const char *path, uint32_t n, uint64_t m, const uint32_t *u, const uint32_t *v, const uint32_t *w) {
+    if (!path || (m && (!u || !v))) { set_error("cac_cache_write: invalid argument"); return CAC_ERR_INVALID; }
+    uint64_t total = 0;
+    for (uint64_t e = 0; e < m; e++) {
+        if (u[e] >= n || v[e] >= n) {
+            set_error("cac_cache_write: edge " + std::to_string(e) + " has an endpoint >= n = " + std::to_string(n));
+            return CAC_ERR_INVALID;
+        }
+        total += w ? w[e] : 1u;
+    }
+    unsigned char hd[kCacheHeader] = {};
+    std::memcpy(hd, kCacheMagic, 4);
+    put_u32(hd + 4, kCacheVersion);
+    put_u32(hd + 8, n);
+    put_u32(hd + 12, w ? 1u : 0u);
+    put_u64(hd + 16, m);
+    put_u64(hd + 24, total);
+    FILE *f = std::fopen(path, "wb");
+    if (!f) { set_error(std::string("cannot create ") + path); return CAC_ERR_IO; }
+    bool ok = std::fwrite(hd, 1, kCacheHeader, f) == kCacheHeader;
+    auto write_u32s = [&](const uint32_t *src) {
+        if (!ok || m == 0) return;
+        if (host_little_endian()) {
+            ok = std::fwrite(src, 4, (size_t)m, f) == (size_t)m;
+            return;
+        }
+        std::vector<unsigned char> tmp(4 * (size_t)std::min<uint64_t>(m, 1 << 20));
+        for (uint64_t e0 = 0; e0 < m && ok; e0 += tmp.size() / 4) {
+            const uint64_t k = std::min<uint64_t>(m - e0, tmp.size() / 4);
+            for (uint64_t i = 0; i < k; i++) put_u32(tmp.data() + 4 * i, src[e0 + i]);
+            ok = std::fwrite(tmp.data(), 4, (size_t)k, f) == (size_t)k;
+        }
+    };
+    write_u32s(u);
+    write_u32s(v);
+    if (w) write_u32s(w);
+    ok = (std::fclose(f) == 0) && ok;
+    if (!ok) { set_error(std::string("writing ") + path + " failed"); return CAC_ERR_IO; }
+    return CAC_OK;
+}
+
+int cac_cache_convert(const char *input_path, const char *cache_path) {
+    if (!input_path || !cache_path) { set_error("cac_cache_convert: invalid argument"); return CAC_ERR_INVALID; }
+    uint32_t n;
+    uint64_t m;
+    CAC_TRY(cac_parse_header(input_path, &n, &m));
+    std::vector<uint32_t> u(m ? m : 1), v(m ? m : 1), w(m ? m : 1);
+    CAC_TRY(cac_parse_file(input_path, &n, &m, u.data(), v.data(), w.data(), m));
+    return cac_cache_write(cache_path, n, m, u.data(), v.data(), w.data());
 }
 
 int cac_graph_load_file(cac_ctx *ctx, const char *path, cac_graph **out) {

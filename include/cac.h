@@ -23,6 +23,8 @@
  *   cac_approx_cut        ApproximateCut::run (src/ApproximateCut.hpp:62, .cpp:10-79), driven as in
  *                         src/executables/approx_cut.cpp:17-38
  *   cac_sitmo_blocks      sitmo::prng_engine block function (lib/prng_engine.hpp:307-343)
+ *   cac_karger_stein      comincut::minimum_cut as src/executables/karger_stein.cpp:34 calls it
+ *   cac_cache_write/_convert  a binary form of the edge-list file (no reference counterpart)
  *
  * Conventions
  *   - Every function returns an int status: CAC_OK (0) or a negative CAC_ERR_* code. The
@@ -92,6 +94,17 @@ int cac_parse_file(const char *path, uint32_t *n, uint64_t *m, uint32_t *u_host,
                    uint32_t *w_host, uint64_t capacity);
 /* Read only the header (vertex and edge counts) of an edge-list file. */
 int cac_parse_header(const char *path, uint32_t *n, uint64_t *m);
+
+/* Binary graph cache: parse a text input once, load it later without parsing (it has no
+ * counterpart in the reference). The edge list of a text input is written once; every loader above (cac_graph_load_file, cac_parse_header,
+ * cac_parse_file) and every command line accepts the cache file in place of the text file (it is
+ * recognised by its magic). Layout, little-endian: "CACG", u32 version 1, u32 n, u32 flags (bit 0:
+ * weights stored), u64 m, u64 total weight, then u[m], v[m] and (bit 0) w[m] as u32. Reading
+ * checks the length, every endpoint < n and the total weight (CAC_ERR_PARSE otherwise). No GPU
+ * is needed for either call. w (nullable) writes an unweighted cache (weights read back as 1). */
+int cac_cache_write(const char *path, uint32_t n, uint64_t m, const uint32_t *u, const uint32_t *v, const uint32_t *w);
+/* Parses a text edge list (all host threads) and writes its cache. */
+int cac_cache_convert(const char *input_path, const char *cache_path);
 
 /* ---- connected components (parallel_cc) ---- */
 typedef struct {

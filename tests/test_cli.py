@@ -143,3 +143,18 @@ def test_seq_square_root_csv(golden, tmp_path):
     # the same trials and answer as square_root on one virtual rank
     one = _run("square_root", "0.95", path, "3", env={"CAC_VIRTUAL_RANKS": "1"}).stdout.strip().split(",")
     assert one[7] == f[7] and one[9] == f[9]
+
+
+@pytest.mark.gpu
+def test_command_lines_read_the_binary_cache(golden, tmp_path, libcac):
+    # the same answers from the text file and from its cache
+    spec = golden("mincut_seeded.json")[0]
+    n, u, v, w = make_graph(spec)
+    text = _write(tmp_path, "g.in", n, u, v, w)
+    cache = str(tmp_path / "g.cacg")
+    libcac.cache_convert(text, cache)
+    for name, args in (("square_root", ["0.95"]), ("approx_cut", ["0.9"]), ("parallel_cc", [])):
+        a = _run(name, *args, text, "1").stdout.strip().split(",")
+        b = _run(name, *args, cache, "1").stdout.strip().split(",")
+        assert a and b and a[3:5] == b[3:5] and a[-1] == b[-1], (name, a, b)
+    assert int(_run("square_root", "0.95", cache, "0").stdout.strip().split(",")[-1]) == spec["exact_cut"]
