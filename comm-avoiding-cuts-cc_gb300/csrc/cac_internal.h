@@ -89,6 +89,7 @@ struct cac_ctx {
     cudaGraphExec_t cc_exec = nullptr;  // its captured launch sequence (second sighting onwards)
     uint32_t *pinned_u32 = nullptr;  // 64 KB pinned staging: [0,256) B scalar results, then descriptors
     void *ks_scratch = nullptr;      // grow-only Karger-Stein scratch buffers (mincut.cu)
+    uint8_t quotient_choice[32] = {};  // autotuned quotient kernel per (N bucket, width); 0: untuned
     cudaStream_t copy_stream = nullptr;  // host-to-device chunks of cac_cc_edges (created on first use)
     cudaEvent_t chunk_ev[40] = {};       // start + one per piece and gap copy in flight
 };
@@ -225,6 +226,14 @@ int mincut_admit_query(cac_ctx *ctx, KsEngine &eng, const MincutQuery &q, uint32
 uint64_t shrink_big_scratch(uint32_t n, uint64_t m, uint32_t B);
 int shrink_big(cac_ctx *ctx, const cac_graph *g, uint32_t target, uint32_t B, const uint32_t *k0, const uint32_t *idx,
                uint32_t *d_lab, uint32_t *d_kout, void *scratch);
+// Quotient kernel choices of the autotuner (cac_ctx::quotient_choice), bucketed by
+// floor(log2 N) and entry width.
+constexpr uint8_t kQuotientWarp = 1, kQuotientShared = 2;
+inline int quotient_bucket(uint32_t N, bool small) {
+    int b = 0;
+    while ((N >> (b + 1)) != 0 && b < 15) b++;
+    return 2 * b + (small ? 1 : 0);
+}
 // Frees the ctx's grow-only Karger-Stein scratch (cac_ctx_destroy).
 void ctx_scratch_free(cac_ctx *ctx);
 // All trials of all queries through one engine, admitted as memory allows.

@@ -17,8 +17,11 @@
 //                                column by block prefix + a 32-entry scan), contraction in draw
 //                                order until max(ceil(n/sqrt 2)+1, 128) vertices, labels by rank
 //                                of the smallest member, member lists by counting sort
-//              quotient_kernel   one CTA per output row: member rows summed by column label in
-//                                shared memory (u64 shared atomics), one coalesced row store
+//              quotient_warp_kernel / quotient_shared_row_kernel
+//                                the child's matrix: member rows summed, every column added into
+//                                its label's slot of the output row in shared memory (integer
+//                                atomics); a warp per output row, or a CTA's 8 warps on one row at
+//                                large N (autotuned per size bucket)
 //              sw_leaf_kernel    one warp per leaf (n <= 128): Stoer-Wagner maximum-adjacency
 //                                phases with Nagamochi-Ono-Ibaraki contractions on the matrix held
 //                                in shared memory (circulant half storage); atomicMin into the
@@ -37,11 +40,11 @@
 namespace cac {
 namespace {
 
-constexpr uint32_t kSharedRowMinN = 2000;  // quotient steps from this N on use the shared-row kernel
+constexpr uint32_t kSharedRowMinN = 2000;  // before tuning: quotient steps from this N on use the shared-row kernel
+constexpr uint32_t kSharedRows = 8;         // output rows per CTA of the shared-row quotient
 constexpr uint32_t kMaxSmemVertices = kMaxDenseVertices;  // union-find of a contraction held in shared memory
 constexpr int kBatch = 1024;                  // draws gathered before the ordered contraction
 constexpr int kNT = 512;                      // threads of the per-trial / per-task CTAs
-constexpr int kQT = 256;                      // threads of the quotient CTAs
 constexpr uint32_t kDropped = 0xFFFFFFFFu;    // task whose source matrix has no edges left
 constexpr uint64_t kU64Max = 0xFFFFFFFFFFFFFFFFull;
 
@@ -528,57 +531,6 @@ __global__ void __launch_bounds__(NT) contract_kernel(const TaskDesc *__restrict
     if (threadIdx.x == 0) k_out[blockIdx.x] = k;
 }
 
-// One CTA per group of `rows` consecutive output rows of one child. For each row a: the sum of the
-// member rows of group a, accumulated column by column in shared memory (each thread owns its
-// columns, one pass per member row, coalesced reads); then every output column b gathers its
-// members' entries of that sum through the member lists (no atomics). The diagonal (b == a) is 0.
-template <int NT, typename Tm>
-__global__ void __launch_bounds__(NT) quotient_kernel(const TaskDesc *__restrict__ tasks,
-                                                      const SrcDesc *__restrict__ srcs,
-                                                      const uint32_t *__restrict__ kdim,
-                                                      const uint64_t *__restrict__ group_task_off, uint32_t ntasks,
-                                                      uint32_t rows, const uint64_t *__restrict__ out_off,
-                                                      unsigned char *out_base) {
-    // out_off[i]: byte offset of task i's matrix in out_base
-    extern __shared__ __align__(16) unsigned char dsm[];
-    const uint64_t gg = blockIdx.x;
-    uint32_t lo = 0, hi = ntasks - 1;
-    while (lo < hi) {  // last task whose first row group <= gg
-        const uint32_t mid = (lo + hi + 1) >> 1;
-        if (group_task_off[mid] <= gg) lo = mid; else hi = mid - 1;
-    }
-    const TaskDesc T = tasks[lo];
-    const SrcDesc S = srcs[T.src];
-    const uint32_t k = kdim[lo];
-    const uint32_t N = S.N;
-    const uint32_t a0 = (uint32_t)(gg - group_task_off[lo]) * rows, a1 = min(k, a0 + rows);
-    if (!width_is<Tm>(S.small)) return;
-    const Tm *mat = reinterpret_cast<const Tm *>(S.mat);
-    uint64_t *rowsum = reinterpret_cast<uint64_t *>(dsm);  // N entries
-    Tm *Qt = reinterpret_cast<Tm *>(out_base + out_off[lo]);
-    for (uint32_t a = a0; a < a1; a++) {
-        const uint32_t p0 = T.memb_off[a], p1 = T.memb_off[a + 1];
-        for (uint32_t p = p0; p < p1; p++) {
-            const uint64_t rb = (uint64_t)T.members[p] * ld_of(N);
-            if (p == p0) {
-                for (uint32_t j = threadIdx.x; j < N; j += NT) rowsum[j] = __ldg(mat + rb + j);
-            } else {
-                for (uint32_t j = threadIdx.x; j < N; j += NT) rowsum[j] += __ldg(mat + rb + j);
-            }
-        }
-        __syncthreads();
-        for (uint32_t b = threadIdx.x; b < k; b += NT) {
-            uint64_t acc = 0;
-            if (b != a) {
-                const uint32_t q1 = T.memb_off[b + 1];
-                for (uint32_t q = T.memb_off[b]; q < q1; q++) acc += rowsum[T.members[q]];
-            }
-            Qt[(uint64_t)a * ld_of(k) + b] = (Tm)acc;
-        }
-        __syncthreads();
-    }
-}
-
 __device__ __forceinline__ void sadd(uint32_t *p, uint64_t v) { atomicAdd(p, (uint32_t)v); }
 __device__ __forceinline__ void sadd(uint64_t *p, uint64_t v) {
     atomicAdd(reinterpret_cast<unsigned long long *>(p), (unsigned long long)v);
@@ -1034,7 +986,6 @@ int upload(cac_ctx *ctx, DevBuf &buf, const std::vector<T> &v) {
 
 size_t leaf_smem(uint32_t N, bool small) { return (size_t)N * (N / 2) * (small ? 4 : 8); }
 size_t contract_smem(uint32_t N) { return kBatch * sizeof(uint2) + kCoarseRows * sizeof(uint64_t) + (size_t)2 * N * 4; }
-size_t quotient_smem(uint32_t N) { return (size_t)N * 8; }
 
 }  // namespace
 
@@ -1290,59 +1241,56 @@ int KsEngine::step() {
     CAC_CUDA_TRY(cudaMemcpyAsync(kk.data(), d_kout.p, tasks.size() * 4, cudaMemcpyDeviceToHost, s));
     CAC_CUDA_TRY(cudaStreamSynchronize(s));
 
-    // quotient matrices of this step, in one stream-ordered buffer
-    std::vector<uint64_t> out_off(tasks.size(), 0), group_task_off(tasks.size(), 0);
+    // quotient matrices of this step, in one stream-ordered buffer: each child's matrix, then
+    // (after all matrices) each child's row sums and 32-column block prefixes, which the quotient
+    // kernels write for the next step's draws
+    std::vector<uint64_t> out_off(2 * tasks.size(), 0);
     std::vector<uint32_t> kq(tasks.size(), 0);
-    uint64_t out_bytes = 0, groups = 0;
-    size_t qsm = 0;
-    const uint32_t qrows = std::max<uint32_t>(1, std::min<uint32_t>(16, 4096 / std::max<uint32_t>(maxN, 1)));
+    uint64_t out_bytes = 0;
+    bool all_small = true;
+    uint32_t kmax = 0;
     for (size_t i = 0; i < tasks.size(); i++) {
         const uint32_t k = kk[i] == kDropped ? 0 : kk[i];
         kq[i] = k;
         out_off[i] = out_bytes;
-        group_task_off[i] = groups;
         out_bytes += ((uint64_t)k * ld_of(k) * (tasks[i].src.small ? 4 : 8) + 15) / 16 * 16;
-        groups += (k + qrows - 1) / qrows;
-        if (k) qsm = std::max(qsm, quotient_smem(tasks[i].src.N));
-    }
-    // warp-per-row quotient with 8 (or 4) warps where three or more of its CTAs fit on an SM
-    // (labels + one k-entry row per warp within 80 KB), else the CTA-per-row-group kernel, whose
-    // 256 threads share one row and keep the SM occupied at large N; large steps take the
-    // shared-row kernel
-    const size_t stage_words = ((size_t)maxN + 3) & ~(size_t)3;  // N u32 labels, 16-byte rounded
-    bool all_small = true;
-    uint32_t kmax = 0;
-    for (size_t i = 0; i < tasks.size(); i++) {
         all_small = all_small && tasks[i].src.small;
-        kmax = std::max(kmax, kq[i]);
+        kmax = std::max(kmax, k);
     }
+    for (size_t i = 0; i < tasks.size(); i++) {
+        out_off[tasks.size() + i] = out_bytes;
+        out_bytes += ((kq[i] + (uint64_t)kq[i] * ((kq[i] + 31) / 32)) * 8 + 15) / 16 * 16;
+    }
+    // Two quotient kernels, identical outputs: warp-per-row (8 or 4 warps, one k-entry row per warp
+    // in shared memory; where three of its CTAs fit an SM: labels + rows within 80 KB) and
+    // shared-row (8 warps on one output row). Which is faster depends on N, k and the task count,
+    // so the step autotunes: the first sizeable step of each (power-of-two bucket of N, entry
+    // width) on this ctx times both on its own data and keeps the faster; smaller steps before
+    // that use the rule measured on GB300 (shared-row from N = 2000 on).
+    const size_t stage_words = ((size_t)maxN + 3) & ~(size_t)3;  // N u32 labels, 16-byte rounded
     const size_t rs_bytes = all_small ? 4 : 8;
-    // from N = 2000 on, the shared-row kernel (8 warps on one output row): K4000 14.5 vs 15.2-15.8
-    // ms per query; from N = 500 or 1000 on it slows the 256-graph batch (by 41% and 9%)
-    const bool shared_row = maxN >= kSharedRowMinN;
-    const uint32_t qwarps = shared_row ? 8u
-                            : stage_words * 4 + 8 * rs_bytes * (size_t)kmax <= 80 * 1024   ? 8u
+    const uint32_t qwarps = stage_words * 4 + 8 * rs_bytes * (size_t)kmax <= 80 * 1024   ? 8u
                             : stage_words * 4 + 4 * rs_bytes * (size_t)kmax <= 80 * 1024 ? 4u
                                                                                          : 0u;
-    const uint32_t wrows = shared_row ? 8u : qwarps * 4;
-    if (qwarps) {
-        groups = 0;
-        // after the matrices: each child's row sums and block prefixes, written by the warp kernel
-        out_off.resize(2 * tasks.size());
+    auto group_offsets = [&](uint32_t rows, std::vector<uint64_t> &gto) {
+        gto.assign(tasks.size(), 0);
+        uint64_t g = 0;
         for (size_t i = 0; i < tasks.size(); i++) {
-            group_task_off[i] = groups;
-            groups += (kq[i] + wrows - 1) / wrows;
-            out_off[tasks.size() + i] = out_bytes;
-            out_bytes += ((kq[i] + (uint64_t)kq[i] * ((kq[i] + 31) / 32)) * 8 + 15) / 16 * 16;
+            gto[i] = g;
+            g += (kq[i] + rows - 1) / rows;
         }
-    }
+        return g;
+    };
+    std::vector<uint64_t> gto_warp, gto_shared;
+    const uint64_t groups_warp = qwarps ? group_offsets(qwarps * 4, gto_warp) : 0;
+    const uint64_t groups_shared = group_offsets(kSharedRows, gto_shared);
     MatBuf *out = nullptr;
-    if (groups) {
+    if (groups_shared) {
         CAC_TRY(alloc(out_bytes, &out));
         CAC_TRY(upload(ctx_, d_qoff, out_off));
-        CAC_TRY(upload(ctx_, d_gto, group_task_off));
         CAC_CUDA_TRY(cudaMemcpyAsync(d_kout.p, kq.data(), tasks.size() * 4, cudaMemcpyHostToDevice, s));
-        if (shared_row) {
+        auto launch_shared = [&]() -> int {
+            CAC_TRY(upload(ctx_, d_gto, gto_shared));
             const size_t ssm = stage_words * 4 + (((size_t)kmax * rs_bytes + 15) & ~(size_t)15) +
                                ((size_t)kmax / 32 + 1) * 8;
             std::vector<decltype(&quotient_shared_row_kernel<uint32_t, uint32_t>)> kerns;
@@ -1353,12 +1301,16 @@ int KsEngine::step() {
             }
             for (auto kern : kerns) {
                 CAC_TRY(smem_optin(ctx_, kern));
-                kern<<<(unsigned)groups, 256, ssm, s>>>(
+                kern<<<(unsigned)groups_shared, 256, ssm, s>>>(
                     d_task.as<TaskDesc>(), d_src.as<SrcDesc>(), d_kout.as<uint32_t>(), d_gto.as<uint64_t>(),
-                    (uint32_t)tasks.size(), wrows, d_qoff.as<uint64_t>(), static_cast<unsigned char *>(out->p),
+                    (uint32_t)tasks.size(), kSharedRows, d_qoff.as<uint64_t>(), static_cast<unsigned char *>(out->p),
                     (uint32_t)stage_words, kmax);
             }
-        } else if (qwarps) {
+            CAC_CUDA_TRY(cudaGetLastError());
+            return CAC_OK;
+        };
+        auto launch_warp = [&]() -> int {
+            CAC_TRY(upload(ctx_, d_gto, gto_warp));
             // shared rows are u32 only when every task's sums fit (all sources small)
             const size_t wsm = stage_words * 4 + (size_t)qwarps * kmax * rs_bytes;
             std::vector<decltype(&quotient_warp_kernel<uint32_t, uint32_t>)> kerns;
@@ -1369,23 +1321,38 @@ int KsEngine::step() {
             }
             for (auto kern : kerns) {
                 CAC_TRY(smem_optin(ctx_, kern));
-                kern<<<(unsigned)groups, qwarps * 32, wsm, s>>>(
+                kern<<<(unsigned)groups_warp, qwarps * 32, wsm, s>>>(
                     d_task.as<TaskDesc>(), d_src.as<SrcDesc>(), d_kout.as<uint32_t>(), d_gto.as<uint64_t>(),
-                    (uint32_t)tasks.size(), wrows, d_qoff.as<uint64_t>(), static_cast<unsigned char *>(out->p),
+                    (uint32_t)tasks.size(), qwarps * 4, d_qoff.as<uint64_t>(), static_cast<unsigned char *>(out->p),
                     (uint32_t)stage_words, kmax);
             }
+            CAC_CUDA_TRY(cudaGetLastError());
+            return CAC_OK;
+        };
+        uint8_t &tuned = ctx_->quotient_choice[quotient_bucket(maxN, all_small)];
+        const bool sizeable = groups_shared >= (uint64_t)4 * ctx_->num_sms;  // enough work to time
+        if (!qwarps) {
+            CAC_TRY(launch_shared());
+        } else if (tuned == kQuotientShared) {
+            CAC_TRY(launch_shared());
+        } else if (tuned == kQuotientWarp) {
+            CAC_TRY(launch_warp());
+        } else if (!sizeable) {
+            CAC_TRY(maxN >= kSharedRowMinN ? launch_shared() : launch_warp());
         } else {
-            std::vector<decltype(&quotient_kernel<kQT, uint32_t>)> kerns;
-            if (t32) kerns.push_back(quotient_kernel<kQT, uint32_t>);
-            if (t64) kerns.push_back(quotient_kernel<kQT, uint64_t>);
-            for (auto kern : kerns) {
-                CAC_TRY(smem_optin(ctx_, kern));
-                kern<<<(unsigned)groups, kQT, qsm, s>>>(
-                    d_task.as<TaskDesc>(), d_src.as<SrcDesc>(), d_kout.as<uint32_t>(), d_gto.as<uint64_t>(),
-                    (uint32_t)tasks.size(), qrows, d_qoff.as<uint64_t>(), static_cast<unsigned char *>(out->p));
-            }
+            // both write the same matrices, row sums and prefixes: time one, then the other
+            cudaEvent_t *ev = ctx_->ev;
+            float t_warp = 0, t_shared = 0;
+            CAC_CUDA_TRY(cudaEventRecord(ev[5], s));
+            CAC_TRY(launch_warp());
+            CAC_CUDA_TRY(cudaEventRecord(ev[6], s));
+            CAC_TRY(launch_shared());
+            CAC_CUDA_TRY(cudaEventRecord(ev[7], s));
+            CAC_CUDA_TRY(cudaEventSynchronize(ev[7]));
+            CAC_CUDA_TRY(cudaEventElapsedTime(&t_warp, ev[5], ev[6]));
+            CAC_CUDA_TRY(cudaEventElapsedTime(&t_shared, ev[6], ev[7]));
+            tuned = t_shared < t_warp ? kQuotientShared : kQuotientWarp;
         }
-        CAC_CUDA_TRY(cudaGetLastError());
     }
     // the sources are read by everything enqueued above: their buffers may now be released
     for (MatBuf *b : consumed) release(b);
@@ -1399,8 +1366,7 @@ int KsEngine::step() {
         nd.N = k;
         nd.is_root = 0;
         nd.mat = static_cast<unsigned char *>(out->p) + out_off[i];
-        nd.pre = qwarps ? reinterpret_cast<uint64_t *>(static_cast<unsigned char *>(out->p) + out_off[tasks.size() + i])
-                        : nullptr;
+        nd.pre = reinterpret_cast<uint64_t *>(static_cast<unsigned char *>(out->p) + out_off[tasks.size() + i]);
         nd.buf = out;
         out->refs++;
         outstanding[nd.query]++;
