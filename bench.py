@@ -172,13 +172,26 @@ def _ks_also(ctx):
             vals = list(pool.map(lambda ri: pyoracle.mincut_trial(n, u, v, w, 0, ri[0], ri[1]), ids))
         cpu_s = time.perf_counter() - t0
         cpu_cut, cpu_trials = min(vals), len(ids)
+        filled = None
+        if n <= 1000:
+            # the same query 64 times with seeds 0..63 in one cac_mincut_batch: the GPU's trial
+            # throughput once it is full (one C1 query has only 60 trials in flight)
+            seeds = list(range(64))
+            ctx.mincut_batch([g] * len(seeds), 0.95, seeds, ranks)  # warm-up
+            t1 = time.perf_counter()
+            rs = ctx.mincut_batch([g] * len(seeds), 0.95, seeds, ranks)
+            bs = time.perf_counter() - t1
+            filled = {"queries": len(seeds), "trials": sum(r.total_trials for r in rs),
+                      "trials_per_s": sum(r.total_trials for r in rs) / bs, "ms_per_batch": bs * 1e3,
+                      "timing": "host wall clock around cac_mincut_batch"}
         out.append({"workload": name, "trials": trials, "cut": int(res.cut),
                     "min_weighted_degree": int(deg.min()), "ms_per_query": statistics.median(ms),
                     "trials_per_s": trials / (statistics.median(ms) / 1e3),
                     "cpu_baseline": {"trials_per_s": cpu_trials / cpu_s, "cores": cores, "kind": "port",
                                      "sample": "%d trial(s) of the oracle's replay on %d host threads"
                                                % (cpu_trials, cores),
-                                     "cut_agrees": (cpu_cut == res.cut) if cpu_trials == trials else None}})
+                                     "cut_agrees": (cpu_cut == res.cut) if cpu_trials == trials else None},
+                    "batched_64_queries": filled})
         g.free()
     return out
 

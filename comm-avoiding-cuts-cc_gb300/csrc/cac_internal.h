@@ -218,9 +218,13 @@ struct MincutQuery {
     uint64_t *d_cuts;  // ranks * per_rank trial cuts (device)
     uint32_t t = 0;    // contraction size before Karger-Stein (0: square_root's intermediate size)
 };
-// Stage 1 and Stage 2 of one query into a running engine: its trial cuts start at 2^64 - 1 and
-// its root nodes carry engine query id `query`; the query is done when outstanding[query] is 0.
-int mincut_admit_query(cac_ctx *ctx, KsEngine &eng, const MincutQuery &q, uint32_t query);
+// Stage 1 and Stage 2 of several queries into a running engine (engine ids ids[i]); their
+// Stage 1 trials share launches. Every trial cut starts at 2^64 - 1 and the root nodes carry the
+// query's engine id; a query is done when outstanding[id] is 0.
+// status[i] is each query's own result (a query that fails its checks fails alone; a failure of
+// the shared admission is every admitted query's).
+int mincut_admit_queries(cac_ctx *ctx, KsEngine &eng, const std::vector<MincutQuery> &qs,
+                         const std::vector<uint32_t> &ids, std::vector<int> &status, std::vector<std::string> &msgs);
 // Stage 1 of B trials (keys k0[b], idx[b]) of a graph with more than 16384 vertices in global
 // memory (shrink_big.cu): labels to d_lab[b * n ..], vertices left to d_kout[b].
 uint64_t shrink_big_scratch(uint32_t n, uint64_t m, uint32_t B);

@@ -1398,6 +1398,9 @@ struct QueryPlan {
     uint32_t query;       // engine bookkeeping id
 };
 
+int admit_stage1(cac_ctx *ctx, KsEngine &eng, const std::vector<const QueryPlan *> &qs);
+int admit_big(cac_ctx *ctx, KsEngine &eng, const QueryPlan &q);
+
 int admit(cac_ctx *ctx, KsEngine &eng, const QueryPlan &q) {
     cudaStream_t s = ctx->stream;
     const cac_graph *g = q.g;
@@ -1428,61 +1431,150 @@ int admit(cac_ctx *ctx, KsEngine &eng, const QueryPlan &q) {
         eng.release(root);
         return CAC_OK;
     }
-    // Stage 1 in chunks whose scratch stays within 4 GB: shared-memory union-find per trial up to
-    // 16384 vertices, the global-memory rounds of shrink_big.cu above
-    const bool big = n > kMaxSmemVertices;
-    const uint64_t per_trial = big ? shrink_big_scratch(n, m, 1) + 4ull * n
-                                   : 8 * std::max<uint64_t>(m, 1) + 4 * (uint64_t)n + 64;
-    const uint64_t chunk = std::max<uint64_t>(1, std::min<uint64_t>({q.trials, (4ull << 30) / per_trial, (uint64_t)65535}));
+    // Stage 1: the global-memory rounds of shrink_big.cu above 16384 vertices, else the
+    // shared-memory kernel, batched with other queries' trials where the caller has several
+    if (n > kMaxSmemVertices) return admit_big(ctx, eng, q);
+    std::vector<const QueryPlan *> one{&q};
+    return admit_stage1(ctx, eng, one);
+}
+
+// Stage 1 and Stage 2 of every trial of the given queries (t < n <= 16384), the trials of all of
+// them together: one Stage 1 launch, one read-back of the contracted sizes and one dense build
+// per chunk, whose scratch stays within 4 GB. Admitting the queries of a batch one by one costs a
+// launch and two host synchronisations per query.
+int admit_stage1(cac_ctx *ctx, KsEngine &eng, const std::vector<const QueryPlan *> &qs) {
+    cudaStream_t s = ctx->stream;
+    struct Item {
+        const QueryPlan *q;
+        uint64_t i;
+    };
+    std::vector<Item> items;
+    for (const QueryPlan *q : qs)
+        for (uint64_t i = 0; i < q->trials; i++) items.push_back({q, i});
     DevBuf &d_pre = scratch(ctx, kSlotPre), &d_lab = scratch(ctx, kSlotLab), &d_k = scratch(ctx, kSlotK),
            &d_sd = scratch(ctx, kSlotSd), &d_dd = scratch(ctx, kSlotDd);
-    const size_t sm = kBatch * sizeof(uint2) + kCoarse * sizeof(uint64_t) + (size_t)std::min(n, kMaxSmemVertices) * 4;
-    if (!big)
-        CAC_TRY(smem_optin(ctx, iss_shrink_kernel<kNT>));
-    for (uint64_t c0 = 0; c0 < q.trials; c0 += chunk) {
-        const uint32_t B = (uint32_t)std::min<uint64_t>(chunk, q.trials - c0);
-        CAC_TRY(d_pre.ensure(big ? shrink_big_scratch(n, m, B) : (size_t)B * std::max<uint64_t>(m, 1) * 8));
-        CAC_TRY(d_lab.ensure((size_t)B * n * 4));
+    CAC_TRY(smem_optin(ctx, iss_shrink_kernel<kNT>));
+    size_t c0 = 0;
+    while (c0 < items.size()) {
+        // a chunk: at most 65535 trials and 4 GB of prefix + label scratch
+        size_t c1 = c0;
+        uint64_t pre_words = 0, lab_words = 0;
+        uint32_t nmax = 1;
+        uint64_t mmax = 1;
+        while (c1 < items.size() && c1 - c0 < 65535) {
+            const cac_graph *g = items[c1].q->g;
+            const uint64_t pw = std::max<uint64_t>(g->m, 1), lw = g->n;
+            if (c1 > c0 && (pre_words + pw) * 8 + (lab_words + lw) * 4 > (4ull << 30)) break;
+            pre_words += pw;
+            lab_words += lw;
+            nmax = std::max(nmax, g->n);
+            mmax = std::max(mmax, g->m);
+            c1++;
+        }
+        const uint32_t B = (uint32_t)(c1 - c0);
+        CAC_TRY(d_pre.ensure(pre_words * 8));
+        CAC_TRY(d_lab.ensure(lab_words * 4));
         CAC_TRY(d_k.ensure((size_t)B * 4));
         std::vector<ShrinkDesc> sd(B);
+        uint64_t po = 0, lo = 0;
         for (uint32_t b = 0; b < B; b++) {
-            const uint64_t i = c0 + b;
+            const QueryPlan &q = *items[c0 + b].q;
+            const uint64_t i = items[c0 + b].i;
             ShrinkDesc &D = sd[b];
-            D.U = g->u;
-            D.V = g->v;
-            D.W = g->w;
-            D.m = m;
-            D.pre = d_pre.as<uint64_t>() + (size_t)b * std::max<uint64_t>(m, 1);
-            D.lab = d_lab.as<uint32_t>() + (size_t)b * n;
+            D.U = q.g->u;
+            D.V = q.g->v;
+            D.W = q.g->w;
+            D.m = q.g->m;
+            D.pre = d_pre.as<uint64_t>() + po;
+            D.lab = d_lab.as<uint32_t>() + lo;
             D.k_out = d_k.as<uint32_t>() + b;
-            D.n = n;
+            D.n = q.g->n;
             D.target = q.t;
             D.k0 = q.seed + (uint32_t)(i / q.per_rank);
             D.idx = (uint32_t)(i % q.per_rank);
+            po += std::max<uint64_t>(q.g->m, 1);
+            lo += q.g->n;
         }
-        if (big) {
-            std::vector<uint32_t> k0(B), idx(B);
-            for (uint32_t b = 0; b < B; b++) {
-                k0[b] = sd[b].k0;
-                idx[b] = sd[b].idx;
+        const size_t sm = kBatch * sizeof(uint2) + kCoarse * sizeof(uint64_t) + (size_t)nmax * 4;
+        CAC_TRY(upload(ctx, d_sd, sd));
+        iss_shrink_kernel<kNT><<<B, kNT, sm, s>>>(d_sd.as<ShrinkDesc>());
+        CAC_CUDA_TRY(cudaGetLastError());
+        std::vector<uint32_t> kdim(B);
+        CAC_CUDA_TRY(cudaMemcpyAsync(kdim.data(), d_k.p, (size_t)B * 4, cudaMemcpyDeviceToHost, s));
+        CAC_CUDA_TRY(cudaStreamSynchronize(s));
+        uint64_t bytes = 0;
+        for (uint32_t b = 0; b < B; b++) {
+            const uint64_t esize = items[c0 + b].q->g->total_weight < (1ull << 32) ? 4 : 8;
+            bytes += ((uint64_t)kdim[b] * ld_of(kdim[b]) * esize + 15) / 16 * 16;
+        }
+        MatBuf *roots = nullptr;
+        CAC_TRY(eng.alloc(std::max<uint64_t>(bytes, 16), &roots));
+        CAC_CUDA_TRY(cudaMemsetAsync(roots->p, 0, bytes, s));
+        std::vector<DenseDesc> dd(B);
+        uint64_t off = 0;
+        for (uint32_t b = 0; b < B; b++) {
+            const cac_graph *g = items[c0 + b].q->g;
+            const uint32_t small = g->total_weight < (1ull << 32) ? 1u : 0u;
+            // no scatter for a trial without a matrix (its labels would index past the buffer)
+            dd[b] = DenseDesc{g->u, g->v, g->w, sd[b].lab, static_cast<unsigned char *>(roots->p) + off,
+                              kdim[b] >= 2 ? g->m : 0, kdim[b], small};
+            off += ((uint64_t)kdim[b] * ld_of(kdim[b]) * (small ? 4 : 8) + 15) / 16 * 16;
+        }
+        CAC_TRY(upload(ctx, d_dd, dd));
+        dim3 grid((unsigned)std::max<uint64_t>(
+                      1, std::min<uint64_t>((mmax + 255) / 256, std::max<uint64_t>(1, (uint64_t)ctx->num_sms * 8 / B))),
+                  B);
+        dense_build_kernel<<<grid, 256, 0, s>>>(d_dd.as<DenseDesc>());
+        CAC_CUDA_TRY(cudaGetLastError());
+        roots->refs++;
+        for (uint32_t b = 0; b < B; b++) {
+            const QueryPlan &q = *items[c0 + b].q;
+            const uint64_t i = items[c0 + b].i;
+            if (kdim[b] < 2) {
+                // a single vertex left, or only isolated vertices: no cut edge
+                fill_u64<<<1, 32, 0, s>>>(q.cuts + i, 1, 0);
+                continue;
             }
-            CAC_TRY(shrink_big(ctx, g, q.t, B, k0.data(), idx.data(), d_lab.as<uint32_t>(), d_k.as<uint32_t>(), d_pre.p));
-        } else {
-            CAC_TRY(upload(ctx, d_sd, sd));
-            iss_shrink_kernel<kNT><<<B, kNT, sm, s>>>(d_sd.as<ShrinkDesc>());
-            CAC_CUDA_TRY(cudaGetLastError());
+            eng.add(KNode{q.cuts + i, sd[b].k0, sd[b].idx, 1, kdim[b], 1, dd[b].small, q.query, dd[b].mat, roots});
         }
+        eng.release(roots);
+        CAC_CUDA_TRY(cudaStreamSynchronize(s));  // the scratch is reused by the next chunk
+        c0 = c1;
+    }
+    return CAC_OK;
+}
+
+// Stage 1 of a query above 16384 vertices: the global-memory rounds of shrink_big.cu, in chunks
+// of trials whose scratch stays within 4 GB.
+int admit_big(cac_ctx *ctx, KsEngine &eng, const QueryPlan &q) {
+    cudaStream_t s = ctx->stream;
+    const cac_graph *g = q.g;
+    const uint32_t n = g->n;
+    const uint64_t m = g->m;
+    const uint32_t small = g->total_weight < (1ull << 32) ? 1u : 0u;
+    const uint64_t per_trial = shrink_big_scratch(n, m, 1) + 4ull * n;
+    const uint64_t chunk = std::max<uint64_t>(1, std::min<uint64_t>({q.trials, (4ull << 30) / per_trial, (uint64_t)65535}));
+    DevBuf &d_pre = scratch(ctx, kSlotPre), &d_lab = scratch(ctx, kSlotLab), &d_k = scratch(ctx, kSlotK),
+           &d_dd = scratch(ctx, kSlotDd);
+    for (uint64_t c0 = 0; c0 < q.trials; c0 += chunk) {
+        const uint32_t B = (uint32_t)std::min<uint64_t>(chunk, q.trials - c0);
+        CAC_TRY(d_pre.ensure(shrink_big_scratch(n, m, B)));
+        CAC_TRY(d_lab.ensure((size_t)B * n * 4));
+        CAC_TRY(d_k.ensure((size_t)B * 4));
+        std::vector<uint32_t> k0(B), idx(B);
+        for (uint32_t b = 0; b < B; b++) {
+            const uint64_t i = c0 + b;
+            k0[b] = q.seed + (uint32_t)(i / q.per_rank);
+            idx[b] = (uint32_t)(i % q.per_rank);
+        }
+        CAC_TRY(shrink_big(ctx, g, q.t, B, k0.data(), idx.data(), d_lab.as<uint32_t>(), d_k.as<uint32_t>(), d_pre.p));
         std::vector<uint32_t> kdim(B);
         CAC_CUDA_TRY(cudaMemcpyAsync(kdim.data(), d_k.p, (size_t)B * 4, cudaMemcpyDeviceToHost, s));
         CAC_CUDA_TRY(cudaStreamSynchronize(s));
         // more than 16384 vertices left only when Stage 1 stopped with no edge between them
         // (a disconnected graph): every vertex is isolated and the trial's cut is exactly 0
-        std::vector<uint8_t> isolated(B, 0);
         for (uint32_t b = 0; b < B; b++)
-            if (kdim[b] > kMaxSmemVertices) {
-                isolated[b] = 1;
-                kdim[b] = 0;
-            }
+            if (kdim[b] > kMaxSmemVertices) kdim[b] = 0;
         const uint64_t esize = small ? 4 : 8;
         uint64_t bytes = 0;
         for (uint32_t b = 0; b < B; b++) bytes += ((uint64_t)kdim[b] * ld_of(kdim[b]) * esize + 15) / 16 * 16;
@@ -1493,8 +1585,8 @@ int admit(cac_ctx *ctx, KsEngine &eng, const QueryPlan &q) {
         uint64_t off = 0;
         for (uint32_t b = 0; b < B; b++) {
             // no scatter for a trial without a matrix (its labels would index past the buffer)
-            dd[b] = DenseDesc{g->u, g->v, g->w, sd[b].lab, static_cast<unsigned char *>(roots->p) + off,
-                              kdim[b] >= 2 ? m : 0, kdim[b], small};
+            dd[b] = DenseDesc{g->u, g->v, g->w, d_lab.as<uint32_t>() + (size_t)b * n,
+                              static_cast<unsigned char *>(roots->p) + off, kdim[b] >= 2 ? m : 0, kdim[b], small};
             off += ((uint64_t)kdim[b] * ld_of(kdim[b]) * esize + 15) / 16 * 16;
         }
         CAC_TRY(upload(ctx, d_dd, dd));
@@ -1507,16 +1599,27 @@ int admit(cac_ctx *ctx, KsEngine &eng, const QueryPlan &q) {
         for (uint32_t b = 0; b < B; b++) {
             const uint64_t i = c0 + b;
             if (kdim[b] < 2) {
-                // a single vertex left, or only isolated vertices: no cut edge
                 fill_u64<<<1, 32, 0, s>>>(q.cuts + i, 1, 0);
                 continue;
             }
-            eng.add(KNode{q.cuts + i, sd[b].k0, sd[b].idx, 1, kdim[b], 1, small, q.query, dd[b].mat, roots});
+            eng.add(KNode{q.cuts + i, k0[b], idx[b], 1, kdim[b], 1, small, q.query, dd[b].mat, roots});
         }
         eng.release(roots);
         CAC_CUDA_TRY(cudaStreamSynchronize(s));  // the scratch is reused by the next chunk
     }
     return CAC_OK;
+}
+
+// Admission of several queries: those with Stage 1 in shared memory go through admit_stage1
+// together, the others one by one.
+int admit_many(cac_ctx *ctx, KsEngine &eng, const std::vector<const QueryPlan *> &qs) {
+    std::vector<const QueryPlan *> batched;
+    for (const QueryPlan *q : qs) {
+        if (q->trials == 0) continue;
+        if (q->t < q->g->n && q->g->n <= kMaxSmemVertices) batched.push_back(q);
+        else CAC_TRY(admit(ctx, eng, *q));
+    }
+    return batched.empty() ? CAC_OK : admit_stage1(ctx, eng, batched);
 }
 
 int check_graph(const cac_graph *g, uint32_t t_override) {
@@ -1534,16 +1637,46 @@ int check_graph(const cac_graph *g, uint32_t t_override) {
 
 }  // namespace
 
-int mincut_admit_query(cac_ctx *ctx, KsEngine &eng, const MincutQuery &q, uint32_t query) {
-    CAC_TRY(check_graph(q.g, q.t));
-    QueryPlan p{q.g, q.seed, q.ranks, q.per_rank, q.t ? q.t : intermediate_size(q.g->n, q.g->m),
-                (uint64_t)q.ranks * q.per_rank,
-                q.d_cuts, query};
-    if (p.trials)
-        fill_u64<<<(unsigned)std::max<uint64_t>(1, std::min<uint64_t>((p.trials + 255) / 256, 4096)), 256, 0,
-                   ctx->stream>>>(p.cuts, p.trials, kU64Max);
-    CAC_CUDA_TRY(cudaGetLastError());
-    return admit(ctx, eng, p);
+int mincut_admit_queries(cac_ctx *ctx, KsEngine &eng, const std::vector<MincutQuery> &qs,
+                         const std::vector<uint32_t> &ids, std::vector<int> &status, std::vector<std::string> &msgs) {
+    status.assign(qs.size(), CAC_OK);
+    msgs.assign(qs.size(), std::string());
+    std::vector<QueryPlan> plans;
+    plans.reserve(qs.size());
+    std::vector<size_t> which;
+    for (size_t i = 0; i < qs.size(); i++) {
+        const MincutQuery &q = qs[i];
+        const int st = check_graph(q.g, q.t);
+        if (st != CAC_OK) {
+            status[i] = st;
+            msgs[i] = cac_last_error();
+            continue;
+        }
+        plans.push_back(QueryPlan{q.g, q.seed, q.ranks, q.per_rank, q.t ? q.t : intermediate_size(q.g->n, q.g->m),
+                                  (uint64_t)q.ranks * q.per_rank, q.d_cuts, ids[i]});
+        which.push_back(i);
+        const QueryPlan &p = plans.back();
+        if (p.trials)
+            fill_u64<<<(unsigned)std::max<uint64_t>(1, std::min<uint64_t>((p.trials + 255) / 256, 4096)), 256, 0,
+                       ctx->stream>>>(p.cuts, p.trials, kU64Max);
+    }
+    if (cudaGetLastError() != cudaSuccess) {
+        set_error("mincut_admit_queries: filling the trial slots failed");
+        for (size_t i : which) {
+            status[i] = CAC_ERR_CUDA;
+            msgs[i] = cac_last_error();
+        }
+        return CAC_ERR_CUDA;
+    }
+    std::vector<const QueryPlan *> ptrs;
+    for (const QueryPlan &p : plans) ptrs.push_back(&p);
+    const int st = admit_many(ctx, eng, ptrs);
+    if (st != CAC_OK)
+        for (size_t i : which) {
+            status[i] = st;
+            msgs[i] = cac_last_error();
+        }
+    return st;
 }
 
 int mincut_run_queries(cac_ctx *ctx, std::vector<MincutQuery> &queries, float *device_ms) {
@@ -1573,14 +1706,19 @@ int mincut_run_queries(cac_ctx *ctx, std::vector<MincutQuery> &queries, float *d
     const uint64_t budget = ctx->budget ? ctx->budget / 2 : (48ull << 30);
     size_t next = 0;
     while (next < plans.size() || !eng.idle()) {
+        // the queries that fit are admitted together (one Stage 1 launch for all of them)
+        std::vector<const QueryPlan *> wave;
+        uint64_t wave_est = 0;
         while (next < plans.size()) {
             const QueryPlan &p = plans[next];
             const uint64_t t = std::min<uint64_t>(p.t, p.g->n);
             const uint64_t est = (p.t < p.g->n ? p.trials : 1) * t * t * 8 * 3;
-            if (!eng.idle() && ctx->held + est > budget) break;
-            CAC_TRY(admit(ctx, eng, p));
+            if ((!eng.idle() || !wave.empty()) && ctx->held + wave_est + est > budget) break;
+            wave.push_back(&p);
+            wave_est += est;
             next++;
         }
+        if (!wave.empty()) CAC_TRY(admit_many(ctx, eng, wave));
         if (!eng.idle()) CAC_TRY(eng.step());
     }
     uint32_t err = 0;

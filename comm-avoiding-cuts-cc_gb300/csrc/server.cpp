@@ -159,18 +159,34 @@ struct CutWorker {
         finish(s, r, st, msg);
     }
 
-    void admit(Request *r) {
-        r->query = take_id();
-        running.push_back(r);
-        int st = stream_alloc(s->cut, &r->d_cuts, std::max<uint64_t>(r->trials, 1) * 8);
-        if (st == CAC_OK) {
-            MincutQuery q{r->req.graph, r->req.seed, r->ranks, r->per_rank, static_cast<uint64_t *>(r->d_cuts)};
-            st = mincut_admit_query(s->cut, *eng, q, r->query);
+    // Admits the queries taken from the queue together: their Stage 1 trials share launches.
+    void admit(const std::vector<Request *> &batch) {
+        std::vector<MincutQuery> qs;
+        std::vector<uint32_t> ids;
+        std::vector<Request *> rs;
+        for (Request *r : batch) {
+            r->query = take_id();
+            running.push_back(r);
+            const int st = stream_alloc(s->cut, &r->d_cuts, std::max<uint64_t>(r->trials, 1) * 8);
+            if (st != CAC_OK) {
+                r->st = st;
+                r->msg = cac_last_error();
+                continue;
+            }
+            qs.push_back(MincutQuery{r->req.graph, r->req.seed, r->ranks, r->per_rank,
+                                     static_cast<uint64_t *>(r->d_cuts)});
+            ids.push_back(r->query);
+            rs.push_back(r);
         }
-        if (st != CAC_OK) {  // nodes already added still write into d_cuts: report once they drain
-            r->st = st;
-            r->msg = cac_last_error();
-        }
+        if (rs.empty()) return;
+        std::vector<int> status;
+        std::vector<std::string> msgs;
+        mincut_admit_queries(s->cut, *eng, qs, ids, status, msgs);
+        for (size_t i = 0; i < rs.size(); i++)
+            if (status[i] != CAC_OK) {  // nodes already added still write into d_cuts: report once they drain
+                rs[i]->st = status[i];
+                rs[i]->msg = msgs[i];
+            }
     }
 
     // Queries with no node left in the engine are finished: reduce their cuts on the host.
@@ -251,7 +267,7 @@ struct CutWorker {
                     batch.push_back(r);
                 }
             }
-            for (Request *r : batch) admit(r);
+            if (!batch.empty()) admit(batch);
             if (!eng->idle()) {
                 const int st = eng->step();
                 if (st != CAC_OK) {
