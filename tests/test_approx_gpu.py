@@ -47,3 +47,17 @@ def test_larger_graph(ctx):
     g = ctx.graph(n, u, v, w)
     res = g.approx_cut(0.9, seed=2)
     assert (res.cut, res.level) == O.approx_cut(n, u, v, w, 0.9, 2, 1)
+
+
+@pytest.mark.parametrize("ranks", [1, 3, 7])
+def test_quad_path_large_graph(ctx, ranks):
+    # more than 2^16 quads of 4 edges: one sitmo block per quad, hooks in slices; the same keep
+    # decisions as the oracle's per-edge draws, so the same level, on 1 and several virtual ranks
+    # (slices of m / P edges, the last with the rest)
+    n, u, v, w = graphgen.erdos_renyi_m(15000, 40.0, 8, wmax=42)  # six or seven levels
+    u, v, w = u[:-5], v[:-5], w[:-5]  # m not a multiple of 4 or of the rank count
+    assert len(u) // 4 >= (1 << 16)
+    g = ctx.graph(n, u, v, w)
+    for seed in (0, 6):
+        res = g.approx_cut(0.9, seed=seed, virtual_ranks=ranks)
+        assert (res.cut, res.level) == O.approx_cut(n, u, v, w, 0.9, seed, ranks)
