@@ -32,6 +32,7 @@ import math
 import os
 import statistics
 import subprocess
+import tempfile
 import sys
 import time
 
@@ -73,7 +74,8 @@ class Clocks:
     def __init__(self, device):
         self.device = device
         self.proc = None
-        self.path = os.path.join(ROOT, "gpurun_out", "clocks_bench_%d.csv" % device)
+        # raw samples (the JSON line carries their summary); CAC_CLOCKS_DIR keeps them elsewhere
+        self.path = os.path.join(os.environ.get("CAC_CLOCKS_DIR", tempfile.gettempdir()), "clocks_bench_%d.csv" % device)
 
     def __enter__(self):
         try:
