@@ -1,5 +1,5 @@
 // Writes the binary cache of a text edge-list file (the reference's input format): every command
-// line of this build accepts the cache in place of the text file and loads it without parsing.
+// line of this package accepts the cache in place of the text file and loads it without parsing.
 //   cache_graph INPUT_FILE CACHE_FILE
 #include <iostream>
 

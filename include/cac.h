@@ -57,7 +57,7 @@ extern "C" {
 #define CAC_ERR_PARSE (-3)       /* malformed edge-list file */
 #define CAC_ERR_CUDA (-4)        /* a CUDA runtime call failed */
 #define CAC_ERR_TIMEOUT (-5)     /* a device-side bounded wait or draw budget ran out */
-#define CAC_ERR_UNSUPPORTED (-6) /* valid request this build does not handle */
+#define CAC_ERR_UNSUPPORTED (-6) /* valid request the library does not handle */
 #define CAC_ERR_IO (-7)          /* file could not be opened or read */
 
 #define CAC_HOST 0

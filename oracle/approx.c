@@ -6,7 +6,7 @@
  * copies and stops at the first level with more than `trials` components; the answer is 2^i
  * (2^0 when no level disconnects). trials = ceil(ln(1-p) / ln(1-e^-0.75)) (:82-87).
  *
- * This build's counter-addressed keep test (the reference draws through libstdc++'s
+ * libcac's counter-addressed keep test (the reference draws through libstdc++'s
  * binomial_distribution): P(Binomial(w, q) > 0) = 1 - (1-q)^w, so edge e of copy j at level i
  * is kept iff x >= F(i, w_e), where x is draw e_local of the stream with key
  * (seed + r, i, j, 1) (r = the virtual rank owning the edge's slice, e_local its index in the

@@ -21,7 +21,7 @@
  *               copy to max(ceil(n/sqrt 2)+1, 128) vertices by weighted random contraction,
  *               base case n <= 128 solved exactly (co_mincut_base_case.hpp:164-221); the trial
  *               value is min(minimum weighted degree, every leaf's exact cut).
- *    What is this build's own definition (the reference draws through libstdc++'s
+ *    What is libcac's own definition (the reference draws through libstdc++'s
  *    uniform_int_distribution and sum_tree, whose consumption is data dependent):
  *      - draw d of round rho of a stream with key K is the u64 word d%4 of the sitmo block at
  *        counter (d/4, rho, 0, 0); trial (r, i) uses key (seed + r, i, tag, 0) with tag 1 for

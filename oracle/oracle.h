@@ -2,7 +2,7 @@
  * ORACLE — test infrastructure, not product code.
  *
  * A plain-C, single-threaded restatement of the reference's min-cut / connected-components
- * hot path (PJK/comm-avoiding-cuts-cc), used only as the CHECKER for the CUDA path:
+ * hot path (PJK/comm-avoiding-cuts-cc), used only to check the CUDA path:
  * tests/, __graft_entry__.smoke() and bench.py's cpu_baseline / reference legs may call
  * it; the product (libcac) never links or runs it.
  *

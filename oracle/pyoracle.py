@@ -1,7 +1,7 @@
 """ORACLE (test infrastructure): ctypes binding of oracle/lib/liboracle.so.
 
 Only tests/, __graft_entry__.smoke() and bench.py's CPU-baseline legs import this module; it
-is the checker, never the product. Build the library with ``make -C oracle``.
+checks the product and is never part of it. Build the library with ``make -C oracle``.
 """
 import ctypes
 import os
