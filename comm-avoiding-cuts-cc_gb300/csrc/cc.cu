@@ -31,7 +31,7 @@ namespace cac {
 namespace {
 
 constexpr int kThreads = 256;
-constexpr int kTileItems = 16;                       // vertices per thread in the labelling tiles
+constexpr int kTileItems = 4;                        // vertices per thread in the labelling tiles
 constexpr int kTile = kThreads * kTileItems;         // vertices per labelling tile
 constexpr size_t kPinnedBytes = 60 * 1024;           // ctx pinned staging available for rank descriptors
 constexpr int kEdgeThreads = 1024;                   // closing-pass CTA (one per SM: the bitmap fills smem)
@@ -41,6 +41,9 @@ constexpr uint32_t kSampleChunk = 32;                // consecutive edges behind
 constexpr uint32_t kSampleSubrounds = 8;             // slices of the sampling round
 constexpr uint32_t kCompressedSubrounds = 3;         // slices followed by a full compression (and the last)
 constexpr uint32_t kMaxRegions = 1024;               // filter CTAs (regions of the survivor buffer)
+// survivor-hook CTAs per SM: about one survivor per thread on BA n=1,024,000 (0.6 M survivors);
+// 8 against 4: 20 vs 22.5 us there, 47 vs 63.5 us on R-MAT scale 22; 16 no better
+constexpr unsigned kSurvivorBlocksPerSm = 8;
 constexpr uint32_t kStreamPieces = 8;                // sample pieces (and gaps) of a host edge list
 constexpr uint32_t kErrWord = 9;                     // a query's error word (after its count and giant root)
 constexpr uint32_t kErrBadId = 1;                    // an edge endpoint was >= n (the edge was skipped)
@@ -645,8 +648,8 @@ int cc_enqueue(cac_ctx *ctx, const CCLaunch &L, bool capturing) {
             }
             CAC_TRY(record(ctx, 4, capturing));
             if (tiles)
-                cc_hook_survivors<<<(unsigned)ctx->num_sms * 4, kThreads, 0, s>>>(L.par, L.surv, L.region_counts,
-                                                                                   regions, per * 256);
+                cc_hook_survivors<<<(unsigned)ctx->num_sms * kSurvivorBlocksPerSm, kThreads, 0, s>>>(
+                    L.par, L.surv, L.region_counts, regions, per * 256);
             const uint64_t done = tiles * 256;
             if (done < m)
                 (L.check ? cc_edge_pass<false, true> : cc_edge_pass<false, false>)<<<grid_for(ctx, m - done, 8), kThreads,
@@ -934,7 +937,7 @@ int stream_enqueue(cac_ctx *ctx, const StreamLaunch &L, bool capturing) {
                 auto filt = L.nwords <= kSmemBitmapWords ? cc_filter<true, true> : cc_filter<false, true>;
                 filt<<<regions, kEdgeThreads, sm, s>>>(L.d_u + e0, L.d_v + e0, tiles, L.bits, L.nwords, L.surv,
                                                        L.region_counts, n, L.total + kErrWord);
-                cc_hook_survivors<<<(unsigned)ctx->num_sms * 4, kThreads, 0, s>>>(L.par, L.surv, L.region_counts,
+                cc_hook_survivors<<<(unsigned)ctx->num_sms * kSurvivorBlocksPerSm, kThreads, 0, s>>>(L.par, L.surv, L.region_counts,
                                                                                    regions, tper * 256);
             }
             const uint64_t done = tiles * 256;
@@ -1086,7 +1089,7 @@ int cc_run_streamed(cac_ctx *ctx, uint32_t n, uint64_t m, const uint32_t *h_u, c
 // single-pass form of the CC query (hook every edge, compress, count, label) with all of its
 // scratch in one file-scope device array of fixed size, so it performs no device allocation of
 // its own. The array belongs to this module: every GPU that loads the library holds it (16 MiB
-// for the parent array plus 8 KiB of tile counters) until the process exits.
+// for the parent array plus 33 KiB of tile counters and offsets) until the process exits.
 namespace cac {
 namespace {
 

@@ -141,7 +141,7 @@ int cac_cc_edges(cac_ctx *ctx, uint32_t n, uint64_t m, const uint32_t *u_host, c
  * memory belongs to that framework's allocator, or a latency-bound serving path that must not
  * take cudaMalloc's implicit synchronisation. The caller passes device inputs and outputs; the
  * scratch is one fixed array of this library that every GPU loading it holds until exit
- * (16 MiB + 8 KiB), so n is limited to 4,194,304 vertices (CAC_ERR_INVALID beyond; cac_cc has no
+ * (16 MiB + 33 KiB), so n is limited to 4,194,304 vertices (CAC_ERR_INVALID beyond; cac_cc has no
  * such limit). No ctx is needed: the work is enqueued on `stream` (a cudaStream_t of the current
  * device, NULL for the default stream) and the call returns without synchronising.
  * labels_dev (nullable) gets the same labels as cac_cc; num_components_dev (nullable, device)
