@@ -120,6 +120,8 @@ EXPORTS = [
     ("cac_exact_cut_small", ctypes.c_int, [_vp, ctypes.c_uint32, _vp, _u64p]),
     ("cac_approx_cut", ctypes.c_int, [_vp, _vp, ctypes.c_double, ctypes.c_uint32, ctypes.c_uint32,
                                       ctypes.POINTER(ApproxResult)]),
+    ("cac_approx_cut_seed_replay", ctypes.c_int, [_vp, _vp, ctypes.c_double, ctypes.c_uint32, ctypes.c_uint32,
+                                      ctypes.POINTER(ApproxResult)]),
     ("cac_sitmo_blocks", ctypes.c_int, [_vp, _u64p, _u64p, ctypes.c_uint64, _vp]),
     ("cac_graph_generate", ctypes.c_int, [_vp, ctypes.POINTER(GenSpec), ctypes.POINTER(_vp)]),
     ("cac_click_edges", ctypes.c_int, [ctypes.c_uint32, ctypes.c_uint32, ctypes.c_uint32, _vp, _vp, _vp,
@@ -351,10 +353,14 @@ class Graph:
         return out.reshape(virtual_ranks, trials_per_rank)
 
     # ApproximateCut::run
-    def approx_cut(self, success_probability=0.9, seed=0, virtual_ranks=1):
+    def approx_cut(self, success_probability=0.9, seed=0, virtual_ranks=1, seed_replay=False):
+        """seed_replay: draw the reference's own random numbers (sitmo(seed + r) through
+        libstdc++'s binomial_distribution), so the answer equals the reference executable's;
+        unit edge weights only."""
         res = ApproxResult()
-        _check(lib().cac_approx_cut(self.ctx.h, self.h, success_probability, seed, virtual_ranks, ctypes.byref(res)),
-               "cac_approx_cut")
+        fn, name = ((lib().cac_approx_cut_seed_replay, "cac_approx_cut_seed_replay") if seed_replay
+                    else (lib().cac_approx_cut, "cac_approx_cut"))
+        _check(fn(self.ctx.h, self.h, success_probability, seed, virtual_ranks, ctypes.byref(res)), name)
         return res
 
 

@@ -33,9 +33,12 @@ int main(int argc, char *argv[]) {
         if (st) return cli_fail("cac_graph_load_file", st);
         cac_graph_info(g, &n, &m, nullptr);
     }
+    // CAC_SEED_REPLAY=1: the reference's own draws, so the line equals the reference's (unit weights)
+    const bool replay = cli_seed_replay();
     cac_approx_result res{};
-    st = cac_approx_cut(ctx, g, success_probability, seed, ranks, &res);
-    if (st) return cli_fail("cac_approx_cut", st);
+    st = replay ? cac_approx_cut_seed_replay(ctx, g, success_probability, seed, ranks, &res)
+                : cac_approx_cut(ctx, g, success_probability, seed, ranks, &res);
+    if (st) return cli_fail(replay ? "cac_approx_cut_seed_replay" : "cac_approx_cut", st);
     std::cout << std::fixed;
     std::cout << argv[2] << "," << seed << "," << ranks << "," << n << "," << m << "," << res.device_ms / 1000.0
               << "," << 0.0 << "," << res.trials << "," << res.cut << std::endl;

@@ -15,6 +15,13 @@ inline unsigned cli_virtual_ranks() {
     return v > 0 ? (unsigned)v : 1;
 }
 
+// CAC_SEED_REPLAY=1 asks for the reference's own random draws where a command line offers them
+// (approx_cut: cac_approx_cut_seed_replay).
+inline bool cli_seed_replay() {
+    const char *s = std::getenv("CAC_SEED_REPLAY");
+    return s && *s && std::string(s) != "0";
+}
+
 inline int cli_device() {
     const char *s = std::getenv("CAC_DEVICE");
     return s && *s ? std::atoi(s) : 0;

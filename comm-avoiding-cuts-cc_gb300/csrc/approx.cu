@@ -15,11 +15,31 @@
 // products; x is draw e_local of stream (seed + r, i, j, 1), r the virtual rank whose slice
 // holds the edge (ApproximateCut::loadFromInput, ApproximateCut.hpp:64-68) and e_local its
 // index in that slice. oracle/approx.c replays the same rule on the host.
+//
+// The level count is the reference's ceil(ln w) of each rank's own slice weight (`w` at :19-30
+// is the calling rank's local sum), the smallest over ranks: the ranks step through the levels'
+// collectives together, so the reference's run is defined only while every rank is still in its
+// loop, and the smallest count gives its answer wherever it has one.
+//
+// Seed replay (approx_run with ref_stream): the keep test instead consumes the reference's own
+// draws. Rank r's engine is sitmo::prng_engine(seed + r) (ApproximateCut.hpp:35, .cpp:33), read in
+// the reference's order: per level, for each copy, for each slice edge one
+// std::binomial_distribution<int>(w, 2^-i) draw, then one raw output for the level's CC seed
+// (:50-58). With w = 1 that draw (libstdc++'s waiting-time method) takes exactly one
+// generate_canonical<double, 53> value U from the two outputs x0, x1 as (x0 + x1 2^32) / 2^64,
+// and returns 1 iff -ln(1 - U) <= -ln(1 - 2^-i). So the draw for copy j and slice edge e of
+// level i reads outputs k and k + 1, k = (i - 1) (2 C len_r + 1) + 2 (j len_r + e), and every
+// edge of every copy is tested independently on the device. The comparison is made on
+// 1 - U >= 1 - 2^-i directly (see stream_keep), which decides exactly as the logarithms do.
+// Graphs with other weights draw a variable number of outputs per edge (a sequential chain per
+// rank), so the replay takes unit weights only.
 #include "cac_internal.h"
 #include "sitmo.cuh"
 
 #include <algorithm>
 #include <cmath>
+#include <cstring>
+#include <vector>
 
 namespace cac {
 namespace {
@@ -129,6 +149,92 @@ __global__ void approx_keep_hook4(uint32_t *par, const uint32_t *__restrict__ U,
     }
 }
 
+// Binomial(1, p) > 0 on the reference's draws: U = generate_canonical<double, 53> of outputs x0, x1
+// (x0 + x1 2^32 in double, scaled by 2^-64, clamped below 1); kept iff -ln(1 - U) <= -ln(1 - p)
+// (libstdc++'s waiting-time test with t = 1). ln is increasing, and for p = 2^-i <= 1/2 every
+// double next to 1 - p lies at least two units in the last place of ln(1 - p) away from it in
+// logarithm, so any logarithm accurate to within one unit orders 1 - U and 1 - p the same way:
+// the test is 1 - U >= 1 - p, in double arithmetic, rounded exactly as the reference rounds it.
+__device__ __forceinline__ bool stream_keep(uint32_t x0, uint32_t x1, double one_minus_p) {
+    const double s = __dadd_rn((double)x0, __dmul_rn((double)x1, 4294967296.0));
+    double U = __dmul_rn(s, 0x1p-64);
+    if (U >= 1.0) U = 0x1.fffffffffffffp-1;
+    return __dadd_rn(1.0, -U) >= one_minus_p;
+}
+
+__device__ __forceinline__ uint64_t word_of(const u64x4 &b, unsigned i) {
+    return i == 0 ? b.x[0] : i == 1 ? b.x[1] : i == 2 ? b.x[2] : b.x[3];
+}
+
+// Seed replay, unit weights: one thread per (copy, quad of 4 slice edges), quads numbered as in
+// approx_keep_hook4. The quad's 4 draws read 8 consecutive outputs of the rank's engine, which lie
+// in one or two sitmo blocks (output k = half k & 1 of word (k >> 1) & 3 of block k >> 3, low half
+// first: lib/prng_engine.hpp:195-212).
+__global__ void approx_stream_keep_hook(uint32_t *par, const uint32_t *__restrict__ U, const uint32_t *__restrict__ V,
+                                        uint64_t m, uint32_t n, uint32_t level, double one_minus_p, uint32_t copies,
+                                        uint32_t seed, uint32_t ranks, uint64_t portion, uint64_t Qf, uint64_t q0,
+                                        uint64_t q1) {
+    const uint32_t j = blockIdx.y;
+    const uint32_t off = j * n;
+    for (uint64_t gq = q0 + (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; gq < q1;
+         gq += (uint64_t)gridDim.x * blockDim.x) {
+        uint32_t r;
+        uint64_t lq;
+        if (portion == 0) {
+            r = ranks - 1;
+            lq = gq;
+        } else {
+            const uint64_t rr = gq / Qf;
+            r = rr < ranks - 1 ? (uint32_t)rr : ranks - 1;
+            lq = gq - (uint64_t)r * Qf;
+        }
+        const uint64_t base = (uint64_t)r * portion;
+        const uint64_t len = r + 1 < ranks ? portion : m - base;
+        const uint64_t k0 = (uint64_t)(level - 1) * (2 * (uint64_t)copies * len + 1) + 2 * ((uint64_t)j * len + 4 * lq);
+        const uint64_t b0 = k0 >> 3;
+        const uint32_t key = seed + r;
+        const u64x4 A = sitmo_block(key, 0, 0, 0, b0, 0, 0, 0);
+        const u64x4 B = ((k0 + 7) >> 3) != b0 ? sitmo_block(key, 0, 0, 0, b0 + 1, 0, 0, 0) : A;
+        auto out = [&](uint64_t k) -> uint32_t {
+            const uint64_t wd = word_of((k >> 3) == b0 ? A : B, (unsigned)(k >> 1) & 3u);
+            return (k & 1) ? (uint32_t)(wd >> 32) : (uint32_t)wd;
+        };
+#pragma unroll
+        for (int k = 0; k < 4; k++) {
+            const uint64_t local = 4 * lq + k;
+            if (local >= len) break;
+            if (!stream_keep(out(k0 + 2 * k), out(k0 + 2 * k + 1), one_minus_p)) continue;
+            aunite(par, U[base + local] + off, V[base + local] + off);
+        }
+    }
+}
+
+// Weight sum of every rank's slice and the number of edges whose weight is not 1. Slices as
+// GraphInputIterator::loadSlice (src/input/GraphInputIterator.hpp:77-93): rank r < P - 1 owns
+// [r portion, (r + 1) portion), the last rank the rest. Ranks along blockIdx.y (strided).
+__global__ void approx_slice_stats(const uint32_t *__restrict__ w, uint64_t m, uint32_t ranks, uint64_t portion,
+                                   unsigned long long *sums, unsigned int *nonunit) {
+    for (uint32_t r = blockIdx.y; r < ranks; r += gridDim.y) {
+        const uint64_t from = (uint64_t)r * portion, to = r + 1 < ranks ? from + portion : m;
+        unsigned long long acc = 0;
+        uint32_t odd = 0;
+        for (uint64_t e = from + (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; e < to;
+             e += (uint64_t)gridDim.x * blockDim.x) {
+            const uint32_t x = w[e];
+            acc += x;
+            odd += x != 1u;
+        }
+        for (int o = 16; o > 0; o >>= 1) {
+            acc += __shfl_xor_sync(0xffffffffu, acc, o);
+            odd += __shfl_xor_sync(0xffffffffu, odd, o);
+        }
+        if ((threadIdx.x & 31) == 0) {
+            if (acc) atomicAdd(&sums[r], acc);
+            if (odd) atomicAdd(nonunit, odd);
+        }
+    }
+}
+
 // Full path compression (read-only walks; only roots are written).
 __global__ void approx_compress(uint32_t *par, uint64_t nv) {
     for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < nv; i += (uint64_t)gridDim.x * blockDim.x) {
@@ -149,7 +255,11 @@ __global__ void approx_count_roots(const uint32_t *par, uint64_t nv, unsigned in
 
 }  // namespace
 
-int approx_run(cac_ctx *ctx, const cac_graph *g, double p, uint32_t seed, uint32_t ranks, cac_approx_result *res) {
+// ApproximateCut.cpp:30: (unsigned) ceil(log(w)), w a rank's slice weight (none for w = 0)
+static uint32_t level_count(uint64_t w) { return w ? (uint32_t)std::ceil(std::log((double)w)) : 0; }
+
+int approx_run(cac_ctx *ctx, const cac_graph *g, double p, uint32_t seed, uint32_t ranks, bool ref_stream,
+               cac_approx_result *res) {
     cudaStream_t s = ctx->stream;
     *res = cac_approx_result{};
     const uint32_t copies = approx_copies(p);
@@ -159,25 +269,65 @@ int approx_run(cac_ctx *ctx, const cac_graph *g, double p, uint32_t seed, uint32
         set_error("approx_cut: n * copies must stay below 2^32");
         return CAC_ERR_UNSUPPORTED;
     }
-    // ApproximateCut.cpp:30: (unsigned) ceil(log(w)); levels beyond 63 cannot occur for 64-bit sums
-    const uint32_t iterations = g->total_weight ? (uint32_t)std::ceil(std::log((double)g->total_weight)) : 0;
-    CAC_TRY(arena_reserve(ctx, align_up(nv * 4 + 4) + 256));
+    const uint64_t portion = g->m / ranks;
+    const bool stats = ranks > 1 || ref_stream;
+    CAC_TRY(arena_reserve(ctx, align_up(nv * 4 + 4) + 256 + (stats ? align_up((uint64_t)ranks * 8 + 8) : 0)));
     arena_reset(ctx);
     uint32_t *par = (uint32_t *)arena_take(ctx, nv * 4 + 4);
     unsigned int *d_count = (unsigned int *)arena_take(ctx, 16);
-    const uint64_t portion = g->m / ranks;
+    CAC_CUDA_TRY(cudaEventRecord(ctx->ev[0], s));
+    // levels: the smallest ceil(ln w_r) over the ranks' slices; one rank: the graph's total weight
+    uint32_t iterations = level_count(g->total_weight);
+    if (stats) {
+        unsigned long long *d_sums = (unsigned long long *)arena_take(ctx, (uint64_t)ranks * 8 + 8);
+        unsigned int *d_nonunit = (unsigned int *)(d_sums + ranks);
+        CAC_CUDA_TRY(cudaMemsetAsync(d_sums, 0, (uint64_t)ranks * 8 + 8, s));
+        const uint64_t longest = g->m - (uint64_t)(ranks - 1) * portion;
+        const uint32_t gy = std::min<uint32_t>(ranks, 65535u);
+        const uint32_t gx = (uint32_t)std::max<uint64_t>(
+            1, std::min<uint64_t>((longest + 4 * kThreads - 1) / (4 * kThreads),
+                                  std::max<uint64_t>(1, (uint64_t)ctx->num_sms * 8 / gy)));
+        approx_slice_stats<<<dim3(gx, gy), kThreads, 0, s>>>(g->w, g->m, ranks, portion, d_sums, d_nonunit);
+        CAC_CUDA_TRY(cudaGetLastError());
+        std::vector<unsigned long long> h((size_t)ranks + 1);
+        CAC_CUDA_TRY(cudaMemcpyAsync(h.data(), d_sums, (uint64_t)ranks * 8 + 8, cudaMemcpyDeviceToHost, s));
+        CAC_CUDA_TRY(cudaStreamSynchronize(s));
+        uint32_t nonunit;
+        std::memcpy(&nonunit, &h[ranks], 4);
+        if (ref_stream && nonunit) {
+            set_error("approx_cut seed replay: every edge weight must be 1 (a weighted edge draws a variable "
+                      "number of outputs)");
+            return CAC_ERR_UNSUPPORTED;
+        }
+        iterations = UINT32_MAX;
+        for (uint32_t r = 0; r < ranks; r++) iterations = std::min(iterations, level_count(h[r]));
+    }
     // quads of 4 edges per rank slice (see approx_keep_hook4)
     const uint64_t Qf = (portion + 3) / 4;
     const uint64_t Q = portion == 0 ? (g->m + 3) / 4 : (ranks - 1) * Qf + (g->m - (uint64_t)(ranks - 1) * portion + 3) / 4;
     const int gi = (int)std::max<uint64_t>(1, std::min<uint64_t>((nv + kThreads - 1) / kThreads, ctx->num_sms * 8));
-    CAC_CUDA_TRY(cudaEventRecord(ctx->ev[0], s));
     uint32_t first = 0;
     for (uint32_t level = 1; level <= iterations && level <= 63; level++) {
         approx_init<<<gi, kThreads, 0, s>>>(par, nv);
         // the kept edges are hooked in kSlices slices, the forest flattened after the first few
         // and the last (the same partition as one pass; one pass from singletons builds long
         // parent chains on large graphs)
-        if (Q < (1u << 16)) {
+        if (ref_stream) {
+            // binomial_distribution's 1 - p12 with p12 = std::pow(2, -int(i)) (ApproximateCut.cpp:37)
+            const double one_minus_p = 1.0 - std::pow(2.0, -(int)level);
+            const uint32_t slices = Q < (1u << 16) ? 1 : kSlices;
+            for (uint32_t sl = 0; sl < slices; sl++) {
+                const uint64_t q0 = Q * sl / slices, q1 = Q * (sl + 1) / slices;
+                if (q1 <= q0) continue;
+                const int ge = (int)std::max<uint64_t>(
+                    1, std::min<uint64_t>((q1 - q0 + kThreads - 1) / kThreads,
+                                          std::max(1, ctx->num_sms * 8 / (int)copies)));
+                approx_stream_keep_hook<<<dim3(ge, copies), kThreads, 0, s>>>(par, g->u, g->v, g->m, g->n, level,
+                                                                              one_minus_p, copies, seed, ranks,
+                                                                              portion, Qf, q0, q1);
+                if (sl < kCompressedSlices && sl + 1 < slices) approx_compress<<<gi, kThreads, 0, s>>>(par, nv);
+            }
+        } else if (Q < (1u << 16)) {
             if (g->m) {
                 const int ge = (int)std::max<uint64_t>(
                     1, std::min<uint64_t>((g->m + kThreads - 1) / kThreads, std::max(1, ctx->num_sms * 8 / (int)copies)));
@@ -186,7 +336,7 @@ int approx_run(cac_ctx *ctx, const cac_graph *g, double p, uint32_t seed, uint32
                                                            portion);
             }
         }
-        const uint32_t slices = Q < (1u << 16) ? 0 : kSlices;
+        const uint32_t slices = ref_stream || Q < (1u << 16) ? 0 : kSlices;
         for (uint32_t sl = 0; sl < slices; sl++) {
             const uint64_t q0 = Q * sl / slices, q1 = Q * (sl + 1) / slices;
             if (q1 <= q0) continue;

@@ -249,7 +249,9 @@ int ks_dense_one(cac_ctx *ctx, uint32_t n, const uint64_t *mat_host, uint32_t se
 int exact_small(cac_ctx *ctx, uint32_t n, const uint64_t *mat_host, uint64_t *cut);
 
 // ---- approx cut (approx.cu) ----
-int approx_run(cac_ctx *ctx, const cac_graph *g, double p, uint32_t seed, uint32_t ranks, cac_approx_result *res);
+// ref_stream: the reference's own draws (seed replay; unit weights only).
+int approx_run(cac_ctx *ctx, const cac_graph *g, double p, uint32_t seed, uint32_t ranks, bool ref_stream,
+               cac_approx_result *res);
 
 // ---- sitmo (sitmo_kernels.cu) ----
 int sitmo_blocks(cac_ctx *ctx, const uint64_t key[4], const uint64_t ctr0[4], uint64_t nblocks, uint64_t *out_host);

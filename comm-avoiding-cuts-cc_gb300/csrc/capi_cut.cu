@@ -199,7 +199,18 @@ int cac_approx_cut(cac_ctx *ctx, const cac_graph *g, double p, uint32_t seed, ui
     }
     if (virtual_ranks == 0) virtual_ranks = 1;
     CAC_CUDA_TRY(cudaSetDevice(ctx->device));
-    return approx_run(ctx, g, p, seed, virtual_ranks, res);
+    return approx_run(ctx, g, p, seed, virtual_ranks, false, res);
+}
+
+int cac_approx_cut_seed_replay(cac_ctx *ctx, const cac_graph *g, double p, uint32_t seed, uint32_t virtual_ranks,
+                               cac_approx_result *res) {
+    if (!ctx || !g || !res || !(p > 0.0 && p < 1.0)) {
+        set_error("cac_approx_cut_seed_replay: invalid argument (success probability must be in (0, 1))");
+        return CAC_ERR_INVALID;
+    }
+    if (virtual_ranks == 0) virtual_ranks = 1;
+    CAC_CUDA_TRY(cudaSetDevice(ctx->device));
+    return approx_run(ctx, g, p, seed, virtual_ranks, true, res);
 }
 
 }  // extern "C"

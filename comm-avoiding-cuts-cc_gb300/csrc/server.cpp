@@ -120,7 +120,7 @@ void graph_worker(cac_server *s) {
             st = run_cc(s->graph, r);
         } else {
             cac_approx_result ar{};
-            st = approx_run(s->graph, r->req.graph, r->req.success_probability, r->req.seed, r->ranks, &ar);
+            st = approx_run(s->graph, r->req.graph, r->req.success_probability, r->req.seed, r->ranks, false, &ar);
             r->resp.cut = ar.cut;
             r->resp.trials = ar.trials;
         }

@@ -209,6 +209,17 @@ typedef struct {
 int cac_approx_cut(cac_ctx *ctx, const cac_graph *g, double success_probability, uint32_t seed,
                    uint32_t virtual_ranks, cac_approx_result *res);
 
+/* approx_cut on the reference's own random draws (seed replay): virtual rank r reads
+ * sitmo::prng_engine(seed + r) in the reference's order through std::binomial_distribution<int>
+ * as libstdc++ (GCC 13) implements it (ApproximateCut.cpp:33-58), so the answer is the one the
+ * reference's approx_cut prints under `mpiexec -n virtual_ranks` with the same seed, where that
+ * run is defined. Every edge weight must be 1 (CAC_ERR_UNSUPPORTED otherwise: a weighted edge
+ * draws a variable number of outputs, which chains the draws of a rank). Both entry points run
+ * min over ranks of ceil(ln w_r) levels, w_r the weight of rank r's slice (the reference's
+ * local `w`, ApproximateCut.cpp:19-30). */
+int cac_approx_cut_seed_replay(cac_ctx *ctx, const cac_graph *g, double success_probability, uint32_t seed,
+                               uint32_t virtual_ranks, cac_approx_result *res);
+
 /* ---- synthetic graphs generated on the device ----
  * Replaces the reference's external generators (utils/generate.py:10-32, er_generator.cpp,
  * sw_generator.cpp, input_generators/rmat_driver.sh:13-16) for the benchmark families. The edge

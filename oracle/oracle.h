@@ -94,6 +94,15 @@ uint64_t orc_keep_threshold(uint32_t level, uint32_t w);
 /* Returns the cut estimate 2^level; *levels_out (nullable) = first disconnected level. */
 uint64_t orc_approx_cut(uint32_t n, uint64_t m, const uint32_t *u, const uint32_t *v, const uint32_t *w,
                         double success_probability, uint32_t seed, uint32_t ranks, uint32_t *levels_out);
+/* The same run on the reference's own draws (libstdc++ binomial_distribution on
+ * sitmo::prng_engine(seed + r)); returns 0 where a draw leaves the restated regime
+ * (weight * 2^-level >= 8). */
+uint64_t orc_approx_cut_stream(uint32_t n, uint64_t m, const uint32_t *u, const uint32_t *v, const uint32_t *w,
+                               double success_probability, uint32_t seed, uint32_t ranks, uint32_t *levels_out);
+/* `count` consecutive draws binomial_distribution<int>(w[k % nw], 2^-level) on
+ * sitmo::prng_engine(seed), then the engine's next raw output; -1 outside the restated regime. */
+int orc_ref_binomial_draws(uint32_t seed, uint32_t level, uint64_t count, const uint32_t *w, uint32_t nw,
+                           int32_t *draws, uint32_t *next_output);
 
 #ifdef __cplusplus
 }

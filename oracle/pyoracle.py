@@ -68,6 +68,11 @@ def lib():
         L.orc_approx_cut.argtypes = [ctypes.c_uint32, ctypes.c_uint64, _u32p, _u32p, _u32p, ctypes.c_double,
                                      ctypes.c_uint32, ctypes.c_uint32, _u32p]
         L.orc_approx_cut.restype = ctypes.c_uint64
+        L.orc_approx_cut_stream.argtypes = L.orc_approx_cut.argtypes
+        L.orc_approx_cut_stream.restype = ctypes.c_uint64
+        L.orc_ref_binomial_draws.argtypes = [ctypes.c_uint32, ctypes.c_uint32, ctypes.c_uint64, _u32p, ctypes.c_uint32,
+                                             ctypes.POINTER(ctypes.c_int32), _u32p]
+        L.orc_ref_binomial_draws.restype = ctypes.c_int
         _LIB = L
     return _LIB
 
@@ -213,3 +218,24 @@ def approx_cut(n, u, v, w, p, seed, ranks=1):
     lv = np.zeros(1, dtype=np.uint32)
     cut = lib().orc_approx_cut(n, len(u), _p32(u), _p32(v), _p32(w), p, seed, ranks, _p32(lv))
     return int(cut), int(lv[0])
+
+
+def approx_cut_stream(n, u, v, w, p, seed, ranks=1):
+    """approx_cut on the reference's own draws (sitmo::prng_engine(seed + r) through libstdc++'s
+    binomial_distribution, src/ApproximateCut.cpp:33-58). Returns (cut, level); None where a draw
+    leaves the restated regime (weight * 2^-level >= 8)."""
+    u, v, w = _c32(u), _c32(v), _c32(w)
+    lv = np.zeros(1, dtype=np.uint32)
+    cut = lib().orc_approx_cut_stream(n, len(u), _p32(u), _p32(v), _p32(w), p, seed, ranks, _p32(lv))
+    return None if cut == 0 else (int(cut), int(lv[0]))
+
+
+def ref_binomial_draws(seed, level, count, weights):
+    """`count` draws binomial_distribution<int>(weights[k % len], 2^-level) on
+    sitmo::prng_engine(seed), and the engine's next raw output."""
+    w = _c32(weights)
+    out = np.zeros(max(count, 1), dtype=np.int32)
+    nxt = np.zeros(1, dtype=np.uint32)
+    st = lib().orc_ref_binomial_draws(seed, level, count, _p32(w), len(w),
+                                      out.ctypes.data_as(ctypes.POINTER(ctypes.c_int32)), _p32(nxt))
+    return None if st else (out[:count].tolist(), int(nxt[0]))

@@ -74,6 +74,24 @@ CUT_SPECS = [
 ]
 
 
+# graphs whose approx_cut answers (one per seed) are taken from the reference's approx_cut
+# executable, to pin the replay of its own draws; "unit": every weight 1
+APPROX_SPECS = [
+    {"name": "er_200_dense", "kind": "er", "n": 200, "p": 0.3, "seed": 31, "wmax": 1, "unit": True},
+    {"name": "er_400", "kind": "er", "n": 400, "p": 0.08, "seed": 32, "wmax": 1, "unit": True},
+    {"name": "k_60", "kind": "complete", "n": 60, "seed": 33, "wmax": 1, "unit": True},
+    {"name": "ws_300_24", "kind": "ws", "n": 300, "k": 24, "p": 0.3, "seed": 34, "wmax": 1, "unit": True},
+    {"name": "ba_800_12", "kind": "ba", "n": 800, "attach": 12, "seed": 35, "unit": True},
+    {"name": "er_200_w15", "kind": "er", "n": 200, "p": 0.06, "seed": 24, "wmax": 15},
+    {"name": "er_m_600_w9", "kind": "er_m", "n": 600, "deg": 6, "seed": 25, "wmax": 9},
+]
+APPROX_SEEDS = list(range(16))
+
+# (seed, level, count, weights) of the binomial_distribution draws dumped by binom_stream
+BINOM_CASES = [(s, lv, cnt, ws) for s in (0, 1, 42, 4294967295)
+               for lv, cnt, ws in ((1, 64, (1,)), (2, 64, (1,)), (5, 40, (1,)), (1, 50, (1, 2, 7, 15, 0)),
+                                   (3, 50, (3, 14, 1)), (9, 30, (15, 1)), (40, 20, (1,)))]
+
 # (vertices, ranks, seed) of the CLICK graphs pinned against the reference's generator
 CLICK_CASES = [(2, 1, 0), (12, 2, 5), (50, 1, 0), (101, 3, 7), (120, 4, 11), (700, 5, 42), (2000, 1, 3)]
 
@@ -155,6 +173,26 @@ def main():
             ks.append({"n": int(n), "p": p, "trials": int(t)})
     with open(os.path.join(HERE, "ks_trials.json"), "w") as f:
         json.dump(ks, f, indent=0)
+    # 6. approx_cut on the reference's own draws: binomial_distribution draws on the sitmo engine
+    # (oracle/refbuild's binom_stream harness) and the approx_cut executable's answers
+    binom = []
+    for seed, level, cnt, ws in BINOM_CASES:
+        head, tail = run("binom_stream", seed, level, cnt, *ws).split(":")
+        binom.append({"seed": seed, "level": level, "count": cnt, "weights": list(ws),
+                      "draws": [int(x) for x in head.split()], "next_output": int(tail)})
+    runs = []
+    with tempfile.TemporaryDirectory() as td:
+        for spec in APPROX_SPECS:
+            n, u, v, w = make_spec(spec)
+            if spec.get("unit"):
+                w = np.ones_like(u)
+            path = os.path.join(td, spec["name"] + ".in")
+            graphgen.write_graph(path, n, u, v, w, spec["name"])
+            answers = [int(run("approx_cut", 0.9, path, sd).strip().split(",")[-1]) for sd in APPROX_SEEDS]
+            runs.append(dict(spec, m=int(len(u)), edges_sha256=digest(np.concatenate([u, v, w])), success_probability=0.9,
+                             seeds=APPROX_SEEDS, weights=answers))
+    with open(os.path.join(HERE, "approx_stream.json"), "w") as f:
+        json.dump({"binomial": binom, "runs": runs}, f, indent=1)
     with open(os.path.join(HERE, "click.json"), "w") as f:
         json.dump(out_click, f, indent=1)
     with open(os.path.join(HERE, "cc_seeded.json"), "w") as f:

@@ -61,3 +61,69 @@ def test_quad_path_large_graph(ctx, ranks):
     for seed in (0, 6):
         res = g.approx_cut(0.9, seed=seed, virtual_ranks=ranks)
         assert (res.cut, res.level) == O.approx_cut(n, u, v, w, 0.9, seed, ranks)
+
+
+# ---- seed replay: the reference's own draws (cac_approx_cut_seed_replay) ----
+
+def _approx_stream_graph(spec):
+    import numpy as np
+    n, u, v, w = make_graph(spec)
+    if spec.get("unit"):
+        w = np.ones_like(u)
+    return n, u, v, w
+
+
+def test_seed_replay_equals_reference_executable(golden, ctx):
+    """The answers of the reference's approx_cut executable (one rank), seed by seed, on the
+    unit-weight graphs of approx_stream.json."""
+    runs = [r for r in golden("approx_stream.json")["runs"] if r.get("unit")]
+    assert len(runs) == 5
+    for spec in runs:
+        n, u, v, w = _approx_stream_graph(spec)
+        g = ctx.graph(n, u, v, w)
+        got = [g.approx_cut(spec["success_probability"], seed=sd, seed_replay=True).cut for sd in spec["seeds"]]
+        assert got == spec["weights"], spec["name"]
+
+
+@pytest.mark.parametrize("ranks", [2, 3, 4])
+def test_seed_replay_ranks_match_oracle(golden, ctx, ranks):
+    """Several virtual ranks: slice r draws from sitmo(seed + r) at the reference's positions
+    (levels after the first start at odd outputs: the CC seed takes one per level)."""
+    for spec in [r for r in golden("approx_stream.json")["runs"] if r.get("unit")]:
+        n, u, v, w = _approx_stream_graph(spec)
+        g = ctx.graph(n, u, v, w)
+        for sd in (0, 3, 9):
+            res = g.approx_cut(0.9, seed=sd, virtual_ranks=ranks, seed_replay=True)
+            assert (res.cut, res.level) == O.approx_cut_stream(n, u, v, w, 0.9, sd, ranks), (spec["name"], sd)
+
+
+@pytest.mark.parametrize("ranks", [1, 3])
+def test_seed_replay_large_graph(ctx, ranks):
+    """More than 2^16 quads (hooks in slices), m not a multiple of 4 or of the rank count."""
+    import numpy as np
+    n, u, v, _ = graphgen.erdos_renyi_m(12000, 48.0, 17, wmax=1)
+    u, v = u[:-3], v[:-3]
+    w = np.ones_like(u)
+    assert len(u) // 4 >= (1 << 16)
+    g = ctx.graph(n, u, v, w)
+    for sd in (0, 5):
+        res = g.approx_cut(0.95, seed=sd, virtual_ranks=ranks, seed_replay=True)
+        want = O.approx_cut_stream(n, u, v, w, 0.95, sd, ranks)
+        assert (res.cut, res.level) == want and res.level >= 2  # levels after the first start at odd outputs
+
+
+def test_seed_replay_refuses_weighted_graphs(ctx, libcac):
+    import cac
+    g = ctx.graph(3, [0, 1], [1, 2], [1, 2])
+    with pytest.raises(cac.CacError, match="weight"):
+        g.approx_cut(0.9, seed=0, seed_replay=True)
+
+
+def test_level_count_follows_rank_slices(ctx):
+    """ceil(ln w_r) of each rank's own slice, the smallest over ranks (ApproximateCut.cpp:19-30)."""
+    n, u, v, w = 4, [0, 1, 2, 0], [1, 2, 3, 3], [1, 1, 1, 100]
+    g = ctx.graph(n, u, v, w)
+    res = g.approx_cut(0.9, seed=0, virtual_ranks=4)
+    assert (res.cut, res.level) == (1, 0) == O.approx_cut(n, u, v, w, 0.9, 0, 4)
+    res = g.approx_cut(0.9, seed=0, virtual_ranks=2)  # slices of weight 2 and 101: one level
+    assert (res.cut, res.level) == O.approx_cut(n, u, v, w, 0.9, 0, 2)

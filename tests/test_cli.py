@@ -87,6 +87,21 @@ def test_approx_cut_csv(golden, tmp_path):
 
 
 @pytest.mark.gpu
+def test_approx_cut_seed_replay_prints_the_reference_line(golden, tmp_path):
+    """CAC_SEED_REPLAY=1: the answer the reference's approx_cut printed for the same file and seed."""
+    import numpy as np
+    spec = next(r for r in golden("approx_stream.json")["runs"] if r["name"] == "er_400")
+    n, u, v, _ = make_graph(spec)
+    path = _write(tmp_path, "er400.in", n, u, v, np.ones_like(u))
+    for sd in (0, 5, 11):
+        out = _run("approx_cut", "0.9", path, sd, env={"CAC_SEED_REPLAY": "1"})
+        assert out.returncode == 0, out.stderr
+        f = out.stdout.strip().split(",")
+        assert int(f[8]) == spec["weights"][sd]
+        assert int(f[7]) == 4 * (spec["weights"][sd].bit_length() - 1)
+
+
+@pytest.mark.gpu
 def test_malformed_file_fails_cleanly(tmp_path):
     p = tmp_path / "bad.graph"
     p.write_text("hdr\n5 2\n0 1 1\n")

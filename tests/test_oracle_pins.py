@@ -158,3 +158,45 @@ def test_threaded_iss_restatement_equals_sequential():
         c4, l4, r4 = O.cc_iss(n, u, v, 5, ranks, 4)
         assert (c1, r1) == (c4, r4) and c1 == want_count
         assert np.array_equal(l1, l4) and np.array_equal(l1, want)
+
+
+def approx_graph(spec):
+    """A graph of approx_stream.json, with unit weights where the spec says so."""
+    n, u, v, w = make_graph(spec)
+    if spec.get("unit"):
+        w = np.ones_like(u)
+    assert digest(np.concatenate([u, v, w])) == spec["edges_sha256"]
+    return n, u, v, w
+
+
+def test_binomial_stream_matches_libstdcxx(golden):
+    """binomial_distribution<int>(w, 2^-level) on sitmo::prng_engine(seed), as the reference's
+    approx_cut draws it: every draw and the engine position after them (its next raw output)."""
+    cases = golden("approx_stream.json")["binomial"]
+    assert len(cases) == 28
+    for c in cases:
+        got = O.ref_binomial_draws(c["seed"], c["level"], c["count"], c["weights"])
+        assert got == (c["draws"], c["next_output"]), c
+
+
+@pytest.mark.parametrize("idx", range(7))
+def test_approx_stream_oracle_matches_reference_executable(golden, idx):
+    """Every seed's answer of the reference's approx_cut executable (one rank) is reproduced by
+    the replay of its own draws."""
+    spec = golden("approx_stream.json")["runs"][idx]
+    n, u, v, w = approx_graph(spec)
+    got = [O.approx_cut_stream(n, u, v, w, spec["success_probability"], sd)[0] for sd in spec["seeds"]]
+    assert got == spec["weights"]
+
+
+def test_approx_level_count_follows_rank_slices():
+    """The level count is ceil(ln w_r) of each rank's own slice (ApproximateCut.cpp:19-30), the
+    smallest over ranks: a slice of weight 1 allows no level, so the answer is 2^0."""
+    n = 4
+    u = np.array([0, 1, 2, 0], dtype=np.uint32)
+    v = np.array([1, 2, 3, 3], dtype=np.uint32)
+    w = np.array([1, 1, 1, 100], dtype=np.uint32)  # slices of 4 ranks: weights 1, 1, 1, 100
+    assert O.approx_cut(n, u, v, w, 0.9, 0, 4) == (1, 0)
+    assert O.approx_cut_stream(n, u, v, w, 0.9, 0, 4) == (1, 0)
+    # one rank: ceil(ln 103) = 5 levels; the cycle's cut (2) disconnects by level 5
+    assert O.approx_cut(n, u, v, w, 0.9, 0, 1)[1] >= 1
