@@ -145,6 +145,35 @@ def _ks_workloads():
             ("square_root K4000 w[1,42]", graphgen.complete(4000, 0), 1, 3)]
 
 
+def _ks_work_model(t, trials_per_s, entry_bytes, hbm_peak, peak_kind):
+    """The Karger-Stein work model of one trial from a t-vertex root (recursion fan-out 2, children
+    of max(ceil(N / sqrt 2) + 1, 128) vertices, leaves of at most 128): bytes B(t) = sum over the
+    recursion nodes of [(N - N_t) 3 N + N^2 + N_t^2] entries plus N_b^2 per leaf, times the entry
+    width; leaf work = sum over the leaves of N_b^3 integer operations (Stoer-Wagner). Both are
+    reported against the trial rate: bytes against the measured HBM copy bandwidth, leaf work
+    against the issue peak of one 32-lane instruction per SM sub-partition per cycle
+    (152 SMs x 4 x 32 lanes x 2.07 GHz)."""
+    entries, ops, level = 0, 0, [t]
+    while level:
+        nxt = []
+        for nv in level:
+            if nv <= 128:
+                entries += nv * nv
+                ops += nv ** 3
+            else:
+                nt = max(int(math.ceil(nv / math.sqrt(2))) + 1, 128)
+                entries += (nv - nt) * 3 * nv + nv * nv + nt * nt
+                nxt += [nt, nt]
+        level = nxt
+    b = entries * entry_bytes
+    issue_peak = 152 * 4 * 32 * 2.07e9
+    return {"root_vertices": t, "entry_bytes": entry_bytes, "bytes_per_trial": b,
+            "achieved_gbs": b * trials_per_s / 1e9, "hbm_peak_gbs": hbm_peak, "peak": peak_kind,
+            "hbm_frac": b * trials_per_s / 1e9 / hbm_peak, "leaf_ops_per_trial": ops,
+            "leaf_tops": ops * trials_per_s / 1e12, "issue_peak_tops": issue_peak / 1e12,
+            "issue_frac": ops * trials_per_s / issue_peak}
+
+
 def _ks_also(ctx):
     """Karger-Stein trials/s of the square_root path (the other half of the metric), each next to a
     bounded sample of the oracle's CPU replay of the same trials on every host core."""
@@ -186,9 +215,13 @@ def _ks_also(ctx):
             filled = {"queries": len(seeds), "trials": sum(r.total_trials for r in rs),
                       "trials_per_s": sum(r.total_trials for r in rs) / bs, "ms_per_batch": bs * 1e3,
                       "timing": "host wall clock around cac_mincut_batch"}
+        peak, peak_kind = _peaks()
+        tps = trials / (statistics.median(ms) / 1e3)
         out.append({"workload": name, "trials": trials, "cut": int(res.cut),
                     "min_weighted_degree": int(deg.min()), "ms_per_query": statistics.median(ms),
-                    "trials_per_s": trials / (statistics.median(ms) / 1e3),
+                    "trials_per_s": tps,
+                    "work_model": _ks_work_model(res.intermediate, tps, 4 if int(w.astype(np.uint64).sum()) < 2 ** 32
+                                                 else 8, peak, peak_kind),
                     "cpu_baseline": {"trials_per_s": cpu_trials / cpu_s, "cores": cores, "kind": "port",
                                      "sample": "%d trial(s) of the oracle's replay on %d host threads"
                                                % (cpu_trials, cores),
@@ -228,6 +261,9 @@ def run_ks(args, rank, world):
             "config": {"workload": name, "vertices": n, "edges": int(len(u)), "virtual_ranks": ranks,
                        "trials_per_query": res.total_trials, "intermediate_size": res.intermediate},
             "clocks": clk.summary()}
+    peak, peak_kind = _peaks()
+    line["work_model"] = _ks_work_model(res.intermediate, res.total_trials / (total_ms / args.steps / 1e3),
+                                        4 if int(w.astype(np.uint64).sum()) < 2 ** 32 else 8, peak, peak_kind)
     if rank == 0:
         print(json.dumps(line))
     g.free()
