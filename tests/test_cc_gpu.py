@@ -220,3 +220,20 @@ def test_graph_with_an_endpoint_out_of_range_is_refused(ctx, libcac):
         ctx.graph(10, np.array([0, 3], np.uint32), np.array([1, 10], np.uint32))
     assert e.value.status == -1
     assert ctx.graph(10, np.array([0, 3], np.uint32), np.array([1, 9], np.uint32)).connected_components()[0] == 8
+
+
+@pytest.mark.slow
+def test_full_size_rmat_scale_22(ctx):
+    """R-MAT scale 22 (4,194,304 vertices, 67,108,864 edges, generated on the device): labels
+    identical to the closed-form labels, device-resident and through the one-call host entry point."""
+    g = ctx.generate("rmat", seed=0, scale=22, edge_factor=16)
+    n = 1 << 22
+    u, v, _ = g.edges()
+    assert len(u) == 67108864
+    want_count, want = O.cc_labels(n, u, v)
+    count, lab, _ = g.connected_components(seed=0, virtual_ranks=4)
+    assert count == want_count
+    assert np.array_equal(lab, want)
+    lab2 = np.full(n, 0xFFFFFFFF, np.uint32)
+    res = ctx.cc_edges(n, u, v, seed=0, virtual_ranks=4, labels=lab2)
+    assert res.num_components == want_count and np.array_equal(lab2, want)

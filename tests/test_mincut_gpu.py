@@ -239,3 +239,23 @@ def test_shared_row_quotient_trials_match_replay(ctx, big):
     got = ctx.graph(n, u, v, w).trials(seed=5, virtual_ranks=1, trials_per_rank=2)
     for i in range(2):
         assert int(got[0, i]) == O.mincut_trial(n, u, v, w, 5, 0, i)
+
+
+@pytest.mark.slow
+def test_full_size_k4000_trials_match_replay(ctx):
+    """The square_root configuration K4000 with weights in [1, 42] at full size: 7 trials, every
+    trial value equal to the oracle's replay of the same counter stream (the trials replayed on
+    host threads at once), and the answer is the minimum weighted degree."""
+    from concurrent.futures import ThreadPoolExecutor
+    n, u, v, w = graphgen.complete(4000, 0)
+    assert len(u) == 7998000 and O.number_of_trials(n, len(u), 0.95) == 7
+    g = ctx.graph(n, u, v, w)
+    res = g.square_root(0.95, seed=0)
+    got = g.trials(seed=0, virtual_ranks=1, trials_per_rank=7)[0]
+    with ThreadPoolExecutor(max_workers=7) as pool:
+        want = list(pool.map(lambda i: O.mincut_trial(n, u, v, w, 0, 0, i), range(7)))
+    assert [int(x) for x in got] == want
+    deg = np.zeros(n, np.uint64)
+    np.add.at(deg, u, w.astype(np.uint64))
+    np.add.at(deg, v, w.astype(np.uint64))
+    assert res.total_trials == 7 and res.cut == min(want) == int(deg.min())
