@@ -271,7 +271,11 @@ int approx_run(cac_ctx *ctx, const cac_graph *g, double p, uint32_t seed, uint32
     }
     const uint64_t portion = g->m / ranks;
     const bool stats = ranks > 1 || ref_stream;
-    CAC_TRY(arena_reserve(ctx, align_up(nv * 4 + 4) + 256 + (stats ? align_up((uint64_t)ranks * 8 + 8) : 0)));
+    // more ranks than edges: every slice but the last is empty, so no level runs; the slice
+    // statistics then only check the weights (one slice: the whole list)
+    const uint32_t sranks = portion == 0 ? 1u : ranks;
+    const uint64_t sportion = portion == 0 ? g->m : portion;
+    CAC_TRY(arena_reserve(ctx, align_up(nv * 4 + 4) + 256 + (stats ? align_up((uint64_t)sranks * 8 + 8) : 0)));
     arena_reset(ctx);
     uint32_t *par = (uint32_t *)arena_take(ctx, nv * 4 + 4);
     unsigned int *d_count = (unsigned int *)arena_take(ctx, 16);
@@ -279,28 +283,29 @@ int approx_run(cac_ctx *ctx, const cac_graph *g, double p, uint32_t seed, uint32
     // levels: the smallest ceil(ln w_r) over the ranks' slices; one rank: the graph's total weight
     uint32_t iterations = level_count(g->total_weight);
     if (stats) {
-        unsigned long long *d_sums = (unsigned long long *)arena_take(ctx, (uint64_t)ranks * 8 + 8);
-        unsigned int *d_nonunit = (unsigned int *)(d_sums + ranks);
-        CAC_CUDA_TRY(cudaMemsetAsync(d_sums, 0, (uint64_t)ranks * 8 + 8, s));
-        const uint64_t longest = g->m - (uint64_t)(ranks - 1) * portion;
-        const uint32_t gy = std::min<uint32_t>(ranks, 65535u);
+        unsigned long long *d_sums = (unsigned long long *)arena_take(ctx, (uint64_t)sranks * 8 + 8);
+        unsigned int *d_nonunit = (unsigned int *)(d_sums + sranks);
+        CAC_CUDA_TRY(cudaMemsetAsync(d_sums, 0, (uint64_t)sranks * 8 + 8, s));
+        const uint64_t longest = g->m - (uint64_t)(sranks - 1) * sportion;
+        const uint32_t gy = std::min<uint32_t>(sranks, 65535u);
         const uint32_t gx = (uint32_t)std::max<uint64_t>(
             1, std::min<uint64_t>((longest + 4 * kThreads - 1) / (4 * kThreads),
                                   std::max<uint64_t>(1, (uint64_t)ctx->num_sms * 8 / gy)));
-        approx_slice_stats<<<dim3(gx, gy), kThreads, 0, s>>>(g->w, g->m, ranks, portion, d_sums, d_nonunit);
+        approx_slice_stats<<<dim3(gx, gy), kThreads, 0, s>>>(g->w, g->m, sranks, sportion, d_sums, d_nonunit);
         CAC_CUDA_TRY(cudaGetLastError());
-        std::vector<unsigned long long> h((size_t)ranks + 1);
-        CAC_CUDA_TRY(cudaMemcpyAsync(h.data(), d_sums, (uint64_t)ranks * 8 + 8, cudaMemcpyDeviceToHost, s));
+        std::vector<unsigned long long> h((size_t)sranks + 1);
+        CAC_CUDA_TRY(cudaMemcpyAsync(h.data(), d_sums, (uint64_t)sranks * 8 + 8, cudaMemcpyDeviceToHost, s));
         CAC_CUDA_TRY(cudaStreamSynchronize(s));
         uint32_t nonunit;
-        std::memcpy(&nonunit, &h[ranks], 4);
+        std::memcpy(&nonunit, &h[sranks], 4);
         if (ref_stream && nonunit) {
             set_error("approx_cut seed replay: every edge weight must be 1 (a weighted edge draws a variable "
                       "number of outputs)");
             return CAC_ERR_UNSUPPORTED;
         }
         iterations = UINT32_MAX;
-        for (uint32_t r = 0; r < ranks; r++) iterations = std::min(iterations, level_count(h[r]));
+        for (uint32_t r = 0; r < sranks; r++) iterations = std::min(iterations, level_count(h[r]));
+        if (portion == 0 && ranks > 1) iterations = 0;
     }
     // quads of 4 edges per rank slice (see approx_keep_hook4)
     const uint64_t Qf = (portion + 3) / 4;

@@ -127,3 +127,15 @@ def test_level_count_follows_rank_slices(ctx):
     assert (res.cut, res.level) == (1, 0) == O.approx_cut(n, u, v, w, 0.9, 0, 4)
     res = g.approx_cut(0.9, seed=0, virtual_ranks=2)  # slices of weight 2 and 101: one level
     assert (res.cut, res.level) == O.approx_cut(n, u, v, w, 0.9, 0, 2)
+
+
+def test_more_ranks_than_edges(ctx):
+    """Every slice but the last is empty: no level runs (ceil(ln 0) levels on those ranks), in both
+    modes, however many ranks are asked for."""
+    n, u, v = 5, [0, 1, 2, 3], [1, 2, 3, 4]
+    g = ctx.graph(n, u, v, [1, 1, 1, 1])
+    for ranks in (5, 1 << 31):
+        for replay in (False, True):
+            res = g.approx_cut(0.9, seed=3, virtual_ranks=ranks, seed_replay=replay)
+            assert (res.cut, res.level) == (1, 0)
+    assert O.approx_cut(n, u, v, [1, 1, 1, 1], 0.9, 3, 5) == (1, 0)
