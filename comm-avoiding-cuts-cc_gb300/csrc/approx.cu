@@ -29,8 +29,9 @@
 // generate_canonical<double, 53> value U from the two outputs x0, x1 as (x0 + x1 2^32) / 2^64,
 // and returns 1 iff -ln(1 - U) <= -ln(1 - 2^-i). So the draw for copy j and slice edge e of
 // level i reads outputs k and k + 1, k = (i - 1) (2 C len_r + 1) + 2 (j len_r + e), and every
-// edge of every copy is tested independently on the device. The comparison is made on
-// 1 - U >= 1 - 2^-i directly (see stream_keep), which decides exactly as the logarithms do.
+// edge of every copy is tested independently on the device. The test is an integer comparison
+// of U 2^64 with a threshold per level (see stream_keep) that decides exactly as the logarithms
+// do; no floating point runs on the device.
 // Graphs with other weights draw a variable number of outputs per edge (a sequential chain per
 // rank), so the replay takes unit weights only.
 #include "cac_internal.h"
@@ -150,16 +151,27 @@ __global__ void approx_keep_hook4(uint32_t *par, const uint32_t *__restrict__ U,
 }
 
 // Binomial(1, p) > 0 on the reference's draws: U = generate_canonical<double, 53> of outputs x0, x1
-// (x0 + x1 2^32 in double, scaled by 2^-64, clamped below 1); kept iff -ln(1 - U) <= -ln(1 - p)
-// (libstdc++'s waiting-time test with t = 1). ln is increasing, and for p = 2^-i <= 1/2 every
-// double next to 1 - p lies at least two units in the last place of ln(1 - p) away from it in
-// logarithm, so any logarithm accurate to within one unit orders 1 - U and 1 - p the same way:
-// the test is 1 - U >= 1 - p, in double arithmetic, rounded exactly as the reference rounds it.
-__device__ __forceinline__ bool stream_keep(uint32_t x0, uint32_t x1, double one_minus_p) {
-    const double s = __dadd_rn((double)x0, __dmul_rn((double)x1, 4294967296.0));
-    double U = __dmul_rn(s, 0x1p-64);
-    if (U >= 1.0) U = 0x1.fffffffffffffp-1;
-    return __dadd_rn(1.0, -U) >= one_minus_p;
+// (x0 + x1 2^32 rounded to a double, scaled by 2^-64, clamped below 1); kept iff
+// -ln(1 - U) <= -ln(1 - p) (libstdc++'s waiting-time test with t = 1). ln is increasing, and for
+// p = 2^-i <= 1/2 every double next to b = 1 - p lies at least two units in the last place of
+// ln(b) away from it in logarithm, so any logarithm accurate to within one unit decides as
+// fl(1 - U) >= b does. That test is made here in integers: with R = U 2^64 (x0 + x1 2^32 rounded
+// to 53 significant bits, to nearest, ties to even), fl(1 - U) >= b iff 1 - R 2^-64 is at least
+// the midpoint between b and the double below it (a tie rounds to b, whose significand is even
+// for i <= 52), i.e. iff R <= T(i) with T(1) = 2^63 + 2^9 and T(i) = 2^(64-i) + 2^10 for
+// 2 <= i <= 52 (levels stop at ceil(ln W) <= 45). R = 2^64 is U = 1, clamped below 1: never kept.
+uint64_t stream_threshold(uint32_t level) {
+    return level == 1 ? (1ull << 63) + (1ull << 9) : (1ull << (64 - level)) + (1ull << 10);
+}
+
+__device__ __forceinline__ bool stream_keep(uint32_t x0, uint32_t x1, uint64_t T) {
+    const uint64_t S = ((uint64_t)x1 << 32) | x0;
+    const int sh = 11 - __clzll(S);  // bits below the 53-bit significand
+    if (sh <= 0) return S <= T;
+    const uint64_t q = S >> sh, rem = S & ((1ull << sh) - 1), half = 1ull << (sh - 1);
+    const uint64_t qr = q + ((rem > half || (rem == half && (q & 1))) ? 1 : 0);
+    if (qr >> (64 - sh)) return false;
+    return (qr << sh) <= T;
 }
 
 __device__ __forceinline__ uint64_t word_of(const u64x4 &b, unsigned i) {
@@ -171,7 +183,7 @@ __device__ __forceinline__ uint64_t word_of(const u64x4 &b, unsigned i) {
 // in one or two sitmo blocks (output k = half k & 1 of word (k >> 1) & 3 of block k >> 3, low half
 // first: lib/prng_engine.hpp:195-212).
 __global__ void approx_stream_keep_hook(uint32_t *par, const uint32_t *__restrict__ U, const uint32_t *__restrict__ V,
-                                        uint64_t m, uint32_t n, uint32_t level, double one_minus_p, uint32_t copies,
+                                        uint64_t m, uint32_t n, uint32_t level, uint64_t keep_max, uint32_t copies,
                                         uint32_t seed, uint32_t ranks, uint64_t portion, uint64_t Qf, uint64_t q0,
                                         uint64_t q1) {
     const uint32_t j = blockIdx.y;
@@ -203,7 +215,7 @@ __global__ void approx_stream_keep_hook(uint32_t *par, const uint32_t *__restric
         for (int k = 0; k < 4; k++) {
             const uint64_t local = 4 * lq + k;
             if (local >= len) break;
-            if (!stream_keep(out(k0 + 2 * k), out(k0 + 2 * k + 1), one_minus_p)) continue;
+            if (!stream_keep(out(k0 + 2 * k), out(k0 + 2 * k + 1), keep_max)) continue;
             aunite(par, U[base + local] + off, V[base + local] + off);
         }
     }
@@ -312,14 +324,14 @@ int approx_run(cac_ctx *ctx, const cac_graph *g, double p, uint32_t seed, uint32
     const uint64_t Q = portion == 0 ? (g->m + 3) / 4 : (ranks - 1) * Qf + (g->m - (uint64_t)(ranks - 1) * portion + 3) / 4;
     const int gi = (int)std::max<uint64_t>(1, std::min<uint64_t>((nv + kThreads - 1) / kThreads, ctx->num_sms * 8));
     uint32_t first = 0;
+    if (ref_stream) iterations = std::min<uint32_t>(iterations, 52);  // ceil(ln W) <= 45 for W < 2^64
     for (uint32_t level = 1; level <= iterations && level <= 63; level++) {
         approx_init<<<gi, kThreads, 0, s>>>(par, nv);
         // the kept edges are hooked in kSlices slices, the forest flattened after the first few
         // and the last (the same partition as one pass; one pass from singletons builds long
         // parent chains on large graphs)
         if (ref_stream) {
-            // binomial_distribution's 1 - p12 with p12 = std::pow(2, -int(i)) (ApproximateCut.cpp:37)
-            const double one_minus_p = 1.0 - std::pow(2.0, -(int)level);
+            const uint64_t keep_max = stream_threshold(level);  // p = 2^-level (ApproximateCut.cpp:37)
             const uint32_t slices = Q < (1u << 16) ? 1 : kSlices;
             for (uint32_t sl = 0; sl < slices; sl++) {
                 const uint64_t q0 = Q * sl / slices, q1 = Q * (sl + 1) / slices;
@@ -328,7 +340,7 @@ int approx_run(cac_ctx *ctx, const cac_graph *g, double p, uint32_t seed, uint32
                     1, std::min<uint64_t>((q1 - q0 + kThreads - 1) / kThreads,
                                           std::max(1, ctx->num_sms * 8 / (int)copies)));
                 approx_stream_keep_hook<<<dim3(ge, copies), kThreads, 0, s>>>(par, g->u, g->v, g->m, g->n, level,
-                                                                              one_minus_p, copies, seed, ranks,
+                                                                              keep_max, copies, seed, ranks,
                                                                               portion, Qf, q0, q1);
                 if (sl < kCompressedSlices && sl + 1 < slices) approx_compress<<<gi, kThreads, 0, s>>>(par, nv);
             }
