@@ -1,6 +1,8 @@
 // Drop-in for the reference's approx_cut executable (src/executables/approx_cut.cpp:5-43):
 // same arguments, same CSV line
 //   input,seed,p,n,m,cuttingTime,mpiTime,trials,weight
+// On unit-weight graphs the draws are the reference's own (seed replay), so the line carries the
+// reference's weight and trials for the same file, seed and CAC_VIRTUAL_RANKS.
 #include <iostream>
 #include <string>
 
@@ -33,12 +35,20 @@ int main(int argc, char *argv[]) {
         if (st) return cli_fail("cac_graph_load_file", st);
         cac_graph_info(g, &n, &m, nullptr);
     }
-    // CAC_SEED_REPLAY=1: the reference's own draws, so the line equals the reference's (unit weights)
-    const bool replay = cli_seed_replay();
+    // The reference's own draws where the graph allows them (unit weights), so the line equals the
+    // reference's; weighted graphs take the counter-addressed keep test unless CAC_SEED_REPLAY=1
+    // demands the replay (then they fail).
+    const int replay = cli_seed_replay();
     cac_approx_result res{};
-    st = replay ? cac_approx_cut_seed_replay(ctx, g, success_probability, seed, ranks, &res)
-                : cac_approx_cut(ctx, g, success_probability, seed, ranks, &res);
-    if (st) return cli_fail(replay ? "cac_approx_cut_seed_replay" : "cac_approx_cut", st);
+    st = CAC_ERR_UNSUPPORTED;
+    if (replay != 0) {
+        st = cac_approx_cut_seed_replay(ctx, g, success_probability, seed, ranks, &res);
+        if (st && (replay == 1 || st != CAC_ERR_UNSUPPORTED)) return cli_fail("cac_approx_cut_seed_replay", st);
+    }
+    if (st) {
+        st = cac_approx_cut(ctx, g, success_probability, seed, ranks, &res);
+        if (st) return cli_fail("cac_approx_cut", st);
+    }
     std::cout << std::fixed;
     std::cout << argv[2] << "," << seed << "," << ranks << "," << n << "," << m << "," << res.device_ms / 1000.0
               << "," << 0.0 << "," << res.trials << "," << res.cut << std::endl;

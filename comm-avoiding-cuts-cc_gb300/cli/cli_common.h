@@ -15,11 +15,13 @@ inline unsigned cli_virtual_ranks() {
     return v > 0 ? (unsigned)v : 1;
 }
 
-// CAC_SEED_REPLAY=1 asks for the reference's own random draws where a command line offers them
-// (approx_cut: cac_approx_cut_seed_replay).
-inline bool cli_seed_replay() {
+// The reference's own random draws where a command line offers them (approx_cut:
+// cac_approx_cut_seed_replay): CAC_SEED_REPLAY=1 requires them, 0 turns them off; unset, they are
+// used wherever the graph allows (approx_cut: unit edge weights). Returns 1, 0 or -1 (unset).
+inline int cli_seed_replay() {
     const char *s = std::getenv("CAC_SEED_REPLAY");
-    return s && *s && std::string(s) != "0";
+    if (!s || !*s) return -1;
+    return std::string(s) != "0" ? 1 : 0;
 }
 
 inline int cli_device() {

@@ -16,7 +16,11 @@ BIN = os.path.join(PKG, "bin")
 
 def _run(name, *args, env=None):
     e = dict(os.environ)
-    e.update(env or {})
+    for k, val in (env or {}).items():  # None: the variable is unset
+        if val is None:
+            e.pop(k, None)
+        else:
+            e[k] = val
     return subprocess.run([os.path.join(BIN, name)] + [str(a) for a in args], capture_output=True, text=True,
                           env=e, timeout=600)
 
@@ -94,11 +98,22 @@ def test_approx_cut_seed_replay_prints_the_reference_line(golden, tmp_path):
     n, u, v, _ = make_graph(spec)
     path = _write(tmp_path, "er400.in", n, u, v, np.ones_like(u))
     for sd in (0, 5, 11):
-        out = _run("approx_cut", "0.9", path, sd, env={"CAC_SEED_REPLAY": "1"})
-        assert out.returncode == 0, out.stderr
+        for mode in ("1", None):  # required, and the default on a unit-weight graph
+            out = _run("approx_cut", "0.9", path, sd, env={"CAC_SEED_REPLAY": mode})
+            assert out.returncode == 0, out.stderr
+            f = out.stdout.strip().split(",")
+            assert int(f[8]) == spec["weights"][sd]
+            assert int(f[7]) == 4 * (spec["weights"][sd].bit_length() - 1)
+        # turned off: the counter-addressed keep test
+        out = _run("approx_cut", "0.9", path, sd, env={"CAC_SEED_REPLAY": "0"})
+        want, level = O.approx_cut(n, u, v, np.ones_like(u), 0.9, sd, 1)
         f = out.stdout.strip().split(",")
-        assert int(f[8]) == spec["weights"][sd]
-        assert int(f[7]) == 4 * (spec["weights"][sd].bit_length() - 1)
+        assert out.returncode == 0 and int(f[8]) == want and int(f[7]) == 4 * level
+    # a weighted graph: the counter-addressed test by default, a clean failure when the replay is required
+    r = golden("ref_test_inputs.json")["complete_4.graph"]
+    wpath = _write(tmp_path, "k4.graph", r["n"], r["u"], r["v"], r["w"])
+    out = _run("approx_cut", "0.9", wpath, "3", env={"CAC_SEED_REPLAY": "1"})
+    assert out.returncode == 1 and "weight" in out.stderr
 
 
 @pytest.mark.gpu
