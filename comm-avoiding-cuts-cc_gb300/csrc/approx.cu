@@ -39,7 +39,6 @@
 
 #include <algorithm>
 #include <cmath>
-#include <cstring>
 #include <vector>
 
 namespace cac {
@@ -221,29 +220,19 @@ __global__ void approx_stream_keep_hook(uint32_t *par, const uint32_t *__restric
     }
 }
 
-// Weight sum of every rank's slice and the number of edges whose weight is not 1. Slices as
-// GraphInputIterator::loadSlice (src/input/GraphInputIterator.hpp:77-93): rank r < P - 1 owns
-// [r portion, (r + 1) portion), the last rank the rest. Ranks along blockIdx.y (strided).
-__global__ void approx_slice_stats(const uint32_t *__restrict__ w, uint64_t m, uint32_t ranks, uint64_t portion,
-                                   unsigned long long *sums, unsigned int *nonunit) {
+// Weight sum of every rank's slice. Slices as GraphInputIterator::loadSlice
+// (src/input/GraphInputIterator.hpp:77-93): rank r < P - 1 owns [r portion, (r + 1) portion), the
+// last rank the rest. Ranks along blockIdx.y (strided).
+__global__ void approx_slice_sums(const uint32_t *__restrict__ w, uint64_t m, uint32_t ranks, uint64_t portion,
+                                  unsigned long long *sums) {
     for (uint32_t r = blockIdx.y; r < ranks; r += gridDim.y) {
         const uint64_t from = (uint64_t)r * portion, to = r + 1 < ranks ? from + portion : m;
         unsigned long long acc = 0;
-        uint32_t odd = 0;
         for (uint64_t e = from + (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; e < to;
-             e += (uint64_t)gridDim.x * blockDim.x) {
-            const uint32_t x = w[e];
-            acc += x;
-            odd += x != 1u;
-        }
-        for (int o = 16; o > 0; o >>= 1) {
-            acc += __shfl_xor_sync(0xffffffffu, acc, o);
-            odd += __shfl_xor_sync(0xffffffffu, odd, o);
-        }
-        if ((threadIdx.x & 31) == 0) {
-            if (acc) atomicAdd(&sums[r], acc);
-            if (odd) atomicAdd(nonunit, odd);
-        }
+             e += (uint64_t)gridDim.x * blockDim.x)
+            acc += w[e];
+        for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
+        if ((threadIdx.x & 31) == 0 && acc) atomicAdd(&sums[r], acc);
     }
 }
 
@@ -282,42 +271,40 @@ int approx_run(cac_ctx *ctx, const cac_graph *g, double p, uint32_t seed, uint32
         return CAC_ERR_UNSUPPORTED;
     }
     const uint64_t portion = g->m / ranks;
-    const bool stats = ranks > 1 || ref_stream;
-    // more ranks than edges: every slice but the last is empty, so no level runs; the slice
-    // statistics then only check the weights (one slice: the whole list)
-    const uint32_t sranks = portion == 0 ? 1u : ranks;
-    const uint64_t sportion = portion == 0 ? g->m : portion;
-    CAC_TRY(arena_reserve(ctx, align_up(nv * 4 + 4) + 256 + (stats ? align_up((uint64_t)sranks * 8 + 8) : 0)));
+    if (ref_stream && !g->unit_weights) {
+        set_error("approx_cut seed replay: every edge weight must be 1 (a weighted edge draws a variable number "
+                  "of outputs)");
+        return CAC_ERR_UNSUPPORTED;
+    }
+    // Levels: the smallest ceil(ln w_r) over the ranks' slices. More ranks than edges leave every
+    // slice but the last empty: no level runs. Unit weights: w_r is the slice length; one rank:
+    // the graph's total weight; otherwise the slice sums are taken on the device.
+    const bool stats = ranks > 1 && portion > 0 && !g->unit_weights;
+    CAC_TRY(arena_reserve(ctx, align_up(nv * 4 + 4) + 256 + (stats ? align_up((uint64_t)ranks * 8) : 0)));
     arena_reset(ctx);
     uint32_t *par = (uint32_t *)arena_take(ctx, nv * 4 + 4);
     unsigned int *d_count = (unsigned int *)arena_take(ctx, 16);
     CAC_CUDA_TRY(cudaEventRecord(ctx->ev[0], s));
-    // levels: the smallest ceil(ln w_r) over the ranks' slices; one rank: the graph's total weight
     uint32_t iterations = level_count(g->total_weight);
-    if (stats) {
-        unsigned long long *d_sums = (unsigned long long *)arena_take(ctx, (uint64_t)sranks * 8 + 8);
-        unsigned int *d_nonunit = (unsigned int *)(d_sums + sranks);
-        CAC_CUDA_TRY(cudaMemsetAsync(d_sums, 0, (uint64_t)sranks * 8 + 8, s));
-        const uint64_t longest = g->m - (uint64_t)(sranks - 1) * sportion;
-        const uint32_t gy = std::min<uint32_t>(sranks, 65535u);
+    if (ranks > 1 && portion == 0) {
+        iterations = 0;
+    } else if (ranks > 1 && g->unit_weights) {
+        iterations = level_count(portion);  // the last slice holds at least `portion` edges
+    } else if (stats) {
+        unsigned long long *d_sums = (unsigned long long *)arena_take(ctx, (uint64_t)ranks * 8);
+        CAC_CUDA_TRY(cudaMemsetAsync(d_sums, 0, (uint64_t)ranks * 8, s));
+        const uint64_t longest = g->m - (uint64_t)(ranks - 1) * portion;
+        const uint32_t gy = std::min<uint32_t>(ranks, 65535u);
         const uint32_t gx = (uint32_t)std::max<uint64_t>(
             1, std::min<uint64_t>((longest + 4 * kThreads - 1) / (4 * kThreads),
                                   std::max<uint64_t>(1, (uint64_t)ctx->num_sms * 8 / gy)));
-        approx_slice_stats<<<dim3(gx, gy), kThreads, 0, s>>>(g->w, g->m, sranks, sportion, d_sums, d_nonunit);
+        approx_slice_sums<<<dim3(gx, gy), kThreads, 0, s>>>(g->w, g->m, ranks, portion, d_sums);
         CAC_CUDA_TRY(cudaGetLastError());
-        std::vector<unsigned long long> h((size_t)sranks + 1);
-        CAC_CUDA_TRY(cudaMemcpyAsync(h.data(), d_sums, (uint64_t)sranks * 8 + 8, cudaMemcpyDeviceToHost, s));
+        std::vector<unsigned long long> h(ranks);  // ranks <= m here
+        CAC_CUDA_TRY(cudaMemcpyAsync(h.data(), d_sums, (uint64_t)ranks * 8, cudaMemcpyDeviceToHost, s));
         CAC_CUDA_TRY(cudaStreamSynchronize(s));
-        uint32_t nonunit;
-        std::memcpy(&nonunit, &h[sranks], 4);
-        if (ref_stream && nonunit) {
-            set_error("approx_cut seed replay: every edge weight must be 1 (a weighted edge draws a variable "
-                      "number of outputs)");
-            return CAC_ERR_UNSUPPORTED;
-        }
         iterations = UINT32_MAX;
-        for (uint32_t r = 0; r < sranks; r++) iterations = std::min(iterations, level_count(h[r]));
-        if (portion == 0 && ranks > 1) iterations = 0;
+        for (uint32_t r = 0; r < ranks; r++) iterations = std::min(iterations, level_count(h[r]));
     }
     // quads of 4 edges per rank slice (see approx_keep_hook4)
     const uint64_t Qf = (portion + 3) / 4;

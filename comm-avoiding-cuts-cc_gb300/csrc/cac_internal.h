@@ -99,6 +99,7 @@ struct cac_graph {
     uint32_t n = 0;
     uint64_t m = 0;
     uint64_t total_weight = 0;
+    bool unit_weights = true;  // every edge weight is 1
     uint32_t *u = nullptr;  // device, m entries
     uint32_t *v = nullptr;  // device, m entries
     uint32_t *w = nullptr;  // device, m entries (all ones when the input had no weights)

@@ -165,12 +165,20 @@ __global__ void fill_u32(uint32_t *p, uint64_t n, uint32_t value) {
         p[i] = value;
 }
 
-__global__ void sum_u32(const uint32_t *p, uint64_t n, unsigned long long *out) {
+// Total of the weights, and a flag set when any weight is not 1.
+__global__ void sum_u32(const uint32_t *p, uint64_t n, unsigned long long *out, unsigned int *nonunit) {
     uint64_t acc = 0;
-    for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (uint64_t)gridDim.x * blockDim.x)
+    uint32_t odd = 0;
+    for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (uint64_t)gridDim.x * blockDim.x) {
         acc += p[i];
+        odd |= p[i] != 1u;
+    }
     for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
-    if ((threadIdx.x & 31) == 0 && acc) atomicAdd(out, (unsigned long long)acc);
+    odd = __any_sync(0xffffffffu, odd);
+    if ((threadIdx.x & 31) == 0) {
+        if (acc) atomicAdd(out, (unsigned long long)acc);
+        if (odd) atomicOr(nonunit, 1u);
+    }
 }
 
 __global__ void check_ids(const uint32_t *u, const uint32_t *v, uint64_t m, uint32_t n, unsigned int *bad) {
@@ -255,7 +263,7 @@ int graph_create(cac_ctx *ctx, uint32_t n, uint64_t m, const uint32_t *u, const 
         unsigned int *d_bad = (unsigned int *)(d_sum + 1);
         cudaMemsetAsync(d_sum, 0, 16, s);
         check_ids<<<grid1(ctx, m), 256, 0, s>>>(g->u, g->v, m, n, d_bad);
-        sum_u32<<<grid1(ctx, m), 256, 0, s>>>(g->w, m, d_sum);
+        sum_u32<<<grid1(ctx, m), 256, 0, s>>>(g->w, m, d_sum, d_bad + 1);
         unsigned long long hsum[2] = {0, 0};
         if (cudaMemcpyAsync(hsum, d_sum, 16, cudaMemcpyDeviceToHost, s) != cudaSuccess ||
             cudaStreamSynchronize(s) != cudaSuccess) {
@@ -267,6 +275,7 @@ int graph_create(cac_ctx *ctx, uint32_t n, uint64_t m, const uint32_t *u, const 
             return fail(CAC_ERR_INVALID);
         }
         g->total_weight = hsum[0];
+        g->unit_weights = (hsum[1] >> 32) == 0;
     }
     ctx->graphs.insert(g);
     *out = g;
