@@ -163,8 +163,7 @@ uint64_t stream_threshold(uint32_t level) {
     return level == 1 ? (1ull << 63) + (1ull << 9) : (1ull << (64 - level)) + (1ull << 10);
 }
 
-__device__ __forceinline__ bool stream_keep(uint32_t x0, uint32_t x1, uint64_t T) {
-    const uint64_t S = ((uint64_t)x1 << 32) | x0;
+__device__ __forceinline__ bool stream_keep(uint64_t S, uint64_t T) {  // S = x0 + x1 2^32
     const int sh = 11 - __clzll(S);  // bits below the 53-bit significand
     if (sh <= 0) return S <= T;
     const uint64_t q = S >> sh, rem = S & ((1ull << sh) - 1), half = 1ull << (sh - 1);
@@ -173,14 +172,12 @@ __device__ __forceinline__ bool stream_keep(uint32_t x0, uint32_t x1, uint64_t T
     return (qr << sh) <= T;
 }
 
-__device__ __forceinline__ uint64_t word_of(const u64x4 &b, unsigned i) {
-    return i == 0 ? b.x[0] : i == 1 ? b.x[1] : i == 2 ? b.x[2] : b.x[3];
-}
-
 // Seed replay, unit weights: one thread per (copy, quad of 4 slice edges), quads numbered as in
-// approx_keep_hook4. The quad's 4 draws read 8 consecutive outputs of the rank's engine, which lie
-// in one or two sitmo blocks (output k = half k & 1 of word (k >> 1) & 3 of block k >> 3, low half
-// first: lib/prng_engine.hpp:195-212).
+// approx_keep_hook4. The quad's 4 draws read the 8 consecutive outputs k0 .. k0 + 7 of the rank's
+// engine (output k = half k & 1 of word k >> 1, low half first: lib/prng_engine.hpp:195-212;
+// words 4b .. 4b + 3 form sitmo block b). Draw d's two outputs give S = x0 + x1 2^32, which is
+// word (k0 >> 1) + d itself when k0 is even and the high half of that word joined to the low half
+// of the next when k0 is odd; the words lie in the blocks k0 >> 3 and the one after it.
 __global__ void approx_stream_keep_hook(uint32_t *par, const uint32_t *__restrict__ U, const uint32_t *__restrict__ V,
                                         uint64_t m, uint32_t n, uint32_t level, uint64_t keep_max, uint32_t copies,
                                         uint32_t seed, uint32_t ranks, uint64_t portion, uint64_t Qf, uint64_t q0,
@@ -203,18 +200,29 @@ __global__ void approx_stream_keep_hook(uint32_t *par, const uint32_t *__restric
         const uint64_t len = r + 1 < ranks ? portion : m - base;
         const uint64_t k0 = (uint64_t)(level - 1) * (2 * (uint64_t)copies * len + 1) + 2 * ((uint64_t)j * len + 4 * lq);
         const uint64_t b0 = k0 >> 3;
+        const unsigned a = (unsigned)(k0 >> 1) & 3u;  // first word inside block b0
+        const bool odd = k0 & 1;
         const uint32_t key = seed + r;
         const u64x4 A = sitmo_block(key, 0, 0, 0, b0, 0, 0, 0);
-        const u64x4 B = ((k0 + 7) >> 3) != b0 ? sitmo_block(key, 0, 0, 0, b0 + 1, 0, 0, 0) : A;
-        auto out = [&](uint64_t k) -> uint32_t {
-            const uint64_t wd = word_of((k >> 3) == b0 ? A : B, (unsigned)(k >> 1) & 3u);
-            return (k & 1) ? (uint32_t)(wd >> 32) : (uint32_t)wd;
-        };
+        u64x4 B = A;
+        if (a != 0 || odd) B = sitmo_block(key, 0, 0, 0, b0 + 1, 0, 0, 0);
+        const uint64_t w[8] = {A.x[0], A.x[1], A.x[2], A.x[3], B.x[0], B.x[1], B.x[2], B.x[3]};
+        uint64_t S[4];
+#define CAC_QUAD_DRAWS(A0)                                                                     \
+    _Pragma("unroll") for (int d = 0; d < 4; d++) S[d] =                                       \
+        odd ? ((w[(A0) + d] >> 32) | (w[(A0) + d + 1] << 32)) : w[(A0) + d];
+        switch (a) {
+            case 0: CAC_QUAD_DRAWS(0) break;
+            case 1: CAC_QUAD_DRAWS(1) break;
+            case 2: CAC_QUAD_DRAWS(2) break;
+            default: CAC_QUAD_DRAWS(3) break;
+        }
+#undef CAC_QUAD_DRAWS
 #pragma unroll
-        for (int k = 0; k < 4; k++) {
-            const uint64_t local = 4 * lq + k;
+        for (int d = 0; d < 4; d++) {
+            const uint64_t local = 4 * lq + d;
             if (local >= len) break;
-            if (!stream_keep(out(k0 + 2 * k), out(k0 + 2 * k + 1), keep_max)) continue;
+            if (!stream_keep(S[d], keep_max)) continue;
             aunite(par, U[base + local] + off, V[base + local] + off);
         }
     }
