@@ -1,8 +1,9 @@
 /*
  * ORACLE — test infrastructure, not product code.
  *
- * A plain-C, single-threaded restatement of the reference's min-cut / connected-components
- * hot path (PJK/comm-avoiding-cuts-cc), used only to check the CUDA path:
+ * A plain-C restatement of the reference's min-cut / connected-components hot path
+ * (PJK/comm-avoiding-cuts-cc; single-threaded except orc_cc_iss_mt, which runs the per-rank
+ * phases on host threads), used only to check the CUDA path:
  * tests/, __graft_entry__.smoke() and bench.py's cpu_baseline / reference legs may call
  * it; the product (libcac) never links or runs it.
  *
@@ -10,10 +11,16 @@
  *   - sitmo block function: known-answer vectors dumped from the reference's own
  *     lib/prng_engine.hpp (tests/golden/sitmo_kat.txt);
  *   - connected components: labels and counts dumped from the reference's own
- *     UnweightedIteratedSparseSampling::connectedComponents (tests/golden/cc_*.txt);
+ *     UnweightedIteratedSparseSampling::connectedComponents (tests/golden/ref_test_inputs.json,
+ *     cc_seeded.json);
  *   - exact minimum cut: values from the reference's test_inputs graph files and from its
- *     comincut::deterministic_minimum_cut on seeded graphs (tests/golden/mincut_*.txt);
- *   - the per-trial replay of the counter-addressed trial semantics has no reference
+ *     comincut::deterministic_minimum_cut on seeded graphs (tests/golden/ref_test_inputs.json,
+ *     mincut_seeded.json);
+ *   - approx_cut on the reference's own draws (orc_approx_cut_stream): libstdc++'s
+ *     binomial_distribution on the reference engine (draws and engine position, from the
+ *     binom_stream harness) and the answers of the reference's approx_cut executable on seeded
+ *     graphs over 16 seeds each (tests/golden/approx_stream.json);
+ *   - the per-trial replay of the counter-addressed square_root trial semantics has no reference
  *     counterpart (the reference's trial streams depend on libstdc++ distribution
  *     internals and on Boost's union-by-rank tie-breaks), so it is pinned at result
  *     level: every trial value is an upper bound on, and the minimum over trials equals,
