@@ -271,6 +271,50 @@ def run_ks(args, rank, world):
     return 0
 
 
+def run_approx(args, rank, world):
+    """--workload approx: approx_cut (success probability 0.9, 4 copies) on G(n = 10^6, M = 10^7)
+    with unit weights, generated on the device; value = edges per second of the seed-replay mode
+    (the reference's own draws, the command line's default on unit-weight graphs), beside the
+    counter-addressed mode. CUDA events on the library stream around each query."""
+    import torch
+    import cac
+    dev = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(dev)
+    stream = torch.cuda.Stream(device=dev)
+    ctx = cac.Context(dev, stream=stream.cuda_stream)
+    g = ctx.generate("erdos_renyi_m", seed=3, n=1000000, avg_degree=20.0, wmin=1, wmax=1)
+    out = {}
+    with Clocks(dev) as clk:
+        for mode, replay in (("seed_replay", True), ("counter", False)):
+            for _ in range(args.warmup):
+                g.approx_cut(0.9, seed=0, virtual_ranks=4, seed_replay=replay)
+            ms = []
+            for i in range(args.steps):
+                res = g.approx_cut(0.9, seed=i, virtual_ranks=4, seed_replay=replay)
+                ms.append(res.device_ms)
+            out[mode] = {"ms_per_query": statistics.median(ms), "total_ms": sum(ms), "level": int(res.level),
+                         "cut": int(res.cut)}
+    total_ms = out["seed_replay"]["total_ms"]
+    if world > 1:
+        t = torch.tensor([total_ms], device="cuda")
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        total_ms = float(t.item())
+    line = {"metric": "approx_cut edges/s (G(10^6, M=10^7), unit weights, 4 virtual ranks)",
+            "value": world * g.m * args.steps / (total_ms / 1e3), "unit": "edges/s", "n_gpus": world,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": total_ms / args.steps,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "u32",
+            "data": "synthetic (seeded, generated on the device)",
+            "config": {"workload": "approx_cut G(n=1000000, M=10000000) unit weights, p=0.9, 4 virtual ranks",
+                       "vertices": g.n, "edges": g.m, "copies": int(res.copies)},
+            "modes": {k: {kk: vv for kk, vv in v.items() if kk != "total_ms"} for k, v in out.items()},
+            "clocks": clk.summary()}
+    if rank == 0:
+        print(json.dumps(line))
+    g.free()
+    ctx.close()
+    return 0
+
+
 def run_reference(args, rank, world):
     if rank != 0:
         return 0
@@ -660,7 +704,7 @@ def main():
     ap.add_argument("--no-ks", action="store_true", help="skip the square_root (Karger-Stein) measurements")
     ap.add_argument("--no-rmat", action="store_true", help="skip the R-MAT scale 22 CC measurement")
     ap.add_argument("--workload", default="cc",
-                    choices=["cc", "cc-rmat22", "ks-er1000", "ks-k4000", "ks-batch", "serve"],
+                    choices=["cc", "cc-rmat22", "ks-er1000", "ks-k4000", "ks-batch", "serve", "approx"],
                     help="cc: the benchmark line; the others: one workload's line")
     ap.add_argument("--graphs", type=int, default=4096, help="ks-batch: graphs in the batch")
     ap.add_argument("--queries", type=int, default=200, help="serve: queries in the trace")
@@ -684,6 +728,8 @@ def main():
             return run_batch(args, rank, world)
         if args.workload == "serve":
             return run_serve(args, rank, world)
+        if args.workload == "approx":
+            return run_approx(args, rank, world)
         return run_cac(args, rank, world)
     finally:
         if world > 1:
