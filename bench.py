@@ -50,6 +50,19 @@ METRIC = "CC edges/s (parallel_cc, BA n=1,024,000 m=16)"
 KERNELS_PER_QUERY = 2 + 8 + 4 + 8
 
 
+def _max_over_ranks(x, world):
+    """The largest x over the ranks (a job takes as long as its slowest replica); the process
+    group's backend decides where the reduction runs (NCCL: on the GPU, gloo: on the host)."""
+    if world <= 1:
+        return x
+    import torch
+    import torch.distributed as dist
+    dev = "cuda" if dist.get_backend() == "nccl" else "cpu"
+    t = torch.tensor([float(x)], dtype=torch.float64, device=dev)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
 def _peaks():
     try:
         with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
@@ -250,10 +263,7 @@ def run_ks(args, rank, world):
             res = g.square_root(0.95, seed=0, virtual_ranks=ranks)
             ms.append(res.device_ms)
     total_ms = sum(ms)
-    if world > 1:
-        t = torch.tensor([total_ms], device="cuda")
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        total_ms = float(t.item())
+    total_ms = _max_over_ranks(total_ms, world)
     line = {"metric": "Karger-Stein trials/s (%s)" % name, "value": world * res.total_trials * args.steps / (total_ms / 1e3),
             "unit": "trials/s", "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
             "ms_per_step": total_ms / args.steps, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
@@ -295,10 +305,7 @@ def run_approx(args, rank, world):
             out[mode] = {"ms_per_query": statistics.median(ms), "total_ms": sum(ms), "level": int(res.level),
                          "cut": int(res.cut)}
     total_ms = out["seed_replay"]["total_ms"]
-    if world > 1:
-        t = torch.tensor([total_ms], device="cuda")
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        total_ms = float(t.item())
+    total_ms = _max_over_ranks(total_ms, world)
     line = {"metric": "approx_cut edges/s (G(10^6, M=10^7), unit weights, 4 virtual ranks)",
             "value": world * g.m * args.steps / (total_ms / 1e3), "unit": "edges/s", "n_gpus": world,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": total_ms / args.steps,
@@ -366,10 +373,7 @@ def _cc_measure(ctx, stream, g, n, hu_np, hv_np, steps, warmup, world, flush):
             assert count == want_count
         torch.cuda.synchronize()
     total_ms = sum(s.elapsed_time(e) for s, e in zip(starts, ends))
-    if world > 1:
-        t = torch.tensor([total_ms], device="cuda")
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        total_ms = float(t.item())
+    total_ms = _max_over_ranks(total_ms, world)
     hl_np = torch.empty(max(n, 1), dtype=torch.int32).pin_memory().numpy().view(np.uint32)
     for _ in range(max(1, warmup)):
         ctx.cc_edges(n, hu_np, hv_np, GRAPH_SEED, 1, hl_np)
@@ -382,10 +386,7 @@ def _cc_measure(ctx, stream, g, n, hu_np, hv_np, steps, warmup, world, flush):
         e2e_ms.append((time.perf_counter() - t0) * 1e3)
         assert r.num_components == want_count
     e2e_total = sum(e2e_ms)
-    if world > 1:
-        t = torch.tensor([e2e_total], device="cuda")
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        e2e_total = float(t.item())
+    e2e_total = _max_over_ranks(e2e_total, world)
     link = _link_gbs(hu_np, hv_np)
     return {"value": world * m * steps / (total_ms / 1e3), "ms_per_step": total_ms / steps,
             "e2e": {"value": world * m * steps / (e2e_total / 1e3), "unit": "edges/s", "h2d_bytes_per_step": 8 * m,
