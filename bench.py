@@ -219,7 +219,7 @@ def _ks_also(ctx):
         filled = None
         if n <= 1000:
             # the same query 64 times with seeds 0..63 in one cac_mincut_batch: the GPU's trial
-            # throughput once it is full (one C1 query has only 60 trials in flight)
+            # throughput once it is full (one ER(1000, 0.05) query has only 60 trials in flight)
             seeds = list(range(64))
             ctx.mincut_batch([g] * len(seeds), 0.95, seeds, ranks)  # warm-up
             t1 = time.perf_counter()

@@ -1,5 +1,6 @@
 """Many square_root queries of uneven graphs in one engine run (cac_mincut_batch): every result equals
-the same query run alone, and the exact cut (BASELINE config 4 shape at test size)."""
+the same query run alone, and the exact cut (Watts-Strogatz and G(n, M) graphs of uneven sizes, the
+shape of the 4096-graph batch workload, at test size)."""
 import numpy as np
 import pytest
 
