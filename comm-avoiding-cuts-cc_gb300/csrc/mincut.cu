@@ -958,9 +958,9 @@ struct DevBuf {
 
 // Grow-only scratch buffers kept by the ctx between calls: a fresh device allocation per query
 // (cudaMalloc, and a cudaFree that waits for the whole device) cost more than the kernels of a
-// small query (admission of square_root on ER(1000, 0.05): 303 us, of which about 100 us of kernels). Slots 0..10 belong to the
-// Karger-Stein engine, 11..15 to admission, 16.. to the one-shot probes; one engine runs per ctx at
-// a time.
+// small query (admission of square_root on ER(1000, 0.05): 303 us, of which about 100 us of
+// kernels). Slots 0..10 belong to the Karger-Stein engine, 11..15 to admission, 16.. to the
+// one-shot probes; one engine runs per ctx at a time.
 enum ScratchSlot : int {
     kSlotSrc, kSlotTask, kSlotLeaf, kSlotRowoff, kSlotKout, kSlotPrep, kSlotTscratch, kSlotQoff, kSlotGto, kSlotErr,
     kSlotPsrc, kSlotPre, kSlotLab, kSlotK, kSlotSd, kSlotDd, kSlotProbe0, kSlotProbe1, kSlotProbe2, kSlotCount
