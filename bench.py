@@ -12,15 +12,24 @@ reference. The metric is edges per second.
              L2 is flushed (a 512 MB write) before every timed query, outside the events.
   e2e        the same query through the one-call C ABI entry point from pinned HOST edge arrays
              to HOST labels, host->device and device->host copies inside the timed region.
-  roofline   the dominant kernel (the closing pass over all edges): algorithmic bytes 8 m per
-             launch (u and v, 4 bytes each) / its CUDA-event duration, against the measured HBM
-             copy bandwidth.
-  cpu_baseline  the oracle's restatement of the reference's CC loop on the host, one virtual rank per
-                host core, each on its own thread (the reference under mpiexec -n <cores>).
+  roofline   the whole query against HBM: algorithmic bytes 8 m + 8 n per query (u and v read
+             once, parent initialised and label written once) / the query's CUDA-event
+             duration, against the measured HBM copy bandwidth; the closing filter pass over all
+             edges (8 m bytes per launch) is reported beside it as its own kernel roofline.
+  cpu_baseline  the oracle's restatement of the reference's CC loop on the host with the same 16
+                virtual ranks, each on its own thread (the reference under mpiexec -n 16).
+  also_*     the other configurations of the metric: CC on R-MAT scale 22, square_root
+             (Karger-Stein trials/s) on ER(1000, 0.05) and K4000, 512 graphs of the uneven
+             batched population (batched vs one call per graph, every cut checked against the
+             exact cut), and a shortened served stream (queries/s, p50/p99).
+
+Both arms run the query with 16 virtual ranks (the reference's mpiexec -n 16; CC labels do not
+depend on the rank count).
 
 --impl reference times the reference's CPU implementation of the path (the oracle port of
 UnweightedIteratedSparseSampling::connectedComponents; the reference sources themselves are not
-present on the GPU host) on the same workload and prints the same JSON line.
+present on the GPU host) on the same workload and prints the same JSON line, with the port's
+measured slowdown against the reference's own build beside it.
 
 N > 1 (torchrun): every rank runs an independent replica of the query on its own GPU ("replicas
 only": the reference's CC has no exchange that a single GPU would need); value = edges of all
@@ -44,6 +53,19 @@ import numpy as np  # noqa: E402
 from concurrent.futures import ThreadPoolExecutor  # noqa: E402
 
 N_VERTICES, ATTACH, GRAPH_SEED = 1024000, 16, 0
+VIRTUAL_RANKS = 16  # both arms: the reference under mpiexec -n 16
+# The oracle port against the reference's own build, one core each, same machine and inputs
+# (oracle/refbuild/port_speed.py, run where both exist): how much the port-based CPU baseline
+# understates the reference.
+_PORT_HOW = ("oracle/refbuild/port_speed.py: one core each of an Intel Xeon @ 2.70 GHz (the x86 build machine), "
+             "the port and the reference's own single-rank build on the same inputs")
+PORT_SLOWDOWN = {
+    "parallel_cc": {"factor": 1.07, "reference_s": 0.359, "port_s": 0.384, "how": _PORT_HOW},
+    "square_root_er1000": {"factor": 5.27, "reference_trials_per_s": 164.6, "port_trials_per_s": 31.2,
+                           "how": _PORT_HOW},
+    "square_root_k4000": {"factor": 2.15, "reference_trials_per_s": 0.220, "port_trials_per_s": 0.102,
+                          "how": _PORT_HOW},
+}
 METRIC = "CC edges/s (parallel_cc, BA n=1,024,000 m=16)"
 # init, sample_draws, 8 x sample_hook, 4 x compress4 (after the first three slices and the last),
 # find_giant, giant_bitmap, filter, hook_survivors, finalize_count, scan_tiles, rank_roots, label_all
@@ -127,27 +149,33 @@ class Clocks:
                 "samples": len(rows)}
 
 
+def _host_cores():
+    return max(1, len(os.sched_getaffinity(0)) if hasattr(os, "sched_getaffinity") else (os.cpu_count() or 1))
+
+
 def _cpu_baseline(n, u, v, budget_s=12.0):
-    """The oracle's restatement of the reference CC loop as `mpiexec -n P` would run it with P =
-    every host core: P ranks, their per-rank phases (slice sampling and rewrite) on P threads, the
-    root's gather, shuffle and prefix union-find sequential; repeated for ~budget_s."""
+    """The oracle's restatement of the reference CC loop as `mpiexec -n 16` runs it: 16 ranks,
+    their per-rank phases (slice sampling and rewrite) on one host thread each, the root's
+    gather, shuffle and prefix union-find sequential; repeated for ~budget_s."""
     sys.path.insert(0, os.path.join(ROOT, "oracle"))
     import pyoracle
-    cores = max(1, len(os.sched_getaffinity(0)) if hasattr(os, "sched_getaffinity") else (os.cpu_count() or 1))
+    threads = min(_host_cores(), VIRTUAL_RANKS)
     times = []
     t_end = time.perf_counter() + budget_s
     while True:
         t0 = time.perf_counter()
-        count, _, rounds = pyoracle.cc_iss(n, u, v, GRAPH_SEED, cores, cores)
+        count, _, rounds = pyoracle.cc_iss(n, u, v, GRAPH_SEED, VIRTUAL_RANKS, threads)
         times.append(time.perf_counter() - t0)
         if time.perf_counter() > t_end or len(times) >= 50:
             break
     med = statistics.median(times)
-    return {"value": len(u) / med, "unit": "edges/s", "cores": cores, "kind": "port",
+    return {"value": len(u) / med, "unit": "edges/s", "cores": threads, "kind": "port",
             "sample": "the full BA-1M graph, %d runs of the oracle's restatement of "
                       "UnweightedIteratedSparseSampling::connectedComponents on %d virtual ranks, one host "
-                      "thread each (%d rounds); median %.3f s" % (len(times), cores, rounds, med),
-            "components": count, "virtual_ranks": cores}
+                      "thread each (%d rounds); median %.3f s" % (len(times), VIRTUAL_RANKS, rounds, med),
+            "components": count, "virtual_ranks": VIRTUAL_RANKS,
+            "port_vs_reference": PORT_SLOWDOWN["parallel_cc"],
+            "reference_estimate": len(u) / med * PORT_SLOWDOWN["parallel_cc"]["factor"]}
 
 
 def _ks_workloads():
@@ -156,6 +184,9 @@ def _ks_workloads():
     import graphgen
     return [("square_root ER n=1000 p=0.05 w[1,42], 4 virtual ranks", graphgen.erdos_renyi(1000, 0.05, 0), 4, 5),
             ("square_root K4000 w[1,42]", graphgen.complete(4000, 0), 1, 3)]
+
+
+_PORT_KEYS = {0: "square_root_er1000", 1: "square_root_k4000"}
 
 
 def _ks_work_model(t, trials_per_s, entry_bytes, hbm_peak, peak_kind):
@@ -193,7 +224,7 @@ def _ks_also(ctx):
     sys.path.insert(0, os.path.join(ROOT, "oracle"))
     import pyoracle
     out = []
-    for name, (n, u, v, w), ranks, reps in _ks_workloads():
+    for wi, (name, (n, u, v, w), ranks, reps) in enumerate(_ks_workloads()):
         g = ctx.graph(n, u, v, w)
         res = g.square_root(0.95, seed=0, virtual_ranks=ranks)  # warm-up (also builds the level buffers)
         ms = []
@@ -206,7 +237,7 @@ def _ks_also(ctx):
         np.add.at(deg, v, w.astype(np.uint64))
         # the oracle replays trials on every host core at once (trials are independent, as across
         # the reference's ranks; the C replay releases the interpreter lock)
-        cores = max(1, len(os.sched_getaffinity(0)) if hasattr(os, "sched_getaffinity") else (os.cpu_count() or 1))
+        cores = _host_cores()
         per = res.trials_per_rank
         ids = [(r, i) for r in range(ranks) for i in range(per)]
         if n > 1000:
@@ -238,7 +269,10 @@ def _ks_also(ctx):
                     "cpu_baseline": {"trials_per_s": cpu_trials / cpu_s, "cores": cores, "kind": "port",
                                      "sample": "%d trial(s) of the oracle's replay on %d host threads"
                                                % (cpu_trials, cores),
-                                     "cut_agrees": (cpu_cut == res.cut) if cpu_trials == trials else None},
+                                     "cut_agrees": (cpu_cut == res.cut) if cpu_trials == trials else None,
+                                     "port_vs_reference": PORT_SLOWDOWN[_PORT_KEYS[wi]],
+                                     "reference_estimate_trials_per_s":
+                                         cpu_trials / cpu_s * PORT_SLOWDOWN[_PORT_KEYS[wi]]["factor"]},
                     "batched_64_queries": filled})
         g.free()
     return out
@@ -348,7 +382,7 @@ def _cc_measure(ctx, stream, g, n, hu_np, hv_np, steps, warmup, world, flush):
     labels = torch.empty(max(n, 1), dtype=torch.int32, device="cuda")
 
     def step():
-        return g.connected_components(seed=GRAPH_SEED, virtual_ranks=1, out=labels)
+        return g.connected_components(seed=GRAPH_SEED, virtual_ranks=VIRTUAL_RANKS, out=labels)
 
     want_count = None
     with torch.cuda.stream(stream):
@@ -376,13 +410,13 @@ def _cc_measure(ctx, stream, g, n, hu_np, hv_np, steps, warmup, world, flush):
     total_ms = _max_over_ranks(total_ms, world)
     hl_np = torch.empty(max(n, 1), dtype=torch.int32).pin_memory().numpy().view(np.uint32)
     for _ in range(max(1, warmup)):
-        ctx.cc_edges(n, hu_np, hv_np, GRAPH_SEED, 1, hl_np)
+        ctx.cc_edges(n, hu_np, hv_np, GRAPH_SEED, VIRTUAL_RANKS, hl_np)
     e2e_ms = []
     for _ in range(steps):
         flush.zero_()
         torch.cuda.synchronize()
         t0 = time.perf_counter()
-        r = ctx.cc_edges(n, hu_np, hv_np, GRAPH_SEED, 1, hl_np)
+        r = ctx.cc_edges(n, hu_np, hv_np, GRAPH_SEED, VIRTUAL_RANKS, hl_np)
         e2e_ms.append((time.perf_counter() - t0) * 1e3)
         assert r.num_components == want_count
     e2e_total = sum(e2e_ms)
@@ -455,7 +489,7 @@ def run_cac(args, rank, world):
                 "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "u32",
                 "data": "synthetic (R-MAT generated on the device, seed 0)",
                 "config": {"workload": r["workload"], "vertices": r["vertices"], "edges": r["edges"],
-                           "virtual_ranks": 1, "l2": "flushed (512 MB write) before every timed query"},
+                           "virtual_ranks": VIRTUAL_RANKS, "l2": "flushed (512 MB write) before every timed query"},
                 "e2e": r["e2e"], "components": r["components"], "phases_ms": r["phases_ms"],
                 "gpu_launches": KERNELS_PER_QUERY * args.steps, "clocks": clk.summary()}
         if rank == 0:
@@ -471,13 +505,17 @@ def run_cac(args, rank, world):
     with Clocks(dev) as clk:
         r = _cc_measure(ctx, stream, g, n, hu_np, hv_np, args.steps, args.warmup, world, flush)
     peak, peak_kind = _peaks()
-    alg_bytes = 8 * m
-    achieved = alg_bytes / (r["edge_avg_ms"] / 1e3) / 1e9
-    traffic = None
-    prof = os.path.join(ROOT, "profiles", "cc_filter_ba1m.json")
-    if os.path.exists(prof):
-        with open(prof) as f:
-            traffic = json.load(f).get("dram_bytes_per_launch")
+    # whole query: 8 m bytes of edges read once + 8 n (parent initialised, label written)
+    query_bytes = 8 * m + 8 * n
+    query_gbs = query_bytes / (r["ms_per_step"] / 1e3) / 1e9
+    filt_bytes = 8 * m
+    filt_gbs = filt_bytes / (r["edge_avg_ms"] / 1e3) / 1e9
+    traffic = {}
+    for key, name in (("query", "cc_query_ba1m.json"), ("filter", "cc_filter_ba1m.json")):
+        prof = os.path.join(ROOT, "profiles", name)
+        if os.path.exists(prof):
+            with open(prof) as f:
+                traffic[key] = json.load(f).get("dram_bytes_per_launch")
     if rank != 0:
         g.free()
         ctx.close()
@@ -488,12 +526,16 @@ def run_cac(args, rank, world):
         "vs_baseline": None, "dtype": "u32", "data": "synthetic (seeded Barabasi-Albert, n=1,024,000, attach 16, "
                                                      "permuted)",
         "config": {"workload": "parallel_cc BA n=1024000 m=16 (16,383,744 edges)", "vertices": n, "edges": m,
-                   "virtual_ranks": 1, "l2": "flushed (512 MB write) before every timed query",
+                   "virtual_ranks": VIRTUAL_RANKS, "l2": "flushed (512 MB write) before every timed query",
                    "parallelism": "replicas" if world > 1 else "single GPU"},
         "e2e": r["e2e"],
-        "roofline": {"bound": "hbm", "kernel": "cc_filter", "achieved": achieved, "peak": peak,
-                     "peak_kind": peak_kind, "unit": "GB/s", "frac": achieved / peak, "traffic": traffic,
-                     "alg_bytes_per_launch": alg_bytes, "avg_launch_ms": r["edge_avg_ms"]},
+        "roofline": {"bound": "hbm", "scope": "whole query (%d kernels)" % KERNELS_PER_QUERY,
+                     "achieved": query_gbs, "peak": peak, "peak_kind": peak_kind, "unit": "GB/s",
+                     "frac": query_gbs / peak, "traffic": traffic.get("query"), "alg_bytes_per_launch": query_bytes,
+                     "avg_launch_ms": r["ms_per_step"],
+                     "filter_kernel": {"kernel": "cc_filter", "achieved": filt_gbs, "frac": filt_gbs / peak,
+                                       "traffic": traffic.get("filter"), "alg_bytes_per_launch": filt_bytes,
+                                       "avg_launch_ms": r["edge_avg_ms"]}},
         "gpu_launches": KERNELS_PER_QUERY * args.steps,
         "phases_ms": r["phases_ms"],
         "clocks": clk.summary(),
@@ -506,23 +548,29 @@ def run_cac(args, rank, world):
                                                      "phases_ms", "generate_s")}
     if not args.no_ks:
         line["also_ks"] = _ks_also(ctx)
-    print(json.dumps(line))
     g.free()
+    if not args.no_batch:
+        line["also_batch"] = _batch_measure(ctx, 512, 2, 1, check_exact=True)
     ctx.close()
+    if not args.no_serve:
+        line["also_serve"] = _serve_measure(dev, 100, (0.6,))
+    print(json.dumps(line))
     return 0
 
 
-def run_batch(args, rank, world):
-    """--workload ks-batch: square_root on a population of uneven graphs (4096 by default) in one
-    batch, next to the plain path (one cac_mincut call per graph) on a subset of the same graphs."""
+SERVE_NOTE = ("served graphs have n = floor(2 sqrt(m)), so square_root's pre-contraction target "
+              "ceil(2 sqrt(m) + 1) is at least n and a query is the Karger-Stein budget on the whole graph (a "
+              "handful of trials); sparse shapes with 10^5 - 10^6 trials per query are not in the served mix")
+
+
+def _batch_measure(ctx, count, steps, warmup, check_exact=False):
+    """square_root on the first `count` graphs of the uneven population in one cac_mincut_batch
+    (host wall clock per batch), next to the plain path (one cac_mincut call per graph) on up to
+    256 of them; every batched cut equals the plain one, and with check_exact also the exact
+    minimum cut (the oracle's exact routine on every host thread, outside the timed region)."""
     import torch
-    import cac
     import workloads
-    dev = int(os.environ.get("LOCAL_RANK", "0"))
-    torch.cuda.set_device(dev)
-    stream = torch.cuda.Stream(device=dev)
-    ctx = cac.Context(dev, stream=stream.cuda_stream)
-    specs = workloads.uneven_population(args.graphs)
+    specs = workloads.uneven_population(4096)[:count]
     t0 = time.perf_counter()
     graphs = [workloads.make(ctx, sp) for sp in specs]
     gen_s = time.perf_counter() - t0
@@ -537,40 +585,70 @@ def run_batch(args, rank, world):
     t0 = time.perf_counter()
     bsub = ctx.mincut_batch(graphs[:sub], 0.9, seeds=seeds[:sub])
     bsub_s = time.perf_counter() - t0
-    assert all(a.cut == b.cut and a.total_trials == b.total_trials for a, b in zip(plain, bsub))
-    for _ in range(args.warmup):
+    equal = all(a.cut == b.cut and a.total_trials == b.total_trials for a, b in zip(plain, bsub))
+    for _ in range(warmup):
         res = ctx.mincut_batch(graphs, 0.9, seeds=seeds)
     wall = []
-    with Clocks(dev) as clk:
-        for _ in range(args.steps):
-            torch.cuda.synchronize()
-            t0 = time.perf_counter()
-            res = ctx.mincut_batch(graphs, 0.9, seeds=seeds)
-            wall.append(time.perf_counter() - t0)
+    for _ in range(steps):
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        res = ctx.mincut_batch(graphs, 0.9, seeds=seeds)
+        wall.append(time.perf_counter() - t0)
+    exact = None
+    if check_exact:
+        sys.path.insert(0, os.path.join(ROOT, "oracle"))
+        import pyoracle
+        want = pyoracle.exact_mincut_many([workloads.host_arrays(sp) for sp in specs], threads=_host_cores())
+        exact = sum(int(r.cut) == x for r, x in zip(res, want))
     trials = sum(r.total_trials for r in res)
-    sub_trials = sum(r.total_trials for r in plain)
     total_s = sum(wall)
-    line = {"metric": "Karger-Stein trials/s (square_root, %d uneven graphs in one batch)" % len(graphs),
-            "value": world * trials * args.steps / total_s, "unit": "trials/s", "n_gpus": world, "steps": args.steps,
-            "warmup": args.warmup, "ms_per_step": total_s / args.steps * 1e3, "higher_is_better": True,
-            "scaling": "weak", "vs_baseline": None, "dtype": "u64",
-            "data": "synthetic (device-generated Watts-Strogatz and G(n, M), seeds base + index)",
-            "config": {"workload": "uneven square_root batch", "graphs": len(graphs),
-                       "edges": int(sum(g.m for g in graphs)), "trials_per_batch": trials,
-                       "success_probability": 0.9, "n_range": [64, 8192], "timing": "host wall clock per batch"},
-            "queries_per_s": world * len(graphs) * args.steps / total_s,
-            "device_ms_per_batch": float(res[0].device_ms),
-            "plain_path_subset": {"graphs": sub, "trials": sub_trials, "one_call_per_graph_s": plain_s,
-                                  "batched_s": bsub_s, "plain_queries_per_s": sub / plain_s,
-                                  "batched_queries_per_s": sub / bsub_s, "speedup": plain_s / bsub_s,
-                                  "cuts_equal": True},
-            "generate_s": round(gen_s, 3), "clocks": clk.summary()}
-    if rank == 0:
-        print(json.dumps(line))
+    out = {"workload": "uneven square_root batch (Watts-Strogatz and G(n, M), n log-uniform in [64, 8192], "
+                       "w in [1, 100], p = 0.9)",
+           "graphs": len(graphs), "edges": int(sum(g.m for g in graphs)), "trials_per_batch": trials,
+           "value": trials * steps / total_s, "unit": "trials/s", "ms_per_step": total_s / steps * 1e3,
+           "steps": steps, "queries_per_s": len(graphs) * steps / total_s,
+           "device_ms_per_batch": float(res[0].device_ms), "timing": "host wall clock per batch",
+           "plain_path_subset": {"graphs": sub, "trials": sum(r.total_trials for r in plain),
+                                 "one_call_per_graph_s": plain_s, "batched_s": bsub_s,
+                                 "plain_queries_per_s": sub / plain_s, "batched_queries_per_s": sub / bsub_s,
+                                 "speedup": plain_s / bsub_s},
+           "results_equal_plain": equal,
+           "cuts_exact": None if exact is None else "%d of %d" % (exact, len(graphs)),
+           "generate_s": round(gen_s, 3)}
     for g in graphs:
         g.free()
+    return out
+
+
+def run_batch(args, rank, world):
+    """--workload ks-batch: square_root on a population of uneven graphs (4096 by default) in one
+    batch, next to the plain path (one cac_mincut call per graph) on a subset of the same graphs."""
+    import torch
+    import cac
+    dev = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(dev)
+    stream = torch.cuda.Stream(device=dev)
+    ctx = cac.Context(dev, stream=stream.cuda_stream)
+    with Clocks(dev) as clk:
+        r = _batch_measure(ctx, args.graphs, args.steps, args.warmup, check_exact=args.check_exact)
+    total_s = r["ms_per_step"] * args.steps / 1e3
+    total_s = _max_over_ranks(total_s, world)
+    line = {"metric": "Karger-Stein trials/s (square_root, %d uneven graphs in one batch)" % r["graphs"],
+            "value": world * r["trials_per_batch"] * args.steps / total_s, "unit": "trials/s", "n_gpus": world,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": total_s / args.steps * 1e3,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "u64",
+            "data": "synthetic (device-generated Watts-Strogatz and G(n, M), seeds base + index)",
+            "config": {"workload": "uneven square_root batch", "graphs": r["graphs"], "edges": r["edges"],
+                       "trials_per_batch": r["trials_per_batch"], "success_probability": 0.9,
+                       "n_range": [64, 8192], "timing": "host wall clock per batch"},
+            "queries_per_s": world * r["graphs"] * args.steps / total_s,
+            "device_ms_per_batch": r["device_ms_per_batch"], "plain_path_subset": r["plain_path_subset"],
+            "results_equal_plain": r["results_equal_plain"], "cuts_exact": r["cuts_exact"],
+            "generate_s": r["generate_s"], "clocks": clk.summary()}
+    if rank == 0:
+        print(json.dumps(line))
     ctx.close()
-    return 0
+    return 0 if r["results_equal_plain"] else 1
 
 
 def _percentile(xs, q):
@@ -581,18 +659,15 @@ def _percentile(xs, q):
     return xs[k]
 
 
-def run_serve(args, rank, world):
-    """--workload serve: a mixed stream of square_root : approx_cut : parallel_cc = 2:1:1 queries
-    over graphs of 10^3 - 10^7 edges, served by cac_server under a 120 GB HBM budget: queries/s at
-    saturation (every query submitted at once), p50/p99 latency and per-query slowdown (latency /
-    time alone) when the same queries arrive as a Poisson stream at 30% and 60% of that rate, and
-    the plain path (one single-query call after another) on the same trace."""
+def _serve_measure(dev, queries, fracs):
+    """A mixed stream of square_root : approx_cut : parallel_cc = 2:1:1 queries over 32 graphs of
+    10^3 - 10^7 edges, served by cac_server under a 120 GB HBM budget: queries/s at saturation
+    (every query submitted at once), the plain path (one single-query call after another) on the
+    same trace, and p50/p99 latency and per-query slowdown (latency / time alone) when the same
+    queries arrive as a Poisson stream at each fraction of the saturated rate."""
     import threading
-    import torch
     import cac
     import workloads
-    dev = int(os.environ.get("LOCAL_RANK", "0"))
-    torch.cuda.set_device(dev)
     specs = workloads.served_population(32)
     ctx = cac.Context(dev)
     srv = cac.Server(dev, hbm_budget_bytes=120 << 30)
@@ -618,11 +693,10 @@ def run_serve(args, rank, world):
             return (int(resp.num_components),)
         return (int(resp.cut), int(resp.trials))
 
-    trace = workloads.served_trace(args.queries, len(specs), None, seed=7)
+    trace = workloads.served_trace(queries, len(specs), None, seed=7)
     for kind in ("square_root", "approx_cut", "parallel_cc"):  # warm-up
         plain_one(kind, 0, 1)
         srv.poll(srv.submit(kind, sg[0], probs[kind], 1))
-    # plain path: one query after another through the single-query calls
     t0 = time.perf_counter()
     plain_lat, want = [], []
     for _, kind, gi, sd in trace:
@@ -630,17 +704,13 @@ def run_serve(args, rank, world):
         want.append(plain_one(kind, gi, sd))
         plain_lat.append((time.perf_counter() - q0) * 1e3)
     plain_s = time.perf_counter() - t0
-    # saturation: every query submitted at once
-    with Clocks(dev) as clk:
-        t0 = time.perf_counter()
-        tickets = [srv.submit(kind, sg[gi], probs[kind], sd) for _, kind, gi, sd in trace]
-        got = [srv.poll(t)[0] for t in tickets]
-        sat_s = time.perf_counter() - t0
+    t0 = time.perf_counter()
+    tickets = [srv.submit(kind, sg[gi], probs[kind], sd) for _, kind, gi, sd in trace]
+    got = [srv.poll(t)[0] for t in tickets]
+    sat_s = time.perf_counter() - t0
     sat_lat = [r.queue_ms + r.service_ms for r in got]
     equal = all(served_value(kind, r) == w for (_, kind, _, _), r, w in zip(trace, got, want))
-    # Poisson arrivals of the same queries at a fraction of the saturated rate: latency = submit to
-    # finish; slowdown = latency / the same query's time alone on the plain path
-    gaps = workloads.served_trace(args.queries, len(specs), 1.0, seed=8)
+    gaps = workloads.served_trace(queries, len(specs), 1.0, seed=8)
 
     def poisson(frac):
         rate = frac * len(trace) / sat_s
@@ -667,32 +737,55 @@ def run_serve(args, rank, world):
         for (_, kind, _, _), x in zip(trace, lat):
             by_kind.setdefault(kind, []).append(x)
         worst = sorted(range(len(trace)), key=lambda i: -lat[i])[:5]
-        return {"rate_per_s": rate, "queries_per_s": len(trace) / span, "p50_ms": _percentile(lat, 50),
-                "p99_ms": _percentile(lat, 99), "p99_ms_by_kind": {k: _percentile(v, 99) for k, v in by_kind.items()},
-                "slowdown_p50": _percentile(slow, 50), "slowdown_p99": _percentile(slow, 99),
-                "slowest": [{"kind": trace[i][1], "edges": int(cg[trace[i][2]].m), "alone_ms": round(plain_lat[i], 3),
-                             "queue_ms": round(res[i].queue_ms, 3), "service_ms": round(res[i].service_ms, 3)}
-                            for i in worst]}
+        ok = all(served_value(kind, r) == w for (_, kind, _, _), r, w in zip(trace, res, want))
+        return ok, {"rate_per_s": rate, "queries_per_s": len(trace) / span, "p50_ms": _percentile(lat, 50),
+                    "p99_ms": _percentile(lat, 99),
+                    "p99_ms_by_kind": {k: _percentile(v, 99) for k, v in by_kind.items()},
+                    "slowdown_p50": _percentile(slow, 50), "slowdown_p99": _percentile(slow, 99),
+                    "slowest": [{"kind": trace[i][1], "edges": int(cg[trace[i][2]].m),
+                                 "alone_ms": round(plain_lat[i], 3), "queue_ms": round(res[i].queue_ms, 3),
+                                 "service_ms": round(res[i].service_ms, 3)} for i in worst]}
 
-    low, mid = poisson(0.3), poisson(0.6)
-    line = {"metric": "served queries/s (square_root : approx_cut : parallel_cc = 2:1:1, 10^3-10^7 edges)",
-            "value": len(trace) / sat_s, "unit": "queries/s", "n_gpus": 1, "steps": len(trace), "warmup": 3,
-            "ms_per_step": sat_s / len(trace) * 1e3, "higher_is_better": True, "scaling": "weak",
-            "vs_baseline": None, "dtype": "u64", "data": "synthetic (device-generated G(n, p) and R-MAT)",
-            "config": {"workload": "served mixed stream", "graphs": len(specs),
-                       "edges_range": [int(min(g.m for g in cg)), int(max(g.m for g in cg))],
-                       "hbm_budget_bytes": 120 << 30, "queries": len(trace)},
-            "saturation": {"queries_per_s": len(trace) / sat_s, "p50_ms": _percentile(sat_lat, 50),
-                           "p99_ms": _percentile(sat_lat, 99)},
-            "poisson_30pct": low, "poisson_60pct": mid,
-            "plain_path": {"queries_per_s": len(trace) / plain_s, "p50_ms": _percentile(plain_lat, 50),
-                           "p99_ms": _percentile(plain_lat, 99)},
-            "speedup_vs_plain": plain_s / sat_s, "results_equal_plain": equal, "clocks": clk.summary()}
-    if rank == 0:
-        print(json.dumps(line))
+    out = {"workload": "served mixed stream (square_root : approx_cut : parallel_cc = 2:1:1, 10^3-10^7 edges, "
+                       "G(n, p) and R-MAT, w in [1, 42], 120 GB budget)",
+           "graphs": len(specs), "queries": len(trace),
+           "edges_range": [int(min(g.m for g in cg)), int(max(g.m for g in cg))],
+           "value": len(trace) / sat_s, "unit": "queries/s",
+           "saturation": {"queries_per_s": len(trace) / sat_s, "p50_ms": _percentile(sat_lat, 50),
+                          "p99_ms": _percentile(sat_lat, 99)},
+           "plain_path": {"queries_per_s": len(trace) / plain_s, "p50_ms": _percentile(plain_lat, 50),
+                          "p99_ms": _percentile(plain_lat, 99)},
+           "speedup_vs_plain": plain_s / sat_s, "note": SERVE_NOTE}
+    for frac in fracs:
+        ok, r = poisson(frac)
+        equal = equal and ok
+        out["poisson_%dpct" % round(frac * 100)] = r
+    out["results_equal_plain"] = equal
     srv.close()
     ctx.close()
-    return 0 if equal else 1
+    return out
+
+
+def run_serve(args, rank, world):
+    """--workload serve: the served mixed stream (see _serve_measure) at saturation and as Poisson
+    streams at 30% and 60% of the saturated rate."""
+    import torch
+    dev = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(dev)
+    with Clocks(dev) as clk:
+        r = _serve_measure(dev, args.queries, (0.3, 0.6))
+    line = {"metric": "served queries/s (square_root : approx_cut : parallel_cc = 2:1:1, 10^3-10^7 edges)",
+            "value": r["value"], "unit": "queries/s", "n_gpus": 1, "steps": r["queries"], "warmup": 3,
+            "ms_per_step": 1e3 / r["value"], "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "u64", "data": "synthetic (device-generated G(n, p) and R-MAT)",
+            "config": {"workload": "served mixed stream", "graphs": r["graphs"], "edges_range": r["edges_range"],
+                       "hbm_budget_bytes": 120 << 30, "queries": r["queries"]},
+            "clocks": clk.summary()}
+    line.update({k: r[k] for k in ("saturation", "poisson_30pct", "poisson_60pct", "plain_path", "speedup_vs_plain",
+                                   "results_equal_plain", "note")})
+    if rank == 0:
+        print(json.dumps(line))
+    return 0 if r["results_equal_plain"] else 1
 
 
 def main():
@@ -709,6 +802,9 @@ def main():
                     help="cc: the benchmark line; the others: one workload's line")
     ap.add_argument("--graphs", type=int, default=4096, help="ks-batch: graphs in the batch")
     ap.add_argument("--queries", type=int, default=200, help="serve: queries in the trace")
+    ap.add_argument("--check-exact", action="store_true", help="ks-batch: check every cut against the exact cut")
+    ap.add_argument("--no-batch", action="store_true", help="skip the batched min-cut measurement")
+    ap.add_argument("--no-serve", action="store_true", help="skip the served-stream measurement")
     args = ap.parse_args()
     if args.steps is None:
         args.steps = {"cc": 20, "cc-rmat22": 20, "ks-batch": 3}.get(args.workload, 10)

@@ -85,16 +85,28 @@ def build_cli():
     return out
 
 
-def build_oracle():
+# Where the reference's source tree is mounted: CAC_REFERENCE_ROOT, else the build container's
+# mount point. The reference checker under oracle/_ref is built only where that tree exists.
+DEFAULT_REFERENCE_ROOT = "/root/reference"
+
+
+def reference_root():
+    return os.environ.get("CAC_REFERENCE_ROOT", DEFAULT_REFERENCE_ROOT)
+
+
+def build_oracle(ref=None):
     _run(["make", "-s", "-C", os.path.join(ROOT, "oracle")])
-    ref = "/root/reference"
-    if os.path.isdir(ref):  # the reference tree exists only where it is mounted
+    ref = ref or reference_root()
+    if os.path.isdir(ref):
         _run(["make", "-s", "-j8", "-C", os.path.join(ROOT, "oracle", "refbuild"), "REF=" + ref])
 
 
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--no-oracle", action="store_true")
+    ap.add_argument("--reference", default=None,
+                    help="reference source tree for oracle/_ref (default: $CAC_REFERENCE_ROOT or %s)"
+                    % DEFAULT_REFERENCE_ROOT)
     ap.add_argument("-v", "--verbose", action="store_true")
     ap.add_argument("--ptxas-info", action="store_true", help="print registers / spills / smem per kernel")
     a = ap.parse_args()
@@ -102,7 +114,7 @@ def main():
     build_lib(verbose=a.verbose or a.ptxas_info, extra_flags=extra)
     build_cli()
     if not a.no_oracle:
-        build_oracle()
+        build_oracle(a.reference)
     print("built", os.path.join(LIBDIR, "libcac.so"))
 
 

@@ -8,6 +8,27 @@
 
 using namespace cac;
 
+namespace {
+
+// SquareRootCut::runLowConcurrencyMaster (SquareRootCut.cpp:99-100): ceil(total / ranks) trials
+// per rank, ranks * that many in all. The product is formed in 64 bits: with many virtual ranks
+// on a dense graph it can pass 2^32, which the result's uint32 columns cannot report.
+int trial_layout(const char *who, double total, uint32_t ranks, uint32_t *per, uint32_t *all) {
+    const double per_d = std::ceil(total / ranks);
+    const uint64_t per64 = per_d < 4294967296.0 ? (uint64_t)per_d : (1ull << 32);
+    const uint64_t all64 = per64 * ranks;
+    if (per64 > 0xFFFFFFFFull || all64 > 0xFFFFFFFFull) {
+        set_error(std::string(who) + ": " + std::to_string(all64) + " trials (" + std::to_string(ranks) +
+                  " virtual ranks) exceed 2^32 - 1");
+        return CAC_ERR_INVALID;
+    }
+    *per = (uint32_t)per64;
+    *all = (uint32_t)all64;
+    return CAC_OK;
+}
+
+}  // namespace
+
 extern "C" {
 
 int cac_mincut_trials(cac_ctx *ctx, const cac_graph *g, uint32_t seed, uint32_t virtual_ranks,
@@ -50,13 +71,14 @@ int cac_mincut(cac_ctx *ctx, const cac_graph *g, double p, uint32_t seed, uint32
     *res = cac_mincut_result{};
     // SquareRootCut::runLowConcurrencyMaster (SquareRootCut.cpp:99-100)
     const double total = number_of_trials(g->n, g->m, p);
-    const uint32_t per = (uint32_t)std::ceil(total / virtual_ranks);
+    uint32_t per = 0, all = 0;
+    CAC_TRY(trial_layout("cac_mincut", total, virtual_ranks, &per, &all));
     res->trials_per_rank = per;
-    res->total_trials = per * virtual_ranks;
+    res->total_trials = all;
     res->intermediate = intermediate_size(g->n, g->m);
     // SquareRootCut::lowConcurrency (SquareRootCut.cpp:11-13): the group variant is chosen when
     // p >= 2 * trials; on one GPU every trial runs in one batch either way.
-    res->high_concurrency = virtual_ranks >= 2u * (uint32_t)total ? 1u : 0u;
+    res->high_concurrency = (double)virtual_ranks >= 2.0 * total ? 1u : 0u;
     const uint64_t n_tr = (uint64_t)res->total_trials;
     void *d = nullptr;
     CAC_TRY(stream_alloc(ctx, &d, n_tr * 8));
@@ -133,12 +155,13 @@ int cac_mincut_batch(cac_ctx *ctx, const cac_mincut_query *queries, uint32_t cou
         }
         const uint32_t ranks = q.virtual_ranks ? q.virtual_ranks : 1;
         const double trials = number_of_trials(q.graph->n, q.graph->m, q.success_probability);
-        const uint32_t per = (uint32_t)std::ceil(trials / ranks);
+        uint32_t per = 0, all = 0;
+        CAC_TRY(trial_layout("cac_mincut_batch", trials, ranks, &per, &all));
         results[i] = cac_mincut_result{};
         results[i].trials_per_rank = per;
-        results[i].total_trials = per * ranks;
+        results[i].total_trials = all;
         results[i].intermediate = intermediate_size(q.graph->n, q.graph->m);
-        results[i].high_concurrency = ranks >= 2u * (uint32_t)trials ? 1u : 0u;
+        results[i].high_concurrency = (double)ranks >= 2.0 * trials ? 1u : 0u;
         qs[i] = MincutQuery{q.graph, q.seed, ranks, per, nullptr};
         total += (uint64_t)per * ranks;
     }

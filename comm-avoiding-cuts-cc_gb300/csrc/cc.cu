@@ -1156,15 +1156,35 @@ __global__ void cc_noalloc_count(const uint32_t *total, uint32_t *out) {
     *out = total[kErrWord] ? 0xFFFFFFFFu : total[0];
 }
 
-// Per-device set-up, done once with that device current: the device address of the scratch
-// array (its host-side name is only a stand-in) and the SM count used to size the grids.
+// Per-device set-up, with that device current: the device address of the scratch array (its
+// host-side name is only a stand-in) and the SM count used to size the grids. A device counts as
+// set up only once both succeeded, so a call that failed here (for instance one made while its
+// stream was being captured, when the module may still have to be loaded) is retried in full by
+// the next call instead of failing for the rest of the process.
 struct NoAllocDevice {
-    std::once_flag once;
+    std::mutex mu;
+    bool ready = false;
     NoAllocScratch *scratch = nullptr;
     int sms = 0;
-    cudaError_t err = cudaSuccess;
 };
 NoAllocDevice g_noalloc_devices[kNoAllocMaxDevices];
+
+cudaError_t noalloc_setup(NoAllocDevice &D, int dev) {
+    std::lock_guard<std::mutex> lock(D.mu);
+    if (D.ready) return cudaSuccess;
+    void *p = nullptr;
+    int sms = 0;
+    cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+    if (e == cudaSuccess) e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    if (e != cudaSuccess) {
+        cudaGetLastError();  // not sticky: the next call tries again
+        return e;
+    }
+    D.scratch = reinterpret_cast<NoAllocScratch *>(p);
+    D.sms = sms;
+    D.ready = true;
+    return cudaSuccess;
+}
 
 }  // namespace
 }  // namespace cac
@@ -1188,14 +1208,10 @@ extern "C" int cac_cc_noalloc(uint32_t n, uint64_t m, const uint32_t *u_dev, con
         return CAC_ERR_INVALID;
     }
     NoAllocDevice &D = g_noalloc_devices[dev];
-    std::call_once(D.once, [&D, dev]() {
-        void *p = nullptr;
-        D.err = cudaGetSymbolAddress(&p, g_noalloc_scratch);
-        if (D.err == cudaSuccess) D.err = cudaDeviceGetAttribute(&D.sms, cudaDevAttrMultiProcessorCount, dev);
-        if (D.err == cudaSuccess) D.scratch = reinterpret_cast<NoAllocScratch *>(p);
-    });
-    if (D.err != cudaSuccess || !D.scratch) {
-        set_error(std::string("cac_cc_noalloc: scratch set-up failed: ") + cudaGetErrorString(D.err));
+    const cudaError_t se = noalloc_setup(D, dev);
+    if (se != cudaSuccess) {
+        set_error(std::string("cac_cc_noalloc: scratch set-up failed (the call may be retried): ") +
+                  cudaGetErrorString(se));
         return CAC_ERR_CUDA;
     }
     cudaStream_t s = (cudaStream_t)stream;
@@ -1204,7 +1220,8 @@ extern "C" int cac_cc_noalloc(uint32_t n, uint64_t m, const uint32_t *u_dev, con
         return (int)std::max<uint64_t>(1, std::min<uint64_t>((work + kThreads - 1) / kThreads, (uint64_t)D.sms * 8));
     };
     if (n == 0) {
-        if (num_components_dev) CAC_CUDA_TRY(cudaMemsetAsync(num_components_dev, 0, 4, s));
+        // no vertices: 0 components, or 0xFFFFFFFF when there are edges (every endpoint is >= n)
+        if (num_components_dev) CAC_CUDA_TRY(cudaMemsetAsync(num_components_dev, m ? 0xFF : 0, 4, s));
         return CAC_OK;
     }
     // Nothing in the scratch needs to start at zero: parent[] is initialised by cc_init, the tile

@@ -369,8 +369,12 @@ int cac_server_submit(cac_server *s, const cac_request *req, uint64_t *ticket) {
             return CAC_ERR_UNSUPPORTED;
         }
         const uint32_t total = number_of_trials(g->n, g->m, req->success_probability);
-        r->per_rank = (total + r->ranks - 1) / r->ranks;
+        r->per_rank = (uint32_t)(((uint64_t)total + r->ranks - 1) / r->ranks);
         r->trials = (uint64_t)r->per_rank * r->ranks;
+        if (r->trials > 0xFFFFFFFFull) {
+            set_error("cac_server_submit: " + std::to_string(r->trials) + " trials exceed 2^32 - 1");
+            return CAC_ERR_INVALID;
+        }
         const uint64_t tt = std::min<uint64_t>(t, g->n);
         r->est_bytes = (t < g->n ? r->trials : 1) * tt * tt * 8 * 3 + r->trials * 8;
     } else if (req->kind == CAC_QUERY_APPROX &&

@@ -147,8 +147,10 @@ int cac_cc_edges(cac_ctx *ctx, uint32_t n, uint64_t m, const uint32_t *u_host, c
  * labels_dev (nullable) gets the same labels as cac_cc; num_components_dev (nullable, device)
  * gets the component count, or 0xFFFFFFFF when an edge endpoint was >= n (such edges are skipped:
  * the edge arrays are not validated beforehand, every endpoint is checked before it is used and
- * the labels are then not valid). The first call on a device resolves the array's device address
- * (make that first call before any stream capture). All calls share the one array: calls whose
+ * the labels are then not valid; with n = 0 and m > 0 every endpoint is out of range, so the count
+ * also reads 0xFFFFFFFF). The first call on a device resolves the array's device address
+ * (make that first call before any stream capture); if that set-up fails the call returns
+ * CAC_ERR_CUDA and a later call retries it. All calls share the one array: calls whose
  * work overlaps on the GPU (other streams, other host threads) race and must be serialised by
  * the caller. */
 int cac_cc_noalloc(uint32_t n, uint64_t m, const uint32_t *u_dev, const uint32_t *v_dev, uint32_t *labels_dev,

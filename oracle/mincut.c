@@ -185,6 +185,106 @@ static uint64_t sw_sparse(uint32_t n, uint64_t m, const uint32_t *u, const uint3
     return best;
 }
 
+/* Nagamochi-Ono-Ibaraki exact minimum cut (H. Nagamochi, T. Ono, T. Ibaraki, "Implementing an
+ * efficient minimum capacity cut algorithm", Math. Programming 67, 1994) for graphs too large for
+ * one Stoer-Wagner phase per vertex. Each phase runs one maximum-adjacency ordering of the
+ * current (merged, loop-free) graph from vertex 0; when vertex x is scanned, every unscanned
+ * neighbour y gets r(y) += w(x, y) and the edge is given q = r(y). The maximum-adjacency lemma
+ * gives q <= lambda(x, y), the local edge connectivity of its ends, so every edge with
+ * q >= best (best = the smallest cut found so far, starting at the minimum weighted degree) can
+ * be contracted without losing a cut below best. The last two vertices of the ordering are
+ * merged too (Stoer-Wagner's lemma: lambda of that pair is r(last) = d(last) >= best), so every
+ * phase removes at least one vertex. After contracting, best takes the new minimum weighted
+ * degree. A vertex left unscanned when the heap empties means the graph is disconnected: 0.
+ * The value is the same as the Stoer-Wagner routines above (checked by the oracle pin tests). */
+typedef struct { uint64_t key; uint64_t w; } kedge;
+static int kedge_cmp(const void *a, const void *b) {
+    const uint64_t x = ((const kedge *)a)->key, y = ((const kedge *)b)->key;
+    return x < y ? -1 : x > y;
+}
+uint64_t orc_exact_mincut_noi(uint32_t n, uint64_t m, const uint32_t *u, const uint32_t *v, const uint32_t *w) {
+    if (n < 2) return U64MAX;
+    kedge *E = (kedge *)malloc(sizeof(kedge) * (m ? m : 1));
+    uint64_t me = 0;
+    for (uint64_t e = 0; e < m; e++) {
+        if (u[e] == v[e] || w[e] == 0) continue;
+        uint32_t a = u[e] < v[e] ? u[e] : v[e], b = u[e] ^ v[e] ^ a;
+        E[me].key = ((uint64_t)a << 32) | b; E[me].w = w[e]; me++;
+    }
+    uint32_t k = n;
+    uint64_t best = U64MAX;
+    uint64_t *off = (uint64_t *)malloc(sizeof(uint64_t) * (n + 1));
+    uint32_t *adj = (uint32_t *)malloc(sizeof(uint32_t) * (2 * me + 1));
+    uint64_t *aw = (uint64_t *)malloc(sizeof(uint64_t) * (2 * me + 1));
+    uint64_t *fill = (uint64_t *)malloc(sizeof(uint64_t) * (n + 1));
+    uint64_t *r = (uint64_t *)malloc(sizeof(uint64_t) * n), *deg = (uint64_t *)malloc(sizeof(uint64_t) * n);
+    uint8_t *done = (uint8_t *)malloc(n);
+    uint32_t *p = (uint32_t *)malloc(sizeof(uint32_t) * n), *lab = (uint32_t *)malloc(sizeof(uint32_t) * n);
+    hnode *heap = (hnode *)malloc(sizeof(hnode) * (2 * me + n + 1));
+    for (;;) {
+        /* merge parallel edges: sort by (min, max) end and sum */
+        qsort(E, me, sizeof(kedge), kedge_cmp);
+        uint64_t j = 0;
+        for (uint64_t e = 0; e < me; e++) {
+            if (j && E[j - 1].key == E[e].key) E[j - 1].w += E[e].w;
+            else E[j++] = E[e];
+        }
+        me = j;
+        memset(deg, 0, sizeof(uint64_t) * k);
+        for (uint64_t e = 0; e < me; e++) { deg[E[e].key >> 32] += E[e].w; deg[(uint32_t)E[e].key] += E[e].w; }
+        for (uint32_t i = 0; i < k; i++) if (deg[i] < best) best = deg[i];
+        if (k <= 2 || best == 0) break;
+        /* CSR, both directions */
+        memset(off, 0, sizeof(uint64_t) * (k + 1));
+        for (uint64_t e = 0; e < me; e++) { off[(E[e].key >> 32) + 1]++; off[(uint32_t)E[e].key + 1]++; }
+        for (uint32_t i = 0; i < k; i++) off[i + 1] += off[i];
+        memcpy(fill, off, sizeof(uint64_t) * (k + 1));
+        for (uint64_t e = 0; e < me; e++) {
+            const uint32_t a = (uint32_t)(E[e].key >> 32), b = (uint32_t)E[e].key;
+            adj[fill[a]] = b; aw[fill[a]++] = E[e].w;
+            adj[fill[b]] = a; aw[fill[b]++] = E[e].w;
+        }
+        /* one maximum-adjacency ordering; contractible pairs joined in a union-find */
+        for (uint32_t i = 0; i < k; i++) { r[i] = 0; done[i] = 0; p[i] = i; }
+        size_t hs = 0;
+        hpush(heap, &hs, 0, 0);
+        uint32_t scanned = 0, prev = 0, last = 0;
+        while (hs > 0) {
+            hnode t = hpop(heap, &hs);
+            const uint32_t x = t.v;
+            if (done[x] || t.k != r[x]) continue;
+            done[x] = 1;
+            scanned++;
+            prev = last; last = x;
+            for (uint64_t q = off[x]; q < off[x + 1]; q++) {
+                const uint32_t y = adj[q];
+                if (done[y]) continue;
+                r[y] += aw[q];
+                if (r[y] >= best) { uint32_t a = sfind(p, x), b = sfind(p, y); if (a != b) p[a < b ? b : a] = a < b ? a : b; }
+                hpush(heap, &hs, r[y], y);
+            }
+        }
+        if (scanned < k) { best = 0; break; }
+        { uint32_t a = sfind(p, prev), b = sfind(p, last); if (a != b) p[a < b ? b : a] = a < b ? a : b; }
+        /* contract: label = rank of each set's smallest member */
+        uint32_t nk = 0;
+        for (uint32_t i = 0; i < k; i++) { const uint32_t rt = sfind(p, i); lab[i] = rt == i ? nk++ : lab[rt]; }
+        j = 0;
+        for (uint64_t e = 0; e < me; e++) {
+            const uint32_t a = lab[E[e].key >> 32], b = lab[(uint32_t)E[e].key];
+            if (a == b) continue;
+            E[j].key = a < b ? ((uint64_t)a << 32) | b : ((uint64_t)b << 32) | a;
+            E[j].w = E[e].w; j++;
+        }
+        me = j;
+        k = nk;
+        if (k < 2) break;
+    }
+    free(E); free(off); free(adj); free(aw); free(fill); free(r); free(deg); free(done); free(p); free(lab);
+    free(heap);
+    return best;
+}
+
 uint64_t orc_exact_mincut(uint32_t n, uint64_t m, const uint32_t *u, const uint32_t *v, const uint32_t *w) {
     if (n < 2) return U64MAX;
     if (n <= 1024) {

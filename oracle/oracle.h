@@ -71,6 +71,8 @@ uint64_t orc_cc_sample_count(uint32_t n, uint64_t edges_left);
 uint64_t orc_stoer_wagner_dense(uint32_t n, uint64_t *mat);
 /* Exact min cut of an edge list (builds the dense matrix; n <= ~10^4). */
 uint64_t orc_exact_mincut(uint32_t n, uint64_t m, const uint32_t *u, const uint32_t *v, const uint32_t *w);
+/* the same value by Nagamochi-Ono-Ibaraki contractions (fast on graphs of thousands of vertices) */
+uint64_t orc_exact_mincut_noi(uint32_t n, uint64_t m, const uint32_t *u, const uint32_t *v, const uint32_t *w);
 
 /* ---- square_root trial semantics ---- */
 /* SquareRootCut::intermediate_size (SquareRootCut.cpp:63-70) with base_case_multiplier 2. */

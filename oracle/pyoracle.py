@@ -42,6 +42,8 @@ def lib():
         L.orc_stoer_wagner_dense.restype = ctypes.c_uint64
         L.orc_exact_mincut.argtypes = [ctypes.c_uint32, ctypes.c_uint64, _u32p, _u32p, _u32p]
         L.orc_exact_mincut.restype = ctypes.c_uint64
+        L.orc_exact_mincut_noi.argtypes = [ctypes.c_uint32, ctypes.c_uint64, _u32p, _u32p, _u32p]
+        L.orc_exact_mincut_noi.restype = ctypes.c_uint64
         L.orc_intermediate_size.argtypes = [ctypes.c_uint32, ctypes.c_uint64]
         L.orc_intermediate_size.restype = ctypes.c_uint32
         L.orc_number_of_trials.argtypes = [ctypes.c_uint32, ctypes.c_uint64, ctypes.c_double]
@@ -139,6 +141,20 @@ def stoer_wagner_dense(mat):
 def exact_mincut(n, u, v, w):
     u, v, w = _c32(u), _c32(v), _c32(w)
     return int(lib().orc_exact_mincut(n, len(u), _p32(u), _p32(v), _p32(w)))
+
+
+def exact_mincut_noi(n, u, v, w):
+    u, v, w = _c32(u), _c32(v), _c32(w)
+    return int(lib().orc_exact_mincut_noi(n, len(u), _p32(u), _p32(v), _p32(w)))
+
+
+def exact_mincut_many(graphs, threads=None):
+    """Exact cuts of [(n, u, v, w), ...] on `threads` host threads (ctypes releases the GIL)."""
+    import concurrent.futures as cf
+    import os
+    threads = threads or os.cpu_count() or 1
+    with cf.ThreadPoolExecutor(max_workers=threads) as ex:
+        return list(ex.map(lambda g: exact_mincut_noi(*g), graphs))
 
 
 def intermediate_size(n, m):

@@ -4,9 +4,10 @@ Runs the reference's own code, compiled unmodified by oracle/refbuild into oracl
 (single-rank MPI stand-in + union-by-rank disjoint-sets stand-in), on
   * the reference's known-answer inputs (test_inputs/*.graph),
   * seeded synthetic graphs from graphgen (regenerated from their specs at test time),
-and records its outputs. Only runs where the reference tree is mounted:
+and records its outputs. Only runs where the reference tree is mounted; its root comes from
+--reference, else $CAC_REFERENCE_ROOT, else the build container's mount point:
 
-    make -C oracle/refbuild REF=/root/reference && python tests/golden/make_golden.py
+    make -C oracle/refbuild REF=<tree> && python tests/golden/make_golden.py --reference <tree>
 """
 import hashlib
 import json
@@ -19,7 +20,7 @@ import numpy as np
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 ROOT = os.path.dirname(os.path.dirname(HERE))
-REF_TREE = "/root/reference"
+REF_TREE = os.environ.get("CAC_REFERENCE_ROOT", "/root/reference")
 REF_BIN = os.path.join(ROOT, "oracle", "_ref")
 sys.path.insert(0, os.path.join(ROOT, "comm-avoiding-cuts-cc_gb300"))
 import graphgen  # noqa: E402
@@ -101,6 +102,11 @@ KS_TRIAL_PROBABILITIES = [0.0, 0.5, 0.9, 0.95, 0.99]
 
 
 def main():
+    global REF_TREE
+    import argparse
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--reference", default=REF_TREE, help="the reference's source tree")
+    REF_TREE = ap.parse_args().reference
     if not os.path.isdir(REF_TREE) or not os.path.exists(os.path.join(REF_BIN, "cc_labels")):
         sys.exit("needs the reference tree and oracle/_ref (make -C oracle/refbuild)")
     # 1. sitmo known answers from the reference engine

@@ -94,6 +94,37 @@ def test_sparse_and_dense_stoer_wagner_agree():
         assert O.exact_mincut(n, u, v, w) == O.stoer_wagner_dense(mat)
 
 
+def test_noi_exact_cut_equals_stoer_wagner(golden):
+    # the Nagamochi-Ono-Ibaraki routine (used for thousands of graphs at a time) against the
+    # Stoer-Wagner routines on the reference-pinned graphs, on random graphs of every family and
+    # weight range (including disconnected ones, cut 0), and on graphs of the batched population
+    import graphgen
+    import workloads
+    for name, r in golden("ref_test_inputs.json").items():
+        if "exact_cut" in r:
+            assert O.exact_mincut_noi(r["n"], r["u"], r["v"], r["w"]) == r["exact_cut"], name
+    for spec in golden("mincut_seeded.json"):
+        n, u, v, w = make_graph(spec)
+        assert O.exact_mincut_noi(n, u, v, w) == spec["exact_cut"]
+    for i in range(120):
+        rng = np.random.default_rng(i)
+        n = int(rng.integers(3, 300))
+        kind = i % 4
+        if kind == 0:
+            g = graphgen.erdos_renyi(n, float(rng.uniform(0.01, 0.3)), i, wmax=int(rng.integers(1, 100)))
+        elif kind == 1:
+            g = graphgen.watts_strogatz(max(n, 12), 6, 0.4, i, wmax=100)
+        elif kind == 2:
+            g = graphgen.erdos_renyi_m(n, float(rng.uniform(1, 10)), i, wmax=5)
+        else:
+            g = graphgen.erdos_renyi(n, 0.02, i, wmax=1)
+        assert O.exact_mincut_noi(*g) == O.exact_mincut(*g), i
+    specs = workloads.uneven_population(4096)
+    for sp in [s for s in specs if 1100 < s["n"] < 1600][:4]:
+        g = workloads.host_arrays(sp)
+        assert O.exact_mincut_noi(*g) == O.exact_mincut(*g), sp
+
+
 def test_trial_values_are_upper_bounds_and_reach_the_cut(golden):
     spec = golden("mincut_seeded.json")[0]
     n, u, v, w = make_graph(spec)

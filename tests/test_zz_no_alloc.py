@@ -20,13 +20,17 @@ def _device_u32(torch, a):
     return torch.from_numpy(np.ascontiguousarray(a, dtype=np.uint32).view(np.int32)).cuda()
 
 
-def _noalloc(libcac, torch, n, u, v):
-    du, dv = _device_u32(torch, u), _device_u32(torch, v)
+def _noalloc(libcac, torch, n, u, v, offset=0, want_labels=True, want_count=True):
+    """One call through the C ABI. offset > 0 places the edge arrays `offset` elements into their
+    device buffers, so they are not 16-byte aligned and the scalar edge pass runs."""
+    du = _device_u32(torch, np.concatenate([np.zeros(offset, np.uint32), u]))[offset:]
+    dv = _device_u32(torch, np.concatenate([np.zeros(offset, np.uint32), v]))[offset:]
     labels = torch.full((max(n, 1),), -1, dtype=torch.int32, device="cuda")
     count = torch.full((1,), -1, dtype=torch.int32, device="cuda")
     stream = torch.cuda.current_stream()
     st = libcac.lib().cac_cc_noalloc(n, len(u), ctypes.c_void_p(du.data_ptr()), ctypes.c_void_p(dv.data_ptr()),
-                                     ctypes.c_void_p(labels.data_ptr()), ctypes.c_void_p(count.data_ptr()),
+                                     ctypes.c_void_p(labels.data_ptr()) if want_labels else None,
+                                     ctypes.c_void_p(count.data_ptr()) if want_count else None,
                                      ctypes.c_void_p(stream.cuda_stream))
     assert st == 0, libcac.lib().cac_last_error()
     stream.synchronize()
@@ -63,3 +67,28 @@ def test_endpoint_out_of_range_is_reported_in_the_count(ctx, libcac):
     count, labels = _noalloc(libcac, torch, n, u, v)
     want_count, want = O.cc_labels(n, u, v)
     assert count == want_count and np.array_equal(labels, want)
+
+
+def test_unaligned_edge_arrays_and_optional_outputs(libcac):
+    # edge arrays one element past a 16-byte boundary run the scalar edge pass; either output may
+    # be left out, and what is asked for is still exact
+    torch = pytest.importorskip("torch")
+    n, u, v, _ = graphgen.erdos_renyi_m(30000, 1.1, 7, wmax=1)
+    want_count, want = O.cc_labels(n, u, v)
+    count, labels = _noalloc(libcac, torch, n, u, v, offset=1)
+    assert count == want_count and np.array_equal(labels, want)
+    count, labels = _noalloc(libcac, torch, n, u, v, offset=3, want_labels=False)
+    assert count == want_count
+    assert np.all(labels == 0xFFFFFFFF)  # untouched
+    count, labels = _noalloc(libcac, torch, n, u, v, want_count=False)
+    assert count == -1 and np.array_equal(labels, want)
+
+
+def test_no_vertices(libcac):
+    # n = 0: no edges gives 0 components; any edge has an endpoint >= n, so the count reads 0xFFFFFFFF
+    torch = pytest.importorskip("torch")
+    empty = np.zeros(0, np.uint32)
+    count, _ = _noalloc(libcac, torch, 0, empty, empty)
+    assert count == 0
+    count, _ = _noalloc(libcac, torch, 0, np.array([0, 1], np.uint32), np.array([1, 2], np.uint32))
+    assert count & 0xFFFFFFFF == 0xFFFFFFFF
