@@ -104,6 +104,9 @@ struct cac_graph {
     uint32_t *v = nullptr;  // device, m entries
     uint32_t *w = nullptr;  // device, m entries (all ones when the input had no weights)
     uint64_t bytes = 0;
+    // smallest weighted vertex degree (a single-vertex cut), computed on first use
+    bool min_degree_known = false;
+    uint64_t min_degree = 0;
 };
 
 namespace cac {
@@ -117,6 +120,10 @@ template <typename F>
 inline int smem_optin(cac_ctx *ctx, F *func) {
     return smem_optin(ctx, reinterpret_cast<const void *>(func));
 }
+
+// The graph's minimum weighted degree: the cut around one vertex, an upper bound of the minimum
+// cut that every square_root answer also takes (computed on ctx's stream once, then cached).
+int graph_min_degree(cac_ctx *ctx, cac_graph *g, uint64_t *out);
 
 // Device memory accounting against the ctx budget.
 int dev_alloc(cac_ctx *ctx, void **p, size_t bytes);

@@ -80,6 +80,8 @@ int cac_mincut(cac_ctx *ctx, const cac_graph *g, double p, uint32_t seed, uint32
     // p >= 2 * trials; on one GPU every trial runs in one batch either way.
     res->high_concurrency = (double)virtual_ranks >= 2.0 * total ? 1u : 0u;
     const uint64_t n_tr = (uint64_t)res->total_trials;
+    uint64_t min_degree = 0;
+    CAC_TRY(graph_min_degree(ctx, const_cast<cac_graph *>(g), &min_degree));
     void *d = nullptr;
     CAC_TRY(stream_alloc(ctx, &d, n_tr * 8));
     float ms = 0;
@@ -88,7 +90,7 @@ int cac_mincut(cac_ctx *ctx, const cac_graph *g, double p, uint32_t seed, uint32
         std::vector<uint64_t> cuts(n_tr);
         cudaError_t e = cudaMemcpy(cuts.data(), d, n_tr * 8, cudaMemcpyDeviceToHost);
         if (e != cudaSuccess) { set_error(cudaGetErrorString(e)); st = CAC_ERR_CUDA; }
-        else res->cut = *std::min_element(cuts.begin(), cuts.end());
+        else res->cut = std::min(min_degree, *std::min_element(cuts.begin(), cuts.end()));
     }
     res->device_ms = ms;
     stream_free(ctx, d, n_tr * 8);
@@ -166,6 +168,9 @@ int cac_mincut_batch(cac_ctx *ctx, const cac_mincut_query *queries, uint32_t cou
         total += (uint64_t)per * ranks;
     }
     if (total == 0) return CAC_OK;
+    std::vector<uint64_t> min_degree(count);
+    for (uint32_t i = 0; i < count; i++)
+        CAC_TRY(graph_min_degree(ctx, const_cast<cac_graph *>(queries[i].graph), &min_degree[i]));
     void *d = nullptr;
     CAC_TRY(stream_alloc(ctx, &d, total * 8));
     uint64_t off = 0;
@@ -185,7 +190,9 @@ int cac_mincut_batch(cac_ctx *ctx, const cac_mincut_query *queries, uint32_t cou
             off = 0;
             for (uint32_t i = 0; i < count; i++) {
                 const uint64_t t = (uint64_t)qs[i].ranks * qs[i].per_rank;
-                results[i].cut = t ? *std::min_element(cuts.begin() + off, cuts.begin() + off + t) : 0;
+                results[i].cut = t ? std::min(min_degree[i], *std::min_element(cuts.begin() + off,
+                                                                                   cuts.begin() + off + t))
+                                   : 0;
                 results[i].device_ms = ms;
                 off += t;
             }

@@ -202,6 +202,26 @@ __global__ void sitmo_blocks_kernel(uint64_t k0, uint64_t k1, uint64_t k2, uint6
     }
 }
 
+// Weighted degree of every vertex (loops skipped), one u64 atomic per endpoint.
+__global__ void degree_add(const uint32_t *u, const uint32_t *v, const uint32_t *w, uint64_t m,
+                           unsigned long long *deg) {
+    for (uint64_t e = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; e < m; e += (uint64_t)gridDim.x * blockDim.x) {
+        const uint32_t a = u[e], b = v[e];
+        if (a == b) continue;
+        atomicAdd(deg + a, (unsigned long long)w[e]);
+        atomicAdd(deg + b, (unsigned long long)w[e]);
+    }
+}
+
+// Minimum over n degrees: a warp minimum, then one atomicMin per warp.
+__global__ void degree_min(const unsigned long long *deg, uint32_t n, unsigned long long *out) {
+    unsigned long long x = ~0ull;
+    for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (uint64_t)gridDim.x * blockDim.x)
+        x = min(x, deg[i]);
+    for (int o = 16; o > 0; o >>= 1) x = min(x, __shfl_xor_sync(0xffffffffu, x, o));
+    if ((threadIdx.x & 31) == 0) atomicMin(out, x);
+}
+
 int grid1(cac_ctx *ctx, uint64_t work) {
     uint64_t need = (work + 255) / 256;
     return (int)std::max<uint64_t>(1, std::min<uint64_t>(need, (uint64_t)ctx->num_sms * 8));
@@ -219,6 +239,40 @@ int sitmo_blocks(cac_ctx *ctx, const uint64_t key[4], const uint64_t ctr0[4], ui
     CAC_CUDA_TRY(cudaGetLastError());
     CAC_CUDA_TRY(cudaMemcpyAsync(out_host, d, nblocks * 32, cudaMemcpyDeviceToHost, ctx->stream));
     CAC_CUDA_TRY(cudaStreamSynchronize(ctx->stream));
+    return CAC_OK;
+}
+
+int graph_min_degree(cac_ctx *ctx, cac_graph *g, uint64_t *out) {
+    static std::mutex mu;  // graphs may be shared by the threads of a server
+    std::lock_guard<std::mutex> lock(mu);
+    if (!g->min_degree_known) {
+        void *d = nullptr;
+        const size_t bytes = ((size_t)g->n + 1) * 8;
+        CAC_TRY(stream_alloc(ctx, &d, bytes));
+        unsigned long long *deg = static_cast<unsigned long long *>(d), *res = deg + g->n;
+        cudaStream_t s = ctx->stream;
+        unsigned long long h = 0;
+        cudaError_t e = cudaMemsetAsync(deg, 0, (size_t)g->n * 8, s);
+        if (e == cudaSuccess) e = cudaMemsetAsync(res, 0xFF, 8, s);
+        if (e == cudaSuccess && g->m) {
+            degree_add<<<grid1(ctx, g->m), 256, 0, s>>>(g->u, g->v, g->w, g->m, deg);
+            e = cudaGetLastError();
+        }
+        if (e == cudaSuccess) {
+            degree_min<<<grid1(ctx, g->n), 256, 0, s>>>(deg, g->n, res);
+            e = cudaGetLastError();
+        }
+        if (e == cudaSuccess) e = cudaMemcpyAsync(&h, res, 8, cudaMemcpyDeviceToHost, s);
+        stream_free(ctx, d, bytes);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+        if (e != cudaSuccess) {
+            set_error(std::string("minimum weighted degree: ") + cudaGetErrorString(e));
+            return CAC_ERR_CUDA;
+        }
+        g->min_degree = h;
+        g->min_degree_known = true;
+    }
+    *out = g->min_degree;
     return CAC_OK;
 }
 

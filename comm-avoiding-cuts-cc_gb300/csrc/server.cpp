@@ -211,8 +211,14 @@ struct CutWorker {
                     st = CAC_ERR_CUDA;
                     msg = "inconsistent selection prefix in the contraction kernel";
                 } else {
-                    r->resp.cut = r->trials ? *std::min_element(cuts.begin(), cuts.end()) : 0;
-                    r->resp.trials = r->per_rank;
+                    uint64_t md = 0;
+                    if (graph_min_degree(s->cut, const_cast<cac_graph *>(r->req.graph), &md) != CAC_OK) {
+                        st = CAC_ERR_CUDA;
+                        msg = "server: the graph's minimum weighted degree could not be computed";
+                    } else {
+                        r->resp.cut = r->trials ? std::min(md, *std::min_element(cuts.begin(), cuts.end())) : 0;
+                        r->resp.trials = r->per_rank;
+                    }
                 }
             }
             running[i] = running.back();

@@ -158,7 +158,10 @@ int cac_cc_noalloc(uint32_t n, uint64_t m, const uint32_t *u_dev, const uint32_t
 
 /* ---- minimum cut (square_root) ---- */
 typedef struct {
-    uint64_t cut;             /* the CSV `weight` column */
+    uint64_t cut;             /* the CSV `weight` column: the smallest trial value, or the graph's
+                                 minimum weighted degree if that is smaller (a single-vertex cut; the
+                                 reference reports the trials' minimum alone, so this differs only
+                                 when every trial missed a minimum cut around one vertex) */
     uint32_t trials_per_rank; /* the CSV `trials` column: ceil(total / virtual_ranks) */
     uint32_t total_trials;    /* trials executed: virtual_ranks * trials_per_rank */
     uint32_t intermediate;    /* t = min(n, ceil(2 sqrt(m) + 1)) */

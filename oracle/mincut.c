@@ -496,7 +496,14 @@ uint64_t orc_square_root(uint32_t n, uint64_t m, const uint32_t *u, const uint32
     double total = orc_number_of_trials(n, m, p);
     uint32_t per = (uint32_t)ceil(total / ranks);
     if (per_rank_out) *per_rank_out = per;
+    /* the answer also takes the graph's minimum weighted degree (a single-vertex cut): libcac's
+       square_root reports min(that, every trial), so a query whose trials all contracted the
+       minimum-degree vertex still reports a minimum cut that is a single-vertex cut */
+    uint64_t *deg = (uint64_t *)calloc(n ? n : 1, sizeof(uint64_t));
+    for (uint64_t e = 0; e < m; e++) if (u[e] != v[e]) { deg[u[e]] += w[e]; deg[v[e]] += w[e]; }
     uint64_t best = U64MAX;
+    for (uint32_t i = 0; i < n; i++) if (deg[i] < best) best = deg[i];
+    free(deg);
     for (uint32_t r = 0; r < ranks; r++)
         for (uint32_t i = 0; i < per; i++) {
             uint64_t c = orc_mincut_trial(n, m, u, v, w, seed, r, i);
