@@ -3,7 +3,7 @@
 //
 // Reference round structure            ->  here
 //   root scatters per-rank draw counts    host restates edgesToSamplePerProcessor (cc_plan)
-//   rank r draws engine()%slice samples   cc_sample_hook: sitmo stream (seed + r, 0, 0, 0),
+//   rank r draws engine()%slice samples   cc_sample_draw_hook: sitmo stream (seed + r, 0, 0, 0),
 //     with sitmo(seed + r)                  output k = word k % 8 of block k / 8, the reference's
 //                                           k-th engine output; it picks a 32-edge chunk of the
 //                                           slice (coalesced) instead of one edge
@@ -14,7 +14,7 @@
 //     and repeat while edges remain         edges whose endpoints already share a root are the
 //                                           dropped loops, the rest hook (the final round)
 //   relabel by first appearance           roots = minima, so label = exclusive scan of the
-//                                           root flags (cc_finalize_count/scan/rank/label)
+//                                           root flags (cc_finalize_rank, cc_label_all)
 //
 // Memory layout in HBM: edge endpoints as two uint32 arrays u[m], v[m] (structure of arrays,
 // 16-byte vector loads, 4 edges per load pair); parent[n] uint32 (L2-resident for n up to
@@ -69,6 +69,8 @@ constexpr unsigned kSurvivorBlocksPerSm = 8;
 constexpr uint32_t kStreamPieces = 8;                // sample pieces (and gaps) of a host edge list
 constexpr uint32_t kErrWord = 9;                     // a query's error word (after its count and giant root)
 constexpr uint32_t kErrBadId = 1;                    // an edge endpoint was >= n (the edge was skipped)
+constexpr uint32_t kErrLookback = 2;                 // a tile's look-back gave up waiting (labels invalid)
+constexpr uint32_t kLookbackSpins = 1u << 24;        // bound on one look-back wait (never reached in practice)
 
 struct RankDesc {
     uint64_t slice_off;
@@ -143,53 +145,52 @@ __global__ void cc_init(uint32_t *par, uint32_t n) {
     for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) par[i] = i;
 }
 
-// The draws of the sampling round, one thread per sitmo block (8 draws of one rank). The reference
-// draws single edges (engine() % slice, a random 8-byte gather each); here draw k of rank r
-// (32-bit output k of stream (seed + r, 0, 0, 0), word k % 8 of block k / 8) selects chunk
-// (output % chunks) of kSampleChunk consecutive edges of the rank's slice. The chunk is stored as
-// (first edge | edge count << 32) at the draw's flattened index.
-__global__ void cc_sample_draws(const RankDesc *__restrict__ ranks, int nranks, uint64_t nblocks,
-                                uint64_t *__restrict__ chunks) {
-    pdl_wait();
-    for (uint64_t gb = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; gb < nblocks;
-         gb += (uint64_t)gridDim.x * blockDim.x) {
-        int lo = 0, hi = nranks - 1;  // last rank whose first block <= gb
-        while (lo < hi) {
-            int mid = (lo + hi + 1) >> 1;
-            if (ranks[mid].block_off <= gb) lo = mid; else hi = mid - 1;
-        }
-        const RankDesc rd = ranks[lo];
-        const uint64_t blk = gb - rd.block_off;  // sitmo block index within the rank's stream
-        const u64x4 o = sitmo_block(rd.key0, 0, 0, 0, blk, 0, 0, 0);
-        const uint64_t nchunks = (rd.slice_len + kSampleChunk - 1) / kSampleChunk;
-        const uint64_t end = rd.slice_off + rd.slice_len;
-#pragma unroll
-        for (int j = 0; j < 8; j++) {
-            const uint64_t k = blk * 8 + j;
-            if (k >= rd.draws) break;  // rd.draws counts chunk draws
-            const uint64_t word = o.x[j >> 1];
-            const uint32_t x = (j & 1) ? (uint32_t)(word >> 32) : (uint32_t)word;
-            const uint64_t first = rd.slice_off + (x % nchunks) * kSampleChunk;
-            const uint64_t count = min((uint64_t)kSampleChunk, end - first);
-            chunks[rd.draw_off + k] = first | (count << 32);
-        }
-    }
-}
-
-// One warp per sampled chunk of the draw range [d0, d1): coalesced loads of its edges, each hooked.
+// The sampling round's draws and hooks in one kernel: CTA b (8 warps) owns sitmo block gb = g0 + b
+// of the flattened block list, i.e. 8 consecutive chunk draws of one rank. Thread 0 computes the
+// block (output k of stream (seed + r, 0, 0, 0) is word k % 8 of block k / 8, the reference
+// engine's k-th output) and leaves the 8 chunk descriptors in shared memory; warp j then hooks
+// the edges of chunk j with coalesced loads (32 consecutive edges of the rank's slice behind
+// each draw, instead of the reference's single edge per draw: one coalesced 128-byte load).
 template <bool kCheck>
-__global__ void cc_sample_hook(uint32_t *par, const uint32_t *__restrict__ u, const uint32_t *__restrict__ v,
-                               const uint64_t *__restrict__ chunks, uint64_t d0, uint64_t d1, uint32_t n,
-                               uint32_t *err) {
+__global__ void __launch_bounds__(kThreads) cc_sample_draw_hook(uint32_t *par, const uint32_t *__restrict__ u,
+                                                               const uint32_t *__restrict__ v,
+                                                               const RankDesc *__restrict__ ranks, int nranks,
+                                                               uint64_t g0, uint64_t g1, uint32_t n, uint32_t *err) {
     pdl_wait();
-    const uint32_t lane = threadIdx.x & 31;
-    const uint64_t warps = ((uint64_t)gridDim.x * blockDim.x) >> 5;
-    for (uint64_t d = d0 + (((uint64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5); d < d1; d += warps) {
-        const uint64_t c = chunks[d];
+    __shared__ uint64_t chunk[8];
+    const uint32_t lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    for (uint64_t gb = g0 + blockIdx.x; gb < g1; gb += gridDim.x) {
+        if (threadIdx.x == 0) {
+            int lo = 0, hi = nranks - 1;  // last rank whose first block <= gb
+            while (lo < hi) {
+                const int mid = (lo + hi + 1) >> 1;
+                if (ranks[mid].block_off <= gb) lo = mid; else hi = mid - 1;
+            }
+            const RankDesc rd = ranks[lo];
+            const uint64_t blk = gb - rd.block_off;
+            const u64x4 o = sitmo_block(rd.key0, 0, 0, 0, blk, 0, 0, 0);
+            const uint64_t nchunks = (rd.slice_len + kSampleChunk - 1) / kSampleChunk;
+            const uint64_t end = rd.slice_off + rd.slice_len;
+#pragma unroll
+            for (int j = 0; j < 8; j++) {
+                const uint64_t k = blk * 8 + j;
+                uint64_t c = 0;  // count 0: no draw
+                if (k < rd.draws) {
+                    const uint64_t word = o.x[j >> 1];
+                    const uint32_t x = (j & 1) ? (uint32_t)(word >> 32) : (uint32_t)word;
+                    const uint64_t first = rd.slice_off + (x % nchunks) * kSampleChunk;
+                    c = first | (min((uint64_t)kSampleChunk, end - first) << 32);
+                }
+                chunk[j] = c;
+            }
+        }
+        __syncthreads();
+        const uint64_t c = chunk[warp];
         if (lane < (uint32_t)(c >> 32)) {
             const uint64_t e = (c & 0xFFFFFFFFull) + lane;
             edge_hook_checked<kCheck>(par, __ldg(u + e), __ldg(v + e), n, err);
         }
+        __syncthreads();
     }
 }
 
@@ -223,20 +224,24 @@ __global__ void cc_compress4(uint32_t *par, uint32_t n4) {
 // the tail (the parent array is 256-byte aligned).
 void compress_all(cac_ctx *ctx, uint32_t *par, uint32_t n, cudaStream_t s);
 
-// The most frequent root among kGiantSample vertices spread over [0, n) (compressed parents):
-// every warp finds the mode of its 32 samples (__match_any_sync groups equal roots; ties to the
-// smaller root), each of those 32 candidates is counted over all samples with shared atomics, and
-// the candidate with the largest count wins (ties: the smaller root). The giant component is the
-// mode of most warps whenever it holds a sizeable share of the vertices; the choice only decides
-// which edges the filter can drop, never the labels.
-__global__ void __launch_bounds__(kGiantSample) cc_find_giant(const uint32_t *par, uint32_t n, uint32_t *giant) {
+// The end of the sampling round in one launch: full compression, the giant component and its
+// membership bitmap. Every CTA (kGiantSample threads) first finds the giant itself, from the
+// roots of the same kGiantSample vertices (fixed spread of positions): every warp finds the mode
+// of its 32 samples (__match_any_sync groups equal roots; ties to the smaller root), each of those
+// 32 candidates is counted over all samples with shared atomics, and the candidate with the
+// largest count wins (ties: the smaller root). The walks only read and no hook runs during this
+// kernel, so every CTA sees the same roots and picks the same giant. The choice only decides which
+// edges the filter can drop, never the labels. Then its warps take 32-vertex words: each lane walks its vertex to the root,
+// writes the root back when it differs (only roots are written, as in cc_compress4), and the
+// warp's ballot of (root == giant) is the word. CTA 0 records the giant for the next kernels.
+__global__ void __launch_bounds__(kGiantSample) cc_compress_giant_bitmap(uint32_t *par, uint32_t n, uint32_t *giant,
+                                                                         uint32_t *bits) {
     pdl_wait();
     __shared__ uint32_t cand[kGiantSample / 32], cnt[kGiantSample / 32];
     __shared__ unsigned long long best;
     const uint32_t i = threadIdx.x, lane = i & 31, w = i >> 5;
-    const uint32_t r = par[((uint64_t)i * 2654435761u) % n];  // fixed spread of sample positions
+    const uint32_t r = find_root_ro(par, (uint32_t)(((uint64_t)i * 2654435761u) % n));
     const uint32_t same = __match_any_sync(0xffffffffu, r);
-    // warp argmax of (count, -root) in two 32-bit reductions
     const uint32_t c = __popc(same);
     const uint32_t top = __reduce_max_sync(0xffffffffu, c);
     const uint32_t lo = __reduce_max_sync(0xffffffffu, c == top ? 0xFFFFFFFFu - r : 0u);
@@ -253,23 +258,23 @@ __global__ void __launch_bounds__(kGiantSample) cc_find_giant(const uint32_t *pa
     if (i < kGiantSample / 32)
         atomicMax(&best, ((unsigned long long)cnt[i] << 32) | (0xFFFFFFFFu - cand[i]));
     __syncthreads();
-    if (i == 0) *giant = 0xFFFFFFFFu - (uint32_t)(best & 0xFFFFFFFFu);
-}
-
-// bit v of the bitmap = (parent[v] == giant root), one warp ballot per 32 vertices
-__global__ void cc_giant_bitmap(const uint32_t *par, uint32_t n, const uint32_t *giant, uint32_t *bits) {
-    pdl_wait();
-    const uint32_t g = *giant;
+    const uint32_t g = 0xFFFFFFFFu - (uint32_t)(best & 0xFFFFFFFFu);
+    if (blockIdx.x == 0 && i == 0) *giant = g;
     const uint64_t nw = ((uint64_t)n + 31) / 32;
     const uint64_t warps = ((uint64_t)gridDim.x * blockDim.x) >> 5;
-    for (uint64_t w = ((uint64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5; w < nw; w += warps) {
-        const uint64_t v = w * 32 + (threadIdx.x & 31);
-        const bool in = v < n && par[v] == g;
+    for (uint64_t wd = ((uint64_t)blockIdx.x * blockDim.x + i) >> 5; wd < nw; wd += warps) {
+        const uint64_t x = wd * 32 + lane;
+        bool in = false;
+        if (x < n) {
+            const uint32_t p = par[x];
+            const uint32_t root = p == (uint32_t)x ? p : find_root_ro(par, p);
+            if (root != p) par[x] = root;
+            in = root == g;
+        }
         const uint32_t word = __ballot_sync(0xffffffffu, in);
-        if ((threadIdx.x & 31) == 0) bits[w] = word;
+        if (lane == 0) bits[wd] = word;
     }
 }
-
 
 // Closing pass without a sampling round: every edge hooks, 4 edges per thread step through
 // 16-byte streaming loads.
@@ -532,12 +537,109 @@ __global__ void __launch_bounds__(kThreads) cc_rank_roots(const uint32_t *par, u
     }
 }
 
+// Final compression, root count and root ranks in one pass (replaces cc_finalize_count +
+// cc_scan_tiles + cc_rank_roots). A CTA takes a ticket (tiles are numbered in the order CTAs
+// start, so every tile before it belongs to a CTA already running), compresses its 1024 vertices,
+// counts their roots and publishes the count in its status word; it then looks back over the
+// status words of the tiles before it (decoupled look-back: an inclusive prefix ends the walk,
+// an aggregate is added and the walk continues) and publishes its own inclusive prefix. Roots are
+// then ranked as in cc_rank_roots. The last tile writes the component count. status[] holds
+// ntiles + 1 words and starts at zero: word 0 is the ticket counter, word 1 + t tile t's state
+// (bit 63: inclusive prefix, bit 62: aggregate, low 32 bits: the value). A wait that exceeds its
+// bound sets kErrLookback in the query's error word instead of spinning on.
+template <bool kLabels>
+__global__ void __launch_bounds__(kThreads) cc_finalize_rank(uint32_t *par, uint32_t n, unsigned long long *status,
+                                                             uint32_t *labels, uint32_t *total, uint32_t *err) {
+    pdl_wait();
+    __shared__ uint32_t sh[32];
+    __shared__ uint32_t s_tile, s_prefix;
+    if (threadIdx.x == 0) s_tile = atomicAdd(reinterpret_cast<unsigned int *>(status), 1u);
+    __syncthreads();
+    const uint32_t tile = s_tile;
+    const uint64_t base = (uint64_t)tile * kTile + (uint64_t)threadIdx.x * kTileItems;
+    uint32_t flags = 0, c = 0;
+#pragma unroll
+    for (int k = 0; k < kTileItems; k++) {
+        const uint64_t i = base + k;
+        if (i < n) {
+            const uint32_t p = par[i];
+            const uint32_t r = p == (uint32_t)i ? p : find_root_ro(par, p);
+            if (r != p) par[i] = r;
+            const uint32_t f = r == (uint32_t)i;
+            flags |= f << k;
+            c += f;
+        }
+    }
+    // exclusive scan of c over the block (thread order == vertex order inside the tile)
+    uint32_t sc = c;
+    const int l = threadIdx.x & 31, w = threadIdx.x >> 5;
+    for (int o = 1; o < 32; o <<= 1) {
+        const uint32_t y = __shfl_up_sync(0xffffffffu, sc, o);
+        if (l >= o) sc += y;
+    }
+    if (l == 31) sh[w] = sc;
+    __syncthreads();
+    if (w == 0) {
+        uint32_t t = l < (kThreads >> 5) ? sh[l] : 0;
+        for (int o = 1; o < 32; o <<= 1) {
+            const uint32_t y = __shfl_up_sync(0xffffffffu, t, o);
+            if (l >= o) t += y;
+        }
+        sh[l] = t;
+    }
+    __syncthreads();
+    const uint32_t tile_sum = sh[(kThreads >> 5) - 1];
+    constexpr unsigned long long kInclusive = 1ull << 63, kAggregate = 1ull << 62;
+    volatile unsigned long long *st = status + 1;
+    if (threadIdx.x == 0) {
+        uint32_t prefix = 0;
+        if (tile == 0) {
+            st[0] = kInclusive | tile_sum;
+        } else {
+            st[tile] = kAggregate | tile_sum;
+            bool gave_up = false;
+            for (int64_t j = (int64_t)tile - 1; j >= 0; j--) {
+                unsigned long long x;
+                uint32_t spins = 0;
+                while (((x = st[j]) & (kInclusive | kAggregate)) == 0) {
+                    if (++spins > kLookbackSpins) break;
+                    __nanosleep(32);
+                }
+                if ((x & (kInclusive | kAggregate)) == 0) {
+                    gave_up = true;
+                    break;
+                }
+                prefix += (uint32_t)x;
+                if (x & kInclusive) break;
+            }
+            if (gave_up) atomicOr(err, kErrLookback);
+            __threadfence();
+            st[tile] = kInclusive | (unsigned long long)(prefix + tile_sum);
+        }
+        s_prefix = prefix;
+        if ((uint64_t)(tile + 1) * kTile >= n) *total = prefix + tile_sum;
+    }
+    __syncthreads();
+    if (kLabels) {
+        uint32_t r = s_prefix + (w ? sh[w - 1] : 0) + sc - c;
+#pragma unroll
+        for (int k = 0; k < kTileItems; k++)
+            if ((flags >> k) & 1u) labels[base + k] = r++;
+    }
+}
+
 __global__ void cc_label_all(const uint32_t *par, uint32_t n, uint32_t *labels) {
     pdl_wait();
     for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
         const uint32_t r = par[i];
         if (r != i) labels[i] = labels[r];
     }
+}
+
+// CTAs of cc_compress_giant_bitmap: two per SM (kGiantSample threads each), fewer for small n.
+unsigned giant_grid(cac_ctx *ctx, uint32_t n) {
+    const uint64_t words = ((uint64_t)n + 31) / 32;
+    return (unsigned)std::max<uint64_t>(1, std::min<uint64_t>((words + 31) / 32, (uint64_t)ctx->num_sms * 2));
 }
 
 int grid_for(cac_ctx *ctx, uint64_t work, int per_sm) {
@@ -607,7 +709,7 @@ size_t cc_scratch_bytes(uint32_t n, uint32_t ranks, uint64_t m) {
     const size_t nwords = ((size_t)n + 31) / 32;
     return align_up((size_t)n * 4) + 2 * align_up(ntiles * 4 + 4) + align_up(256) +
            align_up(sizeof(RankDesc) * (size_t)ranks) + align_up(nwords * 4 + 4) + align_up(kMaxRegions * 4) +
-           align_up((m + 4 * (uint64_t)kMaxRegions) * 8);
+           align_up((m + 4 * (uint64_t)kMaxRegions) * 8) + align_up((ntiles + 1) * 8);
 }
 
 namespace {
@@ -626,7 +728,7 @@ struct CCLaunch {
     const RankDesc *h_ranks = nullptr;
     uint32_t ntiles = 0, nwords = 0;
     uint64_t blocks = 0, draws = 0, drawn = 0;  // sitmo blocks, chunk draws, sampled edges
-    uint64_t *chunks = nullptr;                  // per draw: first edge | count << 32
+    unsigned long long *status = nullptr;        // ticket counter + per-tile look-back state
     uint32_t *err = nullptr;                     // total + kErrWord
     bool vec = false;
     bool check = false;                          // endpoints not validated: every kernel checks them
@@ -645,29 +747,29 @@ int cc_enqueue(cac_ctx *ctx, const CCLaunch &L, bool capturing) {
     const uint64_t m = L.m;
     CAC_TRY(record(ctx, 0, capturing));
     CAC_CUDA_TRY(cudaMemsetAsync(L.err, 0, 4, s));
+    CAC_CUDA_TRY(cudaMemsetAsync(L.status, 0, ((size_t)L.ntiles + 1) * 8, s));
     CAC_CUDA_TRY(launch_pdl(cc_init, grid_for(ctx, n, 8), kThreads, 0, s, L.par, n));
     if (L.draws > 0 && m > 0) {
         CAC_CUDA_TRY(cudaMemcpyAsync(L.d_ranks, L.h_ranks, sizeof(RankDesc) * L.ranks, cudaMemcpyHostToDevice, s));
-        // The draws are hooked in kSampleSubrounds slices: forest building from singletons is the
-        // expensive part of CC, and flattening the trees between the early slices keeps the union
-        // walks of the next slice one or two hops long.
-        CAC_CUDA_TRY(launch_pdl(cc_sample_draws, grid_for(ctx, L.blocks, 8), kThreads, 0, s,
-                                static_cast<const RankDesc *>(L.d_ranks), (int)L.ranks, L.blocks, L.chunks));
-        // The first slices build the forest from singletons and need flat trees after them; later
-        // slices mostly hook small trees onto the giant one, so only the last of them is followed
-        // by a compression (which the giant search needs). Measured against a compression after
-        // every slice: BA n=1,024,000 205 vs 214 us per query, R-MAT scale 22 647 vs 666 us.
-        const uint32_t sub = (uint32_t)std::min<uint64_t>(kSampleSubrounds, L.draws);
+        // The draws are hooked in kSampleSubrounds slices of the sitmo blocks (8 chunk draws
+        // each, drawn inside the hooking CTA): forest building from singletons is the expensive
+        // part of CC, and flattening the trees between the early slices keeps the union walks of
+        // the next slice one or two hops long. Later slices mostly hook small trees onto the giant
+        // one, so only the first kCompressedSubrounds are followed by a compression; the last
+        // slice is followed by the fused compression + giant search + bitmap. Measured against a
+        // compression after every slice: BA n=1,024,000 205 vs 214 us per query, R-MAT scale 22
+        // 647 vs 666 us.
+        const uint32_t sub = (uint32_t)std::min<uint64_t>(kSampleSubrounds, L.blocks);
+        auto hook = L.check ? cc_sample_draw_hook<true> : cc_sample_draw_hook<false>;
         for (uint32_t k = 0; k < sub; k++) {
-            const uint64_t d0 = L.draws * k / sub, d1 = L.draws * (k + 1) / sub;
-            auto hook = L.check ? cc_sample_hook<true> : cc_sample_hook<false>;
-            CAC_CUDA_TRY(launch_pdl(hook, grid_for(ctx, (d1 - d0) * 32, 8), kThreads, 0, s, L.par, L.u, L.v,
-                                    static_cast<const uint64_t *>(L.chunks), d0, d1, n, L.err));
-            if (k < kCompressedSubrounds || k + 1 == sub) compress_all(ctx, L.par, n, s);
+            const uint64_t g0 = L.blocks * k / sub, g1 = L.blocks * (k + 1) / sub;
+            const unsigned grid = (unsigned)std::max<uint64_t>(1, std::min<uint64_t>(g1 - g0, (uint64_t)ctx->num_sms * 8));
+            CAC_CUDA_TRY(launch_pdl(hook, grid, kThreads, 0, s, L.par, L.u, L.v,
+                                    static_cast<const RankDesc *>(L.d_ranks), (int)L.ranks, g0, g1, n, L.err));
+            if (k < kCompressedSubrounds && k + 1 < sub) compress_all(ctx, L.par, n, s);
         }
-        CAC_CUDA_TRY(launch_pdl(cc_find_giant, 1, kGiantSample, 0, s, static_cast<const uint32_t *>(L.par), n, L.giant));
-        CAC_CUDA_TRY(launch_pdl(cc_giant_bitmap, grid_for(ctx, n, 8), kThreads, 0, s,
-                                static_cast<const uint32_t *>(L.par), n, static_cast<const uint32_t *>(L.giant), L.bits));
+        CAC_CUDA_TRY(launch_pdl(cc_compress_giant_bitmap, giant_grid(ctx, n), kGiantSample, 0, s, L.par, n, L.giant,
+                                L.bits));
     }
     CAC_TRY(record(ctx, 1, capturing));
     if (m > 0) {
@@ -706,14 +808,14 @@ int cc_enqueue(cac_ctx *ctx, const CCLaunch &L, bool capturing) {
         CAC_TRY(record(ctx, 4, capturing));
     }
     CAC_TRY(record(ctx, 2, capturing));
-    CAC_CUDA_TRY(launch_pdl(cc_finalize_count, L.ntiles, kThreads, 0, s, L.par, n, L.counts));
-    CAC_CUDA_TRY(launch_pdl(cc_scan_tiles, 1, 1024, 0, s, static_cast<const uint32_t *>(L.counts), L.offsets, L.ntiles,
-                            L.total));
     if (L.labels) {
-        CAC_CUDA_TRY(launch_pdl(cc_rank_roots, L.ntiles, kThreads, 0, s, static_cast<const uint32_t *>(L.par), n,
-                                static_cast<const uint32_t *>(L.offsets), L.labels));
+        CAC_CUDA_TRY(launch_pdl(cc_finalize_rank<true>, L.ntiles, kThreads, 0, s, L.par, n, L.status, L.labels,
+                                L.total, L.err));
         CAC_CUDA_TRY(launch_pdl(cc_label_all, grid_for(ctx, n, 8), kThreads, 0, s,
                                 static_cast<const uint32_t *>(L.par), n, L.labels));
+    } else {
+        CAC_CUDA_TRY(launch_pdl(cc_finalize_rank<false>, L.ntiles, kThreads, 0, s, L.par, n, L.status, L.labels,
+                                L.total, L.err));
     }
     CAC_CUDA_TRY(cudaGetLastError());
     CAC_CUDA_TRY(cudaMemcpyAsync(ctx->pinned_u32, L.total, (kErrWord + 1) * 4, cudaMemcpyDeviceToHost, s));
@@ -723,6 +825,10 @@ int cc_enqueue(cac_ctx *ctx, const CCLaunch &L, bool capturing) {
 
 // The query's error word, copied back with its count.
 int check_ids_word(cac_ctx *ctx, uint32_t n) {
+    if (ctx->pinned_u32[kErrWord] & kErrLookback) {
+        set_error("connected components: a labelling tile's look-back wait exceeded its bound");
+        return CAC_ERR_TIMEOUT;
+    }
     if (ctx->pinned_u32[kErrWord] & kErrBadId) {
         set_error("connected components: an edge endpoint is >= n = " + std::to_string(n) +
                   " (such edges were skipped; the labels are not valid)");
@@ -756,8 +862,6 @@ int cc_run(cac_ctx *ctx, uint32_t n, uint64_t m, const uint32_t *d_u, const uint
         return CAC_OK;
     }
     const CCPlan plan = cc_plan(n, m, ranks);
-    uint64_t chunk_slots = 1;
-    for (uint32_t r = 0; r < ranks; r++) chunk_slots += (plan.draws[r] + kSampleChunk - 1) / kSampleChunk;
     CCLaunch L;
     L.n = n;
     L.m = m;
@@ -770,7 +874,7 @@ int cc_run(cac_ctx *ctx, uint32_t n, uint64_t m, const uint32_t *d_u, const uint
     L.vec = ((reinterpret_cast<uintptr_t>(d_u) | reinterpret_cast<uintptr_t>(d_v)) & 15) == 0;
     L.check = check_ids;
 
-    CAC_TRY(arena_reserve(ctx, cc_scratch_bytes(n, ranks, m) + align_up(chunk_slots * 8)));
+    CAC_TRY(arena_reserve(ctx, cc_scratch_bytes(n, ranks, m)));
     arena_reset(ctx);
     L.par = (uint32_t *)arena_take(ctx, (size_t)n * 4);
     L.counts = (uint32_t *)arena_take(ctx, (size_t)L.ntiles * 4 + 4);
@@ -782,7 +886,7 @@ int cc_run(cac_ctx *ctx, uint32_t n, uint64_t m, const uint32_t *d_u, const uint
     L.bits = (uint32_t *)arena_take(ctx, (size_t)L.nwords * 4 + 4);
     L.region_counts = (uint32_t *)arena_take(ctx, kMaxRegions * 4);
     L.surv = (uint2 *)arena_take(ctx, (m + 4 * (uint64_t)kMaxRegions) * 8);
-    L.chunks = (uint64_t *)arena_take(ctx, chunk_slots * 8);
+    L.status = (unsigned long long *)arena_take(ctx, ((size_t)L.ntiles + 1) * 8);
 
     // rank descriptors go through the ctx's pinned staging page when they fit (async copy)
     std::vector<RankDesc> hv;
@@ -899,8 +1003,9 @@ struct StreamLaunch {
     const uint32_t *h_u = nullptr, *h_v = nullptr;  // host edge arrays (copy-engine source)
     const uint32_t *z_u = nullptr, *z_v = nullptr;  // their device views when pinned and aligned, else null
     uint32_t *d_u = nullptr, *d_v = nullptr, *d_labels = nullptr, *h_labels = nullptr;
-    uint32_t *par = nullptr, *counts = nullptr, *offsets = nullptr, *total = nullptr, *giant = nullptr;
+    uint32_t *par = nullptr, *total = nullptr, *giant = nullptr;
     uint32_t *bits = nullptr, *region_counts = nullptr;
+    unsigned long long *status = nullptr;  // ticket counter + per-tile look-back state
     uint2 *surv = nullptr;
     uint32_t ntiles = 0, nwords = 0;
     bool vec = false, filtered = false;
@@ -929,6 +1034,7 @@ int stream_enqueue(cac_ctx *ctx, const StreamLaunch &L, bool capturing) {
     CAC_TRY(record(ctx, 0, capturing));
     cc_init<<<grid_for(ctx, n, 8), kThreads, 0, s>>>(L.par, n);
     CAC_CUDA_TRY(cudaMemsetAsync(L.total + kErrWord, 0, 4, s));
+    CAC_CUDA_TRY(cudaMemsetAsync(L.status, 0, ((size_t)L.ntiles + 1) * 8, s));
     // the copies start after everything already queued on the ctx stream (the staging buffers
     // may still be read by the previous query)
     cudaEvent_t *ev = ctx->chunk_ev;
@@ -965,11 +1071,11 @@ int stream_enqueue(cac_ctx *ctx, const StreamLaunch &L, bool capturing) {
             // trees are flattened so the next part's walks stay one or two hops long
             cc_edge_pass<false, true><<<grid_for(ctx, len, 8), kThreads, 0, s>>>(L.par, L.d_u + e0, L.d_v + e0, len, n,
                                                                            L.total + kErrWord);
-            if (c + 1 < L.parts.size()) compress_all(ctx, L.par, n, s);
             if (L.filtered && c + 1 == kStreamPieces) {
-                cc_find_giant<<<1, kGiantSample, 0, s>>>(L.par, n, L.giant);
-                cc_giant_bitmap<<<grid_for(ctx, n, 8), kThreads, 0, s>>>(L.par, n, L.giant, L.bits);
+                cc_compress_giant_bitmap<<<giant_grid(ctx, n), kGiantSample, 0, s>>>(L.par, n, L.giant, L.bits);
                 CAC_TRY(record(ctx, 1, capturing));
+            } else if (c + 1 < L.parts.size()) {
+                compress_all(ctx, L.par, n, s);
             }
         } else {
             const uint64_t tiles = len >> 8;  // 256-edge tiles; the rest goes to the scalar pass
@@ -992,11 +1098,13 @@ int stream_enqueue(cac_ctx *ctx, const StreamLaunch &L, bool capturing) {
     }
     if (!L.filtered) CAC_TRY(record(ctx, 1, capturing));
     CAC_TRY(record(ctx, 2, capturing));
-    cc_finalize_count<<<L.ntiles, kThreads, 0, s>>>(L.par, n, L.counts);
-    cc_scan_tiles<<<1, 1024, 0, s>>>(L.counts, L.offsets, L.ntiles, L.total);
     if (L.d_labels) {
-        cc_rank_roots<<<L.ntiles, kThreads, 0, s>>>(L.par, n, L.offsets, L.d_labels);
+        cc_finalize_rank<true><<<L.ntiles, kThreads, 0, s>>>(L.par, n, L.status, L.d_labels, L.total,
+                                                             L.total + kErrWord);
         cc_label_all<<<grid_for(ctx, n, 8), kThreads, 0, s>>>(L.par, n, L.d_labels);
+    } else {
+        cc_finalize_rank<false><<<L.ntiles, kThreads, 0, s>>>(L.par, n, L.status, L.d_labels, L.total,
+                                                              L.total + kErrWord);
     }
     CAC_CUDA_TRY(cudaGetLastError());
     CAC_CUDA_TRY(cudaMemcpyAsync(ctx->pinned_u32, L.total, (kErrWord + 1) * 4, cudaMemcpyDeviceToHost, s));
@@ -1044,14 +1152,13 @@ int cc_run_streamed(cac_ctx *ctx, uint32_t n, uint64_t m, const uint32_t *h_u, c
                                : 0;
     L.filtered = L.vec && seg > 0;
     const uint64_t max_gap = L.filtered ? m - (kStreamPieces - 1) * seg - piece : 0;
-    CAC_TRY(arena_reserve(ctx, align_up((size_t)n * 4) + 2 * align_up((size_t)L.ntiles * 4 + 4) + align_up(256) +
+    CAC_TRY(arena_reserve(ctx, align_up((size_t)n * 4) + align_up(((size_t)L.ntiles + 1) * 8) + align_up(256) +
                                    (L.filtered ? align_up((size_t)L.nwords * 4 + 4) + align_up(kMaxRegions * 4) +
                                                      align_up((max_gap + 4 * (uint64_t)kMaxRegions) * 8)
                                                : 0)));
     arena_reset(ctx);
     L.par = (uint32_t *)arena_take(ctx, (size_t)n * 4);
-    L.counts = (uint32_t *)arena_take(ctx, (size_t)L.ntiles * 4 + 4);
-    L.offsets = (uint32_t *)arena_take(ctx, (size_t)L.ntiles * 4 + 4);
+    L.status = (unsigned long long *)arena_take(ctx, ((size_t)L.ntiles + 1) * 8);
     L.total = (uint32_t *)arena_take(ctx, 256);
     L.giant = L.total + 8;
     if (L.filtered) {
