@@ -3,10 +3,11 @@
 //
 // Reference round structure            ->  here
 //   root scatters per-rank draw counts    host restates edgesToSamplePerProcessor (cc_plan)
-//   rank r draws engine()%slice samples   cc_sample_draw_hook: sitmo stream (seed + r, 0, 0, 0),
-//     with sitmo(seed + r)                  output k = word k % 8 of block k / 8, the reference's
-//                                           k-th engine output; it picks a 32-edge chunk of the
-//                                           slice (coalesced) instead of one edge
+//   rank r draws engine()%slice samples   cc_sample_draws / cc_sample_hook: sitmo stream
+//     with sitmo(seed + r)                  (seed + r, 0, 0, 0), output k = word k % 8 of block
+//                                           k / 8, the reference's k-th engine output; it picks
+//                                           a 32-edge chunk of the slice (coalesced) instead of
+//                                           one edge
 //   root: shuffle + prefix union-find     lock-free union-find in HBM (atomicCAS hooking of
 //     to one component (Boost sets)         the larger root under the smaller, so roots are
 //                                           component minima; order-free for target 1)
@@ -145,52 +146,53 @@ __global__ void cc_init(uint32_t *par, uint32_t n) {
     for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) par[i] = i;
 }
 
-// The sampling round's draws and hooks in one kernel: CTA b (8 warps) owns sitmo block gb = g0 + b
-// of the flattened block list, i.e. 8 consecutive chunk draws of one rank. Thread 0 computes the
-// block (output k of stream (seed + r, 0, 0, 0) is word k % 8 of block k / 8, the reference
-// engine's k-th output) and leaves the 8 chunk descriptors in shared memory; warp j then hooks
-// the edges of chunk j with coalesced loads (32 consecutive edges of the rank's slice behind
-// each draw, instead of the reference's single edge per draw: one coalesced 128-byte load).
-template <bool kCheck>
-__global__ void __launch_bounds__(kThreads) cc_sample_draw_hook(uint32_t *par, const uint32_t *__restrict__ u,
-                                                               const uint32_t *__restrict__ v,
-                                                               const RankDesc *__restrict__ ranks, int nranks,
-                                                               uint64_t g0, uint64_t g1, uint32_t n, uint32_t *err) {
+// The draws of the sampling round, one thread per sitmo block (8 draws of one rank). The reference
+// draws single edges (engine() % slice, a random 8-byte gather each); here draw k of rank r
+// (32-bit output k of stream (seed + r, 0, 0, 0), word k % 8 of block k / 8) selects chunk
+// (output % chunks) of kSampleChunk consecutive edges of the rank's slice. The chunk is stored as
+// (first edge | edge count << 32) at the draw's flattened index.
+__global__ void cc_sample_draws(const RankDesc *__restrict__ ranks, int nranks, uint64_t nblocks,
+                                uint64_t *__restrict__ chunks) {
     pdl_wait();
-    __shared__ uint64_t chunk[8];
-    const uint32_t lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    for (uint64_t gb = g0 + blockIdx.x; gb < g1; gb += gridDim.x) {
-        if (threadIdx.x == 0) {
-            int lo = 0, hi = nranks - 1;  // last rank whose first block <= gb
-            while (lo < hi) {
-                const int mid = (lo + hi + 1) >> 1;
-                if (ranks[mid].block_off <= gb) lo = mid; else hi = mid - 1;
-            }
-            const RankDesc rd = ranks[lo];
-            const uint64_t blk = gb - rd.block_off;
-            const u64x4 o = sitmo_block(rd.key0, 0, 0, 0, blk, 0, 0, 0);
-            const uint64_t nchunks = (rd.slice_len + kSampleChunk - 1) / kSampleChunk;
-            const uint64_t end = rd.slice_off + rd.slice_len;
-#pragma unroll
-            for (int j = 0; j < 8; j++) {
-                const uint64_t k = blk * 8 + j;
-                uint64_t c = 0;  // count 0: no draw
-                if (k < rd.draws) {
-                    const uint64_t word = o.x[j >> 1];
-                    const uint32_t x = (j & 1) ? (uint32_t)(word >> 32) : (uint32_t)word;
-                    const uint64_t first = rd.slice_off + (x % nchunks) * kSampleChunk;
-                    c = first | (min((uint64_t)kSampleChunk, end - first) << 32);
-                }
-                chunk[j] = c;
-            }
+    for (uint64_t gb = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; gb < nblocks;
+         gb += (uint64_t)gridDim.x * blockDim.x) {
+        int lo = 0, hi = nranks - 1;  // last rank whose first block <= gb
+        while (lo < hi) {
+            int mid = (lo + hi + 1) >> 1;
+            if (ranks[mid].block_off <= gb) lo = mid; else hi = mid - 1;
         }
-        __syncthreads();
-        const uint64_t c = chunk[warp];
+        const RankDesc rd = ranks[lo];
+        const uint64_t blk = gb - rd.block_off;  // sitmo block index within the rank's stream
+        const u64x4 o = sitmo_block(rd.key0, 0, 0, 0, blk, 0, 0, 0);
+        const uint64_t nchunks = (rd.slice_len + kSampleChunk - 1) / kSampleChunk;
+        const uint64_t end = rd.slice_off + rd.slice_len;
+#pragma unroll
+        for (int j = 0; j < 8; j++) {
+            const uint64_t k = blk * 8 + j;
+            if (k >= rd.draws) break;  // rd.draws counts chunk draws
+            const uint64_t word = o.x[j >> 1];
+            const uint32_t x = (j & 1) ? (uint32_t)(word >> 32) : (uint32_t)word;
+            const uint64_t first = rd.slice_off + (x % nchunks) * kSampleChunk;
+            const uint64_t count = min((uint64_t)kSampleChunk, end - first);
+            chunks[rd.draw_off + k] = first | (count << 32);
+        }
+    }
+}
+
+// One warp per sampled chunk of the draw range [d0, d1): coalesced loads of its edges, each hooked.
+template <bool kCheck>
+__global__ void cc_sample_hook(uint32_t *par, const uint32_t *__restrict__ u, const uint32_t *__restrict__ v,
+                               const uint64_t *__restrict__ chunks, uint64_t d0, uint64_t d1, uint32_t n,
+                               uint32_t *err) {
+    pdl_wait();
+    const uint32_t lane = threadIdx.x & 31;
+    const uint64_t warps = ((uint64_t)gridDim.x * blockDim.x) >> 5;
+    for (uint64_t d = d0 + (((uint64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5); d < d1; d += warps) {
+        const uint64_t c = chunks[d];
         if (lane < (uint32_t)(c >> 32)) {
             const uint64_t e = (c & 0xFFFFFFFFull) + lane;
             edge_hook_checked<kCheck>(par, __ldg(u + e), __ldg(v + e), n, err);
         }
-        __syncthreads();
     }
 }
 
@@ -591,33 +593,44 @@ __global__ void __launch_bounds__(kThreads) cc_finalize_rank(uint32_t *par, uint
     const uint32_t tile_sum = sh[(kThreads >> 5) - 1];
     constexpr unsigned long long kInclusive = 1ull << 63, kAggregate = 1ull << 62;
     volatile unsigned long long *st = status + 1;
-    if (threadIdx.x == 0) {
+    if (w == 0) {
+        // warp 0 publishes this tile and looks back over windows of 32 predecessors: lane i
+        // reads tile j - i; the closest inclusive prefix in the window ends the walk, the
+        // aggregates before it are added, a window of aggregates only moves the walk 32 back
         uint32_t prefix = 0;
         if (tile == 0) {
-            st[0] = kInclusive | tile_sum;
+            if (l == 0) st[0] = kInclusive | tile_sum;
         } else {
-            st[tile] = kAggregate | tile_sum;
+            if (l == 0) st[tile] = kAggregate | tile_sum;
             bool gave_up = false;
-            for (int64_t j = (int64_t)tile - 1; j >= 0; j--) {
-                unsigned long long x;
-                uint32_t spins = 0;
-                while (((x = st[j]) & (kInclusive | kAggregate)) == 0) {
-                    if (++spins > kLookbackSpins) break;
-                    __nanosleep(32);
+            for (int64_t j = (int64_t)tile - 1;; j -= 32) {
+                const int64_t idx = j - l;
+                unsigned long long x = kInclusive;  // before tile 0: an inclusive prefix of 0
+                if (idx >= 0) {
+                    uint32_t spins = 0;
+                    while (((x = st[idx]) & (kInclusive | kAggregate)) == 0) {
+                        if (++spins > kLookbackSpins) break;
+                        __nanosleep(20);
+                    }
                 }
-                if ((x & (kInclusive | kAggregate)) == 0) {
+                if (__any_sync(0xffffffffu, (x & (kInclusive | kAggregate)) == 0)) {
                     gave_up = true;
                     break;
                 }
-                prefix += (uint32_t)x;
-                if (x & kInclusive) break;
+                const uint32_t incl = __ballot_sync(0xffffffffu, (x & kInclusive) != 0);
+                const int first = incl ? __ffs(incl) - 1 : 32;
+                prefix += __reduce_add_sync(0xffffffffu, l <= first ? (uint32_t)x : 0u);
+                if (incl) break;
             }
-            if (gave_up) atomicOr(err, kErrLookback);
-            __threadfence();
-            st[tile] = kInclusive | (unsigned long long)(prefix + tile_sum);
+            if (l == 0) {
+                if (gave_up) atomicOr(err, kErrLookback);
+                st[tile] = kInclusive | (unsigned long long)(prefix + tile_sum);
+            }
         }
-        s_prefix = prefix;
-        if ((uint64_t)(tile + 1) * kTile >= n) *total = prefix + tile_sum;
+        if (l == 0) {
+            s_prefix = prefix;
+            if ((uint64_t)(tile + 1) * kTile >= n) *total = prefix + tile_sum;
+        }
     }
     __syncthreads();
     if (kLabels) {
@@ -728,6 +741,7 @@ struct CCLaunch {
     const RankDesc *h_ranks = nullptr;
     uint32_t ntiles = 0, nwords = 0;
     uint64_t blocks = 0, draws = 0, drawn = 0;  // sitmo blocks, chunk draws, sampled edges
+    uint64_t *chunks = nullptr;                  // per draw: first edge | count << 32
     unsigned long long *status = nullptr;        // ticket counter + per-tile look-back state
     uint32_t *err = nullptr;                     // total + kErrWord
     bool vec = false;
@@ -751,21 +765,23 @@ int cc_enqueue(cac_ctx *ctx, const CCLaunch &L, bool capturing) {
     CAC_CUDA_TRY(launch_pdl(cc_init, grid_for(ctx, n, 8), kThreads, 0, s, L.par, n));
     if (L.draws > 0 && m > 0) {
         CAC_CUDA_TRY(cudaMemcpyAsync(L.d_ranks, L.h_ranks, sizeof(RankDesc) * L.ranks, cudaMemcpyHostToDevice, s));
-        // The draws are hooked in kSampleSubrounds slices of the sitmo blocks (8 chunk draws
-        // each, drawn inside the hooking CTA): forest building from singletons is the expensive
-        // part of CC, and flattening the trees between the early slices keeps the union walks of
-        // the next slice one or two hops long. Later slices mostly hook small trees onto the giant
-        // one, so only the first kCompressedSubrounds are followed by a compression; the last
-        // slice is followed by the fused compression + giant search + bitmap. Measured against a
-        // compression after every slice: BA n=1,024,000 205 vs 214 us per query, R-MAT scale 22
-        // 647 vs 666 us.
-        const uint32_t sub = (uint32_t)std::min<uint64_t>(kSampleSubrounds, L.blocks);
-        auto hook = L.check ? cc_sample_draw_hook<true> : cc_sample_draw_hook<false>;
+        // The draws are hooked in kSampleSubrounds slices: forest building from singletons is the
+        // expensive part of CC, and flattening the trees between the early slices keeps the union
+        // walks of the next slice one or two hops long. Later slices mostly hook small trees onto
+        // the giant one, so only the first kCompressedSubrounds are followed by a compression; the
+        // last slice is followed by the fused compression + giant search + bitmap. Measured
+        // against a compression after every slice: BA n=1,024,000 205 vs 214 us per query, R-MAT
+        // scale 22 647 vs 666 us. (Drawing inside the hooking CTAs instead of in one kernel up
+        // front measured slower: the rank search and the block cipher then sit on every slice's
+        // critical path.)
+        CAC_CUDA_TRY(launch_pdl(cc_sample_draws, grid_for(ctx, L.blocks, 8), kThreads, 0, s,
+                                static_cast<const RankDesc *>(L.d_ranks), (int)L.ranks, L.blocks, L.chunks));
+        const uint32_t sub = (uint32_t)std::min<uint64_t>(kSampleSubrounds, L.draws);
         for (uint32_t k = 0; k < sub; k++) {
-            const uint64_t g0 = L.blocks * k / sub, g1 = L.blocks * (k + 1) / sub;
-            const unsigned grid = (unsigned)std::max<uint64_t>(1, std::min<uint64_t>(g1 - g0, (uint64_t)ctx->num_sms * 8));
-            CAC_CUDA_TRY(launch_pdl(hook, grid, kThreads, 0, s, L.par, L.u, L.v,
-                                    static_cast<const RankDesc *>(L.d_ranks), (int)L.ranks, g0, g1, n, L.err));
+            const uint64_t d0 = L.draws * k / sub, d1 = L.draws * (k + 1) / sub;
+            auto hook = L.check ? cc_sample_hook<true> : cc_sample_hook<false>;
+            CAC_CUDA_TRY(launch_pdl(hook, grid_for(ctx, (d1 - d0) * 32, 8), kThreads, 0, s, L.par, L.u, L.v,
+                                    static_cast<const uint64_t *>(L.chunks), d0, d1, n, L.err));
             if (k < kCompressedSubrounds && k + 1 < sub) compress_all(ctx, L.par, n, s);
         }
         CAC_CUDA_TRY(launch_pdl(cc_compress_giant_bitmap, giant_grid(ctx, n), kGiantSample, 0, s, L.par, n, L.giant,
@@ -862,6 +878,8 @@ int cc_run(cac_ctx *ctx, uint32_t n, uint64_t m, const uint32_t *d_u, const uint
         return CAC_OK;
     }
     const CCPlan plan = cc_plan(n, m, ranks);
+    uint64_t chunk_slots = 1;
+    for (uint32_t r = 0; r < ranks; r++) chunk_slots += (plan.draws[r] + kSampleChunk - 1) / kSampleChunk;
     CCLaunch L;
     L.n = n;
     L.m = m;
@@ -874,7 +892,7 @@ int cc_run(cac_ctx *ctx, uint32_t n, uint64_t m, const uint32_t *d_u, const uint
     L.vec = ((reinterpret_cast<uintptr_t>(d_u) | reinterpret_cast<uintptr_t>(d_v)) & 15) == 0;
     L.check = check_ids;
 
-    CAC_TRY(arena_reserve(ctx, cc_scratch_bytes(n, ranks, m)));
+    CAC_TRY(arena_reserve(ctx, cc_scratch_bytes(n, ranks, m) + align_up(chunk_slots * 8)));
     arena_reset(ctx);
     L.par = (uint32_t *)arena_take(ctx, (size_t)n * 4);
     L.counts = (uint32_t *)arena_take(ctx, (size_t)L.ntiles * 4 + 4);
@@ -887,6 +905,7 @@ int cc_run(cac_ctx *ctx, uint32_t n, uint64_t m, const uint32_t *d_u, const uint
     L.region_counts = (uint32_t *)arena_take(ctx, kMaxRegions * 4);
     L.surv = (uint2 *)arena_take(ctx, (m + 4 * (uint64_t)kMaxRegions) * 8);
     L.status = (unsigned long long *)arena_take(ctx, ((size_t)L.ntiles + 1) * 8);
+    L.chunks = (uint64_t *)arena_take(ctx, chunk_slots * 8);
 
     // rank descriptors go through the ctx's pinned staging page when they fit (async copy)
     std::vector<RankDesc> hv;
