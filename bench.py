@@ -67,9 +67,10 @@ PORT_SLOWDOWN = {
                           "how": _PORT_HOW},
 }
 METRIC = "CC edges/s (parallel_cc, BA n=1,024,000 m=16)"
-# init, sample_draws, 8 x sample_hook, 3 x compress4 (after the first three slices),
-# compress_giant_bitmap, filter, hook_survivors, finalize_rank, label_all
-KERNELS_PER_QUERY = 2 + 8 + 3 + 1 + 4
+# init, sample_draws, 4 x sample_hook (slices of 1, 1, 2 and 4 eighths), 3 x compress4 (after all
+# but the last slice), compress_giant_bitmap, filter, hook_survivors, finalize_count, scan_tiles,
+# rank_roots, label_all
+KERNELS_PER_QUERY = 2 + 4 + 3 + 1 + 2 + 4
 
 
 def _max_over_ranks(x, world):

@@ -15,7 +15,7 @@
 //     and repeat while edges remain         edges whose endpoints already share a root are the
 //                                           dropped loops, the rest hook (the final round)
 //   relabel by first appearance           roots = minima, so label = exclusive scan of the
-//                                           root flags (cc_finalize_rank, cc_label_all)
+//                                           root flags (cc_finalize_count/scan/rank/label)
 //
 // Memory layout in HBM: edge endpoints as two uint32 arrays u[m], v[m] (structure of arrays,
 // 16-byte vector loads, 4 edges per load pair); parent[n] uint32 (L2-resident for n up to
@@ -61,8 +61,14 @@ constexpr int kEdgeThreads = 1024;                   // closing-pass CTA (one pe
 constexpr uint32_t kSmemBitmapWords = 48 * 1024;     // 192 KB of bitmap in shared memory (1.57M vertices)
 constexpr uint32_t kGiantSample = 1024;              // vertices sampled to find the giant component
 constexpr uint32_t kSampleChunk = 32;                // consecutive edges behind one sampling draw
-constexpr uint32_t kSampleSubrounds = 8;             // slices of the sampling round
-constexpr uint32_t kCompressedSubrounds = 3;         // slices followed by a full compression (and the last)
+// Slices of the sampling round, in eighths of its draws: a first slice above an eighth builds long
+// parent chains from the singletons (2/8 first: 451 vs 209 us per BA n=1,024,000 query), later
+// ones mostly hook small trees onto the giant one and can be larger. Every slice but the last is
+// followed by a full compression; the last by the fused compression + giant search + bitmap.
+// Measured per BA n=1,024,000 query against eight even slices (compressions after the first three
+// and the last): 1,1,2,4 202.0 vs 208.8 us; 1,1,1,5 203.3; 1,1,1,1,4 206.6; 1,1,1,1,1,3 204.9.
+// R-MAT scale 22: 1,1,1,5 647.5 vs 666.4 us.
+constexpr uint32_t kSliceEighths[] = {1, 1, 2, 4};
 constexpr uint32_t kMaxRegions = 1024;               // filter CTAs (regions of the survivor buffer)
 // survivor-hook CTAs per SM: about one survivor per thread on BA n=1,024,000 (0.6 M survivors);
 // 8 against 4: 20 vs 22.5 us there, 47 vs 63.5 us on R-MAT scale 22; 16 no better
@@ -70,8 +76,6 @@ constexpr unsigned kSurvivorBlocksPerSm = 8;
 constexpr uint32_t kStreamPieces = 8;                // sample pieces (and gaps) of a host edge list
 constexpr uint32_t kErrWord = 9;                     // a query's error word (after its count and giant root)
 constexpr uint32_t kErrBadId = 1;                    // an edge endpoint was >= n (the edge was skipped)
-constexpr uint32_t kErrLookback = 2;                 // a tile's look-back gave up waiting (labels invalid)
-constexpr uint32_t kLookbackSpins = 1u << 24;        // bound on one look-back wait (never reached in practice)
 
 struct RankDesc {
     uint64_t slice_off;
@@ -539,108 +543,6 @@ __global__ void __launch_bounds__(kThreads) cc_rank_roots(const uint32_t *par, u
     }
 }
 
-// Final compression, root count and root ranks in one pass (replaces cc_finalize_count +
-// cc_scan_tiles + cc_rank_roots). A CTA takes a ticket (tiles are numbered in the order CTAs
-// start, so every tile before it belongs to a CTA already running), compresses its 1024 vertices,
-// counts their roots and publishes the count in its status word; it then looks back over the
-// status words of the tiles before it (decoupled look-back: an inclusive prefix ends the walk,
-// an aggregate is added and the walk continues) and publishes its own inclusive prefix. Roots are
-// then ranked as in cc_rank_roots. The last tile writes the component count. status[] holds
-// ntiles + 1 words and starts at zero: word 0 is the ticket counter, word 1 + t tile t's state
-// (bit 63: inclusive prefix, bit 62: aggregate, low 32 bits: the value). A wait that exceeds its
-// bound sets kErrLookback in the query's error word instead of spinning on.
-template <bool kLabels>
-__global__ void __launch_bounds__(kThreads) cc_finalize_rank(uint32_t *par, uint32_t n, unsigned long long *status,
-                                                             uint32_t *labels, uint32_t *total, uint32_t *err) {
-    pdl_wait();
-    __shared__ uint32_t sh[32];
-    __shared__ uint32_t s_tile, s_prefix;
-    if (threadIdx.x == 0) s_tile = atomicAdd(reinterpret_cast<unsigned int *>(status), 1u);
-    __syncthreads();
-    const uint32_t tile = s_tile;
-    const uint64_t base = (uint64_t)tile * kTile + (uint64_t)threadIdx.x * kTileItems;
-    uint32_t flags = 0, c = 0;
-#pragma unroll
-    for (int k = 0; k < kTileItems; k++) {
-        const uint64_t i = base + k;
-        if (i < n) {
-            const uint32_t p = par[i];
-            const uint32_t r = p == (uint32_t)i ? p : find_root_ro(par, p);
-            if (r != p) par[i] = r;
-            const uint32_t f = r == (uint32_t)i;
-            flags |= f << k;
-            c += f;
-        }
-    }
-    // exclusive scan of c over the block (thread order == vertex order inside the tile)
-    uint32_t sc = c;
-    const int l = threadIdx.x & 31, w = threadIdx.x >> 5;
-    for (int o = 1; o < 32; o <<= 1) {
-        const uint32_t y = __shfl_up_sync(0xffffffffu, sc, o);
-        if (l >= o) sc += y;
-    }
-    if (l == 31) sh[w] = sc;
-    __syncthreads();
-    if (w == 0) {
-        uint32_t t = l < (kThreads >> 5) ? sh[l] : 0;
-        for (int o = 1; o < 32; o <<= 1) {
-            const uint32_t y = __shfl_up_sync(0xffffffffu, t, o);
-            if (l >= o) t += y;
-        }
-        sh[l] = t;
-    }
-    __syncthreads();
-    const uint32_t tile_sum = sh[(kThreads >> 5) - 1];
-    constexpr unsigned long long kInclusive = 1ull << 63, kAggregate = 1ull << 62;
-    volatile unsigned long long *st = status + 1;
-    if (w == 0) {
-        // warp 0 publishes this tile and looks back over windows of 32 predecessors: lane i
-        // reads tile j - i; the closest inclusive prefix in the window ends the walk, the
-        // aggregates before it are added, a window of aggregates only moves the walk 32 back
-        uint32_t prefix = 0;
-        if (tile == 0) {
-            if (l == 0) st[0] = kInclusive | tile_sum;
-        } else {
-            if (l == 0) st[tile] = kAggregate | tile_sum;
-            bool gave_up = false;
-            for (int64_t j = (int64_t)tile - 1;; j -= 32) {
-                const int64_t idx = j - l;
-                unsigned long long x = kInclusive;  // before tile 0: an inclusive prefix of 0
-                if (idx >= 0) {
-                    uint32_t spins = 0;
-                    while (((x = st[idx]) & (kInclusive | kAggregate)) == 0) {
-                        if (++spins > kLookbackSpins) break;
-                        __nanosleep(20);
-                    }
-                }
-                if (__any_sync(0xffffffffu, (x & (kInclusive | kAggregate)) == 0)) {
-                    gave_up = true;
-                    break;
-                }
-                const uint32_t incl = __ballot_sync(0xffffffffu, (x & kInclusive) != 0);
-                const int first = incl ? __ffs(incl) - 1 : 32;
-                prefix += __reduce_add_sync(0xffffffffu, l <= first ? (uint32_t)x : 0u);
-                if (incl) break;
-            }
-            if (l == 0) {
-                if (gave_up) atomicOr(err, kErrLookback);
-                st[tile] = kInclusive | (unsigned long long)(prefix + tile_sum);
-            }
-        }
-        if (l == 0) {
-            s_prefix = prefix;
-            if ((uint64_t)(tile + 1) * kTile >= n) *total = prefix + tile_sum;
-        }
-    }
-    __syncthreads();
-    if (kLabels) {
-        uint32_t r = s_prefix + (w ? sh[w - 1] : 0) + sc - c;
-#pragma unroll
-        for (int k = 0; k < kTileItems; k++)
-            if ((flags >> k) & 1u) labels[base + k] = r++;
-    }
-}
-
 __global__ void cc_label_all(const uint32_t *par, uint32_t n, uint32_t *labels) {
     pdl_wait();
     for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
@@ -722,7 +624,7 @@ size_t cc_scratch_bytes(uint32_t n, uint32_t ranks, uint64_t m) {
     const size_t nwords = ((size_t)n + 31) / 32;
     return align_up((size_t)n * 4) + 2 * align_up(ntiles * 4 + 4) + align_up(256) +
            align_up(sizeof(RankDesc) * (size_t)ranks) + align_up(nwords * 4 + 4) + align_up(kMaxRegions * 4) +
-           align_up((m + 4 * (uint64_t)kMaxRegions) * 8) + align_up((ntiles + 1) * 8);
+           align_up((m + 4 * (uint64_t)kMaxRegions) * 8);
 }
 
 namespace {
@@ -742,7 +644,6 @@ struct CCLaunch {
     uint32_t ntiles = 0, nwords = 0;
     uint64_t blocks = 0, draws = 0, drawn = 0;  // sitmo blocks, chunk draws, sampled edges
     uint64_t *chunks = nullptr;                  // per draw: first edge | count << 32
-    unsigned long long *status = nullptr;        // ticket counter + per-tile look-back state
     uint32_t *err = nullptr;                     // total + kErrWord
     bool vec = false;
     bool check = false;                          // endpoints not validated: every kernel checks them
@@ -761,28 +662,28 @@ int cc_enqueue(cac_ctx *ctx, const CCLaunch &L, bool capturing) {
     const uint64_t m = L.m;
     CAC_TRY(record(ctx, 0, capturing));
     CAC_CUDA_TRY(cudaMemsetAsync(L.err, 0, 4, s));
-    CAC_CUDA_TRY(cudaMemsetAsync(L.status, 0, ((size_t)L.ntiles + 1) * 8, s));
     CAC_CUDA_TRY(launch_pdl(cc_init, grid_for(ctx, n, 8), kThreads, 0, s, L.par, n));
     if (L.draws > 0 && m > 0) {
         CAC_CUDA_TRY(cudaMemcpyAsync(L.d_ranks, L.h_ranks, sizeof(RankDesc) * L.ranks, cudaMemcpyHostToDevice, s));
-        // The draws are hooked in kSampleSubrounds slices: forest building from singletons is the
-        // expensive part of CC, and flattening the trees between the early slices keeps the union
-        // walks of the next slice one or two hops long. Later slices mostly hook small trees onto
-        // the giant one, so only the first kCompressedSubrounds are followed by a compression; the
-        // last slice is followed by the fused compression + giant search + bitmap. Measured
-        // against a compression after every slice: BA n=1,024,000 205 vs 214 us per query, R-MAT
-        // scale 22 647 vs 666 us. (Drawing inside the hooking CTAs instead of in one kernel up
-        // front measured slower: the rank search and the block cipher then sit on every slice's
-        // critical path.)
+        // The draws are hooked in the slices of kSliceEighths: forest building from singletons is
+        // the expensive part of CC, and flattening the trees between slices keeps the union walks
+        // of the next slice one or two hops long. (Drawing inside the hooking CTAs instead of in
+        // one kernel up front measured slower: the rank search and the block cipher then sit on
+        // every slice's critical path.)
         CAC_CUDA_TRY(launch_pdl(cc_sample_draws, grid_for(ctx, L.blocks, 8), kThreads, 0, s,
                                 static_cast<const RankDesc *>(L.d_ranks), (int)L.ranks, L.blocks, L.chunks));
-        const uint32_t sub = (uint32_t)std::min<uint64_t>(kSampleSubrounds, L.draws);
+        constexpr uint32_t sub = sizeof(kSliceEighths) / sizeof(kSliceEighths[0]);
+        uint32_t eighths = 0;
         for (uint32_t k = 0; k < sub; k++) {
-            const uint64_t d0 = L.draws * k / sub, d1 = L.draws * (k + 1) / sub;
-            auto hook = L.check ? cc_sample_hook<true> : cc_sample_hook<false>;
-            CAC_CUDA_TRY(launch_pdl(hook, grid_for(ctx, (d1 - d0) * 32, 8), kThreads, 0, s, L.par, L.u, L.v,
-                                    static_cast<const uint64_t *>(L.chunks), d0, d1, n, L.err));
-            if (k < kCompressedSubrounds && k + 1 < sub) compress_all(ctx, L.par, n, s);
+            const uint64_t d0 = L.draws * eighths / 8;
+            eighths += kSliceEighths[k];
+            const uint64_t d1 = L.draws * eighths / 8;
+            if (d1 > d0) {
+                auto hook = L.check ? cc_sample_hook<true> : cc_sample_hook<false>;
+                CAC_CUDA_TRY(launch_pdl(hook, grid_for(ctx, (d1 - d0) * 32, 8), kThreads, 0, s, L.par, L.u, L.v,
+                                        static_cast<const uint64_t *>(L.chunks), d0, d1, n, L.err));
+            }
+            if (k + 1 < sub) compress_all(ctx, L.par, n, s);
         }
         CAC_CUDA_TRY(launch_pdl(cc_compress_giant_bitmap, giant_grid(ctx, n), kGiantSample, 0, s, L.par, n, L.giant,
                                 L.bits));
@@ -824,14 +725,16 @@ int cc_enqueue(cac_ctx *ctx, const CCLaunch &L, bool capturing) {
         CAC_TRY(record(ctx, 4, capturing));
     }
     CAC_TRY(record(ctx, 2, capturing));
+    // (A single-pass count and rank by decoupled look-back measured slower: BA n=1,024,000 20.4 vs
+    // 18.5 us, R-MAT scale 22 48.6 vs 34.0 us for the labelling.)
+    CAC_CUDA_TRY(launch_pdl(cc_finalize_count, L.ntiles, kThreads, 0, s, L.par, n, L.counts));
+    CAC_CUDA_TRY(launch_pdl(cc_scan_tiles, 1, 1024, 0, s, static_cast<const uint32_t *>(L.counts), L.offsets, L.ntiles,
+                            L.total));
     if (L.labels) {
-        CAC_CUDA_TRY(launch_pdl(cc_finalize_rank<true>, L.ntiles, kThreads, 0, s, L.par, n, L.status, L.labels,
-                                L.total, L.err));
+        CAC_CUDA_TRY(launch_pdl(cc_rank_roots, L.ntiles, kThreads, 0, s, static_cast<const uint32_t *>(L.par), n,
+                                static_cast<const uint32_t *>(L.offsets), L.labels));
         CAC_CUDA_TRY(launch_pdl(cc_label_all, grid_for(ctx, n, 8), kThreads, 0, s,
                                 static_cast<const uint32_t *>(L.par), n, L.labels));
-    } else {
-        CAC_CUDA_TRY(launch_pdl(cc_finalize_rank<false>, L.ntiles, kThreads, 0, s, L.par, n, L.status, L.labels,
-                                L.total, L.err));
     }
     CAC_CUDA_TRY(cudaGetLastError());
     CAC_CUDA_TRY(cudaMemcpyAsync(ctx->pinned_u32, L.total, (kErrWord + 1) * 4, cudaMemcpyDeviceToHost, s));
@@ -841,10 +744,6 @@ int cc_enqueue(cac_ctx *ctx, const CCLaunch &L, bool capturing) {
 
 // The query's error word, copied back with its count.
 int check_ids_word(cac_ctx *ctx, uint32_t n) {
-    if (ctx->pinned_u32[kErrWord] & kErrLookback) {
-        set_error("connected components: a labelling tile's look-back wait exceeded its bound");
-        return CAC_ERR_TIMEOUT;
-    }
     if (ctx->pinned_u32[kErrWord] & kErrBadId) {
         set_error("connected components: an edge endpoint is >= n = " + std::to_string(n) +
                   " (such edges were skipped; the labels are not valid)");
@@ -904,7 +803,6 @@ int cc_run(cac_ctx *ctx, uint32_t n, uint64_t m, const uint32_t *d_u, const uint
     L.bits = (uint32_t *)arena_take(ctx, (size_t)L.nwords * 4 + 4);
     L.region_counts = (uint32_t *)arena_take(ctx, kMaxRegions * 4);
     L.surv = (uint2 *)arena_take(ctx, (m + 4 * (uint64_t)kMaxRegions) * 8);
-    L.status = (unsigned long long *)arena_take(ctx, ((size_t)L.ntiles + 1) * 8);
     L.chunks = (uint64_t *)arena_take(ctx, chunk_slots * 8);
 
     // rank descriptors go through the ctx's pinned staging page when they fit (async copy)
@@ -1022,9 +920,8 @@ struct StreamLaunch {
     const uint32_t *h_u = nullptr, *h_v = nullptr;  // host edge arrays (copy-engine source)
     const uint32_t *z_u = nullptr, *z_v = nullptr;  // their device views when pinned and aligned, else null
     uint32_t *d_u = nullptr, *d_v = nullptr, *d_labels = nullptr, *h_labels = nullptr;
-    uint32_t *par = nullptr, *total = nullptr, *giant = nullptr;
+    uint32_t *par = nullptr, *counts = nullptr, *offsets = nullptr, *total = nullptr, *giant = nullptr;
     uint32_t *bits = nullptr, *region_counts = nullptr;
-    unsigned long long *status = nullptr;  // ticket counter + per-tile look-back state
     uint2 *surv = nullptr;
     uint32_t ntiles = 0, nwords = 0;
     bool vec = false, filtered = false;
@@ -1053,7 +950,6 @@ int stream_enqueue(cac_ctx *ctx, const StreamLaunch &L, bool capturing) {
     CAC_TRY(record(ctx, 0, capturing));
     cc_init<<<grid_for(ctx, n, 8), kThreads, 0, s>>>(L.par, n);
     CAC_CUDA_TRY(cudaMemsetAsync(L.total + kErrWord, 0, 4, s));
-    CAC_CUDA_TRY(cudaMemsetAsync(L.status, 0, ((size_t)L.ntiles + 1) * 8, s));
     // the copies start after everything already queued on the ctx stream (the staging buffers
     // may still be read by the previous query)
     cudaEvent_t *ev = ctx->chunk_ev;
@@ -1117,13 +1013,11 @@ int stream_enqueue(cac_ctx *ctx, const StreamLaunch &L, bool capturing) {
     }
     if (!L.filtered) CAC_TRY(record(ctx, 1, capturing));
     CAC_TRY(record(ctx, 2, capturing));
+    cc_finalize_count<<<L.ntiles, kThreads, 0, s>>>(L.par, n, L.counts);
+    cc_scan_tiles<<<1, 1024, 0, s>>>(L.counts, L.offsets, L.ntiles, L.total);
     if (L.d_labels) {
-        cc_finalize_rank<true><<<L.ntiles, kThreads, 0, s>>>(L.par, n, L.status, L.d_labels, L.total,
-                                                             L.total + kErrWord);
+        cc_rank_roots<<<L.ntiles, kThreads, 0, s>>>(L.par, n, L.offsets, L.d_labels);
         cc_label_all<<<grid_for(ctx, n, 8), kThreads, 0, s>>>(L.par, n, L.d_labels);
-    } else {
-        cc_finalize_rank<false><<<L.ntiles, kThreads, 0, s>>>(L.par, n, L.status, L.d_labels, L.total,
-                                                              L.total + kErrWord);
     }
     CAC_CUDA_TRY(cudaGetLastError());
     CAC_CUDA_TRY(cudaMemcpyAsync(ctx->pinned_u32, L.total, (kErrWord + 1) * 4, cudaMemcpyDeviceToHost, s));
@@ -1171,13 +1065,14 @@ int cc_run_streamed(cac_ctx *ctx, uint32_t n, uint64_t m, const uint32_t *h_u, c
                                : 0;
     L.filtered = L.vec && seg > 0;
     const uint64_t max_gap = L.filtered ? m - (kStreamPieces - 1) * seg - piece : 0;
-    CAC_TRY(arena_reserve(ctx, align_up((size_t)n * 4) + align_up(((size_t)L.ntiles + 1) * 8) + align_up(256) +
+    CAC_TRY(arena_reserve(ctx, align_up((size_t)n * 4) + 2 * align_up((size_t)L.ntiles * 4 + 4) + align_up(256) +
                                    (L.filtered ? align_up((size_t)L.nwords * 4 + 4) + align_up(kMaxRegions * 4) +
                                                      align_up((max_gap + 4 * (uint64_t)kMaxRegions) * 8)
                                                : 0)));
     arena_reset(ctx);
     L.par = (uint32_t *)arena_take(ctx, (size_t)n * 4);
-    L.status = (unsigned long long *)arena_take(ctx, ((size_t)L.ntiles + 1) * 8);
+    L.counts = (uint32_t *)arena_take(ctx, (size_t)L.ntiles * 4 + 4);
+    L.offsets = (uint32_t *)arena_take(ctx, (size_t)L.ntiles * 4 + 4);
     L.total = (uint32_t *)arena_take(ctx, 256);
     L.giant = L.total + 8;
     if (L.filtered) {
