@@ -92,6 +92,7 @@ _LIB = None
 EXPORTS = [
     ("cac_ctx_create", ctypes.c_int, [ctypes.POINTER(_Config), ctypes.POINTER(_vp)]),
     ("cac_ctx_destroy", ctypes.c_int, [_vp]),
+    ("cac_ctx_set_dense_limit", ctypes.c_int, [_vp, ctypes.c_uint32]),
     ("cac_error_string", ctypes.c_char_p, [ctypes.c_int]),
     ("cac_last_error", ctypes.c_char_p, []),
     ("cac_ctx_device_bytes", ctypes.c_uint64, [_vp]),
@@ -115,6 +116,7 @@ EXPORTS = [
     ("cac_mincut_batch", ctypes.c_int, [_vp, _vp, ctypes.c_uint32, _vp]),
     ("cac_karger_stein", ctypes.c_int, [_vp, _vp, ctypes.c_double, ctypes.c_uint32, ctypes.POINTER(MincutResult)]),
     ("cac_mincut_trials", ctypes.c_int, [_vp, _vp, ctypes.c_uint32, ctypes.c_uint32, ctypes.c_uint32, _vp]),
+    ("cac_karger_stein_trials", ctypes.c_int, [_vp, _vp, ctypes.c_uint32, ctypes.c_uint32, _vp]),
     ("cac_ks_dense", ctypes.c_int, [_vp, ctypes.c_uint32, _vp, ctypes.c_uint32, ctypes.c_uint32, ctypes.c_uint32,
                                     _u64p]),
     ("cac_exact_cut_small", ctypes.c_int, [_vp, ctypes.c_uint32, _vp, _u64p]),
@@ -174,6 +176,10 @@ class Context:
         _check(lib().cac_ctx_create(ctypes.byref(cfg), ctypes.byref(h)), "cac_ctx_create")
         self.h = h
         self._graphs = weakref.WeakSet()
+
+    def set_dense_limit(self, max_dense_vertices):
+        """Karger-Stein nodes above this many vertices (or sparse ones above 128) stay edge lists."""
+        _check(lib().cac_ctx_set_dense_limit(self.h, max_dense_vertices), "cac_ctx_set_dense_limit")
 
     def close(self):
         if self.h:
@@ -345,6 +351,13 @@ class Graph:
         _check(lib().cac_karger_stein(self.ctx.h, self.h, success_probability, seed, ctypes.byref(res)),
                "cac_karger_stein")
         return res
+
+    def karger_stein_trials(self, seed, trials):
+        """Every trial's value of plain Karger-Stein (trials 0 .. trials - 1)."""
+        out = np.zeros(max(trials, 1), dtype=np.uint64)
+        _check(lib().cac_karger_stein_trials(self.ctx.h, self.h, seed, trials, ctypes.c_void_p(out.ctypes.data)),
+               "cac_karger_stein_trials")
+        return out[:trials]
 
     def trials(self, seed, virtual_ranks, trials_per_rank):
         out = np.zeros(virtual_ranks * trials_per_rank, dtype=np.uint64)

@@ -92,6 +92,7 @@ struct cac_ctx {
     uint8_t quotient_choice[32] = {};  // autotuned quotient kernel per (N bucket, width); 0: untuned
     cudaStream_t copy_stream = nullptr;  // host-to-device chunks of cac_cc_edges (created on first use)
     cudaEvent_t chunk_ev[40] = {};       // start + one per piece and gap copy in flight
+    uint32_t dense_limit = 16384;        // Karger-Stein nodes above this many vertices stay edge lists
 };
 
 struct cac_graph {
@@ -220,6 +221,32 @@ class KsEngine {
     void *d_src_, *d_task_, *d_leaf_, *d_rowoff_, *d_kout_, *d_prep_, *d_tscratch_, *d_qoff_, *d_gto_, *d_err_, *d_psrc_;
 };
 
+// A Karger-Stein node kept as an edge list (sparse_ks.cu): a root above the dense limit, or a
+// child of such a node that is still above it or has fewer than N^2 / 32 edges.
+struct SparseNode {
+    uint64_t *cut;            // the trial's cut (device)
+    uint32_t k0, idx;         // stream key words 0, 1
+    uint64_t h;               // heap index
+    uint32_t N;
+    uint64_t m;
+    const uint32_t *a, *b;    // edge ends (device)
+    const void *w;            // weights: u64 when w64, else u32
+    bool w64;
+    bool is_root;             // roots also deliver their minimum weighted degree
+    uint32_t small;           // the query's total weight is below 2^32 (u32 matrix entries)
+    uint32_t query;
+    MatBuf *buf;              // owner of a, b, w (null: the input graph)
+};
+// Dense or sparse: the rule shared with the oracle (above the limit, or above 128 vertices with
+// fewer than N^2 / 32 edges: an edge list).
+inline bool ks_is_dense(const cac_ctx *ctx, uint32_t N, uint64_t m) {
+    return N <= ctx->dense_limit && (N <= 128 || 32 * m >= (uint64_t)N * N);
+}
+// Runs every sparse level of the given nodes (each holding one reference on its buffer): children
+// contracted by the Stage 1 rounds, relabelled, sorted and merged on the device; children that
+// are dense join `eng` as matrices, the others are contracted in turn.
+int sparse_phase(cac_ctx *ctx, KsEngine &eng, std::vector<SparseNode> nodes);
+
 struct MincutQuery {
     const cac_graph *g;
     uint32_t seed, ranks, per_rank;
@@ -236,6 +263,30 @@ int mincut_admit_queries(cac_ctx *ctx, KsEngine &eng, const std::vector<MincutQu
 // Stage 1 of B trials (keys k0[b], idx[b]) of a graph with more than 16384 vertices in global
 // memory (shrink_big.cu): labels to d_lab[b * n ..], vertices left to d_kout[b].
 uint64_t shrink_big_scratch(uint32_t n, uint64_t m, uint32_t B);
+// One contraction task of shrink_tasks: a graph (u32 or u64 weights), its target, the stream key
+// (k0, idx, tag, 0) of its draws, where its labels and its vertex count go.
+struct ShrinkTask {
+    const uint32_t *U, *V;
+    const void *W;
+    bool w64;
+    uint64_t m;
+    uint32_t n, target;
+    uint32_t k0, idx;
+    uint64_t tag;
+    uint32_t *lab;    // n (device)
+    uint32_t *k_out;  // 1 (device)
+};
+uint64_t shrink_task_scratch(uint32_t n, uint64_t m);
+uint64_t shrink_tasks_scratch(const std::vector<ShrinkTask> &tasks);
+int shrink_tasks(cac_ctx *ctx, const std::vector<ShrinkTask> &tasks, void *scratch);
+// Device sort and merge of a relabelled edge list (sort.cu): the pairs of the non-loop edges
+// (lab[a], lab[b]) over k vertices, sorted by (smaller, larger end), equal pairs merged with u64
+// weight sums; *d_count (device) gets the number of pairs.
+uint64_t merge_edges_scratch(uint64_t m);
+template <typename WT>
+int merge_edges(cac_ctx *ctx, const uint32_t *a, const uint32_t *b, const WT *w, uint64_t m, const uint32_t *lab,
+                uint32_t k, uint32_t *oa, uint32_t *ob, uint64_t *ow, uint32_t *d_count, void *scratch);
+int scan_u32(cac_ctx *ctx, uint32_t *x, uint64_t n, uint32_t *sums, uint32_t *total);
 int shrink_big(cac_ctx *ctx, const cac_graph *g, uint32_t target, uint32_t B, const uint32_t *k0, const uint32_t *idx,
                uint32_t *d_lab, uint32_t *d_kout, void *scratch);
 // Quotient kernel choices of the autotuner (cac_ctx::quotient_choice), bucketed by

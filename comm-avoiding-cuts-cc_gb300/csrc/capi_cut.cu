@@ -106,11 +106,6 @@ int cac_karger_stein(cac_ctx *ctx, const cac_graph *g, double p, uint32_t seed, 
         set_error("cac_karger_stein: a cut needs at least two vertices");
         return CAC_ERR_INVALID;
     }
-    if (g->n > kMaxDenseVertices) {
-        // every trial starts from the dense n x n matrix; cac_mincut pre-contracts larger graphs
-        set_error("cac_karger_stein: plain Karger-Stein works on the dense n x n matrix, at most 16384 vertices");
-        return CAC_ERR_UNSUPPORTED;
-    }
     CAC_CUDA_TRY(cudaSetDevice(ctx->device));
     *res = cac_mincut_result{};
     const uint32_t trials = ks_number_of_trials(g->n, p);
@@ -133,6 +128,33 @@ int cac_karger_stein(cac_ctx *ctx, const cac_graph *g, double p, uint32_t seed, 
         }
     }
     res->device_ms = ms;
+    stream_free(ctx, d, (uint64_t)trials * 8);
+    return st;
+}
+
+int cac_karger_stein_trials(cac_ctx *ctx, const cac_graph *g, uint32_t seed, uint32_t trials, uint64_t *cuts_host) {
+    if (!ctx || !g || !cuts_host) {
+        set_error("cac_karger_stein_trials: invalid argument");
+        return CAC_ERR_INVALID;
+    }
+    if (g->n < 2) {
+        set_error("cac_karger_stein_trials: a cut needs at least two vertices");
+        return CAC_ERR_INVALID;
+    }
+    if (trials == 0) return CAC_OK;
+    CAC_CUDA_TRY(cudaSetDevice(ctx->device));
+    void *d = nullptr;
+    CAC_TRY(stream_alloc(ctx, &d, (uint64_t)trials * 8));
+    std::vector<MincutQuery> q{MincutQuery{g, seed, 1, trials, static_cast<uint64_t *>(d), g->n}};
+    float ms = 0;
+    int st = mincut_run_queries(ctx, q, &ms);
+    if (st == CAC_OK) {
+        cudaError_t e = cudaMemcpy(cuts_host, d, (uint64_t)trials * 8, cudaMemcpyDeviceToHost);
+        if (e != cudaSuccess) {
+            set_error(cudaGetErrorString(e));
+            st = CAC_ERR_CUDA;
+        }
+    }
     stream_free(ctx, d, (uint64_t)trials * 8);
     return st;
 }

@@ -963,7 +963,8 @@ struct DevBuf {
 // one-shot probes; one engine runs per ctx at a time.
 enum ScratchSlot : int {
     kSlotSrc, kSlotTask, kSlotLeaf, kSlotRowoff, kSlotKout, kSlotPrep, kSlotTscratch, kSlotQoff, kSlotGto, kSlotErr,
-    kSlotPsrc, kSlotPre, kSlotLab, kSlotK, kSlotSd, kSlotDd, kSlotProbe0, kSlotProbe1, kSlotProbe2, kSlotCount
+    kSlotPsrc, kSlotPre, kSlotLab, kSlotK, kSlotSd, kSlotDd, kSlotSparse, kSlotSparseCount, kSlotProbe0, kSlotProbe1,
+    kSlotProbe2, kSlotCount
 };
 
 struct CtxScratch {
@@ -1401,6 +1402,40 @@ struct QueryPlan {
 int admit_stage1(cac_ctx *ctx, KsEngine &eng, const std::vector<const QueryPlan *> &qs);
 int admit_big(cac_ctx *ctx, KsEngine &eng, const QueryPlan &q);
 
+// The sparse root of one square_root trial contracted to k vertices above the dense limit: the
+// graph's edges relabelled by the trial's Stage 1 labels, sorted and merged on the device (the
+// reference's WeightedIteratedSparseSampling::reduce, .cpp:26-234). The list's buffer carries
+// the node's reference.
+int sparse_root(cac_ctx *ctx, KsEngine &eng, const QueryPlan &q, uint64_t *cut, uint32_t k0, uint32_t idx,
+                const uint32_t *lab, uint32_t k, SparseNode *out) {
+    const cac_graph *g = q.g;
+    const uint64_t cap = std::max<uint64_t>(g->m, 1);
+    MatBuf *list = nullptr;
+    CAC_TRY(eng.alloc(align_up(cap * 4) * 2 + align_up(cap * 8), &list));
+    list->refs++;
+    char *p = static_cast<char *>(list->p);
+    uint32_t *oa = reinterpret_cast<uint32_t *>(p), *ob = reinterpret_cast<uint32_t *>(p + align_up(cap * 4));
+    uint64_t *ow = reinterpret_cast<uint64_t *>(p + 2 * align_up(cap * 4));
+    DevBuf &scr = scratch(ctx, kSlotSparse), &cnt = scratch(ctx, kSlotSparseCount);
+    int st = scr.ensure(merge_edges_scratch(cap));
+    if (st == CAC_OK) st = cnt.ensure(4);
+    if (st == CAC_OK)
+        st = merge_edges<uint32_t>(ctx, g->u, g->v, g->w, g->m, lab, k, oa, ob, ow, cnt.as<uint32_t>(), scr.p);
+    uint32_t mm = 0;
+    if (st == CAC_OK && (cudaMemcpyAsync(&mm, cnt.p, 4, cudaMemcpyDeviceToHost, ctx->stream) != cudaSuccess ||
+                         cudaStreamSynchronize(ctx->stream) != cudaSuccess)) {
+        set_error("square_root: reading the sparse root's edge count failed");
+        st = CAC_ERR_CUDA;
+    }
+    if (st != CAC_OK) {
+        eng.release(list);
+        return st;
+    }
+    *out = SparseNode{cut, k0, idx, 1, k, k >= 2 ? mm : 0, oa, ob, ow, true, true,
+                      g->total_weight < (1ull << 32) ? 1u : 0u, q.query, list};
+    return CAC_OK;
+}
+
 int admit(cac_ctx *ctx, KsEngine &eng, const QueryPlan &q) {
     cudaStream_t s = ctx->stream;
     const cac_graph *g = q.g;
@@ -1408,6 +1443,16 @@ int admit(cac_ctx *ctx, KsEngine &eng, const QueryPlan &q) {
     const uint64_t m = g->m;
     const uint32_t small = g->total_weight < (1ull << 32) ? 1u : 0u;
     if (q.trials == 0) return CAC_OK;
+    if (q.t >= n && !ks_is_dense(ctx, n, m)) {
+        // no pre-contraction and a sparse graph: every trial starts from the input edge list
+        std::vector<SparseNode> roots;
+        for (uint64_t i = 0; i < q.trials; i++) {
+            const uint32_t r = (uint32_t)(i / q.per_rank), idx = (uint32_t)(i % q.per_rank);
+            roots.push_back(SparseNode{q.cuts + i, q.seed + r, idx, 1, n, m, g->u, g->v, g->w, false, true, small,
+                                       q.query, nullptr});
+        }
+        return sparse_phase(ctx, eng, std::move(roots));
+    }
     if (q.t >= n) {
         // no pre-contraction: every trial starts from the same dense matrix, built once
         MatBuf *root = nullptr;
@@ -1502,6 +1547,16 @@ int admit_stage1(cac_ctx *ctx, KsEngine &eng, const std::vector<const QueryPlan 
         std::vector<uint32_t> kdim(B);
         CAC_CUDA_TRY(cudaMemcpyAsync(kdim.data(), d_k.p, (size_t)B * 4, cudaMemcpyDeviceToHost, s));
         CAC_CUDA_TRY(cudaStreamSynchronize(s));
+        // trials contracted to more than the dense limit: sparse roots (sorted, merged edge lists)
+        std::vector<SparseNode> sparse;
+        for (uint32_t b = 0; b < B; b++) {
+            const QueryPlan &q = *items[c0 + b].q;
+            if (q.t <= ctx->dense_limit) continue;
+            SparseNode nd;
+            CAC_TRY(sparse_root(ctx, eng, q, q.cuts + items[c0 + b].i, sd[b].k0, sd[b].idx, sd[b].lab, kdim[b], &nd));
+            sparse.push_back(nd);
+            kdim[b] = 0;  // no dense matrix
+        }
         uint64_t bytes = 0;
         for (uint32_t b = 0; b < B; b++) {
             const uint64_t esize = items[c0 + b].q->g->total_weight < (1ull << 32) ? 4 : 8;
@@ -1530,6 +1585,7 @@ int admit_stage1(cac_ctx *ctx, KsEngine &eng, const std::vector<const QueryPlan 
         for (uint32_t b = 0; b < B; b++) {
             const QueryPlan &q = *items[c0 + b].q;
             const uint64_t i = items[c0 + b].i;
+            if (q.t > ctx->dense_limit) continue;  // a sparse root
             if (kdim[b] < 2) {
                 // a single vertex left, or only isolated vertices: no cut edge
                 fill_u64<<<1, 32, 0, s>>>(q.cuts + i, 1, 0);
@@ -1539,6 +1595,7 @@ int admit_stage1(cac_ctx *ctx, KsEngine &eng, const std::vector<const QueryPlan 
         }
         eng.release(roots);
         CAC_CUDA_TRY(cudaStreamSynchronize(s));  // the scratch is reused by the next chunk
+        if (!sparse.empty()) CAC_TRY(sparse_phase(ctx, eng, std::move(sparse)));
         c0 = c1;
     }
     return CAC_OK;
@@ -1571,10 +1628,21 @@ int admit_big(cac_ctx *ctx, KsEngine &eng, const QueryPlan &q) {
         std::vector<uint32_t> kdim(B);
         CAC_CUDA_TRY(cudaMemcpyAsync(kdim.data(), d_k.p, (size_t)B * 4, cudaMemcpyDeviceToHost, s));
         CAC_CUDA_TRY(cudaStreamSynchronize(s));
-        // more than 16384 vertices left only when Stage 1 stopped with no edge between them
-        // (a disconnected graph): every vertex is isolated and the trial's cut is exactly 0
-        for (uint32_t b = 0; b < B; b++)
-            if (kdim[b] > kMaxSmemVertices) kdim[b] = 0;
+        // trials contracted above the dense limit become sparse roots; otherwise more than 16384
+        // vertices are left only when Stage 1 stopped with no edge between them (a disconnected
+        // graph): every vertex is isolated and the trial's cut is exactly 0
+        std::vector<SparseNode> sparse;
+        for (uint32_t b = 0; b < B; b++) {
+            if (q.t > ctx->dense_limit) {
+                SparseNode nd;
+                CAC_TRY(sparse_root(ctx, eng, q, q.cuts + c0 + b, k0[b], idx[b], d_lab.as<uint32_t>() + (size_t)b * n,
+                                    kdim[b], &nd));
+                sparse.push_back(nd);
+                kdim[b] = 0;
+            } else if (kdim[b] > kMaxSmemVertices) {
+                kdim[b] = 0;
+            }
+        }
         const uint64_t esize = small ? 4 : 8;
         uint64_t bytes = 0;
         for (uint32_t b = 0; b < B; b++) bytes += ((uint64_t)kdim[b] * ld_of(kdim[b]) * esize + 15) / 16 * 16;
@@ -1598,6 +1666,7 @@ int admit_big(cac_ctx *ctx, KsEngine &eng, const QueryPlan &q) {
         roots->refs++;
         for (uint32_t b = 0; b < B; b++) {
             const uint64_t i = c0 + b;
+            if (q.t > ctx->dense_limit) continue;  // a sparse root
             if (kdim[b] < 2) {
                 fill_u64<<<1, 32, 0, s>>>(q.cuts + i, 1, 0);
                 continue;
@@ -1606,6 +1675,7 @@ int admit_big(cac_ctx *ctx, KsEngine &eng, const QueryPlan &q) {
         }
         eng.release(roots);
         CAC_CUDA_TRY(cudaStreamSynchronize(s));  // the scratch is reused by the next chunk
+        if (!sparse.empty()) CAC_TRY(sparse_phase(ctx, eng, std::move(sparse)));
     }
     return CAC_OK;
 }
@@ -1627,11 +1697,7 @@ int check_graph(const cac_graph *g, uint32_t t_override) {
         set_error("total edge weight >= 2^55 is not supported by the Stoer-Wagner leaf kernel");
         return CAC_ERR_UNSUPPORTED;
     }
-    const uint32_t t = t_override ? t_override : intermediate_size(g->n, g->m);
-    if (t > kMaxSmemVertices) {
-        set_error("contracted graphs with more than 16384 vertices are not supported yet");
-        return CAC_ERR_UNSUPPORTED;
-    }
+    (void)t_override;  // contracted sizes above the dense limit run as sparse roots
     return CAC_OK;
 }
 

@@ -342,6 +342,15 @@ using namespace cac;
 
 extern "C" {
 
+int cac_ctx_set_dense_limit(cac_ctx *ctx, uint32_t max_dense_vertices) {
+    if (!ctx || max_dense_vertices < 128 || max_dense_vertices > kMaxDenseVertices) {
+        set_error("cac_ctx_set_dense_limit: the limit must be in [128, 16384]");
+        return CAC_ERR_INVALID;
+    }
+    ctx->dense_limit = max_dense_vertices;
+    return CAC_OK;
+}
+
 const char *cac_error_string(int status) {
     switch (status) {
         case CAC_OK: return "ok";

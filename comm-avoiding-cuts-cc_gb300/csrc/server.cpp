@@ -370,7 +370,7 @@ int cac_server_submit(cac_server *s, const cac_request *req, uint64_t *ticket) {
             return CAC_ERR_INVALID;
         }
         const uint32_t t = intermediate_size(g->n, g->m);
-        if (g->total_weight >= (1ull << 55) || t > 16384) {
+        if (g->total_weight >= (1ull << 55)) {
             set_error("cac_server_submit: graph outside the supported square_root sizes");
             return CAC_ERR_UNSUPPORTED;
         }

@@ -38,7 +38,14 @@ constexpr uint32_t kET = 1024;   // edges per tile (4 per thread)
 constexpr uint32_t kVT = 1024;   // vertices per tile (4 per thread)
 constexpr uint32_t kPhaseOpen = 0, kPhaseRoundDone = 2;
 
+// One contraction task: its graph (edge arrays, u32 or u64 weights), target, stream key and scratch.
 struct BigTrial {
+    const uint32_t *U, *V;
+    const void *W;    // m weights: u32, or u64 when w64
+    uint64_t m;
+    uint32_t n, target;
+    uint32_t etiles, vtiles;
+    uint32_t w64;
     uint32_t *par;    // n
     uint64_t *pre;    // m: inclusive prefix of non-loop weights inside each edge tile
     uint64_t *tsum;   // edge tiles: tile totals, then their inclusive prefix
@@ -48,18 +55,12 @@ struct BigTrial {
     uint32_t *vsum;   // vertex tiles: root counts, then exclusive offsets
     uint32_t *k_out;  // output: vertices left
     uint32_t k0, idx; // stream key words 0, 1
+    uint64_t tag;     // stream key word 2
 };
 
 struct BigState {
     uint64_t W;
     uint32_t count, ndraw, lo, hi, mid, nlog, undo_n, apply_one, round, done, phase, err;
-};
-
-struct BigGraph {
-    const uint32_t *U, *V, *Wt;
-    uint64_t m;
-    uint32_t n, target;
-    uint32_t etiles, vtiles;
 };
 
 template <int NT>
@@ -106,39 +107,54 @@ __device__ __forceinline__ uint32_t groot(const uint32_t *par, uint32_t x) {
     return x;
 }
 
-__global__ void big_init(const BigTrial *T, BigState *st, BigGraph G) {
+__global__ void big_init(const BigTrial *T, BigState *st) {
     const uint32_t b = blockIdx.y;
-    uint32_t *par = T[b].par;
-    for (uint32_t v = blockIdx.x * blockDim.x + threadIdx.x; v < G.n; v += gridDim.x * blockDim.x) par[v] = v;
+    const BigTrial &t = T[b];
+    uint32_t *par = t.par;
+    for (uint32_t v = blockIdx.x * blockDim.x + threadIdx.x; v < t.n; v += gridDim.x * blockDim.x) par[v] = v;
     if (blockIdx.x == 0 && threadIdx.x == 0) {
         BigState s{};
-        s.count = G.n;
-        s.done = G.n <= G.target ? 1u : 0u;
+        s.count = t.n;
+        s.done = t.n <= t.target ? 1u : 0u;
         s.phase = kPhaseRoundDone;
         st[b] = s;
     }
 }
 
-__global__ void __launch_bounds__(kBT) big_edge_tiles(const BigTrial *T, const BigState *st, BigGraph G) {
+// Per 1024-edge tile of one task: the weights of its edges that are not loops under the current
+// union-find, their inclusive prefix inside the tile and the tile total. The 16-byte vector path
+// needs 16-byte aligned arrays (u32 weights; u64 weights are read as two 16-byte halves).
+template <bool kW64>
+__global__ void __launch_bounds__(kBT) big_edge_tiles(const BigTrial *T, const BigState *st) {
     const uint32_t b = blockIdx.y;
-    if (st[b].done) return;
-    const uint32_t *par = T[b].par;
+    const BigTrial &t = T[b];
+    if (st[b].done || blockIdx.x >= t.etiles || (t.w64 != 0) != kW64) return;
+    const uint32_t *par = t.par;
     const uint64_t e0 = (uint64_t)blockIdx.x * kET + threadIdx.x * 4;
-    uint32_t u[4], v[4], w[4];
-    if (e0 + 3 < G.m) {
-        const uint4 uu = *reinterpret_cast<const uint4 *>(G.U + e0);
-        const uint4 vv = *reinterpret_cast<const uint4 *>(G.V + e0);
-        const uint4 ww = *reinterpret_cast<const uint4 *>(G.Wt + e0);
+    uint32_t u[4], v[4];
+    uint64_t w[4];
+    const bool aligned = ((reinterpret_cast<uintptr_t>(t.U) | reinterpret_cast<uintptr_t>(t.V) |
+                           reinterpret_cast<uintptr_t>(t.W)) & 15) == 0;
+    if (e0 + 3 < t.m && aligned) {
+        const uint4 uu = *reinterpret_cast<const uint4 *>(t.U + e0);
+        const uint4 vv = *reinterpret_cast<const uint4 *>(t.V + e0);
         u[0] = uu.x; u[1] = uu.y; u[2] = uu.z; u[3] = uu.w;
         v[0] = vv.x; v[1] = vv.y; v[2] = vv.z; v[3] = vv.w;
-        w[0] = ww.x; w[1] = ww.y; w[2] = ww.z; w[3] = ww.w;
+        if (kW64) {
+            const ulonglong2 w01 = *reinterpret_cast<const ulonglong2 *>(static_cast<const uint64_t *>(t.W) + e0);
+            const ulonglong2 w23 = *reinterpret_cast<const ulonglong2 *>(static_cast<const uint64_t *>(t.W) + e0 + 2);
+            w[0] = w01.x; w[1] = w01.y; w[2] = w23.x; w[3] = w23.y;
+        } else {
+            const uint4 ww = *reinterpret_cast<const uint4 *>(static_cast<const uint32_t *>(t.W) + e0);
+            w[0] = ww.x; w[1] = ww.y; w[2] = ww.z; w[3] = ww.w;
+        }
     } else {
 #pragma unroll
         for (int k = 0; k < 4; k++) {
-            const bool in = e0 + k < G.m;
-            u[k] = in ? G.U[e0 + k] : 0;
-            v[k] = in ? G.V[e0 + k] : 0;
-            w[k] = in ? G.Wt[e0 + k] : 0;
+            const bool in = e0 + k < t.m;
+            u[k] = in ? t.U[e0 + k] : 0;
+            v[k] = in ? t.V[e0 + k] : 0;
+            w[k] = !in ? 0 : kW64 ? static_cast<const uint64_t *>(t.W)[e0 + k] : static_cast<const uint32_t *>(t.W)[e0 + k];
         }
     }
     uint64_t x[4], local = 0;
@@ -149,26 +165,27 @@ __global__ void __launch_bounds__(kBT) big_edge_tiles(const BigTrial *T, const B
     }
     uint64_t tot;
     uint64_t acc = bscan_u64<kBT>(local, tot);
-    uint64_t *pre = T[b].pre;
+    uint64_t *pre = t.pre;
 #pragma unroll
     for (int k = 0; k < 4; k++) {
         acc += x[k];
-        if (e0 + k < G.m) pre[e0 + k] = acc;
+        if (e0 + k < t.m) pre[e0 + k] = acc;
     }
-    if (threadIdx.x == 0) T[b].tsum[blockIdx.x] = tot;
+    if (threadIdx.x == 0) t.tsum[blockIdx.x] = tot;
 }
 
-__global__ void __launch_bounds__(1024) big_tile_scan(const BigTrial *T, BigState *st, BigGraph G) {
+__global__ void __launch_bounds__(1024) big_tile_scan(const BigTrial *T, BigState *st) {
     const uint32_t b = blockIdx.x;
     if (st[b].done) return;
-    uint64_t *ts = T[b].tsum;
+    const BigTrial &t = T[b];
+    uint64_t *ts = t.tsum;
     uint64_t carry = 0;
-    for (uint32_t base = 0; base < G.etiles; base += 1024) {
+    for (uint32_t base = 0; base < t.etiles; base += 1024) {
         const uint32_t i = base + threadIdx.x;
-        const uint64_t x = i < G.etiles ? ts[i] : 0;
+        const uint64_t x = i < t.etiles ? ts[i] : 0;
         uint64_t tot;
         const uint64_t ex = bscan_u64<1024>(x, tot);
-        if (i < G.etiles) ts[i] = carry + ex + x;
+        if (i < t.etiles) ts[i] = carry + ex + x;
         carry += tot;
     }
     if (threadIdx.x == 0) {
@@ -190,19 +207,19 @@ __global__ void __launch_bounds__(1024) big_tile_scan(const BigTrial *T, BigStat
     }
 }
 
-__global__ void __launch_bounds__(kBT) big_draws(const BigTrial *T, const BigState *st, BigGraph G) {
+__global__ void __launch_bounds__(kBT) big_draws(const BigTrial *T, const BigState *st) {
     const uint32_t b = blockIdx.y;
     const BigState s = st[b];
     if (s.done) return;
-    const BigTrial t = T[b];
+    const BigTrial &t = T[b];
     for (uint32_t j = blockIdx.x * kBT + threadIdx.x; j < s.ndraw; j += gridDim.x * kBT) {
-        const uint64_t y = mulhi64(draw64(t.k0, t.idx, 1, 0, s.round, j), s.W);
-        const uint32_t tile = (uint32_t)ub_u64(t.tsum, G.etiles, y);
+        const uint64_t y = mulhi64(draw64(t.k0, t.idx, t.tag, 0, s.round, j), s.W);
+        const uint32_t tile = (uint32_t)ub_u64(t.tsum, t.etiles, y);
         const uint64_t base = tile ? t.tsum[tile - 1] : 0;
         const uint64_t e0 = (uint64_t)tile * kET;
-        const uint64_t len = min((uint64_t)kET, G.m - e0);
+        const uint64_t len = min((uint64_t)kET, t.m - e0);
         const uint64_t e = e0 + ub_u64(t.pre + e0, len, y - base);
-        t.draws[j] = make_uint2(G.U[e], G.V[e]);
+        t.draws[j] = make_uint2(t.U[e], t.V[e]);
     }
 }
 
@@ -228,9 +245,10 @@ __global__ void __launch_bounds__(kBT) big_link(const BigTrial *T, BigState *st)
     }
 }
 
-__global__ void big_decide(BigState *st, uint32_t B, uint32_t target) {
+__global__ void big_decide(const BigTrial *T, BigState *st, uint32_t B) {
     const uint32_t b = blockIdx.x * blockDim.x + threadIdx.x;
     if (b >= B) return;
+    const uint32_t target = T[b].target;
     BigState &s = st[b];
     if (s.done || s.phase != kPhaseOpen) return;
     const uint32_t links = s.nlog;
@@ -261,9 +279,10 @@ __global__ void __launch_bounds__(kBT) big_undo(const BigTrial *T, const BigStat
     for (uint32_t i = blockIdx.x * kBT + threadIdx.x; i < n; i += gridDim.x * kBT) t.par[t.log[i]] = t.log[i];
 }
 
-__global__ void big_apply_one(const BigTrial *T, BigState *st, uint32_t B, uint32_t target) {
+__global__ void big_apply_one(const BigTrial *T, BigState *st, uint32_t B) {
     const uint32_t b = blockIdx.x * blockDim.x + threadIdx.x;
     if (b >= B) return;
+    const uint32_t target = T[b].target;
     BigState &s = st[b];
     s.undo_n = 0;
     if (!s.apply_one) return;
@@ -279,16 +298,18 @@ __global__ void big_apply_one(const BigTrial *T, BigState *st, uint32_t B, uint3
     s.phase = kPhaseRoundDone;
 }
 
-__global__ void big_compress(const BigTrial *T, BigGraph G) {
+__global__ void big_compress(const BigTrial *T) {
     const uint32_t b = blockIdx.y;
     uint32_t *par = T[b].par;
-    for (uint32_t v = blockIdx.x * blockDim.x + threadIdx.x; v < G.n; v += gridDim.x * blockDim.x)
+    const uint32_t n = T[b].n;
+    for (uint32_t v = blockIdx.x * blockDim.x + threadIdx.x; v < n; v += gridDim.x * blockDim.x)
         par[v] = groot(par, v);
 }
 
-__global__ void big_round_end(BigState *st, uint32_t B, uint32_t target, uint32_t *active) {
+__global__ void big_round_end(const BigTrial *T, BigState *st, uint32_t B, uint32_t *active) {
     const uint32_t b = blockIdx.x * blockDim.x + threadIdx.x;
     if (b >= B) return;
+    const uint32_t target = T[b].target;
     BigState &s = st[b];
     if (!s.done && s.phase != kPhaseRoundDone) s.err = 1;  // bisection did not close
     s.round += 1;
@@ -296,13 +317,15 @@ __global__ void big_round_end(BigState *st, uint32_t B, uint32_t target, uint32_
     if (!s.done) atomicAdd(active, 1u);
 }
 
-__global__ void __launch_bounds__(kBT) big_root_count(const BigTrial *T, BigGraph G) {
+__global__ void __launch_bounds__(kBT) big_root_count(const BigTrial *T) {
     const uint32_t b = blockIdx.y;
+    if (blockIdx.x >= T[b].vtiles) return;
     const uint32_t *par = T[b].par;
+    const uint32_t n = T[b].n;
     const uint32_t v0 = blockIdx.x * kVT + threadIdx.x * 4;
     uint32_t c = 0;
 #pragma unroll
-    for (int k = 0; k < 4; k++) c += (v0 + k < G.n && par[v0 + k] == v0 + k) ? 1u : 0u;
+    for (int k = 0; k < 4; k++) c += (v0 + k < n && par[v0 + k] == v0 + k) ? 1u : 0u;
     c = __reduce_add_sync(0xffffffffu, c);
     __shared__ uint32_t ws[kBT / 32];
     if ((threadIdx.x & 31) == 0) ws[threadIdx.x >> 5] = c;
@@ -314,29 +337,31 @@ __global__ void __launch_bounds__(kBT) big_root_count(const BigTrial *T, BigGrap
     }
 }
 
-__global__ void __launch_bounds__(1024) big_vscan(const BigTrial *T, const BigState *st, BigGraph G) {
+__global__ void __launch_bounds__(1024) big_vscan(const BigTrial *T) {
     const uint32_t b = blockIdx.x;
     uint32_t *vs = T[b].vsum;
+    const uint32_t vtiles = T[b].vtiles;
     uint64_t carry = 0;
-    for (uint32_t base = 0; base < G.vtiles; base += 1024) {
+    for (uint32_t base = 0; base < vtiles; base += 1024) {
         const uint32_t i = base + threadIdx.x;
-        const uint64_t x = i < G.vtiles ? vs[i] : 0;
+        const uint64_t x = i < vtiles ? vs[i] : 0;
         uint64_t tot;
         const uint64_t ex = bscan_u64<1024>(x, tot);
-        if (i < G.vtiles) vs[i] = (uint32_t)(carry + ex);
+        if (i < vtiles) vs[i] = (uint32_t)(carry + ex);
         carry += tot;
     }
     if (threadIdx.x == 0) *T[b].k_out = (uint32_t)carry;
 }
 
-__global__ void __launch_bounds__(kBT) big_label_roots(const BigTrial *T, BigGraph G) {
+__global__ void __launch_bounds__(kBT) big_label_roots(const BigTrial *T) {
     const uint32_t b = blockIdx.y;
-    const BigTrial t = T[b];
+    const BigTrial &t = T[b];
+    if (blockIdx.x >= t.vtiles) return;
     const uint32_t v0 = blockIdx.x * kVT + threadIdx.x * 4;
     uint32_t f[4], c = 0;
 #pragma unroll
     for (int k = 0; k < 4; k++) {
-        f[k] = (v0 + k < G.n && t.par[v0 + k] == v0 + k) ? 1u : 0u;
+        f[k] = (v0 + k < t.n && t.par[v0 + k] == v0 + k) ? 1u : 0u;
         c += f[k];
     }
     uint64_t tot;
@@ -346,10 +371,10 @@ __global__ void __launch_bounds__(kBT) big_label_roots(const BigTrial *T, BigGra
         if (f[k]) t.lab[v0 + k] = r++;
 }
 
-__global__ void big_label_rest(const BigTrial *T, BigGraph G) {
+__global__ void big_label_rest(const BigTrial *T) {
     const uint32_t b = blockIdx.y;
-    const BigTrial t = T[b];
-    for (uint32_t v = blockIdx.x * blockDim.x + threadIdx.x; v < G.n; v += gridDim.x * blockDim.x) {
+    const BigTrial &t = T[b];
+    for (uint32_t v = blockIdx.x * blockDim.x + threadIdx.x; v < t.n; v += gridDim.x * blockDim.x) {
         const uint32_t r = t.par[v];
         if (r != v) t.lab[v] = t.lab[r];
     }
@@ -357,21 +382,31 @@ __global__ void big_label_rest(const BigTrial *T, BigGraph G) {
 
 }  // namespace
 
-// Scratch of shrink_big for B trials, carved in the order shrink_big takes it.
-uint64_t shrink_big_scratch(uint32_t n, uint64_t m, uint32_t B) {
+// Scratch of one contraction task, carved in the order shrink_tasks takes it.
+uint64_t shrink_task_scratch(uint32_t n, uint64_t m) {
     const uint64_t etiles = (m + kET - 1) / kET, vtiles = ((uint64_t)n + kVT - 1) / kVT;
-    const uint64_t per = align_up(4ull * n) + align_up(8 * std::max<uint64_t>(m, 1)) +
-                         align_up(8 * std::max<uint64_t>(etiles, 1)) + align_up(8ull * n) + align_up(4ull * n) +
-                         align_up(4 * vtiles);
-    return per * B + align_up(sizeof(BigTrial) * B) + align_up(sizeof(BigState) * B) + align_up(16);
+    return align_up(4ull * n) + align_up(8 * std::max<uint64_t>(m, 1)) + align_up(8 * std::max<uint64_t>(etiles, 1)) +
+           align_up(8ull * n) + align_up(4ull * n) + align_up(4 * std::max<uint64_t>(vtiles, 1));
 }
 
-int shrink_big(cac_ctx *ctx, const cac_graph *g, uint32_t target, uint32_t B, const uint32_t *k0, const uint32_t *idx,
-               uint32_t *d_lab, uint32_t *d_kout, void *scratch) {
+uint64_t shrink_tasks_scratch(const std::vector<ShrinkTask> &tasks) {
+    uint64_t b = align_up(sizeof(BigTrial) * tasks.size()) + align_up(sizeof(BigState) * tasks.size()) + align_up(16);
+    for (const ShrinkTask &t : tasks) b += shrink_task_scratch(t.n, t.m);
+    return b;
+}
+
+// Stage-1 contraction of every task (rounds of weighted draws over the task's edges that are not
+// loops, contracted in draw order until exactly its target is left, or no edge is left), all
+// tasks stepped together: labels (rank of the smallest member) to task.lab, vertices left to
+// *task.k_out. The tasks may have different graphs, sizes, targets and keys.
+int shrink_tasks(cac_ctx *ctx, const std::vector<ShrinkTask> &tasks, void *scratch) {
     cudaStream_t s = ctx->stream;
-    const uint32_t n = g->n;
-    const uint64_t m = g->m;
-    BigGraph G{g->u, g->v, g->w, m, n, target, (uint32_t)((m + kET - 1) / kET), (uint32_t)((n + kVT - 1) / kVT)};
+    const uint32_t B = (uint32_t)tasks.size();
+    if (B == 0) return CAC_OK;
+    if (B > 65535) {
+        set_error("shrink_tasks: more than 65535 tasks in one call");
+        return CAC_ERR_INVALID;
+    }
     std::vector<BigTrial> T(B);
     char *p = static_cast<char *>(scratch);
     auto take = [&](size_t bytes) {
@@ -379,53 +414,73 @@ int shrink_big(cac_ctx *ctx, const cac_graph *g, uint32_t target, uint32_t B, co
         p += align_up(bytes);
         return q;
     };
+    uint32_t nmax = 1, etmax = 1, vtmax = 1;
+    uint64_t mmax = 0;
+    bool any32 = false, any64 = false;
     for (uint32_t b = 0; b < B; b++) {
+        const ShrinkTask &k = tasks[b];
         BigTrial &t = T[b];
-        t.par = reinterpret_cast<uint32_t *>(take(4ull * n));
-        t.pre = reinterpret_cast<uint64_t *>(take(8 * std::max<uint64_t>(m, 1)));
-        t.tsum = reinterpret_cast<uint64_t *>(take(8ull * std::max<uint32_t>(G.etiles, 1)));
-        t.draws = reinterpret_cast<uint2 *>(take(8ull * n));
-        t.log = reinterpret_cast<uint32_t *>(take(4ull * n));
-        t.vsum = reinterpret_cast<uint32_t *>(take(4ull * G.vtiles));
-        t.lab = d_lab + (size_t)b * n;
-        t.k_out = d_kout + b;
-        t.k0 = k0[b];
-        t.idx = idx[b];
+        t.U = k.U;
+        t.V = k.V;
+        t.W = k.W;
+        t.m = k.m;
+        t.n = k.n;
+        t.target = k.target;
+        t.etiles = (uint32_t)((k.m + kET - 1) / kET);
+        t.vtiles = (uint32_t)((k.n + kVT - 1) / kVT);
+        t.w64 = k.w64 ? 1u : 0u;
+        t.par = reinterpret_cast<uint32_t *>(take(4ull * k.n));
+        t.pre = reinterpret_cast<uint64_t *>(take(8 * std::max<uint64_t>(k.m, 1)));
+        t.tsum = reinterpret_cast<uint64_t *>(take(8ull * std::max<uint32_t>(t.etiles, 1)));
+        t.draws = reinterpret_cast<uint2 *>(take(8ull * k.n));
+        t.log = reinterpret_cast<uint32_t *>(take(4ull * k.n));
+        t.vsum = reinterpret_cast<uint32_t *>(take(4ull * std::max<uint32_t>(t.vtiles, 1)));
+        t.lab = k.lab;
+        t.k_out = k.k_out;
+        t.k0 = k.k0;
+        t.idx = k.idx;
+        t.tag = k.tag;
+        nmax = std::max(nmax, k.n);
+        mmax = std::max(mmax, k.m);
+        etmax = std::max(etmax, t.etiles);
+        vtmax = std::max(vtmax, t.vtiles);
+        (k.w64 ? any64 : any32) = true;
     }
     BigTrial *dT = reinterpret_cast<BigTrial *>(take(sizeof(BigTrial) * B));
     BigState *dS = reinterpret_cast<BigState *>(take(sizeof(BigState) * B));
     uint32_t *d_active = reinterpret_cast<uint32_t *>(take(16));
     CAC_CUDA_TRY(cudaMemcpyAsync(dT, T.data(), sizeof(BigTrial) * B, cudaMemcpyHostToDevice, s));
-    const uint32_t vgrid = std::max(1u, std::min<uint32_t>((n + kBT - 1) / kBT, 2048u / std::max(1u, B / 8 + 1)));
-    big_init<<<dim3(vgrid, B), kBT, 0, s>>>(dT, dS, G);
-    const uint32_t dgrid = std::max(1u, std::min<uint32_t>((n + kBT - 1) / kBT, 4096u / B + 1));
+    const uint32_t vgrid = std::max(1u, std::min<uint32_t>((nmax + kBT - 1) / kBT, 2048u / std::max(1u, B / 8 + 1)));
+    big_init<<<dim3(vgrid, B), kBT, 0, s>>>(dT, dS);
+    const uint32_t dgrid = std::max(1u, std::min<uint32_t>((nmax + kBT - 1) / kBT, 4096u / B + 1));
     uint32_t iters = 3;
-    while ((1ull << (iters - 3)) < n) iters++;  // ceil(log2 n) + 3 bisection steps close every round
+    while ((1ull << (iters - 3)) < nmax) iters++;  // ceil(log2 n) + 3 bisection steps close every round
     const unsigned tb = (B + 31) / 32;
     for (uint32_t round = 0;; round++) {
-        if (round > n) {  // every round with edges left links at least its first draw
+        if (round > nmax) {  // every round with edges left links at least its first draw
             set_error("Stage 1: more sampling rounds than vertices");
             return CAC_ERR_CUDA;
         }
-        if (m) {
-            big_edge_tiles<<<dim3(G.etiles, B), kBT, 0, s>>>(dT, dS, G);
-            big_tile_scan<<<B, 1024, 0, s>>>(dT, dS, G);
-            big_draws<<<dim3(dgrid, B), kBT, 0, s>>>(dT, dS, G);
+        if (mmax) {
+            if (any32) big_edge_tiles<false><<<dim3(etmax, B), kBT, 0, s>>>(dT, dS);
+            if (any64) big_edge_tiles<true><<<dim3(etmax, B), kBT, 0, s>>>(dT, dS);
+            big_tile_scan<<<B, 1024, 0, s>>>(dT, dS);
+            big_draws<<<dim3(dgrid, B), kBT, 0, s>>>(dT, dS);
             for (uint32_t it = 0; it < iters; it++) {
                 big_link<<<dim3(dgrid, B), kBT, 0, s>>>(dT, dS);
-                big_decide<<<tb, 32, 0, s>>>(dS, B, target);
+                big_decide<<<tb, 32, 0, s>>>(dT, dS, B);
                 big_undo<<<dim3(dgrid, B), kBT, 0, s>>>(dT, dS);
-                big_apply_one<<<tb, 32, 0, s>>>(dT, dS, B, target);
+                big_apply_one<<<tb, 32, 0, s>>>(dT, dS, B);
             }
         }
-        big_compress<<<dim3(vgrid, B), kBT, 0, s>>>(dT, G);
+        big_compress<<<dim3(vgrid, B), kBT, 0, s>>>(dT);
         CAC_CUDA_TRY(cudaMemsetAsync(d_active, 0, 4, s));
-        big_round_end<<<tb, 32, 0, s>>>(dS, B, target, d_active);
+        big_round_end<<<tb, 32, 0, s>>>(dT, dS, B, d_active);
         CAC_CUDA_TRY(cudaGetLastError());
         uint32_t active = 0;
         CAC_CUDA_TRY(cudaMemcpyAsync(&active, d_active, 4, cudaMemcpyDeviceToHost, s));
         CAC_CUDA_TRY(cudaStreamSynchronize(s));
-        if (!active || !m) break;
+        if (!active || !mmax) break;
     }
     std::vector<BigState> hs(B);
     CAC_CUDA_TRY(cudaMemcpyAsync(hs.data(), dS, sizeof(BigState) * B, cudaMemcpyDeviceToHost, s));
@@ -435,12 +490,27 @@ int shrink_big(cac_ctx *ctx, const cac_graph *g, uint32_t target, uint32_t B, co
             set_error("Stage 1: inconsistent contraction state");
             return CAC_ERR_CUDA;
         }
-    big_root_count<<<dim3(G.vtiles, B), kBT, 0, s>>>(dT, G);
-    big_vscan<<<B, 1024, 0, s>>>(dT, dS, G);
-    big_label_roots<<<dim3(G.vtiles, B), kBT, 0, s>>>(dT, G);
-    big_label_rest<<<dim3(vgrid, B), kBT, 0, s>>>(dT, G);
+    big_root_count<<<dim3(vtmax, B), kBT, 0, s>>>(dT);
+    big_vscan<<<B, 1024, 0, s>>>(dT);
+    big_label_roots<<<dim3(vtmax, B), kBT, 0, s>>>(dT);
+    big_label_rest<<<dim3(vgrid, B), kBT, 0, s>>>(dT);
     CAC_CUDA_TRY(cudaGetLastError());
     return CAC_OK;
+}
+
+// Scratch of shrink_big for B trials of one graph.
+uint64_t shrink_big_scratch(uint32_t n, uint64_t m, uint32_t B) {
+    return shrink_task_scratch(n, m) * B + align_up(sizeof(BigTrial) * B) + align_up(sizeof(BigState) * B) +
+           align_up(16);
+}
+
+int shrink_big(cac_ctx *ctx, const cac_graph *g, uint32_t target, uint32_t B, const uint32_t *k0, const uint32_t *idx,
+               uint32_t *d_lab, uint32_t *d_kout, void *scratch) {
+    std::vector<ShrinkTask> tasks(B);
+    for (uint32_t b = 0; b < B; b++)
+        tasks[b] = ShrinkTask{g->u, g->v, g->w, false, g->m, g->n, target, k0[b], idx[b], 1,
+                              d_lab + (size_t)b * g->n, d_kout + b};
+    return shrink_tasks(ctx, tasks, scratch);
 }
 
 }  // namespace cac

@@ -1,0 +1,287 @@
+// Device sort and merge of weighted edge lists: the GB300 form of the reference's relabel / sort /
+// duplicate-merge step (src/WeightedIteratedSparseSampling.cpp:26-234 with
+// src/sorting/SamplingSorter.hpp:44-180, which sample-sort (u, v, w) triples across ranks and then
+// sum the weights of equal (u, v); src/karger-stein/sparse_graph.hpp:451-545 relabel + compact).
+//
+//   edge_keys         relabel: edge (a, b, w) of the parent becomes key lab[a] * k + lab[b] with
+//                     the smaller label first, or the loop key k * k when both labels agree
+//   radix sort        least-significant-digit, 8-bit digits, stable, (u64 key, u64 weight) pairs:
+//                     per pass a per-tile digit histogram, one exclusive scan over (digit, tile),
+//                     and a stable scatter that ranks equal digits inside a tile by warp match
+//                     voting; only the digits below the key bound are sorted
+//   merge             segment heads (key differs from its predecessor), an exclusive scan of the
+//                     heads gives each distinct key its slot, weights are summed into the slot with
+//                     u64 atomics (integer sums: the result does not depend on their order); loop
+//                     keys are dropped
+// The merged list is sorted by (smaller end, larger end) and holds each pair once.
+#include "cac_internal.h"
+
+#include <algorithm>
+
+namespace cac {
+namespace {
+
+constexpr int kST = 256;                   // threads per sort CTA
+constexpr int kSItems = 16;                // keys per thread in a sort tile
+constexpr int kSTile = kST * kSItems;      // keys per sort tile
+constexpr int kRadix = 256;
+
+// Exclusive scan of n u32 values in place, by tiles of 4096: tile sums, a scan of the sums by one
+// CTA (looped), then every tile adds its offset. *total receives the sum.
+__global__ void __launch_bounds__(kST) scan_tile_sums(const uint32_t *x, uint64_t n, uint32_t *sums) {
+    __shared__ uint32_t ws[kST / 32];
+    const uint64_t base = (uint64_t)blockIdx.x * kSTile;
+    uint32_t s = 0;
+    for (int k = 0; k < kSItems; k++) {
+        const uint64_t i = base + (uint64_t)k * kST + threadIdx.x;
+        if (i < n) s += x[i];
+    }
+    s = __reduce_add_sync(0xffffffffu, s);
+    if ((threadIdx.x & 31) == 0) ws[threadIdx.x >> 5] = s;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        uint32_t t = 0;
+        for (int w = 0; w < kST / 32; w++) t += ws[w];
+        sums[blockIdx.x] = t;
+    }
+}
+
+__global__ void __launch_bounds__(1024) scan_sums(uint32_t *sums, uint32_t nt, uint32_t *total) {
+    __shared__ uint32_t ws[32];
+    __shared__ uint32_t carry;
+    if (threadIdx.x == 0) carry = 0;
+    __syncthreads();
+    const int l = threadIdx.x & 31, w = threadIdx.x >> 5;
+    for (uint32_t base = 0; base < nt; base += 1024) {
+        const uint32_t i = base + threadIdx.x;
+        const uint32_t x = i < nt ? sums[i] : 0;
+        uint32_t s = x;
+        for (int o = 1; o < 32; o <<= 1) {
+            const uint32_t y = __shfl_up_sync(0xffffffffu, s, o);
+            if (l >= o) s += y;
+        }
+        if (l == 31) ws[w] = s;
+        __syncthreads();
+        if (w == 0) {
+            uint32_t t = ws[l];
+            for (int o = 1; o < 32; o <<= 1) {
+                const uint32_t y = __shfl_up_sync(0xffffffffu, t, o);
+                if (l >= o) t += y;
+            }
+            ws[l] = t;
+        }
+        __syncthreads();
+        const uint32_t off = carry + (w ? ws[w - 1] : 0);
+        if (i < nt) sums[i] = off + s - x;
+        __syncthreads();
+        if (threadIdx.x == 1023) carry = off + s;
+        __syncthreads();
+    }
+    if (threadIdx.x == 0 && total) *total = carry;
+}
+
+__global__ void __launch_bounds__(kST) scan_apply(uint32_t *x, uint64_t n, const uint32_t *sums) {
+    __shared__ uint32_t ws[kST / 32];
+    const uint64_t base = (uint64_t)blockIdx.x * kSTile + (uint64_t)threadIdx.x * kSItems;
+    uint32_t v[kSItems], s = 0;
+#pragma unroll
+    for (int k = 0; k < kSItems; k++) {
+        v[k] = base + k < n ? x[base + k] : 0;
+        s += v[k];
+    }
+    const int l = threadIdx.x & 31, w = threadIdx.x >> 5;
+    uint32_t inc = s;
+    for (int o = 1; o < 32; o <<= 1) {
+        const uint32_t y = __shfl_up_sync(0xffffffffu, inc, o);
+        if (l >= o) inc += y;
+    }
+    if (l == 31) ws[w] = inc;
+    __syncthreads();
+    uint32_t before = sums[blockIdx.x];
+    for (int i = 0; i < w; i++) before += ws[i];
+    uint32_t acc = before + inc - s;
+#pragma unroll
+    for (int k = 0; k < kSItems; k++) {
+        if (base + k < n) x[base + k] = acc;
+        acc += v[k];
+    }
+}
+
+// relabelled keys and weights of a parent's edges (loops get the largest key, k * k)
+template <typename WT>
+__global__ void edge_keys(const uint32_t *__restrict__ a, const uint32_t *__restrict__ b, const WT *__restrict__ w,
+                          uint64_t m, const uint32_t *__restrict__ lab, uint32_t k, uint64_t *keys, uint64_t *vals) {
+    for (uint64_t e = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; e < m; e += (uint64_t)gridDim.x * blockDim.x) {
+        uint32_t x = a[e], y = b[e];
+        if (lab) {
+            x = lab[x];
+            y = lab[y];
+        }
+        const uint32_t lo = min(x, y), hi = max(x, y);
+        keys[e] = lo == hi ? (uint64_t)k * k : (uint64_t)lo * k + hi;
+        vals[e] = (uint64_t)w[e];
+    }
+}
+
+// per-tile histogram of digit (key >> shift) & 255, stored digit-major: hist[d * tiles + tile]
+__global__ void __launch_bounds__(kST) radix_hist(const uint64_t *__restrict__ keys, uint64_t n, int shift,
+                                                  uint32_t *hist, uint32_t tiles) {
+    __shared__ uint32_t h[kRadix];
+    h[threadIdx.x] = 0;
+    __syncthreads();
+    const uint64_t base = (uint64_t)blockIdx.x * kSTile;
+    for (int k = 0; k < kSItems; k++) {
+        const uint64_t i = base + (uint64_t)k * kST + threadIdx.x;
+        if (i < n) atomicAdd(&h[(keys[i] >> shift) & 255], 1u);
+    }
+    __syncthreads();
+    hist[(uint64_t)threadIdx.x * tiles + blockIdx.x] = h[threadIdx.x];
+}
+
+// Stable scatter of one tile: rounds of kST keys in order; inside a round, a key's position among
+// the equal digits before it = earlier rounds' count + earlier warps' count + its rank in its warp
+// (match voting). offs[d * tiles + tile] is where this tile's keys of digit d start.
+__global__ void __launch_bounds__(kST) radix_scatter(const uint64_t *__restrict__ keys, const uint64_t *__restrict__ vals,
+                                                     uint64_t n, int shift, const uint32_t *__restrict__ offs,
+                                                     uint32_t tiles, uint64_t *okeys, uint64_t *ovals) {
+    __shared__ uint32_t base[kRadix];
+    __shared__ uint32_t wcnt[kST / 32][kRadix];
+    const int l = threadIdx.x & 31, w = threadIdx.x >> 5;
+    base[threadIdx.x] = offs[(uint64_t)threadIdx.x * tiles + blockIdx.x];
+    for (int j = 0; j < kST / 32; j++) wcnt[j][threadIdx.x] = 0;
+    __syncthreads();
+    const uint64_t t0 = (uint64_t)blockIdx.x * kSTile;
+    for (int k = 0; k < kSItems; k++) {
+        const uint64_t i = t0 + (uint64_t)k * kST + threadIdx.x;
+        const bool in = i < n;
+        const uint64_t key = in ? keys[i] : 0;
+        const uint64_t val = in ? vals[i] : 0;
+        const uint32_t d = in ? (uint32_t)(key >> shift) & 255 : 256u + l;  // off-range lanes match nobody
+        const uint32_t peers = __match_any_sync(0xffffffffu, d);
+        const uint32_t rank = __popc(peers & ((1u << l) - 1));
+        if (in && rank == 0) wcnt[w][d] = __popc(peers);
+        __syncthreads();
+        if (in) {
+            uint32_t pos = base[d] + rank;
+            for (int j = 0; j < w; j++) pos += wcnt[j][d];
+            okeys[pos] = key;
+            ovals[pos] = val;
+        }
+        __syncthreads();
+        uint32_t add = 0;
+        for (int j = 0; j < kST / 32; j++) {
+            add += wcnt[j][threadIdx.x];
+            wcnt[j][threadIdx.x] = 0;
+        }
+        base[threadIdx.x] += add;
+        __syncthreads();
+    }
+}
+
+__global__ void seg_heads(const uint64_t *keys, uint64_t n, uint64_t loop_key, uint32_t *head) {
+    for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (uint64_t)gridDim.x * blockDim.x)
+        head[i] = keys[i] != loop_key && (i == 0 || keys[i] != keys[i - 1]) ? 1u : 0u;
+}
+
+// After the scan, slot[i] is the number of distinct keys before i: a head writes its pair, every
+// key adds its weight into its segment's slot (the head's).
+__global__ void seg_merge(const uint64_t *keys, const uint64_t *vals, uint64_t n, uint64_t loop_key, uint32_t k,
+                          const uint32_t *slot, uint32_t *oa, uint32_t *ob, unsigned long long *ow) {
+    for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (uint64_t)gridDim.x * blockDim.x) {
+        const uint64_t key = keys[i];
+        if (key == loop_key) continue;
+        const bool head = i == 0 || keys[i - 1] != key;
+        const uint32_t s = head ? slot[i] : slot[i] - 1;
+        if (head) {
+            oa[s] = (uint32_t)(key / k);
+            ob[s] = (uint32_t)(key % k);
+        }
+        atomicAdd(ow + s, (unsigned long long)vals[i]);
+    }
+}
+
+unsigned grid_of(cac_ctx *ctx, uint64_t work) {
+    return (unsigned)std::max<uint64_t>(1, std::min<uint64_t>((work + 255) / 256, (uint64_t)ctx->num_sms * 8));
+}
+
+}  // namespace
+
+uint64_t merge_edges_scratch(uint64_t m) {
+    const uint64_t tiles = (m + kSTile - 1) / kSTile;
+    return 4 * align_up(8 * std::max<uint64_t>(m, 1)) + align_up(4 * kRadix * std::max<uint64_t>(tiles, 1)) +
+           align_up(4 * std::max<uint64_t>(m, 1)) + 2 * align_up(4 * ((kRadix * tiles + kSTile - 1) / kSTile + 1)) +
+           align_up(16);
+}
+
+// Exclusive scan of n u32 values in place (tile sums in `sums`, which holds >= ceil(n / 4096)
+// words); *total (device, nullable) receives the sum.
+int scan_u32(cac_ctx *ctx, uint32_t *x, uint64_t n, uint32_t *sums, uint32_t *total) {
+    cudaStream_t s = ctx->stream;
+    const uint64_t nt = (n + kSTile - 1) / kSTile;
+    if (nt == 0) {
+        if (total) CAC_CUDA_TRY(cudaMemsetAsync(total, 0, 4, s));
+        return CAC_OK;
+    }
+    scan_tile_sums<<<(unsigned)nt, kST, 0, s>>>(x, n, sums);
+    scan_sums<<<1, 1024, 0, s>>>(sums, (uint32_t)nt, total);
+    scan_apply<<<(unsigned)nt, kST, 0, s>>>(x, n, sums);
+    CAC_CUDA_TRY(cudaGetLastError());
+    return CAC_OK;
+}
+
+// The child edge list of labels lab (or the identity when lab is null) over k vertices: every
+// non-loop edge (lab[a], lab[b], w) of the parent's m edges, sorted by (smaller, larger end) with
+// equal pairs merged (u64 weight sums). Writes the pairs to oa/ob/ow (room for m entries) and the
+// number of distinct pairs to *d_count (device). k * k must stay below 2^63.
+template <typename WT>
+int merge_edges(cac_ctx *ctx, const uint32_t *a, const uint32_t *b, const WT *w, uint64_t m, const uint32_t *lab,
+                uint32_t k, uint32_t *oa, uint32_t *ob, uint64_t *ow, uint32_t *d_count, void *scratch) {
+    cudaStream_t s = ctx->stream;
+    if (m == 0) {
+        CAC_CUDA_TRY(cudaMemsetAsync(d_count, 0, 4, s));
+        return CAC_OK;
+    }
+    const uint64_t tiles = (m + kSTile - 1) / kSTile;
+    if (tiles * kRadix > 0xFFFFFFFFull || m > 0xFFFFFFFFull) {
+        set_error("merge_edges: too many edges for 32-bit offsets");
+        return CAC_ERR_UNSUPPORTED;
+    }
+    char *p = static_cast<char *>(scratch);
+    auto take = [&](size_t bytes) {
+        char *q = p;
+        p += align_up(bytes);
+        return q;
+    };
+    uint64_t *k0 = reinterpret_cast<uint64_t *>(take(8 * m)), *v0 = reinterpret_cast<uint64_t *>(take(8 * m));
+    uint64_t *k1 = reinterpret_cast<uint64_t *>(take(8 * m)), *v1 = reinterpret_cast<uint64_t *>(take(8 * m));
+    uint32_t *hist = reinterpret_cast<uint32_t *>(take(4 * kRadix * tiles));
+    uint32_t *slot = reinterpret_cast<uint32_t *>(take(4 * m));
+    const uint64_t hn = kRadix * tiles;
+    uint32_t *sums = reinterpret_cast<uint32_t *>(take(4 * ((hn + kSTile - 1) / kSTile + 1)));
+    (void)take(4 * ((hn + kSTile - 1) / kSTile + 1));
+    edge_keys<WT><<<grid_of(ctx, m), 256, 0, s>>>(a, b, w, m, lab, k, k0, v0);
+    const uint64_t loop_key = (uint64_t)k * k;
+    int bits = 1;
+    while (bits < 64 && (loop_key >> bits) != 0) bits++;
+    for (int shift = 0; shift < bits; shift += 8) {
+        radix_hist<<<(unsigned)tiles, kST, 0, s>>>(k0, m, shift, hist, (uint32_t)tiles);
+        CAC_TRY(scan_u32(ctx, hist, hn, sums, nullptr));
+        radix_scatter<<<(unsigned)tiles, kST, 0, s>>>(k0, v0, m, shift, hist, (uint32_t)tiles, k1, v1);
+        std::swap(k0, k1);
+        std::swap(v0, v1);
+    }
+    seg_heads<<<grid_of(ctx, m), 256, 0, s>>>(k0, m, loop_key, slot);
+    CAC_TRY(scan_u32(ctx, slot, m, sums, d_count));
+    CAC_CUDA_TRY(cudaMemsetAsync(ow, 0, 8 * m, s));
+    seg_merge<<<grid_of(ctx, m), 256, 0, s>>>(k0, v0, m, loop_key, k, slot, oa, ob,
+                                              reinterpret_cast<unsigned long long *>(ow));
+    CAC_CUDA_TRY(cudaGetLastError());
+    return CAC_OK;
+}
+
+template int merge_edges<uint32_t>(cac_ctx *, const uint32_t *, const uint32_t *, const uint32_t *, uint64_t,
+                                   const uint32_t *, uint32_t, uint32_t *, uint32_t *, uint64_t *, uint32_t *, void *);
+template int merge_edges<uint64_t>(cac_ctx *, const uint32_t *, const uint32_t *, const uint64_t *, uint64_t,
+                                   const uint32_t *, uint32_t, uint32_t *, uint32_t *, uint64_t *, uint32_t *, void *);
+
+}  // namespace cac

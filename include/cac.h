@@ -74,6 +74,12 @@ typedef struct {
 
 /* ---- context ---- */
 int cac_ctx_create(const cac_config *config, cac_ctx **out);
+/* Karger-Stein recursion nodes with more vertices than this (default and maximum 16384, minimum
+ * 128), or above 128 vertices with fewer than N^2 / 32 edges, are kept as edge lists (the
+ * reference's sparse recursion, co_mincut.h:401-405); the others as dense matrices. It changes the
+ * trials' draws, never the validity of a cut; a lower limit moves more of the recursion to the
+ * sparse form. */
+int cac_ctx_set_dense_limit(cac_ctx *ctx, uint32_t max_dense_vertices);
 /* Destroys the ctx; graphs still alive are released with it and their handles become invalid. */
 int cac_ctx_destroy(cac_ctx *ctx);
 const char *cac_error_string(int status);
@@ -185,8 +191,10 @@ int cac_mincut_batch(cac_ctx *ctx, const cac_mincut_query *queries, uint32_t cou
 /* Plain Karger-Stein on the whole graph, as the reference's karger_stein executable runs
  * comincut::minimum_cut (src/executables/karger_stein.cpp, co_mincut.h:515-521): the Karger-Stein
  * library's own trial count for n vertices (comincut::number_of_trials, co_mincut.cpp:44-73), each
- * trial a recursion from the dense matrix of the whole graph (no sqrt(m) pre-contraction); trial i
- * draws from key (seed, i, 1 + heap index). n <= 16384 (CAC_ERR_UNSUPPORTED above).
+ * trial a recursion from the whole graph (no sqrt(m) pre-contraction): its dense matrix, or its edge
+ * list when the graph is sparse (above the dense limit, or fewer than n^2 / 32 edges above 128
+ * vertices: the reference's switch, co_mincut.h:401-405); trial i draws from key
+ * (seed, i, 1 + heap index).
  * res->trials_per_rank = res->total_trials = the trial count; res->intermediate = n. */
 int cac_karger_stein(cac_ctx *ctx, const cac_graph *g, double success_probability, uint32_t seed,
                      cac_mincut_result *res);
@@ -194,6 +202,10 @@ int cac_karger_stein(cac_ctx *ctx, const cac_graph *g, double success_probabilit
  * cuts_host[r * trials_per_rank + i]. */
 int cac_mincut_trials(cac_ctx *ctx, const cac_graph *g, uint32_t seed, uint32_t virtual_ranks,
                       uint32_t trials_per_rank, uint64_t *cuts_host);
+/* Trials 0 .. trials - 1 of plain Karger-Stein (cac_karger_stein's recursion from the whole graph),
+ * each trial's cut to cuts_host[i]: the loop of comincut::minimum_cut_trials (co_mincut.h:315-342)
+ * with every trial's value kept. */
+int cac_karger_stein_trials(cac_ctx *ctx, const cac_graph *g, uint32_t seed, uint32_t trials, uint64_t *cuts_host);
 /* One Karger-Stein trial (virtual rank, trial index) on a dense symmetric n x n host matrix. */
 int cac_ks_dense(cac_ctx *ctx, uint32_t n, const uint64_t *mat_host, uint32_t seed, uint32_t rank, uint32_t trial,
                  uint64_t *cut);

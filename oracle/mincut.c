@@ -479,14 +479,203 @@ uint32_t orc_shrink_to_dense(uint32_t n, uint64_t m, const uint32_t *u, const ui
     return k;
 }
 
+/* ------------------------------------------------------------------ sparse Karger-Stein nodes
+ * libcac's definition of the sparse part of a trial (the reference's sparse recursion,
+ * co_mincut.h:131-155 and 401-405, contracts a sparse node by exponential edge scores and a prefix
+ * connected components; libcac contracts it by the same weighted rounds as Stage 1):
+ *   - a node is kept as an edge list when it has more than the dense limit (16384 vertices, or
+ *     the value set with orc_set_dense_limit) or, above 128 vertices, fewer than N^2 / 32 edges;
+ *     otherwise it becomes the dense matrix of the dense recursion above;
+ *   - the child with heap index c of a sparse node contracts the node's edge list to
+ *     max(ceil(N / sqrt 2) + 1, 128) vertices by the Stage 1 rounds with key (k0, trial, 1 + c, 0)
+ *     (weighted draws over the edges that are not loops at the start of each round, in the
+ *     list's order; contracted in draw order; early stop when no edge is left);
+ *   - the child's edge list: every edge relabelled by rank-of-minimum labels, loops dropped,
+ *     sorted by (smaller end, larger end), equal pairs merged with their weights summed
+ *     (WeightedIteratedSparseSampling::reduce and SamplingSorter, sparse_graph::relabel/compact);
+ *   - a node without edges has cut 0; a sparse root (plain Karger-Stein on a sparse graph, or a
+ *     square_root trial whose contracted size is above the dense limit) also delivers its minimum
+ *     weighted degree. The root of plain Karger-Stein is the input edge list as given. */
+static uint32_t g_dense_limit = 16384;
+void orc_set_dense_limit(uint32_t n) { g_dense_limit = n < 128 ? 128 : n; }
+
+typedef struct { uint32_t n; uint64_t m; uint32_t *a, *b; uint64_t *w; } sgraph;
+static void sg_free(sgraph *g) { free(g->a); free(g->b); free(g->w); }
+
+static int is_dense(uint32_t n, uint64_t m) {
+    return n <= g_dense_limit && (n <= 128 || 32 * m >= (uint64_t)n * n);
+}
+
+/* Stage 1 rounds on an edge list with u64 weights and key `key`: labels (rank of the smallest
+ * member) to lab, returns the vertex count left */
+static uint32_t stage1(uint32_t n, uint64_t m, const uint32_t *u, const uint32_t *v, const uint64_t *w,
+                       uint32_t target, const uint64_t key[4], uint32_t *lab) {
+    uint32_t *p = (uint32_t *)malloc(sizeof(uint32_t) * (n ? n : 1));
+    for (uint32_t i = 0; i < n; i++) p[i] = i;
+    uint32_t count = n;
+    uint64_t *pre = (uint64_t *)malloc(sizeof(uint64_t) * (m ? m : 1));
+    for (uint64_t round = 0; count > target; round++) {
+        uint64_t W = 0;
+        for (uint64_t e = 0; e < m; e++) {
+            if (qfind(p, u[e]) != qfind(p, v[e])) W += w[e];
+            pre[e] = W;
+        }
+        if (W == 0) break;
+        uint32_t start = count;
+        for (uint64_t d = 0; d < start && count > target; d++) {
+            uint64_t y = mulhi64(orc_draw64(key, round, d), W);
+            uint64_t lo = 0, hi = m - 1;
+            while (lo < hi) { uint64_t mid = (lo + hi) / 2; if (pre[mid] > y) hi = mid; else lo = mid + 1; }
+            uint32_t ra = qfind(p, u[lo]), rb = qfind(p, v[lo]);
+            if (ra != rb) { if (ra < rb) p[rb] = ra; else p[ra] = rb; count--; }
+        }
+    }
+    free(pre);
+    uint32_t k = rank_labels(n, p, lab);
+    free(p);
+    return k;
+}
+
+typedef struct { uint64_t key, w; } kw;
+static int kw_cmp(const void *x, const void *y) {
+    const uint64_t a = ((const kw *)x)->key, b = ((const kw *)y)->key;
+    return a < b ? -1 : a > b;
+}
+
+/* relabel (lab may be NULL: identity), drop loops, sort by (smaller, larger end), merge */
+static void merge_child(uint64_t m, const uint32_t *u, const uint32_t *v, const uint64_t *w, const uint32_t *lab,
+                        uint32_t k, sgraph *out) {
+    kw *e = (kw *)malloc(sizeof(kw) * (m ? m : 1));
+    uint64_t c = 0;
+    for (uint64_t i = 0; i < m; i++) {
+        uint32_t x = lab ? lab[u[i]] : u[i], y = lab ? lab[v[i]] : v[i];
+        if (x == y) continue;
+        uint32_t lo = x < y ? x : y, hi = x ^ y ^ lo;
+        e[c].key = (uint64_t)lo * k + hi;
+        e[c].w = w[i];
+        c++;
+    }
+    qsort(e, c, sizeof(kw), kw_cmp);
+    out->n = k;
+    out->a = (uint32_t *)malloc(sizeof(uint32_t) * (c ? c : 1));
+    out->b = (uint32_t *)malloc(sizeof(uint32_t) * (c ? c : 1));
+    out->w = (uint64_t *)malloc(sizeof(uint64_t) * (c ? c : 1));
+    uint64_t j = 0;
+    for (uint64_t i = 0; i < c; i++) {
+        if (j && (uint64_t)out->a[j - 1] * k + out->b[j - 1] == e[i].key) { out->w[j - 1] += e[i].w; continue; }
+        out->a[j] = (uint32_t)(e[i].key / k);
+        out->b[j] = (uint32_t)(e[i].key % k);
+        out->w[j] = e[i].w;
+        j++;
+    }
+    out->m = j;
+    free(e);
+}
+
+static uint64_t *dense_of(const sgraph *g) {
+    uint64_t *mat = (uint64_t *)calloc((size_t)g->n * g->n, sizeof(uint64_t));
+    for (uint64_t i = 0; i < g->m; i++) {
+        mat[(size_t)g->a[i] * g->n + g->b[i]] += g->w[i];
+        mat[(size_t)g->b[i] * g->n + g->a[i]] += g->w[i];
+    }
+    return mat;
+}
+
+static uint64_t min_degree(uint32_t n, uint64_t m, const uint32_t *u, const uint32_t *v, const uint64_t *w) {
+    uint64_t *deg = (uint64_t *)calloc(n ? n : 1, sizeof(uint64_t));
+    for (uint64_t e = 0; e < m; e++) if (u[e] != v[e]) { deg[u[e]] += w[e]; deg[v[e]] += w[e]; }
+    uint64_t best = U64MAX;
+    for (uint32_t i = 0; i < n; i++) if (deg[i] < best) best = deg[i];
+    free(deg);
+    return best;
+}
+
+static uint64_t ks_sparse(uint32_t n, uint64_t m, const uint32_t *u, const uint32_t *v, const uint64_t *w,
+                          uint32_t seed_r, uint32_t trial, uint64_t h) {
+    if (m == 0) return 0;
+    uint32_t target = (uint32_t)orc_ks_target((int)n);
+    uint32_t *lab = (uint32_t *)malloc(sizeof(uint32_t) * n);
+    uint64_t best = U64MAX;
+    for (uint64_t c = 0; c < 2; c++) {
+        uint64_t child = 2 * h + c;
+        uint64_t key[4] = {seed_r, trial, 1 + child, 0};
+        uint32_t k = stage1(n, m, u, v, w, target, key, lab);
+        sgraph ch;
+        merge_child(m, u, v, w, lab, k, &ch);
+        uint64_t r;
+        if (ch.m == 0) {
+            r = 0;
+        } else if (is_dense(k, ch.m)) {
+            uint64_t *mat = dense_of(&ch);
+            r = ks_node(k, mat, seed_r, trial, child);
+            free(mat);
+        } else {
+            r = ks_sparse(k, ch.m, ch.a, ch.b, ch.w, seed_r, trial, child);
+        }
+        sg_free(&ch);
+        if (r < best) best = r;
+    }
+    free(lab);
+    return best;
+}
+
+/* one trial of a sparse root (already in its list form) */
+static uint64_t sparse_root(uint32_t n, uint64_t m, const uint32_t *u, const uint32_t *v, const uint64_t *w,
+                            uint32_t seed_r, uint32_t trial) {
+    uint64_t ub = min_degree(n, m, u, v, w);
+    uint64_t r = ks_sparse(n, m, u, v, w, seed_r, trial, 1);
+    return r < ub ? r : ub;
+}
+
+static uint64_t *widen(uint64_t m, const uint32_t *w) {
+    uint64_t *x = (uint64_t *)malloc(sizeof(uint64_t) * (m ? m : 1));
+    for (uint64_t i = 0; i < m; i++) x[i] = w[i];
+    return x;
+}
+
 uint64_t orc_mincut_trial(uint32_t n, uint64_t m, const uint32_t *u, const uint32_t *v, const uint32_t *w,
                           uint32_t seed, uint32_t rank, uint32_t trial) {
     if (n < 2) return U64MAX;
     uint32_t t = orc_intermediate_size(n, m);
+    if (t > g_dense_limit) {
+        /* Stage 1 to t, then the sparse root: the contracted graph merged by the device sort */
+        uint64_t *w64 = widen(m, w);
+        uint32_t *lab = (uint32_t *)malloc(sizeof(uint32_t) * n);
+        uint64_t key[4] = {(uint32_t)(seed + rank), trial, 1, 0};
+        uint32_t k = t < n ? stage1(n, m, u, v, w64, t, key, lab) : n;
+        sgraph root;
+        merge_child(m, u, v, w64, t < n ? lab : NULL, k, &root);
+        uint64_t r = (k < 2 || root.m == 0) ? 0 : sparse_root(k, root.m, root.a, root.b, root.w, seed + rank, trial);
+        sg_free(&root);
+        free(lab); free(w64);
+        return r;
+    }
     uint64_t *mat = (uint64_t *)malloc(sizeof(uint64_t) * (size_t)(t < n ? n : t) * (t < n ? n : t));
     uint32_t k = orc_shrink_to_dense(n, m, u, v, w, t, seed, rank, trial, mat);
     uint64_t r = k < 2 ? 0 : orc_ks_dense(k, mat, seed, rank, trial);
     free(mat);
+    return r;
+}
+
+/* one trial of plain Karger-Stein on the whole graph (the karger_stein executable): the root is
+ * dense (the n x n matrix) or sparse (the input edge list as given) by the rule above */
+uint64_t orc_ks_trial(uint32_t n, uint64_t m, const uint32_t *u, const uint32_t *v, const uint32_t *w, uint32_t seed,
+                      uint32_t trial) {
+    if (n < 2) return U64MAX;
+    if (is_dense(n, m)) {
+        uint64_t *mat = (uint64_t *)calloc((size_t)n * n, sizeof(uint64_t));
+        for (uint64_t e = 0; e < m; e++) {
+            if (u[e] == v[e]) continue;
+            mat[(size_t)u[e] * n + v[e]] += w[e];
+            mat[(size_t)v[e] * n + u[e]] += w[e];
+        }
+        uint64_t r = orc_ks_dense(n, mat, seed, 0, trial);
+        free(mat);
+        return r;
+    }
+    uint64_t *w64 = widen(m, w);
+    uint64_t r = sparse_root(n, m, u, v, w64, seed, trial);
+    free(w64);
     return r;
 }
 

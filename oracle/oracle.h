@@ -88,6 +88,10 @@ uint64_t orc_mincut_trial(uint32_t n, uint64_t m, const uint32_t *u, const uint3
                           uint32_t seed, uint32_t rank, uint32_t trial);
 /* Only the Karger-Stein part (Stage 3) on a dense matrix, for kernel-level parity. */
 uint64_t orc_ks_dense(uint32_t n, const uint64_t *mat, uint32_t seed, uint32_t rank, uint32_t trial);
+/* one plain Karger-Stein trial (dense or sparse root) and the dense-node limit of both */
+uint64_t orc_ks_trial(uint32_t n, uint64_t m, const uint32_t *u, const uint32_t *v, const uint32_t *w, uint32_t seed,
+                      uint32_t trial);
+void orc_set_dense_limit(uint32_t n);
 /* Only Stage 1+2: contract to t vertices and emit the dense t' x t' matrix (returns t';
  * `mat_out` must hold n*n entries or NULL to only return t'). */
 uint32_t orc_shrink_to_dense(uint32_t n, uint64_t m, const uint32_t *u, const uint32_t *v, const uint32_t *w,

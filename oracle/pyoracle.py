@@ -42,6 +42,11 @@ def lib():
         L.orc_stoer_wagner_dense.restype = ctypes.c_uint64
         L.orc_exact_mincut.argtypes = [ctypes.c_uint32, ctypes.c_uint64, _u32p, _u32p, _u32p]
         L.orc_exact_mincut.restype = ctypes.c_uint64
+        L.orc_ks_trial.argtypes = [ctypes.c_uint32, ctypes.c_uint64, _u32p, _u32p, _u32p, ctypes.c_uint32,
+                                   ctypes.c_uint32]
+        L.orc_ks_trial.restype = ctypes.c_uint64
+        L.orc_set_dense_limit.argtypes = [ctypes.c_uint32]
+        L.orc_set_dense_limit.restype = None
         L.orc_exact_mincut_noi.argtypes = [ctypes.c_uint32, ctypes.c_uint64, _u32p, _u32p, _u32p]
         L.orc_exact_mincut_noi.restype = ctypes.c_uint64
         L.orc_intermediate_size.argtypes = [ctypes.c_uint32, ctypes.c_uint64]
@@ -182,15 +187,32 @@ def ks_number_of_trials(n, p):
     return trials
 
 
-def karger_stein(n, u, v, w, p, seed):
+def set_dense_limit(n):
+    """The vertex count above which Karger-Stein nodes stay edge lists (default 16384)."""
+    lib().orc_set_dense_limit(n)
+
+
+def ks_trial(n, u, v, w, seed, trial):
+    u, v, w = _c32(u), _c32(v), _c32(w)
+    return int(lib().orc_ks_trial(n, len(u), _p32(u), _p32(v), _p32(w), seed, trial))
+
+
+def karger_stein(n, u, v, w, p, seed, threads=1):
     """Plain Karger-Stein on the whole graph (src/executables/karger_stein.cpp:34): trial i recurses
-    from the full n x n matrix with the counter-addressed draws of (seed, rank 0, trial i); the
-    answer is the minimum over ks_number_of_trials(n, p) trials. Returns (cut, trials)."""
-    k, mat = shrink_to_dense(n, u, v, w, n, seed, 0, 0)
+    from the root with the counter-addressed draws of (seed, rank 0, trial i) -- the dense n x n
+    matrix, or the edge list when the graph is sparse (n above the dense limit, or fewer than
+    n^2 / 32 edges above 128 vertices); the answer is the minimum over ks_number_of_trials(n, p)
+    trials. Returns (cut, trials)."""
     trials = ks_number_of_trials(n, p)
-    if k < 2:
+    if n < 2:
         return 0, trials
-    return min(ks_dense(mat, seed, 0, i) for i in range(trials)), trials
+    if threads > 1:
+        import concurrent.futures as cf
+        with cf.ThreadPoolExecutor(max_workers=threads) as ex:
+            vals = list(ex.map(lambda i: ks_trial(n, u, v, w, seed, i), range(trials)))
+    else:
+        vals = [ks_trial(n, u, v, w, seed, i) for i in range(trials)]
+    return min(vals), trials
 
 
 def ks_target(n):

@@ -219,11 +219,13 @@ def test_karger_stein_probabilities_and_edges(ctx, libcac):
         ctx.graph(1, np.zeros(0, np.uint32), np.zeros(0, np.uint32)).karger_stein(0.9, 0)
 
 
-def test_karger_stein_rejects_graphs_above_the_dense_limit(ctx, libcac):
+def test_karger_stein_above_the_dense_limit_runs_sparse(ctx):
+    # 20,000 vertices: the root and the first levels are edge lists (the reference's sparse
+    # recursion), later levels dense; the answer is the exact cut
     n, u, v, w = _ring_plus_er(20000, 2, 24)
-    with pytest.raises(libcac.CacError) as e:
-        ctx.graph(n, u, v, w).karger_stein(0.9, 0)
-    assert e.value.status == -6
+    res = ctx.graph(n, u, v, w).karger_stein(0.9, 0)
+    assert res.total_trials == O.ks_number_of_trials(n, 0.9)
+    assert int(res.cut) == O.exact_mincut_noi(n, u, v, w)
 
 
 @pytest.mark.parametrize("big", [False, True])
