@@ -206,15 +206,21 @@ unsigned grid_of(cac_ctx *ctx, uint64_t work) {
 
 }  // namespace
 
+// Tile sums of scan_u32 over the larger of its two uses here: the digit histogram (256 words per
+// tile, 1/16 of a word per key) and the segment heads (one word per key).
+uint64_t scan_sum_words(uint64_t m) {
+    const uint64_t tiles = (m + kSTile - 1) / kSTile;
+    return std::max<uint64_t>(tiles, (kRadix * tiles + kSTile - 1) / kSTile) + 1;
+}
+
 uint64_t merge_edges_scratch(uint64_t m) {
     const uint64_t tiles = (m + kSTile - 1) / kSTile;
     return 4 * align_up(8 * std::max<uint64_t>(m, 1)) + align_up(4 * kRadix * std::max<uint64_t>(tiles, 1)) +
-           align_up(4 * std::max<uint64_t>(m, 1)) + 2 * align_up(4 * ((kRadix * tiles + kSTile - 1) / kSTile + 1)) +
-           align_up(16);
+           align_up(4 * std::max<uint64_t>(m, 1)) + align_up(4 * scan_sum_words(m)) + align_up(16);
 }
 
-// Exclusive scan of n u32 values in place (tile sums in `sums`, which holds >= ceil(n / 4096)
-// words); *total (device, nullable) receives the sum.
+// Exclusive scan of n u32 values in place (tile sums in `sums`, which must hold at least
+// ceil(n / 4096) words); *total (device, nullable) receives the sum.
 int scan_u32(cac_ctx *ctx, uint32_t *x, uint64_t n, uint32_t *sums, uint32_t *total) {
     cudaStream_t s = ctx->stream;
     const uint64_t nt = (n + kSTile - 1) / kSTile;
@@ -257,8 +263,7 @@ int merge_edges(cac_ctx *ctx, const uint32_t *a, const uint32_t *b, const WT *w,
     uint32_t *hist = reinterpret_cast<uint32_t *>(take(4 * kRadix * tiles));
     uint32_t *slot = reinterpret_cast<uint32_t *>(take(4 * m));
     const uint64_t hn = kRadix * tiles;
-    uint32_t *sums = reinterpret_cast<uint32_t *>(take(4 * ((hn + kSTile - 1) / kSTile + 1)));
-    (void)take(4 * ((hn + kSTile - 1) / kSTile + 1));
+    uint32_t *sums = reinterpret_cast<uint32_t *>(take(4 * scan_sum_words(m)));
     edge_keys<WT><<<grid_of(ctx, m), 256, 0, s>>>(a, b, w, m, lab, k, k0, v0);
     const uint64_t loop_key = (uint64_t)k * k;
     int bits = 1;
