@@ -316,6 +316,53 @@ def run_ks(args, rank, world):
     return 0
 
 
+def run_ks_sparse(args, rank, world):
+    """--workload ks-ws32k: plain Karger-Stein (the karger_stein executable, p = 0.9) on a Watts-
+    Strogatz graph with 32,000 vertices and 512,000 edges (k = 32, rewiring 0.4, weights in
+    [1, 100]): the shape of the reference's published sequential karger_stein baseline on ws_32k_16
+    (59.6 s median on one core, evaluation/data/e1/baselines.csv:2-3). The root and the upper
+    levels are edge lists (sparse recursion), the lower levels dense matrices. The answer is
+    checked against the oracle's exact cut outside the timed region."""
+    import torch
+    import cac
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import pyoracle
+    dev = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(dev)
+    stream = torch.cuda.Stream(device=dev)
+    ctx = cac.Context(dev, stream=stream.cuda_stream)
+    g = ctx.generate("watts_strogatz", seed=1, n=32000, k=32, p=0.4, wmin=1, wmax=100)
+    for _ in range(args.warmup):
+        res = g.karger_stein(0.9, seed=0)
+    wall = []
+    with Clocks(dev) as clk:
+        for i in range(args.steps):
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            res = g.karger_stein(0.9, seed=i)
+            wall.append(time.perf_counter() - t0)
+    total_s = _max_over_ranks(sum(wall), world)
+    u, v, w = g.edges()
+    exact = pyoracle.exact_mincut_noi(g.n, u, v, w)
+    line = {"metric": "Karger-Stein trials/s (karger_stein, Watts-Strogatz n=32000 m=512000)",
+            "value": world * res.total_trials * args.steps / total_s, "unit": "trials/s", "n_gpus": world,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": total_s / args.steps * 1e3,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "u64",
+            "data": "synthetic (device-generated Watts-Strogatz, k = 32, rewiring 0.4, w in [1, 100])",
+            "config": {"workload": "karger_stein ws_32k_16 shape", "vertices": g.n, "edges": g.m,
+                       "success_probability": 0.9, "trials_per_query": res.total_trials,
+                       "timing": "host wall clock per query"},
+            "cut": int(res.cut), "exact_cut": exact, "cut_exact": int(res.cut) == exact,
+            "published_reference": {"seconds_per_query": 59.6, "hardware": "Piz Daint XC50, 1 core",
+                                    "source": "evaluation/data/e1/baselines.csv:2-3 (ws_32k_16, p = 0.90)"},
+            "clocks": clk.summary()}
+    if rank == 0:
+        print(json.dumps(line))
+    g.free()
+    ctx.close()
+    return 0 if line["cut_exact"] else 1
+
+
 def run_approx(args, rank, world):
     """--workload approx: approx_cut (success probability 0.9, 4 copies) on G(n = 10^6, M = 10^7)
     with unit weights, generated on the device; value = edges per second of the seed-replay mode
@@ -799,7 +846,7 @@ def main():
     ap.add_argument("--no-ks", action="store_true", help="skip the square_root (Karger-Stein) measurements")
     ap.add_argument("--no-rmat", action="store_true", help="skip the R-MAT scale 22 CC measurement")
     ap.add_argument("--workload", default="cc",
-                    choices=["cc", "cc-rmat22", "ks-er1000", "ks-k4000", "ks-batch", "serve", "approx"],
+                    choices=["cc", "cc-rmat22", "ks-er1000", "ks-k4000", "ks-ws32k", "ks-batch", "serve", "approx"],
                     help="cc: the benchmark line; the others: one workload's line")
     ap.add_argument("--graphs", type=int, default=4096, help="ks-batch: graphs in the batch")
     ap.add_argument("--queries", type=int, default=200, help="serve: queries in the trace")
@@ -808,7 +855,7 @@ def main():
     ap.add_argument("--no-serve", action="store_true", help="skip the served-stream measurement")
     args = ap.parse_args()
     if args.steps is None:
-        args.steps = {"cc": 20, "cc-rmat22": 20, "ks-batch": 3}.get(args.workload, 10)
+        args.steps = {"cc": 20, "cc-rmat22": 20, "ks-batch": 3, "ks-ws32k": 3}.get(args.workload, 10)
     if args.warmup is None:
         args.warmup = 5 if args.workload == "cc" else 3
     rank = int(os.environ.get("RANK", "0"))
@@ -824,6 +871,8 @@ def main():
             return run_ks(args, rank, world)
         if args.workload == "ks-batch":
             return run_batch(args, rank, world)
+        if args.workload == "ks-ws32k":
+            return run_ks_sparse(args, rank, world)
         if args.workload == "serve":
             return run_serve(args, rank, world)
         if args.workload == "approx":
