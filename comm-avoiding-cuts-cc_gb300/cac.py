@@ -178,7 +178,7 @@ class Context:
         self._graphs = weakref.WeakSet()
 
     def set_dense_limit(self, max_dense_vertices):
-        """Karger-Stein nodes above this many vertices (or sparse ones above 128) stay edge lists."""
+        """Karger-Stein nodes above this many vertices (or sparse ones above 2048) stay edge lists."""
         _check(lib().cac_ctx_set_dense_limit(self.h, max_dense_vertices), "cac_ctx_set_dense_limit")
 
     def close(self):

@@ -237,10 +237,13 @@ struct SparseNode {
     uint32_t query;
     MatBuf *buf;              // owner of a, b, w (null: the input graph)
 };
-// Dense or sparse: the rule shared with the oracle (above the limit, or above 128 vertices with
-// fewer than N^2 / 32 edges: an edge list).
+// Dense or sparse: the rule shared with the oracle (above the limit, or above kSmallDense vertices
+// with fewer than N^2 / 32 edges: an edge list). Small nodes are dense whatever their density: the
+// dense engine steps thousands of them in one launch per kernel, where edge lists would cost a
+// contraction, a sort and a merge per level.
+constexpr uint32_t kSmallDense = 2048;
 inline bool ks_is_dense(const cac_ctx *ctx, uint32_t N, uint64_t m) {
-    return N <= ctx->dense_limit && (N <= 128 || 32 * m >= (uint64_t)N * N);
+    return N <= ctx->dense_limit && (N <= kSmallDense || 32 * m >= (uint64_t)N * N);
 }
 // Runs every sparse level of the given nodes (each holding one reference on its buffer): children
 // contracted by the Stage 1 rounds, relabelled, sorted and merged on the device; children that
@@ -287,6 +290,19 @@ template <typename WT>
 int merge_edges(cac_ctx *ctx, const uint32_t *a, const uint32_t *b, const WT *w, uint64_t m, const uint32_t *lab,
                 uint32_t k, uint32_t *oa, uint32_t *ob, uint64_t *ow, uint32_t *d_count, void *scratch);
 int scan_u32(cac_ctx *ctx, uint32_t *x, uint64_t n, uint32_t *sums, uint32_t *total);
+// One child of merge_edges_multi: its parent's edges and the labels of its contraction.
+struct MergeTask {
+    const uint32_t *a, *b;  // parent edge ends (device)
+    const void *w;          // parent weights: u64 when w64, else u32
+    uint32_t w64;
+    uint32_t k;             // child vertices
+    uint64_t m;             // parent edges
+    const uint32_t *lab;    // parent vertex -> child label (null: identity)
+    uint64_t in_off, key_off;  // filled in by merge_edges_multi
+};
+int merge_edges_multi(cac_ctx *ctx, std::vector<MergeTask> &tasks, uint32_t *oa, uint32_t *ob, uint64_t *ow,
+                      uint32_t *counts, void *scratch);
+uint64_t merge_edges_multi_scratch(uint64_t M, uint32_t B);
 int shrink_big(cac_ctx *ctx, const cac_graph *g, uint32_t target, uint32_t B, const uint32_t *k0, const uint32_t *idx,
                uint32_t *d_lab, uint32_t *d_kout, void *scratch);
 // Quotient kernel choices of the autotuner (cac_ctx::quotient_choice), bucketed by

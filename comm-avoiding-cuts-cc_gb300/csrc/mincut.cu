@@ -1444,14 +1444,24 @@ int admit(cac_ctx *ctx, KsEngine &eng, const QueryPlan &q) {
     const uint32_t small = g->total_weight < (1ull << 32) ? 1u : 0u;
     if (q.trials == 0) return CAC_OK;
     if (q.t >= n && !ks_is_dense(ctx, n, m)) {
-        // no pre-contraction and a sparse graph: every trial starts from the input edge list
-        std::vector<SparseNode> roots;
-        for (uint64_t i = 0; i < q.trials; i++) {
-            const uint32_t r = (uint32_t)(i / q.per_rank), idx = (uint32_t)(i % q.per_rank);
-            roots.push_back(SparseNode{q.cuts + i, q.seed + r, idx, 1, n, m, g->u, g->v, g->w, false, true, small,
-                                       q.query, nullptr});
+        // No pre-contraction and a sparse graph: every trial starts from the input edge list. The
+        // dense levels below the sparse ones hold about n^2 entries per level and trial, so the
+        // trials run in groups that keep two such levels within the bound, each group to its end.
+        const uint64_t per_trial = 2ull * n * n * (small ? 4 : 8);
+        const uint64_t bound = ctx->budget ? ctx->budget / 2 : (32ull << 30);
+        const uint64_t group = std::max<uint64_t>(1, std::min<uint64_t>(q.trials, bound / per_trial));
+        for (uint64_t g0 = 0; g0 < q.trials; g0 += group) {
+            std::vector<SparseNode> roots;
+            for (uint64_t i = g0; i < std::min(q.trials, g0 + group); i++) {
+                const uint32_t r = (uint32_t)(i / q.per_rank), idx = (uint32_t)(i % q.per_rank);
+                roots.push_back(SparseNode{q.cuts + i, q.seed + r, idx, 1, n, m, g->u, g->v, g->w, false, true, small,
+                                           q.query, nullptr});
+            }
+            CAC_TRY(sparse_phase(ctx, eng, std::move(roots)));
+            if (g0 + group < q.trials)
+                while (!eng.idle()) CAC_TRY(eng.step());
         }
-        return sparse_phase(ctx, eng, std::move(roots));
+        return CAC_OK;
     }
     if (q.t >= n) {
         // no pre-contraction: every trial starts from the same dense matrix, built once

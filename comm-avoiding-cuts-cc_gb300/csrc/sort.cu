@@ -200,6 +200,49 @@ __global__ void seg_merge(const uint64_t *keys, const uint64_t *vals, uint64_t n
     }
 }
 
+// Many children at once: task y writes its edges' keys at in_off, offset by key_off (the sum of the
+// earlier tasks' k^2), so one sort orders every task's pairs after the previous task's; loops of
+// every task get the one key `loop_key` (= the sum of all k^2), which sorts last.
+__global__ void edge_keys_multi(const MergeTask *__restrict__ tasks, uint64_t loop_key, uint64_t *keys,
+                                uint64_t *vals) {
+    const MergeTask t = tasks[blockIdx.y];
+    for (uint64_t e = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; e < t.m; e += (uint64_t)gridDim.x * blockDim.x) {
+        uint32_t x = t.a[e], y = t.b[e];
+        if (t.lab) {
+            x = t.lab[x];
+            y = t.lab[y];
+        }
+        const uint32_t lo = min(x, y), hi = max(x, y);
+        keys[t.in_off + e] = lo == hi ? loop_key : t.key_off + (uint64_t)lo * t.k + hi;
+        vals[t.in_off + e] = t.w64 ? static_cast<const uint64_t *>(t.w)[e] : (uint64_t) static_cast<const uint32_t *>(t.w)[e];
+    }
+}
+
+// The merge of many tasks: as seg_merge, with each head's task found by a binary search over the
+// tasks' key ranges; the head also counts into its task.
+__global__ void seg_merge_multi(const uint64_t *keys, const uint64_t *vals, uint64_t n, uint64_t loop_key,
+                                const MergeTask *__restrict__ tasks, uint32_t ntasks, const uint32_t *slot, uint32_t *oa,
+                                uint32_t *ob, unsigned long long *ow, uint32_t *counts) {
+    for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (uint64_t)gridDim.x * blockDim.x) {
+        const uint64_t key = keys[i];
+        if (key == loop_key) continue;
+        const bool head = i == 0 || keys[i - 1] != key;
+        const uint32_t s = head ? slot[i] : slot[i] - 1;
+        if (head) {
+            uint32_t lo = 0, hi = ntasks - 1;  // last task whose key range starts at or below key
+            while (lo < hi) {
+                const uint32_t mid = (lo + hi + 1) >> 1;
+                if (tasks[mid].key_off <= key) lo = mid; else hi = mid - 1;
+            }
+            const uint64_t r = key - tasks[lo].key_off;
+            oa[s] = (uint32_t)(r / tasks[lo].k);
+            ob[s] = (uint32_t)(r % tasks[lo].k);
+            atomicAdd(counts + lo, 1u);
+        }
+        atomicAdd(ow + s, (unsigned long long)vals[i]);
+    }
+}
+
 unsigned grid_of(cac_ctx *ctx, uint64_t work) {
     return (unsigned)std::max<uint64_t>(1, std::min<uint64_t>((work + 255) / 256, (uint64_t)ctx->num_sms * 8));
 }
@@ -282,6 +325,74 @@ int merge_edges(cac_ctx *ctx, const uint32_t *a, const uint32_t *b, const WT *w,
                                               reinterpret_cast<unsigned long long *>(ow));
     CAC_CUDA_TRY(cudaGetLastError());
     return CAC_OK;
+}
+
+// The children of many tasks in one sort (see MergeTask): every task's merged pairs, task after
+// task, each task's in sorted (smaller, larger end) order; counts[t] (device, zeroed here) gets task
+// t's number of pairs, so task t's pairs start at the sum of the earlier counts. oa/ob/ow have room
+// for the sum of the tasks' m. The tasks' in_off and key_off are filled in here.
+int merge_edges_multi(cac_ctx *ctx, std::vector<MergeTask> &tasks, uint32_t *oa, uint32_t *ob, uint64_t *ow,
+                      uint32_t *counts, void *scratch) {
+    cudaStream_t s = ctx->stream;
+    const uint32_t B = (uint32_t)tasks.size();
+    if (B == 0) return CAC_OK;
+    if (B > 65535) {
+        set_error("merge_edges_multi: more than 65535 tasks in one call");
+        return CAC_ERR_INVALID;
+    }
+    uint64_t M = 0, key_space = 0, mmax = 0;
+    for (MergeTask &t : tasks) {
+        t.in_off = M;
+        t.key_off = key_space;
+        M += t.m;
+        key_space += (uint64_t)t.k * t.k;
+        mmax = std::max(mmax, t.m);
+    }
+    CAC_CUDA_TRY(cudaMemsetAsync(counts, 0, 4ull * B, s));
+    if (M == 0) return CAC_OK;
+    const uint64_t tiles = (M + kSTile - 1) / kSTile;
+    if (tiles * kRadix > 0xFFFFFFFFull || M > 0xFFFFFFFFull || key_space >= (1ull << 62)) {
+        set_error("merge_edges_multi: too many edges for 32-bit offsets");
+        return CAC_ERR_UNSUPPORTED;
+    }
+    char *p = static_cast<char *>(scratch);
+    auto take = [&](size_t bytes) {
+        char *q = p;
+        p += align_up(bytes);
+        return q;
+    };
+    uint64_t *k0 = reinterpret_cast<uint64_t *>(take(8 * M)), *v0 = reinterpret_cast<uint64_t *>(take(8 * M));
+    uint64_t *k1 = reinterpret_cast<uint64_t *>(take(8 * M)), *v1 = reinterpret_cast<uint64_t *>(take(8 * M));
+    uint32_t *hist = reinterpret_cast<uint32_t *>(take(4 * kRadix * tiles));
+    uint32_t *slot = reinterpret_cast<uint32_t *>(take(4 * M));
+    uint32_t *sums = reinterpret_cast<uint32_t *>(take(4 * scan_sum_words(M)));
+    uint32_t *total = reinterpret_cast<uint32_t *>(take(16));
+    MergeTask *dt = reinterpret_cast<MergeTask *>(take(sizeof(MergeTask) * B));
+    CAC_CUDA_TRY(cudaMemcpyAsync(dt, tasks.data(), sizeof(MergeTask) * B, cudaMemcpyHostToDevice, s));
+    const uint64_t hn = kRadix * tiles;
+    const unsigned gx = (unsigned)std::max<uint64_t>(
+        1, std::min<uint64_t>((mmax + 255) / 256, std::max<uint64_t>(1, (uint64_t)ctx->num_sms * 8 / B)));
+    edge_keys_multi<<<dim3(gx, B), 256, 0, s>>>(dt, key_space, k0, v0);
+    int bits = 1;
+    while (bits < 64 && (key_space >> bits) != 0) bits++;
+    for (int shift = 0; shift < bits; shift += 8) {
+        radix_hist<<<(unsigned)tiles, kST, 0, s>>>(k0, M, shift, hist, (uint32_t)tiles);
+        CAC_TRY(scan_u32(ctx, hist, hn, sums, nullptr));
+        radix_scatter<<<(unsigned)tiles, kST, 0, s>>>(k0, v0, M, shift, hist, (uint32_t)tiles, k1, v1);
+        std::swap(k0, k1);
+        std::swap(v0, v1);
+    }
+    seg_heads<<<grid_of(ctx, M), 256, 0, s>>>(k0, M, key_space, slot);
+    CAC_TRY(scan_u32(ctx, slot, M, sums, total));
+    CAC_CUDA_TRY(cudaMemsetAsync(ow, 0, 8 * M, s));
+    seg_merge_multi<<<grid_of(ctx, M), 256, 0, s>>>(k0, v0, M, key_space, dt, B, slot, oa, ob,
+                                                    reinterpret_cast<unsigned long long *>(ow), counts);
+    CAC_CUDA_TRY(cudaGetLastError());
+    return CAC_OK;
+}
+
+uint64_t merge_edges_multi_scratch(uint64_t M, uint32_t B) {
+    return merge_edges_scratch(M) + align_up(16) + align_up(sizeof(MergeTask) * std::max<uint32_t>(B, 1));
 }
 
 template int merge_edges<uint32_t>(cac_ctx *, const uint32_t *, const uint32_t *, const uint32_t *, uint64_t,

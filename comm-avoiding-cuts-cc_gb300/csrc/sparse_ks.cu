@@ -26,6 +26,14 @@
 namespace cac {
 namespace {
 
+// One dense child of a chunk: its merged pairs (slices of the chunk's list buffer) and its matrix.
+struct DenseFromPairs {
+    const uint32_t *a, *b;
+    const uint64_t *w;
+    uint64_t m, ld;
+    void *mat;
+};
+
 template <typename WT>
 __global__ void sparse_degree(const uint32_t *a, const uint32_t *b, const WT *w, uint64_t m, unsigned long long *deg) {
     for (uint64_t e = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; e < m; e += (uint64_t)gridDim.x * blockDim.x) {
@@ -50,15 +58,42 @@ __global__ void cuts_min(unsigned long long *const *cuts, uint32_t count, const 
         atomicMin(cuts[i], value ? *value : 0ull);
 }
 
-// The dense matrix of a merged edge list (each pair once): both directions stored.
+// The dense matrix of a merged edge list (each pair once): both directions stored; CTA row y of
+// the grid serves child y.
 template <typename Tm>
-__global__ void dense_from_pairs(const uint32_t *a, const uint32_t *b, const uint64_t *w, uint64_t m, uint64_t ld,
-                                 Tm *mat) {
-    for (uint64_t e = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; e < m; e += (uint64_t)gridDim.x * blockDim.x) {
-        const uint64_t x = a[e], y = b[e];
-        mat[x * ld + y] = (Tm)w[e];
-        mat[y * ld + x] = (Tm)w[e];
+__global__ void dense_from_pairs(const DenseFromPairs *__restrict__ d) {
+    const DenseFromPairs c = d[blockIdx.y];
+    Tm *mat = static_cast<Tm *>(c.mat);
+    for (uint64_t e = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; e < c.m; e += (uint64_t)gridDim.x * blockDim.x) {
+        const uint64_t x = c.a[e], y = c.b[e];
+        mat[x * c.ld + y] = (Tm)c.w[e];
+        mat[y * c.ld + x] = (Tm)c.w[e];
     }
+}
+
+// The dense children of a chunk, one launch per entry width (descs: room for both lists).
+int dense_children(cac_ctx *ctx, const std::vector<DenseFromPairs> &d32, const std::vector<DenseFromPairs> &d64,
+                   DenseFromPairs *descs) {
+    cudaStream_t s = ctx->stream;
+    const std::vector<DenseFromPairs> *lists[2] = {&d32, &d64};
+    DenseFromPairs *at = descs;
+    for (int wi = 0; wi < 2; wi++) {
+        const std::vector<DenseFromPairs> &v = *lists[wi];
+        for (size_t i0 = 0; i0 < v.size(); i0 += 65535) {
+            const size_t n = std::min<size_t>(65535, v.size() - i0);
+            uint64_t mmax = 1;
+            for (size_t i = i0; i < i0 + n; i++) mmax = std::max(mmax, v[i].m);
+            CAC_CUDA_TRY(cudaMemcpyAsync(at, v.data() + i0, sizeof(DenseFromPairs) * n, cudaMemcpyHostToDevice, s));
+            const dim3 grid((unsigned)std::max<uint64_t>(
+                                1, std::min<uint64_t>((mmax + 255) / 256, std::max<uint64_t>(1, (uint64_t)ctx->num_sms * 8 / n))),
+                            (unsigned)n);
+            if (wi == 0) dense_from_pairs<uint32_t><<<grid, 256, 0, s>>>(at);
+            else dense_from_pairs<uint64_t><<<grid, 256, 0, s>>>(at);
+            CAC_CUDA_TRY(cudaGetLastError());
+            at += n;
+        }
+    }
+    return CAC_OK;
 }
 
 unsigned grid_of(cac_ctx *ctx, uint64_t work) {
@@ -143,6 +178,9 @@ int sparse_phase(cac_ctx *ctx, KsEngine &eng, std::vector<SparseNode> nodes) {
             if (nd.buf) eng.release(nd.buf);
         v.clear();
     };
+    // a chunk of children: contraction scratch within 4 GB and at most kChunkEdges parent edges (the
+    // sort of one chunk takes 40 bytes per parent edge, its merged lists 16)
+    constexpr uint64_t kChunkEdges = 64ull << 20;
     while (!nodes.empty()) {
         st = root_bounds(ctx, nodes);
         // the children of every node with edges: two contraction tasks each
@@ -165,24 +203,24 @@ int sparse_phase(cac_ctx *ctx, KsEngine &eng, std::vector<SparseNode> nodes) {
         std::vector<SparseNode> next;
         size_t c0 = 0;
         while (st == CAC_OK && c0 < children.size()) {
-            // a chunk of tasks whose contraction scratch and labels stay within 4 GB
             size_t c1 = c0;
-            uint64_t bytes = 0, labw = 0, mmax = 1;
-            std::vector<ShrinkTask> tasks;
+            uint64_t bytes = 0, labw = 0, M = 0;
             while (c1 < children.size() && c1 - c0 < 65535) {
                 const SparseNode &nd = *children[c1].src;
                 const uint64_t b = shrink_task_scratch(nd.N, nd.m) + align_up(4ull * nd.N);
-                if (c1 > c0 && bytes + b > (4ull << 30)) break;
+                if (c1 > c0 && (bytes + b > (4ull << 30) || M + nd.m > kChunkEdges)) break;
                 bytes += b;
                 labw += nd.N;
-                mmax = std::max<uint64_t>(mmax, nd.m);
+                M += nd.m;
                 c1++;
             }
             const uint32_t B = (uint32_t)(c1 - c0);
             Temp lab(ctx), kout(ctx), scr(ctx), merge_scr(ctx), counts(ctx);
             if ((st = lab.get(labw * 4)) != CAC_OK || (st = kout.get(B * 4)) != CAC_OK ||
-                (st = counts.get(B * 4)) != CAC_OK || (st = merge_scr.get(merge_edges_scratch(mmax))) != CAC_OK)
+                (st = counts.get(B * 4)) != CAC_OK || (st = merge_scr.get(merge_edges_multi_scratch(M, B))) != CAC_OK)
                 break;
+            // 1. contract every child's copy of its parent (Stage 1 rounds, all tasks together)
+            std::vector<ShrinkTask> tasks;
             uint64_t lo = 0;
             for (size_t i = c0; i < c1; i++) {
                 const SparseNode &nd = *children[i].src;
@@ -200,75 +238,79 @@ int sparse_phase(cac_ctx *ctx, KsEngine &eng, std::vector<SparseNode> nodes) {
                 st = CAC_ERR_CUDA;
                 break;
             }
-            // relabel, sort and merge every child's edges into a list of its own
-            std::vector<MatBuf *> lists(B, nullptr);
+            // 2. relabel, sort and merge every child's edges in one sort; the lists share one buffer
+            std::vector<MergeTask> mt(B);
             lo = 0;
-            for (uint32_t b = 0; b < B && st == CAC_OK; b++) {
+            for (uint32_t b = 0; b < B; b++) {
                 const SparseNode &nd = *children[c0 + b].src;
-                const uint64_t cap = std::max<uint64_t>(nd.m, 1);
-                if ((st = eng.alloc(align_up(cap * 4) * 2 + align_up(cap * 8), &lists[b])) != CAC_OK) break;
-                char *p = static_cast<char *>(lists[b]->p);
-                uint32_t *oa = reinterpret_cast<uint32_t *>(p), *ob = reinterpret_cast<uint32_t *>(p + align_up(cap * 4));
-                uint64_t *ow = reinterpret_cast<uint64_t *>(p + 2 * align_up(cap * 4));
-                const uint32_t *lb = lab.as<uint32_t>() + lo;
+                mt[b] = MergeTask{nd.a, nd.b, nd.w, nd.w64 ? 1u : 0u, kk[b], nd.m, lab.as<uint32_t>() + lo, 0, 0};
                 lo += nd.N;
-                st = nd.w64 ? merge_edges<uint64_t>(ctx, nd.a, nd.b, static_cast<const uint64_t *>(nd.w), nd.m, lb,
-                                                    kk[b], oa, ob, ow, counts.as<uint32_t>() + b, merge_scr.p)
-                            : merge_edges<uint32_t>(ctx, nd.a, nd.b, static_cast<const uint32_t *>(nd.w), nd.m, lb,
-                                                    kk[b], oa, ob, ow, counts.as<uint32_t>() + b, merge_scr.p);
             }
+            const uint64_t cap = std::max<uint64_t>(M, 1);
+            MatBuf *lists = nullptr;
+            if ((st = eng.alloc(align_up(cap * 4) * 2 + align_up(cap * 8), &lists)) != CAC_OK) break;
+            lists->refs++;  // this scope's reference
+            char *p = static_cast<char *>(lists->p);
+            uint32_t *oa = reinterpret_cast<uint32_t *>(p), *ob = reinterpret_cast<uint32_t *>(p + align_up(cap * 4));
+            uint64_t *ow = reinterpret_cast<uint64_t *>(p + 2 * align_up(cap * 4));
+            st = merge_edges_multi(ctx, mt, oa, ob, ow, counts.as<uint32_t>(), merge_scr.p);
             if (st == CAC_OK && (cudaMemcpyAsync(mm.data(), counts.p, B * 4, cudaMemcpyDeviceToHost, s) != cudaSuccess ||
                                  cudaStreamSynchronize(s) != cudaSuccess)) {
                 set_error("sparse Karger-Stein: reading the merged edge counts failed");
                 st = CAC_ERR_CUDA;
             }
-            for (uint32_t b = 0; b < B; b++) {
-                MatBuf *list = lists[b];
-                if (!list) continue;
-                list->refs++;  // held here until the child is placed
-                if (st != CAC_OK) {
-                    eng.release(list);
-                    continue;
-                }
+            // 3. place every child: cut 0 without edges, a dense matrix, or the next sparse level
+            std::vector<uint64_t> start(B + 1, 0);
+            for (uint32_t b = 0; b < B; b++) start[b + 1] = start[b] + mm[b];
+            std::vector<uint64_t *> zcut;
+            std::vector<DenseFromPairs> dense32, dense64;
+            uint64_t dense_bytes = 0;
+            std::vector<uint64_t> mat_off(B, 0);
+            for (uint32_t b = 0; b < B && st == CAC_OK; b++) {
                 const SparseNode &nd = *children[c0 + b].src;
                 const uint32_t k = kk[b];
-                const uint64_t cap = std::max<uint64_t>(nd.m, 1);
-                char *p = static_cast<char *>(list->p);
-                const uint32_t *oa = reinterpret_cast<const uint32_t *>(p);
-                const uint32_t *ob = reinterpret_cast<const uint32_t *>(p + align_up(cap * 4));
-                const uint64_t *ow = reinterpret_cast<const uint64_t *>(p + 2 * align_up(cap * 4));
                 if (mm[b] == 0 || k < 2) {
-                    zero.assign(1, nd.cut);
-                    st = zero_cuts(ctx, zero);
+                    zcut.push_back(nd.cut);
                 } else if (ks_is_dense(ctx, k, mm[b])) {
-                    MatBuf *mat = nullptr;
-                    const uint64_t ld = ld_of(k), es = nd.small ? 4 : 8;
-                    if ((st = eng.alloc(k * ld * es, &mat)) == CAC_OK) {
-                        if (cudaMemsetAsync(mat->p, 0, k * ld * es, s) != cudaSuccess) {
-                            set_error("sparse Karger-Stein: clearing a dense child failed");
-                            st = CAC_ERR_CUDA;
-                        } else if (nd.small) {
-                            dense_from_pairs<uint32_t><<<grid_of(ctx, mm[b]), 256, 0, s>>>(
-                                oa, ob, ow, mm[b], ld, static_cast<uint32_t *>(mat->p));
-                        } else {
-                            dense_from_pairs<uint64_t><<<grid_of(ctx, mm[b]), 256, 0, s>>>(
-                                oa, ob, ow, mm[b], ld, static_cast<uint64_t *>(mat->p));
-                        }
-                        if (st == CAC_OK) {
-                            eng.add(KNode{nd.cut, nd.k0, nd.idx, children[c0 + b].h, k, 0, nd.small, nd.query, mat->p,
-                                          mat});
-                        } else {
-                            mat->refs++;  // a reference to drop: frees the matrix
-                            eng.release(mat);
-                        }
-                    }
-                } else {
-                    list->refs++;  // the next level's node holds it
-                    next.push_back(SparseNode{nd.cut, nd.k0, nd.idx, children[c0 + b].h, k, mm[b], oa, ob, ow, true,
-                                              false, nd.small, nd.query, list});
+                    mat_off[b] = dense_bytes;
+                    dense_bytes += align_up(k * ld_of(k) * (nd.small ? 4 : 8));
                 }
-                eng.release(list);  // this scope's reference (the dense child's matrix is built)
             }
+            MatBuf *mats = nullptr;
+            if (st == CAC_OK && dense_bytes) {
+                st = eng.alloc(dense_bytes, &mats);
+                if (st == CAC_OK) {
+                    mats->refs++;  // this scope's reference
+                    if (cudaMemsetAsync(mats->p, 0, dense_bytes, s) != cudaSuccess) {
+                        set_error("sparse Karger-Stein: clearing the dense children failed");
+                        st = CAC_ERR_CUDA;
+                    }
+                }
+            }
+            if (st == CAC_OK) st = zero_cuts(ctx, zcut);
+            for (uint32_t b = 0; b < B && st == CAC_OK; b++) {
+                const SparseNode &nd = *children[c0 + b].src;
+                const uint32_t k = kk[b];
+                if (mm[b] == 0 || k < 2) continue;
+                const uint64_t first = start[b];
+                if (ks_is_dense(ctx, k, mm[b])) {
+                    unsigned char *mat = static_cast<unsigned char *>(mats->p) + mat_off[b];
+                    (nd.small ? dense32 : dense64)
+                        .push_back(DenseFromPairs{oa + first, ob + first, ow + first, mm[b], ld_of(k), mat});
+                    eng.add(KNode{nd.cut, nd.k0, nd.idx, children[c0 + b].h, k, 0, nd.small, nd.query, mat, mats});
+                } else {
+                    lists->refs++;  // the next level's node holds the shared list buffer
+                    next.push_back(SparseNode{nd.cut, nd.k0, nd.idx, children[c0 + b].h, k, mm[b], oa + first,
+                                              ob + first, ow + first, true, false, nd.small, nd.query, lists});
+                }
+            }
+            Temp descs(ctx);
+            if (st == CAC_OK && (!dense32.empty() || !dense64.empty())) {
+                st = descs.get(sizeof(DenseFromPairs) * (dense32.size() + dense64.size()));
+                if (st == CAC_OK) st = dense_children(ctx, dense32, dense64, descs.as<DenseFromPairs>());
+            }
+            if (mats) eng.release(mats);
+            eng.release(lists);
             if (st == CAC_OK) {
                 const cudaError_t e = cudaStreamSynchronize(s);  // temporaries go out of scope
                 if (e != cudaSuccess) {

@@ -75,7 +75,7 @@ typedef struct {
 /* ---- context ---- */
 int cac_ctx_create(const cac_config *config, cac_ctx **out);
 /* Karger-Stein recursion nodes with more vertices than this (default and maximum 16384, minimum
- * 128), or above 128 vertices with fewer than N^2 / 32 edges, are kept as edge lists (the
+ * 128), or above 2048 vertices with fewer than N^2 / 32 edges, are kept as edge lists (the
  * reference's sparse recursion, co_mincut.h:401-405); the others as dense matrices. It changes the
  * trials' draws, never the validity of a cut; a lower limit moves more of the recursion to the
  * sparse form. */
@@ -192,7 +192,7 @@ int cac_mincut_batch(cac_ctx *ctx, const cac_mincut_query *queries, uint32_t cou
  * comincut::minimum_cut (src/executables/karger_stein.cpp, co_mincut.h:515-521): the Karger-Stein
  * library's own trial count for n vertices (comincut::number_of_trials, co_mincut.cpp:44-73), each
  * trial a recursion from the whole graph (no sqrt(m) pre-contraction): its dense matrix, or its edge
- * list when the graph is sparse (above the dense limit, or fewer than n^2 / 32 edges above 128
+ * list when the graph is sparse (above the dense limit, or fewer than n^2 / 32 edges above 2048
  * vertices: the reference's switch, co_mincut.h:401-405); trial i draws from key
  * (seed, i, 1 + heap index).
  * res->trials_per_rank = res->total_trials = the trial count; res->intermediate = n. */

@@ -484,7 +484,7 @@ uint32_t orc_shrink_to_dense(uint32_t n, uint64_t m, const uint32_t *u, const ui
  * co_mincut.h:131-155 and 401-405, contracts a sparse node by exponential edge scores and a prefix
  * connected components; libcac contracts it by the same weighted rounds as Stage 1):
  *   - a node is kept as an edge list when it has more than the dense limit (16384 vertices, or
- *     the value set with orc_set_dense_limit) or, above 128 vertices, fewer than N^2 / 32 edges;
+ *     the value set with orc_set_dense_limit) or, above 2048 vertices, fewer than N^2 / 32 edges;
  *     otherwise it becomes the dense matrix of the dense recursion above;
  *   - the child with heap index c of a sparse node contracts the node's edge list to
  *     max(ceil(N / sqrt 2) + 1, 128) vertices by the Stage 1 rounds with key (k0, trial, 1 + c, 0)
@@ -503,7 +503,7 @@ typedef struct { uint32_t n; uint64_t m; uint32_t *a, *b; uint64_t *w; } sgraph;
 static void sg_free(sgraph *g) { free(g->a); free(g->b); free(g->w); }
 
 static int is_dense(uint32_t n, uint64_t m) {
-    return n <= g_dense_limit && (n <= 128 || 32 * m >= (uint64_t)n * n);
+    return n <= g_dense_limit && (n <= 2048 || 32 * m >= (uint64_t)n * n);
 }
 
 /* Stage 1 rounds on an edge list with u64 weights and key `key`: labels (rank of the smallest

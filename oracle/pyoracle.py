@@ -201,7 +201,7 @@ def karger_stein(n, u, v, w, p, seed, threads=1):
     """Plain Karger-Stein on the whole graph (src/executables/karger_stein.cpp:34): trial i recurses
     from the root with the counter-addressed draws of (seed, rank 0, trial i) -- the dense n x n
     matrix, or the edge list when the graph is sparse (n above the dense limit, or fewer than
-    n^2 / 32 edges above 128 vertices); the answer is the minimum over ks_number_of_trials(n, p)
+    n^2 / 32 edges above 2048 vertices); the answer is the minimum over ks_number_of_trials(n, p)
     trials. Returns (cut, trials)."""
     trials = ks_number_of_trials(n, p)
     if n < 2:

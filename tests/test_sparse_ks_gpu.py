@@ -1,6 +1,6 @@
 """Sparse Karger-Stein nodes (the reference's sparse recursion, co_mincut.h:131-155 and 401-405,
 with WeightedIteratedSparseSampling::reduce's sort and merge, .cpp:26-234): nodes above the dense
-limit, or above 128 vertices with fewer than N^2 / 32 edges, stay edge lists; their children are
+limit, or above 2048 vertices with fewer than N^2 / 32 edges, stay edge lists; their children are
 contracted by the Stage 1 rounds and relabelled, radix-sorted and merged on the device.
 
 Every trial value equals the oracle's replay of the same counter stream, with the dense limit
