@@ -19,7 +19,9 @@ reference. The metric is edges per second.
   cpu_baseline  the oracle's restatement of the reference's CC loop on the host with the same 16
                 virtual ranks, each on its own thread (the reference under mpiexec -n 16).
   also_*     the other configurations of the metric: CC on R-MAT scale 22, square_root
-             (Karger-Stein trials/s) on ER(1000, 0.05) and K4000, 512 graphs of the uneven
+             (Karger-Stein trials/s) on ER(1000, 0.05) and K4000, plain Karger-Stein on the
+             32,000-vertex Watts-Strogatz shape of the reference's published karger_stein
+             baseline (sparse recursion on top, dense below), 512 graphs of the uneven
              batched population (batched vs one call per graph, every cut checked against the
              exact cut), and a shortened served stream (queries/s, p50/p99).
 
@@ -316,49 +318,61 @@ def run_ks(args, rank, world):
     return 0
 
 
-def run_ks_sparse(args, rank, world):
-    """--workload ks-ws32k: plain Karger-Stein (the karger_stein executable, p = 0.9) on a Watts-
-    Strogatz graph with 32,000 vertices and 512,000 edges (k = 32, rewiring 0.4, weights in
-    [1, 100]): the shape of the reference's published sequential karger_stein baseline on ws_32k_16
-    (59.6 s median on one core, evaluation/data/e1/baselines.csv:2-3). The root and the upper
-    levels are edge lists (sparse recursion), the lower levels dense matrices. The answer is
-    checked against the oracle's exact cut outside the timed region."""
+def _ks_sparse_measure(ctx, steps, warmup):
+    """Plain Karger-Stein (the karger_stein executable, p = 0.9) on a Watts-Strogatz graph with
+    32,000 vertices and 512,000 edges (k = 32, rewiring 0.4, weights in [1, 100]): the shape of the
+    reference's published sequential karger_stein baseline on ws_32k_16 (59.6 s median on one
+    core, evaluation/data/e1/baselines.csv:2-3). The root and the upper levels are edge lists
+    (sparse recursion), the levels from 2048 vertices down dense matrices. The answer is checked
+    against the oracle's exact cut outside the timed region."""
     import torch
-    import cac
     sys.path.insert(0, os.path.join(ROOT, "oracle"))
     import pyoracle
+    g = ctx.generate("watts_strogatz", seed=1, n=32000, k=32, p=0.4, wmin=1, wmax=100)
+    for _ in range(warmup):
+        res = g.karger_stein(0.9, seed=0)
+    wall = []
+    for i in range(steps):
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        res = g.karger_stein(0.9, seed=i)
+        wall.append(time.perf_counter() - t0)
+    u, v, w = g.edges()
+    exact = pyoracle.exact_mincut_noi(g.n, u, v, w)
+    out = {"workload": "karger_stein, Watts-Strogatz n=32000 m=512000 (k = 32, rewiring 0.4, w in [1, 100]), p = 0.9",
+           "value": res.total_trials * steps / sum(wall), "unit": "trials/s", "ms_per_query": sum(wall) / steps * 1e3,
+           "steps": steps, "trials_per_query": res.total_trials, "timing": "host wall clock per query",
+           "cut": int(res.cut), "exact_cut": exact, "cut_exact": int(res.cut) == exact,
+           "published_reference": {"seconds_per_query": 59.6, "hardware": "Piz Daint XC50, 1 core",
+                                   "source": "evaluation/data/e1/baselines.csv:2-3 (ws_32k_16, p = 0.90)"},
+           "speedup_vs_published": 59.6 / (sum(wall) / steps)}
+    g.free()
+    return out
+
+
+def run_ks_sparse(args, rank, world):
+    """--workload ks-ws32k: _ks_sparse_measure as its own line."""
+    import torch
+    import cac
     dev = int(os.environ.get("LOCAL_RANK", "0"))
     torch.cuda.set_device(dev)
     stream = torch.cuda.Stream(device=dev)
     ctx = cac.Context(dev, stream=stream.cuda_stream)
-    g = ctx.generate("watts_strogatz", seed=1, n=32000, k=32, p=0.4, wmin=1, wmax=100)
-    for _ in range(args.warmup):
-        res = g.karger_stein(0.9, seed=0)
-    wall = []
     with Clocks(dev) as clk:
-        for i in range(args.steps):
-            torch.cuda.synchronize()
-            t0 = time.perf_counter()
-            res = g.karger_stein(0.9, seed=i)
-            wall.append(time.perf_counter() - t0)
-    total_s = _max_over_ranks(sum(wall), world)
-    u, v, w = g.edges()
-    exact = pyoracle.exact_mincut_noi(g.n, u, v, w)
+        r = _ks_sparse_measure(ctx, args.steps, args.warmup)
+    total_s = _max_over_ranks(r["ms_per_query"] * args.steps / 1e3, world)
     line = {"metric": "Karger-Stein trials/s (karger_stein, Watts-Strogatz n=32000 m=512000)",
-            "value": world * res.total_trials * args.steps / total_s, "unit": "trials/s", "n_gpus": world,
+            "value": world * r["trials_per_query"] * args.steps / total_s, "unit": "trials/s", "n_gpus": world,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": total_s / args.steps * 1e3,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "u64",
             "data": "synthetic (device-generated Watts-Strogatz, k = 32, rewiring 0.4, w in [1, 100])",
-            "config": {"workload": "karger_stein ws_32k_16 shape", "vertices": g.n, "edges": g.m,
-                       "success_probability": 0.9, "trials_per_query": res.total_trials,
+            "config": {"workload": "karger_stein ws_32k_16 shape", "vertices": 32000, "edges": 512000,
+                       "success_probability": 0.9, "trials_per_query": r["trials_per_query"],
                        "timing": "host wall clock per query"},
-            "cut": int(res.cut), "exact_cut": exact, "cut_exact": int(res.cut) == exact,
-            "published_reference": {"seconds_per_query": 59.6, "hardware": "Piz Daint XC50, 1 core",
-                                    "source": "evaluation/data/e1/baselines.csv:2-3 (ws_32k_16, p = 0.90)"},
             "clocks": clk.summary()}
+    line.update({k: r[k] for k in ("cut", "exact_cut", "cut_exact", "published_reference", "speedup_vs_published")})
     if rank == 0:
         print(json.dumps(line))
-    g.free()
     ctx.close()
     return 0 if line["cut_exact"] else 1
 
@@ -596,6 +610,7 @@ def run_cac(args, rank, world):
                                                      "phases_ms", "generate_s")}
     if not args.no_ks:
         line["also_ks"] = _ks_also(ctx)
+        line["also_ks_sparse"] = _ks_sparse_measure(ctx, 2, 1)
     g.free()
     if not args.no_batch:
         line["also_batch"] = _batch_measure(ctx, 512, 2, 1, check_exact=True)
