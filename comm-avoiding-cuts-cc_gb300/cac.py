@@ -93,6 +93,7 @@ EXPORTS = [
     ("cac_ctx_create", ctypes.c_int, [ctypes.POINTER(_Config), ctypes.POINTER(_vp)]),
     ("cac_ctx_destroy", ctypes.c_int, [_vp]),
     ("cac_ctx_set_dense_limit", ctypes.c_int, [_vp, ctypes.c_uint32]),
+    ("cac_ctx_set_quotient_kernel", ctypes.c_int, [_vp, ctypes.c_int]),
     ("cac_error_string", ctypes.c_char_p, [ctypes.c_int]),
     ("cac_last_error", ctypes.c_char_p, []),
     ("cac_ctx_device_bytes", ctypes.c_uint64, [_vp]),
@@ -180,6 +181,10 @@ class Context:
     def set_dense_limit(self, max_dense_vertices):
         """Karger-Stein nodes above this many vertices (or sparse ones above 2048) stay edge lists."""
         _check(lib().cac_ctx_set_dense_limit(self.h, max_dense_vertices), "cac_ctx_set_dense_limit")
+
+    def set_quotient_kernel(self, kind):
+        """0: autotuned; 1 warp per row; 2 eight warps per row; 3 warp per row with bulk-copy staging."""
+        _check(lib().cac_ctx_set_quotient_kernel(self.h, kind), "cac_ctx_set_quotient_kernel")
 
     def close(self):
         if self.h:

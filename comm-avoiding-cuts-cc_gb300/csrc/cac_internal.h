@@ -90,6 +90,7 @@ struct cac_ctx {
     uint32_t *pinned_u32 = nullptr;  // 64 KB pinned staging: [0,256) B scalar results, then descriptors
     void *ks_scratch = nullptr;      // grow-only Karger-Stein scratch buffers (mincut.cu)
     uint8_t quotient_choice[32] = {};  // autotuned quotient kernel per (N bucket, width); 0: untuned
+    uint8_t quotient_forced = 0;       // a quotient kernel chosen by the caller instead (0: autotuned)
     cudaStream_t copy_stream = nullptr;  // host-to-device chunks of cac_cc_edges (created on first use)
     cudaEvent_t chunk_ev[40] = {};       // start + one per piece and gap copy in flight
     uint32_t dense_limit = 16384;        // Karger-Stein nodes above this many vertices stay edge lists
@@ -250,6 +251,10 @@ inline bool ks_is_dense(const cac_ctx *ctx, uint32_t N, uint64_t m) {
 // are dense join `eng` as matrices, the others are contracted in turn.
 int sparse_phase(cac_ctx *ctx, KsEngine &eng, std::vector<SparseNode> nodes);
 
+// The status and message of a nonzero engine error word (bit 1: a bounded bulk-copy wait ran
+// out; otherwise an inconsistent selection prefix).
+int engine_error(uint32_t err);
+
 struct MincutQuery {
     const cac_graph *g;
     uint32_t seed, ranks, per_rank;
@@ -307,7 +312,7 @@ int shrink_big(cac_ctx *ctx, const cac_graph *g, uint32_t target, uint32_t B, co
                uint32_t *d_lab, uint32_t *d_kout, void *scratch);
 // Quotient kernel choices of the autotuner (cac_ctx::quotient_choice), bucketed by
 // floor(log2 N) and entry width.
-constexpr uint8_t kQuotientWarp = 1, kQuotientShared = 2;
+constexpr uint8_t kQuotientWarp = 1, kQuotientShared = 2, kQuotientBulk = 3;
 inline int quotient_bucket(uint32_t N, bool small) {
     int b = 0;
     while ((N >> (b + 1)) != 0 && b < 15) b++;

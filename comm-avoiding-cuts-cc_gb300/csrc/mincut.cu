@@ -769,6 +769,193 @@ __global__ void __launch_bounds__(256) quotient_warp_kernel(const TaskDesc *__re
     }
 }
 
+// ---------------------------------------------------------------- bulk-copy quotient
+// The warp-per-row quotient with its member rows staged in shared memory by the bulk-copy (TMA)
+// engine instead of loaded into registers: every warp walks its stream of (output row a, member u)
+// pairs; while it adds row u of the source into its label slots from shared memory, the copy
+// engine already fetches the next member row into the warp's other buffer (one 1-D
+// cp.async.bulk per row, completion counted on an mbarrier per buffer). So a warp always has a
+// whole row in flight, and its registers hold no row data. Rows start on 16-byte boundaries (ld_of
+// pads every row to 4 entries) and their length is a multiple of 16 bytes, as the bulk copy needs.
+// Every wait on an mbarrier is bounded: when the bound is reached the kernel sets bit 1 of the
+// engine's error word, waits (bounded again) for the copies it still has in flight and returns.
+constexpr uint32_t kBulkSpin = 1u << 20;  // bound on one mbarrier wait (polls with a short sleep)
+
+__device__ __forceinline__ uint32_t smem_addr(const void *p) {
+    return (uint32_t)__cvta_generic_to_shared(p);
+}
+
+__device__ __forceinline__ void mbar_init(uint64_t *bar, uint32_t count) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_addr(bar)), "r"(count) : "memory");
+}
+
+// lane 0: one bulk copy of `bytes` from global `src` into shared `dst`, completing on `bar`
+__device__ __forceinline__ void bulk_row(void *dst, const void *src, uint32_t bytes, uint64_t *bar) {
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_addr(bar)), "r"(bytes)
+                 : "memory");
+    asm volatile(
+        "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(smem_addr(dst)),
+        "l"(src), "r"(bytes), "r"(smem_addr(bar))
+        : "memory");
+}
+
+// wait until the barrier's phase `parity` has completed; false when the bound ran out
+__device__ __forceinline__ bool mbar_wait(uint64_t *bar, uint32_t parity) {
+    for (uint32_t i = 0; i < kBulkSpin; i++) {
+        uint32_t done;
+        asm volatile(
+            "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}"
+            : "=r"(done)
+            : "r"(smem_addr(bar)), "r"(parity)
+            : "memory");
+        if (done) return true;
+        __nanosleep(32);
+    }
+    return false;
+}
+
+template <typename Ts, typename Tm>
+__global__ void __launch_bounds__(256) quotient_bulk_kernel(const TaskDesc *__restrict__ tasks,
+                                                            const SrcDesc *__restrict__ srcs,
+                                                            const uint32_t *__restrict__ kdim,
+                                                            const uint64_t *__restrict__ group_task_off,
+                                                            uint32_t ntasks, uint32_t rows,
+                                                            const uint64_t *__restrict__ out_off,
+                                                            unsigned char *out_base, uint32_t lab_words,
+                                                            uint32_t kmax, uint32_t row_words, uint32_t *err) {
+    extern __shared__ __align__(128) unsigned char dsm[];
+    const uint64_t gg = blockIdx.x;
+    uint32_t lo = 0, hi = ntasks - 1;
+    while (lo < hi) {  // last task whose first row group <= gg
+        const uint32_t mid = (lo + hi + 1) >> 1;
+        if (group_task_off[mid] <= gg) lo = mid; else hi = mid - 1;
+    }
+    const TaskDesc T = tasks[lo];
+    const SrcDesc S = srcs[T.src];
+    const uint32_t k = kdim[lo];
+    const uint32_t N = S.N;
+    const uint32_t a0 = (uint32_t)(gg - group_task_off[lo]) * rows, a1 = min(k, a0 + rows);
+    if (!width_is<Tm>(S.small)) return;
+    const Tm *mat = reinterpret_cast<const Tm *>(S.mat);
+    constexpr int VEC = 16 / sizeof(Tm);
+    using Vec = typename std::conditional<sizeof(Tm) == 4, uint4, ulonglong2>::type;
+    const uint64_t ldN = ld_of(N);
+    const uint32_t row_bytes = (uint32_t)(ldN * sizeof(Tm));
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+    // shared memory: 16 mbarriers | labels | per warp: two row buffers, then its k-entry row
+    uint64_t *bars = reinterpret_cast<uint64_t *>(dsm);
+    uint32_t *s_lab = reinterpret_cast<uint32_t *>(dsm + 128);
+    const size_t per_warp = (((size_t)row_words * sizeof(Tm)) * 2 + (size_t)kmax * sizeof(Ts) + 15) & ~(size_t)15;
+    unsigned char *wbase = dsm + 128 + (((size_t)lab_words * 4 + 15) & ~(size_t)15) + (size_t)warp * per_warp;
+    Tm *const buf0 = reinterpret_cast<Tm *>(wbase);
+    Tm *const buf1 = reinterpret_cast<Tm *>(wbase + (size_t)row_words * sizeof(Tm));
+    Ts *qrow = reinterpret_cast<Ts *>(wbase + (size_t)row_words * sizeof(Tm) * 2);
+    uint64_t *bar = bars + 2 * warp;
+    for (uint32_t i = threadIdx.x; i < N; i += blockDim.x) s_lab[i] = T.lab[i];
+    if (lane == 0) {
+        mbar_init(bar, 1);
+        mbar_init(bar + 1, 1);
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    __syncthreads();
+    Tm *Qt = reinterpret_cast<Tm *>(out_base + out_off[lo]);
+    uint64_t *rowsum_out = reinterpret_cast<uint64_t *>(out_base + out_off[ntasks + lo]);
+    const uint32_t small = S.small;
+    const uint32_t nbk = (k + 31) / 32;
+    uint64_t *blk = rowsum_out + k;
+    // the warp's stream: rows a = a0 + warp, a0 + warp + nw, ...; members p of each row
+    uint32_t a = a0 + warp;
+    if (a >= a1) return;  // no row for this warp (its barriers were never armed)
+    uint32_t p = T.memb_off[a], pend = T.memb_off[a + 1];
+    // per buffer: the phase to wait for next, and whether a copy into it is in flight (bits 0, 1)
+    uint32_t parity = 0, inflight = 1;
+    bool failed = false;
+    if (lane == 0) bulk_row(buf0, mat + (uint64_t)T.members[p] * ldN, row_bytes, bar);
+    for (uint32_t b = lane; b < k; b += 32) qrow[b] = 0;
+    __syncwarp();
+    for (uint32_t item = 0;; item++) {
+        const int cur = item & 1, nxt = cur ^ 1;
+        // the next item of the stream, fetched while this one is added
+        const bool row_done = p + 1 >= pend;
+        uint32_t na = a, np = p + 1, npend = pend;
+        if (row_done) {
+            na = a + nw;
+            if (na < a1) {
+                np = T.memb_off[na];
+                npend = T.memb_off[na + 1];
+            }
+        }
+        const bool has_next = na < a1;
+        if (has_next) {
+            if (lane == 0) bulk_row(nxt ? buf1 : buf0, mat + (uint64_t)T.members[np] * ldN, row_bytes, bar + nxt);
+            inflight |= 1u << nxt;
+        }
+        if (!mbar_wait(bar + cur, (parity >> cur) & 1u)) {
+            failed = true;
+            break;
+        }
+        parity ^= 1u << cur;
+        inflight &= ~(1u << cur);
+        // add the member row into the label slots of the warp's output row
+        const Vec *row = reinterpret_cast<const Vec *>(cur ? buf1 : buf0);
+        for (uint32_t c = lane * VEC; c < N; c += 32 * VEC) {
+            const Vec q = row[c / VEC];
+            const Tm *e = reinterpret_cast<const Tm *>(&q);
+#pragma unroll
+            for (int t = 0; t < VEC; t++)
+                if (c + t < N && e[t]) sadd(&qrow[s_lab[c + t]], (uint64_t)e[t]);
+        }
+        __syncwarp();  // every lane is done with buf[cur] (it is refilled two items on)
+        if (row_done) {
+            // row a is complete: store it with the diagonal zeroed, its block prefixes and its sum
+            const uint64_t qb = (uint64_t)a * ld_of(k);
+            uint64_t run = 0;
+            for (uint32_t b0 = 0; b0 < k; b0 += 128) {
+                uint64_t acc[4];
+#pragma unroll
+                for (int u = 0; u < 4; u++) {
+                    const uint32_t b = b0 + 32 * u + lane;
+                    acc[u] = (b < k && b != a) ? (uint64_t)qrow[b] : 0;
+                    if (b < k) Qt[qb + b] = (Tm)acc[u];
+                }
+#pragma unroll
+                for (int u = 0; u < 4; u++) {
+                    if (small) {
+                        const uint32_t lo16 = __reduce_add_sync(0xffffffffu, (uint32_t)(acc[u] & 0xFFFFu));
+                        const uint32_t hi16 = __reduce_add_sync(0xffffffffu, (uint32_t)(acc[u] >> 16));
+                        acc[u] = (uint64_t)lo16 + ((uint64_t)hi16 << 16);
+                    } else {
+#pragma unroll
+                        for (int o = 16; o > 0; o >>= 1) acc[u] += __shfl_xor_sync(0xffffffffu, acc[u], o);
+                    }
+                }
+#pragma unroll
+                for (int u = 0; u < 4; u++) {
+                    if (b0 + 32 * u < k) {
+                        run += acc[u];
+                        if (lane == u) blk[(uint64_t)a * nbk + (b0 >> 5) + u] = run;
+                    }
+                }
+            }
+            if (lane == 0) rowsum_out[a] = run;
+            __syncwarp();
+            for (uint32_t b = lane; b < k; b += 32) qrow[b] = 0;
+            __syncwarp();
+        }
+        if (!has_next) break;
+        a = na;
+        p = np;
+        pend = npend;
+    }
+    if (failed) {
+        if (lane == 0) atomicOr(err, 2u);
+        // let the copies still in flight land before the shared memory is released
+        for (int b = 0; b < 2; b++)
+            if ((inflight >> b) & 1u) mbar_wait(bar + b, (parity >> b) & 1u);
+    }
+}
+
 // Exact minimum cut of one leaf (n <= 128) by one warp: maximum-adjacency orderings as in the
 // reference's Stoer-Wagner base case (co_mincut_base_case.hpp:52-144), with the Nagamochi-Ono-
 // Ibaraki contraction rule (Nagamochi & Ibaraki 1992; Nagamochi, Ono & Ibaraki 1994): when vertex
@@ -1025,6 +1212,15 @@ int KsEngine::read_err(uint32_t *err) {
     CAC_CUDA_TRY(cudaMemcpyAsync(err, e->p, 4, cudaMemcpyDeviceToHost, ctx_->stream));
     CAC_CUDA_TRY(cudaStreamSynchronize(ctx_->stream));
     return CAC_OK;
+}
+
+int engine_error(uint32_t err) {
+    if (err & 2u) {
+        set_error("Karger-Stein quotient: a bulk-copy wait exceeded its bound");
+        return CAC_ERR_TIMEOUT;
+    }
+    set_error("inconsistent selection prefix in the contraction kernel");
+    return CAC_ERR_CUDA;
 }
 
 int KsEngine::alloc(size_t bytes, MatBuf **out) {
@@ -1330,29 +1526,66 @@ int KsEngine::step() {
             CAC_CUDA_TRY(cudaGetLastError());
             return CAC_OK;
         };
-        uint8_t &tuned = ctx_->quotient_choice[quotient_bucket(maxN, all_small)];
+        // the bulk-copy variant of the warp quotient: labels, then per warp two staged member rows
+        // and its output row; 8 warps where two CTAs fit an SM, else 4 where one does
+        const size_t row_words = (size_t)ld_of(maxN);
+        const size_t bulk_per_warp = ((row_words * (all_small ? 4 : 8)) * 2 + (size_t)kmax * rs_bytes + 15) & ~(size_t)15;
+        const size_t bulk_base = 128 + ((stage_words * 4 + 15) & ~(size_t)15);
+        const uint32_t bwarps = bulk_base + 8 * bulk_per_warp <= 113 * 1024   ? 8u
+                                : bulk_base + 4 * bulk_per_warp <= 226 * 1024 ? 4u
+                                                                              : 0u;
+        std::vector<uint64_t> gto_bulk;
+        const uint64_t groups_bulk = bwarps ? group_offsets(bwarps * 4, gto_bulk) : 0;
+        auto launch_bulk = [&]() -> int {
+            CAC_TRY(upload(ctx_, d_gto, gto_bulk));
+            const size_t bsm = bulk_base + bwarps * bulk_per_warp;
+            std::vector<decltype(&quotient_bulk_kernel<uint32_t, uint32_t>)> kerns;
+            if (all_small) kerns.push_back(quotient_bulk_kernel<uint32_t, uint32_t>);
+            else {
+                if (t32) kerns.push_back(quotient_bulk_kernel<uint64_t, uint32_t>);
+                if (t64) kerns.push_back(quotient_bulk_kernel<uint64_t, uint64_t>);
+            }
+            for (auto kern : kerns) {
+                CAC_TRY(smem_optin(ctx_, kern));
+                kern<<<(unsigned)groups_bulk, bwarps * 32, bsm, s>>>(
+                    d_task.as<TaskDesc>(), d_src.as<SrcDesc>(), d_kout.as<uint32_t>(), d_gto.as<uint64_t>(),
+                    (uint32_t)tasks.size(), bwarps * 4, d_qoff.as<uint64_t>(), static_cast<unsigned char *>(out->p),
+                    (uint32_t)stage_words, kmax, (uint32_t)row_words, d_err);
+            }
+            CAC_CUDA_TRY(cudaGetLastError());
+            return CAC_OK;
+        };
+        uint8_t &tuned = ctx_->quotient_forced ? ctx_->quotient_forced
+                                               : ctx_->quotient_choice[quotient_bucket(maxN, all_small)];
         const bool sizeable = groups_shared >= (uint64_t)4 * ctx_->num_sms;  // enough work to time
-        if (!qwarps) {
+        if (!qwarps && !bwarps) {
             CAC_TRY(launch_shared());
         } else if (tuned == kQuotientShared) {
             CAC_TRY(launch_shared());
-        } else if (tuned == kQuotientWarp) {
+        } else if (tuned == kQuotientWarp && qwarps) {
             CAC_TRY(launch_warp());
-        } else if (!sizeable) {
-            CAC_TRY(maxN >= kSharedRowMinN ? launch_shared() : launch_warp());
+        } else if (tuned == kQuotientBulk && bwarps) {
+            CAC_TRY(launch_bulk());
+        } else if (!sizeable || tuned) {
+            CAC_TRY(maxN >= kSharedRowMinN || !qwarps ? launch_shared() : launch_warp());
         } else {
-            // both write the same matrices, row sums and prefixes: time one, then the other
+            // all write the same matrices, row sums and prefixes: time each on this step's data
             cudaEvent_t *ev = ctx_->ev;
-            float t_warp = 0, t_shared = 0;
+            float t_warp = 1e30f, t_shared = 0, t_bulk = 1e30f;
+            CAC_CUDA_TRY(cudaEventRecord(ev[4], s));
+            if (qwarps) CAC_TRY(launch_warp());
             CAC_CUDA_TRY(cudaEventRecord(ev[5], s));
-            CAC_TRY(launch_warp());
+            if (bwarps) CAC_TRY(launch_bulk());
             CAC_CUDA_TRY(cudaEventRecord(ev[6], s));
             CAC_TRY(launch_shared());
             CAC_CUDA_TRY(cudaEventRecord(ev[7], s));
             CAC_CUDA_TRY(cudaEventSynchronize(ev[7]));
-            CAC_CUDA_TRY(cudaEventElapsedTime(&t_warp, ev[5], ev[6]));
+            if (qwarps) CAC_CUDA_TRY(cudaEventElapsedTime(&t_warp, ev[4], ev[5]));
+            if (bwarps) CAC_CUDA_TRY(cudaEventElapsedTime(&t_bulk, ev[5], ev[6]));
             CAC_CUDA_TRY(cudaEventElapsedTime(&t_shared, ev[6], ev[7]));
-            tuned = t_shared < t_warp ? kQuotientShared : kQuotientWarp;
+            tuned = t_shared <= t_warp && t_shared <= t_bulk ? kQuotientShared
+                    : t_bulk < t_warp                        ? kQuotientBulk
+                                                             : kQuotientWarp;
         }
     }
     // the sources are read by everything enqueued above: their buffers may now be released
@@ -1803,8 +2036,7 @@ int mincut_run_queries(cac_ctx *ctx, std::vector<MincutQuery> &queries, float *d
     CAC_CUDA_TRY(cudaStreamSynchronize(s));
     if (device_ms) CAC_CUDA_TRY(cudaEventElapsedTime(device_ms, ctx->ev[0], ctx->ev[1]));
     if (err) {
-        set_error("inconsistent selection prefix in the contraction kernel");
-        return CAC_ERR_CUDA;
+        return engine_error(err);
     }
     return CAC_OK;
 }
@@ -1865,8 +2097,7 @@ int ks_dense_one(cac_ctx *ctx, uint32_t n, const uint64_t *mat_host, uint32_t se
         uint32_t err = 0;
         CAC_TRY(eng.read_err(&err));
         if (err) {
-            set_error("inconsistent selection prefix in the contraction kernel");
-            return CAC_ERR_CUDA;
+            return engine_error(err);
         }
     }
     CAC_CUDA_TRY(cudaMemcpyAsync(cut, d_cut.p, 8, cudaMemcpyDeviceToHost, s));

@@ -351,6 +351,15 @@ int cac_ctx_set_dense_limit(cac_ctx *ctx, uint32_t max_dense_vertices) {
     return CAC_OK;
 }
 
+int cac_ctx_set_quotient_kernel(cac_ctx *ctx, int kind) {
+    if (!ctx || kind < 0 || kind > 3) {
+        set_error("cac_ctx_set_quotient_kernel: kind must be 0 (autotuned), 1, 2 or 3");
+        return CAC_ERR_INVALID;
+    }
+    ctx->quotient_forced = (uint8_t)kind;
+    return CAC_OK;
+}
+
 const char *cac_error_string(int status) {
     switch (status) {
         case CAC_OK: return "ok";

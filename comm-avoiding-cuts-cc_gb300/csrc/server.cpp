@@ -208,8 +208,8 @@ struct CutWorker {
                     st = CAC_ERR_CUDA;
                     msg = "server: reading a query's trial cuts failed";
                 } else if (eng->read_err(&err) != CAC_OK || err) {
-                    st = CAC_ERR_CUDA;
-                    msg = "inconsistent selection prefix in the contraction kernel";
+                    st = engine_error(err);
+                    msg = cac_last_error();
                 } else {
                     uint64_t md = 0;
                     if (graph_min_degree(s->cut, const_cast<cac_graph *>(r->req.graph), &md) != CAC_OK) {

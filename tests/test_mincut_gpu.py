@@ -261,3 +261,22 @@ def test_full_size_k4000_trials_match_replay(ctx):
     np.add.at(deg, u, w.astype(np.uint64))
     np.add.at(deg, v, w.astype(np.uint64))
     assert res.total_trials == 7 and res.cut == min(want) == int(deg.min())
+
+
+@pytest.mark.parametrize("kind", [1, 2, 3])
+@pytest.mark.parametrize("heavy", [False, True])
+def test_every_quotient_kernel_matches_replay(libcac, kind, heavy):
+    # the three quotient kernels (warp per row, eight warps per row, warp per row with member rows
+    # staged by bulk copies) each forced for every step: trial values equal the replay, with u32
+    # node matrices and with u64 ones (total weight above 2^32)
+    c = libcac.Context(0)
+    try:
+        c.set_quotient_kernel(kind)
+        if heavy:
+            n, u, v, w = graphgen.erdos_renyi(700, 0.2, 41, wmin=1 << 20, wmax=1 << 22)
+        else:
+            n, u, v, w = graphgen.complete(1500, 42)
+        got = c.graph(n, u, v, w).trials(seed=7, virtual_ranks=1, trials_per_rank=2)
+        assert [int(x) for x in got[0]] == [O.mincut_trial(n, u, v, w, 7, 0, i) for i in range(2)]
+    finally:
+        c.close()
