@@ -10,9 +10,8 @@
 //                     and a stable scatter that ranks equal digits inside a tile by warp match
 //                     voting; only the digits below the key bound are sorted
 //   merge             segment heads (key differs from its predecessor), an exclusive scan of the
-//                     heads gives each distinct key its slot, weights are summed into the slot with
-//                     u64 atomics (integer sums: the result does not depend on their order); loop
-//                     keys are dropped
+//                     heads gives each distinct key its slot, and each head sums its segment's
+//                     weights in list order into its slot (u64, exact); loop keys are dropped
 // The merged list is sorted by (smaller end, larger end) and holds each pair once.
 #include "cac_internal.h"
 
@@ -183,20 +182,26 @@ __global__ void seg_heads(const uint64_t *keys, uint64_t n, uint64_t loop_key, u
         head[i] = keys[i] != loop_key && (i == 0 || keys[i] != keys[i - 1]) ? 1u : 0u;
 }
 
-// After the scan, slot[i] is the number of distinct keys before i: a head writes its pair, every
-// key adds its weight into its segment's slot (the head's).
+// After the scan, slot[i] is the number of distinct keys before i: the head of every segment of
+// equal keys writes its pair and the sum of its segment's weights (read in order from the sorted
+// list; no atomics, so heavily merged pairs cost no contention).
+__device__ __forceinline__ unsigned long long seg_sum(const uint64_t *keys, const uint64_t *vals, uint64_t n,
+                                                      uint64_t i) {
+    const uint64_t key = keys[i];
+    unsigned long long sum = 0;
+    for (uint64_t j = i; j < n && keys[j] == key; j++) sum += vals[j];
+    return sum;
+}
+
 __global__ void seg_merge(const uint64_t *keys, const uint64_t *vals, uint64_t n, uint64_t loop_key, uint32_t k,
                           const uint32_t *slot, uint32_t *oa, uint32_t *ob, unsigned long long *ow) {
     for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (uint64_t)gridDim.x * blockDim.x) {
         const uint64_t key = keys[i];
-        if (key == loop_key) continue;
-        const bool head = i == 0 || keys[i - 1] != key;
-        const uint32_t s = head ? slot[i] : slot[i] - 1;
-        if (head) {
-            oa[s] = (uint32_t)(key / k);
-            ob[s] = (uint32_t)(key % k);
-        }
-        atomicAdd(ow + s, (unsigned long long)vals[i]);
+        if (key == loop_key || (i > 0 && keys[i - 1] == key)) continue;
+        const uint32_t s = slot[i];
+        oa[s] = (uint32_t)(key / k);
+        ob[s] = (uint32_t)(key % k);
+        ow[s] = seg_sum(keys, vals, n, i);
     }
 }
 
@@ -225,21 +230,18 @@ __global__ void seg_merge_multi(const uint64_t *keys, const uint64_t *vals, uint
                                 uint32_t *ob, unsigned long long *ow, uint32_t *counts) {
     for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (uint64_t)gridDim.x * blockDim.x) {
         const uint64_t key = keys[i];
-        if (key == loop_key) continue;
-        const bool head = i == 0 || keys[i - 1] != key;
-        const uint32_t s = head ? slot[i] : slot[i] - 1;
-        if (head) {
-            uint32_t lo = 0, hi = ntasks - 1;  // last task whose key range starts at or below key
-            while (lo < hi) {
-                const uint32_t mid = (lo + hi + 1) >> 1;
-                if (tasks[mid].key_off <= key) lo = mid; else hi = mid - 1;
-            }
-            const uint64_t r = key - tasks[lo].key_off;
-            oa[s] = (uint32_t)(r / tasks[lo].k);
-            ob[s] = (uint32_t)(r % tasks[lo].k);
-            atomicAdd(counts + lo, 1u);
+        if (key == loop_key || (i > 0 && keys[i - 1] == key)) continue;
+        const uint32_t s = slot[i];
+        uint32_t lo = 0, hi = ntasks - 1;  // last task whose key range starts at or below key
+        while (lo < hi) {
+            const uint32_t mid = (lo + hi + 1) >> 1;
+            if (tasks[mid].key_off <= key) lo = mid; else hi = mid - 1;
         }
-        atomicAdd(ow + s, (unsigned long long)vals[i]);
+        const uint64_t r = key - tasks[lo].key_off;
+        oa[s] = (uint32_t)(r / tasks[lo].k);
+        ob[s] = (uint32_t)(r % tasks[lo].k);
+        ow[s] = seg_sum(keys, vals, n, i);
+        atomicAdd(counts + lo, 1u);
     }
 }
 
@@ -320,7 +322,6 @@ int merge_edges(cac_ctx *ctx, const uint32_t *a, const uint32_t *b, const WT *w,
     }
     seg_heads<<<grid_of(ctx, m), 256, 0, s>>>(k0, m, loop_key, slot);
     CAC_TRY(scan_u32(ctx, slot, m, sums, d_count));
-    CAC_CUDA_TRY(cudaMemsetAsync(ow, 0, 8 * m, s));
     seg_merge<<<grid_of(ctx, m), 256, 0, s>>>(k0, v0, m, loop_key, k, slot, oa, ob,
                                               reinterpret_cast<unsigned long long *>(ow));
     CAC_CUDA_TRY(cudaGetLastError());
@@ -384,7 +385,6 @@ int merge_edges_multi(cac_ctx *ctx, std::vector<MergeTask> &tasks, uint32_t *oa,
     }
     seg_heads<<<grid_of(ctx, M), 256, 0, s>>>(k0, M, key_space, slot);
     CAC_TRY(scan_u32(ctx, slot, M, sums, total));
-    CAC_CUDA_TRY(cudaMemsetAsync(ow, 0, 8 * M, s));
     seg_merge_multi<<<grid_of(ctx, M), 256, 0, s>>>(k0, v0, M, key_space, dt, B, slot, oa, ob,
                                                     reinterpret_cast<unsigned long long *>(ow), counts);
     CAC_CUDA_TRY(cudaGetLastError());
