@@ -124,3 +124,14 @@ def test_square_root_contracted_above_16384(ctx):
     trial = g.trials(seed=0, virtual_ranks=1, trials_per_rank=2)[0]
     assert all(int(deg.min()) <= int(x) < 2 ** 63 for x in trial)  # every trial a real cut
     g.free()
+
+
+def test_sparse_trials_with_u64_weights(lowered):
+    # total weight above 2^32: the sparse lists carry u64 weights and the dense children u64
+    # entries; every trial value still equals the replay
+    n, u, v, _ = _barbell(900, 10, 3, 51)
+    w = graphgen.weights(52, len(u), 1 << 22, 1 << 20)
+    assert int(w.astype(np.uint64).sum()) >= 2 ** 32
+    g = lowered.graph(n, u, v, w)
+    got = g.karger_stein_trials(seed=2, trials=2)
+    assert [int(x) for x in got] == [O.ks_trial(n, u, v, w, 2, i) for i in range(2)]
