@@ -1837,7 +1837,9 @@ int admit_stage1(cac_ctx *ctx, KsEngine &eng, const std::vector<const QueryPlan 
             eng.add(KNode{q.cuts + i, sd[b].k0, sd[b].idx, 1, kdim[b], 1, dd[b].small, q.query, dd[b].mat, roots});
         }
         eng.release(roots);
-        CAC_CUDA_TRY(cudaStreamSynchronize(s));  // the scratch is reused by the next chunk
+        // the scratch is refilled from the host for the next chunk (later kernels on the stream
+        // are ordered after these, so the last chunk needs no wait)
+        if (c1 < items.size()) CAC_CUDA_TRY(cudaStreamSynchronize(s));
         if (!sparse.empty()) CAC_TRY(sparse_phase(ctx, eng, std::move(sparse)));
         c0 = c1;
     }
@@ -1917,7 +1919,7 @@ int admit_big(cac_ctx *ctx, KsEngine &eng, const QueryPlan &q) {
             eng.add(KNode{q.cuts + i, k0[b], idx[b], 1, kdim[b], 1, small, q.query, dd[b].mat, roots});
         }
         eng.release(roots);
-        CAC_CUDA_TRY(cudaStreamSynchronize(s));  // the scratch is reused by the next chunk
+        if (c0 + chunk < q.trials) CAC_CUDA_TRY(cudaStreamSynchronize(s));  // the scratch is reused by the next chunk
         if (!sparse.empty()) CAC_TRY(sparse_phase(ctx, eng, std::move(sparse)));
     }
     return CAC_OK;
