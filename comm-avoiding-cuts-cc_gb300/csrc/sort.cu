@@ -224,10 +224,10 @@ __global__ void edge_keys_multi(const MergeTask *__restrict__ tasks, uint64_t lo
 }
 
 // The merge of many tasks: as seg_merge, with each head's task found by a binary search over the
-// tasks' key ranges; the head also counts into its task.
+// tasks' key ranges.
 __global__ void seg_merge_multi(const uint64_t *keys, const uint64_t *vals, uint64_t n, uint64_t loop_key,
                                 const MergeTask *__restrict__ tasks, uint32_t ntasks, const uint32_t *slot, uint32_t *oa,
-                                uint32_t *ob, unsigned long long *ow, uint32_t *counts) {
+                                uint32_t *ob, unsigned long long *ow) {
     for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (uint64_t)gridDim.x * blockDim.x) {
         const uint64_t key = keys[i];
         if (key == loop_key || (i > 0 && keys[i - 1] == key)) continue;
@@ -241,8 +241,32 @@ __global__ void seg_merge_multi(const uint64_t *keys, const uint64_t *vals, uint
         oa[s] = (uint32_t)(r / tasks[lo].k);
         ob[s] = (uint32_t)(r % tasks[lo].k);
         ow[s] = seg_sum(keys, vals, n, i);
-        atomicAdd(counts + lo, 1u);
     }
+}
+
+// first index of the sorted keys[0, n) whose key is >= x
+__device__ __forceinline__ uint64_t lower_bound_u64(const uint64_t *keys, uint64_t n, uint64_t x) {
+    uint64_t lo = 0, hi = n;
+    while (lo < hi) {
+        const uint64_t mid = (lo + hi) >> 1;
+        if (keys[mid] < x) lo = mid + 1; else hi = mid;
+    }
+    return lo;
+}
+
+// Pairs per task: the keys of task t are the sorted range [key_off[t], key_off[t] + k^2), so its
+// pairs are the heads between the two ends of that range: a difference of the heads' exclusive
+// scan at two binary-searched positions (no per-head counter, which would make every head of a
+// task contend on one word).
+__global__ void task_counts(const uint64_t *keys, uint64_t n, const uint32_t *slot, const uint32_t *total,
+                            const MergeTask *__restrict__ tasks, uint32_t ntasks, uint32_t *counts) {
+    const uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= ntasks) return;
+    const MergeTask T = tasks[t];
+    const uint64_t a = lower_bound_u64(keys, n, T.key_off);
+    const uint64_t b = lower_bound_u64(keys, n, T.key_off + (uint64_t)T.k * T.k);
+    const uint32_t sa = a < n ? slot[a] : *total, sb = b < n ? slot[b] : *total;
+    counts[t] = sb - sa;
 }
 
 unsigned grid_of(cac_ctx *ctx, uint64_t work) {
@@ -386,7 +410,8 @@ int merge_edges_multi(cac_ctx *ctx, std::vector<MergeTask> &tasks, uint32_t *oa,
     seg_heads<<<grid_of(ctx, M), 256, 0, s>>>(k0, M, key_space, slot);
     CAC_TRY(scan_u32(ctx, slot, M, sums, total));
     seg_merge_multi<<<grid_of(ctx, M), 256, 0, s>>>(k0, v0, M, key_space, dt, B, slot, oa, ob,
-                                                    reinterpret_cast<unsigned long long *>(ow), counts);
+                                                    reinterpret_cast<unsigned long long *>(ow));
+    task_counts<<<(B + 255) / 256, 256, 0, s>>>(k0, M, slot, total, dt, B, counts);
     CAC_CUDA_TRY(cudaGetLastError());
     return CAC_OK;
 }
