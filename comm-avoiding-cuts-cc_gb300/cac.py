@@ -118,6 +118,7 @@ EXPORTS = [
     ("cac_karger_stein", ctypes.c_int, [_vp, _vp, ctypes.c_double, ctypes.c_uint32, ctypes.POINTER(MincutResult)]),
     ("cac_mincut_trials", ctypes.c_int, [_vp, _vp, ctypes.c_uint32, ctypes.c_uint32, ctypes.c_uint32, _vp]),
     ("cac_karger_stein_trials", ctypes.c_int, [_vp, _vp, ctypes.c_uint32, ctypes.c_uint32, _vp]),
+    ("cac_mincut_group_trials", ctypes.c_int, [_vp, _vp, ctypes.c_uint32, ctypes.c_uint32, _vp]),
     ("cac_ks_dense", ctypes.c_int, [_vp, ctypes.c_uint32, _vp, ctypes.c_uint32, ctypes.c_uint32, ctypes.c_uint32,
                                     _u64p]),
     ("cac_exact_cut_small", ctypes.c_int, [_vp, ctypes.c_uint32, _vp, _u64p]),
@@ -363,6 +364,13 @@ class Graph:
         _check(lib().cac_karger_stein_trials(self.ctx.h, self.h, seed, trials, ctypes.c_void_p(out.ctypes.data)),
                "cac_karger_stein_trials")
         return out[:trials]
+
+    def group_trials(self, seed, groups):
+        """Every group's value of square_root's group variant (groups 0 .. groups - 1)."""
+        out = np.zeros(max(groups, 1), dtype=np.uint64)
+        _check(lib().cac_mincut_group_trials(self.ctx.h, self.h, seed, groups, ctypes.c_void_p(out.ctypes.data)),
+               "cac_mincut_group_trials")
+        return out[:groups]
 
     def trials(self, seed, virtual_ranks, trials_per_rank):
         out = np.zeros(virtual_ranks * trials_per_rank, dtype=np.uint64)

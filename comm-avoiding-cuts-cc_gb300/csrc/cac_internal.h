@@ -258,9 +258,19 @@ int engine_error(uint32_t err);
 struct MincutQuery {
     const cac_graph *g;
     uint32_t seed, ranks, per_rank;
-    uint64_t *d_cuts;  // ranks * per_rank trial cuts (device)
+    uint64_t *d_cuts;  // ranks * per_rank trial cuts (device), or `groups` of them
     uint32_t t = 0;    // contraction size before Karger-Stein (0: square_root's intermediate size)
+    uint32_t groups = 0;  // > 0: the high-concurrency group variant with this many group trials
 };
+// The trial layout of a square_root query (SquareRootCut.cpp:11-13, 99-100, 188-215): the low-
+// concurrency variant's ceil(T / ranks) trials per rank, or, when ranks >= 2 T, the group
+// variant's ranks / 2^floor(log2(ranks / T)) group trials (per_rank is then 1, as the reference's
+// CSV prints). Fails when the trial count passes 2^32 - 1.
+struct TrialLayout {
+    uint32_t per_rank, total, groups;  // groups > 0 only for the group variant
+    bool high;
+};
+int trial_layout(const char *who, uint32_t n, uint64_t m, double p, uint32_t ranks, TrialLayout *out);
 // Stage 1 and Stage 2 of several queries into a running engine (engine ids ids[i]); their
 // Stage 1 trials share launches. Every trial cut starts at 2^64 - 1 and the root nodes carry the
 // query's engine id; a query is done when outstanding[id] is 0.
@@ -283,8 +293,10 @@ struct ShrinkTask {
     uint64_t tag;
     uint32_t *lab;    // n (device)
     uint32_t *k_out;  // 1 (device)
+    uint32_t dpr;     // draws per round: 0 for the round's vertex count (SequentialSquareRootCut's rounds),
+                      // or a fixed count (the group variant's floor(n0^1.05) samples per round)
 };
-uint64_t shrink_task_scratch(uint32_t n, uint64_t m);
+uint64_t shrink_task_scratch(uint32_t n, uint64_t m, uint32_t dpr = 0);
 uint64_t shrink_tasks_scratch(const std::vector<ShrinkTask> &tasks);
 int shrink_tasks(cac_ctx *ctx, const std::vector<ShrinkTask> &tasks, void *scratch);
 // Device sort and merge of a relabelled edge list (sort.cu): the pairs of the non-loop edges
@@ -340,6 +352,7 @@ int sitmo_blocks(cac_ctx *ctx, const uint64_t key[4], const uint64_t ctr0[4], ui
 uint32_t intermediate_size(uint32_t n, uint64_t m);
 uint32_t number_of_trials(uint32_t n, uint64_t m, double p);
 uint32_t ks_number_of_trials(uint32_t n, double p);
+uint32_t group_draws(uint32_t n);  // the group variant's Stage 1 draws per round
 // largest contracted graph the Karger-Stein engine holds as a dense matrix (its contraction
 // union-find lives in shared memory)
 constexpr uint32_t kMaxDenseVertices = 16384;

@@ -8,27 +8,6 @@
 
 using namespace cac;
 
-namespace {
-
-// SquareRootCut::runLowConcurrencyMaster (SquareRootCut.cpp:99-100): ceil(total / ranks) trials
-// per rank, ranks * that many in all. The product is formed in 64 bits: with many virtual ranks
-// on a dense graph it can pass 2^32, which the result's uint32 columns cannot report.
-int trial_layout(const char *who, double total, uint32_t ranks, uint32_t *per, uint32_t *all) {
-    const double per_d = std::ceil(total / ranks);
-    const uint64_t per64 = per_d < 4294967296.0 ? (uint64_t)per_d : (1ull << 32);
-    const uint64_t all64 = per64 * ranks;
-    if (per64 > 0xFFFFFFFFull || all64 > 0xFFFFFFFFull) {
-        set_error(std::string(who) + ": " + std::to_string(all64) + " trials (" + std::to_string(ranks) +
-                  " virtual ranks) exceed 2^32 - 1");
-        return CAC_ERR_INVALID;
-    }
-    *per = (uint32_t)per64;
-    *all = (uint32_t)all64;
-    return CAC_OK;
-}
-
-}  // namespace
-
 extern "C" {
 
 int cac_mincut_trials(cac_ctx *ctx, const cac_graph *g, uint32_t seed, uint32_t virtual_ranks,
@@ -69,23 +48,24 @@ int cac_mincut(cac_ctx *ctx, const cac_graph *g, double p, uint32_t seed, uint32
     if (virtual_ranks == 0) virtual_ranks = 1;
     CAC_CUDA_TRY(cudaSetDevice(ctx->device));
     *res = cac_mincut_result{};
-    // SquareRootCut::runLowConcurrencyMaster (SquareRootCut.cpp:99-100)
-    const double total = number_of_trials(g->n, g->m, p);
-    uint32_t per = 0, all = 0;
-    CAC_TRY(trial_layout("cac_mincut", total, virtual_ranks, &per, &all));
-    res->trials_per_rank = per;
-    res->total_trials = all;
+    // SquareRootCut::lowConcurrency (SquareRootCut.cpp:11-13) picks the variant: ceil(T / p)
+    // trials per rank (runLowConcurrencyMaster, .cpp:99-100), or p >= 2T and one trial per group
+    // of ranks (participateInGroup, .cpp:188-298)
+    TrialLayout L{};
+    CAC_TRY(trial_layout("cac_mincut", g->n, g->m, p, virtual_ranks, &L));
+    res->trials_per_rank = L.per_rank;
+    res->total_trials = L.total;
     res->intermediate = intermediate_size(g->n, g->m);
-    // SquareRootCut::lowConcurrency (SquareRootCut.cpp:11-13): the group variant is chosen when
-    // p >= 2 * trials; on one GPU every trial runs in one batch either way.
-    res->high_concurrency = (double)virtual_ranks >= 2.0 * total ? 1u : 0u;
+    res->high_concurrency = L.high ? 1u : 0u;
     const uint64_t n_tr = (uint64_t)res->total_trials;
     uint64_t min_degree = 0;
     CAC_TRY(graph_min_degree(ctx, const_cast<cac_graph *>(g), &min_degree));
     void *d = nullptr;
     CAC_TRY(stream_alloc(ctx, &d, n_tr * 8));
     float ms = 0;
-    int st = mincut_trials(ctx, g, seed, virtual_ranks, per, (uint64_t *)d, &ms);
+    std::vector<MincutQuery> q{
+        MincutQuery{g, seed, virtual_ranks, L.per_rank, static_cast<uint64_t *>(d), 0, L.high ? L.groups : 0}};
+    int st = mincut_run_queries(ctx, q, &ms);
     if (st == CAC_OK) {
         std::vector<uint64_t> cuts(n_tr);
         cudaError_t e = cudaMemcpy(cuts.data(), d, n_tr * 8, cudaMemcpyDeviceToHost);
@@ -159,6 +139,33 @@ int cac_karger_stein_trials(cac_ctx *ctx, const cac_graph *g, uint32_t seed, uin
     return st;
 }
 
+int cac_mincut_group_trials(cac_ctx *ctx, const cac_graph *g, uint32_t seed, uint32_t groups, uint64_t *cuts_host) {
+    if (!ctx || !g || !cuts_host) {
+        set_error("cac_mincut_group_trials: invalid argument");
+        return CAC_ERR_INVALID;
+    }
+    if (g->n < 2) {
+        set_error("cac_mincut_group_trials: a cut needs at least two vertices");
+        return CAC_ERR_INVALID;
+    }
+    if (groups == 0) return CAC_OK;
+    CAC_CUDA_TRY(cudaSetDevice(ctx->device));
+    void *d = nullptr;
+    CAC_TRY(stream_alloc(ctx, &d, (uint64_t)groups * 8));
+    std::vector<MincutQuery> q{MincutQuery{g, seed, groups, 1, static_cast<uint64_t *>(d), 0, groups}};
+    float ms = 0;
+    int st = mincut_run_queries(ctx, q, &ms);
+    if (st == CAC_OK) {
+        cudaError_t e = cudaMemcpy(cuts_host, d, (uint64_t)groups * 8, cudaMemcpyDeviceToHost);
+        if (e != cudaSuccess) {
+            set_error(cudaGetErrorString(e));
+            st = CAC_ERR_CUDA;
+        }
+    }
+    stream_free(ctx, d, (uint64_t)groups * 8);
+    return st;
+}
+
 int cac_mincut_batch(cac_ctx *ctx, const cac_mincut_query *queries, uint32_t count, cac_mincut_result *results) {
     if (!ctx || (count && (!queries || !results))) {
         set_error("cac_mincut_batch: invalid argument");
@@ -178,16 +185,15 @@ int cac_mincut_batch(cac_ctx *ctx, const cac_mincut_query *queries, uint32_t cou
             return CAC_ERR_INVALID;
         }
         const uint32_t ranks = q.virtual_ranks ? q.virtual_ranks : 1;
-        const double trials = number_of_trials(q.graph->n, q.graph->m, q.success_probability);
-        uint32_t per = 0, all = 0;
-        CAC_TRY(trial_layout("cac_mincut_batch", trials, ranks, &per, &all));
+        TrialLayout L{};
+        CAC_TRY(trial_layout("cac_mincut_batch", q.graph->n, q.graph->m, q.success_probability, ranks, &L));
         results[i] = cac_mincut_result{};
-        results[i].trials_per_rank = per;
-        results[i].total_trials = all;
+        results[i].trials_per_rank = L.per_rank;
+        results[i].total_trials = L.total;
         results[i].intermediate = intermediate_size(q.graph->n, q.graph->m);
-        results[i].high_concurrency = (double)ranks >= 2.0 * trials ? 1u : 0u;
-        qs[i] = MincutQuery{q.graph, q.seed, ranks, per, nullptr};
-        total += (uint64_t)per * ranks;
+        results[i].high_concurrency = L.high ? 1u : 0u;
+        qs[i] = MincutQuery{q.graph, q.seed, ranks, L.per_rank, nullptr, 0, L.high ? L.groups : 0};
+        total += L.total;
     }
     if (total == 0) return CAC_OK;
     std::vector<uint64_t> min_degree(count);
@@ -198,7 +204,7 @@ int cac_mincut_batch(cac_ctx *ctx, const cac_mincut_query *queries, uint32_t cou
     uint64_t off = 0;
     for (auto &q : qs) {
         q.d_cuts = static_cast<uint64_t *>(d) + off;
-        off += (uint64_t)q.ranks * q.per_rank;
+        off += q.groups ? (uint64_t)q.groups : (uint64_t)q.ranks * q.per_rank;
     }
     float ms = 0;
     int st = mincut_run_queries(ctx, qs, &ms);
@@ -211,7 +217,7 @@ int cac_mincut_batch(cac_ctx *ctx, const cac_mincut_query *queries, uint32_t cou
         } else {
             off = 0;
             for (uint32_t i = 0; i < count; i++) {
-                const uint64_t t = (uint64_t)qs[i].ranks * qs[i].per_rank;
+                const uint64_t t = results[i].total_trials;
                 results[i].cut = t ? std::min(min_degree[i], *std::min_element(cuts.begin() + off,
                                                                                    cuts.begin() + off + t))
                                    : 0;

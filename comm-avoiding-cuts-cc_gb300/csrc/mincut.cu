@@ -1630,7 +1630,10 @@ struct QueryPlan {
     uint64_t trials;
     uint64_t *cuts;       // device, one per trial
     uint32_t query;       // engine bookkeeping id
+    uint32_t groups = 0;  // > 0: the high-concurrency group variant (trials = groups)
 };
+
+int admit_groups(cac_ctx *ctx, KsEngine &eng, const QueryPlan &q);
 
 int admit_stage1(cac_ctx *ctx, KsEngine &eng, const std::vector<const QueryPlan *> &qs);
 int admit_big(cac_ctx *ctx, KsEngine &eng, const QueryPlan &q);
@@ -1925,13 +1928,110 @@ int admit_big(cac_ctx *ctx, KsEngine &eng, const QueryPlan &q) {
     return CAC_OK;
 }
 
+// The high-concurrency group variant (SquareRootCut::participateInGroup, SquareRootCut.cpp:188-298):
+// group trial g runs WeightedIteratedSparseSampling::shrink (.cpp:4-24) as Stage 1 rounds of a
+// fixed floor(n^1.05) weighted draws (edgesToSamplePerProcessor, .hpp:66-67) with key
+// (seed + g, 0, 1, 0), builds the contracted graph (reduce, .cpp:26-234: dense, or a sorted and
+// merged sparse root above the dense limit), and, as parallel_cut(.., 2, ..) runs two recursive
+// contractions of it (recursive_contract.cpp:45-83), starts two Karger-Stein recursions from that
+// root with keys (seed + g, 0 | 1, 1 + h, 0). All groups' Stage 1 runs in one grid per chunk
+// (shrink_big.cu with a fixed draw count per round).
+int admit_groups(cac_ctx *ctx, KsEngine &eng, const QueryPlan &q) {
+    cudaStream_t s = ctx->stream;
+    const cac_graph *g = q.g;
+    const uint32_t n = g->n;
+    const uint64_t m = g->m;
+    const uint32_t small = g->total_weight < (1ull << 32) ? 1u : 0u;
+    const bool stage1 = q.t < n;
+    const uint32_t dpr = group_draws(n);
+    const uint64_t tt = std::min<uint64_t>(q.t, n);
+    const uint64_t per_group = (stage1 ? shrink_task_scratch(n, m, dpr) : 0) + 4ull * n +
+                               (q.t > ctx->dense_limit ? 16ull * m : tt * ld_of((uint32_t)tt) * (small ? 4 : 8));
+    const uint64_t chunk = std::max<uint64_t>(1, std::min<uint64_t>({q.trials, (4ull << 30) / per_group, (uint64_t)65535}));
+    DevBuf &d_pre = scratch(ctx, kSlotPre), &d_lab = scratch(ctx, kSlotLab), &d_k = scratch(ctx, kSlotK),
+           &d_dd = scratch(ctx, kSlotDd);
+    for (uint64_t c0 = 0; c0 < q.trials; c0 += chunk) {
+        const uint32_t B = (uint32_t)std::min<uint64_t>(chunk, q.trials - c0);
+        std::vector<uint32_t> kdim(B, n);
+        if (stage1) {
+            std::vector<ShrinkTask> tasks(B);
+            CAC_TRY(d_lab.ensure((size_t)B * n * 4));
+            CAC_TRY(d_k.ensure((size_t)B * 4));
+            for (uint32_t b = 0; b < B; b++)
+                tasks[b] = ShrinkTask{g->u, g->v, g->w, false, m, n, q.t, q.seed + (uint32_t)(c0 + b), 0, 1,
+                                      d_lab.as<uint32_t>() + (size_t)b * n, d_k.as<uint32_t>() + b, dpr};
+            CAC_TRY(d_pre.ensure(shrink_tasks_scratch(tasks)));
+            CAC_TRY(shrink_tasks(ctx, tasks, d_pre.p));
+            CAC_CUDA_TRY(cudaMemcpyAsync(kdim.data(), d_k.p, (size_t)B * 4, cudaMemcpyDeviceToHost, s));
+            CAC_CUDA_TRY(cudaStreamSynchronize(s));
+        }
+        auto lab_of = [&](uint32_t b) -> const uint32_t * {
+            return stage1 ? d_lab.as<uint32_t>() + (size_t)b * n : nullptr;
+        };
+        if (q.t > ctx->dense_limit) {
+            // sparse roots: the merged contracted graph, shared by the group's two recursions
+            std::vector<SparseNode> sparse;
+            for (uint32_t b = 0; b < B; b++) {
+                SparseNode nd;
+                CAC_TRY(sparse_root(ctx, eng, q, q.cuts + c0 + b, q.seed + (uint32_t)(c0 + b), 0, lab_of(b), kdim[b],
+                                    &nd));
+                sparse.push_back(nd);
+                nd.idx = 1;
+                if (nd.buf) nd.buf->refs++;
+                sparse.push_back(nd);
+            }
+            CAC_TRY(sparse_phase(ctx, eng, std::move(sparse)));
+            continue;
+        }
+        // dense roots (more than 16384 vertices left only when Stage 1 found no edge between
+        // them: a disconnected graph, cut 0)
+        for (uint32_t b = 0; b < B; b++)
+            if (kdim[b] > kMaxSmemVertices) kdim[b] = 0;
+        const uint64_t esize = small ? 4 : 8;
+        uint64_t bytes = 0;
+        for (uint32_t b = 0; b < B; b++) bytes += ((uint64_t)kdim[b] * ld_of(kdim[b]) * esize + 15) / 16 * 16;
+        MatBuf *roots = nullptr;
+        CAC_TRY(eng.alloc(std::max<uint64_t>(bytes, 16), &roots));
+        CAC_CUDA_TRY(cudaMemsetAsync(roots->p, 0, bytes, s));
+        std::vector<DenseDesc> dd(B);
+        uint64_t off = 0;
+        for (uint32_t b = 0; b < B; b++) {
+            dd[b] = DenseDesc{g->u, g->v, g->w, lab_of(b), static_cast<unsigned char *>(roots->p) + off,
+                              kdim[b] >= 2 ? m : 0, kdim[b], small};
+            off += ((uint64_t)kdim[b] * ld_of(kdim[b]) * esize + 15) / 16 * 16;
+        }
+        CAC_TRY(upload(ctx, d_dd, dd));
+        if (m) {
+            dim3 grid((unsigned)std::max<uint64_t>(
+                          1, std::min<uint64_t>((m + 255) / 256, std::max<uint64_t>(1, (uint64_t)ctx->num_sms * 8 / B))),
+                      B);
+            dense_build_kernel<<<grid, 256, 0, s>>>(d_dd.as<DenseDesc>());
+            CAC_CUDA_TRY(cudaGetLastError());
+        }
+        roots->refs++;
+        for (uint32_t b = 0; b < B; b++) {
+            const uint64_t i = c0 + b;
+            if (kdim[b] < 2) {
+                fill_u64<<<1, 32, 0, s>>>(q.cuts + i, 1, 0);
+                continue;
+            }
+            for (uint32_t j = 0; j < 2; j++)
+                eng.add(KNode{q.cuts + i, q.seed + (uint32_t)i, j, 1, kdim[b], 1, small, q.query, dd[b].mat, roots});
+        }
+        eng.release(roots);
+        if (c0 + chunk < q.trials) CAC_CUDA_TRY(cudaStreamSynchronize(s));  // the scratch is reused
+    }
+    return CAC_OK;
+}
+
 // Admission of several queries: those with Stage 1 in shared memory go through admit_stage1
 // together, the others one by one.
 int admit_many(cac_ctx *ctx, KsEngine &eng, const std::vector<const QueryPlan *> &qs) {
     std::vector<const QueryPlan *> batched;
     for (const QueryPlan *q : qs) {
         if (q->trials == 0) continue;
-        if (q->t < q->g->n && q->g->n <= kMaxSmemVertices) batched.push_back(q);
+        if (q->groups) CAC_TRY(admit_groups(ctx, eng, *q));
+        else if (q->t < q->g->n && q->g->n <= kMaxSmemVertices) batched.push_back(q);
         else CAC_TRY(admit(ctx, eng, *q));
     }
     return batched.empty() ? CAC_OK : admit_stage1(ctx, eng, batched);
@@ -1964,7 +2064,8 @@ int mincut_admit_queries(cac_ctx *ctx, KsEngine &eng, const std::vector<MincutQu
             continue;
         }
         plans.push_back(QueryPlan{q.g, q.seed, q.ranks, q.per_rank, q.t ? q.t : intermediate_size(q.g->n, q.g->m),
-                                  (uint64_t)q.ranks * q.per_rank, q.d_cuts, ids[i]});
+                                  q.groups ? (uint64_t)q.groups : (uint64_t)q.ranks * q.per_rank, q.d_cuts, ids[i],
+                                  q.groups});
         which.push_back(i);
         const QueryPlan &p = plans.back();
         if (p.trials)
@@ -2005,7 +2106,8 @@ int mincut_run_queries(cac_ctx *ctx, std::vector<MincutQuery> &queries, float *d
         p.ranks = q.ranks;
         p.per_rank = q.per_rank;
         p.t = q.t ? q.t : intermediate_size(q.g->n, q.g->m);
-        p.trials = (uint64_t)q.ranks * q.per_rank;
+        p.trials = q.groups ? (uint64_t)q.groups : (uint64_t)q.ranks * q.per_rank;
+        p.groups = q.groups;
         p.cuts = q.d_cuts;
         p.query = (uint32_t)i;
         if (p.trials)

@@ -138,6 +138,40 @@ uint32_t number_of_trials(uint32_t n, uint64_t m, double p) {
     return (uint32_t)std::ceil(((double)n * ((double)n * std::log(c))) / (2.0 * 2.0 * ((double)m * pk)));
 }
 
+int trial_layout(const char *who, uint32_t n, uint64_t m, double p, uint32_t ranks, TrialLayout *out) {
+    if (ranks == 0) ranks = 1;
+    const uint32_t total = number_of_trials(n, m, p);
+    TrialLayout L{};
+    L.high = (double)ranks >= 2.0 * total;
+    if (L.high) {
+        // participateInGroup: processors_per_trial = p / T (integer), group_size the largest power
+        // of two not above it, group_count = p / group_size
+        const uint32_t per = total ? ranks / total : ranks;
+        uint32_t size = 1;
+        while ((uint64_t)size * 2 <= per) size *= 2;
+        L.groups = ranks / size;
+        L.per_rank = 1;
+        L.total = L.groups;
+    } else {
+        const uint64_t per = (uint64_t)std::ceil((double)total / ranks);
+        const uint64_t all = per * ranks;
+        if (per > 0xFFFFFFFFull || all > 0xFFFFFFFFull) {
+            set_error(std::string(who) + ": " + std::to_string(all) + " trials (" + std::to_string(ranks) +
+                      " virtual ranks) exceed 2^32 - 1");
+            return CAC_ERR_INVALID;
+        }
+        L.per_rank = (uint32_t)per;
+        L.total = (uint32_t)all;
+    }
+    *out = L;
+    return CAC_OK;
+}
+
+uint32_t group_draws(uint32_t n) {
+    // edgesToSamplePerProcessor (WeightedIteratedSparseSampling.hpp:66-67): floor(n0^(1 + 0.1 / 2)) in float
+    return (uint32_t)std::pow((float)n, 1.0f + 0.1f / 2.0f);
+}
+
 uint32_t ks_number_of_trials(uint32_t n, double p) {
     // comincut::number_of_trials (co_mincut.cpp:44-73): multiply the failure probability of one
     // trial until it is at most 1 - p

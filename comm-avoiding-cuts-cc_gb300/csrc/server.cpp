@@ -47,7 +47,7 @@ struct Request {
     bool done = false;
     Clock::time_point t_submit, t_admit;
     // square_root state
-    uint32_t ranks = 1, per_rank = 0, query = 0;
+    uint32_t ranks = 1, per_rank = 0, groups = 0, query = 0;
     uint64_t trials = 0, est_bytes = 0;
     void *d_cuts = nullptr;
     int st = CAC_OK;  // an admission error, reported when the query's nodes have drained
@@ -174,7 +174,7 @@ struct CutWorker {
                 continue;
             }
             qs.push_back(MincutQuery{r->req.graph, r->req.seed, r->ranks, r->per_rank,
-                                     static_cast<uint64_t *>(r->d_cuts)});
+                                     static_cast<uint64_t *>(r->d_cuts), 0, r->groups});
             ids.push_back(r->query);
             rs.push_back(r);
         }
@@ -374,13 +374,11 @@ int cac_server_submit(cac_server *s, const cac_request *req, uint64_t *ticket) {
             set_error("cac_server_submit: graph outside the supported square_root sizes");
             return CAC_ERR_UNSUPPORTED;
         }
-        const uint32_t total = number_of_trials(g->n, g->m, req->success_probability);
-        r->per_rank = (uint32_t)(((uint64_t)total + r->ranks - 1) / r->ranks);
-        r->trials = (uint64_t)r->per_rank * r->ranks;
-        if (r->trials > 0xFFFFFFFFull) {
-            set_error("cac_server_submit: " + std::to_string(r->trials) + " trials exceed 2^32 - 1");
-            return CAC_ERR_INVALID;
-        }
+        TrialLayout L{};
+        CAC_TRY(trial_layout("cac_server_submit", g->n, g->m, req->success_probability, r->ranks, &L));
+        r->per_rank = L.per_rank;
+        r->groups = L.high ? L.groups : 0;
+        r->trials = L.total;
         const uint64_t tt = std::min<uint64_t>(t, g->n);
         r->est_bytes = (t < g->n ? r->trials : 1) * tt * tt * 8 * 3 + r->trials * 8;
     } else if (req->kind == CAC_QUERY_APPROX &&

@@ -56,6 +56,8 @@ struct BigTrial {
     uint32_t *k_out;  // output: vertices left
     uint32_t k0, idx; // stream key words 0, 1
     uint64_t tag;     // stream key word 2
+    uint32_t dpr;     // draws per round (0: the round's vertex count)
+    uint32_t pad;
 };
 
 struct BigState {
@@ -195,10 +197,10 @@ __global__ void __launch_bounds__(1024) big_tile_scan(const BigTrial *T, BigStat
             s.done = 1;
             s.phase = kPhaseRoundDone;
         } else {
-            s.ndraw = s.count;
+            s.ndraw = t.dpr ? t.dpr : s.count;
             s.lo = 0;
-            s.hi = s.count;
-            s.mid = s.count;
+            s.hi = s.ndraw;
+            s.mid = s.ndraw;
             s.nlog = 0;
             s.undo_n = 0;
             s.apply_one = 0;
@@ -382,16 +384,18 @@ __global__ void big_label_rest(const BigTrial *T) {
 
 }  // namespace
 
-// Scratch of one contraction task, carved in the order shrink_tasks takes it.
-uint64_t shrink_task_scratch(uint32_t n, uint64_t m) {
+// Scratch of one contraction task, carved in the order shrink_tasks takes it (dpr: draws per
+// round, 0 for the vertex count; the draw list holds a round's draws).
+uint64_t shrink_task_scratch(uint32_t n, uint64_t m, uint32_t dpr) {
     const uint64_t etiles = (m + kET - 1) / kET, vtiles = ((uint64_t)n + kVT - 1) / kVT;
+    const uint64_t nd = std::max<uint64_t>(n, dpr);
     return align_up(4ull * n) + align_up(8 * std::max<uint64_t>(m, 1)) + align_up(8 * std::max<uint64_t>(etiles, 1)) +
-           align_up(8ull * n) + align_up(4ull * n) + align_up(4 * std::max<uint64_t>(vtiles, 1));
+           align_up(8ull * nd) + align_up(4ull * n) + align_up(4 * std::max<uint64_t>(vtiles, 1));
 }
 
 uint64_t shrink_tasks_scratch(const std::vector<ShrinkTask> &tasks) {
     uint64_t b = align_up(sizeof(BigTrial) * tasks.size()) + align_up(sizeof(BigState) * tasks.size()) + align_up(16);
-    for (const ShrinkTask &t : tasks) b += shrink_task_scratch(t.n, t.m);
+    for (const ShrinkTask &t : tasks) b += shrink_task_scratch(t.n, t.m, t.dpr);
     return b;
 }
 
@@ -414,7 +418,7 @@ int shrink_tasks(cac_ctx *ctx, const std::vector<ShrinkTask> &tasks, void *scrat
         p += align_up(bytes);
         return q;
     };
-    uint32_t nmax = 1, etmax = 1, vtmax = 1;
+    uint32_t nmax = 1, etmax = 1, vtmax = 1, dmax = 1;
     uint64_t mmax = 0;
     bool any32 = false, any64 = false;
     for (uint32_t b = 0; b < B; b++) {
@@ -432,7 +436,7 @@ int shrink_tasks(cac_ctx *ctx, const std::vector<ShrinkTask> &tasks, void *scrat
         t.par = reinterpret_cast<uint32_t *>(take(4ull * k.n));
         t.pre = reinterpret_cast<uint64_t *>(take(8 * std::max<uint64_t>(k.m, 1)));
         t.tsum = reinterpret_cast<uint64_t *>(take(8ull * std::max<uint32_t>(t.etiles, 1)));
-        t.draws = reinterpret_cast<uint2 *>(take(8ull * k.n));
+        t.draws = reinterpret_cast<uint2 *>(take(8ull * std::max<uint32_t>(k.n, k.dpr)));
         t.log = reinterpret_cast<uint32_t *>(take(4ull * k.n));
         t.vsum = reinterpret_cast<uint32_t *>(take(4ull * std::max<uint32_t>(t.vtiles, 1)));
         t.lab = k.lab;
@@ -440,7 +444,10 @@ int shrink_tasks(cac_ctx *ctx, const std::vector<ShrinkTask> &tasks, void *scrat
         t.k0 = k.k0;
         t.idx = k.idx;
         t.tag = k.tag;
+        t.dpr = k.dpr;
+        t.pad = 0;
         nmax = std::max(nmax, k.n);
+        dmax = std::max(dmax, std::max(k.n, k.dpr));
         mmax = std::max(mmax, k.m);
         etmax = std::max(etmax, t.etiles);
         vtmax = std::max(vtmax, t.vtiles);
@@ -452,9 +459,9 @@ int shrink_tasks(cac_ctx *ctx, const std::vector<ShrinkTask> &tasks, void *scrat
     CAC_CUDA_TRY(cudaMemcpyAsync(dT, T.data(), sizeof(BigTrial) * B, cudaMemcpyHostToDevice, s));
     const uint32_t vgrid = std::max(1u, std::min<uint32_t>((nmax + kBT - 1) / kBT, 2048u / std::max(1u, B / 8 + 1)));
     big_init<<<dim3(vgrid, B), kBT, 0, s>>>(dT, dS);
-    const uint32_t dgrid = std::max(1u, std::min<uint32_t>((nmax + kBT - 1) / kBT, 4096u / B + 1));
+    const uint32_t dgrid = std::max(1u, std::min<uint32_t>((dmax + kBT - 1) / kBT, 4096u / B + 1));
     uint32_t iters = 3;
-    while ((1ull << (iters - 3)) < nmax) iters++;  // ceil(log2 n) + 3 bisection steps close every round
+    while ((1ull << (iters - 3)) < dmax) iters++;  // ceil(log2 draws) + 3 bisection steps close every round
     const unsigned tb = (B + 31) / 32;
     for (uint32_t round = 0;; round++) {
         if (round > nmax) {  // every round with edges left links at least its first draw
@@ -500,7 +507,7 @@ int shrink_tasks(cac_ctx *ctx, const std::vector<ShrinkTask> &tasks, void *scrat
 
 // Scratch of shrink_big for B trials of one graph.
 uint64_t shrink_big_scratch(uint32_t n, uint64_t m, uint32_t B) {
-    return shrink_task_scratch(n, m) * B + align_up(sizeof(BigTrial) * B) + align_up(sizeof(BigState) * B) +
+    return shrink_task_scratch(n, m, 0) * B + align_up(sizeof(BigTrial) * B) + align_up(sizeof(BigState) * B) +
            align_up(16);
 }
 
@@ -509,7 +516,7 @@ int shrink_big(cac_ctx *ctx, const cac_graph *g, uint32_t target, uint32_t B, co
     std::vector<ShrinkTask> tasks(B);
     for (uint32_t b = 0; b < B; b++)
         tasks[b] = ShrinkTask{g->u, g->v, g->w, false, g->m, g->n, target, k0[b], idx[b], 1,
-                              d_lab + (size_t)b * g->n, d_kout + b};
+                              d_lab + (size_t)b * g->n, d_kout + b, 0};
     return shrink_tasks(ctx, tasks, scratch);
 }
 

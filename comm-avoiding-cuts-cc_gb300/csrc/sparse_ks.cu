@@ -226,7 +226,7 @@ int sparse_phase(cac_ctx *ctx, KsEngine &eng, std::vector<SparseNode> nodes) {
                 const SparseNode &nd = *children[i].src;
                 tasks.push_back(ShrinkTask{nd.a, nd.b, nd.w, nd.w64, nd.m, nd.N, children[i].target, nd.k0, nd.idx,
                                            1 + children[i].h, lab.as<uint32_t>() + lo,
-                                           kout.as<uint32_t>() + (i - c0)});
+                                           kout.as<uint32_t>() + (i - c0), 0});
                 lo += nd.N;
             }
             if ((st = scr.get(shrink_tasks_scratch(tasks))) != CAC_OK) break;

@@ -17,6 +17,8 @@
  *                         driven as in src/executables/square_root.cpp:22-40
  *   cac_mincut_trials     the per-rank trial loop of SquareRootCut::runLowConcurrencyMaster
  *                         (src/SquareRootCut.cpp:127-138), one value per trial
+ *   cac_mincut_group_trials  one trial of SquareRootCut::participateInGroup
+ *                         (src/SquareRootCut.cpp:188-298) per group, one value per group
  *   cac_ks_dense          comincut::minimum_cut on a dense graph (src/karger-stein/co_mincut.h:491-497)
  *                         for one counter-addressed trial
  *   cac_exact_cut         comincut::deterministic_minimum_cut (src/karger-stein/co_mincut.h:529-541)
@@ -175,9 +177,13 @@ typedef struct {
                                  reference reports the trials' minimum alone, so this differs only
                                  when every trial missed a minimum cut around one vertex) */
     uint32_t trials_per_rank; /* the CSV `trials` column: ceil(total / virtual_ranks) */
-    uint32_t total_trials;    /* trials executed: virtual_ranks * trials_per_rank */
+    uint32_t total_trials;    /* trials executed: virtual_ranks * trials_per_rank, or the group
+                                 count in the group variant */
     uint32_t intermediate;    /* t = min(n, ceil(2 sqrt(m) + 1)) */
-    uint32_t high_concurrency;/* 1 when the reference would have used its group variant */
+    uint32_t high_concurrency;/* 1: the group variant ran (virtual_ranks >= 2 * trials, the
+                                 reference's SquareRootCut::lowConcurrency, .cpp:11-13): the
+                                 ranks form groups of the largest power of two not above
+                                 virtual_ranks / trials, each group one trial, trials_per_rank 1 */
     float device_ms;
 } cac_mincut_result;
 
@@ -212,6 +218,12 @@ int cac_mincut_trials(cac_ctx *ctx, const cac_graph *g, uint32_t seed, uint32_t 
  * each trial's cut to cuts_host[i]: the loop of comincut::minimum_cut_trials (co_mincut.h:315-342)
  * with every trial's value kept. */
 int cac_karger_stein_trials(cac_ctx *ctx, const cac_graph *g, uint32_t seed, uint32_t trials, uint64_t *cuts_host);
+/* Group trials 0 .. groups - 1 of the group variant, each group's cut to cuts_host[g]: Stage 1
+ * contracts to t vertices in rounds of floor(n^1.05) weighted draws
+ * (WeightedIteratedSparseSampling, .hpp:66-67) with key (seed + g, 0, 1, 0), and two Karger-Stein
+ * recursions from the contracted graph (recursive_contract.cpp:45-83 with two trials) take
+ * keys (seed + g, 0 | 1, 1 + level, 0); the group's value is the smaller. */
+int cac_mincut_group_trials(cac_ctx *ctx, const cac_graph *g, uint32_t seed, uint32_t groups, uint64_t *cuts_host);
 /* One Karger-Stein trial (virtual rank, trial index) on a dense symmetric n x n host matrix. */
 int cac_ks_dense(cac_ctx *ctx, uint32_t n, const uint64_t *mat_host, uint32_t seed, uint32_t rank, uint32_t trial,
                  uint64_t *cut);

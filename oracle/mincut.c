@@ -508,8 +508,15 @@ static int is_dense(uint32_t n, uint64_t m) {
 
 /* Stage 1 rounds on an edge list with u64 weights and key `key`: labels (rank of the smallest
  * member) to lab, returns the vertex count left */
+static uint32_t stage1_dpr(uint32_t n, uint64_t m, const uint32_t *u, const uint32_t *v, const uint64_t *w,
+                           uint32_t target, const uint64_t key[4], uint32_t *lab, uint32_t dpr);
 static uint32_t stage1(uint32_t n, uint64_t m, const uint32_t *u, const uint32_t *v, const uint64_t *w,
                        uint32_t target, const uint64_t key[4], uint32_t *lab) {
+    return stage1_dpr(n, m, u, v, w, target, key, lab, 0);
+}
+/* dpr: draws per round (0: the round's vertex count) */
+static uint32_t stage1_dpr(uint32_t n, uint64_t m, const uint32_t *u, const uint32_t *v, const uint64_t *w,
+                           uint32_t target, const uint64_t key[4], uint32_t *lab, uint32_t dpr) {
     uint32_t *p = (uint32_t *)malloc(sizeof(uint32_t) * (n ? n : 1));
     for (uint32_t i = 0; i < n; i++) p[i] = i;
     uint32_t count = n;
@@ -521,7 +528,7 @@ static uint32_t stage1(uint32_t n, uint64_t m, const uint32_t *u, const uint32_t
             pre[e] = W;
         }
         if (W == 0) break;
-        uint32_t start = count;
+        uint32_t start = dpr ? dpr : count;
         for (uint64_t d = 0; d < start && count > target; d++) {
             uint64_t y = mulhi64(orc_draw64(key, round, d), W);
             uint64_t lo = 0, hi = m - 1;
@@ -657,6 +664,57 @@ uint64_t orc_mincut_trial(uint32_t n, uint64_t m, const uint32_t *u, const uint3
     return r;
 }
 
+/* ------------------------------------------------------------------ the group variant
+ * SquareRootCut's high-concurrency variant (SquareRootCut.cpp:188-298), chosen when the virtual
+ * ranks are at least twice the trial count: group_size = 2^floor(log2(p / T)) ranks share one
+ * trial, so there are p / group_size trials. libcac's group trial g: WeightedIteratedSparseSampling
+ * ::shrink (WeightedIteratedSparseSampling.cpp:4-24, edgesToSamplePerProcessor .hpp:66-84) as
+ * Stage 1 rounds of a fixed floor(n^1.05) weighted draws each (not the round's vertex count),
+ * contracted in draw order until t vertices remain, key (seed + g, 0, 1, 0); its contracted graph
+ * (dense, or a sparse root above the dense limit); then, as parallel_cut(.., 2, ..) runs two
+ * recursive contractions of the group's graph (recursive_contract.cpp:45-83), two Karger-Stein
+ * recursions from that root, with keys (seed + g, 0, 1 + h, 0) and (seed + g, 1, 1 + h, 0). The
+ * trial's value is the minimum of both and the root's minimum weighted degree. */
+uint32_t orc_group_count(uint32_t ranks, uint32_t trials) {
+    uint32_t per = trials ? ranks / trials : ranks;
+    uint32_t size = 1;
+    while (size * 2 <= per) size *= 2;
+    return ranks / size;
+}
+
+uint32_t orc_group_draws(uint32_t n) { return (uint32_t)powf((float)n, 1.0f + 0.1f / 2.0f); }
+
+uint64_t orc_mincut_group_trial(uint32_t n, uint64_t m, const uint32_t *u, const uint32_t *v, const uint32_t *w,
+                                uint32_t seed, uint32_t group) {
+    if (n < 2) return U64MAX;
+    uint32_t t = orc_intermediate_size(n, m);
+    uint64_t *w64 = widen(m, w);
+    uint32_t *lab = (uint32_t *)malloc(sizeof(uint32_t) * n);
+    uint64_t key[4] = {(uint32_t)(seed + group), 0, 1, 0};
+    uint32_t k = t < n ? stage1_dpr(n, m, u, v, w64, t, key, lab, orc_group_draws(n)) : n;
+    sgraph root;
+    merge_child(m, u, v, w64, t < n ? lab : NULL, k, &root);
+    uint64_t r = U64MAX;
+    if (k < 2 || root.m == 0) {
+        r = 0;
+    } else if (t <= g_dense_limit) {
+        uint64_t *mat = dense_of(&root);
+        for (uint32_t j = 0; j < 2; j++) {
+            uint64_t c = orc_ks_dense(k, mat, seed, group, j);
+            if (c < r) r = c;
+        }
+        free(mat);
+    } else {
+        for (uint32_t j = 0; j < 2; j++) {
+            uint64_t c = sparse_root(k, root.m, root.a, root.b, root.w, seed + group, j);
+            if (c < r) r = c;
+        }
+    }
+    sg_free(&root);
+    free(lab); free(w64);
+    return r;
+}
+
 /* one trial of plain Karger-Stein on the whole graph (the karger_stein executable): the root is
  * dense (the n x n matrix) or sparse (the input edge list as given) by the rule above */
 uint64_t orc_ks_trial(uint32_t n, uint64_t m, const uint32_t *u, const uint32_t *v, const uint32_t *w, uint32_t seed,
@@ -683,7 +741,8 @@ uint64_t orc_square_root(uint32_t n, uint64_t m, const uint32_t *u, const uint32
                          double p, uint32_t seed, uint32_t ranks, uint32_t *per_rank_out) {
     if (ranks == 0) ranks = 1;
     double total = orc_number_of_trials(n, m, p);
-    uint32_t per = (uint32_t)ceil(total / ranks);
+    const int high = (double)ranks >= 2.0 * total; /* SquareRootCut::lowConcurrency (SquareRootCut.cpp:11-13) */
+    uint32_t per = high ? 1 : (uint32_t)ceil(total / ranks);
     if (per_rank_out) *per_rank_out = per;
     /* the answer also takes the graph's minimum weighted degree (a single-vertex cut): libcac's
        square_root reports min(that, every trial), so a query whose trials all contracted the
@@ -693,6 +752,14 @@ uint64_t orc_square_root(uint32_t n, uint64_t m, const uint32_t *u, const uint32
     uint64_t best = U64MAX;
     for (uint32_t i = 0; i < n; i++) if (deg[i] < best) best = deg[i];
     free(deg);
+    if (high) {
+        uint32_t groups = orc_group_count(ranks, (uint32_t)total);
+        for (uint32_t g = 0; g < groups; g++) {
+            uint64_t c = orc_mincut_group_trial(n, m, u, v, w, seed, g);
+            if (c < best) best = c;
+        }
+        return best;
+    }
     for (uint32_t r = 0; r < ranks; r++)
         for (uint32_t i = 0; i < per; i++) {
             uint64_t c = orc_mincut_trial(n, m, u, v, w, seed, r, i);

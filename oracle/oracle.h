@@ -92,6 +92,11 @@ uint64_t orc_ks_dense(uint32_t n, const uint64_t *mat, uint32_t seed, uint32_t r
 uint64_t orc_ks_trial(uint32_t n, uint64_t m, const uint32_t *u, const uint32_t *v, const uint32_t *w, uint32_t seed,
                       uint32_t trial);
 void orc_set_dense_limit(uint32_t n);
+/* the high-concurrency group variant: trial count for (ranks, trials) and one group's trial */
+uint32_t orc_group_count(uint32_t ranks, uint32_t trials);
+uint32_t orc_group_draws(uint32_t n);
+uint64_t orc_mincut_group_trial(uint32_t n, uint64_t m, const uint32_t *u, const uint32_t *v, const uint32_t *w,
+                                uint32_t seed, uint32_t group);
 /* Only Stage 1+2: contract to t vertices and emit the dense t' x t' matrix (returns t';
  * `mat_out` must hold n*n entries or NULL to only return t'). */
 uint32_t orc_shrink_to_dense(uint32_t n, uint64_t m, const uint32_t *u, const uint32_t *v, const uint32_t *w,

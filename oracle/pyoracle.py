@@ -47,6 +47,13 @@ def lib():
         L.orc_ks_trial.restype = ctypes.c_uint64
         L.orc_set_dense_limit.argtypes = [ctypes.c_uint32]
         L.orc_set_dense_limit.restype = None
+        L.orc_group_count.argtypes = [ctypes.c_uint32, ctypes.c_uint32]
+        L.orc_group_count.restype = ctypes.c_uint32
+        L.orc_group_draws.argtypes = [ctypes.c_uint32]
+        L.orc_group_draws.restype = ctypes.c_uint32
+        L.orc_mincut_group_trial.argtypes = [ctypes.c_uint32, ctypes.c_uint64, _u32p, _u32p, _u32p, ctypes.c_uint32,
+                                             ctypes.c_uint32]
+        L.orc_mincut_group_trial.restype = ctypes.c_uint64
         L.orc_exact_mincut_noi.argtypes = [ctypes.c_uint32, ctypes.c_uint64, _u32p, _u32p, _u32p]
         L.orc_exact_mincut_noi.restype = ctypes.c_uint64
         L.orc_intermediate_size.argtypes = [ctypes.c_uint32, ctypes.c_uint64]
@@ -213,6 +220,21 @@ def karger_stein(n, u, v, w, p, seed, threads=1):
     else:
         vals = [ks_trial(n, u, v, w, seed, i) for i in range(trials)]
     return min(vals), trials
+
+
+def group_count(ranks, trials):
+    """Trials of SquareRootCut's high-concurrency variant: ranks / 2^floor(log2(ranks / trials))."""
+    return int(lib().orc_group_count(ranks, trials))
+
+
+def group_draws(n):
+    return int(lib().orc_group_draws(n))
+
+
+def mincut_group_trial(n, u, v, w, seed, group):
+    """One trial of the high-concurrency group variant (see oracle/mincut.c)."""
+    u, v, w = _c32(u), _c32(v), _c32(w)
+    return int(lib().orc_mincut_group_trial(n, len(u), _p32(u), _p32(v), _p32(w), seed, group))
 
 
 def ks_target(n):

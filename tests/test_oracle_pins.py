@@ -231,3 +231,19 @@ def test_approx_level_count_follows_rank_slices():
     assert O.approx_cut_stream(n, u, v, w, 0.9, 0, 4) == (1, 0)
     # one rank: ceil(ln 103) = 5 levels; the cycle's cut (2) disconnects by level 5
     assert O.approx_cut(n, u, v, w, 0.9, 0, 1)[1] >= 1
+
+
+def test_group_variant_layout_and_answer():
+    """SquareRootCut's group variant (SquareRootCut.cpp:188-298): with p >= 2T ranks the groups
+    have the largest power-of-two size not above p / T (integer division), p / size groups in
+    all, one trial each; Stage 1 draws floor(n0^(1 + 0.1 / 2)) edges per round in float
+    (WeightedIteratedSparseSampling.hpp:66-67). The answer is the smallest group value (or the
+    minimum weighted degree), which is the exact cut on these graphs."""
+    assert [O.group_count(p, t) for p, t in [(24, 6), (100, 7), (12, 6), (13, 6), (1024, 3)]] == [6, 12, 6, 6, 4]
+    assert [O.group_draws(n) for n in (2, 100, 1000, 4096)] == [int(np.float32(n) ** np.float32(1.05))
+                                                               for n in (2, 100, 1000, 4096)]
+    n, u, v, w = make_graph({"kind": "er", "n": 120, "p": 0.15, "seed": 5, "wmax": 30})
+    T = O.number_of_trials(n, len(u), 0.9)
+    cut, per = O.square_root(n, u, v, w, 0.9, 2, ranks=2 * T)
+    groups = [O.mincut_group_trial(n, u, v, w, 2, g) for g in range(O.group_count(2 * T, T))]
+    assert per == 1 and cut <= min(groups) and cut == O.exact_mincut_noi(n, u, v, w)
