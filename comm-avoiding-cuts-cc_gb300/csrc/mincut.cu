@@ -91,8 +91,9 @@ struct TaskDesc {
 };
 
 struct LeafDesc {
-    const void *mat;  // u32 entries when `small`, else u64
+    const void *mat;          // u32 entries when `small`, else u64
     uint64_t *cut;
+    const uint64_t *rowsum;   // the N row sums written with the matrix (a quotient's), or null
     uint32_t N;
     uint32_t small;  // entries fit in 32 bits
 };
@@ -1007,10 +1008,34 @@ __global__ void __launch_bounds__(32) sw_leaf_kernel(const LeafDesc *__restrict_
     const LeafDesc L = leaves[blockIdx.x];
     const uint32_t N = L.N, H = N / 2;
     const int lane = threadIdx.x;
-    for (uint32_t x = lane; x < N * H; x += 32) {
-        const uint32_t i = x / H, d = x - i * H + 1;
-        const uint32_t j = i + d < N ? i + d : i + d - N;
-        M[x] = __ldg(reinterpret_cast<const Tm *>(L.mat) + (size_t)i * ld_of(N) + j);
+    // circulant half: lane owns offsets d = lane + 1 and lane + 33 (H <= 64) of every row; eight
+    // rows per pass keep sixteen independent loads in flight
+    {
+        const Tm *src = reinterpret_cast<const Tm *>(L.mat);
+        const uint64_t ldN = ld_of(N);
+        const uint32_t d0 = (uint32_t)lane + 1, d1 = (uint32_t)lane + 33;
+        const bool has0 = d0 <= H, has1 = d1 <= H;
+        for (uint32_t i0 = 0; i0 < N; i0 += 8) {
+            Tm a0[8], a1[8];
+#pragma unroll
+            for (int r = 0; r < 8; r++) {
+                const uint32_t i = i0 + r;
+                const Tm *row = src + (uint64_t)i * ldN;
+                uint32_t j0 = i + d0, j1 = i + d1;
+                j0 = j0 >= N ? j0 - N : j0;
+                j1 = j1 >= N ? j1 - N : j1;
+                a0[r] = (i < N && has0) ? __ldg(row + j0) : (Tm)0;
+                a1[r] = (i < N && has1) ? __ldg(row + j1) : (Tm)0;
+            }
+#pragma unroll
+            for (int r = 0; r < 8; r++) {
+                const uint32_t i = i0 + r;
+                if (i < N) {
+                    if (has0) M[i * H + d0 - 1] = a0[r];
+                    if (has1) M[i * H + d1 - 1] = a1[r];
+                }
+            }
+        }
     }
     for (uint32_t x = lane; x < 128; x += 32) uf[x] = (uint8_t)x;
     __syncwarp();
@@ -1018,15 +1043,21 @@ __global__ void __launch_bounds__(32) sw_leaf_kernel(const LeafDesc *__restrict_
 #pragma unroll
     for (int s = 0; s < 4; s++)
         if ((uint32_t)(lane + 32 * s) < N) active |= 1u << s;
-    // lambda starts at the minimum weighted degree (a cut of the leaf)
+    // lambda starts at the minimum weighted degree (a cut of the leaf): the row sums that came with
+    // the matrix, else summed here (row i's own half, then the entries (i - e, i) stored in the
+    // rows before it)
     uint64_t deg_min = kU64Max;
 #pragma unroll
     for (int s = 0; s < 4; s++) {
         if ((active >> s) & 1u) {
             const uint32_t i = lane + 32 * s;
             uint64_t d = 0;
-            for (uint32_t x = 0; x < N; x++)
-                if (x != i) d += (uint64_t)M[cpos(i, x, N, H)];
+            if (L.rowsum) {
+                d = __ldg(L.rowsum + i);
+            } else {
+                for (uint32_t e = 1; e <= H; e++) d += (uint64_t)M[i * H + e - 1];
+                for (uint32_t e = 1; e + H < N; e++) d += (uint64_t)M[(i >= e ? i - e : i + N - e) * H + e - 1];
+            }
             deg_min = d < deg_min ? d : deg_min;
         }
     }
@@ -1087,12 +1118,32 @@ __global__ void __launch_bounds__(32) sw_leaf_kernel(const LeafDesc *__restrict_
             if (lane == 0) npairs = base + __popc(bal);
             __syncwarp();
         }
-        const uint32_t np = npairs;
-        for (uint32_t q = 0; q < np && cnt > 1; q++) {
-            uint32_t x = pairs[q] >> 8, y = pairs[q] & 255u;
-            while (uf[x] != x) x = uf[x];
-            while (uf[y] != y) y = uf[y];
-            if (x == y) continue;  // already merged (warp-uniform)
+        // the merges, in list order: lane 0 joins the pairs' slots (union-find with path halving)
+        // and rewrites the list as the (root, root) merges actually made
+        if (lane == 0) {
+            const uint32_t np = npairs;
+            uint32_t made = 0;
+            for (uint32_t q = 0; q < np && cnt - made > 1; q++) {
+                uint32_t x = pairs[q] >> 8, y = pairs[q] & 255u;
+                while (uf[x] != x) {
+                    uf[x] = uf[uf[x]];
+                    x = uf[x];
+                }
+                while (uf[y] != y) {
+                    uf[y] = uf[uf[y]];
+                    y = uf[y];
+                }
+                if (x == y) continue;  // already merged
+                uf[y] = (uint8_t)x;
+                pairs[made++] = (x << 8) | y;
+            }
+            npairs = made;
+        }
+        __syncwarp();
+        const uint32_t nm = npairs;
+        if (cnt - nm <= 1) break;  // one vertex left: lambda is the leaf's cut, no matrix to update
+        for (uint32_t q = 0; q < nm; q++) {
+            const uint32_t x = pairs[q] >> 8, y = pairs[q] & 255u;
             // merge y into x: entry (x, v) += entry (y, v) for every other active v
 #pragma unroll
             for (int s = 0; s < 4; s++) {
@@ -1104,10 +1155,8 @@ __global__ void __launch_bounds__(32) sw_leaf_kernel(const LeafDesc *__restrict_
             }
             if ((uint32_t)lane == (y & 31u)) active &= ~(1u << (y >> 5));
             __syncwarp();
-            if (lane == 0) uf[y] = (uint8_t)x;
-            __syncwarp();
-            cnt--;
         }
+        cnt -= nm;
     }
     if (lane == 0) atomicMin((unsigned long long *)L.cut, (unsigned long long)lambda);
 }
@@ -1287,7 +1336,7 @@ int KsEngine::step() {
     for (const KNode &nd : nodes_) {
         if (nd.N <= 128) {
             if (nd.N >= 2) {
-                leaves.push_back(LeafDesc{nd.mat, nd.cut, nd.N, nd.small});
+                leaves.push_back(LeafDesc{nd.mat, nd.cut, nd.pre, nd.N, nd.small});
             }
             consumed.push_back(nd.buf);
             outstanding[nd.query]--;
@@ -2219,7 +2268,7 @@ int exact_small(cac_ctx *ctx, uint32_t n, const uint64_t *mat_host, uint64_t *cu
     CAC_TRY(d_cuts.ensure(8));
     CAC_CUDA_TRY(cudaMemcpyAsync(buf.p, dev.data(), dev.size(), cudaMemcpyHostToDevice, s));
     fill_u64<<<1, 32, 0, s>>>(d_cuts.as<uint64_t>(), 1, kU64Max);
-    std::vector<LeafDesc> leaves{LeafDesc{buf.p, d_cuts.as<uint64_t>(), n, small}};
+    std::vector<LeafDesc> leaves{LeafDesc{buf.p, d_cuts.as<uint64_t>(), nullptr, n, small}};
     CAC_TRY(upload(ctx, d_leaf, leaves));
     if (small) {
         const size_t sm = leaf_smem(n, true);
