@@ -22,7 +22,8 @@
 //                                its label's slot of the output row in shared memory (integer
 //                                atomics); a warp per output row, or a CTA's 8 warps on one row at
 //                                large N (autotuned per size bucket)
-//              sw_leaf_kernel    one warp per leaf (n <= 128): Stoer-Wagner maximum-adjacency
+//              sw_leaf_kernel    one 128-thread CTA per leaf (n <= 128), a thread per vertex:
+//                                Stoer-Wagner maximum-adjacency
 //                                phases with Nagamochi-Ono-Ibaraki contractions on the matrix held
 //                                in shared memory (circulant half storage); atomicMin into the
 //                                trial's cut
@@ -957,18 +958,24 @@ __global__ void __launch_bounds__(256) quotient_bulk_kernel(const TaskDesc *__re
     }
 }
 
-// Exact minimum cut of one leaf (n <= 128) by one warp: maximum-adjacency orderings as in the
-// reference's Stoer-Wagner base case (co_mincut_base_case.hpp:52-144), with the Nagamochi-Ono-
-// Ibaraki contraction rule (Nagamochi & Ibaraki 1992; Nagamochi, Ono & Ibaraki 1994): when vertex
-// w's key reaches q >= lambda while vertex v is scanned, then lambda(v, w) >= q, so the edge (v, w)
-// can be contracted without losing any cut below lambda, the best cut value found so far (initially
-// the leaf's minimum weighted degree). Every ordering contracts all such certified edges plus the
-// last two vertices (the cut of the phase updates lambda), so far fewer orderings are needed than
-// the n - 1 of plain Stoer-Wagner; the returned value is the exact minimum cut of the leaf.
-//   lane l owns vertices l, l+32, l+64, l+96; argmax by warp reduction of (key << 8 | 255 - v),
-//   ties to the smallest vertex; keys stay below 2^56 (total graph weight checked on the host).
-//   The full matrix sits in shared memory so that a row read is conflict-free; contractions use a
-//   small union-find over vertex slots in shared memory.
+// Exact minimum cut of one leaf (n <= 128) by one CTA of 128 threads: maximum-adjacency orderings
+// as in the reference's Stoer-Wagner base case (co_mincut_base_case.hpp:52-144), with the
+// Nagamochi-Ono-Ibaraki contraction rule (Nagamochi & Ibaraki 1992; Nagamochi, Ono & Ibaraki
+// 1994): when vertex w's key reaches q >= lambda while vertex v is scanned, then lambda(v, w) >= q,
+// so the edge (v, w) can be contracted without losing any cut below lambda, the best cut value found
+// so far (initially the leaf's minimum weighted degree). Every ordering contracts all such
+// certified edges plus the last two vertices (the cut of the phase updates lambda), so far fewer
+// orderings are needed than the n - 1 of plain Stoer-Wagner; the returned value is the exact
+// minimum cut of the leaf.
+//   Thread v owns vertex v. A step of an ordering is one warp argmax of (key, smallest vertex), a
+//   cross-warp maximum through a double-buffered shared word per warp (one barrier per step), and
+//   one key update per thread from the scanned vertex's row. Every certified edge and the pair
+//   (second to last, last) joins a vertex to one scanned before it, so when all but the first
+//   vertex of the ordering are so joined the leaf contracts to one vertex and the ordering's result
+//   is final: a barrier count decides this without building the contraction (the usual case:
+//   Karger-Stein leaves of 128 vertices mostly finish in one ordering). Otherwise the pairs are
+//   joined by a union-find over vertex slots and the matrix entries are merged pair by pair.
+//   Keys stay below 2^56 (total graph weight checked on the host); u32 matrices keep 32-bit keys.
 __device__ __forceinline__ uint64_t warp_min_u64(uint64_t x) {
     const uint32_t hi = (uint32_t)(x >> 32);
     const uint32_t top = __reduce_min_sync(0xffffffffu, hi);
@@ -998,129 +1005,132 @@ __device__ __forceinline__ void cset(Tm *M, uint32_t i, uint32_t j, uint32_t N, 
     }
 }
 
+__device__ __forceinline__ uint64_t warp_max_u64(uint64_t x) {
+    const uint32_t hi = (uint32_t)(x >> 32);
+    const uint32_t top = __reduce_max_sync(0xffffffffu, hi);
+    const uint32_t lo = __reduce_max_sync(0xffffffffu, hi == top ? (uint32_t)x : 0u);
+    return ((uint64_t)top << 32) | lo;
+}
+
+constexpr uint32_t kLeafThreads = 128;
+
 template <typename Tm>
-__global__ void __launch_bounds__(32) sw_leaf_kernel(const LeafDesc *__restrict__ leaves) {
+__global__ void __launch_bounds__(kLeafThreads) sw_leaf_kernel(const LeafDesc *__restrict__ leaves) {
     extern __shared__ __align__(16) unsigned char dsm[];
     Tm *M = reinterpret_cast<Tm *>(dsm);
     __shared__ uint8_t uf[128];
     __shared__ uint32_t pairs[128];
     __shared__ uint32_t npairs;
+    __shared__ __align__(16) uint64_t wbest[2][4];
     const LeafDesc L = leaves[blockIdx.x];
     const uint32_t N = L.N, H = N / 2;
-    const int lane = threadIdx.x;
-    // circulant half: lane owns offsets d = lane + 1 and lane + 33 (H <= 64) of every row; eight
-    // rows per pass keep sixteen independent loads in flight
+    const uint32_t v = threadIdx.x, lane = v & 31u, warp = v >> 5;
+    // circulant half: thread v loads offset d = v % 64 + 1 of every second row (rows v / 64,
+    // v / 64 + 2, ...), eight rows per pass in flight
     {
         const Tm *src = reinterpret_cast<const Tm *>(L.mat);
         const uint64_t ldN = ld_of(N);
-        const uint32_t d0 = (uint32_t)lane + 1, d1 = (uint32_t)lane + 33;
-        const bool has0 = d0 <= H, has1 = d1 <= H;
-        for (uint32_t i0 = 0; i0 < N; i0 += 8) {
-            Tm a0[8], a1[8];
+        const uint32_t d = (v & 63u) + 1, r0 = v >> 6;
+        const bool has = d <= H;
+        for (uint32_t i0 = r0; i0 < N; i0 += 16) {
+            Tm a[8];
 #pragma unroll
             for (int r = 0; r < 8; r++) {
-                const uint32_t i = i0 + r;
-                const Tm *row = src + (uint64_t)i * ldN;
-                uint32_t j0 = i + d0, j1 = i + d1;
-                j0 = j0 >= N ? j0 - N : j0;
-                j1 = j1 >= N ? j1 - N : j1;
-                a0[r] = (i < N && has0) ? __ldg(row + j0) : (Tm)0;
-                a1[r] = (i < N && has1) ? __ldg(row + j1) : (Tm)0;
+                const uint32_t i = i0 + 2 * r;
+                uint32_t j = i + d;
+                j = j >= N ? j - N : j;
+                a[r] = (i < N && has) ? __ldg(src + (uint64_t)i * ldN + j) : (Tm)0;
             }
 #pragma unroll
             for (int r = 0; r < 8; r++) {
-                const uint32_t i = i0 + r;
-                if (i < N) {
-                    if (has0) M[i * H + d0 - 1] = a0[r];
-                    if (has1) M[i * H + d1 - 1] = a1[r];
-                }
+                const uint32_t i = i0 + 2 * r;
+                if (i < N && has) M[i * H + d - 1] = a[r];
             }
         }
     }
-    for (uint32_t x = lane; x < 128; x += 32) uf[x] = (uint8_t)x;
-    __syncwarp();
-    uint32_t active = 0;
-#pragma unroll
-    for (int s = 0; s < 4; s++)
-        if ((uint32_t)(lane + 32 * s) < N) active |= 1u << s;
+    uf[v] = (uint8_t)v;
+    bool active = v < N;
+    __syncthreads();
     // lambda starts at the minimum weighted degree (a cut of the leaf): the row sums that came with
-    // the matrix, else summed here (row i's own half, then the entries (i - e, i) stored in the
-    // rows before it)
-    uint64_t deg_min = kU64Max;
-#pragma unroll
-    for (int s = 0; s < 4; s++) {
-        if ((active >> s) & 1u) {
-            const uint32_t i = lane + 32 * s;
-            uint64_t d = 0;
-            if (L.rowsum) {
-                d = __ldg(L.rowsum + i);
-            } else {
-                for (uint32_t e = 1; e <= H; e++) d += (uint64_t)M[i * H + e - 1];
-                for (uint32_t e = 1; e + H < N; e++) d += (uint64_t)M[(i >= e ? i - e : i + N - e) * H + e - 1];
-            }
-            deg_min = d < deg_min ? d : deg_min;
+    // the matrix, else summed here (row v's own half, then the entries (v - e, v) stored in the rows
+    // before it)
+    uint64_t deg = kU64Max;
+    if (active) {
+        if (L.rowsum) {
+            deg = __ldg(L.rowsum + v);
+        } else {
+            deg = 0;
+            for (uint32_t e = 1; e <= H; e++) deg += (uint64_t)M[v * H + e - 1];
+            for (uint32_t e = 1; e + H < N; e++) deg += (uint64_t)M[(v >= e ? v - e : v + N - e) * H + e - 1];
         }
     }
-    uint64_t lambda = warp_min_u64(deg_min);
-    uint32_t cnt = N;
+    {
+        const uint64_t wm = warp_min_u64(deg);
+        if (lane == 0) wbest[1][warp] = wm;  // the first step writes wbest[0]
+    }
+    __syncthreads();
+    uint64_t lambda = wbest[1][0];
+    for (int w = 1; w < 4; w++) lambda = wbest[1][w] < lambda ? wbest[1][w] : lambda;
+    using Kt = typename std::conditional<sizeof(Tm) == 4, uint32_t, uint64_t>::type;
+    uint32_t cnt = N, par = 0;
     while (cnt > 1) {
-        uint64_t key[4] = {0, 0, 0, 0};
-        uint32_t in_a = 0;
-        uint32_t mark[4] = {0xFFu, 0xFFu, 0xFFu, 0xFFu};  // vertex to contract into, 0xFF: none
+        Kt key = 0;
+        const Kt lam = lambda > (uint64_t)(Kt)~(Kt)0 ? (Kt)~(Kt)0 : (Kt)lambda;
+        bool in_a = false;
+        uint32_t mark = 0xFFu;  // vertex to contract into, 0xFF: none
         uint32_t prev = 0, last = 0;
         uint64_t cut_phase = 0;
         for (uint32_t step = 0; step < cnt; step++) {
-            uint64_t local = 0;
-#pragma unroll
-            for (int s = 0; s < 4; s++) {
-                if (((active & ~in_a) >> s) & 1u) {
-                    const uint64_t cand = (key[s] << 8) | (uint64_t)(255 - (lane + 32 * s));
-                    local = cand > local ? cand : local;
-                }
+            const bool elig = active && !in_a;
+            uint64_t wb;  // this warp's best as (key << 8 | 255 - vertex), 0 for none
+            if constexpr (sizeof(Tm) == 4) {
+                const uint32_t top = __reduce_max_sync(0xffffffffu, elig ? key : 0u);
+                const uint32_t vmin = __reduce_min_sync(0xffffffffu, (elig && key == top) ? v : 255u);
+                wb = vmin == 255u ? 0 : (((uint64_t)top << 8) | (uint64_t)(255u - vmin));
+            } else {
+                wb = warp_max_u64(elig ? ((key << 8) | (uint64_t)(255u - v)) : 0);
             }
-            const uint32_t hi = (uint32_t)(local >> 32);
-            const uint32_t top = __reduce_max_sync(0xffffffffu, hi);
-            const uint32_t lo = __reduce_max_sync(0xffffffffu, hi == top ? (uint32_t)local : 0u);
-            local = ((uint64_t)top << 32) | lo;
-            const uint32_t sv = 255u - (uint32_t)(local & 255u);
-            if (step + 1 == cnt) {
-                last = sv;
-                cut_phase = local >> 8;
+            if (lane == 0) wbest[par][warp] = wb;
+            __syncthreads();
+            const ulonglong2 b01 = *reinterpret_cast<const ulonglong2 *>(&wbest[par][0]);
+            const ulonglong2 b23 = *reinterpret_cast<const ulonglong2 *>(&wbest[par][2]);
+            par ^= 1u;
+            const uint64_t m01 = b01.x > b01.y ? b01.x : b01.y, m23 = b23.x > b23.y ? b23.x : b23.y;
+            const uint64_t best = m01 > m23 ? m01 : m23;
+            const uint32_t sv = 255u - (uint32_t)(best & 255u);
+            if (sv >= N) {  // no candidate: cannot happen (cnt - step vertices are unscanned)
+                cut_phase = kU64Max;
                 break;
             }
-            if ((uint32_t)lane == (sv & 31u)) in_a |= 1u << (sv >> 5);
+            if (step + 1 == cnt) {
+                last = sv;
+                cut_phase = best >> 8;
+                break;
+            }
+            in_a = in_a || v == sv;
             prev = sv;
-#pragma unroll
-            for (int s = 0; s < 4; s++) {
-                if (((active & ~in_a) >> s) & 1u) {
-                    const uint64_t c = (uint64_t)M[cpos(sv, lane + 32 * s, N, H)];
-                    if (c) {
-                        key[s] += c;
-                        if (key[s] >= lambda) mark[s] = sv;  // lambda(sv, v) >= key: contractible
-                    }
-                }
+            if (active && !in_a) {
+                const Kt c = (Kt)M[cpos(sv, v, N, H)];
+                key += c;
+                if (c && key >= lam) mark = sv;  // lambda(sv, v) >= key: contractible
             }
         }
+        if (cut_phase == kU64Max) break;
         lambda = cut_phase < lambda ? cut_phase : lambda;
-        // contraction list: (prev, last), then every certified edge (v, mark[v])
-        if (lane == 0) {
+        // one vertex left when every vertex but the first of the ordering is joined to an earlier one
+        const uint32_t linked = (uint32_t)__syncthreads_count(active && (mark != 0xFFu || v == last));
+        if (linked + 1 >= cnt) break;
+        // contraction list: (prev, last), then every certified edge (mark[v], v)
+        if (v == 0) {
             pairs[0] = (prev << 8) | last;
             npairs = 1;
         }
-        __syncwarp();
-#pragma unroll
-        for (int s = 0; s < 4; s++) {
-            const bool has = ((active >> s) & 1u) && mark[s] != 0xFFu;
-            const uint32_t bal = __ballot_sync(0xffffffffu, has);
-            const uint32_t base = npairs;
-            if (has) pairs[base + __popc(bal & ((1u << lane) - 1u))] = (mark[s] << 8) | (uint32_t)(lane + 32 * s);
-            __syncwarp();
-            if (lane == 0) npairs = base + __popc(bal);
-            __syncwarp();
-        }
-        // the merges, in list order: lane 0 joins the pairs' slots (union-find with path halving)
-        // and rewrites the list as the (root, root) merges actually made
-        if (lane == 0) {
+        __syncthreads();
+        if (active && mark != 0xFFu) pairs[atomicAdd(&npairs, 1u)] = (mark << 8) | v;
+        __syncthreads();
+        // thread 0 joins the pairs' slots (union-find with path halving) and rewrites the list as
+        // the (root, root) merges actually made
+        if (v == 0) {
             const uint32_t np = npairs;
             uint32_t made = 0;
             for (uint32_t q = 0; q < np && cnt - made > 1; q++) {
@@ -1139,26 +1149,22 @@ __global__ void __launch_bounds__(32) sw_leaf_kernel(const LeafDesc *__restrict_
             }
             npairs = made;
         }
-        __syncwarp();
+        __syncthreads();
         const uint32_t nm = npairs;
-        if (cnt - nm <= 1) break;  // one vertex left: lambda is the leaf's cut, no matrix to update
+        if (cnt - nm <= 1) break;
         for (uint32_t q = 0; q < nm; q++) {
             const uint32_t x = pairs[q] >> 8, y = pairs[q] & 255u;
             // merge y into x: entry (x, v) += entry (y, v) for every other active v
-#pragma unroll
-            for (int s = 0; s < 4; s++) {
-                const uint32_t v = lane + 32 * s;
-                if (((active >> s) & 1u) && v != x && v != y) {
-                    const Tm val = M[cpos(x, v, N, H)] + M[cpos(y, v, N, H)];
-                    cset(M, x, v, N, H, val);
-                }
+            if (active && v != x && v != y) {
+                const Tm val = M[cpos(x, v, N, H)] + M[cpos(y, v, N, H)];
+                cset(M, x, v, N, H, val);
             }
-            if ((uint32_t)lane == (y & 31u)) active &= ~(1u << (y >> 5));
-            __syncwarp();
+            if (v == y) active = false;
+            __syncthreads();
         }
         cnt -= nm;
     }
-    if (lane == 0) atomicMin((unsigned long long *)L.cut, (unsigned long long)lambda);
+    if (v == 0) atomicMin((unsigned long long *)L.cut, (unsigned long long)lambda);
 }
 
 __global__ void fill_u64(uint64_t *p, uint64_t n, uint64_t value) {
@@ -1359,11 +1365,11 @@ int KsEngine::step() {
             if (leaves[first].small) {
                 const size_t sm = leaf_smem(N, true);
                 CAC_TRY(smem_optin(ctx_, sw_leaf_kernel<uint32_t>));
-                sw_leaf_kernel<uint32_t><<<(unsigned)(last - first), 32, sm, s>>>(dl);
+                sw_leaf_kernel<uint32_t><<<(unsigned)(last - first), kLeafThreads, sm, s>>>(dl);
             } else {
                 const size_t sm = leaf_smem(N, false);
                 CAC_TRY(smem_optin(ctx_, sw_leaf_kernel<uint64_t>));
-                sw_leaf_kernel<uint64_t><<<(unsigned)(last - first), 32, sm, s>>>(dl);
+                sw_leaf_kernel<uint64_t><<<(unsigned)(last - first), kLeafThreads, sm, s>>>(dl);
             }
             first = last;
         }
@@ -2273,11 +2279,11 @@ int exact_small(cac_ctx *ctx, uint32_t n, const uint64_t *mat_host, uint64_t *cu
     if (small) {
         const size_t sm = leaf_smem(n, true);
         CAC_TRY(smem_optin(ctx, sw_leaf_kernel<uint32_t>));
-        sw_leaf_kernel<uint32_t><<<1, 32, sm, s>>>(d_leaf.as<LeafDesc>());
+        sw_leaf_kernel<uint32_t><<<1, kLeafThreads, sm, s>>>(d_leaf.as<LeafDesc>());
     } else {
         const size_t sm = leaf_smem(n, false);
         CAC_TRY(smem_optin(ctx, sw_leaf_kernel<uint64_t>));
-        sw_leaf_kernel<uint64_t><<<1, 32, sm, s>>>(d_leaf.as<LeafDesc>());
+        sw_leaf_kernel<uint64_t><<<1, kLeafThreads, sm, s>>>(d_leaf.as<LeafDesc>());
     }
     CAC_CUDA_TRY(cudaGetLastError());
     CAC_CUDA_TRY(cudaMemcpyAsync(cut, d_cuts.p, 8, cudaMemcpyDeviceToHost, s));
