@@ -1022,6 +1022,8 @@ __global__ void __launch_bounds__(kLeafThreads) sw_leaf_kernel(const LeafDesc *_
     __shared__ uint32_t pairs[128];
     __shared__ uint32_t npairs;
     __shared__ __align__(16) uint64_t wbest[2][4];
+    __shared__ __align__(16) uint32_t wbest32[2][4];
+    __shared__ uint64_t wsum[4];
     const LeafDesc L = leaves[blockIdx.x];
     const uint32_t N = L.N, H = N / 2;
     const uint32_t v = threadIdx.x, lane = v & 31u, warp = v >> 5;
@@ -1066,11 +1068,24 @@ __global__ void __launch_bounds__(kLeafThreads) sw_leaf_kernel(const LeafDesc *_
     }
     {
         const uint64_t wm = warp_min_u64(deg);
-        if (lane == 0) wbest[1][warp] = wm;  // the first step writes wbest[0]
+        // the degree sum (u32 matrices: every degree below 2^32, summed as two 16-bit halves)
+        const uint32_t d = active && deg < (1ull << 32) ? (uint32_t)deg : 0u;
+        const uint64_t ws = (uint64_t)__reduce_add_sync(0xffffffffu, d & 0xFFFFu) +
+                            ((uint64_t)__reduce_add_sync(0xffffffffu, d >> 16) << 16);
+        if (lane == 0) {
+            wbest[1][warp] = wm;  // the first step writes wbest[0]
+            wsum[warp] = ws;
+        }
     }
     __syncthreads();
-    uint64_t lambda = wbest[1][0];
-    for (int w = 1; w < 4; w++) lambda = wbest[1][w] < lambda ? wbest[1][w] : lambda;
+    uint64_t lambda = wbest[1][0], deg_sum = wsum[0];
+    for (int w = 1; w < 4; w++) {
+        lambda = wbest[1][w] < lambda ? wbest[1][w] : lambda;
+        deg_sum += wsum[w];
+    }
+    // a key never exceeds the leaf's total weight (half its degree sum, which merges only lower):
+    // below 2^24, (key << 8 | 255 - v) is one 32-bit word and the argmax one reduction
+    const bool packed32 = sizeof(Tm) == 4 && deg_sum < (1ull << 25);
     using Kt = typename std::conditional<sizeof(Tm) == 4, uint32_t, uint64_t>::type;
     uint32_t cnt = N, par = 0;
     while (cnt > 1) {
@@ -1082,6 +1097,18 @@ __global__ void __launch_bounds__(kLeafThreads) sw_leaf_kernel(const LeafDesc *_
         uint64_t cut_phase = 0;
         for (uint32_t step = 0; step < cnt; step++) {
             const bool elig = active && !in_a;
+            uint32_t sv;
+            uint64_t top_key;
+            if (packed32) {
+                const uint32_t wb = __reduce_max_sync(0xffffffffu, elig ? (((uint32_t)key << 8) | (255u - v)) : 0u);
+                if (lane == 0) wbest32[par][warp] = wb;
+                __syncthreads();
+                const uint4 b = *reinterpret_cast<const uint4 *>(&wbest32[par][0]);
+                par ^= 1u;
+                const uint32_t best = max(max(b.x, b.y), max(b.z, b.w));
+                sv = 255u - (best & 255u);
+                top_key = best >> 8;
+            } else {
             uint64_t wb;  // this warp's best as (key << 8 | 255 - vertex), 0 for none
             if constexpr (sizeof(Tm) == 4) {
                 const uint32_t top = __reduce_max_sync(0xffffffffu, elig ? key : 0u);
@@ -1097,14 +1124,16 @@ __global__ void __launch_bounds__(kLeafThreads) sw_leaf_kernel(const LeafDesc *_
             par ^= 1u;
             const uint64_t m01 = b01.x > b01.y ? b01.x : b01.y, m23 = b23.x > b23.y ? b23.x : b23.y;
             const uint64_t best = m01 > m23 ? m01 : m23;
-            const uint32_t sv = 255u - (uint32_t)(best & 255u);
+            sv = 255u - (uint32_t)(best & 255u);
+            top_key = best >> 8;
+            }
             if (sv >= N) {  // no candidate: cannot happen (cnt - step vertices are unscanned)
                 cut_phase = kU64Max;
                 break;
             }
             if (step + 1 == cnt) {
                 last = sv;
-                cut_phase = best >> 8;
+                cut_phase = top_key;
                 break;
             }
             in_a = in_a || v == sv;

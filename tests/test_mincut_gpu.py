@@ -28,7 +28,7 @@ def _dense(n, u, v, w):
 def _random_dense(n, seed, density=0.3, wmax=42, big=False):
     rng = np.random.default_rng(seed)
     mask = np.triu(rng.random((n, n)) < density, 1)
-    w = rng.integers(1, wmax + 1, size=(n, n)).astype(np.uint64)
+    w = rng.integers(1, wmax + 1, size=(n, n), dtype=np.uint64)
     if big:
         w = w << np.uint64(33)
     mat = np.where(mask, w, 0).astype(np.uint64)
@@ -42,6 +42,35 @@ def test_leaf_stoer_wagner_kernel(ctx, n, density, big):
     for seed in range(3):
         mat = _random_dense(n, seed, density, big=big)
         assert ctx.exact_cut_small(mat) == O.stoer_wagner_dense(mat)
+
+
+# The leaf kernel keeps 32-bit keys packed with the vertex (one reduction per step) while the leaf
+# weighs less than 2^24, 32-bit keys with a two-step argmax up to 2^32, 64-bit keys above: one
+# case per form, on random leaves and on two dense clusters joined by a few light edges (the
+# minimum cut is the bridge, below every degree, so orderings contract each cluster first and a
+# second ordering finds the bridge).
+def _two_clusters(n, seed, wmax, bridges=3):
+    mat = _random_dense(n, seed, 0.6, wmax=wmax)
+    h = n // 2
+    mat[:h, h:] = 0
+    mat[h:, :h] = 0
+    rng = np.random.default_rng(seed + 1000)
+    for _ in range(bridges):
+        a, b = int(rng.integers(0, h)), int(rng.integers(h, n))
+        mat[a, b] = mat[b, a] = mat[a, b] + 1
+    return mat
+
+
+@pytest.mark.parametrize("wmax", [42, 1 << 18, 1 << 40])
+@pytest.mark.parametrize("n", [128, 77, 6])
+def test_leaf_kernel_key_widths_and_clusters(ctx, n, wmax):
+    for seed in range(3):
+        mat = _random_dense(n, seed, 0.5, wmax=wmax)
+        assert ctx.exact_cut_small(mat) == O.stoer_wagner_dense(mat)
+        mat = _two_clusters(n, seed, wmax)
+        got = ctx.exact_cut_small(mat)
+        assert got == O.stoer_wagner_dense(mat)
+        assert got <= 3
 
 
 @pytest.mark.parametrize("n,density", [(129, 0.5), (200, 0.1), (318, 0.15), (500, 0.05)])
