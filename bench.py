@@ -290,6 +290,8 @@ def run_ks(args, rank, world):
     name, (n, u, v, w), ranks, _ = _ks_workloads()[0 if args.workload == "ks-er1000" else 1]
     stream = torch.cuda.Stream(device=dev)
     ctx = cac.Context(dev, stream=stream.cuda_stream)
+    if args.quotient_kernel:
+        ctx.set_quotient_kernel(args.quotient_kernel)
     g = ctx.graph(n, u, v, w)
     for _ in range(args.warmup):
         res = g.square_root(0.95, seed=0, virtual_ranks=ranks)
@@ -306,7 +308,8 @@ def run_ks(args, rank, world):
             "ms_per_step": total_ms / args.steps, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
             "dtype": "u64", "data": "synthetic (seeded)", "cut": int(res.cut),
             "config": {"workload": name, "vertices": n, "edges": int(len(u)), "virtual_ranks": ranks,
-                       "trials_per_query": res.total_trials, "intermediate_size": res.intermediate},
+                       "trials_per_query": res.total_trials, "intermediate_size": res.intermediate,
+                       "quotient_kernel": args.quotient_kernel or "autotuned"},
             "clocks": clk.summary()}
     peak, peak_kind = _peaks()
     line["work_model"] = _ks_work_model(res.intermediate, res.total_trials / (total_ms / args.steps / 1e3),
@@ -695,6 +698,8 @@ def run_batch(args, rank, world):
     torch.cuda.set_device(dev)
     stream = torch.cuda.Stream(device=dev)
     ctx = cac.Context(dev, stream=stream.cuda_stream)
+    if args.quotient_kernel:
+        ctx.set_quotient_kernel(args.quotient_kernel)
     with Clocks(dev) as clk:
         r = _batch_measure(ctx, args.graphs, args.steps, args.warmup, check_exact=args.check_exact)
     total_s = r["ms_per_step"] * args.steps / 1e3
@@ -706,7 +711,8 @@ def run_batch(args, rank, world):
             "data": "synthetic (device-generated Watts-Strogatz and G(n, M), seeds base + index)",
             "config": {"workload": "uneven square_root batch", "graphs": r["graphs"], "edges": r["edges"],
                        "trials_per_batch": r["trials_per_batch"], "success_probability": 0.9,
-                       "n_range": [64, 8192], "timing": "host wall clock per batch"},
+                       "n_range": [64, 8192], "timing": "host wall clock per batch",
+                       "quotient_kernel": args.quotient_kernel or "autotuned"},
             "queries_per_s": world * r["graphs"] * args.steps / total_s,
             "device_ms_per_batch": r["device_ms_per_batch"], "plain_path_subset": r["plain_path_subset"],
             "results_equal_plain": r["results_equal_plain"], "cuts_exact": r["cuts_exact"],
@@ -871,6 +877,10 @@ def main():
     ap.add_argument("--check-exact", action="store_true", help="ks-batch: check every cut against the exact cut")
     ap.add_argument("--no-batch", action="store_true", help="skip the batched min-cut measurement")
     ap.add_argument("--no-serve", action="store_true", help="skip the served-stream measurement")
+    ap.add_argument("--quotient-kernel", type=int, default=0, choices=[0, 1, 2, 3],
+                    help="ks-er1000 / ks-k4000 / ks-batch: 0 autotuned; 1 warp per row, 2 eight warps per row, "
+                         "3 warp per row with bulk-copy staging forced for every Karger-Stein step "
+                         "(a profiling aid: under ncu the autotuner's timings are distorted)")
     args = ap.parse_args()
     if args.steps is None:
         args.steps = {"cc": 20, "cc-rmat22": 20, "ks-batch": 3, "ks-ws32k": 3}.get(args.workload, 10)
