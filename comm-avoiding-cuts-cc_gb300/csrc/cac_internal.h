@@ -219,7 +219,7 @@ class KsEngine {
     std::vector<KNode> nodes_;
     std::vector<KTask> carried_;
     bool release_err_ = false;
-    void *d_src_, *d_task_, *d_leaf_, *d_rowoff_, *d_kout_, *d_prep_, *d_tscratch_, *d_qoff_, *d_gto_, *d_err_, *d_psrc_;
+    void *d_kout_, *d_prep_, *d_tscratch_, *d_err_;  // the ctx's grow-only scratch (mincut.cu)
 };
 
 // A Karger-Stein node kept as an edge list (sparse_ks.cu): a root above the dense limit, or a

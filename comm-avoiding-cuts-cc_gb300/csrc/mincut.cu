@@ -35,6 +35,7 @@
 
 #include <algorithm>
 #include <cmath>
+#include <cstring>
 #include <numeric>
 #include <type_traits>
 
@@ -1230,23 +1231,84 @@ struct DevBuf {
 // Grow-only scratch buffers kept by the ctx between calls: a fresh device allocation per query
 // (cudaMalloc, and a cudaFree that waits for the whole device) cost more than the kernels of a
 // small query (admission of square_root on ER(1000, 0.05): 303 us, of which about 100 us of
-// kernels). Slots 0..10 belong to the Karger-Stein engine, 11..15 to admission, 16.. to the
+// kernels). Slots 0..3 belong to the Karger-Stein engine, 4..10 to admission, 11.. to the
 // one-shot probes; one engine runs per ctx at a time.
 enum ScratchSlot : int {
-    kSlotSrc, kSlotTask, kSlotLeaf, kSlotRowoff, kSlotKout, kSlotPrep, kSlotTscratch, kSlotQoff, kSlotGto, kSlotErr,
-    kSlotPsrc, kSlotPre, kSlotLab, kSlotK, kSlotSd, kSlotDd, kSlotSparse, kSlotSparseCount, kSlotProbe0, kSlotProbe1,
-    kSlotProbe2, kSlotCount
+    kSlotKout, kSlotPrep, kSlotTscratch, kSlotErr, kSlotPre, kSlotLab, kSlotK, kSlotSd, kSlotDd, kSlotSparse,
+    kSlotSparseCount, kSlotProbe0, kSlotProbe1, kSlotProbe2, kSlotCount
+};
+
+// Descriptor staging of one phase of an engine step: the phase's small host arrays are packed
+// (16-byte aligned) into one pinned host buffer and sent with a single copy into one device
+// buffer, instead of one pageable copy per array (each a driver call on the host's critical path
+// between a step's read-back and its next launches). An event after the copy guards the pinned
+// buffer: it is refilled only once its previous copy has run (at once in the usual flow, where
+// every step synchronises in its middle).
+struct Staging {
+    cac_ctx *ctx;
+    DevBuf dev;
+    unsigned char *host = nullptr;
+    size_t hcap = 0, used = 0;
+    cudaEvent_t done = nullptr;
+    bool pending = false;
+    explicit Staging(cac_ctx *c) : ctx(c), dev(c) {}
+    Staging(const Staging &) = delete;
+    Staging &operator=(const Staging &) = delete;
+    ~Staging() {
+        if (pending) cudaEventSynchronize(done);
+        if (host) cudaFreeHost(host);
+        if (done) cudaEventDestroy(done);
+    }
+    template <typename T> static size_t bytes_of(const std::vector<T> &v) {
+        return (sizeof(T) * std::max<size_t>(v.size(), 1) + 15) & ~(size_t)15;
+    }
+    int begin(size_t bytes) {
+        if (!done) CAC_CUDA_TRY(cudaEventCreateWithFlags(&done, cudaEventDisableTiming));
+        if (pending) {
+            CAC_CUDA_TRY(cudaEventSynchronize(done));
+            pending = false;
+        }
+        bytes = std::max<size_t>(bytes, 16);
+        if (bytes > hcap) {
+            if (host) CAC_CUDA_TRY(cudaFreeHost(host));
+            host = nullptr;
+            hcap = 0;
+            const size_t want = align_up(bytes, 1 << 16);
+            CAC_CUDA_TRY(cudaHostAlloc(reinterpret_cast<void **>(&host), want, cudaHostAllocDefault));
+            hcap = want;
+        }
+        CAC_TRY(dev.ensure(bytes));
+        used = 0;
+        return CAC_OK;
+    }
+    // copies v into the host buffer; returns where it will be on the device
+    template <typename T> T *put(const std::vector<T> &v) {
+        const size_t off = used;
+        if (!v.empty()) std::memcpy(host + off, v.data(), sizeof(T) * v.size());
+        used += bytes_of(v);
+        return reinterpret_cast<T *>(static_cast<unsigned char *>(dev.p) + off);
+    }
+    int flush() {
+        if (!used) return CAC_OK;
+        CAC_CUDA_TRY(cudaMemcpyAsync(dev.p, host, used, cudaMemcpyHostToDevice, ctx->stream));
+        CAC_CUDA_TRY(cudaEventRecord(done, ctx->stream));
+        pending = true;
+        return CAC_OK;
+    }
 };
 
 struct CtxScratch {
     std::vector<DevBuf> slots;
-    explicit CtxScratch(cac_ctx *ctx) : slots(kSlotCount, DevBuf(ctx)) {}
+    Staging leaf, pre, post;  // an engine step's leaves, then its descriptors before and after its read-back
+    explicit CtxScratch(cac_ctx *ctx) : slots(kSlotCount, DevBuf(ctx)), leaf(ctx), pre(ctx), post(ctx) {}
 };
 
-DevBuf &scratch(cac_ctx *ctx, ScratchSlot slot) {
+CtxScratch &ctx_scratch(cac_ctx *ctx) {
     if (!ctx->ks_scratch) ctx->ks_scratch = new CtxScratch(ctx);
-    return static_cast<CtxScratch *>(ctx->ks_scratch)->slots[slot];
+    return *static_cast<CtxScratch *>(ctx->ks_scratch);
 }
+
+DevBuf &scratch(cac_ctx *ctx, ScratchSlot slot) { return ctx_scratch(ctx).slots[slot]; }
 
 template <typename T>
 int upload(cac_ctx *ctx, DevBuf &buf, const std::vector<T> &v) {
@@ -1269,10 +1331,8 @@ void ctx_scratch_free(cac_ctx *ctx) {
 // ---- Karger-Stein engine (declared in cac_internal.h) ----
 
 KsEngine::KsEngine(cac_ctx *ctx)
-    : ctx_(ctx), d_src_(&scratch(ctx, kSlotSrc)), d_task_(&scratch(ctx, kSlotTask)), d_leaf_(&scratch(ctx, kSlotLeaf)),
-      d_rowoff_(&scratch(ctx, kSlotRowoff)), d_kout_(&scratch(ctx, kSlotKout)), d_prep_(&scratch(ctx, kSlotPrep)),
-      d_tscratch_(&scratch(ctx, kSlotTscratch)), d_qoff_(&scratch(ctx, kSlotQoff)), d_gto_(&scratch(ctx, kSlotGto)),
-      d_err_(&scratch(ctx, kSlotErr)), d_psrc_(&scratch(ctx, kSlotPsrc)) {}
+    : ctx_(ctx), d_kout_(&scratch(ctx, kSlotKout)), d_prep_(&scratch(ctx, kSlotPrep)),
+      d_tscratch_(&scratch(ctx, kSlotTscratch)), d_err_(&scratch(ctx, kSlotErr)) {}
 
 KsEngine::~KsEngine() {
     cudaStreamSynchronize(ctx_->stream);
@@ -1356,11 +1416,8 @@ int KsEngine::step() {
         set_error("Karger-Stein engine: a level buffer was released more often than referenced or could not be freed");
         return CAC_ERR_CUDA;
     }
-    DevBuf &d_src = *static_cast<DevBuf *>(d_src_), &d_task = *static_cast<DevBuf *>(d_task_);
-    DevBuf &d_leaf = *static_cast<DevBuf *>(d_leaf_), &d_rowoff = *static_cast<DevBuf *>(d_rowoff_);
     DevBuf &d_kout = *static_cast<DevBuf *>(d_kout_), &d_prep = *static_cast<DevBuf *>(d_prep_);
-    DevBuf &d_tscratch = *static_cast<DevBuf *>(d_tscratch_), &d_qoff = *static_cast<DevBuf *>(d_qoff_);
-    DevBuf &d_gto = *static_cast<DevBuf *>(d_gto_), &d_psrc = *static_cast<DevBuf *>(d_psrc_);
+    DevBuf &d_tscratch = *static_cast<DevBuf *>(d_tscratch_);
     uint32_t *d_err = static_cast<DevBuf *>(d_err_)->as<uint32_t>();
     std::vector<MatBuf *> consumed;
 
@@ -1380,17 +1437,17 @@ int KsEngine::step() {
         }
     }
     nodes_.clear();
-    if (!leaves.empty()) {
-        std::sort(leaves.begin(), leaves.end(),
-                  [](const LeafDesc &a, const LeafDesc &b) { return a.N != b.N ? a.N > b.N : a.small > b.small; });
-        CAC_TRY(upload(ctx_, d_leaf, leaves));
+    std::sort(leaves.begin(), leaves.end(),
+              [](const LeafDesc &a, const LeafDesc &b) { return a.N != b.N ? a.N > b.N : a.small > b.small; });
+    // the leaves, grouped by size and entry width, one launch each (after the descriptor copy)
+    auto launch_leaves = [&](const LeafDesc *d_leaves) -> int {
         size_t first = 0;
         while (first < leaves.size()) {
             size_t last = first;
             while (last < leaves.size() && leaves[last].N == leaves[first].N && leaves[last].small == leaves[first].small)
                 last++;
             const uint32_t N = leaves[first].N;
-            const LeafDesc *dl = d_leaf.as<LeafDesc>() + first;
+            const LeafDesc *dl = d_leaves + first;
             if (leaves[first].small) {
                 const size_t sm = leaf_smem(N, true);
                 CAC_TRY(smem_optin(ctx_, sw_leaf_kernel<uint32_t>));
@@ -1403,6 +1460,15 @@ int KsEngine::step() {
             first = last;
         }
         CAC_CUDA_TRY(cudaGetLastError());
+        return CAC_OK;
+    };
+    Staging &leaf_st = ctx_scratch(ctx_).leaf, &pre_st = ctx_scratch(ctx_).pre, &post_st = ctx_scratch(ctx_).post;
+    // the leaves go first: they run while the host plans the step's contractions
+    if (!leaves.empty()) {
+        CAC_TRY(leaf_st.begin(Staging::bytes_of(leaves)));
+        const LeafDesc *dl = leaf_st.put(leaves);
+        CAC_TRY(leaf_st.flush());
+        CAC_TRY(launch_leaves(dl));
     }
 
     // sources: inner nodes (two children each) and the matrices of tasks continuing another round
@@ -1458,21 +1524,6 @@ int KsEngine::step() {
         S.blk = S.rowpre + nd.N;
         if (!nd.pre) psrcs.push_back(S);
     }
-    CAC_TRY(upload(ctx_, d_src, srcs));
-    if (rows) {
-        CAC_TRY(upload(ctx_, d_rowoff, row_off));
-        CAC_TRY(upload(ctx_, d_psrc, psrcs));
-        bool p32 = false, p64 = false;
-        for (const SrcDesc &S : psrcs) (S.small ? p32 : p64) = true;
-        const unsigned pg = (unsigned)((rows * 32 + 255) / 256);
-        if (p32)
-            prep_rows_kernel<uint32_t><<<pg, 256, 0, s>>>(d_psrc.as<SrcDesc>(), d_rowoff.as<uint64_t>(),
-                                                          (uint32_t)row_off.size(), rows);
-        if (p64)
-            prep_rows_kernel<uint64_t><<<pg, 256, 0, s>>>(d_psrc.as<SrcDesc>(), d_rowoff.as<uint64_t>(),
-                                                          (uint32_t)row_off.size(), rows);
-    }
-    prefix_rows_kernel<kNT><<<(unsigned)srcs.size(), kNT, 0, s>>>(d_src.as<SrcDesc>());
 
     // contraction of every child
     uint64_t tscratch = 0;
@@ -1500,8 +1551,25 @@ int KsEngine::step() {
         d.memb_off = d.members + t.src.N;
         ts += 3 * (uint64_t)t.src.N + 1;
     }
-    CAC_TRY(upload(ctx_, d_task, td));
     CAC_TRY(d_kout.ensure(tasks.size() * 4));
+    // one descriptor copy for the sources, the row-prep list and the tasks
+    CAC_TRY(pre_st.begin(Staging::bytes_of(srcs) + Staging::bytes_of(row_off) + Staging::bytes_of(psrcs) +
+                         Staging::bytes_of(td)));
+    const SrcDesc *dv_src = pre_st.put(srcs);
+    const uint64_t *dv_rowoff = pre_st.put(row_off);
+    const SrcDesc *dv_psrc = pre_st.put(psrcs);
+    const TaskDesc *dv_task = pre_st.put(td);
+    CAC_TRY(pre_st.flush());
+    if (rows) {
+        bool p32 = false, p64 = false;
+        for (const SrcDesc &S : psrcs) (S.small ? p32 : p64) = true;
+        const unsigned pg = (unsigned)((rows * 32 + 255) / 256);
+        if (p32)
+            prep_rows_kernel<uint32_t><<<pg, 256, 0, s>>>(dv_psrc, dv_rowoff, (uint32_t)row_off.size(), rows);
+        if (p64)
+            prep_rows_kernel<uint64_t><<<pg, 256, 0, s>>>(dv_psrc, dv_rowoff, (uint32_t)row_off.size(), rows);
+    }
+    prefix_rows_kernel<kNT><<<(unsigned)srcs.size(), kNT, 0, s>>>(dv_src);
     bool t32 = false, t64 = false;  // entry widths present among the tasks' sources
     for (const KTask &t : tasks) (t.src.small ? t32 : t64) = true;
     {
@@ -1509,12 +1577,12 @@ int KsEngine::step() {
         if (t32) {
             CAC_TRY(smem_optin(ctx_, contract_kernel<kNT, uint32_t>));
             contract_kernel<kNT, uint32_t><<<(unsigned)tasks.size(), kNT, sm, s>>>(
-                d_task.as<TaskDesc>(), d_src.as<SrcDesc>(), d_kout.as<uint32_t>(), d_err);
+                dv_task, dv_src, d_kout.as<uint32_t>(), d_err);
         }
         if (t64) {
             CAC_TRY(smem_optin(ctx_, contract_kernel<kNT, uint64_t>));
             contract_kernel<kNT, uint64_t><<<(unsigned)tasks.size(), kNT, sm, s>>>(
-                d_task.as<TaskDesc>(), d_src.as<SrcDesc>(), d_kout.as<uint32_t>(), d_err);
+                dv_task, dv_src, d_kout.as<uint32_t>(), d_err);
         }
         CAC_CUDA_TRY(cudaGetLastError());
     }
@@ -1542,12 +1610,13 @@ int KsEngine::step() {
         out_off[tasks.size() + i] = out_bytes;
         out_bytes += ((kq[i] + (uint64_t)kq[i] * ((kq[i] + 31) / 32)) * 8 + 15) / 16 * 16;
     }
-    // Two quotient kernels, identical outputs: warp-per-row (8 or 4 warps, one k-entry row per warp
-    // in shared memory; where three of its CTAs fit an SM: labels + rows within 80 KB) and
-    // shared-row (8 warps on one output row). Which is faster depends on N, k and the task count,
-    // so the step autotunes: the first sizeable step of each (power-of-two bucket of N, entry
-    // width) on this ctx times both on its own data and keeps the faster; smaller steps before
-    // that use the rule measured on GB300 (shared-row from N = 2000 on).
+    // Three quotient kernels, identical outputs: warp-per-row (8 or 4 warps, one k-entry row per
+    // warp in shared memory; where three of its CTAs fit an SM: labels + rows within 80 KB), its
+    // bulk-copy variant, and shared-row (8 warps on one output row). Which is fastest depends on
+    // N, k and the task count, so the step autotunes: the first sizeable step of each
+    // (power-of-two bucket of N, entry width) on this ctx times them on its own data and keeps the
+    // fastest; smaller steps before that use the rule measured on GB300 (shared-row from N = 2000
+    // on).
     const size_t stage_words = ((size_t)maxN + 3) & ~(size_t)3;  // N u32 labels, 16-byte rounded
     const size_t rs_bytes = all_small ? 4 : 8;
     const uint32_t qwarps = stage_words * 4 + 8 * rs_bytes * (size_t)kmax <= 80 * 1024   ? 8u
@@ -1565,13 +1634,31 @@ int KsEngine::step() {
     std::vector<uint64_t> gto_warp, gto_shared;
     const uint64_t groups_warp = qwarps ? group_offsets(qwarps * 4, gto_warp) : 0;
     const uint64_t groups_shared = group_offsets(kSharedRows, gto_shared);
+    // the bulk-copy variant of the warp quotient: labels, then per warp two staged member rows
+    // and its output row; 8 warps where two CTAs fit an SM, else 4 where one does
+    const size_t row_words = (size_t)ld_of(maxN);
+    const size_t bulk_per_warp = ((row_words * (all_small ? 4 : 8)) * 2 + (size_t)kmax * rs_bytes + 15) & ~(size_t)15;
+    const size_t bulk_base = 128 + ((stage_words * 4 + 15) & ~(size_t)15);
+    const uint32_t bwarps = bulk_base + 8 * bulk_per_warp <= 113 * 1024   ? 8u
+                            : bulk_base + 4 * bulk_per_warp <= 226 * 1024 ? 4u
+                                                                          : 0u;
+    std::vector<uint64_t> gto_bulk;
+    const uint64_t groups_bulk = bwarps ? group_offsets(bwarps * 4, gto_bulk) : 0;
     MatBuf *out = nullptr;
     if (groups_shared) {
         CAC_TRY(alloc(out_bytes, &out));
-        CAC_TRY(upload(ctx_, d_qoff, out_off));
-        CAC_CUDA_TRY(cudaMemcpyAsync(d_kout.p, kq.data(), tasks.size() * 4, cudaMemcpyHostToDevice, s));
+        // one descriptor copy for the output offsets, the children's sizes and the row groups
+        CAC_TRY(post_st.begin(Staging::bytes_of(out_off) + Staging::bytes_of(kq) + Staging::bytes_of(gto_shared) +
+                              Staging::bytes_of(gto_warp) + Staging::bytes_of(gto_bulk)));
+        const uint64_t *dv_qoff = post_st.put(out_off);
+        const uint32_t *dv_k = post_st.put(kq);
+        const uint64_t *dv_gto_shared = post_st.put(gto_shared);
+        const uint64_t *dv_gto_warp = post_st.put(gto_warp);
+        const uint64_t *dv_gto_bulk = post_st.put(gto_bulk);
+        CAC_TRY(post_st.flush());
+        unsigned char *obase = static_cast<unsigned char *>(out->p);
+        const uint32_t ntk = (uint32_t)tasks.size();
         auto launch_shared = [&]() -> int {
-            CAC_TRY(upload(ctx_, d_gto, gto_shared));
             const size_t ssm = stage_words * 4 + (((size_t)kmax * rs_bytes + 15) & ~(size_t)15) +
                                ((size_t)kmax / 32 + 1) * 8;
             std::vector<decltype(&quotient_shared_row_kernel<uint32_t, uint32_t>)> kerns;
@@ -1582,16 +1669,13 @@ int KsEngine::step() {
             }
             for (auto kern : kerns) {
                 CAC_TRY(smem_optin(ctx_, kern));
-                kern<<<(unsigned)groups_shared, 256, ssm, s>>>(
-                    d_task.as<TaskDesc>(), d_src.as<SrcDesc>(), d_kout.as<uint32_t>(), d_gto.as<uint64_t>(),
-                    (uint32_t)tasks.size(), kSharedRows, d_qoff.as<uint64_t>(), static_cast<unsigned char *>(out->p),
-                    (uint32_t)stage_words, kmax);
+                kern<<<(unsigned)groups_shared, 256, ssm, s>>>(dv_task, dv_src, dv_k, dv_gto_shared, ntk, kSharedRows,
+                                                               dv_qoff, obase, (uint32_t)stage_words, kmax);
             }
             CAC_CUDA_TRY(cudaGetLastError());
             return CAC_OK;
         };
         auto launch_warp = [&]() -> int {
-            CAC_TRY(upload(ctx_, d_gto, gto_warp));
             // shared rows are u32 only when every task's sums fit (all sources small)
             const size_t wsm = stage_words * 4 + (size_t)qwarps * kmax * rs_bytes;
             std::vector<decltype(&quotient_warp_kernel<uint32_t, uint32_t>)> kerns;
@@ -1602,26 +1686,14 @@ int KsEngine::step() {
             }
             for (auto kern : kerns) {
                 CAC_TRY(smem_optin(ctx_, kern));
-                kern<<<(unsigned)groups_warp, qwarps * 32, wsm, s>>>(
-                    d_task.as<TaskDesc>(), d_src.as<SrcDesc>(), d_kout.as<uint32_t>(), d_gto.as<uint64_t>(),
-                    (uint32_t)tasks.size(), qwarps * 4, d_qoff.as<uint64_t>(), static_cast<unsigned char *>(out->p),
-                    (uint32_t)stage_words, kmax);
+                kern<<<(unsigned)groups_warp, qwarps * 32, wsm, s>>>(dv_task, dv_src, dv_k, dv_gto_warp, ntk,
+                                                                     qwarps * 4, dv_qoff, obase,
+                                                                     (uint32_t)stage_words, kmax);
             }
             CAC_CUDA_TRY(cudaGetLastError());
             return CAC_OK;
         };
-        // the bulk-copy variant of the warp quotient: labels, then per warp two staged member rows
-        // and its output row; 8 warps where two CTAs fit an SM, else 4 where one does
-        const size_t row_words = (size_t)ld_of(maxN);
-        const size_t bulk_per_warp = ((row_words * (all_small ? 4 : 8)) * 2 + (size_t)kmax * rs_bytes + 15) & ~(size_t)15;
-        const size_t bulk_base = 128 + ((stage_words * 4 + 15) & ~(size_t)15);
-        const uint32_t bwarps = bulk_base + 8 * bulk_per_warp <= 113 * 1024   ? 8u
-                                : bulk_base + 4 * bulk_per_warp <= 226 * 1024 ? 4u
-                                                                              : 0u;
-        std::vector<uint64_t> gto_bulk;
-        const uint64_t groups_bulk = bwarps ? group_offsets(bwarps * 4, gto_bulk) : 0;
         auto launch_bulk = [&]() -> int {
-            CAC_TRY(upload(ctx_, d_gto, gto_bulk));
             const size_t bsm = bulk_base + bwarps * bulk_per_warp;
             std::vector<decltype(&quotient_bulk_kernel<uint32_t, uint32_t>)> kerns;
             if (all_small) kerns.push_back(quotient_bulk_kernel<uint32_t, uint32_t>);
@@ -1631,10 +1703,10 @@ int KsEngine::step() {
             }
             for (auto kern : kerns) {
                 CAC_TRY(smem_optin(ctx_, kern));
-                kern<<<(unsigned)groups_bulk, bwarps * 32, bsm, s>>>(
-                    d_task.as<TaskDesc>(), d_src.as<SrcDesc>(), d_kout.as<uint32_t>(), d_gto.as<uint64_t>(),
-                    (uint32_t)tasks.size(), bwarps * 4, d_qoff.as<uint64_t>(), static_cast<unsigned char *>(out->p),
-                    (uint32_t)stage_words, kmax, (uint32_t)row_words, d_err);
+                kern<<<(unsigned)groups_bulk, bwarps * 32, bsm, s>>>(dv_task, dv_src, dv_k, dv_gto_bulk, ntk,
+                                                                     bwarps * 4, dv_qoff, obase,
+                                                                     (uint32_t)stage_words, kmax,
+                                                                     (uint32_t)row_words, d_err);
             }
             CAC_CUDA_TRY(cudaGetLastError());
             return CAC_OK;
