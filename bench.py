@@ -877,10 +877,10 @@ def main():
     ap.add_argument("--check-exact", action="store_true", help="ks-batch: check every cut against the exact cut")
     ap.add_argument("--no-batch", action="store_true", help="skip the batched min-cut measurement")
     ap.add_argument("--no-serve", action="store_true", help="skip the served-stream measurement")
-    ap.add_argument("--quotient-kernel", type=int, default=0, choices=[0, 1, 2, 3],
+    ap.add_argument("--quotient-kernel", type=int, default=0, choices=[0, 1, 2, 3, 4],
                     help="ks-er1000 / ks-k4000 / ks-batch: 0 autotuned; 1 warp per row, 2 eight warps per row, "
-                         "3 warp per row with bulk-copy staging forced for every Karger-Stein step "
-                         "(a profiling aid: under ncu the autotuner's timings are distorted)")
+                         "3 warp per row with bulk-copy staging forced for every Karger-Stein step; 4 the fixed "
+                         "size rule without timing (a profiling aid: under ncu the autotuner's timings are distorted)")
     args = ap.parse_args()
     if args.steps is None:
         args.steps = {"cc": 20, "cc-rmat22": 20, "ks-batch": 3, "ks-ws32k": 3}.get(args.workload, 10)

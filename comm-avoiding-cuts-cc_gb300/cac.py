@@ -184,7 +184,8 @@ class Context:
         _check(lib().cac_ctx_set_dense_limit(self.h, max_dense_vertices), "cac_ctx_set_dense_limit")
 
     def set_quotient_kernel(self, kind):
-        """0: autotuned; 1 warp per row; 2 eight warps per row; 3 warp per row with bulk-copy staging."""
+        """0: autotuned; 1 warp per row; 2 eight warps per row; 3 warp per row with bulk-copy staging;
+        4 the fixed size rule (eight warps per row from N = 2000 on), without timing."""
         _check(lib().cac_ctx_set_quotient_kernel(self.h, kind), "cac_ctx_set_quotient_kernel")
 
     def close(self):

@@ -324,7 +324,7 @@ int shrink_big(cac_ctx *ctx, const cac_graph *g, uint32_t target, uint32_t B, co
                uint32_t *d_lab, uint32_t *d_kout, void *scratch);
 // Quotient kernel choices of the autotuner (cac_ctx::quotient_choice), bucketed by
 // floor(log2 N) and entry width.
-constexpr uint8_t kQuotientWarp = 1, kQuotientShared = 2, kQuotientBulk = 3;
+constexpr uint8_t kQuotientWarp = 1, kQuotientShared = 2, kQuotientBulk = 3, kQuotientRule = 4;
 inline int quotient_bucket(uint32_t N, bool small) {
     int b = 0;
     while ((N >> (b + 1)) != 0 && b < 15) b++;

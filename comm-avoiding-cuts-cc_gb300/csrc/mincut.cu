@@ -1722,7 +1722,7 @@ int KsEngine::step() {
             CAC_TRY(launch_warp());
         } else if (tuned == kQuotientBulk && bwarps) {
             CAC_TRY(launch_bulk());
-        } else if (!sizeable || tuned) {
+        } else if (!sizeable || tuned) {  // too small to time, already timed, or kQuotientRule forced
             CAC_TRY(maxN >= kSharedRowMinN || !qwarps ? launch_shared() : launch_warp());
         } else {
             // all write the same matrices, row sums and prefixes: time each on this step's data

@@ -386,8 +386,8 @@ int cac_ctx_set_dense_limit(cac_ctx *ctx, uint32_t max_dense_vertices) {
 }
 
 int cac_ctx_set_quotient_kernel(cac_ctx *ctx, int kind) {
-    if (!ctx || kind < 0 || kind > 3) {
-        set_error("cac_ctx_set_quotient_kernel: kind must be 0 (autotuned), 1, 2 or 3");
+    if (!ctx || kind < 0 || kind > 4) {
+        set_error("cac_ctx_set_quotient_kernel: kind must be 0 (autotuned), 1, 2, 3 or 4 (the size rule)");
         return CAC_ERR_INVALID;
     }
     ctx->quotient_forced = (uint8_t)kind;

@@ -84,9 +84,11 @@ int cac_ctx_create(const cac_config *config, cac_ctx **out);
 int cac_ctx_set_dense_limit(cac_ctx *ctx, uint32_t max_dense_vertices);
 /* The quotient kernel of the dense Karger-Stein steps: 0 (default) lets the ctx time the candidates
  * on the first sizeable step of each size bucket and keep the fastest; 1 warp per output row,
- * 2 eight warps per output row, 3 warp per output row with member rows staged by bulk copies. All
- * give identical matrices; a kernel that does not fit a step's shared memory is replaced by one that
- * does. (No reference counterpart: a tuning control.) */
+ * 2 eight warps per output row, 3 warp per output row with member rows staged by bulk copies, 4 the
+ * fixed size rule without timing (eight warps per row from 2000 source vertices on, else one; for
+ * profilers, whose serialised replays distort the timings). All give identical matrices; a kernel
+ * that does not fit a step's shared memory is replaced by one that does. (No reference
+ * counterpart: a tuning control.) */
 int cac_ctx_set_quotient_kernel(cac_ctx *ctx, int kind);
 /* Destroys the ctx; graphs still alive are released with it and their handles become invalid. */
 int cac_ctx_destroy(cac_ctx *ctx);

@@ -292,12 +292,12 @@ def test_full_size_k4000_trials_match_replay(ctx):
     assert res.total_trials == 7 and res.cut == min(want) == int(deg.min())
 
 
-@pytest.mark.parametrize("kind", [1, 2, 3])
+@pytest.mark.parametrize("kind", [1, 2, 3, 4])
 @pytest.mark.parametrize("heavy", [False, True])
 def test_every_quotient_kernel_matches_replay(libcac, kind, heavy):
     # the three quotient kernels (warp per row, eight warps per row, warp per row with member rows
-    # staged by bulk copies) each forced for every step: trial values equal the replay, with u32
-    # node matrices and with u64 ones (total weight above 2^32)
+    # staged by bulk copies) each forced for every step, and the size rule without timing: trial
+    # values equal the replay, with u32 node matrices and with u64 ones (total weight above 2^32)
     c = libcac.Context(0)
     try:
         c.set_quotient_kernel(kind)
