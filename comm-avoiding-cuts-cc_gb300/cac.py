@@ -94,6 +94,8 @@ EXPORTS = [
     ("cac_ctx_destroy", ctypes.c_int, [_vp]),
     ("cac_ctx_set_dense_limit", ctypes.c_int, [_vp, ctypes.c_uint32]),
     ("cac_ctx_set_quotient_kernel", ctypes.c_int, [_vp, ctypes.c_int]),
+    ("cac_ctx_set_plan_ahead", ctypes.c_int, [_vp, ctypes.c_int]),
+    ("cac_ctx_plan_redos", ctypes.c_uint64, [_vp]),
     ("cac_error_string", ctypes.c_char_p, [ctypes.c_int]),
     ("cac_last_error", ctypes.c_char_p, []),
     ("cac_ctx_device_bytes", ctypes.c_uint64, [_vp]),
@@ -182,6 +184,14 @@ class Context:
     def set_dense_limit(self, max_dense_vertices):
         """Karger-Stein nodes above this many vertices (or sparse ones above 2048) stay edge lists."""
         _check(lib().cac_ctx_set_dense_limit(self.h, max_dense_vertices), "cac_ctx_set_dense_limit")
+
+    def set_plan_ahead(self, enabled):
+        """Karger-Stein levels planned at their target sizes (default) or read back level by level."""
+        _check(lib().cac_ctx_set_plan_ahead(self.h, 1 if enabled else 0), "cac_ctx_set_plan_ahead")
+
+    def plan_redos(self):
+        """Runs redone level by level after a child stopped off its planned size."""
+        return int(lib().cac_ctx_plan_redos(self.h))
 
     def set_quotient_kernel(self, kind):
         """0: autotuned; 1 warp per row; 2 eight warps per row; 3 warp per row with bulk-copy staging;

@@ -91,6 +91,8 @@ struct cac_ctx {
     void *ks_scratch = nullptr;      // grow-only Karger-Stein scratch buffers (mincut.cu)
     uint8_t quotient_choice[32] = {};  // autotuned quotient kernel per (N bucket, width); 0: untuned
     uint8_t quotient_forced = 0;       // a quotient kernel chosen by the caller instead (0: autotuned)
+    bool plan_ahead = true;            // Karger-Stein levels planned at their target sizes (mincut.cu)
+    uint64_t plan_redos = 0;           // runs redone level by level after a child stopped off its target
     cudaStream_t copy_stream = nullptr;  // host-to-device chunks of cac_cc_edges (created on first use)
     cudaEvent_t chunk_ev[40] = {};       // start + one per piece and gap copy in flight
     uint32_t dense_limit = 16384;        // Karger-Stein nodes above this many vertices stay edge lists
@@ -209,6 +211,10 @@ class KsEngine {
     void release(MatBuf *b);                // drops one reference
     void add(const KNode &nd);              // takes one reference on nd.buf
     bool idle() const { return nodes_.empty() && carried_.empty(); }
+    // Planning ahead: every child is taken to stop at its target size, so a step needs no read-back
+    // of the children's sizes; a child that stops elsewhere (a round that ran out of draws, or a
+    // source without edges) sets bit 4 of the error word and the caller redoes the run without it.
+    void set_plan_ahead(bool on) { plan_ahead_ = on; }
     int step();
     int init_err();
     int read_err(uint32_t *err);
@@ -219,6 +225,7 @@ class KsEngine {
     std::vector<KNode> nodes_;
     std::vector<KTask> carried_;
     bool release_err_ = false;
+    bool plan_ahead_ = false;
     void *d_kout_, *d_prep_, *d_tscratch_, *d_err_;  // the ctx's grow-only scratch (mincut.cu)
 };
 

@@ -44,6 +44,10 @@ namespace {
 
 constexpr uint32_t kSharedRowMinN = 2000;  // before tuning: quotient steps from this N on use the shared-row kernel
 constexpr uint32_t kSharedRows = 8;         // output rows per CTA of the shared-row quotient
+// Engine error word bits: 1 an inconsistent selection prefix in a contraction, 2 a bulk-copy wait
+// past its bound, 4 a child planned at its target size that stopped elsewhere (the run is redone
+// without planning ahead)
+constexpr uint32_t kErrPlan = 4u;
 constexpr uint32_t kMaxSmemVertices = kMaxDenseVertices;  // union-find of a contraction held in shared memory
 constexpr int kBatch = 1024;                  // draws gathered before the ordered contraction
 constexpr int kNT = 512;                      // threads of the per-trial / per-task CTAs
@@ -557,7 +561,8 @@ __global__ void __launch_bounds__(256, 5) quotient_shared_row_kernel(const TaskD
                                                                   uint32_t ntasks, uint32_t rows,
                                                                   const uint64_t *__restrict__ out_off,
                                                                   unsigned char *out_base, uint32_t lab_words,
-                                                                  uint32_t kmax) {
+                                                                  uint32_t kmax, const uint32_t *__restrict__ kact,
+                                                                  uint32_t *err) {
     extern __shared__ __align__(16) unsigned char dsm[];
     const uint64_t gg = blockIdx.x;
     uint32_t lo = 0, hi = ntasks - 1;
@@ -568,6 +573,10 @@ __global__ void __launch_bounds__(256, 5) quotient_shared_row_kernel(const TaskD
     const TaskDesc T = tasks[lo];
     const SrcDesc S = srcs[T.src];
     const uint32_t k = kdim[lo];
+    if (kact && kact[lo] != k) {  // planned ahead, and this child stopped off its target: redo the run
+        if (threadIdx.x == 0) atomicOr(err, kErrPlan);
+        return;
+    }
     const uint32_t N = S.N;
     const uint32_t a0 = (uint32_t)(gg - group_task_off[lo]) * rows, a1 = min(k, a0 + rows);
     if (!width_is<Tm>(S.small)) return;
@@ -673,7 +682,8 @@ __global__ void __launch_bounds__(256) quotient_warp_kernel(const TaskDesc *__re
                                                             uint32_t ntasks, uint32_t rows,
                                                             const uint64_t *__restrict__ out_off,
                                                             unsigned char *out_base, uint32_t lab_words,
-                                                            uint32_t kmax) {
+                                                            uint32_t kmax, const uint32_t *__restrict__ kact,
+                                                            uint32_t *err) {
     // out_off[i]: byte offset of task i's matrix; out_off[ntasks + i]: of its row sums and block
     // prefixes (the next step's row prep)
     extern __shared__ __align__(16) unsigned char dsm[];
@@ -686,6 +696,10 @@ __global__ void __launch_bounds__(256) quotient_warp_kernel(const TaskDesc *__re
     const TaskDesc T = tasks[lo];
     const SrcDesc S = srcs[T.src];
     const uint32_t k = kdim[lo];
+    if (kact && kact[lo] != k) {  // planned ahead, and this child stopped off its target: redo the run
+        if (threadIdx.x == 0) atomicOr(err, kErrPlan);
+        return;
+    }
     const uint32_t N = S.N;
     const uint32_t a0 = (uint32_t)(gg - group_task_off[lo]) * rows, a1 = min(k, a0 + rows);
     if (!width_is<Tm>(S.small)) return;
@@ -826,7 +840,8 @@ __global__ void __launch_bounds__(256) quotient_bulk_kernel(const TaskDesc *__re
                                                             uint32_t ntasks, uint32_t rows,
                                                             const uint64_t *__restrict__ out_off,
                                                             unsigned char *out_base, uint32_t lab_words,
-                                                            uint32_t kmax, uint32_t row_words, uint32_t *err) {
+                                                            uint32_t kmax, uint32_t row_words, uint32_t *err,
+                                                            const uint32_t *__restrict__ kact) {
     extern __shared__ __align__(128) unsigned char dsm[];
     const uint64_t gg = blockIdx.x;
     uint32_t lo = 0, hi = ntasks - 1;
@@ -837,6 +852,10 @@ __global__ void __launch_bounds__(256) quotient_bulk_kernel(const TaskDesc *__re
     const TaskDesc T = tasks[lo];
     const SrcDesc S = srcs[T.src];
     const uint32_t k = kdim[lo];
+    if (kact && kact[lo] != k) {  // planned ahead, and this child stopped off its target: redo the run
+        if (threadIdx.x == 0) atomicOr(err, kErrPlan);
+        return;
+    }
     const uint32_t N = S.N;
     const uint32_t a0 = (uint32_t)(gg - group_task_off[lo]) * rows, a1 = min(k, a0 + rows);
     if (!width_is<Tm>(S.small)) return;
@@ -1586,9 +1605,17 @@ int KsEngine::step() {
         }
         CAC_CUDA_TRY(cudaGetLastError());
     }
+    // the children's sizes: read back, or (planning ahead) taken to be their targets, which the
+    // quotient kernels check against the contraction's own counts on the device
     std::vector<uint32_t> kk(tasks.size());
-    CAC_CUDA_TRY(cudaMemcpyAsync(kk.data(), d_kout.p, tasks.size() * 4, cudaMemcpyDeviceToHost, s));
-    CAC_CUDA_TRY(cudaStreamSynchronize(s));
+    const uint32_t *kact = nullptr;
+    if (plan_ahead_) {
+        for (size_t i = 0; i < tasks.size(); i++) kk[i] = tasks[i].target;
+        kact = d_kout.as<uint32_t>();
+    } else {
+        CAC_CUDA_TRY(cudaMemcpyAsync(kk.data(), d_kout.p, tasks.size() * 4, cudaMemcpyDeviceToHost, s));
+        CAC_CUDA_TRY(cudaStreamSynchronize(s));
+    }
 
     // quotient matrices of this step, in one stream-ordered buffer: each child's matrix, then
     // (after all matrices) each child's row sums and 32-column block prefixes, which the quotient
@@ -1670,7 +1697,8 @@ int KsEngine::step() {
             for (auto kern : kerns) {
                 CAC_TRY(smem_optin(ctx_, kern));
                 kern<<<(unsigned)groups_shared, 256, ssm, s>>>(dv_task, dv_src, dv_k, dv_gto_shared, ntk, kSharedRows,
-                                                               dv_qoff, obase, (uint32_t)stage_words, kmax);
+                                                               dv_qoff, obase, (uint32_t)stage_words, kmax, kact,
+                                                               d_err);
             }
             CAC_CUDA_TRY(cudaGetLastError());
             return CAC_OK;
@@ -1688,7 +1716,7 @@ int KsEngine::step() {
                 CAC_TRY(smem_optin(ctx_, kern));
                 kern<<<(unsigned)groups_warp, qwarps * 32, wsm, s>>>(dv_task, dv_src, dv_k, dv_gto_warp, ntk,
                                                                      qwarps * 4, dv_qoff, obase,
-                                                                     (uint32_t)stage_words, kmax);
+                                                                     (uint32_t)stage_words, kmax, kact, d_err);
             }
             CAC_CUDA_TRY(cudaGetLastError());
             return CAC_OK;
@@ -1706,7 +1734,7 @@ int KsEngine::step() {
                 kern<<<(unsigned)groups_bulk, bwarps * 32, bsm, s>>>(dv_task, dv_src, dv_k, dv_gto_bulk, ntk,
                                                                      bwarps * 4, dv_qoff, obase,
                                                                      (uint32_t)stage_words, kmax,
-                                                                     (uint32_t)row_words, d_err);
+                                                                     (uint32_t)row_words, d_err, kact);
             }
             CAC_CUDA_TRY(cudaGetLastError());
             return CAC_OK;
@@ -2247,11 +2275,15 @@ int mincut_admit_queries(cac_ctx *ctx, KsEngine &eng, const std::vector<MincutQu
     return st;
 }
 
-int mincut_run_queries(cac_ctx *ctx, std::vector<MincutQuery> &queries, float *device_ms) {
+namespace {
+
+// One run of the queries through one engine; *redo is set when a run that planned ahead met a child
+// off its target (its cuts are then not valid, and the caller runs the queries again without).
+int run_queries(cac_ctx *ctx, std::vector<MincutQuery> &queries, float *device_ms, bool plan_ahead, bool *redo) {
     cudaStream_t s = ctx->stream;
-    for (const MincutQuery &q : queries) CAC_TRY(check_graph(q.g, q.t));
     CAC_CUDA_TRY(cudaEventRecord(ctx->ev[0], s));
     KsEngine eng(ctx);
+    eng.set_plan_ahead(plan_ahead);
     CAC_TRY(eng.init_err());
     std::vector<QueryPlan> plans(queries.size());
     for (size_t i = 0; i < queries.size(); i++) {
@@ -2295,9 +2327,31 @@ int mincut_run_queries(cac_ctx *ctx, std::vector<MincutQuery> &queries, float *d
     CAC_CUDA_TRY(cudaEventRecord(ctx->ev[1], s));
     CAC_CUDA_TRY(cudaStreamSynchronize(s));
     if (device_ms) CAC_CUDA_TRY(cudaEventElapsedTime(device_ms, ctx->ev[0], ctx->ev[1]));
-    if (err) {
-        return engine_error(err);
+    if (plan_ahead && (err & kErrPlan)) {
+        *redo = true;
+        return CAC_OK;
     }
+    if (err) return engine_error(err);
+    return CAC_OK;
+}
+
+}  // namespace
+
+// Runs the queries planning ahead (no read-back of children's sizes between levels) when the ctx
+// allows it; the rare run in which a child stops off its target is run again level by level. Both
+// give the same cuts: every draw is addressed by its trial, node and round, not by the schedule.
+int mincut_run_queries(cac_ctx *ctx, std::vector<MincutQuery> &queries, float *device_ms) {
+    for (const MincutQuery &q : queries) CAC_TRY(check_graph(q.g, q.t));
+    bool redo = false;
+    float ms = 0;
+    CAC_TRY(run_queries(ctx, queries, &ms, ctx->plan_ahead, &redo));
+    if (redo) {
+        float ms2 = 0;
+        CAC_TRY(run_queries(ctx, queries, &ms2, false, &redo));
+        ms += ms2;
+        ctx->plan_redos++;
+    }
+    if (device_ms) *device_ms = ms;
     return CAC_OK;
 }
 

@@ -394,6 +394,17 @@ int cac_ctx_set_quotient_kernel(cac_ctx *ctx, int kind) {
     return CAC_OK;
 }
 
+int cac_ctx_set_plan_ahead(cac_ctx *ctx, int enabled) {
+    if (!ctx) {
+        set_error("cac_ctx_set_plan_ahead: invalid argument");
+        return CAC_ERR_INVALID;
+    }
+    ctx->plan_ahead = enabled != 0;
+    return CAC_OK;
+}
+
+uint64_t cac_ctx_plan_redos(const cac_ctx *ctx) { return ctx ? ctx->plan_redos : 0; }
+
 const char *cac_error_string(int status) {
     switch (status) {
         case CAC_OK: return "ok";

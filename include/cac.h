@@ -90,6 +90,13 @@ int cac_ctx_set_dense_limit(cac_ctx *ctx, uint32_t max_dense_vertices);
  * that does not fit a step's shared memory is replaced by one that does. (No reference
  * counterpart: a tuning control.) */
 int cac_ctx_set_quotient_kernel(cac_ctx *ctx, int kind);
+/* Karger-Stein levels planned ahead (default 1): every child is taken to stop at its target size,
+ * so the levels of a run follow one another without reading the children's sizes back; a child
+ * that stops elsewhere (rare: a round that runs out of draws, or a source without edges) is
+ * detected on the device and the run is redone level by level. Cuts are identical either way.
+ * cac_ctx_plan_redos counts the redone runs. (No reference counterpart: a scheduling control.) */
+int cac_ctx_set_plan_ahead(cac_ctx *ctx, int enabled);
+uint64_t cac_ctx_plan_redos(const cac_ctx *ctx);
 /* Destroys the ctx; graphs still alive are released with it and their handles become invalid. */
 int cac_ctx_destroy(cac_ctx *ctx);
 const char *cac_error_string(int status);

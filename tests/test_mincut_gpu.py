@@ -309,3 +309,51 @@ def test_every_quotient_kernel_matches_replay(libcac, kind, heavy):
         assert [int(x) for x in got[0]] == [O.mincut_trial(n, u, v, w, 7, 0, i) for i in range(2)]
     finally:
         c.close()
+
+
+# Planning ahead (the default): the Karger-Stein levels of a run follow one another with every
+# child taken at its target size, and a child that stops elsewhere sends the run back to the
+# level-by-level schedule. Either way every trial equals the oracle's replay: on graphs whose
+# children all reach their targets (no redo), on a complete graph with one dominant edge (rounds
+# run out of draws: children are carried into another round, so the planned run is redone) and on
+# a disconnected graph (sources without edges).
+def _heavy_complete(n, seed):
+    n, u, v, w = graphgen.complete(n, seed, wmax=1)
+    w = np.asarray(w, np.uint32).copy()
+    w[0] = 1000000
+    return n, u, v, w
+
+
+@pytest.mark.parametrize("case", ["er", "ws", "heavy", "disconnected"])
+def test_plan_ahead_and_level_by_level_agree(libcac, case):
+    if case == "er":
+        n, u, v, w = graphgen.erdos_renyi(1000, 0.05, 0, wmax=42)
+    elif case == "ws":
+        n, u, v, w = graphgen.watts_strogatz(3000, 10, 0.3, 4, wmax=100)
+    elif case == "heavy":
+        n, u, v, w = _heavy_complete(300, 1)
+    else:  # 200 disjoint triangles: Stage 1 stops at 200 isolated vertices, the root has no edges
+        base = np.arange(200, dtype=np.uint32) * 3
+        u = np.concatenate([base, base, base + 1])
+        v = np.concatenate([base + 1, base + 2, base + 2])
+        w = np.full(600, 7, np.uint32)
+        n = 600
+    got = {}
+    redos = {}
+    for plan in (True, False):
+        c = libcac.Context(0)
+        try:
+            c.set_plan_ahead(plan)
+            got[plan] = c.graph(n, u, v, w).trials(seed=3, virtual_ranks=2, trials_per_rank=2)
+            redos[plan] = c.plan_redos()
+        finally:
+            c.close()
+    assert np.array_equal(got[True], got[False])
+    for r in range(2):
+        for i in range(2):
+            assert int(got[True][r, i]) == O.mincut_trial(n, u, v, w, 3, r, i), (case, r, i)
+    assert redos[False] == 0
+    if case in ("er", "ws"):
+        assert redos[True] == 0
+    else:
+        assert redos[True] == 1
