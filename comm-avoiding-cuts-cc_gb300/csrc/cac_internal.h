@@ -215,6 +215,8 @@ class KsEngine {
     // of the children's sizes; a child that stops elsewhere (a round that ran out of draws, or a
     // source without edges) sets bit 4 of the error word and the caller redoes the run without it.
     void set_plan_ahead(bool on) { plan_ahead_ = on; }
+    bool plan_ahead() const { return plan_ahead_; }
+    uint32_t *err_word() const;             // the engine's device error word
     int step();
     int init_err();
     int read_err(uint32_t *err);

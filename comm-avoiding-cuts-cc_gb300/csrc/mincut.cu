@@ -72,6 +72,9 @@ struct DenseDesc {
     void *mat;            // k x k, u32 entries when `small`, else u64
     uint64_t m;
     uint32_t k, small;
+    // planned ahead: k is the trial's target, checked against Stage 1's own count before any write
+    const uint32_t *k_act = nullptr;
+    uint32_t *err = nullptr;
 };
 
 struct SrcDesc {
@@ -356,6 +359,10 @@ __global__ void __launch_bounds__(NT) iss_shrink_kernel(const ShrinkDesc *__rest
 
 __global__ void dense_build_kernel(const DenseDesc *__restrict__ descs) {
     const DenseDesc D = descs[blockIdx.y];
+    if (D.k_act && *D.k_act != D.k) {  // Stage 1 stopped off the target: redo the run
+        if (blockIdx.x == 0 && threadIdx.x == 0) atomicOr(D.err, kErrPlan);
+        return;
+    }
     const uint64_t ldk = ld_of(D.k);
     for (uint64_t e = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; e < D.m; e += (uint64_t)gridDim.x * blockDim.x) {
         uint32_t a = D.U[e], b = D.V[e];
@@ -1368,6 +1375,8 @@ int KsEngine::init_err() {
     return CAC_OK;
 }
 
+uint32_t *KsEngine::err_word() const { return static_cast<DevBuf *>(d_err_)->as<uint32_t>(); }
+
 int KsEngine::read_err(uint32_t *err) {
     DevBuf *e = static_cast<DevBuf *>(d_err_);
     *err = 0;
@@ -1974,9 +1983,18 @@ int admit_stage1(cac_ctx *ctx, KsEngine &eng, const std::vector<const QueryPlan 
         CAC_TRY(upload(ctx, d_sd, sd));
         iss_shrink_kernel<kNT><<<B, kNT, sm, s>>>(d_sd.as<ShrinkDesc>());
         CAC_CUDA_TRY(cudaGetLastError());
+        // the contracted sizes: read back, or (planning ahead, no sparse root in the chunk) taken to
+        // be the targets, which the dense build checks against Stage 1's counts on the device
+        bool sparse_roots = false;
+        for (uint32_t b = 0; b < B; b++) sparse_roots = sparse_roots || items[c0 + b].q->t > ctx->dense_limit;
+        const bool planned = eng.plan_ahead() && !sparse_roots;
         std::vector<uint32_t> kdim(B);
-        CAC_CUDA_TRY(cudaMemcpyAsync(kdim.data(), d_k.p, (size_t)B * 4, cudaMemcpyDeviceToHost, s));
-        CAC_CUDA_TRY(cudaStreamSynchronize(s));
+        if (planned) {
+            for (uint32_t b = 0; b < B; b++) kdim[b] = items[c0 + b].q->t;
+        } else {
+            CAC_CUDA_TRY(cudaMemcpyAsync(kdim.data(), d_k.p, (size_t)B * 4, cudaMemcpyDeviceToHost, s));
+            CAC_CUDA_TRY(cudaStreamSynchronize(s));
+        }
         // trials contracted to more than the dense limit: sparse roots (sorted, merged edge lists)
         std::vector<SparseNode> sparse;
         for (uint32_t b = 0; b < B; b++) {
@@ -2003,6 +2021,10 @@ int admit_stage1(cac_ctx *ctx, KsEngine &eng, const std::vector<const QueryPlan 
             // no scatter for a trial without a matrix (its labels would index past the buffer)
             dd[b] = DenseDesc{g->u, g->v, g->w, sd[b].lab, static_cast<unsigned char *>(roots->p) + off,
                               kdim[b] >= 2 ? g->m : 0, kdim[b], small};
+            if (planned) {
+                dd[b].k_act = sd[b].k_out;
+                dd[b].err = eng.err_word();
+            }
             off += ((uint64_t)kdim[b] * ld_of(kdim[b]) * (small ? 4 : 8) + 15) / 16 * 16;
         }
         CAC_TRY(upload(ctx, d_dd, dd));
