@@ -849,7 +849,7 @@ __global__ void __launch_bounds__(256) quotient_bulk_kernel(const TaskDesc *__re
                                                             unsigned char *out_base, uint32_t lab_words,
                                                             uint32_t kmax, uint32_t row_words, uint32_t *err,
                                                             const uint32_t *__restrict__ kact) {
-    extern __shared__ __align__(128) unsigned char dsm[];
+    extern __shared__ __align__(16) unsigned char dsm[];  // bulk copies need 16-byte alignment
     const uint64_t gg = blockIdx.x;
     uint32_t lo = 0, hi = ntasks - 1;
     while (lo < hi) {  // last task whose first row group <= gg
@@ -1451,7 +1451,6 @@ int KsEngine::step() {
 
     // leaves (n <= 128) -> exact cut; grouped by size and entry width, one launch each
     std::vector<LeafDesc> leaves;
-    std::vector<uint8_t> leaf_small;
     std::vector<KNode> inner;
     for (const KNode &nd : nodes_) {
         if (nd.N <= 128) {
