@@ -334,6 +334,10 @@ int shrink_big(cac_ctx *ctx, const cac_graph *g, uint32_t target, uint32_t B, co
 // Quotient kernel choices of the autotuner (cac_ctx::quotient_choice), bucketed by
 // floor(log2 N) and entry width.
 constexpr uint8_t kQuotientWarp = 1, kQuotientShared = 2, kQuotientBulk = 3, kQuotientRule = 4;
+// Engine error word bits: 1 an inconsistent selection prefix in a contraction, 2 a bulk-copy wait
+// past its bound, 4 a child planned at its target size that stopped elsewhere (the run is redone
+// without planning ahead)
+constexpr uint32_t kErrPlan = 4u;
 inline int quotient_bucket(uint32_t N, bool small) {
     int b = 0;
     while ((N >> (b + 1)) != 0 && b < 15) b++;

@@ -44,10 +44,7 @@ namespace {
 
 constexpr uint32_t kSharedRowMinN = 2000;  // before tuning: quotient steps from this N on use the shared-row kernel
 constexpr uint32_t kSharedRows = 8;         // output rows per CTA of the shared-row quotient
-// Engine error word bits: 1 an inconsistent selection prefix in a contraction, 2 a bulk-copy wait
-// past its bound, 4 a child planned at its target size that stopped elsewhere (the run is redone
-// without planning ahead)
-constexpr uint32_t kErrPlan = 4u;
+
 constexpr uint32_t kMaxSmemVertices = kMaxDenseVertices;  // union-find of a contraction held in shared memory
 constexpr int kBatch = 1024;                  // draws gathered before the ordered contraction
 constexpr int kNT = 512;                      // threads of the per-trial / per-task CTAs

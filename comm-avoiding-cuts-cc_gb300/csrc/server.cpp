@@ -136,6 +136,7 @@ struct CutWorker {
     std::vector<uint32_t> free_ids;  // engine query ids are recycled
     uint32_t next_id = 0;
     uint64_t held_est = 0;
+    bool planning = true;  // levels planned ahead, except while running queries are being redone
 
     uint32_t take_id() {
         if (!free_ids.empty()) {
@@ -148,7 +149,33 @@ struct CutWorker {
 
     int new_engine() {
         eng.reset(new KsEngine(s->cut));
+        eng->set_plan_ahead(planning && s->cut->plan_ahead);
         return eng->init_err();
+    }
+
+    // A planned level met a child off its target size. Which running queries it touched is not
+    // known, so all of them run again: the engine drains them (their cuts are discarded), its error
+    // word is cleared, and they are admitted again with the levels stepped one by one. Planning
+    // resumes once the engine is idle. Queries collected earlier were read with a clean error word
+    // after a synchronisation, so every kernel of theirs had run without a miss.
+    int redo_running() {
+        while (!eng->idle()) CAC_TRY(eng->step());
+        std::vector<Request *> again;
+        for (Request *r : running) {
+            free_ids.push_back(r->query);
+            if (r->d_cuts) stream_free(s->cut, r->d_cuts, std::max<uint64_t>(r->trials, 1) * 8);
+            r->d_cuts = nullptr;
+            r->st = CAC_OK;
+            r->msg.clear();
+            again.push_back(r);
+        }
+        running.clear();
+        CAC_TRY(eng->init_err());
+        planning = false;
+        eng->set_plan_ahead(false);
+        s->cut->plan_redos++;
+        admit(again);
+        return CAC_OK;
     }
 
     void retire(Request *r, int st, const std::string &msg) {
@@ -189,8 +216,18 @@ struct CutWorker {
             }
     }
 
-    // Queries with no node left in the engine are finished: reduce their cuts on the host.
-    void collect() {
+    // Queries with no node left in the engine are finished: reduce their cuts on the host (after a
+    // check that no planned level missed its target; if one did, the running queries are redone).
+    int collect() {
+        bool any_done = false;
+        for (const Request *r : running)
+            any_done = any_done || !(r->query < eng->outstanding.size() && eng->outstanding[r->query] > 0);
+        if (!any_done) return CAC_OK;
+        if (planning) {
+            uint32_t err = 0;
+            CAC_TRY(eng->read_err(&err));
+            if (err & kErrPlan) return redo_running();
+        }
         for (size_t i = 0; i < running.size();) {
             Request *r = running[i];
             if (r->query < eng->outstanding.size() && eng->outstanding[r->query] > 0) {
@@ -225,6 +262,7 @@ struct CutWorker {
             running.pop_back();
             retire(r, st, msg);
         }
+        return CAC_OK;
     }
 
     void fail_all(int st, const std::string &msg) {
@@ -274,18 +312,20 @@ struct CutWorker {
                 }
             }
             if (!batch.empty()) admit(batch);
-            if (!eng->idle()) {
-                const int st = eng->step();
-                if (st != CAC_OK) {
-                    fail_all(st, cac_last_error());
-                    if (new_engine() != CAC_OK) {
-                        fail_queue(cac_last_error());
-                        return;
-                    }
-                    continue;
+            int st = eng->idle() ? CAC_OK : eng->step();
+            if (st == CAC_OK) st = collect();
+            if (st != CAC_OK) {
+                fail_all(st, cac_last_error());
+                if (new_engine() != CAC_OK) {
+                    fail_queue(cac_last_error());
+                    return;
                 }
+                continue;
             }
-            collect();
+            if (!planning && running.empty() && eng->idle()) {  // the redone queries are through
+                planning = true;
+                eng->set_plan_ahead(s->cut->plan_ahead);
+            }
         }
     }
 };

@@ -150,3 +150,25 @@ def test_over_budget_query_fails_alone(libcac):
             srv.poll(t1)
         assert e.value.status == -2
         assert srv.poll(t2)[0].cut == O.exact_mincut(n, u, v, w)
+
+
+def test_planned_levels_redone_in_the_serving_loop(libcac, ctx):
+    # a complete graph with one dominant edge makes a planned level miss its target (a child's
+    # round runs out of draws); the serving loop then runs every query in flight again level by
+    # level, and every response still equals the single-query answer and the oracle's
+    n, u, v, w = graphgen.complete(300, 1, wmax=1)
+    w = np.asarray(w, np.uint32).copy()
+    w[0] = 1000000
+    specs = [(n, u, v, w), graphgen.erdos_renyi_m(1500, 12.0, 4, wmax=100),
+             graphgen.watts_strogatz(300, 10, 0.3, 2, wmax=100)]
+    singles = [ctx.graph(*s) for s in specs]
+    qs = [(gi, sd) for sd in range(3) for gi in range(3)]
+    expect = [(int(singles[gi].square_root(0.9, seed=sd).cut)) for gi, sd in qs]
+    with libcac.Server(0) as srv:
+        sg = [srv.graph(*s) for s in specs]
+        tickets = [srv.submit("square_root", sg[gi], 0.9, seed=sd) for gi, sd in qs]
+        got = [int(srv.poll(t)[0].cut) for t in tickets]
+    assert got == expect
+    for (gi, sd), c in zip(qs, got):
+        sn, su, sv, sw = specs[gi]
+        assert c == O.square_root(sn, su, sv, sw, 0.9, sd, ranks=1)[0]
