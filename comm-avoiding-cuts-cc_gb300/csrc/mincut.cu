@@ -1977,7 +1977,13 @@ int admit_stage1(cac_ctx *ctx, KsEngine &eng, const std::vector<const QueryPlan 
         }
         const size_t sm = kBatch * sizeof(uint2) + kCoarse * sizeof(uint64_t) + (size_t)nmax * 4;
         CAC_TRY(upload(ctx, d_sd, sd));
-        iss_shrink_kernel<kNT><<<B, kNT, sm, s>>>(d_sd.as<ShrinkDesc>());
+        // fewer trials than SMs: one trial per SM either way, so each trial gets 1024 threads
+        if (B < (uint32_t)ctx->num_sms) {
+            CAC_TRY(smem_optin(ctx, iss_shrink_kernel<2 * kNT>));
+            iss_shrink_kernel<2 * kNT><<<B, 2 * kNT, sm, s>>>(d_sd.as<ShrinkDesc>());
+        } else {
+            iss_shrink_kernel<kNT><<<B, kNT, sm, s>>>(d_sd.as<ShrinkDesc>());
+        }
         CAC_CUDA_TRY(cudaGetLastError());
         // the contracted sizes: read back, or (planning ahead, no sparse root in the chunk) taken to
         // be the targets, which the dense build checks against Stage 1's counts on the device
