@@ -600,9 +600,10 @@ __global__ void __launch_bounds__(256, 5) quotient_shared_row_kernel(const TaskD
     const uint32_t nbk = (k + 31) / 32;
     uint64_t *blk = rowsum_out + k;
     const uint32_t nchunk = (N + 32 * VEC - 1) / (32 * VEC);
+    // the row is zeroed once here, then by the output pass of every row as it reads it
+    for (uint32_t b = threadIdx.x; b < k; b += blockDim.x) qrow[b] = 0;
+    __syncthreads();  // labels staged, row zeroed
     for (uint32_t a = a0; a < a1; a++) {
-        for (uint32_t b = threadIdx.x; b < k; b += blockDim.x) qrow[b] = 0;
-        __syncthreads();  // labels staged (first row), row zeroed
         const uint32_t p0 = T.memb_off[a], p1 = T.memb_off[a + 1];
         for (uint32_t c0 = warp; c0 < nchunk; c0 += 4 * NWARP) {
             Tm x[4][VEC];
@@ -636,7 +637,10 @@ __global__ void __launch_bounds__(256, 5) quotient_shared_row_kernel(const TaskD
         for (uint32_t b0 = warp * 32; b0 < k; b0 += NWARP * 32) {
             const uint32_t b = b0 + lane;
             uint64_t v = (b < k && b != a) ? (uint64_t)qrow[b] : 0;
-            if (b < k) Qt[qb + b] = (Tm)v;
+            if (b < k) {
+                Qt[qb + b] = (Tm)v;
+                qrow[b] = 0;  // for the next row (the barrier below orders it before that row's adds)
+            }
             if (small) {  // every entry < 2^32: two 32-bit reductions of the 16-bit halves are exact
                 const uint32_t lo16 = __reduce_add_sync(0xffffffffu, (uint32_t)(v & 0xFFFFu));
                 const uint32_t hi16 = __reduce_add_sync(0xffffffffu, (uint32_t)(v >> 16));
@@ -722,9 +726,10 @@ __global__ void __launch_bounds__(256) quotient_warp_kernel(const TaskDesc *__re
     const uint32_t small = S.small;
     const uint32_t nbk = (k + 31) / 32;
     uint64_t *blk = rowsum_out + k;
+    // the warp's row is zeroed once here, then by the output pass of every row as it reads it
+    for (uint32_t b = lane; b < k; b += 32) qrow[b] = 0;
+    __syncwarp();
     for (uint32_t a = a0 + warp; a < a1; a += nw) {
-        for (uint32_t b = lane; b < k; b += 32) qrow[b] = 0;
-        __syncwarp();
         const uint32_t p0 = T.memb_off[a], p1 = T.memb_off[a + 1];
         // 16-byte loads: lane l reads columns j0 + (32 u + l) VEC .. + VEC - 1 (4 loads per pass);
         // the padding columns of a row are read but never scattered
@@ -764,7 +769,10 @@ __global__ void __launch_bounds__(256) quotient_warp_kernel(const TaskDesc *__re
             for (int u = 0; u < 4; u++) {
                 const uint32_t b = b0 + 32 * u + lane;
                 acc[u] = (b < k && b != a) ? (uint64_t)qrow[b] : 0;
-                if (b < k) Qt[qb + b] = (Tm)acc[u];
+                if (b < k) {
+                    Qt[qb + b] = (Tm)acc[u];
+                    qrow[b] = 0;  // for the next row (the warp barrier after this row orders it)
+                }
             }
 #pragma unroll
             for (int u = 0; u < 4; u++) {
