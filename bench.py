@@ -361,6 +361,8 @@ def run_ks_sparse(args, rank, world):
     torch.cuda.set_device(dev)
     stream = torch.cuda.Stream(device=dev)
     ctx = cac.Context(dev, stream=stream.cuda_stream)
+    if args.quotient_kernel:
+        ctx.set_quotient_kernel(args.quotient_kernel)
     with Clocks(dev) as clk:
         r = _ks_sparse_measure(ctx, args.steps, args.warmup)
     total_s = _max_over_ranks(r["ms_per_query"] * args.steps / 1e3, world)
@@ -878,7 +880,7 @@ def main():
     ap.add_argument("--no-batch", action="store_true", help="skip the batched min-cut measurement")
     ap.add_argument("--no-serve", action="store_true", help="skip the served-stream measurement")
     ap.add_argument("--quotient-kernel", type=int, default=0, choices=[0, 1, 2, 3, 4],
-                    help="ks-er1000 / ks-k4000 / ks-batch: 0 autotuned; 1 warp per row, 2 eight warps per row, "
+                    help="ks-er1000 / ks-k4000 / ks-batch / ks-ws32k: 0 autotuned; 1 warp per row, 2 eight warps per row, "
                          "3 warp per row with bulk-copy staging forced for every Karger-Stein step; 4 the fixed "
                          "size rule without timing (a profiling aid: under ncu the autotuner's timings are distorted)")
     args = ap.parse_args()
